@@ -1,0 +1,327 @@
+#!/usr/bin/env python
+"""Benchmark of the induced-dipole solve (time to a 1e-8 residual).
+
+Workload (default): 10,000 rigid waters = 30,000 polarizable sites, FMM
+expansion order 5, theta 0.5, ncrit 64, Thole damping a = 2.1304, one
+right-hand side = field of 12 point charges + static multipole field, solved
+from the reference's first-call guess alpha*F to ||F - B mu||_2 < 1e-8 with
+the FP64 FMM operator.  A step is one complete solve.
+
+value     mixed-precision solve (FP32 inner PCG + FP64 refinement), inputs and
+          outputs resident on the GPU, CUDA events on the library's stream.
+e2e       the same solve through the C ABI with host buffers
+          (cppe_gpu_solve: H2D of F, D2H of mu inside the timed region).
+plain     the plain FP64 GPU PCG (the reference's algorithm on the GPU) on the
+          same system, reported next to the headline.
+
+`--impl reference` times the reference algorithm on the host cores (the
+oracle's C++ restatement with OpenMP, all threads) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIGS = {
+    # name: (waters, seed, summation, order, description)
+    "c0": (333, 0, "direct", 5, "999 sites, direct summation"),
+    "c1": (10000, 1, "fmm", 5, "30,000 sites, FMM order 5, theta 0.5, ncrit 64"),
+    "c2": (100000, 2, "fmm", 6, "300,000 sites, FMM order 6, theta 0.5, ncrit 64"),
+}
+METRIC = "induced-dipole solve time to 1e-8 residual"
+FLOP_PER_PAIR = 45  # damped dipole pair, see include/cppe_gpu/work_model.h
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), \
+        int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4)
+                          if len(r) > 3 + k and r[3 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def make_problem(cfg):
+    from cppe_gb300 import synthetic
+    nw, seed, summation, order, _ = CONFIGS[cfg]
+    b = synthetic.water_box(nw, seed=seed)
+    return b, summation, order
+
+
+def static_rhs_gpu(b, summation, order):
+    from cppe_gb300 import capi
+    Fm = capi.multipole_fields(b.xyz, b.q, b.mu, b.quad, 2, np.ones(b.n, np.int32),
+                               b.alpha_iso, b.excl_ptr, b.excl_idx,
+                               fmm=(summation == "fmm"), ncrit=64, order=order)
+    return b.external_field() + Fm
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def run_reference(args):
+    """The reference algorithm on the host cores (oracle restatement)."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    if not os.path.exists(O.PORT_LIB):
+        O.build_port()
+    P = O.port()
+    b, summation, order = make_problem(args.config)
+    fmm = summation == "fmm"
+    sites = O.Sites(xyz=b.xyz, elements=b.elements, q=b.q, mu=b.mu, quad=b.quad, max_order=2,
+                    alpha6=b.alpha6, polarizable=np.ones(b.n, np.int32), excl_ptr=b.excl_ptr,
+                    excl_idx=b.excl_idx)
+    rhs = b.external_field() + P.multipole_fields(sites, fmm=fmm, order=order)
+    kw = dict(fmm=int(fmm), ncrit=64, order=order, theta=0.5, damping=2.1304, thresh=1e-8)
+    for _ in range(args.warmup):
+        P.solve(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, rhs, **kw)
+    times, its = [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        mu, it, hist, ok = P.solve(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, rhs, **kw)
+        times.append(time.perf_counter() - t0)
+        its.append(it)
+    v = float(np.mean(times))
+    cores = os.cpu_count()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded water box)",
+        "config": {"workload": f"{args.config}: {CONFIGS[args.config][4]}, Thole damping, "
+                               "tol 1e-8, PCG from alpha*F", "sites": b.n, "parallelism":
+                               "host threads"},
+        "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} full solves ({int(np.mean(its))} CG "
+                                   "iterations each), OpenMP over all host threads"},
+        "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_sample(b, rhs, summation, order):
+    """One bounded CPU solve of the same workload (oracle restatement)."""
+    from oracle import oracle as O
+    if not os.path.exists(O.PORT_LIB):
+        O.build_port()
+    P = O.port()
+    kw = dict(fmm=int(summation == "fmm"), ncrit=64, order=order, theta=0.5, damping=2.1304,
+              thresh=1e-8)
+    t0 = time.perf_counter()
+    mu, it, hist, ok = P.solve(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, rhs, **kw)
+    dt = time.perf_counter() - t0
+    return {"value": dt, "unit": "s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"1 full solve of the same system ({it} CG iterations), OpenMP over all "
+                      "host threads"}, mu
+
+
+def run_ours(args):
+    import torch
+    from cppe_gb300 import capi
+
+    rank, world, local = dist_env()
+    dev = local
+    torch.cuda.set_device(dev)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    b, summation, order = make_problem(args.config)
+    rhs = static_rhs_gpu(b, summation, order)
+    summ = capi.FMM if summation == "fmm" else capi.DIRECT
+    kw = dict(summation=summ, ncrit=64, order=order, theta=0.5, damp=True, thresh=1e-8,
+              device=dev)
+    smx = capi.System(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, precision=capi.MIXED, **kw)
+    s64 = capi.System(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, precision=capi.FP64, **kw)
+    d_rhs = torch.tensor(rhs, dtype=torch.float64, device=f"cuda:{dev}")
+    d_mu = torch.zeros_like(d_rhs)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{dev}")  # 256 MB
+    ext = torch.cuda.ExternalStream(smx.stream())
+    ext64 = torch.cuda.ExternalStream(s64.stream())
+
+    def timed_solve(sys_, stream):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        it, hist = sys_.solve_device(d_rhs.data_ptr(), d_mu.data_ptr(), make_guess=True)
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) * 1e-3, it
+
+    for _ in range(args.warmup):
+        timed_solve(smx, ext)
+        timed_solve(s64, ext64)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    l0 = capi.launch_count()
+    times = []
+    with ClockSampler(dev) as clk:
+        for _ in range(args.steps):
+            t, it = timed_solve(smx, ext)
+            times.append(t)
+    torch.cuda.synchronize()
+    launches = capi.launch_count() - l0
+    st = smx.stats()
+    mu_mx = d_mu.cpu().numpy()
+    t_mixed = float(np.mean(times))
+    if world > 1:
+        tt = torch.tensor([t_mixed], device=f"cuda:{dev}")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_mixed = float(tt.item())
+
+    # plain FP64 GPU PCG on the same system
+    t64 = []
+    for _ in range(max(1, min(args.steps, 3))):
+        t, it64 = timed_solve(s64, ext64)
+        t64.append(t)
+    mu64 = d_mu.cpu().numpy()
+    st64 = s64.stats()
+    plain = float(np.mean(t64))
+
+    # end to end through the C ABI with host buffers
+    rhs_h = np.ascontiguousarray(rhs)
+    e2e = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        mu_h, _, _, _ = smx.solve(rhs_h)
+        e2e.append(time.perf_counter() - t0)
+    e2e_v = float(np.mean(e2e))
+
+    # roofline of the dominant kernel (FP32 near-field pair pass)
+    tim32, alg_pairs, m2l_pairs = smx.kernel_timings(capi.MIXED, reps=5)
+    tim64, _, _ = s64.kernel_timings(capi.FP64, reps=3)
+    fp32_peak = capi.fma_peak_tflops(False, dev)
+    fp64_peak = capi.fma_peak_tflops(True, dev)
+    achieved = alg_pairs * FLOP_PER_PAIR / (tim32["near"] * 1e-3) / 1e12
+    achieved64 = alg_pairs * FLOP_PER_PAIR / (tim64["near"] * 1e-3) / 1e12
+    pk, pk_kind = peaks()
+
+    resid = float(np.linalg.norm(rhs - s64.apply(mu_mx)))
+    E = b.external_field()
+    de = float(abs(0.5 * (mu_mx - mu64) @ E))
+    if rank != 0:
+        return
+    cpu, _ = cpu_baseline_sample(b, rhs, summation, order) if not args.no_cpu else (None, None)
+    total = world
+    line = {
+        "metric": METRIC, "value": t_mixed, "unit": "s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_mixed * 1e3,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (seeded water box, 12 point charges)",
+        "config": {"workload": f"{args.config}: {CONFIGS[args.config][4]}, Thole damping "
+                               "2.1304, 1 RHS, tol 1e-8 (FP64 residual), PCG from alpha*F",
+                   "sites": b.n, "l2": "256 MB buffer written between timed steps",
+                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+        "solves_per_s": total / t_mixed,
+        "plain_fp64_s": plain, "speedup_vs_plain_fp64": plain / t_mixed,
+        "iterations": {"mixed_fp32_applies": st["fp32_applies"],
+                       "mixed_fp64_applies": st["fp64_applies"],
+                       "plain_fp64_iterations": st64["fp64_applies"]},
+        "parity": {"fp64_residual_of_mixed": resid, "mu_maxabs_vs_fp64": float(
+            np.abs(mu_mx - mu64).max()), "epol_diff_hartree": de},
+        "roofline": {"bound": "fp32", "kernel": "k_p2p<float,1,damped> (near field)",
+                     "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp32_peak, "traffic": None,
+                     "peak_kind": "measured FFMA probe (cppe_gpu_fma_peak), no FP32 CUDA-core "
+                                  "figure in MEASURED_PEAKS.json",
+                     "algorithmic": f"{alg_pairs} pairs x {FLOP_PER_PAIR} FLOP per launch"},
+        "roofline_fp64": {"bound": "fp64", "achieved": achieved64, "peak": fp64_peak,
+                          "unit": "TFLOP/s", "frac": achieved64 / fp64_peak},
+        "phases_ms": {"fp32": tim32, "fp64": tim64},
+        "peaks": {"hbm_gbs": pk.get("hbm_gbs"), "bf16_tflops": pk.get("bf16_tflops"),
+                  "kind": pk_kind, "fp32_fma_tflops": fp32_peak, "fp64_fma_tflops": fp64_peak},
+        "e2e": {"value": e2e_v, "unit": "s", "h2d_bytes_per_step": int(rhs.nbytes),
+                "d2h_bytes_per_step": int(rhs.nbytes)},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c1", choices=sorted(CONFIGS))
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,271 @@
+"""ctypes binding of libcppe_gpu.so (the C ABI of include/cppe_gpu.h).
+
+This is the binding a Python caller (or the reference's own code through
+ctypes) uses to reach the GPU library without the pybind11 layer; tests and
+bench.py use it too."""
+import ctypes
+import os
+import re
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(ROOT, "cppe_gb300", "libcppe_gpu.so")
+HEADER = os.path.join(ROOT, "include", "cppe_gpu.h")
+
+OK, NOT_CONVERGED, INVALID_ARG, CUDA_ERROR, TIMEOUT, NO_DEVICE = range(6)
+DIRECT, FMM = 0, 1
+FP64, MIXED = 0, 1
+
+D = ctypes.POINTER(ctypes.c_double)
+I = ctypes.POINTER(ctypes.c_int)
+L = ctypes.POINTER(ctypes.c_long)
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("summation", ctypes.c_int), ("tree_ncrit", ctypes.c_int),
+                ("tree_expansion_order", ctypes.c_int), ("theta", ctypes.c_double),
+                ("damp", ctypes.c_int), ("damping_factor", ctypes.c_double),
+                ("induced_thresh", ctypes.c_double), ("maxiter", ctypes.c_int),
+                ("precision", ctypes.c_int), ("device", ctypes.c_int)]
+
+
+def declared_functions():
+    """Names of the functions declared in include/cppe_gpu.h."""
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(cppe_gpu_\w+)\s*\(", src)))
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = ctypes.CDLL(LIB_PATH)
+        l = _lib
+        l.cppe_gpu_default_options.argtypes = [ctypes.POINTER(Options)]
+        l.cppe_gpu_default_options.restype = None
+        l.cppe_gpu_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+        l.cppe_gpu_create.argtypes = [ctypes.c_int, D, D, I, I, ctypes.POINTER(Options),
+                                      ctypes.POINTER(ctypes.c_void_p)]
+        l.cppe_gpu_destroy.argtypes = [ctypes.c_void_p]
+        for f in ("cppe_gpu_bmatrix_apply", "cppe_gpu_bmatrix_apply_fp32",
+                  "cppe_gpu_apply_diagonal", "cppe_gpu_apply_diagonal_inverse"):
+            getattr(l, f).argtypes = [ctypes.c_void_p, D, D]
+        l.cppe_gpu_to_dense.argtypes = [ctypes.c_void_p, D]
+        l.cppe_gpu_direct_inverse.argtypes = [ctypes.c_void_p, D]
+        l.cppe_gpu_solve.argtypes = [ctypes.c_void_p, D, D, ctypes.c_int, D, I, D, ctypes.c_int]
+        l.cppe_gpu_last_solve_stats.argtypes = [ctypes.c_void_p, D, I, I]
+        l.cppe_gpu_multipole_fields.argtypes = [
+            ctypes.c_int, D, D, D, D, ctypes.c_int, I, D, I, I, ctypes.c_int, ctypes.c_int,
+            ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_int, D]
+        l.cppe_gpu_tree_info.argtypes = [ctypes.c_int, D, ctypes.c_int, ctypes.c_double, I, I,
+                                         L, L, L]
+        l.cppe_gpu_tree_lists.argtypes = [ctypes.c_int, D, ctypes.c_int, ctypes.c_double, I, I]
+        l.cppe_gpu_device_count.argtypes = [I]
+        l.cppe_gpu_batch_create.argtypes = [ctypes.c_int, I, D, D, I, I, ctypes.c_int,
+                                            ctypes.c_int, ctypes.POINTER(Options),
+                                            ctypes.POINTER(ctypes.c_void_p)]
+        l.cppe_gpu_batch_destroy.argtypes = [ctypes.c_void_p]
+        l.cppe_gpu_batch_solve.argtypes = [ctypes.c_void_p, D, D, I]
+        l.cppe_gpu_batch_solve_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p,
+                                                  ctypes.c_void_p, I]
+        l.cppe_gpu_solve_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                            ctypes.c_int, ctypes.c_void_p, I, D, ctypes.c_int]
+        l.cppe_gpu_bmatrix_apply_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p,
+                                                    ctypes.c_void_p]
+        l.cppe_gpu_stream.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]
+        l.cppe_gpu_launch_count.argtypes = [ctypes.POINTER(ctypes.c_longlong)]
+        l.cppe_gpu_kernel_timings.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, D,
+                                              ctypes.POINTER(ctypes.c_longlong),
+                                              ctypes.POINTER(ctypes.c_longlong)]
+        l.cppe_gpu_fma_peak.argtypes = [ctypes.c_int, ctypes.c_int, D]
+    return _lib
+
+
+def launch_count():
+    c = ctypes.c_longlong(0)
+    lib().cppe_gpu_launch_count(ctypes.byref(c))
+    return c.value
+
+
+def fma_peak_tflops(fp64=False, device=0):
+    t = ctypes.c_double(0)
+    check(lib().cppe_gpu_fma_peak(device, int(fp64), ctypes.byref(t)))
+    return t.value
+
+
+def last_error():
+    buf = ctypes.create_string_buffer(1024)
+    lib().cppe_gpu_last_error(buf, 1024)
+    return buf.value.decode()
+
+
+def check(rc, allow=(OK,)):
+    if rc not in allow:
+        raise RuntimeError(f"cppe_gpu status {rc}: {last_error()}")
+    return rc
+
+
+def f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def dp(a):
+    return None if a is None else a.ctypes.data_as(D)
+
+
+def ip(a):
+    return None if a is None else a.ctypes.data_as(I)
+
+
+def options(summation=DIRECT, ncrit=64, order=5, theta=0.5, damp=False, damping=2.1304,
+            thresh=1e-8, maxiter=50, precision=FP64, device=0):
+    o = Options()
+    lib().cppe_gpu_default_options(ctypes.byref(o))
+    o.summation, o.tree_ncrit, o.tree_expansion_order, o.theta = summation, ncrit, order, theta
+    o.damp, o.damping_factor, o.induced_thresh, o.maxiter = int(damp), damping, thresh, maxiter
+    o.precision, o.device = precision, device
+    return o
+
+
+def device_count():
+    c = ctypes.c_int(0)
+    lib().cppe_gpu_device_count(ctypes.byref(c))
+    return c.value
+
+
+class System:
+    """One cppe_gpu_system."""
+
+    def __init__(self, xyz, alpha6, excl_ptr=None, excl_idx=None, **opts):
+        self._keep = [f64(xyz), f64(alpha6), i32(excl_ptr) if excl_ptr is not None else None,
+                      i32(excl_idx) if excl_idx is not None else None]
+        self.n = self._keep[0].shape[0]
+        self.opts = options(**opts)
+        h = ctypes.c_void_p()
+        check(lib().cppe_gpu_create(self.n, dp(self._keep[0]), dp(self._keep[1]),
+                                    ip(self._keep[2]), ip(self._keep[3]),
+                                    ctypes.byref(self.opts), ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().cppe_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def apply(self, v, fp32=False):
+        v = f64(v)
+        out = np.zeros_like(v)
+        fn = lib().cppe_gpu_bmatrix_apply_fp32 if fp32 else lib().cppe_gpu_bmatrix_apply
+        check(fn(self.h, dp(v), dp(out)))
+        return out
+
+    def apply_diagonal(self, v, inverse=False):
+        v = f64(v)
+        out = np.zeros_like(v)
+        fn = lib().cppe_gpu_apply_diagonal_inverse if inverse else lib().cppe_gpu_apply_diagonal
+        check(fn(self.h, dp(v), dp(out)))
+        return out
+
+    def dense(self):
+        out = np.zeros((3 * self.n, 3 * self.n))
+        check(lib().cppe_gpu_to_dense(self.h, dp(out)))
+        return out
+
+    def inverse(self):
+        out = np.zeros((3 * self.n, 3 * self.n))
+        check(lib().cppe_gpu_direct_inverse(self.h, dp(out)))
+        return out
+
+    def solve(self, rhs, guess=None, make_guess=True, allow_not_converged=False):
+        rhs = f64(rhs)
+        mu = np.zeros_like(rhs)
+        it = ctypes.c_int(0)
+        cap = self.opts.maxiter + 64
+        hist = np.zeros(cap)
+        g = f64(guess) if guess is not None else None
+        rc = lib().cppe_gpu_solve(self.h, dp(rhs), dp(g), int(make_guess), dp(mu),
+                                  ctypes.byref(it), dp(hist), cap)
+        check(rc, (OK, NOT_CONVERGED) if allow_not_converged else (OK,))
+        return mu, it.value, hist[: it.value], rc
+
+    def solve_device(self, d_rhs, d_mu, make_guess=True, d_guess=None):
+        """Device-pointer solve (ints from e.g. torch.Tensor.data_ptr())."""
+        it = ctypes.c_int(0)
+        cap = self.opts.maxiter + 64
+        hist = np.zeros(cap)
+        rc = lib().cppe_gpu_solve_device(self.h, d_rhs, d_guess, int(make_guess), d_mu,
+                                         ctypes.byref(it), dp(hist), cap)
+        check(rc)
+        return it.value, hist[: it.value]
+
+    def stream(self):
+        s = ctypes.c_void_p()
+        check(lib().cppe_gpu_stream(self.h, ctypes.byref(s)))
+        return s.value or 0
+
+    def kernel_timings(self, precision=FP64, reps=5):
+        ms = np.zeros(6)
+        npair, nm2l = ctypes.c_longlong(0), ctypes.c_longlong(0)
+        check(lib().cppe_gpu_kernel_timings(self.h, precision, reps, dp(ms), ctypes.byref(npair),
+                                            ctypes.byref(nm2l)))
+        names = ["near", "p2m_m2m", "m2l", "l2l", "finish", "apply"]
+        return dict(zip(names, ms)), npair.value, nm2l.value
+
+    def stats(self):
+        r = ctypes.c_double(0)
+        a = ctypes.c_int(0)
+        b = ctypes.c_int(0)
+        check(lib().cppe_gpu_last_solve_stats(self.h, ctypes.byref(r), ctypes.byref(a),
+                                              ctypes.byref(b)))
+        return dict(rnorm=r.value, fp64_applies=a.value, fp32_applies=b.value)
+
+
+def multipole_fields(xyz, q, mu, quad, max_order, polarizable=None, alpha_iso=None,
+                     excl_ptr=None, excl_idx=None, fmm=False, ncrit=64, order=5, theta=0.5,
+                     damp=False, damping=2.1304, device=0):
+    xyz = f64(xyz)
+    n = xyz.shape[0]
+    F = np.zeros(3 * n)
+    args = [f64(q), f64(mu), f64(quad), i32(polarizable) if polarizable is not None else None,
+            f64(alpha_iso) if alpha_iso is not None else None,
+            i32(excl_ptr) if excl_ptr is not None else None,
+            i32(excl_idx) if excl_idx is not None else None]
+    check(lib().cppe_gpu_multipole_fields(
+        n, dp(xyz), dp(args[0]), dp(args[1]), dp(args[2]), max_order, ip(args[3]),
+        dp(args[4]), ip(args[5]), ip(args[6]), FMM if fmm else DIRECT, ncrit, order, theta,
+        int(damp), damping, device, dp(F)))
+    return F
+
+
+def tree_info(xyz, ncrit=64, theta=0.5):
+    xyz = f64(xyz)
+    nc, nl = ctypes.c_int(0), ctypes.c_int(0)
+    nm, npp, pairs = ctypes.c_long(0), ctypes.c_long(0), ctypes.c_long(0)
+    check(lib().cppe_gpu_tree_info(xyz.shape[0], dp(xyz), ncrit, theta, ctypes.byref(nc),
+                                   ctypes.byref(nl), ctypes.byref(nm), ctypes.byref(npp),
+                                   ctypes.byref(pairs)))
+    return dict(ncells=nc.value, nleaves=nl.value, nm2l=nm.value, np2p=npp.value,
+                p2p_pairs=pairs.value)
+
+
+def tree_lists(xyz, ncrit=64, theta=0.5):
+    info = tree_info(xyz, ncrit, theta)
+    xyz = f64(xyz)
+    m2l = np.zeros((info["nm2l"], 2), np.int32)
+    p2p = np.zeros((info["np2p"], 2), np.int32)
+    check(lib().cppe_gpu_tree_lists(xyz.shape[0], dp(xyz), ncrit, theta, ip(m2l), ip(p2p)))
+    return info, m2l, p2p

@@ -1,0 +1,130 @@
+// The field engine: evaluates F_i = sum_j field(r_i - r_j; S_j) over the
+// sites of one system, by direct summation or by the reference's FMM, on one
+// CUDA stream.  Sites live on the device in a fixed permuted order (leaf-
+// contiguous for FMM, caller order for direct summation).
+#pragma once
+
+#include <memory>
+#include <vector>
+
+#include "common.cuh"
+#include "fmm_ops.h"
+#include "tree.h"
+
+namespace cg {
+
+struct TreeView {
+  int n, ncells, nleaves;
+  const double4_32a* center;  // x, y, z, r
+  const int* parent;
+  const int* child_ptr;
+  const int* child_idx;
+  const int* is_leaf;
+  const int* leaf_cell;
+  const int* leaf_start;
+  const int* site_leaf;  // leaf of each (permuted) site
+  const int* m2l_ptr;
+  const int* m2l_src;
+  const int* p2p_ptr;
+  const int* p2p_src;
+};
+
+struct OpsView {
+  int m, p, msize, lsize, nt, nm2l_terms, nl2p;
+  const int* exps;
+  const int *p2m_ptr, *p2m_k, *p2m_j;
+  const int *m2m_ptr, *m2m_k, *m2m_j;
+  const int *l2l_ptr, *l2l_k, *l2l_j;
+  const int *l2p_c, *l2p_n, *l2p_j;
+  const int* m2l_kw;  // k | w << 16
+  const int* slots;
+  const int* row_slot_ptr;
+  const int* row_slot_id;
+  const int* drec;
+};
+
+// Site coordinates as the kernels read them (permuted order).
+struct SiteView64 {
+  const double4_32a* pos;  // x, y, z, s = alpha_iso^(-1/6) (0: no damping partner)
+};
+struct SiteView32 {
+  const float4* hi;  // float(x), float(y), float(z), s
+  const float4* lo;  // x - hi, ...  (hi + lo carries ~48 bits of each coordinate)
+};
+
+struct DeviceOps {
+  OpTables host;
+  DBuf<int> exps, p2m_ptr, p2m_k, p2m_j, m2m_ptr, m2m_k, m2m_j, l2l_ptr, l2l_k, l2l_j, l2p_c,
+        l2p_n, l2p_j, m2l_kw, slots, row_slot_ptr, row_slot_id, drec;
+  void build(int m, int p, cudaStream_t s);
+  OpsView view() const;
+};
+
+// Geometry: the sites, their permutation and the interaction structure.
+struct Geometry {
+  int n       = 0;
+  bool fmm    = false;
+  int ncrit   = 64;
+  double theta = 0.5;
+  int nsplit  = 1;  // source splits of the near-field pass
+  TreeLayout layout;
+  std::vector<int> level_start;
+  DBuf<double> center;
+  DBuf<int> parent, child_ptr, child_idx, is_leaf, leaf_cell, leaf_start, site_leaf, m2l_ptr,
+        m2l_src, p2p_ptr, p2p_src;
+  DBuf<int> perm, inv_perm;  // perm[k] = caller index of site k
+  DBuf<double4_32a> pos64;
+  DBuf<float4> hi32, lo32;
+  // pairs the reference skips (exclusions) that the near-field pass computed
+  DBuf<int> corr_ptr, corr_idx;
+  long near_pairs = 0;  // ordered pairs evaluated by the near-field pass
+  long alg_pairs  = 0;  // of these, the pairs the reference evaluates
+
+  // xyz in caller order; s_damp: alpha_iso^(-1/6) per site (0 = undamped partner);
+  // exclusions in caller indices (CSR, may be null).
+  void build(int n, const double* xyz, const double* s_damp, const int* excl_ptr,
+             const int* excl_idx, bool fmm, int ncrit, double theta, cudaStream_t s);
+  TreeView view() const;
+  SiteView64 v64() const { return {pos64.p}; }
+  SiteView32 v32() const { return {hi32.p, lo32.p}; }
+};
+
+// Work buffers of one (geometry, m, p, precision) evaluation.
+template <typename T>
+struct FieldWork {
+  DBuf<T> M, L, Fnear;
+};
+
+// Output modes of the finishing pass.
+enum FinishMode { FINISH_APPLY = 0, FINISH_FIELD = 1 };
+
+// Per-launch scalar reduction slots (device).
+struct ReduceSlots {
+  double* partials;   // >= nblocks * 4 doubles
+  unsigned* ticket;   // one counter, zero between uses
+  double* out;        // receives the totals
+};
+
+// Evaluates the field of sources `src` (ns = ncomp(m) values per permuted
+// site, precision T).  FINISH_APPLY: out (T, 3n) = F + ainv6 . src and, when
+// dot != nullptr, dot->out[0] = sum_i src_i . out_i (FP64).  FINISH_FIELD:
+// out64 (double, 3n) += sign * F.
+// Optional phase markers: recorded on the stream at the start, after P2M+M2M,
+// after M2L, after L2L, after the near-field pass and after the finishing pass.
+struct PhaseEvents {
+  cudaEvent_t ev[6];
+};
+
+template <typename T>
+void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m, const T* src,
+                bool damp, double damping, FinishMode mode, const T* ainv6, T* out,
+                double* out64, double sign, const ReduceSlots* dot, cudaStream_t s,
+                const PhaseEvents* pe = nullptr);
+
+// Permutation helpers (caller order <-> device order), all 3-vectors.
+void permute_in(const Geometry& g, const double* in_caller, double* out_perm, int ncomp,
+                cudaStream_t s);
+void permute_out(const Geometry& g, const double* in_perm, double* out_caller, int ncomp,
+                 cudaStream_t s);
+
+}  // namespace cg

@@ -1,0 +1,495 @@
+// Solvers of one system: the reference's Jacobi-preconditioned CG in FP64
+// (InducedMoments::compute, src/core/electric_fields.cc:191-239) and the
+// mixed-precision form (FP32 inner PCG, FP64 residual and refinement).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <tuple>
+
+#include "system.h"
+
+namespace cg {
+
+constexpr int VB = 256;  // threads per block of the vector kernels
+
+// ---------------------------------------------------------------------------
+// Vector kernels: thread per site; 3x3 symmetric blocks as 6 upper values.
+// Scalars live in device memory so a whole iteration can run without the host.
+// ---------------------------------------------------------------------------
+template <typename A, typename B>
+__device__ __forceinline__ void sym3(const A* a, const B* v, B* o) {
+  o[0] = (B)(a[0] * v[0] + a[1] * v[1] + a[2] * v[2]);
+  o[1] = (B)(a[1] * v[0] + a[3] * v[1] + a[4] * v[2]);
+  o[2] = (B)(a[2] * v[0] + a[4] * v[1] + a[5] * v[2]);
+}
+
+// r = F - Ax (Ax may be null: zero start), z = alpha r, p = z; rz, rr.
+template <typename T>
+__global__ void k_cg_start(int n, const double* __restrict__ F, const T* __restrict__ Ax,
+                           const T* __restrict__ a6, T* __restrict__ r, T* __restrict__ z,
+                           T* __restrict__ p, ReduceSlots rs, double* scal, int* flags) {
+  __shared__ double sh[64];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double v[2] = {0.0, 0.0};
+  if (i < n) {
+    T rv[3], zv[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) rv[c] = (T)(F[3 * i + c] - (Ax ? (double)Ax[3 * i + c] : 0.0));
+    sym3(a6 + 6 * (size_t)i, rv, zv);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      r[3 * i + c] = rv[c], z[3 * i + c] = zv[c], p[3 * i + c] = zv[c];
+      v[0] += (double)rv[c] * zv[c];
+      v[1] += (double)rv[c] * rv[c];
+    }
+  }
+  if (grid_sum_last<2>(v, sh, rs.partials, rs.ticket, rs.out)) {
+    scal[S_RZ]    = rs.out[0];
+    scal[S_RR]    = rs.out[1];
+    scal[S_RNORM] = sqrt(rs.out[1]);
+    flags[0]      = 0;
+    flags[1]      = 0;
+  }
+}
+
+// One CG update after Ap and p.Ap are known:
+//   a = rz / pAp; x += a p; r -= a Ap; z = alpha r; beta = r'z' / rz.
+// Sets flags[0] = 1 when ||r|| < thresh, 2 when the iteration limit is hit.
+template <typename T>
+__global__ void k_cg_update(int n, const T* __restrict__ p, const T* __restrict__ Ap,
+                            const T* __restrict__ a6, T* __restrict__ x, T* __restrict__ r,
+                            T* __restrict__ z, ReduceSlots rs, double* scal, int* flags,
+                            double* hist, double thresh, int maxiter) {
+  __shared__ double sh[64];
+  if (flags[0]) return;
+  const double a = scal[S_RZ] / scal[S_PAP];
+  const T aT     = (T)a;
+  const int i    = blockIdx.x * blockDim.x + threadIdx.x;
+  double v[2]    = {0.0, 0.0};
+  if (i < n) {
+    T rv[3], zv[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const size_t k = 3 * (size_t)i + c;
+      x[k] += aT * p[k];
+      rv[c] = r[k] - aT * Ap[k];
+      r[k]  = rv[c];
+    }
+    sym3(a6 + 6 * (size_t)i, rv, zv);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      z[3 * (size_t)i + c] = zv[c];
+      v[0] += (double)rv[c] * rv[c];
+      v[1] += (double)rv[c] * zv[c];
+    }
+  }
+  if (grid_sum_last<2>(v, sh, rs.partials, rs.ticket, rs.out)) {
+    const double rn = sqrt(rs.out[0]);
+    const int it    = flags[1];
+    if (hist) hist[it] = rn;
+    flags[1]      = it + 1;
+    scal[S_RNORM] = rn;
+    scal[S_BETA]  = rs.out[1] / scal[S_RZ];
+    scal[S_RZ]    = rs.out[1];
+    if (rn < thresh)
+      flags[0] = 1;
+    else if (it + 1 >= maxiter)
+      flags[0] = 2;
+  }
+}
+
+template <typename T>
+__global__ void k_cg_dir(int n3, const T* __restrict__ z, T* __restrict__ p,
+                         const double* scal, const int* flags) {
+  if (flags[0]) return;
+  const T b   = (T)scal[S_BETA];
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n3) p[k] = z[k] + b * p[k];
+}
+
+// r = F - Ax in FP64; ||r||.
+__global__ void k_residual(int n3, const double* __restrict__ F, const double* __restrict__ Ax,
+                           double* __restrict__ r, ReduceSlots rs, double* scal) {
+  __shared__ double sh[32];
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  double v[1] = {0.0};
+  if (k < n3) {
+    const double d = F[k] - (Ax ? Ax[k] : 0.0);
+    r[k]           = d;
+    v[0]           = d * d;
+  }
+  if (grid_sum_last<1>(v, sh, rs.partials, rs.ticket, rs.out)) scal[S_RNORM] = sqrt(rs.out[0]);
+}
+
+// x += d (FP64 += FP32); d is then cleared.
+__global__ void k_accumulate(int n3, double* __restrict__ x, float* __restrict__ d) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n3) {
+    x[k] += (double)d[k];
+    d[k] = 0.f;
+  }
+}
+
+__global__ void k_to_f32(int n3, const double* __restrict__ a, float* __restrict__ b) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n3) b[k] = (float)a[k];
+}
+
+__global__ void k_to_f64(int n3, const float* __restrict__ a, double* __restrict__ b) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n3) b[k] = (double)a[k];
+}
+
+__global__ void k_sym_apply(int n, const double* __restrict__ a6, const double* __restrict__ in,
+                            double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) sym3(a6 + 6 * (size_t)i, in + 3 * (size_t)i, out + 3 * (size_t)i);
+}
+
+// ---------------------------------------------------------------------------
+// System
+// ---------------------------------------------------------------------------
+System::~System() {
+  if (stream) {
+    cudaSetDevice(device);
+    cudaStreamSynchronize(stream);
+    cudaStreamDestroy(stream);
+  }
+  if (h_flags) cudaFreeHost(h_flags);
+  if (h_scal) cudaFreeHost(h_scal);
+}
+
+static void inv_sym3(const double* s, double* o6) {
+  const double a = s[0], b = s[1], c = s[2], d = s[3], e = s[4], f = s[5];
+  const double A = d * f - e * e, B = c * e - b * f, C = b * e - c * d;
+  const double det = a * A + b * B + c * C;
+  const double id  = 1.0 / det;
+  o6[0] = A * id;
+  o6[1] = B * id;
+  o6[2] = C * id;
+  o6[3] = (a * f - c * c) * id;
+  o6[4] = (b * c - a * e) * id;
+  o6[5] = (a * d - b * b) * id;
+}
+
+void System::init(int n_, const double* xyz, const double* alpha6, const int* excl_ptr,
+                  const int* excl_idx, const cppe_gpu_options& o) {
+  n   = n_;
+  opt = o;
+  if (n <= 0) fail(CPPE_GPU_INVALID_ARG, "system has no polarizable sites");
+  if (!xyz || !alpha6) fail(CPPE_GPU_INVALID_ARG, "xyz and alpha6 are required");
+  const bool fmm = o.summation == CPPE_GPU_FMM;
+  if (fmm && (o.tree_expansion_order < 2 || o.tree_expansion_order > 7))
+    fail(CPPE_GPU_INVALID_ARG,
+         "tree_expansion_order must be in [2, 7] for induced dipoles (the reference "
+         "silently skips unsupported orders)");
+  if (fmm && o.tree_ncrit < 1) fail(CPPE_GPU_INVALID_ARG, "tree_ncrit must be >= 1");
+  if (o.maxiter < 0) fail(CPPE_GPU_INVALID_ARG, "maxiter must be >= 0");
+  int ndev = 0;
+  CG_CUDA(cudaGetDeviceCount(&ndev));
+  if (o.device < 0 || o.device >= ndev) fail(CPPE_GPU_INVALID_ARG, "bad CUDA device ordinal");
+  device = o.device;
+  CG_CUDA(cudaSetDevice(device));
+  CG_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+
+  // Coincident sites make the pair kernels singular (and the reference's tree
+  // build recurse without end): reject them up front.
+  {
+    std::vector<int> idx(n);
+    std::iota(idx.begin(), idx.end(), 0);
+    auto key = [&](int i) { return std::make_tuple(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]); };
+    std::sort(idx.begin(), idx.end(), [&](int a, int b) { return key(a) < key(b); });
+    for (int k = 1; k < n; ++k)
+      if (key(idx[k]) == key(idx[k - 1]))
+        fail(CPPE_GPU_INVALID_ARG, "sites " + std::to_string(idx[k - 1]) + " and " +
+                                         std::to_string(idx[k]) + " coincide");
+  }
+  if (excl_ptr) {
+    excl_ptr_h.assign(excl_ptr, excl_ptr + n + 1);
+    excl_idx_h.assign(excl_idx, excl_idx + excl_ptr[n]);
+  }
+  std::vector<double> sd(n, 0.0), ainv(6 * (size_t)n), al(6 * (size_t)n);
+  for (int i = 0; i < n; ++i) {
+    const double* a = alpha6 + 6 * (size_t)i;
+    const double iso = (a[0] + a[3] + a[5]) / 3.0;
+    if (o.damp && iso > 0.0) sd[i] = std::pow(iso, -1.0 / 6.0);
+  }
+  geo.build(n, xyz, sd.data(), excl_ptr, excl_idx, fmm, o.tree_ncrit, o.theta, stream);
+  if (fmm) {
+    ops = std::make_unique<DeviceOps>();
+    ops->build(1, o.tree_expansion_order, stream);
+  }
+  for (int k = 0; k < n; ++k) {
+    const double* a = alpha6 + 6 * (size_t)geo.layout.perm[k];
+    inv_sym3(a, &ainv[6 * (size_t)k]);
+    std::copy(a, a + 6, &al[6 * (size_t)k]);
+  }
+  std::vector<float> ainvf(ainv.begin(), ainv.end()), alf(al.begin(), al.end());
+  ainv64.upload(ainv, stream);
+  alpha64.upload(al, stream);
+  ainv32.upload(ainvf, stream);
+  alpha32.upload(alf, stream);
+  const size_t n3 = 3 * (size_t)n;
+  for (auto* b : {&F, &x, &r, &z, &p, &Ap, &tmp_in, &tmp_out}) b->alloc(n3);
+  for (auto* b : {&r32, &z32, &p32, &Ap32, &d32}) b->alloc(n3);
+  scal.alloc(S_NSCAL);
+  scal.zero(stream);
+  const size_t maxblocks = std::max<size_t>(1024, (n + VB - 1) / VB + 1);
+  partials.alloc(4 * maxblocks);
+  hist.alloc(std::max(1, o.maxiter) + 64);
+  ticket.alloc(1);
+  ticket.zero(stream);
+  flags.alloc(4);
+  flags.zero(stream);
+  CG_CUDA(cudaMallocHost(&h_flags, 4 * sizeof(int)));
+  CG_CUDA(cudaMallocHost(&h_scal, S_NSCAL * sizeof(double)));
+  CG_CUDA(cudaStreamSynchronize(stream));
+}
+
+void System::apply32_widen(const double* in, double* out) {
+  const int n3 = 3 * n;
+  k_to_f32<<<(n3 + VB - 1) / VB, VB, 0, stream>>>(n3, in, p32.p);
+  CG_LAUNCH();
+  apply32(p32.p, Ap32.p, false);
+  k_to_f64<<<(n3 + VB - 1) / VB, VB, 0, stream>>>(n3, Ap32.p, out);
+  CG_LAUNCH();
+}
+
+void System::phase_timings(int precision, int reps, double* ms) {
+  CG_CUDA(cudaSetDevice(device));
+  PhaseEvents pe;
+  for (auto& e : pe.ev) CG_CUDA(cudaEventCreate(&e));
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  const int n3 = 3 * n;
+  k_to_f32<<<(n3 + VB - 1) / VB, VB, 0, stream>>>(n3, tmp_in.p, p32.p);
+  CG_LAUNCH();
+  for (int r = 0; r < reps; ++r) {
+    if (precision == CPPE_GPU_MIXED) {
+      ReduceSlots rs = slots(S_PAP);
+      eval_field<float>(geo, ops.get(), w32, 1, p32.p, opt.damp != 0, opt.damping_factor,
+                        FINISH_APPLY, ainv32.p, Ap32.p, nullptr, 1.0, &rs, stream, &pe);
+    } else {
+      ReduceSlots rs = slots(S_PAP);
+      eval_field<double>(geo, ops.get(), w64, 1, tmp_in.p, opt.damp != 0, opt.damping_factor,
+                         FINISH_APPLY, ainv64.p, tmp_out.p, nullptr, 1.0, &rs, stream, &pe);
+    }
+    CG_CUDA(cudaEventSynchronize(pe.ev[5]));
+    float t;
+    const int from[6] = {3, 0, 1, 2, 4, 0}, to[6] = {4, 1, 2, 3, 5, 5};
+    for (int k = 0; k < 6; ++k) {
+      CG_CUDA(cudaEventElapsedTime(&t, pe.ev[from[k]], pe.ev[to[k]]));
+      acc[k] += t;
+    }
+  }
+  for (auto& e : pe.ev) cudaEventDestroy(e);
+  for (int k = 0; k < 6; ++k) ms[k] = acc[k] / std::max(1, reps);
+}
+
+ReduceSlots System::slots(int k) const { return ReduceSlots{partials.p, ticket.p, scal.p + k}; }
+
+void System::apply64(const double* in, double* out, bool with_dot) {
+  ReduceSlots rs = slots(S_PAP);
+  eval_field<double>(geo, ops.get(), w64, 1, in, opt.damp != 0, opt.damping_factor,
+                     FINISH_APPLY, ainv64.p, out, nullptr, 1.0, with_dot ? &rs : nullptr,
+                     stream);
+}
+
+void System::apply32(const float* in, float* out, bool with_dot) {
+  ReduceSlots rs = slots(S_PAP);
+  eval_field<float>(geo, ops.get(), w32, 1, in, opt.damp != 0, opt.damping_factor,
+                    FINISH_APPLY, ainv32.p, out, nullptr, 1.0, with_dot ? &rs : nullptr,
+                    stream);
+}
+
+namespace {
+// Host side of a device-resident loop: after each iteration the done flag is
+// copied to pinned memory and the previous iteration's copy is inspected, so
+// the GPU always has the next iteration queued.
+struct Poller {
+  cudaStream_t s;
+  int* d_flags;
+  int* h_flags;
+  cudaEvent_t ev[2];
+  int k = 0;
+  Poller(cudaStream_t s_, int* d, int* h) : s(s_), d_flags(d), h_flags(h) {
+    CG_CUDA(cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming));
+    CG_CUDA(cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming));
+  }
+  ~Poller() {
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+  }
+  // Returns true once a finished state has been observed.
+  bool after_iteration() {
+    CG_CUDA(cudaMemcpyAsync(h_flags, d_flags, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    CG_CUDA(cudaEventRecord(ev[k & 1], s));
+    bool done = false;
+    if (k > 0) {
+      CG_CUDA(cudaEventSynchronize(ev[(k - 1) & 1]));
+      done = ((volatile int*)h_flags)[0] != 0;
+    }
+    ++k;
+    return done;
+  }
+};
+}  // namespace
+
+int System::solve_fp64(bool zero_guess, double* hist_out, int hist_cap, int* iters) {
+  const int nb   = (n + VB - 1) / VB;
+  const int n3   = 3 * n;
+  const double t = opt.induced_thresh;
+  last           = SolveStats();
+  if (!zero_guess) {
+    apply64(x.p, Ap.p, false);
+    last.fp64_applies++;
+  }
+  k_cg_start<double><<<nb, VB, 0, stream>>>(n, F.p, zero_guess ? nullptr : Ap.p, alpha64.p,
+                                            r.p, z.p, p.p, slots(S_RED), scal.p, flags.p);
+  CG_LAUNCH();
+  if (zero_guess) CG_CUDA(cudaMemsetAsync(x.p, 0, sizeof(double) * n3, stream));
+  Poller poll(stream, flags.p, h_flags);
+  for (int k = 0; k < opt.maxiter; ++k) {
+    apply64(p.p, Ap.p, true);
+    last.fp64_applies++;
+    k_cg_update<double><<<nb, VB, 0, stream>>>(n, p.p, Ap.p, alpha64.p, x.p, r.p, z.p,
+                                               slots(S_RED), scal.p, flags.p, hist.p, t,
+                                               opt.maxiter);
+    CG_LAUNCH();
+    k_cg_dir<double><<<(n3 + VB - 1) / VB, VB, 0, stream>>>(n3, z.p, p.p, scal.p, flags.p);
+    CG_LAUNCH();
+    if (poll.after_iteration()) break;
+  }
+  CG_CUDA(cudaMemcpyAsync(h_flags, flags.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream));
+  CG_CUDA(cudaMemcpyAsync(h_scal, scal.p, S_NSCAL * sizeof(double), cudaMemcpyDeviceToHost,
+                          stream));
+  CG_CUDA(cudaStreamSynchronize(stream));
+  const int it = h_flags[1];
+  // applies queued after convergence did no work on x
+  last.fp64_applies = std::min(last.fp64_applies, it + (zero_guess ? 0 : 1));
+  last.iterations   = it;
+  last.final_rnorm  = h_scal[S_RNORM];
+  if (iters) *iters = it;
+  if (hist_out && hist_cap > 0 && it > 0)
+    CG_CUDA(cudaMemcpy(hist_out, hist.p, sizeof(double) * std::min(it, hist_cap),
+                       cudaMemcpyDeviceToHost));
+  return h_flags[0] == 1 ? CPPE_GPU_OK : CPPE_GPU_NOT_CONVERGED;
+}
+
+int System::solve_mixed(bool zero_guess, double* hist_out, int hist_cap, int* iters) {
+  const int nb   = (n + VB - 1) / VB;
+  const int n3   = 3 * n;
+  const int nb3  = (n3 + VB - 1) / VB;
+  const double t = opt.induced_thresh;
+  const double eta = 3e-6;   // relative residual reduction asked of each FP32 inner solve
+  const int max_outer = 12;
+  last = SolveStats();
+  std::vector<double> outer_hist;
+  int total_inner = 0;
+  CG_CUDA(cudaMemsetAsync(d32.p, 0, sizeof(float) * n3, stream));
+  // First residual: FP32 operator on the start vector (the refinement below
+  // removes its error), or the rhs itself for a zero start.
+  if (zero_guess) {
+    CG_CUDA(cudaMemsetAsync(x.p, 0, sizeof(double) * n3, stream));
+    k_residual<<<nb3, VB, 0, stream>>>(n3, F.p, nullptr, r.p, slots(S_RED), scal.p);
+    CG_LAUNCH();
+  } else {
+    k_to_f32<<<nb3, VB, 0, stream>>>(n3, x.p, p32.p);
+    CG_LAUNCH();
+    apply32(p32.p, Ap32.p, false);
+    last.fp32_applies++;
+    k_cg_start<float><<<nb, VB, 0, stream>>>(n, F.p, Ap32.p, alpha32.p, r32.p, z32.p, p32.p,
+                                             slots(S_RED), scal.p, flags.p);
+    CG_LAUNCH();
+  }
+  bool have_inner_start = !zero_guess;
+  int status            = CPPE_GPU_NOT_CONVERGED;
+  for (int outer = 0; outer < max_outer; ++outer) {
+    double rnorm;
+    if (!have_inner_start) {
+      // r holds the FP64 residual; read its norm and set up the inner solve.
+      CG_CUDA(cudaMemcpyAsync(h_scal, scal.p, S_NSCAL * sizeof(double), cudaMemcpyDeviceToHost,
+                              stream));
+      CG_CUDA(cudaStreamSynchronize(stream));
+      rnorm = h_scal[S_RNORM];
+      outer_hist.push_back(rnorm);
+      if (rnorm < t) {
+        status = CPPE_GPU_OK;
+        break;
+      }
+      // inner right-hand side: the FP64 residual
+      k_cg_start<float><<<nb, VB, 0, stream>>>(n, r.p, nullptr, alpha32.p, r32.p, z32.p,
+                                               p32.p, slots(S_RED), scal.p, flags.p);
+      CG_LAUNCH();
+    } else {
+      CG_CUDA(cudaMemcpyAsync(h_scal, scal.p, S_NSCAL * sizeof(double), cudaMemcpyDeviceToHost,
+                              stream));
+      CG_CUDA(cudaStreamSynchronize(stream));
+      rnorm = h_scal[S_RNORM];
+    }
+    have_inner_start = false;
+    const double tol = std::max(eta * rnorm, 0.25 * t);
+    Poller poll(stream, flags.p, h_flags);
+    for (int k = 0; k < std::max(1, opt.maxiter); ++k) {
+      apply32(p32.p, Ap32.p, true);
+      last.fp32_applies++;
+      k_cg_update<float><<<nb, VB, 0, stream>>>(n, p32.p, Ap32.p, alpha32.p, d32.p, r32.p,
+                                                z32.p, slots(S_RED), scal.p, flags.p, nullptr,
+                                                tol, std::max(1, opt.maxiter));
+      CG_LAUNCH();
+      k_cg_dir<float><<<nb3, VB, 0, stream>>>(n3, z32.p, p32.p, scal.p, flags.p);
+      CG_LAUNCH();
+      if (poll.after_iteration()) break;
+    }
+    CG_CUDA(cudaMemcpyAsync(h_flags, flags.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CG_CUDA(cudaStreamSynchronize(stream));
+    total_inner += h_flags[1];
+    last.fp32_applies = std::min(last.fp32_applies, total_inner + (zero_guess ? 0 : 1));
+    // x += d; r = F - B64 x
+    k_accumulate<<<nb3, VB, 0, stream>>>(n3, x.p, d32.p);
+    CG_LAUNCH();
+    apply64(x.p, Ap.p, false);
+    last.fp64_applies++;
+    k_residual<<<nb3, VB, 0, stream>>>(n3, F.p, Ap.p, r.p, slots(S_RED), scal.p);
+    CG_LAUNCH();
+  }
+  if (status != CPPE_GPU_OK) {
+    CG_CUDA(cudaMemcpyAsync(h_scal, scal.p, S_NSCAL * sizeof(double), cudaMemcpyDeviceToHost,
+                            stream));
+    CG_CUDA(cudaStreamSynchronize(stream));
+    if (h_scal[S_RNORM] < t) status = CPPE_GPU_OK;
+    outer_hist.push_back(h_scal[S_RNORM]);
+  }
+  last.iterations  = total_inner;
+  last.final_rnorm = outer_hist.empty() ? 0.0 : outer_hist.back();
+  // one recorded norm per FP64 refinement residual
+  if (iters) *iters = (int)outer_hist.size();
+  if (hist_out)
+    for (int k = 0; k < std::min<int>(hist_cap, (int)outer_hist.size()); ++k)
+      hist_out[k] = outer_hist[k];
+  return status;
+}
+
+int System::solve_device(const double* d_rhs, const double* d_guess, int make_guess,
+                         double* d_mu, int* iters, double* hist_out, int hist_cap) {
+  CG_CUDA(cudaSetDevice(device));
+  const int n3 = 3 * n;
+  permute_in(geo, d_rhs, F.p, 3, stream);
+  bool zero = false;
+  if (make_guess) {
+    k_sym_apply<<<(n + VB - 1) / VB, VB, 0, stream>>>(n, alpha64.p, F.p, x.p);
+    CG_LAUNCH();
+  } else if (d_guess) {
+    permute_in(geo, d_guess, x.p, 3, stream);
+  } else {
+    zero = true;
+  }
+  (void)n3;
+  int st = opt.precision == CPPE_GPU_MIXED ? solve_mixed(zero, hist_out, hist_cap, iters)
+                                           : solve_fp64(zero, hist_out, hist_cap, iters);
+  permute_out(geo, x.p, d_mu, 3, stream);
+  CG_CUDA(cudaStreamSynchronize(stream));
+  return st;
+}
+
+}  // namespace cg

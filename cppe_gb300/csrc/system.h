@@ -1,0 +1,71 @@
+// One polarizable system on the GPU: geometry, operator data, the work
+// buffers of the FP64 and mixed-precision solvers, and its stream.
+#pragma once
+
+#include <memory>
+
+#include "engine.h"
+
+namespace cg {
+
+// Scalar slots of the solver (device, FP64).
+enum Scalar {
+  S_RZ = 0,   // r . z of the current iterate
+  S_PAP,      // p . Ap
+  S_RR,       // r . r
+  S_RZNEW,    // r' . z'
+  S_BETA,     // beta
+  S_RNORM,    // ||r||_2 after the last update
+  S_TOL,      // stopping threshold of the running loop
+  S_RED = 8,  // 4 slots receiving grid reductions
+  S_NSCAL = 16
+};
+
+struct SolveStats {
+  double final_rnorm = 0.0;
+  int fp64_applies = 0, fp32_applies = 0, iterations = 0;
+};
+
+struct System {
+  int n = 0;
+  cppe_gpu_options opt{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  Geometry geo;
+  std::unique_ptr<DeviceOps> ops;  // m = 1, p = order (FMM only)
+  FieldWork<double> w64;
+  FieldWork<float> w32;
+  // operator data in device order
+  DBuf<double> ainv64, alpha64;  // 6 per site
+  DBuf<float> ainv32, alpha32;
+  // solver vectors (device order, 3n)
+  DBuf<double> F, x, r, z, p, Ap, tmp_in, tmp_out;
+  DBuf<float> r32, z32, p32, Ap32, d32;
+  DBuf<double> scal, partials, hist;
+  DBuf<unsigned> ticket;
+  DBuf<int> flags;  // [0] done, [1] iteration counter
+  int* h_flags = nullptr;     // pinned mirror
+  double* h_scal = nullptr;   // pinned mirror
+  SolveStats last;
+  std::vector<int> excl_ptr_h, excl_idx_h;  // caller-order exclusions (dense matrix)
+
+  ~System();
+  void init(int n, const double* xyz, const double* alpha6, const int* excl_ptr,
+            const int* excl_idx, const cppe_gpu_options& o);
+  // FP64 / FP32 operator on device-order vectors.
+  void apply64(const double* in, double* out, bool with_dot);
+  void apply32(const float* in, float* out, bool with_dot);
+  // FP32 operator on FP64 device-order vectors (rounded in, widened out).
+  void apply32_widen(const double* in, double* out);
+  ReduceSlots slots(int k) const;
+  // Average device time (ms) per phase of `reps` applies: near field, P2M+M2M,
+  // M2L, L2L, finishing pass, whole apply.
+  void phase_timings(int precision, int reps, double* ms);
+  // solves in device order: F holds the rhs, x the start vector
+  int solve_fp64(bool zero_guess, double* hist_out, int hist_cap, int* iters);
+  int solve_mixed(bool zero_guess, double* hist_out, int hist_cap, int* iters);
+  int solve_device(const double* d_rhs, const double* d_guess, int make_guess, double* d_mu,
+                   int* iters, double* hist_out, int hist_cap);
+};
+
+}  // namespace cg

@@ -1,0 +1,200 @@
+/*
+ * cppe_gpu.h -- C ABI of the GB300 (sm_103a) induced-dipole library.
+ *
+ * Plain pointers and sizes only.  Every function returns a cppe_gpu_status;
+ * cppe_gpu_last_error() gives the message of the last failure on the calling
+ * thread.  Host buffers are read/written synchronously unless the name ends in
+ * _device, in which case the pointers are device pointers on the handle's
+ * device and the call is ordered on the handle's stream.
+ *
+ * Vectors follow the reference layout: site-major xyz, 3*n doubles, sites in
+ * the caller's (polarizable-site) order.  alpha6 holds the polarizability
+ * upper triangle xx,xy,xz,yy,yz,zz per site (Polarizability,
+ * src/core/potential.hh:45-72).  Exclusions are a CSR list of 0-based site
+ * indices (Potential::m_exclusions, potential.hh:79); as in the reference they
+ * are compared against polarizable-site indices (tree.cc:145).
+ *
+ * Reference interfaces each entry point replaces (maxscheurer/cppe):
+ *   cppe_gpu_create / destroy        BMatrix::BMatrix        src/core/bmatrix.hh:19-36
+ *                                    InducedMoments ctor     src/core/electric_fields.hh:62-66
+ *   cppe_gpu_bmatrix_apply[_device]  BMatrix::apply          src/core/bmatrix.cc:9-40
+ *   cppe_gpu_apply_diagonal          BMatrix::apply_diagonal src/core/bmatrix.cc:53-62
+ *   cppe_gpu_apply_diagonal_inverse  BMatrix::apply_diagonal_inverse src/core/bmatrix.cc:42-51
+ *   cppe_gpu_to_dense                BMatrix::to_dense_matrix src/core/bmatrix.cc:64-92
+ *   cppe_gpu_direct_inverse          BMatrix::direct_inverse src/core/bmatrix.cc:94-97
+ *   cppe_gpu_solve[_device]          InducedMoments::compute src/core/electric_fields.cc:191-239
+ *   cppe_gpu_multipole_fields        MultipoleFields::compute src/core/electric_fields.cc:106-189
+ *   cppe_gpu_charge_fields           NuclearFields::compute  src/core/electric_fields.cc:58-75
+ *   cppe_gpu_multipole_potential_energy
+ *                                    MultipoleExpansion::interaction_energy
+ *                                                            src/core/multipole_expansion.cc:10-33
+ *   cppe_gpu_tree_info               build_shared_tree + interact_dehnen_lazy
+ *                                    src/core/fmm/tree.cc:134-237, calculate.cc:74-127
+ *                                    (host-only; no GPU needed)
+ *   cppe_gpu_batch_*                 no single counterpart: many InducedMoments::compute
+ *                                    calls (snapshots x right-hand sides) in one launch
+ */
+#ifndef CPPE_GPU_H
+#define CPPE_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  CPPE_GPU_OK            = 0,
+  CPPE_GPU_NOT_CONVERGED = 1, /* "Failed to converge induced dipole moments." */
+  CPPE_GPU_INVALID_ARG   = 2,
+  CPPE_GPU_CUDA_ERROR    = 3,
+  CPPE_GPU_TIMEOUT       = 4,
+  CPPE_GPU_NO_DEVICE     = 5
+} cppe_gpu_status;
+
+/* Summation schemes (PeOptions::summation_induced_fields, pe_options.hh:28-29):
+ * any string other than "fmm" means direct summation (bmatrix.cc:31-36). */
+enum { CPPE_GPU_DIRECT = 0, CPPE_GPU_FMM = 1 };
+
+/* Arithmetic of the solve (no counterpart in PeOptions; GPU-only knob).
+ *   FP64  : every apply, dot and update in FP64 (the reference's arithmetic).
+ *   MIXED : inner PCG in FP32 (pair kernels, FMM, apply) with FP64 dots;
+ *           FP64 residual recomputation and iterative refinement outside;
+ *           convergence is still ||F - B x||_2 < induced_thresh in FP64. */
+enum { CPPE_GPU_FP64 = 0, CPPE_GPU_MIXED = 1 };
+
+typedef struct {
+  int summation;             /* CPPE_GPU_DIRECT or CPPE_GPU_FMM               */
+  int tree_ncrit;            /* PeOptions::tree_ncrit            (default 64)  */
+  int tree_expansion_order;  /* PeOptions::tree_expansion_order  (default 5)   */
+  double theta;              /* PeOptions::theta                 (default 0.5) */
+  int damp;                  /* PeOptions::damp_induced          (default 0)   */
+  double damping_factor;     /* PeOptions::damping_factor_induced (2.1304)     */
+  double induced_thresh;     /* PeOptions::induced_thresh        (1e-8)        */
+  int maxiter;               /* PeOptions::maxiter               (50)          */
+  int precision;             /* CPPE_GPU_FP64 or CPPE_GPU_MIXED                */
+  int device;                /* CUDA device ordinal                            */
+} cppe_gpu_options;
+
+typedef struct cppe_gpu_system cppe_gpu_system;
+
+/* Fills opts with the reference defaults (pe_options.hh:17-33). */
+void cppe_gpu_default_options(cppe_gpu_options* opts);
+
+/* Message of the last failure on this thread (always NUL-terminated). */
+int cppe_gpu_last_error(char* buf, size_t len);
+
+/* Number of visible CUDA devices (0 when there is none). */
+int cppe_gpu_device_count(int* count);
+
+/* One polarizable system: n sites, positions (bohr), polarizabilities and
+ * exclusions.  Builds the octree and interaction lists once (for FMM) and
+ * uploads everything; later applies/solves reuse it. */
+int cppe_gpu_create(int n, const double* xyz, const double* alpha6, const int* excl_ptr,
+                    const int* excl_idx, const cppe_gpu_options* opts,
+                    cppe_gpu_system** out);
+int cppe_gpu_destroy(cppe_gpu_system* sys);
+
+/* out = B in, B = alpha^-1 - T (T: (Thole-damped) dipole field tensor). */
+int cppe_gpu_bmatrix_apply(cppe_gpu_system* sys, const double* in, double* out);
+int cppe_gpu_bmatrix_apply_device(cppe_gpu_system* sys, const double* d_in, double* d_out);
+/* Same operator in FP32 arithmetic (inputs/outputs still FP64). */
+int cppe_gpu_bmatrix_apply_fp32(cppe_gpu_system* sys, const double* in, double* out);
+int cppe_gpu_apply_diagonal(cppe_gpu_system* sys, const double* in, double* out);
+int cppe_gpu_apply_diagonal_inverse(cppe_gpu_system* sys, const double* in, double* out);
+/* Dense 3n x 3n B (row-major), and its inverse. */
+int cppe_gpu_to_dense(cppe_gpu_system* sys, double* out);
+int cppe_gpu_direct_inverse(cppe_gpu_system* sys, double* out);
+
+/* Induced dipoles: solves B mu = rhs to ||rhs - B mu||_2 < induced_thresh.
+ * guess may be NULL; make_guess != 0 uses alpha * rhs (electric_fields.cc:198-202).
+ * iters receives the number of recorded residual norms and rnorm_hist
+ * (capacity hist_cap, may be NULL) the norms themselves: in FP64 one per CG
+ * iteration, exactly the values the reference prints; in MIXED one per FP64
+ * refinement residual (the FP32 inner iterations are counted by
+ * cppe_gpu_last_solve_stats).  Returns CPPE_GPU_NOT_CONVERGED after maxiter. */
+int cppe_gpu_solve(cppe_gpu_system* sys, const double* rhs, const double* guess,
+                   int make_guess, double* mu, int* iters, double* rnorm_hist,
+                   int hist_cap);
+int cppe_gpu_solve_device(cppe_gpu_system* sys, const double* d_rhs, const double* d_guess,
+                          int make_guess, double* d_mu, int* iters, double* rnorm_hist,
+                          int hist_cap);
+/* Final FP64 residual norm and number of FP64 / FP32 operator applications of
+ * the last solve on this handle. */
+int cppe_gpu_last_solve_stats(cppe_gpu_system* sys, double* final_rnorm, int* fp64_applies,
+                              int* fp32_applies);
+
+/* Static multipole field at all n sites (MultipoleFields::compute): +F(q)
+ * -F(mu) +F(theta') with theta' = quadrupoles with halved diagonal; q (n),
+ * mu (3n), quad (6n, xx,xy,xz,yy,yz,zz, traceless) may be NULL when max_order
+ * is lower.  polarizable/alpha_iso give the Thole damping partners (damp != 0).
+ * summation/ncrit/order/theta as in cppe_gpu_options. */
+int cppe_gpu_multipole_fields(int n, const double* xyz, const double* q, const double* mu,
+                              const double* quad, int max_order, const int* polarizable,
+                              const double* alpha_iso, const int* excl_ptr,
+                              const int* excl_idx, int summation, int ncrit, int order,
+                              double theta, int damp, double damping_factor, int device,
+                              double* F);
+
+/* Field of point charges (charges q at xyz_src, nsrc of them) at ntgt points:
+ * F_i = sum_k q_k (r_i - R_k)/|r_i - R_k|^3 (NuclearFields::compute). */
+int cppe_gpu_charge_fields(int ntgt, const double* xyz_tgt, int nsrc, const double* xyz_src,
+                           const double* q, int device, double* F);
+
+/* sum_atoms Z_a * phi_multipoles(R_a) (MultipoleExpansion::interaction_energy). */
+int cppe_gpu_multipole_potential_energy(int n, const double* xyz, const double* q,
+                                        const double* mu, const double* quad, int max_order,
+                                        int natoms, const double* atom_xyz,
+                                        const double* atom_charge, int device,
+                                        double* energy);
+
+/* Host-only: octree and interaction-list sizes for a geometry (no GPU). */
+int cppe_gpu_tree_info(int n, const double* xyz, int ncrit, double theta, int* ncells,
+                       int* nleaves, long* nm2l, long* np2p, long* p2p_pairs);
+/* Host-only: the interaction lists themselves in the reference's cell
+ * numbering (creation order): m2l (nm2l x 2, (source, target)) and p2p
+ * (np2p x 2, (target, source)). */
+int cppe_gpu_tree_lists(int n, const double* xyz, int ncrit, double theta, int* m2l,
+                        int* p2p);
+
+/* ---------------------------------------------------------------------------
+ * Instrumentation (no counterpart in the reference).
+ * ------------------------------------------------------------------------- */
+/* The cudaStream_t the system's work is ordered on (for caller-side events). */
+int cppe_gpu_stream(cppe_gpu_system* sys, void** stream);
+/* Number of kernels this library has launched in this process. */
+int cppe_gpu_launch_count(long long* count);
+/* Average device time in ms of each phase over `reps` operator applies in the
+ * given precision, bracketed by CUDA events on the system's stream:
+ * out_ms[0] near-field pair pass, [1] P2M+M2M, [2] M2L, [3] L2L,
+ * [4] finishing pass (L2P, exclusions, alpha^-1, dot), [5] whole apply.
+ * near_pairs: ordered site pairs of the near-field pass that the reference
+ * evaluates (self and excluded pairs not counted); m2l_pairs: M2L cell pairs. */
+int cppe_gpu_kernel_timings(cppe_gpu_system* sys, int precision, int reps, double* out_ms,
+                            long long* near_pairs, long long* m2l_pairs);
+/* Measured FMA throughput of the device in TFLOP/s (2 FLOP per FMA), FP32 or FP64. */
+int cppe_gpu_fma_peak(int device, int fp64, double* tflops);
+
+/* ---------------------------------------------------------------------------
+ * Batched solves: nsys independent systems (snapshots) of uneven size, each
+ * with nrhs right-hand sides, solved together.  Site arrays are concatenated
+ * over systems; site_offset (nsys+1) gives each system's range.  Exclusion
+ * indices are local to their system.  rhs and mu are [system][rhs][3*n_s]
+ * concatenated (offset 3*nrhs*site_offset[s]).  Systems with fewer than
+ * direct_below sites use direct summation, the rest FMM with opts.
+ * ------------------------------------------------------------------------- */
+typedef struct cppe_gpu_batch cppe_gpu_batch;
+int cppe_gpu_batch_create(int nsys, const int* site_offset, const double* xyz,
+                          const double* alpha6, const int* excl_ptr, const int* excl_idx,
+                          int nrhs, int direct_below, const cppe_gpu_options* opts,
+                          cppe_gpu_batch** out);
+int cppe_gpu_batch_destroy(cppe_gpu_batch* b);
+int cppe_gpu_batch_solve(cppe_gpu_batch* b, const double* rhs, double* mu, int* iters);
+int cppe_gpu_batch_solve_device(cppe_gpu_batch* b, const double* d_rhs, double* d_mu,
+                                int* iters);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CPPE_GPU_H */

@@ -1,0 +1,178 @@
+"""CPU-side checks of the product: the C ABI library loads and exports every
+declared symbol, the host tree build matches the reference's lists, and the
+reference-facing Python API (options, potfile reader, data classes) behaves
+like the reference's on CPU (no GPU calls)."""
+import ctypes
+import hashlib
+
+import numpy as np
+import pytest
+
+import cabi
+
+
+def test_library_exports_every_declared_symbol():
+    lib = ctypes.CDLL(cabi.LIB_PATH)
+    names = cabi.declared_functions()
+    assert len(names) >= 20
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_default_options_match_reference():
+    o = cabi.options()
+    assert (o.tree_ncrit, o.tree_expansion_order, o.theta, o.maxiter) == (64, 5, 0.5, 50)
+    assert o.induced_thresh == 1e-8 and o.damping_factor == 2.1304 and o.damp == 0
+
+
+def _hash(m2l, p2p):
+    h = hashlib.sha256()
+    h.update(np.sort(m2l.view(np.int64).ravel()).tobytes())
+    h.update(np.sort(p2p.view(np.int64).ravel()).tobytes())
+    return h.hexdigest()
+
+
+@pytest.mark.parametrize("tag,nw,seed", [("c0", 333, 0), ("c1", 10000, 1)])
+def test_tree_lists_match_reference(golden_vectors, tag, nw, seed):
+    from cppe_gb300 import synthetic
+    b = synthetic.water_box(nw, seed=seed)
+    info, m2l, p2p = cabi.tree_lists(b.xyz, ncrit=64, theta=0.5)
+    counts = golden_vectors[f"tree_{tag}_counts"]
+    assert (info["ncells"], info["nm2l"], info["np2p"]) == tuple(counts)
+    assert _hash(m2l, p2p) == str(golden_vectors[f"tree_{tag}_hash"][0])
+
+
+def test_tree_lists_match_oracle_deep_tree(loprop, port):
+    # ncrit 16 puts many cell pairs exactly on the theta = 0.5 boundary
+    info, m2l, p2p = cabi.tree_lists(loprop.xyz, ncrit=16, theta=0.5)
+    t = port.tree_lists(loprop.xyz, ncrit=16, theta=0.5)
+    np.testing.assert_array_equal(p2p, t["p2p"])
+    np.testing.assert_array_equal(np.sort(m2l.view(np.int64).ravel()),
+                                  np.sort(t["m2l"].view(np.int64).ravel()))
+
+
+def test_tree_rejects_coincident_sites():
+    xyz = np.zeros((80, 3))
+    with pytest.raises(RuntimeError, match="coincide"):
+        cabi.tree_info(xyz, ncrit=64)
+
+
+# --- reference-facing Python API (host side only) ----------------------------
+@pytest.fixture(scope="module")
+def cppe():
+    import cppe_gb300
+    return cppe_gb300
+
+
+DEFAULT_OPTIONS = {
+    "iso_pol": False, "induced_thresh": 1e-8, "maxiter": 50, "damp_induced": False,
+    "damp_multipole": False, "damping_factor_induced": 2.1304,
+    "damping_factor_multipole": 2.1304, "summation_induced_fields": "direct",
+    "tree_expansion_order": 5, "tree_ncrit": 64, "theta": 0.5, "pe_border": False,
+    "border_type": "remove", "border_rmin": 2.2, "border_nredist": -1,
+    "border_redist_order": 1, "border_redist_pol": False,
+}
+
+
+def test_options_defaults(cppe, unpacked):
+    # tests/test_options.py:35-44
+    s = cppe.CppeState({"potfile": unpacked["pna_6w.pot"]})
+    opts = dict(s.options)
+    opts.pop("potfile")
+    assert len(opts) == len(DEFAULT_OPTIONS)
+    for k, v in DEFAULT_OPTIONS.items():
+        assert opts[k] == v
+
+
+def test_options_set_all(cppe, unpacked):
+    # tests/test_options.py:46-71
+    custom = {"potfile": unpacked["pna_6w.pot"], "iso_pol": True, "induced_thresh": 1e-4,
+              "maxiter": 500, "damp_induced": True, "damp_multipole": True,
+              "damping_factor_induced": 213.04, "damping_factor_multipole": 213.04,
+              "summation_induced_fields": "fmm", "tree_expansion_order": 4, "tree_ncrit": 12,
+              "theta": 0.2, "pe_border": True, "border_type": "redist", "border_rmin": 2.6,
+              "border_nredist": 2, "border_redist_order": 2, "border_redist_pol": True}
+    s = cppe.CppeState(custom)
+    for k, v in custom.items():
+        assert s.options[k] == v
+
+
+def test_options_invalid_key(cppe):
+    # tests/test_options.py:73-77
+    with pytest.raises(ValueError):
+        cppe.CppeState({"invalid_key": 42})
+    assert len(cppe.valid_option_keys) == 18
+
+
+def test_read_potfile(cppe, unpacked):
+    # tests/test_functionality.py:33-36
+    pots = cppe.PotfileReader(unpacked["pna_6w.pot"]).read()
+    assert len(pots) == 18
+    p = pots[0]
+    np.testing.assert_allclose(p.position, np.array([9.371, 2.953, -6.078]) * 1.8897261246)
+    assert p.exclusions == [1, 2] and p.excludes_site(2) and not p.excludes_site(3)
+    assert [m.k for m in p.multipoles] == [0, 1, 2]
+    q = p.multipoles[2].values
+    assert abs(q[0] + q[3] + q[5]) < 1e-12  # traceless after reading
+    np.testing.assert_allclose(p.polarizability.values,
+                               [2.30791521, 0.59643991, 0.58658837, 2.61100398, -0.10257978,
+                                2.60785108])
+    with pytest.raises(RuntimeError, match="does not exist"):
+        cppe.PotfileReader("/nonexistent.pot")
+
+
+def test_potfile_reader_matches_oracle_reader(cppe, unpacked, loprop):
+    pots = cppe.PotfileReader(unpacked["loprop_solvated_20.pot"]).read()
+    assert len(pots) == loprop.n
+    xyz = np.array([p.position for p in pots])
+    np.testing.assert_array_equal(xyz, loprop.xyz)
+    quad = np.array([p.multipoles[2].values for p in pots])
+    np.testing.assert_allclose(quad, loprop.quad, atol=1e-15)
+
+
+def test_iso_pol_makes_isotropic(cppe, unpacked):
+    s = cppe.CppeState({"potfile": unpacked["pna_6w.pot"], "iso_pol": True})
+    r = cppe.CppeState({"potfile": unpacked["pna_6w_isopol.pot"]})
+    for pt, pr in zip(s.potentials, r.potentials):
+        np.testing.assert_almost_equal(pt.polarizability.values, pr.polarizability.values)
+
+
+def test_state_positions_and_counts(cppe, unpacked):
+    s = cppe.CppeState({"potfile": unpacked["pna_6w.pot"]})
+    assert s.get_polarizable_site_number() == 18
+    assert s.positions.shape == (18, 3) and s.positions_polarizable.shape == (18, 3)
+    assert len(s.get_induced_moments()) == 54
+    en = s.energies["Electrostatic"]
+    en["Nuclear"] = -10.0
+    assert s.energies["Electrostatic"]["Nuclear"] == -10.0
+
+
+def test_math_helpers(cppe):
+    assert cppe.factorial(5) == 120 and cppe.trinom(1, 1, 0) == 2
+    assert cppe.multipole_components(2) == 6
+    assert list(cppe.symmetry_factors(2)) == [1, 2, 2, 1, 2, 1]
+    np.testing.assert_allclose(cppe.prefactors(1), [-1, -1, -1])
+    np.testing.assert_allclose(cppe.prefactors_nuclei(2), [0.5, 1, 1, 0.5, 1, 0.5])
+    m = cppe.triangle_to_mat([1, 2, 3, 4, 5, 6])
+    np.testing.assert_array_equal(cppe.mat_to_triangle(m), [1, 2, 3, 4, 5, 6])
+
+
+def test_gpu_calls_fail_loudly_without_device(cppe, unpacked):
+    if cabi.device_count() > 0:
+        pytest.skip("a GPU is present")
+    pots = cppe.PotfileReader(unpacked["pna_6w.pot"]).read()
+    b = cppe.BMatrix(cppe.get_polarizable_sites(pots), {})
+    with pytest.raises(RuntimeError):
+        b.apply(np.zeros(54))
+
+
+def test_synthetic_potfile_round_trip(cppe, tmp_path):
+    from cppe_gb300 import synthetic
+    b = synthetic.water_box(40, seed=5)
+    path = str(tmp_path / "w.pot")
+    synthetic.write_potfile(b, path)
+    pots = cppe.PotfileReader(path).read()
+    xyz = np.array([p.position for p in pots])
+    np.testing.assert_allclose(xyz, b.xyz, atol=1e-10)
+    assert all(p.exclusions == list(b.excl_idx[2 * i:2 * i + 2]) for i, p in enumerate(pots))
+    np.testing.assert_allclose([p.polarizability.isotropic_value for p in pots], b.alpha_iso)
