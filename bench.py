@@ -195,6 +195,14 @@ def run_ours(args):
               device=dev)
     smx = capi.System(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, precision=capi.MIXED, **kw)
     s64 = capi.System(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, precision=capi.FP64, **kw)
+    if args.apply_only:
+        # operator applies only (FP32 then FP64), e.g. for kernel profiling
+        t32 = smx.kernel_timings(capi.MIXED, reps=args.apply_only)
+        t64 = s64.kernel_timings(capi.FP64, reps=args.apply_only)
+        print(json.dumps({"apply_only": args.apply_only, "config": args.config,
+                          "fp32_ms": t32[0], "fp64_ms": t64[0], "alg_pairs": t32[1],
+                          "m2l_pairs": t32[2]}), flush=True)
+        return
     d_rhs = torch.tensor(rhs, dtype=torch.float64, device=f"cuda:{dev}")
     d_mu = torch.zeros_like(d_rhs)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{dev}")  # 256 MB
@@ -314,6 +322,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="c1", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--apply-only", type=int, default=0, metavar="K",
+                    help="run K FP32 and K FP64 operator applies and print phase timings")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

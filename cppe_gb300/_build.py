@@ -67,6 +67,8 @@ def _headers(d):
 
 def build_gpu_lib(jobs=8, verbose=False):
     os.makedirs(BUILD, exist_ok=True)
+    # straight-line fixed-order M2L translations (rewritten only when changed)
+    _run([sys.executable, os.path.join(CSRC, "gen_m2l.py"), os.path.join(CSRC, "m2l_gen.cuh")])
     nvcc = _nvcc()
     hdrs = _headers(CSRC)
     steps = []

@@ -82,7 +82,169 @@ def lib():
                                               ctypes.POINTER(ctypes.c_longlong),
                                               ctypes.POINTER(ctypes.c_longlong)]
         l.cppe_gpu_fma_peak.argtypes = [ctypes.c_int, ctypes.c_int, D]
+        l.cppe_gpu_batch_stats.argtypes = [ctypes.c_void_p, I, I, D]
+        l.cppe_gpu_batch_stream.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]
+        F = ctypes.POINTER(ctypes.c_float)
+        l.cppe_gpu_mlp_nparams.argtypes = [I]
+        l.cppe_gpu_mlp_create.argtypes = [ctypes.c_int, ctypes.c_uint,
+                                          ctypes.POINTER(ctypes.c_void_p)]
+        l.cppe_gpu_mlp_destroy.argtypes = [ctypes.c_void_p]
+        l.cppe_gpu_mlp_get_params.argtypes = [ctypes.c_void_p, F]
+        l.cppe_gpu_mlp_set_params.argtypes = [ctypes.c_void_p, F]
+        l.cppe_gpu_mlp_normalization.argtypes = [ctypes.c_void_p, F, F, F, F]
+        l.cppe_gpu_mlp_forward.argtypes = [ctypes.c_void_p, ctypes.c_int, F, F]
+        l.cppe_gpu_mlp_loss_grad.argtypes = [ctypes.c_void_p, ctypes.c_int, F, F,
+                                             ctypes.c_float, D, F]
+        l.cppe_gpu_mlp_train.argtypes = [ctypes.c_void_p, ctypes.c_int, F, F, ctypes.c_int,
+                                         ctypes.c_int, ctypes.c_float, ctypes.c_float,
+                                         ctypes.c_uint, D]
+        l.cppe_gpu_learned_data.argtypes = [ctypes.c_void_p, D, D, F, F]
+        l.cppe_gpu_set_model.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
     return _lib
+
+
+def f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def fp(a):
+    return None if a is None else a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+N_IN, N_OUT, TROW = 64, 4, 24
+
+
+class Mlp:
+    """The learned-guess network (cppe_gpu_mlp) on the GPU."""
+
+    def __init__(self, seed=0, device=0):
+        h = ctypes.c_void_p()
+        check(lib().cppe_gpu_mlp_create(device, seed, ctypes.byref(h)))
+        self.h = h
+        n = ctypes.c_int(0)
+        lib().cppe_gpu_mlp_nparams(ctypes.byref(n))
+        self.nparams = n.value
+
+    def close(self):
+        if self.h:
+            lib().cppe_gpu_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def params(self):
+        out = np.zeros(self.nparams, np.float32)
+        check(lib().cppe_gpu_mlp_get_params(self.h, fp(out)))
+        return out
+
+    @params.setter
+    def params(self, p):
+        p = f32(p)
+        assert p.size == self.nparams
+        check(lib().cppe_gpu_mlp_set_params(self.h, fp(p)))
+
+    def set_normalization(self, mean, inv_std):
+        check(lib().cppe_gpu_mlp_normalization(self.h, fp(f32(mean)), fp(f32(inv_std)), None,
+                                               None))
+
+    def normalization(self):
+        m = np.zeros(N_IN, np.float32)
+        s = np.zeros(N_IN, np.float32)
+        check(lib().cppe_gpu_mlp_normalization(self.h, None, None, fp(m), fp(s)))
+        return m, s
+
+    def forward(self, feats):
+        feats = f32(feats)
+        y = np.zeros((feats.shape[0], N_OUT), np.float32)
+        check(lib().cppe_gpu_mlp_forward(self.h, feats.shape[0], fp(feats), fp(y)))
+        return y
+
+    def loss_grad(self, feats, rows, lam=1.0):
+        feats, rows = f32(feats), f32(rows)
+        g = np.zeros(self.nparams, np.float32)
+        l = ctypes.c_double(0)
+        check(lib().cppe_gpu_mlp_loss_grad(self.h, feats.shape[0], fp(feats), fp(rows), lam,
+                                           ctypes.byref(l), fp(g)))
+        return l.value, g
+
+    def train(self, feats, rows, steps, batch=4096, lr=3e-3, lam=1.0, seed=0):
+        feats, rows = f32(feats), f32(rows)
+        hist = np.zeros(max(steps, 1))
+        check(lib().cppe_gpu_mlp_train(self.h, feats.shape[0], fp(feats), fp(rows), steps,
+                                       batch, lr, lam, seed, dp(hist)))
+        return hist[:steps]
+
+
+class Batch:
+    """One cppe_gpu_batch: snapshots x right-hand sides solved together.
+
+    systems: list of objects with xyz (n,3), alpha6 (n,6), excl_ptr, excl_idx.
+    rhs / mu layout: [system][rhs][3 n_s] concatenated."""
+
+    def __init__(self, systems, nrhs, direct_below=4000, **opts):
+        off = np.zeros(len(systems) + 1, np.int32)
+        off[1:] = np.cumsum([s.xyz.shape[0] for s in systems])
+        self.off = off
+        self.nrhs = nrhs
+        xyz = f64(np.concatenate([s.xyz for s in systems]))
+        a6 = f64(np.concatenate([s.alpha6 for s in systems]))
+        ep = [0]
+        ei = []
+        for s in systems:
+            ep.extend(int(ep[-1]) + np.asarray(s.excl_ptr[1:]) - s.excl_ptr[0])
+            ei.append(np.asarray(s.excl_idx))
+        ep = i32(ep)
+        ei = i32(np.concatenate(ei)) if ei else i32([0])
+        self._keep = [off, xyz, a6, ep, ei]
+        self.opts = options(**opts)
+        h = ctypes.c_void_p()
+        check(lib().cppe_gpu_batch_create(len(systems), ip(off), dp(xyz), dp(a6), ip(ep), ip(ei),
+                                          nrhs, direct_below, ctypes.byref(self.opts),
+                                          ctypes.byref(h)))
+        self.h = h
+        self.nseg = len(systems) * nrhs
+
+    def close(self):
+        if self.h:
+            lib().cppe_gpu_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def solve(self, rhs, allow_not_converged=False):
+        rhs = f64(rhs)
+        mu = np.zeros_like(rhs)
+        its = np.zeros(self.nseg, np.int32)
+        rc = lib().cppe_gpu_batch_solve(self.h, dp(rhs), dp(mu), ip(its))
+        check(rc, (OK, NOT_CONVERGED) if allow_not_converged else (OK,))
+        return mu, its
+
+    def solve_device(self, d_rhs, d_mu):
+        its = np.zeros(self.nseg, np.int32)
+        lib().cppe_gpu_batch_solve_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p,
+                                                      ctypes.c_void_p, I]
+        check(lib().cppe_gpu_batch_solve_device(self.h, d_rhs, d_mu, ip(its)))
+        return its
+
+    def stats(self):
+        a, b, r = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_double(0)
+        check(lib().cppe_gpu_batch_stats(self.h, ctypes.byref(a), ctypes.byref(b),
+                                         ctypes.byref(r)))
+        return dict(fp64_applies=a.value, fp32_applies=b.value, max_rnorm=r.value)
+
+    def stream(self):
+        s = ctypes.c_void_p()
+        check(lib().cppe_gpu_batch_stream(self.h, ctypes.byref(s)))
+        return s.value or 0
 
 
 def launch_count():
@@ -216,6 +378,18 @@ class System:
         s = ctypes.c_void_p()
         check(lib().cppe_gpu_stream(self.h, ctypes.byref(s)))
         return s.value or 0
+
+    def learned_data(self, rhs, mu_star):
+        """Descriptor rows (n x 64) and target rows (n x 24) of one solve."""
+        rhs, mu_star = f64(rhs), f64(mu_star)
+        feats = np.zeros((self.n, N_IN), np.float32)
+        rows = np.zeros((self.n, TROW), np.float32)
+        check(lib().cppe_gpu_learned_data(self.h, dp(rhs), dp(mu_star), fp(feats), fp(rows)))
+        return feats, rows
+
+    def set_model(self, mlp):
+        self._model = mlp
+        check(lib().cppe_gpu_set_model(self.h, mlp.h if mlp is not None else None))
 
     def kernel_timings(self, precision=FP64, reps=5):
         ms = np.zeros(6)

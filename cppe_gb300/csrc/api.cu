@@ -4,8 +4,10 @@
 #include <cmath>
 #include <cstring>
 #include <memory>
+#include <random>
 #include <string>
 
+#include "batch.h"
 #include "system.h"
 
 namespace cg {
@@ -179,12 +181,6 @@ __global__ void k_mp_energy(int n, const double* __restrict__ xyz, const double*
   grid_sum_last<1>(e, sh, rs.partials, rs.ticket, rs.out);
 }
 
-struct Batch {
-  std::vector<std::unique_ptr<System>> sys;
-  std::vector<int> off;  // site offsets
-  int nrhs = 1;
-};
-
 }  // namespace cg
 
 using namespace cg;
@@ -193,7 +189,10 @@ struct cppe_gpu_system {
   System s;
 };
 struct cppe_gpu_batch {
-  Batch b;
+  BatchSystem b;
+};
+struct cppe_gpu_mlp {
+  Mlp m;
 };
 
 extern "C" {
@@ -651,32 +650,17 @@ int cppe_gpu_tree_lists(int n, const double* xyz, int ncrit, double theta, int* 
   });
 }
 
-// Batched solves: one System per snapshot, all right-hand sides of all
-// snapshots solved on the GPU in turn.
+// Batched solves: all (snapshot, right-hand side) segments in one
+// concatenated geometry, one kernel launch per pass for all of them.
 int cppe_gpu_batch_create(int nsys, const int* site_offset, const double* xyz,
                           const double* alpha6, const int* excl_ptr, const int* excl_idx,
                           int nrhs, int direct_below, const cppe_gpu_options* opts,
                           cppe_gpu_batch** out) {
   return guard([&]() -> int {
     need(out && opts && site_offset && xyz && alpha6 && nsys > 0 && nrhs > 0, "null argument");
-    auto h    = std::make_unique<cppe_gpu_batch>();
-    h->b.nrhs = nrhs;
-    h->b.off.assign(site_offset, site_offset + nsys + 1);
-    for (int s = 0; s < nsys; ++s) {
-      const int o0 = site_offset[s], ns = site_offset[s + 1] - o0;
-      cppe_gpu_options o = *opts;
-      o.summation        = ns < direct_below ? CPPE_GPU_DIRECT : CPPE_GPU_FMM;
-      std::vector<int> ep, ei;
-      if (excl_ptr) {
-        ep.resize(ns + 1);
-        for (int i = 0; i <= ns; ++i) ep[i] = excl_ptr[o0 + i] - excl_ptr[o0];
-        ei.assign(excl_idx + excl_ptr[o0], excl_idx + excl_ptr[o0 + ns]);
-      }
-      auto sys = std::make_unique<System>();
-      sys->init(ns, xyz + 3 * (size_t)o0, alpha6 + 6 * (size_t)o0, excl_ptr ? ep.data() : nullptr,
-                excl_ptr ? (ei.empty() ? nullptr : ei.data()) : nullptr, o);
-      h->b.sys.push_back(std::move(sys));
-    }
+    *out   = nullptr;
+    auto h = std::make_unique<cppe_gpu_batch>();
+    h->b.init(nsys, site_offset, xyz, alpha6, excl_ptr, excl_idx, nrhs, direct_below, *opts);
     *out = h.release();
     return CPPE_GPU_OK;
   });
@@ -693,36 +677,226 @@ int cppe_gpu_batch_solve_device(cppe_gpu_batch* bh, const double* d_rhs, double*
                                 int* iters) {
   return guard([&]() -> int {
     need(bh && d_rhs && d_mu, "null argument");
-    Batch& B   = bh->b;
-    int status = CPPE_GPU_OK;
-    for (size_t s = 0; s < B.sys.size(); ++s) {
-      System& S         = *B.sys[s];
-      const size_t base = 3 * (size_t)B.nrhs * B.off[s];
-      for (int k = 0; k < B.nrhs; ++k) {
-        const size_t o = base + 3 * (size_t)k * S.n;
-        int it         = 0;
-        int st = S.solve_device(d_rhs + o, nullptr, 1, d_mu + o, &it, nullptr, 0);
-        if (iters) iters[s * B.nrhs + k] = it;
-        if (st != CPPE_GPU_OK) status = st;
-      }
-    }
-    return status;
+    return bh->b.solve_device(d_rhs, d_mu, iters);
   });
 }
 
 int cppe_gpu_batch_solve(cppe_gpu_batch* bh, const double* rhs, double* mu, int* iters) {
   return guard([&]() -> int {
     need(bh && rhs && mu, "null argument");
-    Batch& B        = bh->b;
-    const size_t n3 = 3 * (size_t)B.nrhs * B.off.back();
+    BatchSystem& B  = bh->b;
+    const size_t n3 = 3 * (size_t)B.n;
+    CG_CUDA(cudaSetDevice(B.device));
     DBuf<double> dr, dm;
-    CG_CUDA(cudaSetDevice(B.sys[0]->device));
-    dr.upload(rhs, n3, 0);
+    dr.upload(rhs, n3, B.stream);
     dm.alloc(n3);
-    CG_CUDA(cudaDeviceSynchronize());
-    int st = cppe_gpu_batch_solve_device(bh, dr.p, dm.p, iters);
-    CG_CUDA(cudaMemcpy(mu, dm.p, n3 * sizeof(double), cudaMemcpyDeviceToHost));
+    int st = B.solve_device(dr.p, dm.p, iters);
+    CG_CUDA(cudaMemcpyAsync(mu, dm.p, n3 * sizeof(double), cudaMemcpyDeviceToHost, B.stream));
+    CG_CUDA(cudaStreamSynchronize(B.stream));
     return st;
+  });
+}
+
+int cppe_gpu_batch_stats(cppe_gpu_batch* bh, int* fp64_applies, int* fp32_applies,
+                         double* max_rnorm) {
+  return guard([&]() -> int {
+    need(bh, "null argument");
+    BatchSystem& B = bh->b;
+    if (fp64_applies) *fp64_applies = B.stats.fp64_applies;
+    if (fp32_applies) *fp32_applies = B.stats.fp32_applies;
+    if (max_rnorm)
+      *max_rnorm = B.last_rnorm.empty()
+                         ? 0.0
+                         : *std::max_element(B.last_rnorm.begin(), B.last_rnorm.end());
+    return CPPE_GPU_OK;
+  });
+}
+
+int cppe_gpu_batch_stream(cppe_gpu_batch* bh, void** stream) {
+  return guard([&]() -> int {
+    need(bh && stream, "null argument");
+    *stream = (void*)bh->b.stream;
+    return CPPE_GPU_OK;
+  });
+}
+
+// ---------------------------------------------------------------------------
+// Learned initial guess / preconditioner: the MLP and its training data
+// ---------------------------------------------------------------------------
+int cppe_gpu_mlp_nparams(int* n) {
+  if (!n) return CPPE_GPU_INVALID_ARG;
+  *n = Mlp::NPARAM;
+  return CPPE_GPU_OK;
+}
+
+int cppe_gpu_mlp_create(int device, unsigned seed, cppe_gpu_mlp** out) {
+  return guard([&]() -> int {
+    need(out, "null argument");
+    *out   = nullptr;
+    auto h = std::make_unique<cppe_gpu_mlp>();
+    h->m.init(device, seed);
+    *out = h.release();
+    return CPPE_GPU_OK;
+  });
+}
+
+int cppe_gpu_mlp_destroy(cppe_gpu_mlp* m) {
+  return guard([&]() -> int {
+    delete m;
+    return CPPE_GPU_OK;
+  });
+}
+
+int cppe_gpu_mlp_get_params(cppe_gpu_mlp* h, float* out) {
+  return guard([&]() -> int {
+    need(h && out, "null argument");
+    CG_CUDA(cudaSetDevice(h->m.device));
+    CG_CUDA(cudaMemcpy(out, h->m.params.p, Mlp::NPARAM * sizeof(float), cudaMemcpyDeviceToHost));
+    return CPPE_GPU_OK;
+  });
+}
+
+int cppe_gpu_mlp_set_params(cppe_gpu_mlp* h, const float* in) {
+  return guard([&]() -> int {
+    need(h && in, "null argument");
+    CG_CUDA(cudaSetDevice(h->m.device));
+    CG_CUDA(cudaMemcpy(h->m.params.p, in, Mlp::NPARAM * sizeof(float), cudaMemcpyHostToDevice));
+    return CPPE_GPU_OK;
+  });
+}
+
+int cppe_gpu_mlp_normalization(cppe_gpu_mlp* h, const float* mean, const float* inv_std,
+                               float* mean_out, float* inv_std_out) {
+  return guard([&]() -> int {
+    need(h, "null argument");
+    CG_CUDA(cudaSetDevice(h->m.device));
+    if (mean) CG_CUDA(cudaMemcpy(h->m.feat_mean.p, mean, Mlp::IN * 4, cudaMemcpyHostToDevice));
+    if (inv_std)
+      CG_CUDA(cudaMemcpy(h->m.feat_inv_std.p, inv_std, Mlp::IN * 4, cudaMemcpyHostToDevice));
+    if (mean_out)
+      CG_CUDA(cudaMemcpy(mean_out, h->m.feat_mean.p, Mlp::IN * 4, cudaMemcpyDeviceToHost));
+    if (inv_std_out)
+      CG_CUDA(cudaMemcpy(inv_std_out, h->m.feat_inv_std.p, Mlp::IN * 4, cudaMemcpyDeviceToHost));
+    return CPPE_GPU_OK;
+  });
+}
+
+int cppe_gpu_mlp_forward(cppe_gpu_mlp* h, int rows, const float* feats, float* y) {
+  return guard([&]() -> int {
+    need(h && feats && y && rows > 0, "null argument");
+    Mlp& M = h->m;
+    CG_CUDA(cudaSetDevice(M.device));
+    DBuf<float> f, yo;
+    f.upload(feats, (size_t)rows * Mlp::IN, M.stream);
+    yo.alloc((size_t)rows * Mlp::OUT);
+    M.forward(rows, f.p, yo.p, M.stream);
+    CG_CUDA(cudaMemcpyAsync(y, yo.p, (size_t)rows * Mlp::OUT * 4, cudaMemcpyDeviceToHost, M.stream));
+    CG_CUDA(cudaStreamSynchronize(M.stream));
+    return CPPE_GPU_OK;
+  });
+}
+
+int cppe_gpu_mlp_loss_grad(cppe_gpu_mlp* h, int rows, const float* feats, const float* targets,
+                           float lam, double* loss, float* grads) {
+  return guard([&]() -> int {
+    need(h && feats && targets && rows > 0, "null argument");
+    Mlp& M = h->m;
+    CG_CUDA(cudaSetDevice(M.device));
+    DBuf<float> f, t;
+    f.upload(feats, (size_t)rows * Mlp::IN, M.stream);
+    t.upload(targets, (size_t)rows * Mlp::TROW, M.stream);
+    const double l = M.loss_grad(rows, f.p, t.p, lam);
+    if (loss) *loss = l;
+    if (grads)
+      CG_CUDA(cudaMemcpy(grads, M.grads.p, Mlp::NPARAM * sizeof(float), cudaMemcpyDeviceToHost));
+    return CPPE_GPU_OK;
+  });
+}
+
+__global__ void k_gather_rows(int rows, int width, const int* __restrict__ idx,
+                              const float* __restrict__ src, float* __restrict__ dst) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)rows * width) return;
+  const int r = (int)(t / width), c = (int)(t % width);
+  dst[t] = src[(size_t)idx[r] * width + c];
+}
+
+int cppe_gpu_mlp_train(cppe_gpu_mlp* h, int rows, const float* feats, const float* targets,
+                       int steps, int batch, float lr, float lam, unsigned seed,
+                       double* loss_hist) {
+  return guard([&]() -> int {
+    need(h && feats && targets && rows > 0 && steps >= 0 && batch > 0, "null argument");
+    Mlp& M = h->m;
+    CG_CUDA(cudaSetDevice(M.device));
+    DBuf<float> f, t, fb, tb;
+    DBuf<int> idx;
+    f.upload(feats, (size_t)rows * Mlp::IN, M.stream);
+    t.upload(targets, (size_t)rows * Mlp::TROW, M.stream);
+    batch = std::min(batch, rows);
+    fb.alloc((size_t)batch * Mlp::IN);
+    tb.alloc((size_t)batch * Mlp::TROW);
+    idx.alloc(batch);
+    std::mt19937 rng(seed);
+    std::uniform_int_distribution<int> pick(0, rows - 1);
+    std::vector<int> ih(batch);
+    for (int st = 0; st < steps; ++st) {
+      for (int b = 0; b < batch; ++b) ih[b] = pick(rng);
+      CG_CUDA(cudaMemcpyAsync(idx.p, ih.data(), batch * sizeof(int), cudaMemcpyHostToDevice,
+                              M.stream));
+      k_gather_rows<<<(unsigned)(((long)batch * Mlp::IN + 255) / 256), 256, 0, M.stream>>>(
+            batch, Mlp::IN, idx.p, f.p, fb.p);
+      CG_LAUNCH();
+      k_gather_rows<<<(unsigned)(((long)batch * Mlp::TROW + 255) / 256), 256, 0, M.stream>>>(
+            batch, Mlp::TROW, idx.p, t.p, tb.p);
+      CG_LAUNCH();
+      const double l = M.loss_grad(batch, fb.p, tb.p, lam);
+      M.adam(lr);
+      if (loss_hist) loss_hist[st] = l;
+    }
+    CG_CUDA(cudaStreamSynchronize(M.stream));
+    return CPPE_GPU_OK;
+  });
+}
+
+int cppe_gpu_learned_data(cppe_gpu_system* sys, const double* rhs, const double* mu_star,
+                          float* feats, float* rows) {
+  return guard([&]() -> int {
+    need(sys && rhs && mu_star && feats && rows, "null argument");
+    System& S = sys->s;
+    CG_CUDA(cudaSetDevice(S.device));
+    const size_t n3 = 3 * (size_t)S.n;
+    DBuf<double> dr, dm, dmp;
+    dr.upload(rhs, n3, S.stream);
+    dm.upload(mu_star, n3, S.stream);
+    dmp.alloc(n3);
+    permute_in(S.geo, dr.p, S.F.p, 3, S.stream);
+    permute_in(S.geo, dm.p, dmp.p, 3, S.stream);
+    std::vector<float> f, r;
+    S.learned_rows(dmp.p, f, r);
+    // weights of the loss terms, regularised by 1% of their system mean
+    double ms = 0, mt = 0;
+    for (int i = 0; i < S.n; ++i) ms += r[(size_t)i * Mlp::TROW + 21], mt += r[(size_t)i * Mlp::TROW + 22];
+    ms /= S.n, mt /= S.n;
+    for (int i = 0; i < S.n; ++i) {
+      r[(size_t)i * Mlp::TROW + 21] += (float)(0.01 * ms + 1e-30);
+      r[(size_t)i * Mlp::TROW + 22] += (float)(0.01 * mt + 1e-30);
+    }
+    std::copy(f.begin(), f.end(), feats);
+    std::copy(r.begin(), r.end(), rows);
+    return CPPE_GPU_OK;
+  });
+}
+
+int cppe_gpu_set_model(cppe_gpu_system* sys, cppe_gpu_mlp* mlp) {
+  return guard([&]() -> int {
+    need(sys, "null argument");
+    sys->s.model = mlp ? &mlp->m : nullptr;
+    if (mlp) {
+      CG_CUDA(cudaSetDevice(sys->s.device));
+      sys->s.learned_setup();
+      CG_CUDA(cudaStreamSynchronize(sys->s.stream));
+    }
+    return CPPE_GPU_OK;
   });
 }
 

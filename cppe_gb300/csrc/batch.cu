@@ -1,0 +1,566 @@
+// Batched solves: many independent systems (snapshots), each with several
+// right-hand sides, solved together.  Every (snapshot, right-hand side) pair
+// is a "segment": the segments' geometries are concatenated into one
+// Geometry (Geometry::combine) so that each pass of the operator is one
+// kernel launch over all segments, and the PCG keeps one set of scalars per
+// segment (InducedMoments::compute, src/core/electric_fields.cc:191-239, run
+// for every segment at once; a converged segment stops updating).
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <numeric>
+
+#include "batch.h"
+
+namespace cg {
+
+constexpr int BB = 256;
+
+// ---------------------------------------------------------------------------
+// Geometry concatenation
+// ---------------------------------------------------------------------------
+void Geometry::combine(const std::vector<const Geometry*>& parts, int copies, Geometry& out) {
+  out = Geometry();
+  const int np = (int)parts.size();
+  std::vector<int> site_off(np + 1, 0);
+  for (int g = 0; g < np; ++g) site_off[g + 1] = site_off[g] + parts[g]->n;
+  const int nseg = np * copies;
+  auto part_of   = [&](int s) { return s / copies; };
+  auto copy_of   = [&](int s) { return s % copies; };
+  int maxl       = 1;
+  bool any_fmm   = false;
+  for (auto* p : parts) {
+    maxl = std::max(maxl, (int)p->level_start.size() - 1);
+    any_fmm |= p->fmm;
+  }
+  TreeLayout& L = out.layout;
+  out.fmm       = any_fmm;
+  out.ncrit     = parts[0]->ncrit;
+  out.theta     = parts[0]->theta;
+  // cells: by (level, segment, cell)
+  std::vector<std::vector<int>> cmap(nseg);
+  for (int s = 0; s < nseg; ++s) cmap[s].assign(parts[part_of(s)]->layout.ncells, -1);
+  L.level_start.assign(maxl + 1, 0);
+  int nc = 0;
+  for (int l = 0; l < maxl; ++l) {
+    L.level_start[l] = nc;
+    for (int s = 0; s < nseg; ++s) {
+      const Geometry* p = parts[part_of(s)];
+      if (l + 1 >= (int)p->level_start.size()) continue;
+      for (int c = p->level_start[l]; c < p->level_start[l + 1]; ++c) cmap[s][c] = nc++;
+    }
+  }
+  L.level_start[maxl] = nc;
+  L.ncells            = nc;
+  L.nlevels           = maxl;
+  L.center.assign(4 * (size_t)nc, 0.0);
+  L.parent.assign(nc, -1);
+  L.is_leaf.assign(nc, 0);
+  std::vector<int> seg_of_cell(nc), local_of_cell(nc);
+  for (int s = 0; s < nseg; ++s)
+    for (int c = 0; c < (int)cmap[s].size(); ++c) {
+      const int k      = cmap[s][c];
+      seg_of_cell[k]   = s;
+      local_of_cell[k] = c;
+    }
+  L.child_ptr.assign(nc + 1, 0);
+  L.m2l_ptr.assign(nc + 1, 0);
+  for (int k = 0; k < nc; ++k) {
+    const int s = seg_of_cell[k], c = local_of_cell[k];
+    const TreeLayout& P = parts[part_of(s)]->layout;
+    for (int q = 0; q < 4; ++q) L.center[4 * (size_t)k + q] = P.center[4 * (size_t)c + q];
+    L.parent[k]  = P.parent[c] < 0 ? -1 : cmap[s][P.parent[c]];
+    L.is_leaf[k] = P.is_leaf[c];
+    for (int q = P.child_ptr[c]; q < P.child_ptr[c + 1]; ++q)
+      L.child_idx.push_back(cmap[s][P.child_idx[q]]);
+    L.child_ptr[k + 1] = (int)L.child_idx.size();
+    for (int q = P.m2l_ptr[c]; q < P.m2l_ptr[c + 1]; ++q)
+      L.m2l_src.push_back(cmap[s][P.m2l_src[q]]);
+    L.m2l_ptr[k + 1] = (int)L.m2l_src.size();
+  }
+  // leaves and particles: segment after segment
+  L.leaf_of_cell.assign(nc, -1);
+  L.leaf_start.assign(1, 0);
+  L.p2p_ptr.assign(1, 0);
+  L.n = 0;
+  for (int s = 0; s < nseg; ++s) {
+    const Geometry* p   = parts[part_of(s)];
+    const TreeLayout& P = p->layout;
+    const int r = copy_of(s), pi = part_of(s);
+    const int leaf0 = (int)L.leaf_cell.size(), site0 = L.n;
+    for (int a = 0; a < P.nleaves; ++a) {
+      const int k = cmap[s][P.leaf_cell[a]];
+      L.leaf_cell.push_back(k);
+      L.leaf_of_cell[k] = leaf0 + a;
+      L.leaf_start.push_back(site0 + P.leaf_start[a + 1]);
+      for (int q = P.p2p_ptr[a]; q < P.p2p_ptr[a + 1]; ++q) L.p2p_src.push_back(leaf0 + P.p2p_src[q]);
+      L.p2p_ptr.push_back((int)L.p2p_src.size());
+    }
+    const int caller0 = copies * site_off[pi] + r * p->n;
+    for (int k = 0; k < p->n; ++k) {
+      L.perm.push_back(caller0 + P.perm[k]);
+      out.h_site_leaf.push_back(leaf0 + p->h_site_leaf[k]);
+      out.h_pos64.push_back(p->h_pos64[k]);
+      out.h_hi.push_back(p->h_hi[k]);
+      out.h_lo.push_back(p->h_lo[k]);
+    }
+    if (out.h_cptr.empty()) out.h_cptr.push_back(0);
+    for (int k = 0; k < p->n; ++k) {
+      for (int q = p->h_cptr[k]; q < p->h_cptr[k + 1]; ++q) out.h_cidx.push_back(site0 + p->h_cidx[q]);
+      out.h_cptr.push_back((int)out.h_cidx.size());
+    }
+    L.n += p->n;
+    L.p2p_pairs += P.p2p_pairs;
+    out.near_pairs += p->near_pairs;
+    out.alg_pairs += p->alg_pairs;
+  }
+  L.nleaves = (int)L.leaf_cell.size();
+  out.n     = L.n;
+  L.inv_perm.assign(L.n, -1);
+  for (int k = 0; k < L.n; ++k) L.inv_perm[L.perm[k]] = k;
+  out.level_start = L.level_start;
+  out.make_items();
+}
+
+// ---------------------------------------------------------------------------
+// Segmented PCG kernels
+// ---------------------------------------------------------------------------
+template <typename A, typename B>
+__device__ __forceinline__ void bsym3(const A* a, const B* v, B* o) {
+  o[0] = (B)(a[0] * v[0] + a[1] * v[1] + a[2] * v[2]);
+  o[1] = (B)(a[1] * v[0] + a[3] * v[1] + a[4] * v[2]);
+  o[2] = (B)(a[2] * v[0] + a[4] * v[1] + a[5] * v[2]);
+}
+
+// Per-segment sums of one or two per-site arrays: block per segment.
+__global__ void k_seg_sum(const int* __restrict__ seg_start, const double* __restrict__ a,
+                          const double* __restrict__ b, double* __restrict__ oa,
+                          double* __restrict__ ob) {
+  __shared__ double sh[64];
+  const int g = blockIdx.x;
+  double v[2] = {0.0, 0.0};
+  for (int i = seg_start[g] + threadIdx.x; i < seg_start[g + 1]; i += blockDim.x) {
+    v[0] += a[i];
+    if (b) v[1] += b[i];
+  }
+  block_sum<2>(v, sh);
+  if (threadIdx.x == 0) {
+    oa[g] = v[0];
+    if (b) ob[g] = v[1];
+  }
+}
+
+// r = F - Ax, z = alpha r, p = z per site; site values r.z and r.r.
+template <typename T>
+__global__ void k_bcg_start(int n, const double* __restrict__ F, const T* __restrict__ Ax,
+                            const T* __restrict__ a6, T* __restrict__ r, T* __restrict__ z,
+                            T* __restrict__ p, double* __restrict__ s_rz,
+                            double* __restrict__ s_rr) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  T rv[3], zv[3];
+  for (int c = 0; c < 3; ++c) rv[c] = (T)(F[3 * i + c] - (Ax ? (double)Ax[3 * i + c] : 0.0));
+  bsym3(a6 + 6 * (size_t)i, rv, zv);
+  double rz = 0, rr = 0;
+  for (int c = 0; c < 3; ++c) {
+    r[3 * i + c] = rv[c], z[3 * i + c] = zv[c], p[3 * i + c] = zv[c];
+    rz += (double)rv[c] * zv[c];
+    rr += (double)rv[c] * rv[c];
+  }
+  s_rz[i] = rz, s_rr[i] = rr;
+}
+
+__global__ void k_bcg_init_seg(int nseg, const double* __restrict__ rz, const double* __restrict__ rr,
+                               double* __restrict__ seg_rz, double* __restrict__ seg_rnorm,
+                               int* __restrict__ done, int* __restrict__ iters,
+                               const double* __restrict__ tol) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= nseg) return;
+  seg_rz[g]    = rz[g];
+  seg_rnorm[g] = sqrt(rr[g]);
+  iters[g]     = 0;
+  // a segment whose residual already meets its tolerance takes no step
+  done[g] = (tol && seg_rnorm[g] < tol[g]) ? 1 : 0;
+}
+
+template <typename T>
+__global__ void k_bcg_update(int n, const int* __restrict__ site_seg, const T* __restrict__ p,
+                             const T* __restrict__ Ap, const T* __restrict__ a6,
+                             T* __restrict__ x, T* __restrict__ r, T* __restrict__ z,
+                             const double* __restrict__ seg_rz, const double* __restrict__ seg_pap,
+                             const int* __restrict__ done, double* __restrict__ s_rr,
+                             double* __restrict__ s_rz) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int g = site_seg[i];
+  if (done[g]) {
+    s_rr[i] = 0.0, s_rz[i] = 0.0;
+    return;
+  }
+  const T a = (T)(seg_rz[g] / seg_pap[g]);
+  T rv[3], zv[3];
+  for (int c = 0; c < 3; ++c) {
+    const size_t k = 3 * (size_t)i + c;
+    x[k] += a * p[k];
+    rv[c] = r[k] - a * Ap[k];
+    r[k]  = rv[c];
+  }
+  bsym3(a6 + 6 * (size_t)i, rv, zv);
+  double rr = 0, rz = 0;
+  for (int c = 0; c < 3; ++c) {
+    z[3 * (size_t)i + c] = zv[c];
+    rr += (double)rv[c] * rv[c];
+    rz += (double)rv[c] * zv[c];
+  }
+  s_rr[i] = rr, s_rz[i] = rz;
+}
+
+// Per segment: ||r||, beta, convergence; counts the segments still running.
+__global__ void k_bcg_finalize(int nseg, const double* __restrict__ rr,
+                               const double* __restrict__ rznew, double* __restrict__ seg_rz,
+                               double* __restrict__ seg_beta, double* __restrict__ seg_rnorm,
+                               int* __restrict__ done, int* __restrict__ iters,
+                               const double* __restrict__ tol, int maxiter,
+                               int* __restrict__ active) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= nseg) return;
+  if (done[g]) return;
+  const double rn = sqrt(rr[g]);
+  seg_rnorm[g]    = rn;
+  seg_beta[g]     = rznew[g] / seg_rz[g];
+  seg_rz[g]       = rznew[g];
+  const int it    = iters[g] + 1;
+  iters[g]        = it;
+  if (rn < tol[g])
+    done[g] = 1;
+  else if (it >= maxiter)
+    done[g] = 2;
+  else
+    atomicAdd(active, 1);
+}
+
+template <typename T>
+__global__ void k_bcg_dir(int n, const int* __restrict__ site_seg, const T* __restrict__ z,
+                          T* __restrict__ p, const double* __restrict__ seg_beta,
+                          const int* __restrict__ done) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int g = site_seg[i];
+  if (done[g]) return;
+  const T b = (T)seg_beta[g];
+  for (int c = 0; c < 3; ++c) p[3 * i + c] = z[3 * i + c] + b * p[3 * i + c];
+}
+
+__global__ void k_bres(int n, const double* __restrict__ F, const double* __restrict__ Ax,
+                       const float* __restrict__ Bd, double* __restrict__ r,
+                       double* __restrict__ s_rr) {
+  // r = F - Ax (Ax given) or r -= Bd (Bd given); site values of r.r
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double rr = 0;
+  for (int c = 0; c < 3; ++c) {
+    const size_t k = 3 * (size_t)i + c;
+    const double v = Ax ? F[k] - Ax[k] : r[k] - (double)Bd[k];
+    r[k]           = v;
+    rr += v * v;
+  }
+  s_rr[i] = rr;
+}
+
+__global__ void k_bsqrt(int nseg, const double* __restrict__ rr, double* __restrict__ rn) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g < nseg) rn[g] = sqrt(rr[g]);
+}
+
+__global__ void k_bacc(int n3, double* __restrict__ x, float* __restrict__ d) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n3) x[k] += (double)d[k], d[k] = 0.f;
+}
+
+__global__ void k_bf32(int n3, const double* __restrict__ a, float* __restrict__ b) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n3) b[k] = (float)a[k];
+}
+
+__global__ void k_bguess(int n, const double* __restrict__ a6, const double* __restrict__ F,
+                         double* __restrict__ x) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) bsym3(a6 + 6 * (size_t)i, F + 3 * (size_t)i, x + 3 * (size_t)i);
+}
+
+// ---------------------------------------------------------------------------
+// BatchSystem
+// ---------------------------------------------------------------------------
+BatchSystem::~BatchSystem() {
+  if (stream) {
+    cudaSetDevice(device);
+    cudaStreamSynchronize(stream);
+    cudaStreamDestroy(stream);
+  }
+  if (h_active) cudaFreeHost(h_active);
+}
+
+void BatchSystem::init(int nsys, const int* site_offset, const double* xyz, const double* alpha6,
+                       const int* excl_ptr, const int* excl_idx, int nrhs_, int direct_below,
+                       const cppe_gpu_options& o) {
+  opt  = o;
+  nrhs = nrhs_;
+  if (nsys < 1 || nrhs < 1) fail(CPPE_GPU_INVALID_ARG, "empty batch");
+  const bool any = true;
+  (void)any;
+  int ndev = 0;
+  CG_CUDA(cudaGetDeviceCount(&ndev));
+  if (o.device < 0 || o.device >= ndev) fail(CPPE_GPU_INVALID_ARG, "bad CUDA device ordinal");
+  device = o.device;
+  CG_CUDA(cudaSetDevice(device));
+  CG_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  if (o.tree_expansion_order < 2 || o.tree_expansion_order > 7)
+    fail(CPPE_GPU_INVALID_ARG, "tree_expansion_order must be in [2, 7]");
+  std::vector<Geometry> parts(nsys);
+  std::vector<const Geometry*> pp;
+  std::vector<double> a_inv, a_dir;
+  sys_sites.assign(site_offset, site_offset + nsys + 1);
+  for (int s = 0; s < nsys; ++s) {
+    const int o0 = site_offset[s], ns = site_offset[s + 1] - o0;
+    if (ns < 1) fail(CPPE_GPU_INVALID_ARG, "snapshot without sites");
+    std::vector<double> sd(ns, 0.0);
+    for (int i = 0; i < ns; ++i) {
+      const double* a = alpha6 + 6 * (size_t)(o0 + i);
+      const double iso = (a[0] + a[3] + a[5]) / 3.0;
+      if (o.damp && iso > 0.0) sd[i] = std::pow(iso, -1.0 / 6.0);
+    }
+    std::vector<int> ep, ei;
+    if (excl_ptr) {
+      ep.resize(ns + 1);
+      for (int i = 0; i <= ns; ++i) ep[i] = excl_ptr[o0 + i] - excl_ptr[o0];
+      ei.assign(excl_idx + excl_ptr[o0], excl_idx + excl_ptr[o0 + ns]);
+    }
+    const bool fmm = ns >= direct_below;
+    parts[s].prepare(ns, xyz + 3 * (size_t)o0, sd.data(), excl_ptr ? ep.data() : nullptr,
+                     ei.empty() ? nullptr : ei.data(), fmm, o.tree_ncrit, o.theta);
+    pp.push_back(&parts[s]);
+  }
+  Geometry::combine(pp, nrhs, geo);
+  geo.upload(stream);
+  if (geo.fmm) {
+    ops = std::make_unique<DeviceOps>();
+    ops->build(1, o.tree_expansion_order, stream);
+  }
+  n    = geo.n;
+  nseg = nsys * nrhs;
+  // segments in device order and per-site operator data
+  std::vector<int> seg_start_h(nseg + 1, 0), site_seg_h(n);
+  {
+    int k = 0;
+    for (int s = 0; s < nsys; ++s)
+      for (int r = 0; r < nrhs; ++r) {
+        const int ns = site_offset[s + 1] - site_offset[s];
+        for (int i = 0; i < ns; ++i) site_seg_h[k + i] = s * nrhs + r;
+        k += ns;
+        seg_start_h[s * nrhs + r + 1] = k;
+      }
+  }
+  std::vector<double> ainv(6 * (size_t)n), al(6 * (size_t)n);
+  for (int k = 0; k < n; ++k) {
+    // caller index -> (system, site)
+    const int c  = geo.layout.perm[k];
+    const int g  = site_seg_h[k];
+    const int sy = g / nrhs;
+    const int ns = site_offset[sy + 1] - site_offset[sy];
+    const int local = (c - nrhs * site_offset[sy]) % ns;
+    const double* a = alpha6 + 6 * (size_t)(site_offset[sy] + local);
+    const double A = a[3] * a[5] - a[4] * a[4], B = a[2] * a[4] - a[1] * a[5],
+                 C = a[1] * a[4] - a[2] * a[3];
+    const double id = 1.0 / (a[0] * A + a[1] * B + a[2] * C);
+    double* iv = &ainv[6 * (size_t)k];
+    iv[0] = A * id, iv[1] = B * id, iv[2] = C * id, iv[3] = (a[0] * a[5] - a[2] * a[2]) * id;
+    iv[4] = (a[1] * a[2] - a[0] * a[4]) * id, iv[5] = (a[0] * a[3] - a[1] * a[1]) * id;
+    std::copy(a, a + 6, &al[6 * (size_t)k]);
+  }
+  std::vector<float> ainvf(ainv.begin(), ainv.end()), alf(al.begin(), al.end());
+  ainv64.upload(ainv, stream);
+  alpha64.upload(al, stream);
+  ainv32.upload(ainvf, stream);
+  alpha32.upload(alf, stream);
+  seg_start.upload(seg_start_h, stream);
+  site_seg.upload(site_seg_h, stream);
+  const size_t n3 = 3 * (size_t)n;
+  for (auto* b : {&F, &x, &r, &z, &p, &Ap}) b->alloc(n3);
+  for (auto* b : {&r32, &z32, &p32, &Ap32, &d32}) b->alloc(n3);
+  for (auto* b : {&site_a, &site_b}) b->alloc(n);
+  for (auto* b : {&seg_rz, &seg_pap, &seg_rr, &seg_rznew, &seg_beta, &seg_rnorm, &seg_tol})
+    b->alloc(nseg);
+  done.alloc(nseg);
+  iters.alloc(nseg);
+  active.alloc(1);
+  CG_CUDA(cudaMallocHost(&h_active, sizeof(int)));
+  CG_CUDA(cudaStreamSynchronize(stream));
+}
+
+template <typename T>
+void BatchSystem::apply_seg(const T* in, T* out, bool fast_exp) {
+  ReduceSlots rs{nullptr, nullptr, nullptr};
+  rs.site_values = site_a.p;
+  FieldWork<T>& w = work<T>();
+  const T* ainv   = std::is_same<T, double>::value ? (const T*)ainv64.p : (const T*)ainv32.p;
+  eval_field<T>(geo, ops.get(), w, 1, in, opt.damp != 0, opt.damping_factor, FINISH_APPLY, ainv,
+                out, nullptr, 1.0, &rs, stream, nullptr, fast_exp);
+  k_seg_sum<<<nseg, BB, 0, stream>>>(seg_start.p, site_a.p, nullptr, seg_pap.p, nullptr);
+  CG_LAUNCH();
+}
+
+template <typename T>
+int BatchSystem::run_pcg(T* xv, T* rv, T* zv, T* pv, T* Apv, const T* a6, int maxiter) {
+  // (r, z, p, per-segment rz / rnorm / done set by the caller's start step)
+  const int nb = (n + BB - 1) / BB, gb = (nseg + 127) / 128;
+  int k = 0;
+  for (; k < maxiter; ++k) {
+    apply_seg<T>(pv, Apv);
+    if (std::is_same<T, double>::value)
+      stats.fp64_applies++;
+    else
+      stats.fp32_applies++;
+    k_bcg_update<T><<<nb, BB, 0, stream>>>(n, site_seg.p, pv, Apv, a6, xv, rv, zv, seg_rz.p,
+                                           seg_pap.p, done.p, site_a.p, site_b.p);
+    CG_LAUNCH();
+    k_seg_sum<<<nseg, BB, 0, stream>>>(seg_start.p, site_a.p, site_b.p, seg_rr.p, seg_rznew.p);
+    CG_LAUNCH();
+    CG_CUDA(cudaMemsetAsync(active.p, 0, sizeof(int), stream));
+    k_bcg_finalize<<<gb, 128, 0, stream>>>(nseg, seg_rr.p, seg_rznew.p, seg_rz.p, seg_beta.p,
+                                           seg_rnorm.p, done.p, iters.p, seg_tol.p, maxiter,
+                                           active.p);
+    CG_LAUNCH();
+    k_bcg_dir<T><<<nb, BB, 0, stream>>>(n, site_seg.p, zv, pv, seg_beta.p, done.p);
+    CG_LAUNCH();
+    CG_CUDA(cudaMemcpyAsync(h_active, active.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CG_CUDA(cudaStreamSynchronize(stream));
+    if (*h_active == 0) {
+      ++k;
+      break;
+    }
+  }
+  return k;
+}
+
+void BatchSystem::seg_norms_from_site_b() {
+  k_seg_sum<<<nseg, BB, 0, stream>>>(seg_start.p, site_b.p, nullptr, seg_rr.p, nullptr);
+  CG_LAUNCH();
+  k_bsqrt<<<(nseg + 127) / 128, 128, 0, stream>>>(nseg, seg_rr.p, seg_rnorm.p);
+  CG_LAUNCH();
+}
+
+int BatchSystem::solve_device(const double* d_rhs, double* d_mu, int* iters_out) {
+  CG_CUDA(cudaSetDevice(device));
+  stats = SolveStats();
+  const int nb = (n + BB - 1) / BB, n3 = 3 * n, nb3 = (n3 + BB - 1) / BB;
+  const double t = opt.induced_thresh;
+  permute_in(geo, d_rhs, F.p, 3, stream);
+  // first-call guess alpha F (electric_fields.cc:198-202)
+  k_bguess<<<nb, BB, 0, stream>>>(n, alpha64.p, F.p, x.p);
+  CG_LAUNCH();
+  std::vector<double> tolv(nseg, t);
+  CG_CUDA(cudaMemcpyAsync(seg_tol.p, tolv.data(), nseg * sizeof(double), cudaMemcpyHostToDevice,
+                          stream));
+  int status = CPPE_GPU_NOT_CONVERGED;
+  std::vector<int> it_h(nseg, 0), total(nseg, 0);
+  if (opt.precision != CPPE_GPU_MIXED) {
+    apply_seg<double>(x.p, Ap.p);
+    stats.fp64_applies++;
+    k_bcg_start<double><<<nb, BB, 0, stream>>>(n, F.p, Ap.p, alpha64.p, r.p, z.p, p.p, site_a.p,
+                                               site_b.p);
+    CG_LAUNCH();
+    k_seg_sum<<<nseg, BB, 0, stream>>>(seg_start.p, site_a.p, site_b.p, seg_rz.p, seg_rr.p);
+    CG_LAUNCH();
+    k_bcg_init_seg<<<(nseg + 127) / 128, 128, 0, stream>>>(nseg, seg_rz.p, seg_rr.p, seg_rz.p,
+                                                            seg_rnorm.p, done.p, iters.p, nullptr);
+    CG_LAUNCH();
+    run_pcg<double>(x.p, r.p, z.p, p.p, Ap.p, alpha64.p, std::max(1, opt.maxiter));
+    std::vector<int> dn(nseg);
+    CG_CUDA(cudaMemcpyAsync(dn.data(), done.p, nseg * sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CG_CUDA(cudaMemcpyAsync(it_h.data(), iters.p, nseg * sizeof(int), cudaMemcpyDeviceToHost,
+                            stream));
+    CG_CUDA(cudaStreamSynchronize(stream));
+    status = std::all_of(dn.begin(), dn.end(), [](int d) { return d == 1; }) ? CPPE_GPU_OK
+                                                                             : CPPE_GPU_NOT_CONVERGED;
+    total = it_h;
+  } else {
+    // mixed precision, as System::solve_mixed but with per-segment scalars
+    const double eta = 3e-6;
+    k_bf32<<<nb3, BB, 0, stream>>>(n3, x.p, p32.p);
+    CG_LAUNCH();
+    apply_seg<float>(p32.p, Ap32.p);
+    stats.fp32_applies++;
+    CG_CUDA(cudaMemsetAsync(d32.p, 0, sizeof(float) * n3, stream));
+    k_bcg_start<float><<<nb, BB, 0, stream>>>(n, F.p, Ap32.p, alpha32.p, r32.p, z32.p, p32.p,
+                                              site_a.p, site_b.p);
+    CG_LAUNCH();
+    k_seg_sum<<<nseg, BB, 0, stream>>>(seg_start.p, site_a.p, site_b.p, seg_rz.p, seg_rr.p);
+    CG_LAUNCH();
+    std::vector<double> rn(nseg);
+    k_bsqrt<<<(nseg + 127) / 128, 128, 0, stream>>>(nseg, seg_rr.p, seg_rnorm.p);
+    CG_LAUNCH();
+    CG_CUDA(cudaMemcpyAsync(rn.data(), seg_rnorm.p, nseg * sizeof(double), cudaMemcpyDeviceToHost,
+                            stream));
+    CG_CUDA(cudaStreamSynchronize(stream));
+    bool exact = false;
+    for (int outer = 0; outer < 12; ++outer) {
+      // inner tolerances; segments already below the threshold stay put
+      for (int g = 0; g < nseg; ++g) tolv[g] = std::max(eta * rn[g], 0.25 * t);
+      if (outer > 0) {
+        if (std::all_of(rn.begin(), rn.end(), [&](double v) { return v < t; })) {
+          status = CPPE_GPU_OK;
+          break;
+        }
+        for (int g = 0; g < nseg; ++g)
+          if (rn[g] < t) tolv[g] = 1e300;  // done at once
+        k_bcg_start<float><<<nb, BB, 0, stream>>>(n, r.p, nullptr, alpha32.p, r32.p, z32.p,
+                                                  p32.p, site_a.p, site_b.p);
+        CG_LAUNCH();
+        k_seg_sum<<<nseg, BB, 0, stream>>>(seg_start.p, site_a.p, site_b.p, seg_rz.p, seg_rr.p);
+        CG_LAUNCH();
+      }
+      CG_CUDA(cudaMemcpyAsync(seg_tol.p, tolv.data(), nseg * sizeof(double),
+                              cudaMemcpyHostToDevice, stream));
+      k_bcg_init_seg<<<(nseg + 127) / 128, 128, 0, stream>>>(
+            nseg, seg_rz.p, seg_rr.p, seg_rz.p, seg_rnorm.p, done.p, iters.p, seg_tol.p);
+      CG_LAUNCH();
+      run_pcg<float>(d32.p, r32.p, z32.p, p32.p, Ap32.p, alpha32.p, std::max(1, opt.maxiter));
+      CG_CUDA(cudaMemcpyAsync(it_h.data(), iters.p, nseg * sizeof(int), cudaMemcpyDeviceToHost,
+                              stream));
+      const double rmax = *std::max_element(rn.begin(), rn.end());
+      if (!(exact && rmax * 1e-4 < t)) {
+        k_bacc<<<nb3, BB, 0, stream>>>(n3, x.p, d32.p);
+        CG_LAUNCH();
+        apply_seg<double>(x.p, Ap.p, true);
+        stats.fp64_applies++;
+        k_bres<<<nb, BB, 0, stream>>>(n, F.p, Ap.p, nullptr, r.p, site_b.p);
+        CG_LAUNCH();
+        exact = true;
+      } else {
+        apply_seg<float>(d32.p, Ap32.p);
+        stats.fp32_applies++;
+        k_bres<<<nb, BB, 0, stream>>>(n, nullptr, nullptr, Ap32.p, r.p, site_b.p);
+        CG_LAUNCH();
+        k_bacc<<<nb3, BB, 0, stream>>>(n3, x.p, d32.p);
+        CG_LAUNCH();
+      }
+      seg_norms_from_site_b();
+      CG_CUDA(cudaMemcpyAsync(rn.data(), seg_rnorm.p, nseg * sizeof(double),
+                              cudaMemcpyDeviceToHost, stream));
+      CG_CUDA(cudaStreamSynchronize(stream));
+      for (int g = 0; g < nseg; ++g) total[g] += it_h[g];
+    }
+    if (status != CPPE_GPU_OK && std::all_of(rn.begin(), rn.end(), [&](double v) { return v < t; }))
+      status = CPPE_GPU_OK;
+    last_rnorm = rn;
+  }
+  if (iters_out) {
+    // caller order: [system][rhs]
+    for (int g = 0; g < nseg; ++g) iters_out[g] = total[g];
+  }
+  permute_out(geo, x.p, d_mu, 3, stream);
+  CG_CUDA(cudaStreamSynchronize(stream));
+  return status;
+}
+
+}  // namespace cg

@@ -1,0 +1,54 @@
+// Batched solves over many (snapshot, right-hand side) segments at once.
+#pragma once
+
+#include <memory>
+#include <type_traits>
+
+#include "system.h"
+
+namespace cg {
+
+struct BatchSystem {
+  int nrhs = 1, nseg = 0, n = 0;
+  cppe_gpu_options opt{};
+  int device          = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<int> sys_sites;  // site offsets of the snapshots (caller layout)
+  Geometry geo;                // all segments concatenated
+  std::unique_ptr<DeviceOps> ops;
+  FieldWork<double> w64;
+  FieldWork<float> w32;
+  DBuf<double> ainv64, alpha64;
+  DBuf<float> ainv32, alpha32;
+  DBuf<int> seg_start, site_seg;
+  DBuf<double> F, x, r, z, p, Ap;
+  DBuf<float> r32, z32, p32, Ap32, d32;
+  DBuf<double> site_a, site_b;  // per-site values of the segmented dots
+  DBuf<double> seg_rz, seg_pap, seg_rr, seg_rznew, seg_beta, seg_rnorm, seg_tol;
+  DBuf<int> done, iters, active;
+  int* h_active = nullptr;
+  SolveStats stats;
+  std::vector<double> last_rnorm;
+
+  ~BatchSystem();
+  void init(int nsys, const int* site_offset, const double* xyz, const double* alpha6,
+            const int* excl_ptr, const int* excl_idx, int nrhs, int direct_below,
+            const cppe_gpu_options& o);
+  // rhs / mu in the caller layout [system][rhs][3 n_s]; iters per segment.
+  int solve_device(const double* d_rhs, double* d_mu, int* iters);
+
+  template <typename T>
+  FieldWork<T>& work() {
+    if constexpr (std::is_same<T, double>::value)
+      return w64;
+    else
+      return w32;
+  }
+  template <typename T>
+  void apply_seg(const T* in, T* out, bool fast_exp = false);
+  template <typename T>
+  int run_pcg(T* x, T* r, T* z, T* p, T* Ap, const T* a6, int maxiter);
+  void seg_norms_from_site_b();
+};
+
+}  // namespace cg

@@ -18,6 +18,7 @@
 #include <numeric>
 
 #include "engine.h"
+#include "m2l_fixed.cuh"
 
 namespace cg {
 
@@ -76,6 +77,12 @@ TreeView Geometry::view() const {
 void Geometry::build(int n_, const double* xyz, const double* s_damp, const int* excl_ptr,
                      const int* excl_idx, bool fmm_, int ncrit_, double theta_,
                      cudaStream_t s) {
+  prepare(n_, xyz, s_damp, excl_ptr, excl_idx, fmm_, ncrit_, theta_);
+  upload(s);
+}
+
+void Geometry::prepare(int n_, const double* xyz, const double* s_damp, const int* excl_ptr,
+                       const int* excl_idx, bool fmm_, int ncrit_, double theta_) {
   n     = n_;
   fmm   = fmm_;
   ncrit = ncrit_;
@@ -121,17 +128,19 @@ void Geometry::build(int n_, const double* xyz, const double* s_damp, const int*
     level_start = L.level_start;
   }
   near_pairs = L.p2p_pairs;
-  // Source splits so that the near-field grid covers the GPU (152 SMs).
-  const int want = 4 * 152;
-  nsplit         = std::max(1, std::min(64, (want + L.nleaves - 1) / L.nleaves));
 
-  std::vector<int> site_leaf_h(n);
+  h_site_leaf.assign(n, 0);
+  std::vector<int>& site_leaf_h = h_site_leaf;
   for (int a = 0; a < L.nleaves; ++a)
     for (int k = L.leaf_start[a]; k < L.leaf_start[a + 1]; ++k) site_leaf_h[k] = a;
 
   // Coordinates in device order.
-  std::vector<double4_32a> p64(n);
-  std::vector<float4> hi(n), lo(n);
+  h_pos64.assign(n, double4_32a{});
+  h_hi.assign(n, float4{});
+  h_lo.assign(n, float4{});
+  auto& p64 = h_pos64;
+  auto& hi  = h_hi;
+  auto& lo  = h_lo;
   for (int k = 0; k < n; ++k) {
     const int i  = L.perm[k];
     const double x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
@@ -146,7 +155,10 @@ void Geometry::build(int n_, const double* xyz, const double* s_damp, const int*
   // includes.  Direct: every listed exclusion; FMM: those whose source sits in
   // a leaf of the target leaf's P2P list (exclusions are honoured only in P2P,
   // calculate.cc:37).
-  std::vector<int> cptr(n + 1, 0), cidx;
+  h_cptr.assign(n + 1, 0);
+  h_cidx.clear();
+  auto& cptr = h_cptr;
+  auto& cidx = h_cidx;
   if (excl_ptr) {
     std::vector<std::vector<int>> sorted_src;
     if (fmm) {
@@ -178,8 +190,57 @@ void Geometry::build(int n_, const double* xyz, const double* s_damp, const int*
   // algorithmic pairs: the ordered pairs the reference evaluates in its
   // near-field / direct loops (self pairs and excluded pairs are skipped there)
   alg_pairs = near_pairs - n - (long)cidx.size();
-  if (cidx.empty()) cidx.push_back(0);
+  make_items();
+}
 
+// Cuts every target leaf's source list into pieces of about `W` pairs so that
+// blocks get similar work, and orders the pieces largest first.
+void Geometry::make_items() {
+  const TreeLayout& L = layout;
+  long total          = 0;
+  for (int a = 0; a < L.nleaves; ++a) {
+    const long na = L.leaf_start[a + 1] - L.leaf_start[a];
+    for (int q = L.p2p_ptr[a]; q < L.p2p_ptr[a + 1]; ++q) {
+      const int b = L.p2p_src[q];
+      total += na * (L.leaf_start[b + 1] - L.leaf_start[b]);
+    }
+  }
+  const long W = std::max<long>(8192, total / (32L * 152));
+  struct It {
+    long w;
+    int4 v;
+  };
+  std::vector<It> its;
+  h_leaf_nslot.assign(L.nleaves, 0);
+  for (int a = 0; a < L.nleaves; ++a) {
+    const long na = L.leaf_start[a + 1] - L.leaf_start[a];
+    int q0 = L.p2p_ptr[a], slot = 0;
+    long acc = 0;
+    for (int q = L.p2p_ptr[a]; q < L.p2p_ptr[a + 1]; ++q) {
+      const int b = L.p2p_src[q];
+      acc += na * (L.leaf_start[b + 1] - L.leaf_start[b]);
+      if (acc >= W || q + 1 == L.p2p_ptr[a + 1]) {
+        its.push_back({acc, make_int4(a, q0, q + 1, slot++)});
+        q0  = q + 1;
+        acc = 0;
+      }
+    }
+    if (slot == 0) its.push_back({0, make_int4(a, q0, q0, slot++)});  // empty list: zeros
+    h_leaf_nslot[a] = slot;
+  }
+  std::stable_sort(its.begin(), its.end(), [](const It& x, const It& y) { return x.w > y.w; });
+  h_items.resize(its.size());
+  nslot = 1;
+  for (size_t k = 0; k < its.size(); ++k) {
+    h_items[k] = its[k].v;
+    nslot      = std::max(nslot, its[k].v.w + 1);
+  }
+}
+
+void Geometry::upload(cudaStream_t s) {
+  items.upload(h_items, s);
+  leaf_nslot.upload(h_leaf_nslot, s);
+  const TreeLayout& L = layout;
   center.upload(L.center, s);
   parent.upload(L.parent, s);
   child_ptr.upload(L.child_ptr, s);
@@ -187,18 +248,18 @@ void Geometry::build(int n_, const double* xyz, const double* s_damp, const int*
   is_leaf.upload(L.is_leaf, s);
   leaf_cell.upload(L.leaf_cell, s);
   leaf_start.upload(L.leaf_start, s);
-  site_leaf.upload(site_leaf_h, s);
+  site_leaf.upload(h_site_leaf, s);
   m2l_ptr.upload(L.m2l_ptr, s);
   m2l_src.upload(L.m2l_src.empty() ? std::vector<int>{0} : L.m2l_src, s);
   p2p_ptr.upload(L.p2p_ptr, s);
   p2p_src.upload(L.p2p_src, s);
   perm.upload(L.perm, s);
   inv_perm.upload(L.inv_perm, s);
-  pos64.upload(p64, s);
-  hi32.upload(hi, s);
-  lo32.upload(lo, s);
-  corr_ptr.upload(cptr, s);
-  corr_idx.upload(cidx, s);
+  pos64.upload(h_pos64, s);
+  hi32.upload(h_hi, s);
+  lo32.upload(h_lo, s);
+  corr_ptr.upload(h_cptr, s);
+  corr_idx.upload(h_cidx.empty() ? std::vector<int>{0} : h_cidx, s);
   CG_CUDA(cudaStreamSynchronize(s));
 }
 
@@ -247,14 +308,14 @@ __device__ __forceinline__ void sep(const SiteRec<float>& a, const SiteRec<float
   z = (a.z - b.z) + (a.lz - b.lz);
 }
 
-template <typename T, int M, bool DAMP>
+template <typename T, int M, bool DAMP, bool FAST = false>
 __device__ __forceinline__ void pair_field(const SiteRec<T>& ti, T ai, const SiteRec<T>& sj,
                                            const T* S, T& fx, T& fy, T& fz) {
   T x, y, z;
   sep(ti, sj, x, y, z);
   const T r2 = x * x + y * y + z * z;
   T G[3];
-  radial<T, M + 1>(r2, DAMP ? ai * sj.s : T(0), G);
+  radial<T, M + 1, FAST>(r2, DAMP ? ai * sj.s : T(0), G);
   if (M == 0) field_m0(x, y, z, G, S[0], fx, fy, fz);
   if (M == 1) field_m1(x, y, z, G, S[0], S[1], S[2], fx, fy, fz);
   if (M == 2) field_m2(x, y, z, G, S, fx, fy, fz);
@@ -288,90 +349,132 @@ struct Comp3<float> {
 };
 
 // ---------------------------------------------------------------------------
-// Near field: block per (target leaf, source split).  Each target site is
-// served by S = 128 / n_A thread groups that stride over the staged sources;
-// group partials are added in group order at the end.
+// Near field: block per work item (target leaf, piece of its source list).
+// Every thread serves two target sites of the leaf against a stride of the
+// staged sources (S = 128 / ceil(n_A / 2) groups), so each source read from
+// shared memory feeds two pair evaluations; group partials are added in group
+// order at the end and written to the item's output slot.
 // ---------------------------------------------------------------------------
-template <typename T, int M, bool DAMP>
+template <typename T, int M, bool DAMP, bool FAST>
 __global__ void __launch_bounds__(P2P_BLOCK)
-      k_p2p(int n, const int* __restrict__ leaf_start, const int* __restrict__ p2p_ptr,
-            const int* __restrict__ p2p_src, int nsplit, PosArgs<T> pa,
-            const T* __restrict__ src, T damping, T* __restrict__ Fnear) {
+      k_p2p(int n, const int* __restrict__ leaf_start, const int4* __restrict__ items,
+            const int* __restrict__ p2p_src, PosArgs<T> pa, const T* __restrict__ src,
+            T damping, T* __restrict__ Fnear) {
   constexpr int NS = ncomp(M);
   __shared__ SiteRec<T> s_rec[P2P_TILE];
   __shared__ T s_S[P2P_TILE * NS];
-  __shared__ int s_pstart[P2P_PIECES], s_poff[P2P_PIECES + 1];
-  __shared__ int s_np, s_cur, s_curoff;
-  __shared__ T s_red[P2P_BLOCK * 3];
+  __shared__ int s_pstart[33], s_poff[34];
+  __shared__ int s_np, s_cur, s_coff;
+  __shared__ T s_red[P2P_BLOCK * 6];
 
-  const int A = blockIdx.x, split = blockIdx.y;
+  const int4 it = items[blockIdx.x];
+  const int A = it.x, b0 = it.y, b1 = it.z, slot = it.w;
   const int a0 = leaf_start[A], nA = leaf_start[A + 1] - a0;
-  const int l0 = p2p_ptr[A], l1 = p2p_ptr[A + 1];
-  const int per = (l1 - l0 + nsplit - 1) / nsplit;
-  const int b0 = min(l1, l0 + split * per), b1 = min(l1, b0 + per);
+  const int lane = threadIdx.x & 31;
 
-  for (int tb = 0; tb < nA; tb += P2P_BLOCK) {
-    const int nT = min(P2P_BLOCK, nA - tb);
-    const int S  = P2P_BLOCK / nT;
-    const int t = threadIdx.x % nT, g = threadIdx.x / nT;
+  for (int tb = 0; tb < nA; tb += 2 * P2P_BLOCK) {
+    const int nT = min(2 * P2P_BLOCK, nA - tb);
+    const int T2 = (nT + 1) >> 1;
+    const int S  = P2P_BLOCK / T2;
+    const int t = threadIdx.x % T2, g = threadIdx.x / T2;
     const bool active = g < S;
-    const SiteRec<T> me = pa.load(a0 + tb + t);
-    const T ai          = damping * me.s;
-    Comp3<T> acc;
-    if (threadIdx.x == 0) s_cur = b0, s_curoff = 0;
+    const bool has1   = t + T2 < nT;
+    const SiteRec<T> me0 = pa.load(a0 + tb + t);
+    const SiteRec<T> me1 = pa.load(a0 + tb + (has1 ? t + T2 : t));
+    const T ai0 = damping * me0.s, ai1 = damping * me1.s;
+    Comp3<T> acc0, acc1;
+    if (threadIdx.x == 0) s_cur = b0, s_coff = 0;
     __syncthreads();
     while (true) {
-      if (threadIdx.x == 0) {
-        int k = 0, off = 0, cur = s_cur, coff = s_curoff;
-        while (k < P2P_PIECES && off < P2P_TILE && cur < b1) {
-          const int Lb = p2p_src[cur];
-          const int ls = leaf_start[Lb] + coff;
-          const int lc = leaf_start[Lb + 1] - ls;
-          const int take = min(lc, P2P_TILE - off);
-          s_pstart[k] = ls, s_poff[k] = off;
-          off += take, ++k;
-          if (take == lc)
-            ++cur, coff = 0;
-          else
-            coff += take;
+      if (threadIdx.x < 32) {
+        // Plan the next tile: the next (up to) 32 source pieces, their sizes
+        // prefix-summed across the warp; pieces that start inside the tile
+        // are taken, the last one possibly in part.
+        const int cur = s_cur, coff = s_coff;
+        const int e   = cur + lane;
+        int start = 0, cnt = 0;
+        if (e < b1) {
+          const int Lb = p2p_src[e];
+          start        = leaf_start[Lb];
+          cnt          = leaf_start[Lb + 1] - start;
+          if (lane == 0) start += coff, cnt -= coff;
         }
-        s_poff[k] = off, s_np = k, s_cur = cur, s_curoff = coff;
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int v = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += v;
+        }
+        const int excl     = incl - cnt;
+        const bool take    = e < b1 && excl < P2P_TILE;
+        const int takecnt  = take ? min(cnt, P2P_TILE - excl) : 0;
+        const unsigned msk = __ballot_sync(0xffffffffu, take);
+        const int np       = __popc(msk);
+        const int last     = max(np - 1, 0);
+        const int tot      = __shfl_sync(0xffffffffu, excl + takecnt, last);
+        const int lastcnt  = __shfl_sync(0xffffffffu, cnt, last);
+        const int lasttake = __shfl_sync(0xffffffffu, takecnt, last);
+        if (take) s_pstart[lane] = start, s_poff[lane] = excl;
+        if (lane == 0) {
+          s_np       = np;
+          s_poff[np] = np ? tot : 0;
+          if (np > 0) {
+            if (lasttake == lastcnt)
+              s_cur = cur + np, s_coff = 0;
+            else
+              s_cur = cur + last, s_coff = (last == 0 ? coff : 0) + lasttake;
+          }
+        }
       }
       __syncthreads();
-      const int np = s_np, total = s_poff[np];
-      if (total == 0) break;
+      const int np = s_np;
+      if (np == 0) break;
+      const int total = s_poff[np];
       for (int q = threadIdx.x; q < total; q += P2P_BLOCK) {
-        int k = 0;
-        while (q >= s_poff[k + 1]) ++k;
-        const int j = s_pstart[k] + (q - s_poff[k]);
+        int lo = 0, hi = np - 1;  // piece k with s_poff[k] <= q < s_poff[k + 1]
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (s_poff[mid] <= q)
+            lo = mid;
+          else
+            hi = mid - 1;
+        }
+        const int j = s_pstart[lo] + (q - s_poff[lo]);
         s_rec[q]    = pa.load(j);
 #pragma unroll
         for (int c = 0; c < NS; ++c) s_S[q * NS + c] = src[(size_t)j * NS + c];
       }
       __syncthreads();
       if (active) {
-        T fx = 0, fy = 0, fz = 0;
-        for (int jj = g; jj < total; jj += S)
-          pair_field<T, M, DAMP>(me, ai, s_rec[jj], &s_S[jj * NS], fx, fy, fz);
-        acc.add(fx, fy, fz);
+        T fx0 = 0, fy0 = 0, fz0 = 0, fx1 = 0, fy1 = 0, fz1 = 0;
+        for (int jj = g; jj < total; jj += S) {
+          const SiteRec<T> sj = s_rec[jj];
+          const T* Sj         = &s_S[jj * NS];
+          pair_field<T, M, DAMP, FAST>(me0, ai0, sj, Sj, fx0, fy0, fz0);
+          pair_field<T, M, DAMP, FAST>(me1, ai1, sj, Sj, fx1, fy1, fz1);
+        }
+        acc0.add(fx0, fy0, fz0);
+        acc1.add(fx1, fy1, fz1);
       }
       __syncthreads();
     }
     if (active) {
-      s_red[(g * nT + t) * 3 + 0] = acc.gx();
-      s_red[(g * nT + t) * 3 + 1] = acc.gy();
-      s_red[(g * nT + t) * 3 + 2] = acc.gz();
+      T* r = &s_red[(g * T2 + t) * 6];
+      r[0] = acc0.gx(), r[1] = acc0.gy(), r[2] = acc0.gz();
+      r[3] = acc1.gx(), r[4] = acc1.gy(), r[5] = acc1.gz();
     }
     __syncthreads();
-    if (threadIdx.x < nT) {
-      T fx = 0, fy = 0, fz = 0;
-      for (int gg = 0; gg < S; ++gg) {
-        fx += s_red[(gg * nT + threadIdx.x) * 3 + 0];
-        fy += s_red[(gg * nT + threadIdx.x) * 3 + 1];
-        fz += s_red[(gg * nT + threadIdx.x) * 3 + 2];
+    if (threadIdx.x < T2) {
+      T f[6] = {0, 0, 0, 0, 0, 0};
+      for (int gg = 0; gg < S; ++gg)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) f[c] += s_red[(gg * T2 + threadIdx.x) * 6 + c];
+      T* o = Fnear + (size_t)slot * 3 * n + 3 * (size_t)(a0 + tb + threadIdx.x);
+      o[0] = f[0], o[1] = f[1], o[2] = f[2];
+      if (threadIdx.x + T2 < nT) {
+        T* o1 = Fnear + (size_t)slot * 3 * n + 3 * (size_t)(a0 + tb + threadIdx.x + T2);
+        o1[0] = f[3], o1[1] = f[4], o1[2] = f[5];
       }
-      T* o = Fnear + (size_t)split * 3 * n + 3 * (size_t)(a0 + tb + threadIdx.x);
-      o[0] = fx, o[1] = fy, o[2] = fz;
     }
     __syncthreads();
   }
@@ -552,7 +655,8 @@ __global__ void __launch_bounds__(32 * M2L_WARPS)
 // adds alpha^-1 src (apply) or accumulates sign * F into an FP64 field.
 // ---------------------------------------------------------------------------
 template <typename T, int M, int MODE>
-__global__ void k_finish(int n, int nsplit, const T* __restrict__ Fnear, int use_fmm,
+__global__ void k_finish(int n, const int* __restrict__ leaf_nslot, const T* __restrict__ Fnear,
+                         int use_fmm,
                          TreeView tv, OpsView ov, const T* __restrict__ L, PosArgs<T> pa,
                          const double4_32a* __restrict__ pos64, const T* __restrict__ src,
                          int damp, T damping, const int* __restrict__ corr_ptr,
@@ -565,7 +669,8 @@ __global__ void k_finish(int n, int nsplit, const T* __restrict__ Fnear, int use
   double dv[1] = {0.0};
   if (i < n) {
     T f[3] = {0, 0, 0};
-    for (int s = 0; s < nsplit; ++s) {
+    const int nsl = leaf_nslot[tv.site_leaf[i]];
+    for (int s = 0; s < nsl; ++s) {
       const T* q = Fnear + (size_t)s * 3 * n + 3 * (size_t)i;
       f[0] += q[0], f[1] += q[1], f[2] += q[2];
     }
@@ -612,7 +717,11 @@ __global__ void k_finish(int n, int nsplit, const T* __restrict__ Fnear, int use
       out64[3 * (size_t)i + 2] += sign * (double)f[2];
     }
   }
-  if (dot.partials) grid_sum_last<1>(dv, sh, dot.partials, dot.ticket, dot.out);
+  if (dot.site_values) {
+    if (i < n) dot.site_values[i] = dv[0];
+  } else if (dot.partials) {
+    grid_sum_last<1>(dv, sh, dot.partials, dot.ticket, dot.out);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -630,17 +739,19 @@ PosArgs<float> pos_args<float>(const Geometry& g) {
 }
 
 template <typename T, int M>
-static void launch_p2p(const Geometry& g, bool damp, const T* src, T damping, T* Fnear,
-                       cudaStream_t s) {
-  dim3 grid(g.layout.nleaves, g.nsplit);
-  if (damp)
-    k_p2p<T, M, true><<<grid, P2P_BLOCK, 0, s>>>(g.n, g.leaf_start.p, g.p2p_ptr.p,
-                                                 g.p2p_src.p, g.nsplit, pos_args<T>(g), src,
-                                                 damping, Fnear);
+static void launch_p2p(const Geometry& g, bool damp, bool fast, const T* src, T damping,
+                       T* Fnear, cudaStream_t s) {
+  const int grid = (int)g.h_items.size();
+#define CG_P2P(D, F)                                                                            \
+  k_p2p<T, M, D, F><<<grid, P2P_BLOCK, 0, s>>>(g.n, g.leaf_start.p, g.items.p, g.p2p_src.p, \
+                                               pos_args<T>(g), src, damping, Fnear)
+  if (damp && fast)
+    CG_P2P(true, true);
+  else if (damp)
+    CG_P2P(true, false);
   else
-    k_p2p<T, M, false><<<grid, P2P_BLOCK, 0, s>>>(g.n, g.leaf_start.p, g.p2p_ptr.p,
-                                                  g.p2p_src.p, g.nsplit, pos_args<T>(g), src,
-                                                  damping, Fnear);
+    CG_P2P(false, false);
+#undef CG_P2P
   CG_LAUNCH();
 }
 
@@ -648,7 +759,7 @@ template <typename T>
 void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m, const T* src,
                 bool damp, double damping, FinishMode mode, const T* ainv6, T* out,
                 double* out64, double sign, const ReduceSlots* dot, cudaStream_t s,
-                const PhaseEvents* pe) {
+                const PhaseEvents* pe, bool fast_exp) {
   const TreeView tv = g.view();
   OpsView ov{};
   const int n = g.n;
@@ -675,7 +786,9 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
       CG_LAUNCH();
     }
     mark(1);
-    {
+    if (launch_m2l_fixed<T>(tv, ov.m, ov.p, w.M.p, w.L.p, s)) {
+      CG_LAUNCH();
+    } else {
       size_t smem = (size_t)(ov.nm2l_terms + 9 * ov.nt) * sizeof(int);
       smem        = (smem + 15) & ~(size_t)15;
       smem += (size_t)M2L_WARPS * (ov.nt + ov.msize + 32 * M2L_SLOTS) * sizeof(T);
@@ -701,11 +814,11 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
   } else {
     mark(1), mark(2), mark(3);
   }
-  w.Fnear.alloc((size_t)g.nsplit * 3 * n);
+  w.Fnear.alloc((size_t)g.nslot * 3 * n);
   const T dampT = (T)damping;
-  if (m == 0) launch_p2p<T, 0>(g, damp, src, dampT, w.Fnear.p, s);
-  if (m == 1) launch_p2p<T, 1>(g, damp, src, dampT, w.Fnear.p, s);
-  if (m == 2) launch_p2p<T, 2>(g, damp, src, dampT, w.Fnear.p, s);
+  if (m == 0) launch_p2p<T, 0>(g, damp, fast_exp, src, dampT, w.Fnear.p, s);
+  if (m == 1) launch_p2p<T, 1>(g, damp, fast_exp, src, dampT, w.Fnear.p, s);
+  if (m == 2) launch_p2p<T, 2>(g, damp, fast_exp, src, dampT, w.Fnear.p, s);
   mark(4);
 
   const int FB = 256;
@@ -714,7 +827,7 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
   if (dot) rs = *dot;
   const T* Lp = g.fmm ? w.L.p : nullptr;
 #define CG_FINISH(TT, MM, MODE)                                                               \
-  k_finish<TT, MM, MODE><<<nb, FB, 0, s>>>(n, g.nsplit, w.Fnear.p, g.fmm ? 1 : 0, tv, ov, Lp, \
+  k_finish<TT, MM, MODE><<<nb, FB, 0, s>>>(n, g.leaf_nslot.p, w.Fnear.p, g.fmm ? 1 : 0, tv, ov, Lp, \
                                            pos_args<TT>(g), g.pos64.p, src, damp ? 1 : 0,    \
                                            dampT, g.corr_ptr.p, g.corr_idx.p, ainv6, out,    \
                                            out64, sign, rs)
@@ -734,11 +847,11 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
 template void eval_field<double>(const Geometry&, const DeviceOps*, FieldWork<double>&, int,
                                  const double*, bool, double, FinishMode, const double*,
                                  double*, double*, double, const ReduceSlots*, cudaStream_t,
-                                 const PhaseEvents*);
+                                 const PhaseEvents*, bool);
 template void eval_field<float>(const Geometry&, const DeviceOps*, FieldWork<float>&, int,
                                 const float*, bool, double, FinishMode, const float*, float*,
                                 double*, double, const ReduceSlots*, cudaStream_t,
-                                const PhaseEvents*);
+                                const PhaseEvents*, bool);
 
 // ---------------------------------------------------------------------------
 // Permutations

@@ -66,7 +66,6 @@ struct Geometry {
   bool fmm    = false;
   int ncrit   = 64;
   double theta = 0.5;
-  int nsplit  = 1;  // source splits of the near-field pass
   TreeLayout layout;
   std::vector<int> level_start;
   DBuf<double> center;
@@ -80,10 +79,36 @@ struct Geometry {
   long near_pairs = 0;  // ordered pairs evaluated by the near-field pass
   long alg_pairs  = 0;  // of these, the pairs the reference evaluates
 
+  // Near-field work items (target leaf, first and last+1 position in its
+  // P2P list, output slot), largest first; a leaf's items write slots
+  // 0..leaf_nslot-1 of the near-field buffer.
+  int nslot = 1;
+  std::vector<int4> h_items;
+  std::vector<int> h_leaf_nslot;
+  DBuf<int4> items;
+  DBuf<int> leaf_nslot;
+  void make_items();
+
+  // host copies of the device arrays that are not part of `layout`
+  std::vector<int> h_site_leaf, h_cptr, h_cidx;
+  std::vector<double4_32a> h_pos64;
+  std::vector<float4> h_hi, h_lo;
+
   // xyz in caller order; s_damp: alpha_iso^(-1/6) per site (0 = undamped partner);
   // exclusions in caller indices (CSR, may be null).
   void build(int n, const double* xyz, const double* s_damp, const int* excl_ptr,
              const int* excl_idx, bool fmm, int ncrit, double theta, cudaStream_t s);
+  // host half of build(): layout, permuted coordinates, exclusion corrections
+  void prepare(int n, const double* xyz, const double* s_damp, const int* excl_ptr,
+               const int* excl_idx, bool fmm, int ncrit, double theta);
+  void upload(cudaStream_t s);
+  // Concatenates prepared geometries, each repeated `copies` times, into one
+  // geometry whose passes cover all of them: cells are renumbered by (level,
+  // part, cell), particles and leaves stay part-contiguous.  Direct-summation
+  // parts contribute their chunks as level-0 cells without interaction lists.
+  // The caller index of site i of copy r of part g is
+  //   copies * site_offset[g] + r * n_g + i.
+  static void combine(const std::vector<const Geometry*>& parts, int copies, Geometry& out);
   TreeView view() const;
   SiteView64 v64() const { return {pos64.p}; }
   SiteView32 v32() const { return {hi32.p, lo32.p}; }
@@ -103,6 +128,9 @@ struct ReduceSlots {
   double* partials;   // >= nblocks * 4 doubles
   unsigned* ticket;   // one counter, zero between uses
   double* out;        // receives the totals
+  // when set, the per-site values are stored here instead of being summed
+  // (segmented reductions of batched solves add them per segment)
+  double* site_values = nullptr;
 };
 
 // Evaluates the field of sources `src` (ns = ncomp(m) values per permuted
@@ -119,7 +147,7 @@ template <typename T>
 void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m, const T* src,
                 bool damp, double damping, FinishMode mode, const T* ainv6, T* out,
                 double* out64, double sign, const ReduceSlots* dot, cudaStream_t s,
-                const PhaseEvents* pe = nullptr);
+                const PhaseEvents* pe = nullptr, bool fast_exp = false);
 
 // Permutation helpers (caller order <-> device order), all 3-vectors.
 void permute_in(const Geometry& g, const double* in_caller, double* out_perm, int ncomp,

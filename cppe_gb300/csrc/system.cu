@@ -60,7 +60,7 @@ template <typename T>
 __global__ void k_cg_update(int n, const T* __restrict__ p, const T* __restrict__ Ap,
                             const T* __restrict__ a6, T* __restrict__ x, T* __restrict__ r,
                             T* __restrict__ z, ReduceSlots rs, double* scal, int* flags,
-                            double* hist, double thresh, int maxiter) {
+                            double* hist, double thresh, int maxiter, T* __restrict__ r_old) {
   __shared__ double sh[64];
   if (flags[0]) return;
   const double a = scal[S_RZ] / scal[S_PAP];
@@ -73,6 +73,7 @@ __global__ void k_cg_update(int n, const T* __restrict__ p, const T* __restrict_
     for (int c = 0; c < 3; ++c) {
       const size_t k = 3 * (size_t)i + c;
       x[k] += aT * p[k];
+      if (r_old) r_old[k] = r[k];
       rv[c] = r[k] - aT * Ap[k];
       r[k]  = rv[c];
     }
@@ -90,6 +91,7 @@ __global__ void k_cg_update(int n, const T* __restrict__ p, const T* __restrict_
     if (hist) hist[it] = rn;
     flags[1]      = it + 1;
     scal[S_RNORM] = rn;
+    scal[S_RZOLD] = scal[S_RZ];
     scal[S_BETA]  = rs.out[1] / scal[S_RZ];
     scal[S_RZ]    = rs.out[1];
     if (rn < thresh)
@@ -116,6 +118,20 @@ __global__ void k_residual(int n3, const double* __restrict__ F, const double* _
   double v[1] = {0.0};
   if (k < n3) {
     const double d = F[k] - (Ax ? Ax[k] : 0.0);
+    r[k]           = d;
+    v[0]           = d * d;
+  }
+  if (grid_sum_last<1>(v, sh, rs.partials, rs.ticket, rs.out)) scal[S_RNORM] = sqrt(rs.out[0]);
+}
+
+// r -= Bd (FP64 -= FP32); ||r||.
+__global__ void k_residual_update(int n3, const float* __restrict__ Bd, double* __restrict__ r,
+                                  ReduceSlots rs, double* scal) {
+  __shared__ double sh[32];
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  double v[1] = {0.0};
+  if (k < n3) {
+    const double d = r[k] - (double)Bd[k];
     r[k]           = d;
     v[0]           = d * d;
   }
@@ -288,11 +304,11 @@ void System::phase_timings(int precision, int reps, double* ms) {
 
 ReduceSlots System::slots(int k) const { return ReduceSlots{partials.p, ticket.p, scal.p + k}; }
 
-void System::apply64(const double* in, double* out, bool with_dot) {
+void System::apply64(const double* in, double* out, bool with_dot, bool fast_exp) {
   ReduceSlots rs = slots(S_PAP);
   eval_field<double>(geo, ops.get(), w64, 1, in, opt.damp != 0, opt.damping_factor,
                      FINISH_APPLY, ainv64.p, out, nullptr, 1.0, with_dot ? &rs : nullptr,
-                     stream);
+                     stream, nullptr, fast_exp);
 }
 
 void System::apply32(const float* in, float* out, bool with_dot) {
@@ -347,6 +363,7 @@ int System::solve_fp64(bool zero_guess, double* hist_out, int hist_cap, int* ite
   k_cg_start<double><<<nb, VB, 0, stream>>>(n, F.p, zero_guess ? nullptr : Ap.p, alpha64.p,
                                             r.p, z.p, p.p, slots(S_RED), scal.p, flags.p);
   CG_LAUNCH();
+  if (use_model) learned_precond<double>(z.p, r.p, p.p, true);
   if (zero_guess) CG_CUDA(cudaMemsetAsync(x.p, 0, sizeof(double) * n3, stream));
   Poller poll(stream, flags.p, h_flags);
   for (int k = 0; k < opt.maxiter; ++k) {
@@ -354,8 +371,9 @@ int System::solve_fp64(bool zero_guess, double* hist_out, int hist_cap, int* ite
     last.fp64_applies++;
     k_cg_update<double><<<nb, VB, 0, stream>>>(n, p.p, Ap.p, alpha64.p, x.p, r.p, z.p,
                                                slots(S_RED), scal.p, flags.p, hist.p, t,
-                                               opt.maxiter);
+                                               opt.maxiter, use_model ? lf_rold64.p : nullptr);
     CG_LAUNCH();
+    if (use_model) learned_precond<double>(z.p, r.p, p.p, false);
     k_cg_dir<double><<<(n3 + VB - 1) / VB, VB, 0, stream>>>(n3, z.p, p.p, scal.p, flags.p);
     CG_LAUNCH();
     if (poll.after_iteration()) break;
@@ -401,9 +419,11 @@ int System::solve_mixed(bool zero_guess, double* hist_out, int hist_cap, int* it
     k_cg_start<float><<<nb, VB, 0, stream>>>(n, F.p, Ap32.p, alpha32.p, r32.p, z32.p, p32.p,
                                              slots(S_RED), scal.p, flags.p);
     CG_LAUNCH();
+    if (use_model) learned_precond<float>(z32.p, r32.p, p32.p, true);
   }
-  bool have_inner_start = !zero_guess;
-  int status            = CPPE_GPU_NOT_CONVERGED;
+  bool have_inner_start   = !zero_guess;
+  bool have_fp64_residual = zero_guess;  // r = F is exact for a zero start
+  int status              = CPPE_GPU_NOT_CONVERGED;
   for (int outer = 0; outer < max_outer; ++outer) {
     double rnorm;
     if (!have_inner_start) {
@@ -421,6 +441,7 @@ int System::solve_mixed(bool zero_guess, double* hist_out, int hist_cap, int* it
       k_cg_start<float><<<nb, VB, 0, stream>>>(n, r.p, nullptr, alpha32.p, r32.p, z32.p,
                                                p32.p, slots(S_RED), scal.p, flags.p);
       CG_LAUNCH();
+      if (use_model) learned_precond<float>(z32.p, r32.p, p32.p, true);
     } else {
       CG_CUDA(cudaMemcpyAsync(h_scal, scal.p, S_NSCAL * sizeof(double), cudaMemcpyDeviceToHost,
                               stream));
@@ -435,8 +456,10 @@ int System::solve_mixed(bool zero_guess, double* hist_out, int hist_cap, int* it
       last.fp32_applies++;
       k_cg_update<float><<<nb, VB, 0, stream>>>(n, p32.p, Ap32.p, alpha32.p, d32.p, r32.p,
                                                 z32.p, slots(S_RED), scal.p, flags.p, nullptr,
-                                                tol, std::max(1, opt.maxiter));
+                                                tol, std::max(1, opt.maxiter),
+                                                use_model ? lf_rold32.p : nullptr);
       CG_LAUNCH();
+      if (use_model) learned_precond<float>(z32.p, r32.p, p32.p, false);
       k_cg_dir<float><<<nb3, VB, 0, stream>>>(n3, z32.p, p32.p, scal.p, flags.p);
       CG_LAUNCH();
       if (poll.after_iteration()) break;
@@ -445,13 +468,29 @@ int System::solve_mixed(bool zero_guess, double* hist_out, int hist_cap, int* it
     CG_CUDA(cudaStreamSynchronize(stream));
     total_inner += h_flags[1];
     last.fp32_applies = std::min(last.fp32_applies, total_inner + (zero_guess ? 0 : 1));
-    // x += d; r = F - B64 x
-    k_accumulate<<<nb3, VB, 0, stream>>>(n3, x.p, d32.p);
-    CG_LAUNCH();
-    apply64(x.p, Ap.p, false);
-    last.fp64_applies++;
-    k_residual<<<nb3, VB, 0, stream>>>(n3, F.p, Ap.p, r.p, slots(S_RED), scal.p);
-    CG_LAUNCH();
+    // An FP32 update of the residual errs by ~1e-7 ||B d|| ~ 1e-7 ||r||; it is
+    // used only on top of an exact residual small enough that this error is
+    // below 1e-3 of the threshold.
+    if (!(have_fp64_residual && rnorm * 1e-4 < t)) {
+      // x += d; r = F - B64 x: the residual recomputed with the FP64 operator
+      k_accumulate<<<nb3, VB, 0, stream>>>(n3, x.p, d32.p);
+      CG_LAUNCH();
+      apply64(x.p, Ap.p, false, true);
+      last.fp64_applies++;
+      k_residual<<<nb3, VB, 0, stream>>>(n3, F.p, Ap.p, r.p, slots(S_RED), scal.p);
+      CG_LAUNCH();
+      have_fp64_residual = true;
+    } else {
+      // Later corrections are small: r -= B d with B d in FP32 (its error is
+      // ~1e-7 of ||B d|| ~ ||r||, far below the threshold), accumulated into
+      // the FP64 residual; then x += d.
+      apply32(d32.p, Ap32.p, false);
+      last.fp32_applies++;
+      k_residual_update<<<nb3, VB, 0, stream>>>(n3, Ap32.p, r.p, slots(S_RED), scal.p);
+      CG_LAUNCH();
+      k_accumulate<<<nb3, VB, 0, stream>>>(n3, x.p, d32.p);
+      CG_LAUNCH();
+    }
   }
   if (status != CPPE_GPU_OK) {
     CG_CUDA(cudaMemcpyAsync(h_scal, scal.p, S_NSCAL * sizeof(double), cudaMemcpyDeviceToHost,
@@ -476,7 +515,10 @@ int System::solve_device(const double* d_rhs, const double* d_guess, int make_gu
   const int n3 = 3 * n;
   permute_in(geo, d_rhs, F.p, 3, stream);
   bool zero = false;
-  if (make_guess) {
+  use_model = make_guess && model != nullptr;
+  if (use_model) {
+    learned_start();
+  } else if (make_guess) {
     k_sym_apply<<<(n + VB - 1) / VB, VB, 0, stream>>>(n, alpha64.p, F.p, x.p);
     CG_LAUNCH();
   } else if (d_guess) {
@@ -487,9 +529,117 @@ int System::solve_device(const double* d_rhs, const double* d_guess, int make_gu
   (void)n3;
   int st = opt.precision == CPPE_GPU_MIXED ? solve_mixed(zero, hist_out, hist_cap, iters)
                                            : solve_fp64(zero, hist_out, hist_cap, iters);
+  if (use_model && st != CPPE_GPU_OK) {
+    // plain PCG is the fallback of the learned start and preconditioner
+    use_model = false;
+    k_sym_apply<<<(n + VB - 1) / VB, VB, 0, stream>>>(n, alpha64.p, F.p, x.p);
+    CG_LAUNCH();
+    st = opt.precision == CPPE_GPU_MIXED ? solve_mixed(false, hist_out, hist_cap, iters)
+                                         : solve_fp64(false, hist_out, hist_cap, iters);
+  }
+  use_model = false;
   permute_out(geo, x.p, d_mu, 3, stream);
   CG_CUDA(cudaStreamSynchronize(stream));
   return st;
+}
+
+// ---------------------------------------------------------------------------
+// Learned initial guess and preconditioner correction
+// ---------------------------------------------------------------------------
+__global__ void k_rows(int n, const float* __restrict__ v1, const float* __restrict__ v2,
+                       const float* __restrict__ v3, const double* __restrict__ mu,
+                       const float* __restrict__ a, const float* __restrict__ w,
+                       const double* __restrict__ x0, float* __restrict__ rows) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float* o = rows + (size_t)i * Mlp::TROW;
+  float s = 0.f, t = 0.f;
+  for (int c = 0; c < 3; ++c) {
+    const size_t k = 3 * (size_t)i + c;
+    o[c] = v1[k], o[3 + c] = v2[k], o[6 + c] = v3[k], o[9 + c] = (float)mu[k];
+    o[12 + c] = a[k], o[15 + c] = w[k], o[18 + c] = (float)(mu[k] - x0[k]);
+    s += v1[k] * v1[k];
+    t += a[k] * a[k];
+  }
+  o[21] = s, o[22] = t, o[23] = 0.f;
+}
+
+void System::learned_setup() {
+  if (near) return;
+  near = std::make_unique<NearGrid>();
+  near->build(geo, excl_ptr_h.empty() ? nullptr : excl_ptr_h.data(),
+              excl_idx_h.empty() ? nullptr : excl_idx_h.data(), stream);
+  const size_t n3 = 3 * (size_t)n;
+  lf_feats.alloc((size_t)n * Mlp::IN);
+  for (auto* b : {&lf_v1, &lf_v2, &lf_v3, &lf_w32, &lf_rold32}) b->alloc(n3);
+  lf_Y.alloc((size_t)n * Mlp::OUT);
+  lf_c.alloc(n);
+  lf_w64.alloc(n3);
+  lf_rold64.alloc(n3);
+}
+
+void System::learned_features_for_F() {
+  learned_setup();
+  const NearGridView ng = view(*near);
+  learned_features(ng, geo.pos64.p, alpha32.p, F.p, lf_feats.p, lf_v1.p, stream);
+  near_T<float>(ng, geo.pos64.p, alpha32.p, opt.damp, opt.damping_factor, lf_v1.p, lf_v2.p, stream);
+  near_T<float>(ng, geo.pos64.p, alpha32.p, opt.damp, opt.damping_factor, lf_v2.p, lf_v3.p, stream);
+  learned_basis_features(n, lf_v1.p, lf_v2.p, lf_v3.p, lf_feats.p, stream);
+}
+
+void System::learned_start() {
+  learned_features_for_F();
+  CG_CUDA(cudaStreamSynchronize(stream));
+  model->forward(n, lf_feats.p, lf_Y.p, model->stream);
+  CG_CUDA(cudaStreamSynchronize(model->stream));
+  learned_guess(n, lf_Y.p, lf_v1.p, lf_v2.p, lf_v3.p, x.p, lf_c.p, stream);
+}
+
+template <typename T>
+void System::learned_precond(T* zv, const T* rv, T* pv, bool start) {
+  const NearGridView ng = view(*near);
+  if constexpr (std::is_same<T, double>::value) {
+    near_T<double>(ng, geo.pos64.p, alpha64.p, opt.damp, opt.damping_factor, zv, lf_w64.p, stream);
+    precond_fix<double>(n, zv, lf_w64.p, lf_c.p, rv, lf_rold64.p, pv, start, partials.p, ticket.p,
+                        scal.p, flags.p, stream);
+  } else {
+    near_T<float>(ng, geo.pos64.p, alpha32.p, opt.damp, opt.damping_factor, zv, lf_w32.p, stream);
+    precond_fix<float>(n, zv, lf_w32.p, lf_c.p, rv, lf_rold32.p, pv, start, partials.p, ticket.p,
+                       scal.p, flags.p, stream);
+  }
+}
+template void System::learned_precond<double>(double*, const double*, double*, bool);
+template void System::learned_precond<float>(float*, const float*, float*, bool);
+
+void System::learned_rows(const double* mu_dev, std::vector<float>& feats, std::vector<float>& rows) {
+  // F holds the rhs (device order); x0 = alpha F; r0 = F - B x0 (FP64)
+  learned_features_for_F();
+  const int nb = (n + VB - 1) / VB;
+  k_sym_apply<<<nb, VB, 0, stream>>>(n, alpha64.p, F.p, x.p);
+  CG_LAUNCH();
+  apply64(x.p, Ap.p, false);
+  k_residual<<<(3 * n + VB - 1) / VB, VB, 0, stream>>>(3 * n, F.p, Ap.p, r.p, slots(S_RED),
+                                                        scal.p);
+  CG_LAUNCH();
+  // a = alpha r0 (FP64 -> FP32), w = alpha T_near a
+  k_sym_apply<<<nb, VB, 0, stream>>>(n, alpha64.p, r.p, tmp_out.p);
+  CG_LAUNCH();
+  k_to_f32<<<(3 * n + VB - 1) / VB, VB, 0, stream>>>(3 * n, tmp_out.p, lf_w32.p);
+  CG_LAUNCH();
+  near_T<float>(view(*near), geo.pos64.p, alpha32.p, opt.damp, opt.damping_factor, lf_w32.p,
+                lf_rold32.p, stream);
+  DBuf<float> rows_d;
+  rows_d.alloc((size_t)n * Mlp::TROW);
+  k_rows<<<nb, VB, 0, stream>>>(n, lf_v1.p, lf_v2.p, lf_v3.p, mu_dev, lf_w32.p, lf_rold32.p, x.p,
+                                rows_d.p);
+  CG_LAUNCH();
+  feats.resize((size_t)n * Mlp::IN);
+  rows.resize((size_t)n * Mlp::TROW);
+  CG_CUDA(cudaMemcpyAsync(feats.data(), lf_feats.p, feats.size() * sizeof(float),
+                          cudaMemcpyDeviceToHost, stream));
+  CG_CUDA(cudaMemcpyAsync(rows.data(), rows_d.p, rows.size() * sizeof(float),
+                          cudaMemcpyDeviceToHost, stream));
+  CG_CUDA(cudaStreamSynchronize(stream));
 }
 
 }  // namespace cg

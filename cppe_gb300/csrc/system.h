@@ -5,6 +5,7 @@
 #include <memory>
 
 #include "engine.h"
+#include "learned.h"
 
 namespace cg {
 
@@ -17,6 +18,7 @@ enum Scalar {
   S_BETA,     // beta
   S_RNORM,    // ||r||_2 after the last update
   S_TOL,      // stopping threshold of the running loop
+  S_RZOLD,    // r . z before the last update (flexible CG)
   S_RED = 8,  // 4 slots receiving grid reductions
   S_NSCAL = 16
 };
@@ -49,11 +51,31 @@ struct System {
   SolveStats last;
   std::vector<int> excl_ptr_h, excl_idx_h;  // caller-order exclusions (dense matrix)
 
+  // learned initial guess + preconditioner correction (optional, not owned)
+  Mlp* model = nullptr;
+  bool use_model = false;  // set while a learned solve runs
+  std::unique_ptr<NearGrid> near;
+  DBuf<float> lf_feats, lf_v1, lf_v2, lf_v3, lf_Y, lf_c, lf_w32, lf_rold32;
+  DBuf<double> lf_w64, lf_rold64;
+  void learned_setup();
+  // descriptors and basis vectors for the current F (device order)
+  void learned_features_for_F();
+  // x = learned guess, lf_c = preconditioner weights
+  void learned_start();
+  // z correction after a CG start/update (flexible CG)
+  template <typename T>
+  void learned_precond(T* z, const T* r, T* p, bool start);
+  // training rows for rhs F (device order) and converged mu (device order)
+  void learned_rows(const double* mu_star_dev, std::vector<float>& feats,
+                    std::vector<float>& rows);
+
   ~System();
   void init(int n, const double* xyz, const double* alpha6, const int* excl_ptr,
             const int* excl_idx, const cppe_gpu_options& o);
   // FP64 / FP32 operator on device-order vectors.
-  void apply64(const double* in, double* out, bool with_dot);
+  // fast_exp: FP32 exponential for damping arguments >= 20 (residuals of the
+  // mixed solver; the plain FP64 solver keeps the FP64 exponential)
+  void apply64(const double* in, double* out, bool with_dot, bool fast_exp = false);
   void apply32(const float* in, float* out, bool with_dot);
   // FP32 operator on FP64 device-order vectors (rounded in, widened out).
   void apply32_widen(const double* in, double* out);

@@ -179,6 +179,47 @@ int cppe_gpu_bmatrix_apply_direct_noalloc(int n, const double* d_xyz, const doub
                                           double* d_out, void* stream);
 
 /* ---------------------------------------------------------------------------
+ * Learned initial guess and preconditioner correction (no counterpart in the
+ * reference).  An MLP (64 -> 128 -> 128 -> 4, GELU, FP32) maps 64
+ * rotation-invariant descriptors of each site's environment within 6 A to
+ * coefficients y: the first-call guess mu0 = y0 v1 + y1 v2 + y2 v3 with the
+ * equivariant vectors v1 = alpha F, v2 = alpha T_near v1, v3 = alpha T_near v2,
+ * and a preconditioner z = alpha r + y3 alpha T_near alpha r used by a
+ * flexible PCG.  Plain PCG is the fallback: a learned solve that does not
+ * converge is repeated from alpha F with the Jacobi preconditioner, and the
+ * stopping rule is unchanged.  Training runs on the GPU (hand-written GEMM,
+ * GELU, loss and Adam kernels) from rows produced by cppe_gpu_learned_data.
+ * ------------------------------------------------------------------------- */
+typedef struct cppe_gpu_mlp cppe_gpu_mlp;
+int cppe_gpu_mlp_nparams(int* n);
+int cppe_gpu_mlp_create(int device, unsigned seed, cppe_gpu_mlp** out);
+int cppe_gpu_mlp_destroy(cppe_gpu_mlp* m);
+int cppe_gpu_mlp_get_params(cppe_gpu_mlp* m, float* out);
+int cppe_gpu_mlp_set_params(cppe_gpu_mlp* m, const float* in);
+/* Descriptor normalisation (64 means and inverse standard deviations); any
+ * pointer may be NULL; the *_out pointers read the current values back. */
+int cppe_gpu_mlp_normalization(cppe_gpu_mlp* m, const float* mean, const float* inv_std,
+                               float* mean_out, float* inv_std_out);
+/* y (rows x 4) for raw descriptors (rows x 64), host buffers. */
+int cppe_gpu_mlp_forward(cppe_gpu_mlp* m, int rows, const float* feats, float* y);
+/* Loss and gradient (cppe_gpu_mlp_nparams floats) of one batch; targets are
+ * rows of 24 floats: v1 v2 v3 mu* a w e (3 each), the two loss weights, pad. */
+int cppe_gpu_mlp_loss_grad(cppe_gpu_mlp* m, int rows, const float* feats,
+                           const float* targets, float lam, double* loss, float* grads);
+/* `steps` Adam steps on random batches of `batch` rows; loss_hist (steps) may be NULL. */
+int cppe_gpu_mlp_train(cppe_gpu_mlp* m, int rows, const float* feats, const float* targets,
+                       int steps, int batch, float lr, float lam, unsigned seed,
+                       double* loss_hist);
+/* Training rows of one solve: descriptors (n x 64) and targets (n x 24) for
+ * the right-hand side rhs and its converged solution mu_star (caller order
+ * in, device-order rows out). */
+int cppe_gpu_learned_data(cppe_gpu_system* sys, const double* rhs, const double* mu_star,
+                          float* feats, float* rows);
+/* Attach a model to a system (NULL detaches); first-call solves
+ * (make_guess != 0) then use the learned guess and preconditioner. */
+int cppe_gpu_set_model(cppe_gpu_system* sys, cppe_gpu_mlp* m);
+
+/* ---------------------------------------------------------------------------
  * Instrumentation (no counterpart in the reference).
  * ------------------------------------------------------------------------- */
 /* The cudaStream_t the system's work is ordered on (for caller-side events). */
@@ -213,6 +254,12 @@ int cppe_gpu_batch_destroy(cppe_gpu_batch* b);
 int cppe_gpu_batch_solve(cppe_gpu_batch* b, const double* rhs, double* mu, int* iters);
 int cppe_gpu_batch_solve_device(cppe_gpu_batch* b, const double* d_rhs, double* d_mu,
                                 int* iters);
+/* Operator applications of the last batched solve (each covers every
+ * segment) and the largest final residual norm over the segments. */
+int cppe_gpu_batch_stats(cppe_gpu_batch* b, int* fp64_applies, int* fp32_applies,
+                         double* max_rnorm);
+/* The cudaStream_t the batch's work is ordered on. */
+int cppe_gpu_batch_stream(cppe_gpu_batch* b, void** stream);
 
 #ifdef __cplusplus
 }
