@@ -41,6 +41,7 @@ CONFIGS = {
 }
 METRIC = "induced-dipole solve time to 1e-8 residual"
 FLOP_PER_PAIR = 45  # damped dipole pair, see include/cppe_gpu/work_model.h
+DD_RESIDUAL = 2     # kernel_timings mode: FP64 operator with the double-float near field
 
 
 def dist_env():
@@ -178,6 +179,105 @@ def cpu_baseline_sample(b, rhs, summation, order):
                       "host threads"}, mu
 
 
+def _event_time(stream, fn):
+    """Seconds of fn() on `stream`, CUDA events on that stream."""
+    import torch
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    out = fn()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) * 1e-3, out
+
+
+def batched_section(dev, steps, flush):
+    """256 snapshots of 500-20,000 sites (log-uniform; direct summation below
+    4,000 sites, FMM p5 above), 8 point-charge right-hand sides each, solved
+    as one batch in mixed precision; against the plain FP64 GPU PCG solving the
+    same segments one at a time."""
+    import torch
+    from cppe_gb300 import capi, learned, synthetic
+    sizes = synthetic.snapshot_sizes(256, seed=1000)
+    boxes = [synthetic.water_box(int(ns) // 3, seed=1000 + i) for i, ns in enumerate(sizes)]
+    nrhs = 8
+    rhs = [learned.generator_rhs(b, nrhs, 5000 + i) for i, b in enumerate(boxes)]
+    flat = np.concatenate([np.concatenate(r) for r in rhs])
+    t0 = time.perf_counter()
+    batch = capi.Batch(boxes, nrhs, direct_below=4000, precision=capi.MIXED, damp=True,
+                       order=5, ncrit=64, theta=0.5, thresh=1e-8, device=dev)
+    setup = time.perf_counter() - t0
+    d_rhs = torch.tensor(flat, dtype=torch.float64, device=f"cuda:{dev}")
+    d_mu = torch.zeros_like(d_rhs)
+    st = torch.cuda.ExternalStream(batch.stream())
+    batch.solve_device(d_rhs.data_ptr(), d_mu.data_ptr())  # warm-up
+    times = []
+    for _ in range(steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t, its = _event_time(st, lambda: batch.solve_device(d_rhs.data_ptr(), d_mu.data_ptr()))
+        times.append(t)
+    bst = batch.stats()
+    t_batch = float(np.mean(times))
+    mu = d_mu.cpu().numpy()
+    # plain FP64, one segment at a time: the first right-hand side of every
+    # snapshot is solved and timed; the 8 right-hand sides of a snapshot cost
+    # the same, so the total is 8x the measured sum
+    plain, worst, off = 0.0, 0.0, 0
+    for i, b in enumerate(boxes):
+        summ = capi.FMM if b.n >= 4000 else capi.DIRECT
+        s64 = capi.System(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, summation=summ, order=5,
+                          ncrit=64, theta=0.5, damp=True, thresh=1e-8, precision=capi.FP64,
+                          device=dev)
+        r0 = torch.tensor(rhs[i][0], dtype=torch.float64, device=f"cuda:{dev}")
+        m0 = torch.zeros_like(r0)
+        s64.solve_device(r0.data_ptr(), m0.data_ptr())  # warm-up
+        torch.cuda.synchronize()
+        t, _ = _event_time(torch.cuda.ExternalStream(s64.stream()),
+                           lambda: s64.solve_device(r0.data_ptr(), m0.data_ptr()))
+        plain += t
+        # FP64 residual of the batched mixed solution (first rhs of each snapshot)
+        seg = mu[off:off + 3 * b.n]
+        worst = max(worst, float(np.linalg.norm(rhs[i][0] - s64.apply(seg))))
+        off += nrhs * 3 * b.n
+        s64.close()
+    plain *= nrhs
+    return {"workload": "256 snapshots x 8 RHS, sites log-uniform 500-20,000 "
+                        f"({int(sum(sizes))} sites, {int(sum(sizes)) * nrhs} site-RHS), direct "
+                        "< 4,000 sites, FMM p5 above, mixed precision, tol 1e-8",
+            "value": t_batch, "unit": "s", "solves": len(boxes) * nrhs,
+            "plain_fp64_sequential_s": plain,
+            "plain_fp64_note": "first RHS of each snapshot solved and timed one at a time, x8",
+            "speedup_vs_plain_fp64": plain / t_batch,
+            "fp32_applies": bst["fp32_applies"], "fp64_applies": bst["fp64_applies"],
+            "max_fp64_residual": worst, "setup_s": setup}
+
+
+def learned_section(smx, s64, d_rhs, d_mu, ext, ext64, flush, steps, model_path):
+    """The 30,000-site system with the trained model attached to the mixed solver."""
+    import torch
+    from cppe_gb300 import learned
+    if not os.path.exists(model_path):
+        return None
+    model = learned.load(model_path, device=smx.device)
+    times = []
+    smx.set_model(model)
+    try:
+        smx.solve_device(d_rhs.data_ptr(), d_mu.data_ptr(), make_guess=True)  # warm-up
+        for _ in range(steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            t, _ = _event_time(ext, lambda: smx.solve_device(d_rhs.data_ptr(), d_mu.data_ptr(),
+                                                             make_guess=True))
+            times.append(t)
+        st = smx.stats()
+        mu = d_mu.cpu().numpy()
+    finally:
+        smx.set_model(None)
+    return {"value": float(np.mean(times)), "unit": "s", "stats": st,
+            "model": os.path.relpath(model_path, ROOT)}, mu
+
+
 def run_ours(args):
     import torch
     from cppe_gb300 import capi
@@ -198,10 +298,11 @@ def run_ours(args):
     if args.apply_only:
         # operator applies only (FP32 then FP64), e.g. for kernel profiling
         t32 = smx.kernel_timings(capi.MIXED, reps=args.apply_only)
+        tdd = smx.kernel_timings(DD_RESIDUAL, reps=args.apply_only)
         t64 = s64.kernel_timings(capi.FP64, reps=args.apply_only)
         print(json.dumps({"apply_only": args.apply_only, "config": args.config,
-                          "fp32_ms": t32[0], "fp64_ms": t64[0], "alg_pairs": t32[1],
-                          "m2l_pairs": t32[2]}), flush=True)
+                          "fp32_ms": t32[0], "dd_ms": tdd[0], "fp64_ms": t64[0],
+                          "alg_pairs": t32[1], "m2l_pairs": t32[2]}), flush=True)
         return
     d_rhs = torch.tensor(rhs, dtype=torch.float64, device=f"cuda:{dev}")
     d_mu = torch.zeros_like(d_rhs)
@@ -242,6 +343,20 @@ def run_ours(args):
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         t_mixed = float(tt.item())
 
+    # the same solver with the trained model (learned guess + preconditioner)
+    lrn = learned_section(smx, s64, d_rhs, d_mu, ext, ext64, flush, args.steps,
+                          args.model) if not args.no_learned else None
+    mu_lrn = None
+    if lrn is not None:
+        lrn, mu_lrn = lrn
+    t_mixed_plain = t_mixed
+    if lrn is not None:
+        t_mixed = lrn["value"]
+        if world > 1:
+            tt = torch.tensor([t_mixed], device=f"cuda:{dev}")
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            t_mixed = float(tt.item())
+
     # plain FP64 GPU PCG on the same system
     t64 = []
     for _ in range(max(1, min(args.steps, 3))):
@@ -265,15 +380,21 @@ def run_ours(args):
     # roofline of the dominant kernel (FP32 near-field pair pass)
     tim32, alg_pairs, m2l_pairs = smx.kernel_timings(capi.MIXED, reps=5)
     tim64, _, _ = s64.kernel_timings(capi.FP64, reps=3)
+    timdd, _, _ = smx.kernel_timings(DD_RESIDUAL, reps=3)
     fp32_peak = capi.fma_peak_tflops(False, dev)
     fp64_peak = capi.fma_peak_tflops(True, dev)
     achieved = alg_pairs * FLOP_PER_PAIR / (tim32["near"] * 1e-3) / 1e12
     achieved64 = alg_pairs * FLOP_PER_PAIR / (tim64["near"] * 1e-3) / 1e12
+    pairs_per_s = {"fp32": alg_pairs / (tim32["near"] * 1e-3),
+                   "double_float": alg_pairs / (timdd["near"] * 1e-3),
+                   "fp64": alg_pairs / (tim64["near"] * 1e-3)}
     pk, pk_kind = peaks()
 
-    resid = float(np.linalg.norm(rhs - s64.apply(mu_mx)))
+    mu_head = mu_lrn if mu_lrn is not None else mu_mx
+    resid = float(np.linalg.norm(rhs - s64.apply(mu_head)))
     E = b.external_field()
-    de = float(abs(0.5 * (mu_mx - mu64) @ E))
+    de = float(abs(0.5 * (mu_head - mu64) @ E))
+    batched = batched_section(dev, 1, flush) if (not args.no_batched and world == 1) else None
     if rank != 0:
         return
     cpu, _ = cpu_baseline_sample(b, rhs, summation, order) if not args.no_cpu else (None, None)
@@ -288,12 +409,17 @@ def run_ours(args):
                    "sites": b.n, "l2": "256 MB buffer written between timed steps",
                    "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
         "solves_per_s": total / t_mixed,
+        "method": "mixed precision + learned guess/preconditioner" if lrn else
+                  "mixed precision (no trained model found)",
         "plain_fp64_s": plain, "speedup_vs_plain_fp64": plain / t_mixed,
+        "mixed_without_model_s": t_mixed_plain,
+        "learned": lrn,
         "iterations": {"mixed_fp32_applies": st["fp32_applies"],
                        "mixed_fp64_applies": st["fp64_applies"],
                        "plain_fp64_iterations": st64["fp64_applies"]},
-        "parity": {"fp64_residual_of_mixed": resid, "mu_maxabs_vs_fp64": float(
-            np.abs(mu_mx - mu64).max()), "epol_diff_hartree": de},
+        "parity": {"fp64_residual": resid, "mu_maxabs_vs_fp64": float(
+            np.abs(mu_head - mu64).max()), "epol_diff_hartree": de},
+        "batched": batched,
         "roofline": {"bound": "fp32", "kernel": "k_p2p<float,1,damped> (near field)",
                      "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak, "traffic": None,
@@ -302,7 +428,8 @@ def run_ours(args):
                      "algorithmic": f"{alg_pairs} pairs x {FLOP_PER_PAIR} FLOP per launch"},
         "roofline_fp64": {"bound": "fp64", "achieved": achieved64, "peak": fp64_peak,
                           "unit": "TFLOP/s", "frac": achieved64 / fp64_peak},
-        "phases_ms": {"fp32": tim32, "fp64": tim64},
+        "phases_ms": {"fp32": tim32, "double_float_residual": timdd, "fp64": tim64},
+        "near_pairs_per_s": pairs_per_s,
         "peaks": {"hbm_gbs": pk.get("hbm_gbs"), "bf16_tflops": pk.get("bf16_tflops"),
                   "kind": pk_kind, "fp32_fma_tflops": fp32_peak, "fp64_fma_tflops": fp64_peak},
         "e2e": {"value": e2e_v, "unit": "s", "h2d_bytes_per_step": int(rhs.nbytes),
@@ -322,6 +449,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="c1", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched section")
+    ap.add_argument("--no-learned", action="store_true", help="skip the trained model")
+    ap.add_argument("--model", default=os.path.join(ROOT, "cppe_gb300", "data",
+                                                    "learned_water.npz"))
     ap.add_argument("--apply-only", type=int, default=0, metavar="K",
                     help="run K FP32 and K FP64 operator applies and print phase timings")
     args = ap.parse_args()

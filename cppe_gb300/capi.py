@@ -52,6 +52,7 @@ def lib():
                                       ctypes.POINTER(ctypes.c_void_p)]
         l.cppe_gpu_destroy.argtypes = [ctypes.c_void_p]
         for f in ("cppe_gpu_bmatrix_apply", "cppe_gpu_bmatrix_apply_fp32",
+                  "cppe_gpu_bmatrix_apply_dd",
                   "cppe_gpu_apply_diagonal", "cppe_gpu_apply_diagonal_inverse"):
             getattr(l, f).argtypes = [ctypes.c_void_p, D, D]
         l.cppe_gpu_to_dense.argtypes = [ctypes.c_void_p, D]
@@ -311,6 +312,7 @@ class System:
                       i32(excl_idx) if excl_idx is not None else None]
         self.n = self._keep[0].shape[0]
         self.opts = options(**opts)
+        self.device = self.opts.device
         h = ctypes.c_void_p()
         check(lib().cppe_gpu_create(self.n, dp(self._keep[0]), dp(self._keep[1]),
                                     ip(self._keep[2]), ip(self._keep[3]),
@@ -328,10 +330,11 @@ class System:
         except Exception:
             pass
 
-    def apply(self, v, fp32=False):
+    def apply(self, v, fp32=False, dd=False):
         v = f64(v)
         out = np.zeros_like(v)
-        fn = lib().cppe_gpu_bmatrix_apply_fp32 if fp32 else lib().cppe_gpu_bmatrix_apply
+        fn = (lib().cppe_gpu_bmatrix_apply_fp32 if fp32 else
+              lib().cppe_gpu_bmatrix_apply_dd if dd else lib().cppe_gpu_bmatrix_apply)
         check(fn(self.h, dp(v), dp(out)))
         return out
 

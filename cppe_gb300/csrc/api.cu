@@ -251,7 +251,8 @@ int cppe_gpu_destroy(cppe_gpu_system* sys) {
   });
 }
 
-static int apply_host(cppe_gpu_system* sys, const double* in, double* out, bool fp32) {
+// arith: 0 FP64, 1 FP32, 2 FP64 with the double-float near field
+static int apply_host(cppe_gpu_system* sys, const double* in, double* out, int arith) {
   return guard([&]() -> int {
     need(sys && in && out, "null argument");
     System& S = sys->s;
@@ -260,10 +261,10 @@ static int apply_host(cppe_gpu_system* sys, const double* in, double* out, bool 
     CG_CUDA(cudaMemcpyAsync(S.tmp_out.p, in, n3 * sizeof(double), cudaMemcpyHostToDevice,
                             S.stream));
     permute_in(S.geo, S.tmp_out.p, S.tmp_in.p, 3, S.stream);
-    if (fp32)
+    if (arith == 1)
       S.apply32_widen(S.tmp_in.p, S.tmp_out.p);
     else
-      S.apply64(S.tmp_in.p, S.tmp_out.p, false);
+      S.apply64(S.tmp_in.p, S.tmp_out.p, false, arith == 2 ? NEAR_DD : NEAR_FP64);
     permute_out(S.geo, S.tmp_out.p, S.tmp_in.p, 3, S.stream);
     CG_CUDA(cudaMemcpyAsync(out, S.tmp_in.p, n3 * sizeof(double), cudaMemcpyDeviceToHost,
                             S.stream));
@@ -273,10 +274,13 @@ static int apply_host(cppe_gpu_system* sys, const double* in, double* out, bool 
 }
 
 int cppe_gpu_bmatrix_apply(cppe_gpu_system* sys, const double* in, double* out) {
-  return apply_host(sys, in, out, false);
+  return apply_host(sys, in, out, 0);
 }
 int cppe_gpu_bmatrix_apply_fp32(cppe_gpu_system* sys, const double* in, double* out) {
-  return apply_host(sys, in, out, true);
+  return apply_host(sys, in, out, 1);
+}
+int cppe_gpu_bmatrix_apply_dd(cppe_gpu_system* sys, const double* in, double* out) {
+  return apply_host(sys, in, out, 2);
 }
 
 int cppe_gpu_bmatrix_apply_device(cppe_gpu_system* sys, const double* d_in, double* d_out) {
@@ -577,6 +581,7 @@ int cppe_gpu_kernel_timings(cppe_gpu_system* sys, int precision, int reps, doubl
                             long long* near_pairs, long long* m2l_pairs) {
   return guard([&]() -> int {
     need(sys && out_ms && reps > 0, "null argument");
+    need(precision >= 0 && precision <= 2, "precision must be 0, 1 or 2");
     System& S = sys->s;
     S.phase_timings(precision, reps, out_ms);
     if (near_pairs) *near_pairs = S.geo.alg_pairs;

@@ -295,6 +295,8 @@ BatchSystem::~BatchSystem() {
   if (stream) {
     cudaSetDevice(device);
     cudaStreamSynchronize(stream);
+    if (side.s) cudaStreamSynchronize(side.s);
+    side.destroy();
     cudaStreamDestroy(stream);
   }
   if (h_active) cudaFreeHost(h_active);
@@ -306,14 +308,13 @@ void BatchSystem::init(int nsys, const int* site_offset, const double* xyz, cons
   opt  = o;
   nrhs = nrhs_;
   if (nsys < 1 || nrhs < 1) fail(CPPE_GPU_INVALID_ARG, "empty batch");
-  const bool any = true;
-  (void)any;
   int ndev = 0;
   CG_CUDA(cudaGetDeviceCount(&ndev));
   if (o.device < 0 || o.device >= ndev) fail(CPPE_GPU_INVALID_ARG, "bad CUDA device ordinal");
   device = o.device;
   CG_CUDA(cudaSetDevice(device));
   CG_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  side.create();
   if (o.tree_expansion_order < 2 || o.tree_expansion_order > 7)
     fail(CPPE_GPU_INVALID_ARG, "tree_expansion_order must be in [2, 7]");
   std::vector<Geometry> parts(nsys);
@@ -398,13 +399,13 @@ void BatchSystem::init(int nsys, const int* site_offset, const double* xyz, cons
 }
 
 template <typename T>
-void BatchSystem::apply_seg(const T* in, T* out, bool fast_exp) {
+void BatchSystem::apply_seg(const T* in, T* out, int near_mode) {
   ReduceSlots rs{nullptr, nullptr, nullptr};
   rs.site_values = site_a.p;
   FieldWork<T>& w = work<T>();
   const T* ainv   = std::is_same<T, double>::value ? (const T*)ainv64.p : (const T*)ainv32.p;
   eval_field<T>(geo, ops.get(), w, 1, in, opt.damp != 0, opt.damping_factor, FINISH_APPLY, ainv,
-                out, nullptr, 1.0, &rs, stream, nullptr, fast_exp);
+                out, nullptr, 1.0, &rs, stream, nullptr, near_mode, &side);
   k_seg_sum<<<nseg, BB, 0, stream>>>(seg_start.p, site_a.p, nullptr, seg_pap.p, nullptr);
   CG_LAUNCH();
 }
@@ -531,7 +532,7 @@ int BatchSystem::solve_device(const double* d_rhs, double* d_mu, int* iters_out)
       if (!(exact && rmax * 1e-4 < t)) {
         k_bacc<<<nb3, BB, 0, stream>>>(n3, x.p, d32.p);
         CG_LAUNCH();
-        apply_seg<double>(x.p, Ap.p, true);
+        apply_seg<double>(x.p, Ap.p, NEAR_DD);
         stats.fp64_applies++;
         k_bres<<<nb, BB, 0, stream>>>(n, F.p, Ap.p, nullptr, r.p, site_b.p);
         CG_LAUNCH();

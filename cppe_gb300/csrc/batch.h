@@ -13,6 +13,7 @@ struct BatchSystem {
   cppe_gpu_options opt{};
   int device          = 0;
   cudaStream_t stream = nullptr;
+  SideStream side;  // far-field passes, concurrent with the near field
   std::vector<int> sys_sites;  // site offsets of the snapshots (caller layout)
   Geometry geo;                // all segments concatenated
   std::unique_ptr<DeviceOps> ops;
@@ -45,7 +46,7 @@ struct BatchSystem {
       return w32;
   }
   template <typename T>
-  void apply_seg(const T* in, T* out, bool fast_exp = false);
+  void apply_seg(const T* in, T* out, int near_mode = NEAR_FP64);
   template <typename T>
   int run_pcg(T* x, T* r, T* z, T* p, T* Ap, const T* a6, int maxiter);
   void seg_norms_from_site_b();

@@ -14,17 +14,19 @@
 // Every output element is owned by exactly one thread (no atomics), so
 // results are bitwise reproducible run to run.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <numeric>
+#include <type_traits>
 
 #include "engine.h"
+#include "dd.cuh"
 #include "m2l_fixed.cuh"
 
 namespace cg {
 
 constexpr int P2P_BLOCK  = 128;
 constexpr int P2P_TILE   = 512;  // source sites staged in shared memory per tile
-constexpr int P2P_PIECES = 16;   // contiguous source ranges per tile
 constexpr int M2L_WARPS  = 4;
 
 // ---------------------------------------------------------------------------
@@ -138,6 +140,20 @@ void Geometry::prepare(int n_, const double* xyz, const double* s_damp, const in
   h_pos64.assign(n, double4_32a{});
   h_hi.assign(n, float4{});
   h_lo.assign(n, float4{});
+  // FP32 coordinates: relative to the bounding-box centre, snapped to a grid
+  // of spacing 2^e with |x| < 2^(e+22), so that every difference of two high
+  // parts is exact in FP32; the remainders go to `lo` (the FP32 and DD pair
+  // passes use only differences).  s = alpha^(-1/6) is split the same way.
+  double lo_c[3] = {1e300, 1e300, 1e300}, hi_c[3] = {-1e300, -1e300, -1e300};
+  for (int i = 0; i < n; ++i)
+    for (int c = 0; c < 3; ++c)
+      lo_c[c] = std::min(lo_c[c], xyz[3 * i + c]), hi_c[c] = std::max(hi_c[c], xyz[3 * i + c]);
+  double ctr[3], ext = 1.0;
+  for (int c = 0; c < 3; ++c) {
+    ctr[c] = n ? 0.5 * (lo_c[c] + hi_c[c]) : 0.0;
+    if (n) ext = std::max(ext, 0.5 * (hi_c[c] - lo_c[c]) * 1.0001);
+  }
+  const double quantum = std::ldexp(1.0, (int)std::ceil(std::log2(ext)) - 22);
   auto& p64 = h_pos64;
   auto& hi  = h_hi;
   auto& lo  = h_lo;
@@ -146,9 +162,15 @@ void Geometry::prepare(int n_, const double* xyz, const double* s_damp, const in
     const double x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
     const double sd = s_damp ? s_damp[i] : 0.0;
     p64[k]         = make_double4_32a(x, y, z, sd);
-    const float hx = (float)x, hy = (float)y, hz = (float)z;
-    hi[k]          = make_float4(hx, hy, hz, (float)sd);
-    lo[k]          = make_float4((float)(x - hx), (float)(y - hy), (float)(z - hz), 0.f);
+    double r[3]    = {x - ctr[0], y - ctr[1], z - ctr[2]};
+    float h[3], l[3];
+    for (int c = 0; c < 3; ++c) {
+      h[c] = (float)(std::nearbyint(r[c] / quantum) * quantum);
+      l[c] = (float)(r[c] - (double)h[c]);
+    }
+    const float sh = (float)sd;
+    hi[k]          = make_float4(h[0], h[1], h[2], sh);
+    lo[k]          = make_float4(l[0], l[1], l[2], (float)(sd - (double)sh));
   }
 
   // Exclusion corrections: pairs the reference skips but the near-field pass
@@ -272,9 +294,11 @@ template <>
 struct SiteRec<double> {
   double x, y, z, s;
 };
+// FP32 record: grid-snapped coordinates (x, y, z), their remainders
+// (lx, ly, lz), and s = alpha^(-1/6) as s + ls.
 template <>
 struct SiteRec<float> {
-  float x, y, z, s, lx, ly, lz, pad;
+  float x, y, z, s, lx, ly, lz, ls;
 };
 
 template <typename T>
@@ -293,7 +317,7 @@ struct PosArgs<float> {
   const float4* lo;
   __device__ SiteRec<float> load(int k) const {
     float4 h = hi[k], l = lo[k];
-    return {h.x, h.y, h.z, h.w, l.x, l.y, l.z, 0.f};
+    return {h.x, h.y, h.z, h.w, l.x, l.y, l.z, l.w};
   }
 };
 
@@ -349,6 +373,72 @@ struct Comp3<float> {
 };
 
 // ---------------------------------------------------------------------------
+// Tile planning of the near-field pass.  An item covers positions [cur, b1)
+// of its target leaf's P2P list; each round warp 0 takes the next (up to) 32
+// source leaves, prefix-sums their sizes across the warp and keeps those that
+// start inside a tile of P2P_TILE sites, the last one possibly in part
+// (`coff` sites of the first leaf were taken by the previous round).
+// ---------------------------------------------------------------------------
+struct TilePlan {
+  int pstart[33];  // first site of each piece
+  int poff[34];    // tile offset of each piece (poff[np] = tile size)
+  int np, cur, coff;
+};
+
+__device__ __forceinline__ void plan_tile(TilePlan& tp, int b1, const int* __restrict__ p2p_src,
+                                          const int* __restrict__ leaf_start) {
+  const int lane = threadIdx.x & 31;
+  const int cur = tp.cur, coff = tp.coff;
+  const int e   = cur + lane;
+  int start = 0, cnt = 0;
+  if (e < b1) {
+    const int Lb = p2p_src[e];
+    start        = leaf_start[Lb];
+    cnt          = leaf_start[Lb + 1] - start;
+    if (lane == 0) start += coff, cnt -= coff;
+  }
+  int incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  const int excl     = incl - cnt;
+  const bool take    = e < b1 && excl < P2P_TILE;
+  const int takecnt  = take ? min(cnt, P2P_TILE - excl) : 0;
+  const unsigned msk = __ballot_sync(0xffffffffu, take);
+  const int np       = __popc(msk);
+  const int last     = max(np - 1, 0);
+  const int tot      = __shfl_sync(0xffffffffu, excl + takecnt, last);
+  const int lastcnt  = __shfl_sync(0xffffffffu, cnt, last);
+  const int lasttake = __shfl_sync(0xffffffffu, takecnt, last);
+  if (take) tp.pstart[lane] = start, tp.poff[lane] = excl;
+  if (lane == 0) {
+    tp.np       = np;
+    tp.poff[np] = np ? tot : 0;
+    if (np > 0) {
+      if (lasttake == lastcnt)
+        tp.cur = cur + np, tp.coff = 0;
+      else
+        tp.cur = cur + last, tp.coff = (last == 0 ? coff : 0) + lasttake;
+    }
+  }
+}
+
+// Site index of tile slot q (the piece k with poff[k] <= q < poff[k + 1]).
+__device__ __forceinline__ int tile_site(const TilePlan& tp, int q) {
+  int lo = 0, hi = tp.np - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tp.poff[mid] <= q)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return tp.pstart[lo] + (q - tp.poff[lo]);
+}
+
+// ---------------------------------------------------------------------------
 // Near field: block per work item (target leaf, piece of its source list).
 // Every thread serves two target sites of the leaf against a stride of the
 // staged sources (S = 128 / ceil(n_A / 2) groups), so each source read from
@@ -363,14 +453,12 @@ __global__ void __launch_bounds__(P2P_BLOCK)
   constexpr int NS = ncomp(M);
   __shared__ SiteRec<T> s_rec[P2P_TILE];
   __shared__ T s_S[P2P_TILE * NS];
-  __shared__ int s_pstart[33], s_poff[34];
-  __shared__ int s_np, s_cur, s_coff;
+  __shared__ TilePlan s_plan;
   __shared__ T s_red[P2P_BLOCK * 6];
 
   const int4 it = items[blockIdx.x];
   const int A = it.x, b0 = it.y, b1 = it.z, slot = it.w;
   const int a0 = leaf_start[A], nA = leaf_start[A + 1] - a0;
-  const int lane = threadIdx.x & 31;
 
   for (int tb = 0; tb < nA; tb += 2 * P2P_BLOCK) {
     const int nT = min(2 * P2P_BLOCK, nA - tb);
@@ -383,63 +471,16 @@ __global__ void __launch_bounds__(P2P_BLOCK)
     const SiteRec<T> me1 = pa.load(a0 + tb + (has1 ? t + T2 : t));
     const T ai0 = damping * me0.s, ai1 = damping * me1.s;
     Comp3<T> acc0, acc1;
-    if (threadIdx.x == 0) s_cur = b0, s_coff = 0;
+    if (threadIdx.x == 0) s_plan.cur = b0, s_plan.coff = 0;
     __syncthreads();
     while (true) {
-      if (threadIdx.x < 32) {
-        // Plan the next tile: the next (up to) 32 source pieces, their sizes
-        // prefix-summed across the warp; pieces that start inside the tile
-        // are taken, the last one possibly in part.
-        const int cur = s_cur, coff = s_coff;
-        const int e   = cur + lane;
-        int start = 0, cnt = 0;
-        if (e < b1) {
-          const int Lb = p2p_src[e];
-          start        = leaf_start[Lb];
-          cnt          = leaf_start[Lb + 1] - start;
-          if (lane == 0) start += coff, cnt -= coff;
-        }
-        int incl = cnt;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const int v = __shfl_up_sync(0xffffffffu, incl, o);
-          if (lane >= o) incl += v;
-        }
-        const int excl     = incl - cnt;
-        const bool take    = e < b1 && excl < P2P_TILE;
-        const int takecnt  = take ? min(cnt, P2P_TILE - excl) : 0;
-        const unsigned msk = __ballot_sync(0xffffffffu, take);
-        const int np       = __popc(msk);
-        const int last     = max(np - 1, 0);
-        const int tot      = __shfl_sync(0xffffffffu, excl + takecnt, last);
-        const int lastcnt  = __shfl_sync(0xffffffffu, cnt, last);
-        const int lasttake = __shfl_sync(0xffffffffu, takecnt, last);
-        if (take) s_pstart[lane] = start, s_poff[lane] = excl;
-        if (lane == 0) {
-          s_np       = np;
-          s_poff[np] = np ? tot : 0;
-          if (np > 0) {
-            if (lasttake == lastcnt)
-              s_cur = cur + np, s_coff = 0;
-            else
-              s_cur = cur + last, s_coff = (last == 0 ? coff : 0) + lasttake;
-          }
-        }
-      }
+      if (threadIdx.x < 32) plan_tile(s_plan, b1, p2p_src, leaf_start);
       __syncthreads();
-      const int np = s_np;
+      const int np = s_plan.np;
       if (np == 0) break;
-      const int total = s_poff[np];
+      const int total = s_plan.poff[np];
       for (int q = threadIdx.x; q < total; q += P2P_BLOCK) {
-        int lo = 0, hi = np - 1;  // piece k with s_poff[k] <= q < s_poff[k + 1]
-        while (lo < hi) {
-          const int mid = (lo + hi + 1) >> 1;
-          if (s_poff[mid] <= q)
-            lo = mid;
-          else
-            hi = mid - 1;
-        }
-        const int j = s_pstart[lo] + (q - s_poff[lo]);
+        const int j = tile_site(s_plan, q);
         s_rec[q]    = pa.load(j);
 #pragma unroll
         for (int c = 0; c < NS; ++c) s_S[q * NS + c] = src[(size_t)j * NS + c];
@@ -473,6 +514,260 @@ __global__ void __launch_bounds__(P2P_BLOCK)
       o[0] = f[0], o[1] = f[1], o[2] = f[2];
       if (threadIdx.x + T2 < nT) {
         T* o1 = Fnear + (size_t)slot * 3 * n + 3 * (size_t)(a0 + tb + threadIdx.x + T2);
+        o1[0] = f[3], o1[1] = f[4], o1[2] = f[5];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Near field, FP32, dipole sources: the inner pass of the mixed solver.
+// Positions are taken relative to the first site of the target leaf once per
+// staged source (hi/lo differences, ~FP32 accuracy of the relative vector),
+// so a pair costs one subtraction per component; the v < 50 cut of the FP64
+// path is not needed (expf underflows to 0 there).  Sources are staged as
+// float4 {x, y, z, s} and {mu_x, mu_y, mu_z, -}: two shared loads feed the
+// two targets of a thread.
+// ---------------------------------------------------------------------------
+template <bool DAMP>
+__device__ __forceinline__ void f32_pair_m1(const float4& ti, float ai, const float4& sj,
+                                            const float4& mu, float& fx, float& fy, float& fz) {
+  const float x = ti.x - sj.x, y = ti.y - sj.y, z = ti.z - sj.z;
+  const float r2 = fmaf(x, x, fmaf(y, y, z * z));
+  const float ir = r2 > 0.f ? rsqrtf(r2) : 0.f;
+  const float ir2 = ir * ir;
+  const float ir3 = ir2 * ir;
+  float A = ir3, B = 3.f * ir3 * ir2;  // G1 = -A, G2 = B
+  if (DAMP) {
+    const float a = ai * sj.w;
+    if (a > 0.f) {
+      const float v  = a * (r2 * ir);
+      const float e  = __expf(-v);
+      const float fE = fmaf(-fmaf(v, fmaf(v, 0.5f, 1.f), 1.f), e, 1.f);
+      const float fT = fmaf(-(v * v) * (v * (1.f / 6.f)), e, fE);
+      A *= fE, B *= fT;
+    }
+  }
+  const float C = (mu.x * x + mu.y * y + mu.z * z) * B;
+  fx = fmaf(mu.x, A, fmaf(-x, C, fx));
+  fy = fmaf(mu.y, A, fmaf(-y, C, fy));
+  fz = fmaf(mu.z, A, fmaf(-z, C, fz));
+}
+
+template <bool DAMP>
+__global__ void __launch_bounds__(P2P_BLOCK)
+      k_p2p32_m1(int n, const int* __restrict__ leaf_start, const int4* __restrict__ items,
+                 const int* __restrict__ p2p_src, const float4* __restrict__ hi,
+                 const float4* __restrict__ lo, const float* __restrict__ src, float damping,
+                 float* __restrict__ Fnear) {
+  __shared__ float4 s_pos[P2P_TILE];
+  __shared__ float4 s_mu[P2P_TILE];
+  __shared__ TilePlan s_plan;
+  __shared__ float s_red[P2P_BLOCK * 6];
+
+  const int4 it = items[blockIdx.x];
+  const int A = it.x, b0 = it.y, b1 = it.z, slot = it.w;
+  const int a0 = leaf_start[A], nA = leaf_start[A + 1] - a0;
+  const float4 oh = hi[a0], ol = lo[a0];
+  auto rel = [&](int k) {
+    const float4 h = hi[k], l = lo[k];
+    return make_float4((h.x - oh.x) + (l.x - ol.x), (h.y - oh.y) + (l.y - ol.y),
+                       (h.z - oh.z) + (l.z - ol.z), h.w);
+  };
+
+  for (int tb = 0; tb < nA; tb += 2 * P2P_BLOCK) {
+    const int nT = min(2 * P2P_BLOCK, nA - tb);
+    const int T2 = (nT + 1) >> 1;
+    const int S  = P2P_BLOCK / T2;
+    const int t = threadIdx.x % T2, g = threadIdx.x / T2;
+    const bool active = g < S;
+    const bool has1   = t + T2 < nT;
+    const float4 me0 = rel(a0 + tb + t);
+    const float4 me1 = rel(a0 + tb + (has1 ? t + T2 : t));
+    const float ai0 = damping * me0.w, ai1 = damping * me1.w;
+    Comp3<float> acc0, acc1;
+    if (threadIdx.x == 0) s_plan.cur = b0, s_plan.coff = 0;
+    __syncthreads();
+    while (true) {
+      if (threadIdx.x < 32) plan_tile(s_plan, b1, p2p_src, leaf_start);
+      __syncthreads();
+      const int np = s_plan.np;
+      if (np == 0) break;
+      const int total = s_plan.poff[np];
+      for (int q = threadIdx.x; q < total; q += P2P_BLOCK) {
+        const int j = tile_site(s_plan, q);
+        s_pos[q]    = rel(j);
+        s_mu[q]     = make_float4(src[3 * (size_t)j], src[3 * (size_t)j + 1],
+                                  src[3 * (size_t)j + 2], 0.f);
+      }
+      __syncthreads();
+      if (active) {
+        float fx0 = 0, fy0 = 0, fz0 = 0, fx1 = 0, fy1 = 0, fz1 = 0;
+        for (int jj = g; jj < total; jj += S) {
+          const float4 sj = s_pos[jj];
+          const float4 mu = s_mu[jj];
+          f32_pair_m1<DAMP>(me0, ai0, sj, mu, fx0, fy0, fz0);
+          f32_pair_m1<DAMP>(me1, ai1, sj, mu, fx1, fy1, fz1);
+        }
+        acc0.add(fx0, fy0, fz0);
+        acc1.add(fx1, fy1, fz1);
+      }
+      __syncthreads();
+    }
+    if (active) {
+      float* r = &s_red[(g * T2 + t) * 6];
+      r[0] = acc0.gx(), r[1] = acc0.gy(), r[2] = acc0.gz();
+      r[3] = acc1.gx(), r[4] = acc1.gy(), r[5] = acc1.gz();
+    }
+    __syncthreads();
+    if (threadIdx.x < T2) {
+      float f[6] = {0, 0, 0, 0, 0, 0};
+      for (int gg = 0; gg < S; ++gg)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) f[c] += s_red[(gg * T2 + threadIdx.x) * 6 + c];
+      float* o = Fnear + (size_t)slot * 3 * n + 3 * (size_t)(a0 + tb + threadIdx.x);
+      o[0] = f[0], o[1] = f[1], o[2] = f[2];
+      if (threadIdx.x + T2 < nT) {
+        float* o1 = Fnear + (size_t)slot * 3 * n + 3 * (size_t)(a0 + tb + threadIdx.x + T2);
+        o1[0] = f[3], o1[1] = f[4], o1[2] = f[5];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Near field in double-float arithmetic (dipole sources): the FP64-accurate
+// pass of the mixed solver's residual B x, on the FP32 pipe.  Same items and
+// tiles as k_p2p; each pair is evaluated in DD (about 1e-13 relative per
+// term), accumulated in DD and written in FP64.  Separations are exact in
+// their high parts because the FP32 coordinates are snapped to a common grid.
+// ---------------------------------------------------------------------------
+template <bool DAMP>
+__device__ __forceinline__ void dd_pair_m1(const SiteRec<float>& ti, dd ai,
+                                           const SiteRec<float>& sj, const float* mu,
+                                           const float2* etab, dd (&f)[3]) {
+  const dd x = {ti.x - sj.x, ti.lx - sj.lx};
+  const dd y = {ti.y - sj.y, ti.ly - sj.ly};
+  const dd z = {ti.z - sj.z, ti.lz - sj.lz};
+  const dd r2 = dd_add(dd_add_lazy(dd_sqr_full(x), dd_sqr_full(y)), dd_sqr_full(z));
+  if (r2.h == 0.f) return;  // a site paired with itself (direct summation)
+  const dd ir  = dd_rsqrt(r2);
+  const dd ir2 = dd_sqr(ir);
+  const dd ir3 = dd_mul(ir2, ir);
+  dd G1        = dd_neg(ir3);
+  dd G2        = dd_mul_f(dd_mul(ir3, ir2), 3.f);
+  if (DAMP) {
+    const dd a = dd_mul(ai, dd{sj.s, sj.ls});
+    if (a.h > 0.f) {
+      const dd v = dd_mul(a, dd_mul(r2, ir));
+      if (v.h < 50.f) {
+        dd fE, fT;
+        if (v.h < 20.f) {
+          const dd e  = dd_exp_neg(v, etab);
+          const dd v2 = dd_sqr(v);
+          const dd u  = dd_add(dd_two_sum(1.f, v.h), dd{0.5f * v2.h, v.l + 0.5f * v2.l});
+          const dd w  = dd_mul(dd_mul(v2, v), dd{1.f / 6.f, DD_SIXTH_LO});
+          fE          = dd_sub(dd{1.f, 0.f}, dd_mul(u, e));
+          fT          = dd_sub(fE, dd_mul(w, e));
+        } else {
+          // (1 + v + v^2/2) e^-v < 5e-7 here: FP32 suffices for the deficit
+          const float e = expf(-v.h);
+          const float u = fmaf(v.h, fmaf(v.h, 0.5f, 1.f), 1.f) * e;
+          const float w = v.h * v.h * v.h * (1.f / 6.f) * e;
+          fE            = dd_fast_two_sum(1.f, -u);
+          fT            = dd_fast_two_sum(1.f, -(u + w));
+        }
+        G1 = dd_mul(G1, fE);
+        G2 = dd_mul(G2, fT);
+      }
+    }
+  }
+  const dd mx = {mu[0], mu[3]}, my = {mu[1], mu[4]}, mz = {mu[2], mu[5]};
+  const dd mr = dd_add(dd_add_lazy(dd_mul(mx, x), dd_mul(my, y)), dd_mul(mz, z));
+  const dd sg = dd_mul(mr, G2);
+  f[0] = dd_add_lazy(f[0], dd_neg(dd_add_lazy(dd_mul(mx, G1), dd_mul(sg, x))));
+  f[1] = dd_add_lazy(f[1], dd_neg(dd_add_lazy(dd_mul(my, G1), dd_mul(sg, y))));
+  f[2] = dd_add_lazy(f[2], dd_neg(dd_add_lazy(dd_mul(mz, G1), dd_mul(sg, z))));
+}
+
+template <bool DAMP>
+__global__ void __launch_bounds__(P2P_BLOCK)
+      k_p2p_dd(int n, const int* __restrict__ leaf_start, const int4* __restrict__ items,
+               const int* __restrict__ p2p_src, PosArgs<float> pa,
+               const double* __restrict__ src, double damping, double* __restrict__ Fnear) {
+  __shared__ SiteRec<float> s_rec[P2P_TILE];
+  __shared__ float s_mu[P2P_TILE * 6];
+  __shared__ float2 s_etab[DD_EXP_TAB];
+  __shared__ TilePlan s_plan;
+  __shared__ double s_red[P2P_BLOCK * 6];
+
+  for (int k = threadIdx.x; k < DD_EXP_TAB; k += P2P_BLOCK) {
+    const double e = exp(-0.0625 * k);
+    const float h  = (float)e;
+    s_etab[k]      = make_float2(h, (float)(e - (double)h));
+  }
+  const int4 it = items[blockIdx.x];
+  const int A = it.x, b0 = it.y, b1 = it.z, slot = it.w;
+  const int a0 = leaf_start[A], nA = leaf_start[A + 1] - a0;
+  const dd dmp = dd_from(damping);
+
+  for (int tb = 0; tb < nA; tb += 2 * P2P_BLOCK) {
+    const int nT = min(2 * P2P_BLOCK, nA - tb);
+    const int T2 = (nT + 1) >> 1;
+    const int S  = P2P_BLOCK / T2;
+    const int t = threadIdx.x % T2, g = threadIdx.x / T2;
+    const bool active = g < S;
+    const bool has1   = t + T2 < nT;
+    const SiteRec<float> me0 = pa.load(a0 + tb + t);
+    const SiteRec<float> me1 = pa.load(a0 + tb + (has1 ? t + T2 : t));
+    const dd ai0 = dd_mul(dmp, dd{me0.s, me0.ls}), ai1 = dd_mul(dmp, dd{me1.s, me1.ls});
+    dd f0[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    dd f1[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    if (threadIdx.x == 0) s_plan.cur = b0, s_plan.coff = 0;
+    __syncthreads();
+    while (true) {
+      if (threadIdx.x < 32) plan_tile(s_plan, b1, p2p_src, leaf_start);
+      __syncthreads();
+      const int np = s_plan.np;
+      if (np == 0) break;
+      const int total = s_plan.poff[np];
+      for (int q = threadIdx.x; q < total; q += P2P_BLOCK) {
+        const int j = tile_site(s_plan, q);
+        s_rec[q]    = pa.load(j);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const dd m = dd_from(src[3 * (size_t)j + c]);
+          s_mu[q * 6 + c] = m.h, s_mu[q * 6 + 3 + c] = m.l;
+        }
+      }
+      __syncthreads();
+      if (active) {
+        for (int jj = g; jj < total; jj += S) {
+          const SiteRec<float> sj = s_rec[jj];
+          const float* mu         = &s_mu[jj * 6];
+          dd_pair_m1<DAMP>(me0, ai0, sj, mu, s_etab, f0);
+          dd_pair_m1<DAMP>(me1, ai1, sj, mu, s_etab, f1);
+        }
+      }
+      __syncthreads();
+    }
+    if (active) {
+      double* r = &s_red[(g * T2 + t) * 6];
+      r[0] = dd_to(f0[0]), r[1] = dd_to(f0[1]), r[2] = dd_to(f0[2]);
+      r[3] = dd_to(f1[0]), r[4] = dd_to(f1[1]), r[5] = dd_to(f1[2]);
+    }
+    __syncthreads();
+    if (threadIdx.x < T2) {
+      double f[6] = {0, 0, 0, 0, 0, 0};
+      for (int gg = 0; gg < S; ++gg)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) f[c] += s_red[(gg * T2 + threadIdx.x) * 6 + c];
+      double* o = Fnear + (size_t)slot * 3 * n + 3 * (size_t)(a0 + tb + threadIdx.x);
+      o[0] = f[0], o[1] = f[1], o[2] = f[2];
+      if (threadIdx.x + T2 < nT) {
+        double* o1 = Fnear + (size_t)slot * 3 * n + 3 * (size_t)(a0 + tb + threadIdx.x + T2);
         o1[0] = f[3], o1[1] = f[4], o1[2] = f[5];
       }
     }
@@ -742,6 +1037,16 @@ template <typename T, int M>
 static void launch_p2p(const Geometry& g, bool damp, bool fast, const T* src, T damping,
                        T* Fnear, cudaStream_t s) {
   const int grid = (int)g.h_items.size();
+  if constexpr (std::is_same<T, float>::value && M == 1) {
+    if (damp)
+      k_p2p32_m1<true><<<grid, P2P_BLOCK, 0, s>>>(g.n, g.leaf_start.p, g.items.p, g.p2p_src.p,
+                                                  g.hi32.p, g.lo32.p, src, damping, Fnear);
+    else
+      k_p2p32_m1<false><<<grid, P2P_BLOCK, 0, s>>>(g.n, g.leaf_start.p, g.items.p, g.p2p_src.p,
+                                                   g.hi32.p, g.lo32.p, src, damping, Fnear);
+    CG_LAUNCH();
+    return;
+  }
 #define CG_P2P(D, F)                                                                            \
   k_p2p<T, M, D, F><<<grid, P2P_BLOCK, 0, s>>>(g.n, g.leaf_start.p, g.items.p, g.p2p_src.p, \
                                                pos_args<T>(g), src, damping, Fnear)
@@ -755,11 +1060,35 @@ static void launch_p2p(const Geometry& g, bool damp, bool fast, const T* src, T 
   CG_LAUNCH();
 }
 
+void SideStream::create() {
+  CG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  CG_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+  CG_CUDA(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
+}
+void SideStream::destroy() {
+  if (join) cudaEventDestroy(join);
+  if (fork) cudaEventDestroy(fork);
+  if (s) cudaStreamDestroy(s);
+  s = nullptr, fork = join = nullptr;
+}
+
+static void launch_p2p_dd(const Geometry& g, bool damp, const double* src, double damping,
+                          double* Fnear, cudaStream_t s) {
+  const int grid = (int)g.h_items.size();
+  if (damp)
+    k_p2p_dd<true><<<grid, P2P_BLOCK, 0, s>>>(g.n, g.leaf_start.p, g.items.p, g.p2p_src.p,
+                                              pos_args<float>(g), src, damping, Fnear);
+  else
+    k_p2p_dd<false><<<grid, P2P_BLOCK, 0, s>>>(g.n, g.leaf_start.p, g.items.p, g.p2p_src.p,
+                                               pos_args<float>(g), src, damping, Fnear);
+  CG_LAUNCH();
+}
+
 template <typename T>
 void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m, const T* src,
                 bool damp, double damping, FinishMode mode, const T* ainv6, T* out,
                 double* out64, double sign, const ReduceSlots* dot, cudaStream_t s,
-                const PhaseEvents* pe, bool fast_exp) {
+                const PhaseEvents* pe, int near_mode, const SideStream* side) {
   const TreeView tv = g.view();
   OpsView ov{};
   const int n = g.n;
@@ -767,6 +1096,14 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
     if (pe) CG_CUDA(cudaEventRecord(pe->ev[k], s));
   };
   mark(0);
+  // far-field passes on the side stream when one is given (not while phases
+  // are being timed)
+  cudaStream_t fs = s;
+  if (g.fmm && side && side->s && !pe) {
+    CG_CUDA(cudaEventRecord(side->fork, s));
+    CG_CUDA(cudaStreamWaitEvent(side->s, side->fork, 0));
+    fs = side->s;
+  }
   if (g.fmm) {
     if (!ops || ops->host.m != m) fail(CPPE_GPU_INVALID_ARG, "FMM tables missing for order");
     ov = ops->view();
@@ -775,18 +1112,18 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
     const int TB = 128;
     {
       long work = (long)tv.nleaves * ov.msize;
-      k_p2m<T><<<(unsigned)((work + TB - 1) / TB), TB, 0, s>>>(tv, ov, g.pos64.p, src, w.M.p);
+      k_p2m<T><<<(unsigned)((work + TB - 1) / TB), TB, 0, fs>>>(tv, ov, g.pos64.p, src, w.M.p);
       CG_LAUNCH();
     }
     for (int l = (int)g.level_start.size() - 3; l >= 0; --l) {
       const int c0 = g.level_start[l], c1 = g.level_start[l + 1];
       long work    = (long)(c1 - c0) * ov.msize;
       if (work == 0) continue;
-      k_m2m<T><<<(unsigned)((work + TB - 1) / TB), TB, 0, s>>>(tv, ov, c0, c1, w.M.p);
+      k_m2m<T><<<(unsigned)((work + TB - 1) / TB), TB, 0, fs>>>(tv, ov, c0, c1, w.M.p);
       CG_LAUNCH();
     }
     mark(1);
-    if (launch_m2l_fixed<T>(tv, ov.m, ov.p, w.M.p, w.L.p, s)) {
+    if (launch_m2l_fixed<T>(tv, ov.m, ov.p, w.M.p, w.L.p, fs)) {
       CG_LAUNCH();
     } else {
       size_t smem = (size_t)(ov.nm2l_terms + 9 * ov.nt) * sizeof(int);
@@ -799,7 +1136,7 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
         attr_set[sizeof(T) == 8] = true;
       }
       const int blocks = (tv.ncells + M2L_WARPS - 1) / M2L_WARPS;
-      k_m2l<T><<<blocks, 32 * M2L_WARPS, smem, s>>>(tv, ov, w.M.p, w.L.p);
+      k_m2l<T><<<blocks, 32 * M2L_WARPS, smem, fs>>>(tv, ov, w.M.p, w.L.p);
       CG_LAUNCH();
     }
     mark(2);
@@ -807,19 +1144,29 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
       const int c0 = g.level_start[l], c1 = g.level_start[l + 1];
       long work    = (long)(c1 - c0) * ov.lsize;
       if (work == 0) continue;
-      k_l2l<T><<<(unsigned)((work + TB - 1) / TB), TB, 0, s>>>(tv, ov, c0, c1, w.L.p);
+      k_l2l<T><<<(unsigned)((work + TB - 1) / TB), TB, 0, fs>>>(tv, ov, c0, c1, w.L.p);
       CG_LAUNCH();
     }
     mark(3);
+    if (fs != s) CG_CUDA(cudaEventRecord(side->join, fs));
   } else {
     mark(1), mark(2), mark(3);
   }
   w.Fnear.alloc((size_t)g.nslot * 3 * n);
   const T dampT = (T)damping;
-  if (m == 0) launch_p2p<T, 0>(g, damp, fast_exp, src, dampT, w.Fnear.p, s);
-  if (m == 1) launch_p2p<T, 1>(g, damp, fast_exp, src, dampT, w.Fnear.p, s);
-  if (m == 2) launch_p2p<T, 2>(g, damp, fast_exp, src, dampT, w.Fnear.p, s);
+  const bool fast = near_mode != NEAR_FP64;
+  bool done       = false;
+  if constexpr (std::is_same<T, double>::value) {
+    if (near_mode == NEAR_DD && m == 1) {
+      launch_p2p_dd(g, damp, src, damping, w.Fnear.p, s);
+      done = true;
+    }
+  }
+  if (!done && m == 0) launch_p2p<T, 0>(g, damp, fast, src, dampT, w.Fnear.p, s);
+  if (!done && m == 1) launch_p2p<T, 1>(g, damp, fast, src, dampT, w.Fnear.p, s);
+  if (!done && m == 2) launch_p2p<T, 2>(g, damp, fast, src, dampT, w.Fnear.p, s);
   mark(4);
+  if (fs != s) CG_CUDA(cudaStreamWaitEvent(s, side->join, 0));
 
   const int FB = 256;
   const int nb = (n + FB - 1) / FB;
@@ -847,11 +1194,11 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
 template void eval_field<double>(const Geometry&, const DeviceOps*, FieldWork<double>&, int,
                                  const double*, bool, double, FinishMode, const double*,
                                  double*, double*, double, const ReduceSlots*, cudaStream_t,
-                                 const PhaseEvents*, bool);
+                                 const PhaseEvents*, int, const SideStream*);
 template void eval_field<float>(const Geometry&, const DeviceOps*, FieldWork<float>&, int,
                                 const float*, bool, double, FinishMode, const float*, float*,
                                 double*, double, const ReduceSlots*, cudaStream_t,
-                                const PhaseEvents*, bool);
+                                const PhaseEvents*, int, const SideStream*);
 
 // ---------------------------------------------------------------------------
 // Permutations

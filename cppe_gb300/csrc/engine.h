@@ -143,11 +143,29 @@ struct PhaseEvents {
   cudaEvent_t ev[6];
 };
 
+// A second stream for the far-field passes (P2M, M2M, M2L, L2L), which run
+// concurrently with the near-field pass and join before the finishing pass.
+struct SideStream {
+  cudaStream_t s     = nullptr;
+  cudaEvent_t fork   = nullptr;
+  cudaEvent_t join   = nullptr;
+  void create();
+  void destroy();
+};
+
+// Arithmetic of the near-field pass of an FP64 evaluation.
+enum NearMode {
+  NEAR_FP64     = 0,  // native FP64 throughout
+  NEAR_FAST_EXP = 1,  // FP64, FP32 exponential where the damping argument is >= 20
+  NEAR_DD       = 2   // double-float on the FP32 pipe (dipole sources; others use FAST_EXP)
+};
+
 template <typename T>
 void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m, const T* src,
                 bool damp, double damping, FinishMode mode, const T* ainv6, T* out,
                 double* out64, double sign, const ReduceSlots* dot, cudaStream_t s,
-                const PhaseEvents* pe = nullptr, bool fast_exp = false);
+                const PhaseEvents* pe = nullptr, int near_mode = NEAR_FP64,
+                const SideStream* side = nullptr);
 
 // Permutation helpers (caller order <-> device order), all 3-vectors.
 void permute_in(const Geometry& g, const double* in_caller, double* out_perm, int ncomp,

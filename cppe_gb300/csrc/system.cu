@@ -170,6 +170,8 @@ System::~System() {
   if (stream) {
     cudaSetDevice(device);
     cudaStreamSynchronize(stream);
+    if (side.s) cudaStreamSynchronize(side.s);
+    side.destroy();
     cudaStreamDestroy(stream);
   }
   if (h_flags) cudaFreeHost(h_flags);
@@ -208,6 +210,7 @@ void System::init(int n_, const double* xyz, const double* alpha6, const int* ex
   device = o.device;
   CG_CUDA(cudaSetDevice(device));
   CG_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  side.create();
 
   // Coincident sites make the pair kernels singular (and the reference's tree
   // build recurse without end): reject them up front.
@@ -288,7 +291,8 @@ void System::phase_timings(int precision, int reps, double* ms) {
     } else {
       ReduceSlots rs = slots(S_PAP);
       eval_field<double>(geo, ops.get(), w64, 1, tmp_in.p, opt.damp != 0, opt.damping_factor,
-                         FINISH_APPLY, ainv64.p, tmp_out.p, nullptr, 1.0, &rs, stream, &pe);
+                         FINISH_APPLY, ainv64.p, tmp_out.p, nullptr, 1.0, &rs, stream, &pe,
+                         precision == 2 ? NEAR_DD : NEAR_FP64);
     }
     CG_CUDA(cudaEventSynchronize(pe.ev[5]));
     float t;
@@ -304,18 +308,18 @@ void System::phase_timings(int precision, int reps, double* ms) {
 
 ReduceSlots System::slots(int k) const { return ReduceSlots{partials.p, ticket.p, scal.p + k}; }
 
-void System::apply64(const double* in, double* out, bool with_dot, bool fast_exp) {
+void System::apply64(const double* in, double* out, bool with_dot, int near_mode) {
   ReduceSlots rs = slots(S_PAP);
   eval_field<double>(geo, ops.get(), w64, 1, in, opt.damp != 0, opt.damping_factor,
                      FINISH_APPLY, ainv64.p, out, nullptr, 1.0, with_dot ? &rs : nullptr,
-                     stream, nullptr, fast_exp);
+                     stream, nullptr, near_mode, &side);
 }
 
 void System::apply32(const float* in, float* out, bool with_dot) {
   ReduceSlots rs = slots(S_PAP);
   eval_field<float>(geo, ops.get(), w32, 1, in, opt.damp != 0, opt.damping_factor,
                     FINISH_APPLY, ainv32.p, out, nullptr, 1.0, with_dot ? &rs : nullptr,
-                    stream);
+                    stream, nullptr, NEAR_FP64, &side);
 }
 
 namespace {
@@ -475,7 +479,7 @@ int System::solve_mixed(bool zero_guess, double* hist_out, int hist_cap, int* it
       // x += d; r = F - B64 x: the residual recomputed with the FP64 operator
       k_accumulate<<<nb3, VB, 0, stream>>>(n3, x.p, d32.p);
       CG_LAUNCH();
-      apply64(x.p, Ap.p, false, true);
+      apply64(x.p, Ap.p, false, NEAR_DD);
       last.fp64_applies++;
       k_residual<<<nb3, VB, 0, stream>>>(n3, F.p, Ap.p, r.p, slots(S_RED), scal.p);
       CG_LAUNCH();

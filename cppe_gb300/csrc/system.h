@@ -33,6 +33,7 @@ struct System {
   cppe_gpu_options opt{};
   int device = 0;
   cudaStream_t stream = nullptr;
+  SideStream side;  // far-field passes, concurrent with the near field
   Geometry geo;
   std::unique_ptr<DeviceOps> ops;  // m = 1, p = order (FMM only)
   FieldWork<double> w64;
@@ -73,9 +74,9 @@ struct System {
   void init(int n, const double* xyz, const double* alpha6, const int* excl_ptr,
             const int* excl_idx, const cppe_gpu_options& o);
   // FP64 / FP32 operator on device-order vectors.
-  // fast_exp: FP32 exponential for damping arguments >= 20 (residuals of the
-  // mixed solver; the plain FP64 solver keeps the FP64 exponential)
-  void apply64(const double* in, double* out, bool with_dot, bool fast_exp = false);
+  // near_mode (NearMode): the plain FP64 solver keeps NEAR_FP64; the mixed
+  // solver's residuals use the double-float near field (NEAR_DD)
+  void apply64(const double* in, double* out, bool with_dot, int near_mode = NEAR_FP64);
   void apply32(const float* in, float* out, bool with_dot);
   // FP32 operator on FP64 device-order vectors (rounded in, widened out).
   void apply32_widen(const double* in, double* out);

@@ -10,6 +10,8 @@ preconditioner, and fall back to plain PCG if they do not converge.
 """
 from __future__ import annotations
 
+import os
+
 import numpy as np
 
 from . import capi
@@ -98,3 +100,33 @@ def load(path, device=0):
     model.params = d["params"]
     model.set_normalization(d["mean"], d["inv_std"])
     return model
+
+
+DEFAULT_MODEL = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data",
+                             "learned_water.npz")
+
+
+def main(argv=None):
+    """Trains the shipped model on the GPU: `python -m cppe_gb300.learned --out PATH`."""
+    import argparse
+    import time
+    ap = argparse.ArgumentParser(description=main.__doc__)
+    ap.add_argument("--out", default=DEFAULT_MODEL)
+    ap.add_argument("--snapshots", type=int, default=250)
+    ap.add_argument("--nrhs", type=int, default=8)
+    ap.add_argument("--steps", type=int, default=1500)
+    ap.add_argument("--seed", type=int, default=7)
+    ap.add_argument("--device", type=int, default=0)
+    a = ap.parse_args(argv)
+    t0 = time.time()
+    model, losses, rows = train_from_generators(n_snapshots=a.snapshots, nrhs=a.nrhs,
+                                                steps=a.steps, seed=a.seed, device=a.device)
+    os.makedirs(os.path.dirname(a.out) or ".", exist_ok=True)
+    save(model, a.out)
+    print(f"trained on {a.snapshots * a.nrhs} solves ({rows} site rows), loss "
+          f"{losses[:10].mean():.4g} -> {losses[-50:].mean():.4g}, {time.time() - t0:.1f} s; "
+          f"wrote {a.out}", flush=True)
+
+
+if __name__ == "__main__":
+    main()

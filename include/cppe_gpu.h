@@ -100,6 +100,10 @@ int cppe_gpu_bmatrix_apply(cppe_gpu_system* sys, const double* in, double* out);
 int cppe_gpu_bmatrix_apply_device(cppe_gpu_system* sys, const double* d_in, double* d_out);
 /* Same operator in FP32 arithmetic (inputs/outputs still FP64). */
 int cppe_gpu_bmatrix_apply_fp32(cppe_gpu_system* sys, const double* in, double* out);
+/* Same operator as the mixed solver evaluates its FP64 residuals: near-field
+ * pairs in double-float arithmetic on the FP32 pipe (about 1e-13 relative per
+ * pair), FMM passes and the finishing pass in FP64. */
+int cppe_gpu_bmatrix_apply_dd(cppe_gpu_system* sys, const double* in, double* out);
 int cppe_gpu_apply_diagonal(cppe_gpu_system* sys, const double* in, double* out);
 int cppe_gpu_apply_diagonal_inverse(cppe_gpu_system* sys, const double* in, double* out);
 /* Dense 3n x 3n B (row-major), and its inverse. */
@@ -226,8 +230,11 @@ int cppe_gpu_set_model(cppe_gpu_system* sys, cppe_gpu_mlp* m);
 int cppe_gpu_stream(cppe_gpu_system* sys, void** stream);
 /* Number of kernels this library has launched in this process. */
 int cppe_gpu_launch_count(long long* count);
-/* Average device time in ms of each phase over `reps` operator applies in the
- * given precision, bracketed by CUDA events on the system's stream:
+/* Average device time in ms of each phase over `reps` operator applies,
+ * bracketed by CUDA events on the system's stream, phases run one after the
+ * other; precision: CPPE_GPU_FP64, CPPE_GPU_MIXED (the FP32 operator of the
+ * inner solve) or 2 (the FP64 operator with the double-float near field of the
+ * mixed solver's residuals):
  * out_ms[0] near-field pair pass, [1] P2M+M2M, [2] M2L, [3] L2L,
  * [4] finishing pass (L2P, exclusions, alpha^-1, dot), [5] whole apply.
  * near_pairs: ordered site pairs of the near-field pass that the reference

@@ -158,6 +158,25 @@ def test_mixed_precision_solve(gpu, port, fmm):
     np.testing.assert_allclose(mumx, mu64, atol=1e-7)
 
 
+@pytest.mark.parametrize("fmm,damp", [(False, True), (True, True), (True, False)])
+def test_double_float_apply_matches_fp64(gpu, fmm, damp):
+    """The mixed solver's residual operator (double-float near field) equals
+    the FP64 operator to FP64-level accuracy."""
+    from cppe_gb300 import synthetic
+    b = synthetic.water_box(1500, seed=31)
+    s = cabi.System(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx,
+                    summation=cabi.FMM if fmm else cabi.DIRECT, damp=damp)
+    v = np.random.default_rng(5).normal(0, 0.1, size=3 * b.n)
+    a64 = s.apply(v)
+    add = s.apply(v, dd=True)
+    a32 = s.apply(v, fp32=True)
+    err_dd = np.linalg.norm(add - a64) / np.linalg.norm(a64)
+    err_32 = np.linalg.norm(a32 - a64) / np.linalg.norm(a64)
+    # DD pairs carry ~1e-13 relative error; sums with cancellation reach ~1e-12
+    assert err_dd < 5e-12, err_dd
+    assert err_dd < 1e-3 * err_32
+
+
 def test_fmm_solve_matches_oracle(gpu, port):
     from cppe_gb300 import synthetic
     b = synthetic.water_box(1500, seed=4)
