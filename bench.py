@@ -35,9 +35,10 @@ sys.path.insert(0, ROOT)
 
 CONFIGS = {
     # name: (waters, seed, summation, order, description)
-    "c0": (333, 0, "direct", 5, "999 sites, direct summation"),
-    "c1": (10000, 1, "fmm", 5, "30,000 sites, FMM order 5, theta 0.5, ncrit 64"),
-    "c2": (100000, 2, "fmm", 6, "300,000 sites, FMM order 6, theta 0.5, ncrit 64"),
+    "999-direct": (333, 0, "direct", 5, "999 sites, direct summation"),
+    "30k-fmm5": (10000, 1, "fmm", 5, "30,000 sites, FMM order 5, theta 0.5, ncrit 64"),
+    "300k-fmm6": (100000, 2, "fmm", 6, "300,000 sites, FMM order 6, theta 0.5, ncrit 64"),
+    "1m-fmm6": (333334, 4, "fmm", 6, "1,000,002 sites, FMM order 6, theta 0.5, ncrit 64"),
 }
 METRIC = "induced-dipole solve time to 1e-8 residual"
 FLOP_PER_PAIR = 45  # damped dipole pair, see include/cppe_gpu/work_model.h
@@ -309,6 +310,23 @@ def run_ours(args):
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{dev}")  # 256 MB
     ext = torch.cuda.ExternalStream(smx.stream())
     ext64 = torch.cuda.ExternalStream(s64.stream())
+    if args.solve_only:
+        # mixed solves only (with the model when given), e.g. for launch lists
+        if args.model and os.path.exists(args.model) and not args.no_learned:
+            from cppe_gb300 import learned
+            smx.set_model(learned.load(args.model, device=dev))
+        ts = []
+        for k in range(args.warmup + args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            t, _ = _event_time(ext, lambda: smx.solve_device(d_rhs.data_ptr(), d_mu.data_ptr(),
+                                                             make_guess=True))
+            if k >= args.warmup:
+                ts.append(t)
+        print(json.dumps({"solve_only": args.steps, "config": args.config, "ms": [t * 1e3 for t in ts],
+                          "stats": smx.stats(), "learned": smx._model is not None
+                          if hasattr(smx, "_model") else False}), flush=True)
+        return
 
     def timed_solve(sys_, stream):
         flush.fill_(1.0)
@@ -447,12 +465,14 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c1", choices=sorted(CONFIGS))
+    ap.add_argument("--config", default="30k-fmm5", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched section")
     ap.add_argument("--no-learned", action="store_true", help="skip the trained model")
     ap.add_argument("--model", default=os.path.join(ROOT, "cppe_gb300", "data",
                                                     "learned_water.npz"))
+    ap.add_argument("--solve-only", action="store_true",
+                    help="time the mixed solves only (no FP64, e2e or CPU legs)")
     ap.add_argument("--apply-only", type=int, default=0, metavar="K",
                     help="run K FP32 and K FP64 operator applies and print phase timings")
     args = ap.parse_args()

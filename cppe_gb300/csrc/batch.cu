@@ -119,7 +119,7 @@ void Geometry::combine(const std::vector<const Geometry*>& parts, int copies, Ge
   L.inv_perm.assign(L.n, -1);
   for (int k = 0; k < L.n; ++k) L.inv_perm[L.perm[k]] = k;
   out.level_start = L.level_start;
-  out.make_items();
+  out.make_schedules();
 }
 
 // ---------------------------------------------------------------------------

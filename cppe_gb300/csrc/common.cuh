@@ -195,7 +195,10 @@ __device__ __forceinline__ void block_sum(double (&v)[K], double* sh /* >= 32*K 
 }
 
 // Returns true in thread 0 of the last block; partials[b*K + k] hold the
-// per-block sums, and `out` receives the totals (in block order).
+// per-block sums, and `out` receives the totals.  The last block adds the
+// partials with all its threads (thread t takes blocks t, t + blockDim, ...,
+// then a block reduction): a fixed order, so the result does not depend on
+// which block finishes last.
 template <int K>
 __device__ __forceinline__ bool grid_sum_last(double (&v)[K], double* sh, double* partials,
                                               unsigned* ticket, double* out) {
@@ -210,14 +213,17 @@ __device__ __forceinline__ bool grid_sum_last(double (&v)[K], double* sh, double
   }
   __syncthreads();
   if (!last) return false;
-  if (threadIdx.x == 0) {
-    __threadfence();
+  __threadfence();
+  double s[K];
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-      double s = 0.0;
-      for (unsigned b = 0; b < gridDim.x; ++b) s += ((volatile double*)partials)[b * K + k];
-      out[k] = s;
-    }
+  for (int k = 0; k < K; ++k) s[k] = 0.0;
+  for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x)
+#pragma unroll
+    for (int k = 0; k < K; ++k) s[k] += __ldcg(partials + b * K + k);
+  block_sum<K>(s, sh);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) out[k] = s[k];
     *ticket = 0;
   }
   return threadIdx.x == 0;

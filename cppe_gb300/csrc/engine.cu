@@ -1,16 +1,20 @@
 // Field engine kernels: near-field pair sums (direct summation and FMM P2P),
-// the FMM passes (P2M, M2M, M2L, L2L, L2P) and the finishing pass.
+// the FMM passes and the finishing pass.
 //
 // Reference counterparts (maxscheurer/cppe, src/core/fmm/):
-//   k_p2p      evaluate_direct{,_damping} calculate.cc:262-300,
+//   k_p2p, k_p2p32_m1, k_p2p_dd
+//              evaluate_direct{,_damping} calculate.cc:262-300,
 //              evaluate_P2P_lazy + P2P_Cells{,_damping} calculate.cc:29-72,205-225
-//   k_p2m      evaluate_P2M  calculate.cc:129-157
-//   k_m2m      evaluate_M2M  calculate.cc:159-184
-//   k_m2l      evaluate_M2L_lazy calculate.cc:186-203
-//   k_l2l      evaluate_L2L  calculate.cc:227-243
-//   k_finish   evaluate_L2P  calculate.cc:245-260, the exclusion rule of
-//              P2P_Cells (calculate.cc:37), and BMatrix::apply's "+ alpha^-1 mu"
-//              (bmatrix.cc:39)
+//   k_p2m_tasks + k_msum
+//              evaluate_P2M + evaluate_M2M calculate.cc:129-184 (each cell's
+//              multipole formed directly from its subtree: the same moments
+//              the M2M shifts produce, without the level-by-level passes)
+//   k_m2l, k_m2l_m1_p5/p6 (m2l_fixed.cuh)
+//              evaluate_M2L_lazy calculate.cc:186-203
+//   k_finish   evaluate_L2L + evaluate_L2P calculate.cc:227-260 (L2P of every
+//              ancestor's M2L-only expansion in place of the L2L shifts), the
+//              exclusion rule of P2P_Cells (calculate.cc:37), and
+//              BMatrix::apply's "+ alpha^-1 mu" (bmatrix.cc:39)
 // Every output element is owned by exactly one thread (no atomics), so
 // results are bitwise reproducible run to run.
 #include <algorithm>
@@ -28,6 +32,11 @@ namespace cg {
 constexpr int P2P_BLOCK  = 128;
 constexpr int P2P_TILE   = 512;  // source sites staged in shared memory per tile
 constexpr int M2L_WARPS  = 4;
+constexpr int P2M_LEAF_SITES  = 128;  // sites staged per round of the leaf P2M
+constexpr int M2M_TASK_LEAVES = 8;    // leaf multipoles shifted per upward-pass task
+constexpr int M2L_CHUNK       = 64;   // sources of one target cell per M2L warp
+constexpr int PW = PMAX + 1;          // powers 0..PMAX of one coordinate
+constexpr int FINISH_BLOCK = 128;
 
 // ---------------------------------------------------------------------------
 // Table uploads
@@ -70,6 +79,8 @@ TreeView Geometry::view() const {
   v.is_leaf   = is_leaf.p, v.leaf_cell = leaf_cell.p, v.leaf_start = leaf_start.p;
   v.site_leaf = site_leaf.p, v.m2l_ptr = m2l_ptr.p, v.m2l_src = m2l_src.p;
   v.p2p_ptr = p2p_ptr.p, v.p2p_src = p2p_src.p;
+  v.cell_off = cell_off.p, v.cell_ref = cell_ref.p;
+  v.lanc_ptr = lanc_ptr.p, v.lanc_cell = lanc_cell.p;
   return v;
 }
 
@@ -212,13 +223,66 @@ void Geometry::prepare(int n_, const double* xyz, const double* s_damp, const in
   // algorithmic pairs: the ordered pairs the reference evaluates in its
   // near-field / direct loops (self pairs and excluded pairs are skipped there)
   alg_pairs = near_pairs - n - (long)cidx.size();
-  make_items();
+  make_schedules();
 }
 
 // Cuts every target leaf's source list into pieces of about `W` pairs so that
 // blocks get similar work, and orders the pieces largest first.
-void Geometry::make_items() {
+void Geometry::make_schedules() {
   const TreeLayout& L = layout;
+  // ---- FMM upward / downward schedules
+  h_p2m_tasks.clear(), h_task_leaf.clear(), h_lanc_cell.clear();
+  h_cell_task_ptr.assign(L.ncells + 1, 0);
+  h_lanc_ptr.assign(L.nleaves + 1, 0);
+  h_cell_ref.assign(L.ncells, 0);
+  h_cell_off.assign(L.ncells, make_float4(0.f, 0.f, 0.f, 0.f));
+  if (fmm && L.ncells > 0) {
+    std::vector<char> need_m(L.ncells, 0), has_l(L.ncells, 0);
+    for (int c = 0; c < L.ncells; ++c) {
+      has_l[c] = L.m2l_ptr[c + 1] > L.m2l_ptr[c];
+      for (int q = L.m2l_ptr[c]; q < L.m2l_ptr[c + 1]; ++q) need_m[L.m2l_src[q]] = 1;
+    }
+    std::vector<std::vector<int>> sub(L.ncells);  // subtree leaves of the cells needing M
+    std::vector<int> ref(L.ncells, -1);
+    for (int a = 0; a < L.nleaves; ++a) {
+      for (int c = L.leaf_cell[a]; c >= 0; c = L.parent[c]) {
+        if (need_m[c]) sub[c].push_back(a);
+        if (ref[c] < 0 && L.leaf_start[a + 1] > L.leaf_start[a]) ref[c] = L.leaf_start[a];
+        if (has_l[c]) h_lanc_cell.push_back(c);
+      }
+      h_lanc_ptr[a + 1] = (int)h_lanc_cell.size();
+    }
+    for (int c = 0; c < L.ncells; ++c) {
+      const int r    = std::max(0, ref[c]);
+      h_cell_ref[c]  = r;
+      const double* cc = &L.center[4 * (size_t)c];
+      h_cell_off[c] = make_float4((float)(cc[0] - h_pos64[r].x), (float)(cc[1] - h_pos64[r].y),
+                                  (float)(cc[2] - h_pos64[r].z), 0.f);
+      // non-leaf cells: tasks of <= M2M_TASK_LEAVES subtree leaves (leaf
+      // multipoles are formed by k_p2m_leaf)
+      if (!L.is_leaf[c]) {
+        for (size_t k0 = 0; k0 < sub[c].size(); k0 += M2M_TASK_LEAVES) {
+          const size_t k1 = std::min(sub[c].size(), k0 + M2M_TASK_LEAVES);
+          const int first = (int)h_task_leaf.size();
+          for (size_t k = k0; k < k1; ++k) h_task_leaf.push_back(sub[c][k]);
+          h_p2m_tasks.push_back(make_int4(c, first, (int)h_task_leaf.size(), 0));
+        }
+      }
+      h_cell_task_ptr[c + 1] = (int)h_p2m_tasks.size();
+    }
+  }
+  if (h_task_leaf.empty()) h_task_leaf.push_back(0);
+  // M2L chunks: at most M2L_CHUNK sources of one target cell each
+  h_m2l_chunks.clear();
+  h_cell_chunk_ptr.assign(L.ncells + 1, 0);
+  if (fmm)
+    for (int c = 0; c < L.ncells; ++c) {
+      for (int q = L.m2l_ptr[c]; q < L.m2l_ptr[c + 1]; q += M2L_CHUNK)
+        h_m2l_chunks.push_back(make_int4(c, q, std::min(q + M2L_CHUNK, L.m2l_ptr[c + 1]), 0));
+      h_cell_chunk_ptr[c + 1] = (int)h_m2l_chunks.size();
+    }
+  if (h_lanc_cell.empty()) h_lanc_cell.push_back(0);
+  // ---- near-field work items
   long total          = 0;
   for (int a = 0; a < L.nleaves; ++a) {
     const long na = L.leaf_start[a + 1] - L.leaf_start[a];
@@ -260,8 +324,25 @@ void Geometry::make_items() {
 }
 
 void Geometry::upload(cudaStream_t s) {
+  {
+    std::vector<float2> tab(DD_EXP_TAB);
+    for (int k = 0; k < DD_EXP_TAB; ++k) {
+      const double e = std::exp(-0.0625 * k);
+      tab[k]         = make_float2((float)e, (float)(e - (double)(float)e));
+    }
+    dd_exp.upload(tab, s);
+  }
   items.upload(h_items, s);
   leaf_nslot.upload(h_leaf_nslot, s);
+  if (!h_p2m_tasks.empty()) p2m_tasks.upload(h_p2m_tasks, s);
+  task_leaf.upload(h_task_leaf, s);
+  if (!h_m2l_chunks.empty()) m2l_chunks.upload(h_m2l_chunks, s);
+  cell_chunk_ptr.upload(h_cell_chunk_ptr, s);
+  cell_task_ptr.upload(h_cell_task_ptr, s);
+  lanc_ptr.upload(h_lanc_ptr, s);
+  lanc_cell.upload(h_lanc_cell, s);
+  cell_ref.upload(h_cell_ref.empty() ? std::vector<int>{0} : h_cell_ref, s);
+  cell_off.upload(h_cell_off.empty() ? std::vector<float4>{float4{}} : h_cell_off, s);
   const TreeLayout& L = layout;
   center.upload(L.center, s);
   parent.upload(L.parent, s);
@@ -523,36 +604,77 @@ __global__ void __launch_bounds__(P2P_BLOCK)
 
 // ---------------------------------------------------------------------------
 // Near field, FP32, dipole sources: the inner pass of the mixed solver.
-// Positions are taken relative to the first site of the target leaf once per
-// staged source (hi/lo differences, ~FP32 accuracy of the relative vector),
-// so a pair costs one subtraction per component; the v < 50 cut of the FP64
-// path is not needed (expf underflows to 0 there).  Sources are staged as
-// float4 {x, y, z, s} and {mu_x, mu_y, mu_z, -}: two shared loads feed the
-// two targets of a thread.
+// Each thread evaluates two targets of the leaf against one staged source
+// per step with packed FP32x2 arithmetic (__ffma2_rn / __fmul2_rn /
+// __fadd2_rn, sm_100 and later): the two targets occupy the two halves of
+// every float2, and the source is staged pre-broadcast ({x, x, y, y} ...), so
+// a pair costs about half the issue slots of scalar code.
+//  - Positions are relative to the first site of the target leaf, formed once
+//    per staged source from the hi/lo coordinates; separations are taken as
+//    source - target (the dipole field is even in r).
+//  - Damped: 1/R is capped at 1e4 (real pairs have R > 1e-4 bohr), which
+//    turns the self pair (R = 0, v = 0, f_E = f_T = 0) into an exact zero
+//    without a branch; sources without a damping partner (s = 0) are staged
+//    with s = 1e15, i.e. e^-v = 0 and f = 1.
+//  - Undamped: the self pair is removed by a select on R^2 > 0.
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+struct Src2 {
+  float4 xy;  // x, x, y, y
+  float4 zs;  // z, z, s, s
+  float4 mxy; // mx, mx, my, my
+  float2 mz;  // mz, mz
+};
+
 template <bool DAMP>
-__device__ __forceinline__ void f32_pair_m1(const float4& ti, float ai, const float4& sj,
-                                            const float4& mu, float& fx, float& fy, float& fz) {
-  const float x = ti.x - sj.x, y = ti.y - sj.y, z = ti.z - sj.z;
-  const float r2 = fmaf(x, x, fmaf(y, y, z * z));
-  const float ir = r2 > 0.f ? rsqrtf(r2) : 0.f;
-  const float ir2 = ir * ir;
-  const float ir3 = ir2 * ir;
-  float A = ir3, B = 3.f * ir3 * ir2;  // G1 = -A, G2 = B
+__device__ __forceinline__ void f32x2_pair_m1(const float2& nX, const float2& nY,
+                                              const float2& nZ, const float2& AI,
+                                              const Src2& q, float2& FX, float2& FY,
+                                              float2& FZ) {
+  const float2 x  = __fadd2_rn(make_float2(q.xy.x, q.xy.y), nX);
+  const float2 y  = __fadd2_rn(make_float2(q.xy.z, q.xy.w), nY);
+  const float2 z  = __fadd2_rn(make_float2(q.zs.x, q.zs.y), nZ);
+  const float2 r2 = __ffma2_rn(x, x, __ffma2_rn(y, y, __fmul2_rn(z, z)));
+  float2 ir;
   if (DAMP) {
-    const float a = ai * sj.w;
-    if (a > 0.f) {
-      const float v  = a * (r2 * ir);
-      const float e  = __expf(-v);
-      const float fE = fmaf(-fmaf(v, fmaf(v, 0.5f, 1.f), 1.f), e, 1.f);
-      const float fT = fmaf(-(v * v) * (v * (1.f / 6.f)), e, fE);
-      A *= fE, B *= fT;
-    }
+    ir.x = fminf(rsqrtf(r2.x), 1e4f);
+    ir.y = fminf(rsqrtf(r2.y), 1e4f);
+  } else {
+    ir.x = r2.x > 0.f ? rsqrtf(r2.x) : 0.f;
+    ir.y = r2.y > 0.f ? rsqrtf(r2.y) : 0.f;
   }
-  const float C = (mu.x * x + mu.y * y + mu.z * z) * B;
-  fx = fmaf(mu.x, A, fmaf(-x, C, fx));
-  fy = fmaf(mu.y, A, fmaf(-y, C, fy));
-  fz = fmaf(mu.z, A, fmaf(-z, C, fz));
+  const float2 ir2 = __fmul2_rn(ir, ir);
+  const float2 ir3 = __fmul2_rn(ir2, ir);
+  const float2 ir5 = __fmul2_rn(ir3, ir2);
+  float2 A, Bn;  // field = mu A - r (mu.r) B, Bn = -B
+  if (DAMP) {
+    const float2 a  = __fmul2_rn(AI, make_float2(q.zs.z, q.zs.w));
+    const float2 v  = __fmul2_rn(a, __fmul2_rn(r2, ir));
+    const float2 t  = __fmul2_rn(v, f2(-1.4426950408889634f));
+    const float2 e  = make_float2(ex2_approx(t.x), ex2_approx(t.y));
+    const float2 p  = __ffma2_rn(v, __ffma2_rn(v, f2(0.5f), f2(1.f)), f2(1.f));
+    const float2 d1 = __fmul2_rn(p, e);  // 1 - f_E
+    const float2 w  = __fmul2_rn(__fmul2_rn(__fmul2_rn(v, v), f2(1.f / 6.f)), v);
+    const float2 d2 = __ffma2_rn(w, e, d1);  // 1 - f_T
+    A  = __fmul2_rn(ir3, __ffma2_rn(d1, f2(-1.f), f2(1.f)));
+    Bn = __fmul2_rn(ir5, __ffma2_rn(d2, f2(3.f), f2(-3.f)));
+  } else {
+    A  = ir3;
+    Bn = __fmul2_rn(ir5, f2(-3.f));
+  }
+  const float2 mx = make_float2(q.mxy.x, q.mxy.y), my = make_float2(q.mxy.z, q.mxy.w);
+  const float2 mz = q.mz;
+  const float2 md = __ffma2_rn(mx, x, __ffma2_rn(my, y, __fmul2_rn(mz, z)));
+  const float2 nC = __fmul2_rn(md, Bn);
+  FX = __ffma2_rn(x, nC, __ffma2_rn(mx, A, FX));
+  FY = __ffma2_rn(y, nC, __ffma2_rn(my, A, FY));
+  FZ = __ffma2_rn(z, nC, __ffma2_rn(mz, A, FZ));
 }
 
 template <bool DAMP>
@@ -561,8 +683,7 @@ __global__ void __launch_bounds__(P2P_BLOCK)
                  const int* __restrict__ p2p_src, const float4* __restrict__ hi,
                  const float4* __restrict__ lo, const float* __restrict__ src, float damping,
                  float* __restrict__ Fnear) {
-  __shared__ float4 s_pos[P2P_TILE];
-  __shared__ float4 s_mu[P2P_TILE];
+  __shared__ Src2 s_src[P2P_TILE];
   __shared__ TilePlan s_plan;
   __shared__ float s_red[P2P_BLOCK * 6];
 
@@ -573,7 +694,7 @@ __global__ void __launch_bounds__(P2P_BLOCK)
   auto rel = [&](int k) {
     const float4 h = hi[k], l = lo[k];
     return make_float4((h.x - oh.x) + (l.x - ol.x), (h.y - oh.y) + (l.y - ol.y),
-                       (h.z - oh.z) + (l.z - ol.z), h.w);
+                       (h.z - oh.z) + (l.z - ol.z), h.w > 0.f ? h.w : 1e15f);
   };
 
   for (int tb = 0; tb < nA; tb += 2 * P2P_BLOCK) {
@@ -585,7 +706,9 @@ __global__ void __launch_bounds__(P2P_BLOCK)
     const bool has1   = t + T2 < nT;
     const float4 me0 = rel(a0 + tb + t);
     const float4 me1 = rel(a0 + tb + (has1 ? t + T2 : t));
-    const float ai0 = damping * me0.w, ai1 = damping * me1.w;
+    const float2 nX = make_float2(-me0.x, -me1.x), nY = make_float2(-me0.y, -me1.y);
+    const float2 nZ = make_float2(-me0.z, -me1.z);
+    const float2 AI = make_float2(damping * me0.w, damping * me1.w);
     Comp3<float> acc0, acc1;
     if (threadIdx.x == 0) s_plan.cur = b0, s_plan.coff = 0;
     __syncthreads();
@@ -596,22 +719,25 @@ __global__ void __launch_bounds__(P2P_BLOCK)
       if (np == 0) break;
       const int total = s_plan.poff[np];
       for (int q = threadIdx.x; q < total; q += P2P_BLOCK) {
-        const int j = tile_site(s_plan, q);
-        s_pos[q]    = rel(j);
-        s_mu[q]     = make_float4(src[3 * (size_t)j], src[3 * (size_t)j + 1],
-                                  src[3 * (size_t)j + 2], 0.f);
+        const int j    = tile_site(s_plan, q);
+        const float4 r = rel(j);
+        const float mx = src[3 * (size_t)j], my = src[3 * (size_t)j + 1],
+                    mz = src[3 * (size_t)j + 2];
+        s_src[q].xy  = make_float4(r.x, r.x, r.y, r.y);
+        s_src[q].zs  = make_float4(r.z, r.z, r.w, r.w);
+        s_src[q].mxy = make_float4(mx, mx, my, my);
+        s_src[q].mz  = make_float2(mz, mz);
       }
       __syncthreads();
       if (active) {
-        float fx0 = 0, fy0 = 0, fz0 = 0, fx1 = 0, fy1 = 0, fz1 = 0;
+        float2 FX = f2(0.f), FY = f2(0.f), FZ = f2(0.f);
+#pragma unroll 4
         for (int jj = g; jj < total; jj += S) {
-          const float4 sj = s_pos[jj];
-          const float4 mu = s_mu[jj];
-          f32_pair_m1<DAMP>(me0, ai0, sj, mu, fx0, fy0, fz0);
-          f32_pair_m1<DAMP>(me1, ai1, sj, mu, fx1, fy1, fz1);
+          const Src2 q = s_src[jj];
+          f32x2_pair_m1<DAMP>(nX, nY, nZ, AI, q, FX, FY, FZ);
         }
-        acc0.add(fx0, fy0, fz0);
-        acc1.add(fx1, fy1, fz1);
+        acc0.add(FX.x, FY.x, FZ.x);
+        acc1.add(FX.y, FY.y, FZ.y);
       }
       __syncthreads();
     }
@@ -696,18 +822,15 @@ template <bool DAMP>
 __global__ void __launch_bounds__(P2P_BLOCK)
       k_p2p_dd(int n, const int* __restrict__ leaf_start, const int4* __restrict__ items,
                const int* __restrict__ p2p_src, PosArgs<float> pa,
-               const double* __restrict__ src, double damping, double* __restrict__ Fnear) {
+               const float2* __restrict__ src, const float2* __restrict__ etab,
+               double damping, double* __restrict__ Fnear) {
   __shared__ SiteRec<float> s_rec[P2P_TILE];
   __shared__ float s_mu[P2P_TILE * 6];
   __shared__ float2 s_etab[DD_EXP_TAB];
   __shared__ TilePlan s_plan;
   __shared__ double s_red[P2P_BLOCK * 6];
 
-  for (int k = threadIdx.x; k < DD_EXP_TAB; k += P2P_BLOCK) {
-    const double e = exp(-0.0625 * k);
-    const float h  = (float)e;
-    s_etab[k]      = make_float2(h, (float)(e - (double)h));
-  }
+  for (int k = threadIdx.x; k < DD_EXP_TAB; k += P2P_BLOCK) s_etab[k] = etab[k];
   const int4 it = items[blockIdx.x];
   const int A = it.x, b0 = it.y, b1 = it.z, slot = it.w;
   const int a0 = leaf_start[A], nA = leaf_start[A + 1] - a0;
@@ -738,8 +861,8 @@ __global__ void __launch_bounds__(P2P_BLOCK)
         s_rec[q]    = pa.load(j);
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          const dd m = dd_from(src[3 * (size_t)j + c]);
-          s_mu[q * 6 + c] = m.h, s_mu[q * 6 + 3 + c] = m.l;
+          const float2 m = src[3 * (size_t)j + c];
+          s_mu[q * 6 + c] = m.x, s_mu[q * 6 + 3 + c] = m.y;
         }
       }
       __syncthreads();
@@ -790,71 +913,184 @@ template <typename T>
 __device__ __forceinline__ T mono(const T* px, const T* py, const T* pz, int e) {
   return px[e & 15] * py[(e >> 4) & 15] * pz[e >> 8];
 }
-
-// P2M: thread per (leaf, M row); multipole of the leaf's sites about its centre.
+// Powers of an offset, kept in shared memory (x, y, z blocks of PW values)
+// so that the table-driven monomials index them without local memory.
 template <typename T>
-__global__ void k_p2m(TreeView tv, OpsView ov, const double4_32a* __restrict__ pos,
-                      const T* __restrict__ src, T* __restrict__ M) {
-  const int gid  = blockIdx.x * blockDim.x + threadIdx.x;
-  const int leaf = gid / ov.msize, row = gid - (gid / ov.msize) * ov.msize;
-  if (leaf >= tv.nleaves) return;
-  const int cell  = tv.leaf_cell[leaf];
-  const double4_32a c = tv.center[cell];
-  const int ns    = ncomp(ov.m);
-  const int t0 = ov.p2m_ptr[row], t1 = ov.p2m_ptr[row + 1];
-  T acc = 0;
-  for (int q = tv.leaf_start[leaf]; q < tv.leaf_start[leaf + 1]; ++q) {
-    const double4_32a x = pos[q];
-    T px[PMAX + 1], py[PMAX + 1], pz[PMAX + 1];
-    powers<T>((T)(c.x - x.x), ov.p, px);
-    powers<T>((T)(c.y - x.y), ov.p, py);
-    powers<T>((T)(c.z - x.z), ov.p, pz);
-    for (int t = t0; t < t1; ++t)
-      acc += mono(px, py, pz, ov.exps[ov.p2m_j[t]]) * src[(size_t)q * ns + ov.p2m_k[t]];
-  }
-  M[(size_t)cell * ov.msize + row] = acc;
+__device__ __forceinline__ void powers3(T x, T y, T z, int p, T* pw) {
+  powers<T>(x, p, pw);
+  powers<T>(y, p, pw + PW);
+  powers<T>(z, p, pw + 2 * PW);
+}
+template <typename T>
+__device__ __forceinline__ T mono3(const T* pw, int e) {
+  return pw[e & 15] * pw[PW + ((e >> 4) & 15)] * pw[2 * PW + (e >> 8)];
 }
 
-// M2M for the non-leaf cells of one level: thread per (cell, M row).
+// Offset c - x_q of site q from the expansion centre of cell c.
 template <typename T>
-__global__ void k_m2m(TreeView tv, OpsView ov, int c0, int c1, T* __restrict__ M) {
-  const int gid  = blockIdx.x * blockDim.x + threadIdx.x;
-  const int cell = c0 + gid / ov.msize, row = gid % ov.msize;
-  if (cell >= c1 || tv.is_leaf[cell]) return;
-  const double4_32a cp = tv.center[cell];
+struct CellPos;
+template <>
+struct CellPos<double> {
+  const double4_32a* center;
+  const double4_32a* pos;
+  __device__ void d(int c, int q, double& x, double& y, double& z) const {
+    const double4_32a cc = center[c], p = pos[q];
+    x = cc.x - p.x, y = cc.y - p.y, z = cc.z - p.z;
+  }
+};
+template <>
+struct CellPos<float> {
+  const float4* off;
+  const int* ref;
+  const float4* hi;
+  const float4* lo;
+  __device__ void d(int c, int q, float& x, float& y, float& z) const {
+    const float4 o = off[c];
+    const int r    = ref[c];
+    const float4 hr = hi[r], lr = lo[r], hq = hi[q], lq = lo[q];
+    x = o.x + ((hr.x - hq.x) + (lr.x - lq.x));
+    y = o.y + ((hr.y - hq.y) + (lr.y - lq.y));
+    z = o.z + ((hr.z - hq.z) + (lr.z - lq.z));
+  }
+};
+
+// Centre difference c_a - c_b (FP32 path: through the cells' reference sites).
+template <typename T>
+__device__ __forceinline__ void centre_diff(const TreeView& tv, const CellPos<T>& cp, int a, int b,
+                                            T& x, T& y, T& z);
+template <>
+__device__ __forceinline__ void centre_diff<double>(const TreeView& tv, const CellPos<double>& cp,
+                                                    int a, int b, double& x, double& y,
+                                                    double& z) {
+  const double4_32a ca = tv.center[a], cb = tv.center[b];
+  x = ca.x - cb.x, y = ca.y - cb.y, z = ca.z - cb.z;
+}
+template <>
+__device__ __forceinline__ void centre_diff<float>(const TreeView& tv, const CellPos<float>& cp,
+                                                   int a, int b, float& x, float& y, float& z) {
+  // c_a - c_b = (c_a - x_ref(a)) - (c_b - x_ref(b)) + (x_ref(a) - x_ref(b))
+  const float4 oa = cp.off[a], ob = cp.off[b];
+  const int ra = cp.ref[a], rb = cp.ref[b];
+  const float4 ha = cp.hi[ra], la = cp.lo[ra], hb = cp.hi[rb], lb = cp.lo[rb];
+  x = (oa.x - ob.x) + ((ha.x - hb.x) + (la.x - lb.x));
+  y = (oa.y - ob.y) + ((ha.y - hb.y) + (la.y - lb.y));
+  z = (oa.z - ob.z) + ((ha.z - hb.z) + (la.z - lb.z));
+}
+
+// Leaf multipoles (P2M): block per leaf, thread per multipole row; the powers
+// of each site's offset from the leaf centre and its moments are staged in
+// shared memory.
+template <typename T>
+__global__ void __launch_bounds__(128)
+      k_p2m_leaf(TreeView tv, OpsView ov, CellPos<T> cp, const T* __restrict__ src,
+                 T* __restrict__ M) {
+  __shared__ T s_pw[P2M_LEAF_SITES * 3 * PW];
+  __shared__ T s_src[P2M_LEAF_SITES * 6];
+  const int leaf = blockIdx.x, cell = tv.leaf_cell[leaf];
+  const int ns = ncomp(ov.m), row = threadIdx.x;
+  const int a0 = tv.leaf_start[leaf], a1 = tv.leaf_start[leaf + 1];
+  int t0 = 0, t1 = 0;
+  if (row < ov.msize) t0 = ov.p2m_ptr[row], t1 = ov.p2m_ptr[row + 1];
+  T acc = 0;
+  for (int b0 = a0; b0 < a1; b0 += P2M_LEAF_SITES) {
+    const int nb = min(P2M_LEAF_SITES, a1 - b0);
+    __syncthreads();
+    for (int t = threadIdx.x; t < nb; t += blockDim.x) {
+      T x, y, z;
+      cp.d(cell, b0 + t, x, y, z);
+      powers3<T>(x, y, z, ov.p, s_pw + 3 * PW * t);
+      for (int c = 0; c < ns; ++c) s_src[ns * t + c] = src[(size_t)(b0 + t) * ns + c];
+    }
+    __syncthreads();
+    if (row < ov.msize)
+      for (int q = 0; q < nb; ++q)
+        for (int t = t0; t < t1; ++t)
+          acc += mono3(s_pw + 3 * PW * q, ov.exps[ov.p2m_j[t]]) * s_src[ns * q + ov.p2m_k[t]];
+  }
+  if (row < ov.msize) M[(size_t)cell * ov.msize + row] = acc;
+}
+
+// Upward pass above the leaves, one block per task {cell, leaves}: thread
+// `row` adds the M2M shifts of the task's leaf multipoles straight to the
+// cell centre (the shift is exact, so going through the intermediate levels
+// changes nothing).  Partial expansions per task; k_msum adds a cell's tasks.
+template <typename T>
+__global__ void __launch_bounds__(128)
+      k_m2m_tasks(TreeView tv, OpsView ov, const int4* __restrict__ tasks,
+                  const int* __restrict__ task_leaf, CellPos<T> cp, const T* __restrict__ M,
+                  T* __restrict__ Mpart) {
+  __shared__ T s_pw[M2M_TASK_LEAVES * 3 * PW];
+  __shared__ int s_lc[M2M_TASK_LEAVES];
+  const int4 tk  = tasks[blockIdx.x];
+  const int cell = tk.x, row = threadIdx.x, nl = tk.z - tk.y;
+  if (threadIdx.x < nl) {
+    const int lc = tv.leaf_cell[task_leaf[tk.y + threadIdx.x]];
+    T x, y, z;
+    centre_diff<T>(tv, cp, cell, lc, x, y, z);
+    powers3<T>(x, y, z, ov.p, s_pw + 3 * PW * threadIdx.x);
+    s_lc[threadIdx.x] = lc;
+  }
+  __syncthreads();
+  if (row >= ov.msize) return;
   const int t0 = ov.m2m_ptr[row], t1 = ov.m2m_ptr[row + 1];
   T acc = 0;
-  for (int k = tv.child_ptr[cell]; k < tv.child_ptr[cell + 1]; ++k) {
-    const int ch     = tv.child_idx[k];
-    const double4_32a cc = tv.center[ch];
-    T px[PMAX + 1], py[PMAX + 1], pz[PMAX + 1];
-    powers<T>((T)(cp.x - cc.x), ov.p, px);
-    powers<T>((T)(cp.y - cc.y), ov.p, py);
-    powers<T>((T)(cp.z - cc.z), ov.p, pz);
-    const T* Mc = M + (size_t)ch * ov.msize;
-    for (int t = t0; t < t1; ++t) acc += mono(px, py, pz, ov.exps[ov.m2m_j[t]]) * Mc[ov.m2m_k[t]];
+  for (int k = 0; k < nl; ++k) {
+    const T* Mc = M + (size_t)s_lc[k] * ov.msize;
+    const T* pw = s_pw + 3 * PW * k;
+    for (int t = t0; t < t1; ++t) acc += mono3(pw, ov.exps[ov.m2m_j[t]]) * Mc[ov.m2m_k[t]];
   }
-  M[(size_t)cell * ov.msize + row] = acc;
+  Mpart[(size_t)blockIdx.x * ov.msize + row] = acc;
 }
 
-// L2L for the cells of one level (>= 1): thread per (cell, L row).
+// Downward pass: block per leaf, thread per local-expansion row; the M2L-only
+// expansions of the cells on the leaf's path to the root are shifted to the
+// leaf centre and summed (the leaf's own, at zero shift, included).
+constexpr int L2L_STAGE = 32;
 template <typename T>
-__global__ void k_l2l(TreeView tv, OpsView ov, int c0, int c1, T* __restrict__ L) {
-  const int gid  = blockIdx.x * blockDim.x + threadIdx.x;
-  const int cell = c0 + gid / ov.lsize, row = gid % ov.lsize;
-  if (cell >= c1) return;
-  const int par    = tv.parent[cell];
-  const double4_32a cc = tv.center[cell], cp = tv.center[par];
-  T px[PMAX + 1], py[PMAX + 1], pz[PMAX + 1];
+__global__ void __launch_bounds__(128)
+      k_l2l_leaf(TreeView tv, OpsView ov, CellPos<T> cp, const T* __restrict__ L,
+                 T* __restrict__ Lleaf) {
+  __shared__ T s_pw[L2L_STAGE * 3 * PW];
+  __shared__ int s_c[L2L_STAGE];
+  const int leaf = blockIdx.x, lc = tv.leaf_cell[leaf], row = threadIdx.x;
+  const int u0 = tv.lanc_ptr[leaf], u1 = tv.lanc_ptr[leaf + 1];
   const int q = ov.p - ov.m;
-  powers<T>((T)(cc.x - cp.x), q, px);
-  powers<T>((T)(cc.y - cp.y), q, py);
-  powers<T>((T)(cc.z - cp.z), q, pz);
-  const T* Lp = L + (size_t)par * ov.lsize;
-  T acc       = 0;
-  for (int t = ov.l2l_ptr[row]; t < ov.l2l_ptr[row + 1]; ++t)
-    acc += mono(px, py, pz, ov.exps[ov.l2l_j[t]]) * Lp[ov.l2l_k[t]];
-  L[(size_t)cell * ov.lsize + row] += acc;
+  int t0 = 0, t1 = 0;
+  if (row < ov.lsize) t0 = ov.l2l_ptr[row], t1 = ov.l2l_ptr[row + 1];
+  T acc = 0;
+  for (int b0 = u0; b0 < u1; b0 += L2L_STAGE) {
+    const int nb = min(L2L_STAGE, u1 - b0);
+    __syncthreads();
+    if (threadIdx.x < nb) {
+      const int c = tv.lanc_cell[b0 + threadIdx.x];
+      T x, y, z;
+      centre_diff<T>(tv, cp, lc, c, x, y, z);
+      powers3<T>(x, y, z, q, s_pw + 3 * PW * threadIdx.x);
+      s_c[threadIdx.x] = c;
+    }
+    __syncthreads();
+    if (row < ov.lsize)
+      for (int k = 0; k < nb; ++k) {
+        const T* Lc = L + (size_t)s_c[k] * ov.lsize;
+        const T* pw = s_pw + 3 * PW * k;
+        for (int t = t0; t < t1; ++t) acc += mono3(pw, ov.exps[ov.l2l_j[t]]) * Lc[ov.l2l_k[t]];
+      }
+  }
+  if (row < ov.lsize) Lleaf[(size_t)leaf * ov.lsize + row] = acc;
+}
+
+// M of every cell with upward tasks: the sum of its task partials in order.
+template <typename T>
+__global__ void k_msum(int ncells, int msize, const int* __restrict__ cell_task_ptr,
+                       const T* __restrict__ Mpart, T* __restrict__ M) {
+  const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int cell = (int)(gid / msize), row = (int)(gid % msize);
+  if (cell >= ncells) return;
+  const int t0 = cell_task_ptr[cell], t1 = cell_task_ptr[cell + 1];
+  if (t0 == t1) return;
+  T acc = 0;
+  for (int t = t0; t < t1; ++t) acc += Mpart[(size_t)t * msize + row];
+  M[(size_t)cell * msize + row] = acc;
 }
 
 // M2L: warp per target cell.  Per source cell the warp builds the derivative
@@ -950,16 +1186,17 @@ __global__ void __launch_bounds__(32 * M2L_WARPS)
 // adds alpha^-1 src (apply) or accumulates sign * F into an FP64 field.
 // ---------------------------------------------------------------------------
 template <typename T, int M, int MODE>
-__global__ void k_finish(int n, const int* __restrict__ leaf_nslot, const T* __restrict__ Fnear,
+__global__ void __launch_bounds__(FINISH_BLOCK) k_finish(int n, const int* __restrict__ leaf_nslot, const T* __restrict__ Fnear,
                          int use_fmm,
                          TreeView tv, OpsView ov, const T* __restrict__ L, PosArgs<T> pa,
-                         const double4_32a* __restrict__ pos64, const T* __restrict__ src,
+                         CellPos<T> cp, const T* __restrict__ src,
                          int damp, T damping, const int* __restrict__ corr_ptr,
                          const int* __restrict__ corr_idx, const T* __restrict__ ainv6,
                          T* __restrict__ out, double* __restrict__ out64, double sign,
                          ReduceSlots dot) {
   constexpr int NS = ncomp(M);
   __shared__ double sh[32];
+  __shared__ T s_pw[FINISH_BLOCK * 3 * PW];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double dv[1] = {0.0};
   if (i < n) {
@@ -970,17 +1207,20 @@ __global__ void k_finish(int n, const int* __restrict__ leaf_nslot, const T* __r
       f[0] += q[0], f[1] += q[1], f[2] += q[2];
     }
     if (use_fmm) {
-      const int cell  = tv.leaf_cell[tv.site_leaf[i]];
-      const double4_32a c = tv.center[cell];
-      const double4_32a x = pos64[i];
-      T px[PMAX + 1], py[PMAX + 1], pz[PMAX + 1];
-      const int q = ov.p - ov.m;
-      powers<T>((T)(x.x - c.x), q, px);
-      powers<T>((T)(x.y - c.y), q, py);
-      powers<T>((T)(x.z - c.z), q, pz);
-      const T* Lc = L + (size_t)cell * ov.lsize;
-      for (int u = 0; u < ov.nl2p; ++u)
-        f[ov.l2p_c[u]] -= mono(px, py, pz, ov.exps[ov.l2p_j[u]]) * Lc[ov.l2p_n[u]];
+      // L2P of the leaf's accumulated local expansion
+      const int leaf = tv.site_leaf[i];
+      T* pw          = s_pw + 3 * PW * threadIdx.x;
+      T dx, dy, dz;
+      cp.d(tv.leaf_cell[leaf], i, dx, dy, dz);
+      powers3<T>(-dx, -dy, -dz, ov.p - ov.m, pw);
+      const T* Lc = L + (size_t)leaf * ov.lsize;
+      for (int w = 0; w < ov.nl2p; ++w) {
+        const T v   = mono3(pw, ov.exps[ov.l2p_j[w]]) * Lc[ov.l2p_n[w]];
+        const int c = ov.l2p_c[w];  // (no dynamic index into f: keeps it in registers)
+        f[0] -= c == 0 ? v : T(0);
+        f[1] -= c == 1 ? v : T(0);
+        f[2] -= c == 2 ? v : T(0);
+      }
     }
     const int e0 = corr_ptr[i], e1 = corr_ptr[i + 1];
     if (e0 < e1) {
@@ -1032,6 +1272,16 @@ template <>
 PosArgs<float> pos_args<float>(const Geometry& g) {
   return PosArgs<float>{g.hi32.p, g.lo32.p};
 }
+template <typename T>
+static CellPos<T> cell_pos(const Geometry& g);
+template <>
+CellPos<double> cell_pos<double>(const Geometry& g) {
+  return CellPos<double>{reinterpret_cast<const double4_32a*>(g.center.p), g.pos64.p};
+}
+template <>
+CellPos<float> cell_pos<float>(const Geometry& g) {
+  return CellPos<float>{g.cell_off.p, g.cell_ref.p, g.hi32.p, g.lo32.p};
+}
 
 template <typename T, int M>
 static void launch_p2p(const Geometry& g, bool damp, bool fast, const T* src, T damping,
@@ -1061,7 +1311,11 @@ static void launch_p2p(const Geometry& g, bool damp, bool fast, const T* src, T 
 }
 
 void SideStream::create() {
-  CG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  // highest priority: the short far-field chain is scheduled ahead of the
+  // near-field pass's blocks instead of after them
+  int least = 0, greatest = 0;
+  CG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+  CG_CUDA(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, greatest));
   CG_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
   CG_CUDA(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
 }
@@ -1072,15 +1326,29 @@ void SideStream::destroy() {
   s = nullptr, fork = join = nullptr;
 }
 
+__global__ void k_split_dd(long n, const double* __restrict__ in, float2* __restrict__ out) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double v = in[i];
+  const float h  = (float)v;
+  out[i]         = make_float2(h, (float)(v - (double)h));
+}
+
 static void launch_p2p_dd(const Geometry& g, bool damp, const double* src, double damping,
-                          double* Fnear, cudaStream_t s) {
+                          FieldWork<double>& w, cudaStream_t s) {
+  const long n3 = 3L * g.n;
+  w.dd_src.alloc(std::max(1L, n3));
+  k_split_dd<<<(unsigned)((n3 + 255) / 256), 256, 0, s>>>(n3, src, w.dd_src.p);
+  CG_LAUNCH();
   const int grid = (int)g.h_items.size();
   if (damp)
     k_p2p_dd<true><<<grid, P2P_BLOCK, 0, s>>>(g.n, g.leaf_start.p, g.items.p, g.p2p_src.p,
-                                              pos_args<float>(g), src, damping, Fnear);
+                                              pos_args<float>(g), w.dd_src.p, g.dd_exp.p,
+                                              damping, w.Fnear.p);
   else
     k_p2p_dd<false><<<grid, P2P_BLOCK, 0, s>>>(g.n, g.leaf_start.p, g.items.p, g.p2p_src.p,
-                                               pos_args<float>(g), src, damping, Fnear);
+                                               pos_args<float>(g), w.dd_src.p, g.dd_exp.p,
+                                               damping, w.Fnear.p);
   CG_LAUNCH();
 }
 
@@ -1110,21 +1378,25 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
     w.M.alloc((size_t)tv.ncells * ov.msize);
     w.L.alloc((size_t)tv.ncells * ov.lsize);
     const int TB = 128;
-    {
-      long work = (long)tv.nleaves * ov.msize;
-      k_p2m<T><<<(unsigned)((work + TB - 1) / TB), TB, 0, fs>>>(tv, ov, g.pos64.p, src, w.M.p);
+    const int ntask = (int)g.h_p2m_tasks.size();
+    if (tv.nleaves > 0) {
+      k_p2m_leaf<T><<<tv.nleaves, TB, 0, fs>>>(tv, ov, cell_pos<T>(g), src, w.M.p);
       CG_LAUNCH();
     }
-    for (int l = (int)g.level_start.size() - 3; l >= 0; --l) {
-      const int c0 = g.level_start[l], c1 = g.level_start[l + 1];
-      long work    = (long)(c1 - c0) * ov.msize;
-      if (work == 0) continue;
-      k_m2m<T><<<(unsigned)((work + TB - 1) / TB), TB, 0, fs>>>(tv, ov, c0, c1, w.M.p);
+    if (ntask > 0) {
+      w.Mpart.alloc((size_t)ntask * ov.msize);
+      k_m2m_tasks<T><<<ntask, TB, 0, fs>>>(tv, ov, g.p2m_tasks.p, g.task_leaf.p, cell_pos<T>(g),
+                                          w.M.p, w.Mpart.p);
+      CG_LAUNCH();
+      const long work = (long)tv.ncells * ov.msize;
+      k_msum<T><<<(unsigned)((work + 255) / 256), 256, 0, fs>>>(
+            tv.ncells, ov.msize, g.cell_task_ptr.p, w.Mpart.p, w.M.p);
       CG_LAUNCH();
     }
     mark(1);
-    if (launch_m2l_fixed<T>(tv, ov.m, ov.p, w.M.p, w.L.p, fs)) {
-      CG_LAUNCH();
+    w.Lpart.alloc((size_t)std::max<size_t>(1, g.h_m2l_chunks.size()) * ov.lsize);
+    if (launch_m2l_fixed<T>(tv, ov.m, ov.p, g.m2l_chunks.p, (int)g.h_m2l_chunks.size(),
+                            g.cell_chunk_ptr.p, w.M.p, w.Lpart.p, w.L.p, ov.lsize, fs)) {
     } else {
       size_t smem = (size_t)(ov.nm2l_terms + 9 * ov.nt) * sizeof(int);
       smem        = (smem + 15) & ~(size_t)15;
@@ -1140,11 +1412,9 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
       CG_LAUNCH();
     }
     mark(2);
-    for (int l = 1; l < (int)g.level_start.size() - 1; ++l) {
-      const int c0 = g.level_start[l], c1 = g.level_start[l + 1];
-      long work    = (long)(c1 - c0) * ov.lsize;
-      if (work == 0) continue;
-      k_l2l<T><<<(unsigned)((work + TB - 1) / TB), TB, 0, fs>>>(tv, ov, c0, c1, w.L.p);
+    w.Lleaf.alloc((size_t)std::max(1, tv.nleaves) * ov.lsize);
+    if (tv.nleaves > 0) {
+      k_l2l_leaf<T><<<tv.nleaves, 128, 0, fs>>>(tv, ov, cell_pos<T>(g), w.L.p, w.Lleaf.p);
       CG_LAUNCH();
     }
     mark(3);
@@ -1158,7 +1428,7 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
   bool done       = false;
   if constexpr (std::is_same<T, double>::value) {
     if (near_mode == NEAR_DD && m == 1) {
-      launch_p2p_dd(g, damp, src, damping, w.Fnear.p, s);
+      launch_p2p_dd(g, damp, src, damping, w, s);
       done = true;
     }
   }
@@ -1168,14 +1438,14 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
   mark(4);
   if (fs != s) CG_CUDA(cudaStreamWaitEvent(s, side->join, 0));
 
-  const int FB = 256;
+  const int FB = FINISH_BLOCK;
   const int nb = (n + FB - 1) / FB;
   ReduceSlots rs{nullptr, nullptr, nullptr};
   if (dot) rs = *dot;
-  const T* Lp = g.fmm ? w.L.p : nullptr;
+  const T* Lp = g.fmm ? w.Lleaf.p : nullptr;
 #define CG_FINISH(TT, MM, MODE)                                                               \
   k_finish<TT, MM, MODE><<<nb, FB, 0, s>>>(n, g.leaf_nslot.p, w.Fnear.p, g.fmm ? 1 : 0, tv, ov, Lp, \
-                                           pos_args<TT>(g), g.pos64.p, src, damp ? 1 : 0,    \
+                                           pos_args<TT>(g), cell_pos<TT>(g), src, damp ? 1 : 0, \
                                            dampT, g.corr_ptr.p, g.corr_idx.p, ainv6, out,    \
                                            out64, sign, rs)
   if (mode == FINISH_APPLY) {

@@ -27,6 +27,13 @@ struct TreeView {
   const int* m2l_src;
   const int* p2p_ptr;
   const int* p2p_src;
+  // expansion centres relative to a reference site of each cell (FP32 path):
+  // c - x_q = cell_off[c] + (x_ref(c) - x_q), the last term from hi/lo
+  const float4* cell_off;
+  const int* cell_ref;
+  // per leaf: the cells on its path to the root that receive M2L terms
+  const int* lanc_ptr;
+  const int* lanc_cell;
 };
 
 struct OpsView {
@@ -74,6 +81,7 @@ struct Geometry {
   DBuf<int> perm, inv_perm;  // perm[k] = caller index of site k
   DBuf<double4_32a> pos64;
   DBuf<float4> hi32, lo32;
+  DBuf<float2> dd_exp;  // e^-(k/16), k = 0..320, as double-float pairs
   // pairs the reference skips (exclusions) that the near-field pass computed
   DBuf<int> corr_ptr, corr_idx;
   long near_pairs = 0;  // ordered pairs evaluated by the near-field pass
@@ -87,7 +95,29 @@ struct Geometry {
   std::vector<int> h_leaf_nslot;
   DBuf<int4> items;
   DBuf<int> leaf_nslot;
-  void make_items();
+
+  // Upward pass without level-by-level M2M: leaf multipoles (P2M), then the
+  // multipole of every non-leaf cell that is an M2L source from M2M shifts of
+  // its subtree's leaf multipoles straight to its centre, in tasks
+  // {cell, first, last} over task_leaf[] (<= 8 leaves per task);
+  // cell_task_ptr (CSR over cells) lists a cell's tasks, whose partial
+  // expansions are summed in order.  The downward pass shifts the M2L-only
+  // local expansions of the cells on each leaf's path to the root (lanc_*)
+  // straight to the leaf centre, in place of level-by-level L2L: both are
+  // exact re-expansions of the same polynomials, so the operator is unchanged.
+  std::vector<int4> h_p2m_tasks;
+  std::vector<int> h_task_leaf, h_cell_task_ptr, h_lanc_ptr, h_lanc_cell, h_cell_ref;
+  // M2L work: chunks {cell, first, last} of the cells' source lists (warp each)
+  std::vector<int4> h_m2l_chunks;
+  std::vector<int> h_cell_chunk_ptr;
+  DBuf<int4> m2l_chunks;
+  DBuf<int> cell_chunk_ptr;
+  std::vector<float4> h_cell_off;
+  DBuf<int4> p2m_tasks;
+  DBuf<int> task_leaf, cell_task_ptr, lanc_ptr, lanc_cell, cell_ref;
+  DBuf<float4> cell_off;
+  // builds both schedules from `layout` and h_pos64
+  void make_schedules();
 
   // host copies of the device arrays that are not part of `layout`
   std::vector<int> h_site_leaf, h_cptr, h_cidx;
@@ -117,7 +147,8 @@ struct Geometry {
 // Work buffers of one (geometry, m, p, precision) evaluation.
 template <typename T>
 struct FieldWork {
-  DBuf<T> M, L, Fnear;
+  DBuf<T> M, L, Fnear, Mpart, Lleaf, Lpart;
+  DBuf<float2> dd_src;  // double-float copy of the sources (double-float pass)
 };
 
 // Output modes of the finishing pass.

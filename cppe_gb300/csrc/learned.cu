@@ -7,17 +7,78 @@
 
 namespace cg {
 
-void NearGrid::build(const Geometry& g, const int* cep, const int* cei, cudaStream_t s) {
+// ---------------------------------------------------------------------------
+// Neighbour lists: sites are binned on the host into cubic cells of edge rc;
+// a thread per site scans the 27 cells around its own twice on the GPU (count,
+// then fill), with FP32 separations from the grid-snapped hi/lo coordinates.
+// ---------------------------------------------------------------------------
+struct CellGridView {
+  int dx, dy, dz;
+  const int* cell_start;
+  const int* cell_site;
+  const int* site_cell;
+  const int* excl_ptr;  // device-order exclusions
+  const int* excl_idx;
+};
+
+template <bool FILL>
+__global__ void k_near_build(int n, CellGridView cgv, const float4* __restrict__ hi,
+                             const float4* __restrict__ lo, float rc2, int damp, float damping,
+                             int* __restrict__ count, const int* __restrict__ ptr,
+                             int* __restrict__ idx, float* __restrict__ t6,
+                             float4* __restrict__ d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 hi_i = hi[i], lo_i = lo[i];
+  const int c  = cgv.site_cell[i];
+  const int cx = c % cgv.dx, cy = (c / cgv.dx) % cgv.dy, cz = c / (cgv.dx * cgv.dy);
+  const int e0 = cgv.excl_ptr[i], e1 = cgv.excl_ptr[i + 1];
+  const float ai = damping * hi_i.w;
+  int k = FILL ? ptr[i] : 0;
+  for (int zz = max(0, cz - 1); zz <= min(cgv.dz - 1, cz + 1); ++zz)
+    for (int yy = max(0, cy - 1); yy <= min(cgv.dy - 1, cy + 1); ++yy)
+      for (int xx = max(0, cx - 1); xx <= min(cgv.dx - 1, cx + 1); ++xx) {
+        const int cc = (zz * cgv.dy + yy) * cgv.dx + xx;
+        for (int q = cgv.cell_start[cc]; q < cgv.cell_start[cc + 1]; ++q) {
+          const int j = cgv.cell_site[q];
+          if (j == i) continue;
+          const float4 hj = hi[j], lj = lo[j];
+          const float x = (hj.x - hi_i.x) + (lj.x - lo_i.x);
+          const float y = (hj.y - hi_i.y) + (lj.y - lo_i.y);
+          const float z = (hj.z - hi_i.z) + (lj.z - lo_i.z);
+          const float r2 = x * x + y * y + z * z;
+          if (r2 >= rc2) continue;
+          // excluded partners stay in the list (the descriptors see them) with
+          // a zero tensor (the operator skips them)
+          bool excluded = false;
+          for (int e = e0; e < e1; ++e) excluded |= cgv.excl_idx[e] == j;
+          if (FILL) {
+            float G[2];
+            radial<float, 2>(r2, damp ? ai * hj.w : 0.f, G);
+            if (excluded) G[0] = G[1] = 0.f;
+            idx[k] = j;
+            float* t = t6 + 6 * (size_t)k;
+            t[0] = G[0] + G[1] * x * x, t[1] = G[1] * x * y, t[2] = G[1] * x * z;
+            t[3] = G[0] + G[1] * y * y, t[4] = G[1] * y * z, t[5] = G[0] + G[1] * z * z;
+            d[k] = make_float4(x, y, z, sqrtf(r2));
+          }
+          ++k;
+        }
+      }
+  if (!FILL) count[i] = k;
+}
+
+void NearList::build(const Geometry& g, const int* cep, const int* cei, int damp,
+                     double damping, cudaStream_t s) {
   n = g.n;
+  const double rc = LEARN_RC;
   double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
   for (int k = 0; k < n; ++k) {
     const double p[3] = {g.h_pos64[k].x, g.h_pos64[k].y, g.h_pos64[k].z};
     for (int c = 0; c < 3; ++c) lo[c] = std::min(lo[c], p[c]), hi[c] = std::max(hi[c], p[c]);
   }
-  for (int c = 0; c < 3; ++c) {
-    origin[c] = lo[c];
-    dims[c]   = std::max(1, (int)std::floor((hi[c] - lo[c]) / rc) + 1);
-  }
+  int dims[3];
+  for (int c = 0; c < 3; ++c) dims[c] = std::max(1, (int)std::floor((hi[c] - lo[c]) / rc) + 1);
   const long ncell = (long)dims[0] * dims[1] * dims[2];
   if (ncell > (1L << 28)) fail(CPPE_GPU_INVALID_ARG, "neighbour grid too large");
   std::vector<int> cnt(ncell + 1, 0), cell_of(n), sites(n);
@@ -25,7 +86,7 @@ void NearGrid::build(const Geometry& g, const int* cep, const int* cei, cudaStre
     const double p[3] = {g.h_pos64[k].x, g.h_pos64[k].y, g.h_pos64[k].z};
     int ci[3];
     for (int c = 0; c < 3; ++c)
-      ci[c] = std::min(dims[c] - 1, std::max(0, (int)std::floor((p[c] - origin[c]) / rc)));
+      ci[c] = std::min(dims[c] - 1, std::max(0, (int)std::floor((p[c] - lo[c]) / rc)));
     cell_of[k] = (ci[2] * dims[1] + ci[1]) * dims[0] + ci[0];
     cnt[cell_of[k] + 1]++;
   }
@@ -44,50 +105,49 @@ void NearGrid::build(const Geometry& g, const int* cep, const int* cei, cudaStre
     }
   }
   if (ei.empty()) ei.push_back(-1);
-  cell_start.upload(cnt, s);
-  cell_site.upload(sites, s);
-  excl_ptr.upload(ep, s);
-  excl_idx.upload(ei, s);
+  DBuf<int> d_cell_start, d_cell_site, d_site_cell, d_ep, d_ei, d_count;
+  d_cell_start.upload(cnt, s);
+  d_cell_site.upload(sites, s);
+  d_site_cell.upload(cell_of, s);
+  d_ep.upload(ep, s);
+  d_ei.upload(ei, s);
+  d_count.alloc(std::max(1, n));
+  const CellGridView cv{dims[0], dims[1], dims[2], d_cell_start.p, d_cell_site.p,
+                        d_site_cell.p, d_ep.p, d_ei.p};
+  const float rc2 = (float)(rc * rc);
+  const int nb    = (n + 127) / 128;
+  if (n > 0) {
+    k_near_build<false><<<nb, 128, 0, s>>>(n, cv, g.hi32.p, g.lo32.p, rc2, damp, (float)damping,
+                                           d_count.p, nullptr, nullptr, nullptr, nullptr);
+    CG_LAUNCH();
+  }
+  std::vector<int> c_h(n), p_h(n + 1, 0);
+  if (n > 0)
+    CG_CUDA(cudaMemcpyAsync(c_h.data(), d_count.p, n * sizeof(int), cudaMemcpyDeviceToHost, s));
+  CG_CUDA(cudaStreamSynchronize(s));
+  for (int i = 0; i < n; ++i) p_h[i + 1] = p_h[i] + c_h[i];
+  nnz = p_h[n];
+  ptr.upload(p_h, s);
+  idx.alloc(std::max(1L, nnz));
+  t6.alloc(6 * std::max(1L, nnz));
+  d.alloc(std::max(1L, nnz));
+  if (n > 0) {
+    k_near_build<true><<<nb, 128, 0, s>>>(n, cv, g.hi32.p, g.lo32.p, rc2, damp, (float)damping,
+                                          nullptr, ptr.p, idx.p, t6.p, d.p);
+    CG_LAUNCH();
+  }
+  CG_CUDA(cudaStreamSynchronize(s));  // the temporaries above are freed on return
 }
 
-NearGridView view(const NearGrid& g) {
-  return NearGridView{g.n,       g.rc,         g.origin[0],     g.origin[1],     g.origin[2],
-                      g.dims[0], g.dims[1],    g.dims[2],       g.cell_start.p,  g.cell_site.p,
-                      g.excl_ptr.p, g.excl_idx.p};
-}
-
-// Visits the neighbours j != i within rc of site i (27 grid cells).
-template <class F>
-__device__ __forceinline__ void for_neighbours(const NearGridView& ng, const double4_32a* pos,
-                                               int i, F&& f) {
-  const double4_32a pi = pos[i];
-  const int cx = min(ng.dx - 1, max(0, (int)floor((pi.x - ng.ox) / ng.rc)));
-  const int cy = min(ng.dy - 1, max(0, (int)floor((pi.y - ng.oy) / ng.rc)));
-  const int cz = min(ng.dz - 1, max(0, (int)floor((pi.z - ng.oz) / ng.rc)));
-  const double rc2 = ng.rc * ng.rc;
-  for (int zz = max(0, cz - 1); zz <= min(ng.dz - 1, cz + 1); ++zz)
-    for (int yy = max(0, cy - 1); yy <= min(ng.dy - 1, cy + 1); ++yy)
-      for (int xx = max(0, cx - 1); xx <= min(ng.dx - 1, cx + 1); ++xx) {
-        const int c = (zz * ng.dy + yy) * ng.dx + xx;
-        for (int q = ng.cell_start[c]; q < ng.cell_start[c + 1]; ++q) {
-          const int j = ng.cell_site[q];
-          if (j == i) continue;
-          const double4_32a pj = pos[j];
-          const double dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
-          const double r2 = dx * dx + dy * dy + dz * dz;
-          if (r2 >= rc2) continue;
-          f(j, (float)dx, (float)dy, (float)dz, pj.w);
-        }
-      }
-}
+NearListView view(const NearList& g) { return NearListView{g.n, g.ptr.p, g.idx.p, g.t6.p, g.d.p}; }
 
 __device__ __forceinline__ float aiso6(const float* a) { return (a[0] + a[3] + a[5]) / 3.f; }
 
-__global__ void k_features(NearGridView ng, const double4_32a* __restrict__ pos,
-                           const float* __restrict__ a6, const double* __restrict__ F,
-                           float* __restrict__ feats, float* __restrict__ v1) {
+__global__ void k_features(NearListView nl, const float* __restrict__ a6,
+                           const double* __restrict__ F, float* __restrict__ feats,
+                           float* __restrict__ v1) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= ng.n) return;
+  if (i >= nl.n) return;
   const float* ai = a6 + 6 * (size_t)i;
   const float f0 = (float)F[3 * i], f1 = (float)F[3 * i + 1], f2 = (float)F[3 * i + 2];
   v1[3 * i]     = ai[0] * f0 + ai[1] * f1 + ai[2] * f2;
@@ -99,65 +159,71 @@ __global__ void k_features(NearGridView ng, const double4_32a* __restrict__ pos,
   float f[Mlp::IN];
 #pragma unroll
   for (int k = 0; k < Mlp::IN; ++k) f[k] = 0.f;
-  const float rc = (float)ng.rc;
+  const float rc = (float)LEARN_RC;
   const float w16 = (rc - 1.f) / 15.f, w8 = (rc - 1.f) / 7.f;
-  int count = 0;
-  for_neighbours(ng, pos, i, [&](int j, float dx, float dy, float dz, double) {
-    const float r  = sqrtf(dx * dx + dy * dy + dz * dz);
-    const float fc = 0.5f * (__cosf(3.14159265f * r / rc) + 1.f);
-    const float aj = aiso6(a6 + 6 * (size_t)j) * 0.25f;
+  const int k0 = nl.ptr[i], k1 = nl.ptr[i + 1];
+  for (int k = k0; k < k1; ++k) {
+    const float4 dv = nl.d[k];
+    const int j     = nl.idx[k];
+    const float r   = dv.w;
+    const float fc  = 0.5f * (__cosf(3.14159265f * r / rc) + 1.f);
+    const float aj  = aiso6(a6 + 6 * (size_t)j) * 0.25f;
 #pragma unroll
-    for (int k = 0; k < 16; ++k) {
-      const float t = (r - (1.f + k * w16)) / w16;
+    for (int q = 0; q < 16; ++q) {
+      const float t = (r - (1.f + q * w16)) / w16;
       const float g = __expf(-t * t) * fc;
-      f[1 + k] += g;
-      f[17 + k] += aj * g;
+      f[1 + q] += g;
+      f[17 + q] += aj * g;
     }
-    const float ct = (ux * dx + uy * dy + uz * dz) / r;
+    const float ct = (ux * dv.x + uy * dv.y + uz * dv.z) / r;
     const float p2 = 1.5f * ct * ct - 0.5f;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      const float t = (r - (1.f + k * w8)) / w8;
+    for (int q = 0; q < 8; ++q) {
+      const float t = (r - (1.f + q * w8)) / w8;
       const float g = __expf(-t * t) * fc;
-      f[33 + k] += g * ct;
-      f[41 + k] += g * p2;
-      f[55 + k] += g * ct * aj;
+      f[33 + q] += g * ct;
+      f[41 + q] += g * p2;
+      f[55 + q] += g * ct * aj;
     }
-    ++count;
-  });
+  }
   f[0]  = aiso6(ai) * 0.25f - 1.f;
-  f[63] = count * 0.01f;
+  f[63] = (k1 - k0) * 0.01f;
   float* o = feats + (size_t)i * Mlp::IN;
 #pragma unroll
   for (int k = 0; k < Mlp::IN; ++k)
     if (k < 49 || k > 54) o[k] = f[k];
 }
 
+// out_i = alpha_i sum_j T_ij in_j: eight lanes per site stride over its list
+// (coalesced reads of the stored tensors), then a shuffle reduction.
 template <typename T>
-__global__ void k_near_T(NearGridView ng, const double4_32a* __restrict__ pos,
-                         const T* __restrict__ a6, int damp, T damping, const T* __restrict__ in,
+__global__ void k_near_T(NearListView nl, const T* __restrict__ a6, const T* __restrict__ in,
                          T* __restrict__ out) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= ng.n) return;
-  const T ai = damping * (T)pos[i].w;
-  const int e0 = ng.excl_ptr[i], e1 = ng.excl_ptr[i + 1];
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = gid >> 3, sub = gid & 7;
   T fx = 0, fy = 0, fz = 0;
-  for_neighbours(ng, pos, i, [&](int j, float, float, float, double sj) {
-    for (int e = e0; e < e1; ++e)
-      if (ng.excl_idx[e] == j) return;
-    const double4_32a pi = pos[i], pj = pos[j];
-    const T x = (T)(pi.x - pj.x), y = (T)(pi.y - pj.y), z = (T)(pi.z - pj.z);
-    T G[2];
-    radial<T, 2>(x * x + y * y + z * z, damp ? ai * (T)sj : T(0), G);
-    // field_m1 returns -T v; accumulate T v
-    T gx = 0, gy = 0, gz = 0;
-    field_m1(x, y, z, G, in[3 * j], in[3 * j + 1], in[3 * j + 2], gx, gy, gz);
-    fx -= gx, fy -= gy, fz -= gz;
-  });
-  const T* a = a6 + 6 * (size_t)i;
-  out[3 * i]     = a[0] * fx + a[1] * fy + a[2] * fz;
-  out[3 * i + 1] = a[1] * fx + a[3] * fy + a[4] * fz;
-  out[3 * i + 2] = a[2] * fx + a[4] * fy + a[5] * fz;
+  if (i < nl.n) {
+    for (int k = nl.ptr[i] + sub; k < nl.ptr[i + 1]; k += 8) {
+      const int j    = nl.idx[k];
+      const float* t = nl.t6 + 6 * (size_t)k;
+      const T vx = in[3 * (size_t)j], vy = in[3 * (size_t)j + 1], vz = in[3 * (size_t)j + 2];
+      fx += (T)t[0] * vx + (T)t[1] * vy + (T)t[2] * vz;
+      fy += (T)t[1] * vx + (T)t[3] * vy + (T)t[4] * vz;
+      fz += (T)t[2] * vx + (T)t[4] * vy + (T)t[5] * vz;
+    }
+  }
+#pragma unroll
+  for (int o = 4; o > 0; o >>= 1) {
+    fx += __shfl_down_sync(0xffffffffu, fx, o, 8);
+    fy += __shfl_down_sync(0xffffffffu, fy, o, 8);
+    fz += __shfl_down_sync(0xffffffffu, fz, o, 8);
+  }
+  if (i < nl.n && sub == 0) {
+    const T* a     = a6 + 6 * (size_t)i;
+    out[3 * i]     = a[0] * fx + a[1] * fy + a[2] * fz;
+    out[3 * i + 1] = a[1] * fx + a[3] * fy + a[4] * fz;
+    out[3 * i + 2] = a[2] * fx + a[4] * fy + a[5] * fz;
+  }
 }
 
 __global__ void k_basis_features(int n, const float* __restrict__ v1, const float* __restrict__ v2,
@@ -222,22 +288,22 @@ __global__ void k_precond_fix(int n, T* __restrict__ z, const T* __restrict__ w,
   }
 }
 
-void learned_features(const NearGridView& ng, const double4_32a* pos, const float* a6f,
-                      const double* F, float* feats, float* v1, cudaStream_t s) {
-  k_features<<<(ng.n + 127) / 128, 128, 0, s>>>(ng, pos, a6f, F, feats, v1);
+void learned_features(const NearListView& nl, const float* a6f, const double* F, float* feats,
+                      float* v1, cudaStream_t s) {
+  k_features<<<(nl.n + 127) / 128, 128, 0, s>>>(nl, a6f, F, feats, v1);
   CG_LAUNCH();
 }
 
 template <typename T>
-void near_T(const NearGridView& ng, const double4_32a* pos, const T* a6, int damp, double damping,
-            const T* in, T* out, cudaStream_t s) {
-  k_near_T<T><<<(ng.n + 127) / 128, 128, 0, s>>>(ng, pos, a6, damp, (T)damping, in, out);
+void near_T(const NearListView& nl, const T* a6, const T* in, T* out, cudaStream_t s) {
+  const long threads = 8L * nl.n;
+  k_near_T<T><<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(nl, a6, in, out);
   CG_LAUNCH();
 }
-template void near_T<float>(const NearGridView&, const double4_32a*, const float*, int, double,
-                            const float*, float*, cudaStream_t);
-template void near_T<double>(const NearGridView&, const double4_32a*, const double*, int, double,
-                             const double*, double*, cudaStream_t);
+template void near_T<float>(const NearListView&, const float*, const float*, float*,
+                            cudaStream_t);
+template void near_T<double>(const NearListView&, const double*, const double*, double*,
+                             cudaStream_t);
 
 void learned_basis_features(int n, const float* v1, const float* v2, const float* v3,
                             float* feats, cudaStream_t s) {

@@ -21,36 +21,40 @@ namespace cg {
 
 constexpr double LEARN_RC = 6.0 * 1.8897261246;  // 6 A in bohr
 
-struct NearGrid {
-  int n = 0;
-  double rc = LEARN_RC;
-  double origin[3] = {0, 0, 0};
-  int dims[3]      = {1, 1, 1};
-  DBuf<int> cell_start, cell_site, excl_ptr, excl_idx;
-  // sites in device order; exclusions given in caller indices
+// Neighbour lists within LEARN_RC of every site (device order, the site
+// itself removed), built once per system on the GPU, with the damped dipole
+// tensor of each pair stored as its six upper-triangle components:
+// T_ij = G1 I + G2 r r^T (r = r_i - r_j; G1, G2 the radial factors of the
+// operator), so that (T v)_i = sum_j T_ij v_j is the field at i of dipoles v;
+// excluded pairs are listed (for the descriptors) with T_ij = 0.  Entry k of site i (ptr[i] <= k < ptr[i+1]) holds idx[k] = j,
+// t6[6k..6k+5] and d[k] = (r_j - r_i, |r_j - r_i|).
+struct NearList {
+  int n    = 0;
+  long nnz = 0;
+  DBuf<int> ptr, idx;
+  DBuf<float> t6;
+  DBuf<float4> d;
+  // exclusions in caller indices (CSR, may be null)
   void build(const Geometry& g, const int* caller_excl_ptr, const int* caller_excl_idx,
-             cudaStream_t s);
+             int damp, double damping, cudaStream_t s);
 };
 
-struct NearGridView {
+struct NearListView {
   int n;
-  double rc, ox, oy, oz;
-  int dx, dy, dz;
-  const int* cell_start;
-  const int* cell_site;
-  const int* excl_ptr;
-  const int* excl_idx;
+  const int* ptr;
+  const int* idx;
+  const float* t6;
+  const float4* d;
 };
 
-NearGridView view(const NearGrid& g);
+NearListView view(const NearList& g);
 
 // descriptors (n x 64) and v1 (3n) from the field F (device order)
-void learned_features(const NearGridView& ng, const double4_32a* pos, const float* a6f,
-                      const double* F, float* feats, float* v1, cudaStream_t s);
-// out_i = alpha_i sum_{j near} T_ij in_j  (T damped with a_ij = damping s_i s_j)
+void learned_features(const NearListView& nl, const float* a6f, const double* F, float* feats,
+                      float* v1, cudaStream_t s);
+// out_i = alpha_i sum_{j near} T_ij in_j
 template <typename T>
-void near_T(const NearGridView& ng, const double4_32a* pos, const T* a6, int damp, double damping,
-            const T* in, T* out, cudaStream_t s);
+void near_T(const NearListView& nl, const T* a6, const T* in, T* out, cudaStream_t s);
 void learned_basis_features(int n, const float* v1, const float* v2, const float* v3,
                             float* feats, cudaStream_t s);
 void learned_guess(int n, const float* Y, const float* v1, const float* v2, const float* v3,

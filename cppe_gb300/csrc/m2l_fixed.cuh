@@ -20,15 +20,17 @@ namespace cg {
 #define CPPE_DEF_M2L_KERNEL(M, P, NAME, LS, MS)                                            \
   template <typename T>                                                                    \
   __global__ void __launch_bounds__(128)                                                   \
-        k_##NAME(TreeView tv, const T* __restrict__ Mexp, T* __restrict__ L) {             \
+        k_##NAME(TreeView tv, const int4* __restrict__ chunks, int nchunks,                \
+                 const T* __restrict__ Mexp, T* __restrict__ Lpart) {                      \
     const int lane = threadIdx.x & 31;                                                     \
-    const int A    = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;                         \
-    if (A >= tv.ncells) return;                                                            \
+    const int w    = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;                         \
+    if (w >= nchunks) return;                                                              \
+    const int4 ch = chunks[w];                                                             \
+    const int A   = ch.x;                                                                  \
     T acc[LS];                                                                             \
     _Pragma("unroll") for (int q = 0; q < LS; ++q) acc[q] = T(0);                          \
     const double4_32a cA = tv.center[A];                                                   \
-    const int s1         = tv.m2l_ptr[A + 1];                                              \
-    for (int idx = tv.m2l_ptr[A] + lane; idx < s1; idx += 32) {                            \
+    for (int idx = ch.y + lane; idx < ch.z; idx += 32) {                                   \
       const int B          = tv.m2l_src[idx];                                              \
       const double4_32a cB = tv.center[B];                                                 \
       NAME<T>((T)(cA.x - cB.x), (T)(cA.y - cB.y), (T)(cA.z - cB.z),                        \
@@ -40,26 +42,53 @@ namespace cg {
             __shfl_xor_sync(0xffffffffu, v, off);                                          \
       acc[q] = v;                                                                          \
     }                                                                                      \
-    T* LA = L + (size_t)A * (LS);                                                          \
+    T* LA = Lpart + (size_t)w * (LS);                                                      \
     _Pragma("unroll") for (int q = 0; q < LS; ++q) if ((q & 31) == lane) LA[q] = acc[q];   \
   }
 
 CPPE_M2L_GENERATED(CPPE_DEF_M2L_KERNEL)
 #undef CPPE_DEF_M2L_KERNEL
 
-// Launches the fixed-order kernel when one is compiled for (m, p); returns
-// false otherwise.
+// L of every cell: the sum of its chunk partials in order (0 without chunks).
 template <typename T>
-bool launch_m2l_fixed(const TreeView& tv, int m, int p, const T* Mexp, T* L, cudaStream_t s) {
-  const int blocks = (int)(((long)tv.ncells * 32 + 127) / 128);
-#define CPPE_LAUNCH_M2L(MM, PP, NAME, LS, MS)                 \
-  if (m == MM && p == PP) {                                   \
-    k_##NAME<T><<<blocks, 128, 0, s>>>(tv, Mexp, L);          \
-    return true;                                              \
+__global__ void k_lsum(int ncells, int lsize, const int* __restrict__ cell_chunk_ptr,
+                       const T* __restrict__ Lpart, T* __restrict__ L) {
+  const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int cell = (int)(gid / lsize), row = (int)(gid % lsize);
+  if (cell >= ncells) return;
+  T acc = 0;
+  for (int t = cell_chunk_ptr[cell]; t < cell_chunk_ptr[cell + 1]; ++t)
+    acc += Lpart[(size_t)t * lsize + row];
+  L[(size_t)cell * lsize + row] = acc;
+}
+
+// Launches the fixed-order kernel when one is compiled for (m, p): a warp per
+// chunk of at most M2L_CHUNK sources of one target cell (so that the GPU holds
+// several warps per cell), then the per-cell sums.  Returns false otherwise.
+template <typename T>
+bool launch_m2l_fixed(const TreeView& tv, int m, int p, const int4* chunks, int nchunks,
+                      const int* cell_chunk_ptr, const T* Mexp, T* Lpart, T* L, int lsize,
+                      cudaStream_t s) {
+  const int blocks = (int)(((long)std::max(1, nchunks) * 32 + 127) / 128);
+  bool ok = false;
+#define CPPE_LAUNCH_M2L(MM, PP, NAME, LS, MS)                              \
+  if (!ok && m == MM && p == PP) {                                         \
+    if (nchunks > 0) {                                                     \
+      k_##NAME<T><<<blocks, 128, 0, s>>>(tv, chunks, nchunks, Mexp, Lpart); \
+      CG_LAUNCH();                                                         \
+    }                                                                      \
+    ok = true;                                                             \
   }
   CPPE_M2L_GENERATED(CPPE_LAUNCH_M2L)
 #undef CPPE_LAUNCH_M2L
-  return false;
+  if (!ok) return false;
+  const long work = (long)tv.ncells * lsize;
+  if (work > 0) {
+    k_lsum<T><<<(unsigned)((work + 255) / 256), 256, 0, s>>>(tv.ncells, lsize, cell_chunk_ptr,
+                                                             Lpart, L);
+    CG_LAUNCH();
+  }
+  return true;
 }
 
 }  // namespace cg

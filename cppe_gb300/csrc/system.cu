@@ -570,9 +570,10 @@ __global__ void k_rows(int n, const float* __restrict__ v1, const float* __restr
 
 void System::learned_setup() {
   if (near) return;
-  near = std::make_unique<NearGrid>();
+  near = std::make_unique<NearList>();
   near->build(geo, excl_ptr_h.empty() ? nullptr : excl_ptr_h.data(),
-              excl_idx_h.empty() ? nullptr : excl_idx_h.data(), stream);
+              excl_idx_h.empty() ? nullptr : excl_idx_h.data(), opt.damp, opt.damping_factor,
+              stream);
   const size_t n3 = 3 * (size_t)n;
   lf_feats.alloc((size_t)n * Mlp::IN);
   for (auto* b : {&lf_v1, &lf_v2, &lf_v3, &lf_w32, &lf_rold32}) b->alloc(n3);
@@ -584,10 +585,10 @@ void System::learned_setup() {
 
 void System::learned_features_for_F() {
   learned_setup();
-  const NearGridView ng = view(*near);
-  learned_features(ng, geo.pos64.p, alpha32.p, F.p, lf_feats.p, lf_v1.p, stream);
-  near_T<float>(ng, geo.pos64.p, alpha32.p, opt.damp, opt.damping_factor, lf_v1.p, lf_v2.p, stream);
-  near_T<float>(ng, geo.pos64.p, alpha32.p, opt.damp, opt.damping_factor, lf_v2.p, lf_v3.p, stream);
+  const NearListView nl = view(*near);
+  learned_features(nl, alpha32.p, F.p, lf_feats.p, lf_v1.p, stream);
+  near_T<float>(nl, alpha32.p, lf_v1.p, lf_v2.p, stream);
+  near_T<float>(nl, alpha32.p, lf_v2.p, lf_v3.p, stream);
   learned_basis_features(n, lf_v1.p, lf_v2.p, lf_v3.p, lf_feats.p, stream);
 }
 
@@ -601,13 +602,13 @@ void System::learned_start() {
 
 template <typename T>
 void System::learned_precond(T* zv, const T* rv, T* pv, bool start) {
-  const NearGridView ng = view(*near);
+  const NearListView nl = view(*near);
   if constexpr (std::is_same<T, double>::value) {
-    near_T<double>(ng, geo.pos64.p, alpha64.p, opt.damp, opt.damping_factor, zv, lf_w64.p, stream);
+    near_T<double>(nl, alpha64.p, zv, lf_w64.p, stream);
     precond_fix<double>(n, zv, lf_w64.p, lf_c.p, rv, lf_rold64.p, pv, start, partials.p, ticket.p,
                         scal.p, flags.p, stream);
   } else {
-    near_T<float>(ng, geo.pos64.p, alpha32.p, opt.damp, opt.damping_factor, zv, lf_w32.p, stream);
+    near_T<float>(nl, alpha32.p, zv, lf_w32.p, stream);
     precond_fix<float>(n, zv, lf_w32.p, lf_c.p, rv, lf_rold32.p, pv, start, partials.p, ticket.p,
                        scal.p, flags.p, stream);
   }
@@ -630,8 +631,7 @@ void System::learned_rows(const double* mu_dev, std::vector<float>& feats, std::
   CG_LAUNCH();
   k_to_f32<<<(3 * n + VB - 1) / VB, VB, 0, stream>>>(3 * n, tmp_out.p, lf_w32.p);
   CG_LAUNCH();
-  near_T<float>(view(*near), geo.pos64.p, alpha32.p, opt.damp, opt.damping_factor, lf_w32.p,
-                lf_rold32.p, stream);
+  near_T<float>(view(*near), alpha32.p, lf_w32.p, lf_rold32.p, stream);
   DBuf<float> rows_d;
   rows_d.alloc((size_t)n * Mlp::TROW);
   k_rows<<<nb, VB, 0, stream>>>(n, lf_v1.p, lf_v2.p, lf_v3.p, mu_dev, lf_w32.p, lf_rold32.p, x.p,

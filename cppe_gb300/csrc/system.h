@@ -55,7 +55,7 @@ struct System {
   // learned initial guess + preconditioner correction (optional, not owned)
   Mlp* model = nullptr;
   bool use_model = false;  // set while a learned solve runs
-  std::unique_ptr<NearGrid> near;
+  std::unique_ptr<NearList> near;
   DBuf<float> lf_feats, lf_v1, lf_v2, lf_v3, lf_Y, lf_c, lf_w32, lf_rold32;
   DBuf<double> lf_w64, lf_rold64;
   void learned_setup();
