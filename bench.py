@@ -51,34 +51,82 @@ def dist_env():
 
 
 class ClockSampler:
-    """nvidia-smi clocks/throttle sampling during the timed region."""
+    """SM clock and clock-event reasons sampled during the timed region: NVML
+    through ctypes every ~2 ms when libnvidia-ml loads (read-only queries),
+    else nvidia-smi every 50 ms."""
 
+    # clock-event reason bits of NVML (nvmlClocksEventReason*)
+    BITS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+            0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
     Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
     def __init__(self, device):
         self.device = device
-        self.rows = []
+        self.rows = []  # (sm_mhz, max_mhz, reasons set)
         self.proc = None
+        self.nvml = None
+        self.stop = threading.Event()
+
+    def _nvml_open(self):
+        import ctypes
+        lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            return None
+        h = ctypes.c_void_p()
+        if lib.nvmlDeviceGetHandleByIndex_v2(self.device, ctypes.byref(h)) != 0:
+            return None
+        reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            getattr(lib, "nvmlDeviceGetCurrentClocksThrottleReasons")
+        return lib, h, reasons
+
+    def _nvml_loop(self):
+        import ctypes
+        lib, h, reasons = self.nvml
+        clk, mx, rs = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_ulonglong()
+        lib.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx))
+        while not self.stop.is_set():
+            if lib.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(clk)) == 0 and \
+                    reasons(h, ctypes.byref(rs)) == 0:
+                self.rows.append((float(clk.value), float(mx.value),
+                                  {n for bit, n in self.BITS.items() if rs.value & bit}))
+            time.sleep(0.002)
+
+    def _smi_loop(self):
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.proc.stdout:
+            r = [c.strip() for c in line.split(",")]
+            try:
+                self.rows.append((float(r[0]), float(r[1]),
+                                  {names[k] for k in range(4) if r[3 + k].lower() == "active"}))
+            except (ValueError, IndexError):
+                pass
 
     def __enter__(self):
         try:
+            self.nvml = self._nvml_open()
+        except (OSError, AttributeError):
+            self.nvml = None
+        if self.nvml:
+            self.t = threading.Thread(target=self._nvml_loop, daemon=True)
+            self.t.start()
+            return self
+        try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t = threading.Thread(target=self._smi_loop, daemon=True)
             self.t.start()
         except FileNotFoundError:
             self.proc = None
         return self
 
-    def _read(self):
-        for line in self.proc.stdout:
-            self.rows.append([c.strip() for c in line.split(",")])
-
     def __exit__(self, *a):
+        self.stop.set()
+        if self.nvml:
+            self.t.join(timeout=1)
         if self.proc:
             self.proc.terminate()
             try:
@@ -87,16 +135,20 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
-        if not self.rows:
+        rows = list(self.rows)
+        if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
-        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[k] for r in self.rows for k in range(4)
-                          if len(r) > 3 + k and r[3 + k].lower() == "active"})
-        return {"sm_mhz": statistics.median(sm) if sm else None,
-                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
-                "samples": len(self.rows)}
+        return {"sm_mhz": statistics.median(r[0] for r in rows),
+                "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": sorted(set().union(*(r[2] for r in rows))),
+                "samples": len(rows), "source": "nvml" if self.nvml else "nvidia-smi"}
+
+
+def workload_config(cfg, n):
+    """The workload as both arms report it."""
+    return {"workload": f"{cfg}: {CONFIGS[cfg][4]}, Thole damping 2.1304, 1 RHS (12 point "
+                        "charges + static multipole field), tol 1e-8 on ||F - B mu||_2 with "
+                        "the FP64 operator, PCG from alpha*F", "sites": n}
 
 
 def make_problem(cfg):
@@ -152,10 +204,8 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3,
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded water box)",
-        "config": {"workload": f"{args.config}: {CONFIGS[args.config][4]}, Thole damping, "
-                               "tol 1e-8, PCG from alpha*F", "sites": b.n, "parallelism":
-                               "host threads"},
+        "data": "synthetic (seeded water box, 12 point charges)",
+        "config": dict(workload_config(args.config, b.n), parallelism="host threads"),
         "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port",
                          "sample": f"{args.steps} full solves ({int(np.mean(its))} CG "
                                    "iterations each), OpenMP over all host threads"},
@@ -254,29 +304,81 @@ def batched_section(dev, steps, flush):
             "max_fp64_residual": worst, "setup_s": setup}
 
 
-def learned_section(smx, s64, d_rhs, d_mu, ext, ext64, flush, steps, model_path):
-    """The 30,000-site system with the trained model attached to the mixed solver."""
+def large_section(cfg, dev, flush, model_path=None, zero_guess=True):
+    """One larger system solved once per arithmetic: plain FP64 PCG (from
+    alpha*F and, optionally, from zero), mixed precision, and mixed precision
+    with the trained model.  Errors of the mixed solutions against the FP64
+    one: induced dipoles, polarization energy (-1/2 mu.E_ext), the induced
+    field B mu and the FP64 residual."""
     import torch
-    from cppe_gb300 import learned
-    if not os.path.exists(model_path):
+    from cppe_gb300 import capi, learned
+    t0 = time.perf_counter()
+    b, summation, order = make_problem(cfg)
+    rhs = static_rhs_gpu(b, summation, order)
+    setup = time.perf_counter() - t0
+    kw = dict(summation=capi.FMM, ncrit=64, order=order, theta=0.5, damp=True, thresh=1e-8,
+              device=dev)
+    d_rhs = torch.tensor(rhs, dtype=torch.float64, device=f"cuda:{dev}")
+    d_mu = torch.zeros_like(d_rhs)
+    E = b.external_field()
+    out = {"workload": f"{cfg}: {CONFIGS[cfg][4]}, Thole damping, tol 1e-8", "sites": b.n,
+           "setup_s": setup}
+
+    def timed(sys_, make_guess=True):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t, _ = _event_time(torch.cuda.ExternalStream(sys_.stream()),
+                           lambda: sys_.solve_device(d_rhs.data_ptr(), d_mu.data_ptr(),
+                                                     make_guess=make_guess))
+        return t, d_mu.cpu().numpy(), sys_.stats()
+
+    s64 = capi.System(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, precision=capi.FP64, **kw)
+    t64, mu64, st64 = timed(s64)
+    out["plain_fp64"] = {"s": t64, "iterations": st64["fp64_applies"] - 1}
+    if zero_guess:
+        tz, _, stz = timed(s64, make_guess=False)
+        out["plain_fp64_zero_guess"] = {"s": tz, "iterations": stz["fp64_applies"]}
+    Bmu64 = s64.apply(mu64)
+    smx = capi.System(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, precision=capi.MIXED, **kw)
+    timed(smx)  # warm-up (first-use allocations)
+    variants = [("mixed", None)]
+    if model_path and os.path.exists(model_path):
+        variants.append(("mixed_learned", learned.load(model_path, device=dev)))
+    for name, model in variants:
+        smx.set_model(model)
+        if model is not None:
+            timed(smx)
+        t, mu, st = timed(smx)
+        Bmu = s64.apply(mu)
+        out[name] = {
+            "s": t, "fp32_applies": st["fp32_applies"], "fp64_applies": st["fp64_applies"],
+            "speedup_vs_plain_fp64": t64 / t,
+            "error_vs_fp64": {
+                "mu_maxabs": float(np.abs(mu - mu64).max()),
+                "epol_hartree": float(abs(0.5 * (mu - mu64) @ E)),
+                "induced_field_rel": float(np.linalg.norm(Bmu - Bmu64) / np.linalg.norm(Bmu64)),
+                "fp64_residual": float(np.linalg.norm(rhs - Bmu))}}
+    smx.set_model(None)
+    smx.close()
+    s64.close()
+    return out
+
+
+def profiled_traffic(md_name):
+    """DRAM bytes (read + write) per launch from a committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", md_name)
+    if not os.path.exists(path):
         return None
-    model = learned.load(model_path, device=smx.device)
-    times = []
-    smx.set_model(model)
-    try:
-        smx.solve_device(d_rhs.data_ptr(), d_mu.data_ptr(), make_guess=True)  # warm-up
-        for _ in range(steps):
-            flush.fill_(1.0)
-            torch.cuda.synchronize()
-            t, _ = _event_time(ext, lambda: smx.solve_device(d_rhs.data_ptr(), d_mu.data_ptr(),
-                                                             make_guess=True))
-            times.append(t)
-        st = smx.stats()
-        mu = d_mu.cpu().numpy()
-    finally:
-        smx.set_model(None)
-    return {"value": float(np.mean(times)), "unit": "s", "stats": st,
-            "model": os.path.relpath(model_path, ROOT)}, mu
+    scale = {"byte": 1.0, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9}
+    tot, found = 0.0, 0
+    with open(path) as f:
+        for line in f:
+            for key in ("dram__bytes_read.sum", "dram__bytes_write.sum"):
+                if f"`{key}`" in line:
+                    cells = [c.strip() for c in line.strip().strip("|").split("|")]
+                    tot += float(cells[1]) * scale.get(cells[2], 1.0)
+                    found += 1
+    return tot if found == 2 else None
 
 
 def run_ours(args):
@@ -339,6 +441,12 @@ def run_ours(args):
         e1.synchronize()
         return e0.elapsed_time(e1) * 1e-3, it
 
+    # the method: mixed precision, with the trained model when one is shipped
+    model = None
+    if not args.no_learned and args.model and os.path.exists(args.model):
+        from cppe_gb300 import learned
+        model = learned.load(args.model, device=dev)
+    smx.set_model(model)
     for _ in range(args.warmup):
         timed_solve(smx, ext)
         timed_solve(s64, ext64)
@@ -351,40 +459,17 @@ def run_ours(args):
         for _ in range(args.steps):
             t, it = timed_solve(smx, ext)
             times.append(t)
-    torch.cuda.synchronize()
+        torch.cuda.synchronize()
     launches = capi.launch_count() - l0
     st = smx.stats()
-    mu_mx = d_mu.cpu().numpy()
-    t_mixed = float(np.mean(times))
+    mu_head = d_mu.cpu().numpy()
+    t_head = float(np.mean(times))
     if world > 1:
-        tt = torch.tensor([t_mixed], device=f"cuda:{dev}")
+        tt = torch.tensor([t_head], device=f"cuda:{dev}")
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_mixed = float(tt.item())
+        t_head = float(tt.item())
 
-    # the same solver with the trained model (learned guess + preconditioner)
-    lrn = learned_section(smx, s64, d_rhs, d_mu, ext, ext64, flush, args.steps,
-                          args.model) if not args.no_learned else None
-    mu_lrn = None
-    if lrn is not None:
-        lrn, mu_lrn = lrn
-    t_mixed_plain = t_mixed
-    if lrn is not None:
-        t_mixed = lrn["value"]
-        if world > 1:
-            tt = torch.tensor([t_mixed], device=f"cuda:{dev}")
-            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-            t_mixed = float(tt.item())
-
-    # plain FP64 GPU PCG on the same system
-    t64 = []
-    for _ in range(max(1, min(args.steps, 3))):
-        t, it64 = timed_solve(s64, ext64)
-        t64.append(t)
-    mu64 = d_mu.cpu().numpy()
-    st64 = s64.stats()
-    plain = float(np.mean(t64))
-
-    # end to end through the C ABI with host buffers
+    # end to end through the C ABI with host buffers (same method)
     rhs_h = np.ascontiguousarray(rhs)
     e2e = []
     for _ in range(args.steps):
@@ -394,6 +479,28 @@ def run_ours(args):
         mu_h, _, _, _ = smx.solve(rhs_h)
         e2e.append(time.perf_counter() - t0)
     e2e_v = float(np.mean(e2e))
+
+    # the mixed solver without the model, for the learned part's gain
+    without = None
+    if model is not None:
+        smx.set_model(None)
+        timed_solve(smx, ext)
+        tw = [timed_solve(smx, ext)[0] for _ in range(args.steps)]
+        without = {"s": float(np.mean(tw)), "stats": smx.stats()}
+    lrn = None
+    if model is not None:
+        lrn = {"with_model_s": t_head, "with_model_stats": st, "without_model_s": without["s"],
+               "without_model_stats": without["stats"],
+               "model": os.path.relpath(args.model, ROOT)}
+
+    # plain FP64 GPU PCG on the same system
+    t64 = []
+    for _ in range(max(1, min(args.steps, 3))):
+        t, it64 = timed_solve(s64, ext64)
+        t64.append(t)
+    mu64 = d_mu.cpu().numpy()
+    st64 = s64.stats()
+    plain = float(np.mean(t64))
 
     # roofline of the dominant kernel (FP32 near-field pair pass)
     tim32, alg_pairs, m2l_pairs = smx.kernel_timings(capi.MIXED, reps=5)
@@ -408,39 +515,46 @@ def run_ours(args):
                    "fp64": alg_pairs / (tim64["near"] * 1e-3)}
     pk, pk_kind = peaks()
 
-    mu_head = mu_lrn if mu_lrn is not None else mu_mx
     resid = float(np.linalg.norm(rhs - s64.apply(mu_head)))
     E = b.external_field()
     de = float(abs(0.5 * (mu_head - mu64) @ E))
     batched = batched_section(dev, 1, flush) if (not args.no_batched and world == 1) else None
+    large = {}
+    if not args.no_large and world == 1:
+        large["precision_300k"] = large_section("300k-fmm6", dev, flush, zero_guess=False)
+        large["learned_1m"] = large_section("1m-fmm6", dev, flush, model_path=args.model)
     if rank != 0:
         return
     cpu, _ = cpu_baseline_sample(b, rhs, summation, order) if not args.no_cpu else (None, None)
     total = world
     line = {
-        "metric": METRIC, "value": t_mixed, "unit": "s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_mixed * 1e3,
+        "metric": METRIC, "value": t_head, "unit": "s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_head * 1e3,
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic (seeded water box, 12 point charges)",
-        "config": {"workload": f"{args.config}: {CONFIGS[args.config][4]}, Thole damping "
-                               "2.1304, 1 RHS, tol 1e-8 (FP64 residual), PCG from alpha*F",
-                   "sites": b.n, "l2": "256 MB buffer written between timed steps",
-                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
-        "solves_per_s": total / t_mixed,
+        "config": dict(workload_config(args.config, b.n),
+                       l2="256 MB buffer written between timed steps",
+                       parallelism=f"replicas x{world}" if world > 1 else "1 GPU"),
+        "solves_per_s": total / t_head,
         "method": "mixed precision + learned guess/preconditioner" if lrn else
                   "mixed precision (no trained model found)",
-        "plain_fp64_s": plain, "speedup_vs_plain_fp64": plain / t_mixed,
-        "mixed_without_model_s": t_mixed_plain,
+        "plain_fp64_s": plain, "speedup_vs_plain_fp64": plain / t_head,
         "learned": lrn,
-        "iterations": {"mixed_fp32_applies": st["fp32_applies"],
-                       "mixed_fp64_applies": st["fp64_applies"],
+        "iterations": {"fp32_applies": st["fp32_applies"],
+                       "fp64_applies": st["fp64_applies"],
                        "plain_fp64_iterations": st64["fp64_applies"]},
         "parity": {"fp64_residual": resid, "mu_maxabs_vs_fp64": float(
             np.abs(mu_head - mu64).max()), "epol_diff_hartree": de},
         "batched": batched,
-        "roofline": {"bound": "fp32", "kernel": "k_p2p<float,1,damped> (near field)",
+        "large": large or None,
+        "roofline": {"bound": "fp32", "kernel": "k_p2p32_m1<true> (FP32 dipole near field)",
                      "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": achieved / fp32_peak, "traffic": None,
+                     "frac": achieved / fp32_peak,
+                     "traffic": profiled_traffic("k_p2p32_m1_30k_sites.md")
+                     if args.config == "30k-fmm5" else None,
+                     "traffic_note": "DRAM bytes per launch from the committed ncu capture of "
+                                     "this workload (profiles/k_p2p32_m1_30k_sites.md); the "
+                                     "kernel's working set is L2-resident",
                      "peak_kind": "measured FFMA probe (cppe_gpu_fma_peak), no FP32 CUDA-core "
                                   "figure in MEASURED_PEAKS.json",
                      "algorithmic": f"{alg_pairs} pairs x {FLOP_PER_PAIR} FLOP per launch"},
@@ -468,6 +582,8 @@ def main():
     ap.add_argument("--config", default="30k-fmm5", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched section")
+    ap.add_argument("--no-large", action="store_true",
+                    help="skip the 300k- and 1M-site sections")
     ap.add_argument("--no-learned", action="store_true", help="skip the trained model")
     ap.add_argument("--model", default=os.path.join(ROOT, "cppe_gb300", "data",
                                                     "learned_water.npz"))
