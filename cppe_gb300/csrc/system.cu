@@ -94,7 +94,7 @@ __global__ void k_cg_update(int n, const T* __restrict__ p, const T* __restrict_
     scal[S_RZOLD] = scal[S_RZ];
     scal[S_BETA]  = rs.out[1] / scal[S_RZ];
     scal[S_RZ]    = rs.out[1];
-    if (rn < thresh)
+    if (rn < (thresh < 0.0 ? scal[S_TOL] : thresh))
       flags[0] = 1;
     else if (it + 1 >= maxiter)
       flags[0] = 2;
@@ -170,6 +170,8 @@ System::~System() {
   if (stream) {
     cudaSetDevice(device);
     cudaStreamSynchronize(stream);
+    for (auto& e : inner_exec)
+      if (e) cudaGraphExecDestroy(e);
     if (side.s) cudaStreamSynchronize(side.s);
     side.destroy();
     cudaStreamDestroy(stream);
@@ -398,6 +400,90 @@ int System::solve_fp64(bool zero_guess, double* hist_out, int hist_cap, int* ite
   return h_flags[0] == 1 ? CPPE_GPU_OK : CPPE_GPU_NOT_CONVERGED;
 }
 
+// Continues the inner graph's while loop until the solve has stopped.
+__global__ void k_while_running(cudaGraphConditionalHandle h, const int* flags) {
+  cudaGraphSetConditional(h, flags[0] == 0 ? 1u : 0u);
+}
+
+// One inner FP32 PCG iteration (apply with p.Ap, update, optional learned
+// correction, new direction); every kernel is a no-op once flags[0] is set.
+void System::inner_iteration_fp32(int nb, int nb3) {
+  apply32(p32.p, Ap32.p, true);
+  k_cg_update<float><<<nb, VB, 0, stream>>>(n, p32.p, Ap32.p, alpha32.p, d32.p, r32.p, z32.p,
+                                            slots(S_RED), scal.p, flags.p, nullptr, -1.0,
+                                            std::max(1, opt.maxiter),
+                                            use_model ? lf_rold32.p : nullptr);
+  CG_LAUNCH();
+  if (use_model) learned_precond<float>(z32.p, r32.p, p32.p, false);
+  k_cg_dir<float><<<nb3, VB, 0, stream>>>(3 * n, z32.p, p32.p, scal.p, flags.p);
+  CG_LAUNCH();
+}
+
+// The inner loop as a CUDA graph with a conditional while node: the body is
+// one iteration captured from the stream (including the far-field side
+// stream's fork and join), repeated on the device until k_cg_update sets
+// flags[0] (converged, or the iteration limit).  Built once per system and
+// learned/plain variant, after the buffers it uses exist.  Where graph
+// construction is refused, the iterations are launched from the host.
+void System::run_inner_fp32(int nb, int nb3) {
+  const int v = use_model ? 1 : 0;
+  if (!inner_exec[v] && !inner_graph_failed) {
+    cudaGraph_t g = nullptr;
+    bool ok       = cudaGraphCreate(&g, 0) == cudaSuccess;
+    cudaGraphConditionalHandle h{};
+    cudaGraphNode_t node{};
+    cudaGraphNodeParams np{};
+    ok = ok && cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) ==
+                     cudaSuccess;
+    if (ok) {
+      np.type                 = cudaGraphNodeTypeConditional;
+      np.conditional.handle   = h;
+      np.conditional.type     = cudaGraphCondTypeWhile;
+      np.conditional.size     = 1;
+      ok = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np) == cudaSuccess;
+    }
+    if (ok) {
+      cudaGraph_t body = np.conditional.phGraph_out[0];
+      ok = cudaStreamBeginCaptureToGraph(stream, body, nullptr, nullptr, 0,
+                                         cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+      if (ok) {
+        const long long c0 = launch_counter();
+        try {
+          inner_iteration_fp32(nb, nb3);
+          k_while_running<<<1, 1, 0, stream>>>(h, flags.p);
+          CG_LAUNCH();
+        } catch (const Failure&) {
+          ok = false;
+        }
+        inner_body_launches[v] = launch_counter() - c0;
+        launch_counter()       = c0;
+        cudaGraph_t captured   = nullptr;
+        ok = (cudaStreamEndCapture(stream, &captured) == cudaSuccess) && ok;
+      }
+    }
+    if (ok) ok = cudaGraphInstantiate(&inner_exec[v], g, 0) == cudaSuccess;
+    if (g) cudaGraphDestroy(g);
+    if (!ok) {
+      cudaGetLastError();  // clear the refusal; fall back to host-launched iterations
+      if (inner_exec[v]) cudaGraphExecDestroy(inner_exec[v]);
+      inner_exec[v]      = nullptr;
+      inner_graph_failed = true;
+    }
+  }
+  if (inner_exec[v]) {
+    CG_CUDA(cudaGraphLaunch(inner_exec[v], stream));
+    CG_CUDA(cudaMemcpyAsync(h_flags, flags.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CG_CUDA(cudaStreamSynchronize(stream));
+    launch_counter() += inner_body_launches[v] * std::max(1, h_flags[1]);
+    return;
+  }
+  Poller poll(stream, flags.p, h_flags);
+  for (int k = 0; k < std::max(1, opt.maxiter); ++k) {
+    inner_iteration_fp32(nb, nb3);
+    if (poll.after_iteration()) break;
+  }
+}
+
 int System::solve_mixed(bool zero_guess, double* hist_out, int hist_cap, int* iters) {
   const int nb   = (n + VB - 1) / VB;
   const int n3   = 3 * n;
@@ -454,24 +540,16 @@ int System::solve_mixed(bool zero_guess, double* hist_out, int hist_cap, int* it
     }
     have_inner_start = false;
     const double tol = std::max(eta * rnorm, 0.25 * t);
-    Poller poll(stream, flags.p, h_flags);
-    for (int k = 0; k < std::max(1, opt.maxiter); ++k) {
-      apply32(p32.p, Ap32.p, true);
-      last.fp32_applies++;
-      k_cg_update<float><<<nb, VB, 0, stream>>>(n, p32.p, Ap32.p, alpha32.p, d32.p, r32.p,
-                                                z32.p, slots(S_RED), scal.p, flags.p, nullptr,
-                                                tol, std::max(1, opt.maxiter),
-                                                use_model ? lf_rold32.p : nullptr);
-      CG_LAUNCH();
-      if (use_model) learned_precond<float>(z32.p, r32.p, p32.p, false);
-      k_cg_dir<float><<<nb3, VB, 0, stream>>>(n3, z32.p, p32.p, scal.p, flags.p);
-      CG_LAUNCH();
-      if (poll.after_iteration()) break;
-    }
+    // the threshold of this inner solve goes to the device; the loop itself
+    // runs as one graph launch (device-side while loop)
+    h_scal[S_TOL] = tol;
+    CG_CUDA(cudaMemcpyAsync(scal.p + S_TOL, h_scal + S_TOL, sizeof(double),
+                            cudaMemcpyHostToDevice, stream));
+    run_inner_fp32(nb, nb3);
     CG_CUDA(cudaMemcpyAsync(h_flags, flags.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream));
     CG_CUDA(cudaStreamSynchronize(stream));
     total_inner += h_flags[1];
-    last.fp32_applies = std::min(last.fp32_applies, total_inner + (zero_guess ? 0 : 1));
+    last.fp32_applies += h_flags[1];
     // An FP32 update of the residual errs by ~1e-7 ||B d|| ~ 1e-7 ||r||; it is
     // used only on top of an exact residual small enough that this error is
     // below 1e-3 of the threshold.

@@ -87,6 +87,12 @@ struct System {
   // solves in device order: F holds the rhs, x the start vector
   int solve_fp64(bool zero_guess, double* hist_out, int hist_cap, int* iters);
   int solve_mixed(bool zero_guess, double* hist_out, int hist_cap, int* iters);
+  // inner FP32 PCG loop of the mixed solver (graph-launched when possible)
+  void inner_iteration_fp32(int nb, int nb3);
+  void run_inner_fp32(int nb, int nb3);
+  cudaGraphExec_t inner_exec[2] = {nullptr, nullptr};  // plain / learned body
+  long long inner_body_launches[2] = {0, 0};
+  bool inner_graph_failed = false;
   int solve_device(const double* d_rhs, const double* d_guess, int make_guess, double* d_mu,
                    int* iters, double* hist_out, int hist_cap);
 };
