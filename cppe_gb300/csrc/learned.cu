@@ -25,7 +25,7 @@ template <bool FILL>
 __global__ void k_near_build(int n, CellGridView cgv, const float4* __restrict__ hi,
                              const float4* __restrict__ lo, float rc2, int damp, float damping,
                              int* __restrict__ count, const int* __restrict__ ptr,
-                             int* __restrict__ idx, float* __restrict__ t6,
+                             int* __restrict__ idx, __half* __restrict__ t6,
                              float4* __restrict__ d) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -57,9 +57,10 @@ __global__ void k_near_build(int n, CellGridView cgv, const float4* __restrict__
             radial<float, 2>(r2, damp ? ai * hj.w : 0.f, G);
             if (excluded) G[0] = G[1] = 0.f;
             idx[k] = j;
-            float* t = t6 + 6 * (size_t)k;
-            t[0] = G[0] + G[1] * x * x, t[1] = G[1] * x * y, t[2] = G[1] * x * z;
-            t[3] = G[0] + G[1] * y * y, t[4] = G[1] * y * z, t[5] = G[0] + G[1] * z * z;
+            __half* t = t6 + 6 * (size_t)k;
+            t[0] = __float2half(G[0] + G[1] * x * x), t[1] = __float2half(G[1] * x * y);
+            t[2] = __float2half(G[1] * x * z), t[3] = __float2half(G[0] + G[1] * y * y);
+            t[4] = __float2half(G[1] * y * z), t[5] = __float2half(G[0] + G[1] * z * z);
             d[k] = make_float4(x, y, z, sqrtf(r2));
           }
           ++k;
@@ -143,16 +144,17 @@ NearListView view(const NearList& g) { return NearListView{g.n, g.ptr.p, g.idx.p
 
 __device__ __forceinline__ float aiso6(const float* a) { return (a[0] + a[3] + a[5]) / 3.f; }
 
+// Descriptors: eight lanes per site stride over its neighbour list and the
+// partial sums are reduced by shuffles.
 __global__ void k_features(NearListView nl, const float* __restrict__ a6,
                            const double* __restrict__ F, float* __restrict__ feats,
                            float* __restrict__ v1) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nl.n) return;
-  const float* ai = a6 + 6 * (size_t)i;
-  const float f0 = (float)F[3 * i], f1 = (float)F[3 * i + 1], f2 = (float)F[3 * i + 2];
-  v1[3 * i]     = ai[0] * f0 + ai[1] * f1 + ai[2] * f2;
-  v1[3 * i + 1] = ai[1] * f0 + ai[3] * f1 + ai[4] * f2;
-  v1[3 * i + 2] = ai[2] * f0 + ai[4] * f1 + ai[5] * f2;
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = gid >> 3, sub = gid & 7;
+  const bool ok = i < nl.n;
+  const int ii  = ok ? i : 0;
+  const float* ai = a6 + 6 * (size_t)ii;
+  const float f0 = (float)F[3 * ii], f1 = (float)F[3 * ii + 1], f2 = (float)F[3 * ii + 2];
   const float fn  = sqrtf(f0 * f0 + f1 * f1 + f2 * f2);
   const float ifn = fn > 0.f ? 1.f / fn : 0.f;
   const float ux = f0 * ifn, uy = f1 * ifn, uz = f2 * ifn;
@@ -161,8 +163,8 @@ __global__ void k_features(NearListView nl, const float* __restrict__ a6,
   for (int k = 0; k < Mlp::IN; ++k) f[k] = 0.f;
   const float rc = (float)LEARN_RC;
   const float w16 = (rc - 1.f) / 15.f, w8 = (rc - 1.f) / 7.f;
-  const int k0 = nl.ptr[i], k1 = nl.ptr[i + 1];
-  for (int k = k0; k < k1; ++k) {
+  const int k0 = ok ? nl.ptr[ii] : 0, k1 = ok ? nl.ptr[ii + 1] : 0;
+  for (int k = k0 + sub; k < k1; k += 8) {
     const float4 dv = nl.d[k];
     const int j     = nl.idx[k];
     const float r   = dv.w;
@@ -186,12 +188,28 @@ __global__ void k_features(NearListView nl, const float* __restrict__ a6,
       f[55 + q] += g * ct * aj;
     }
   }
+#pragma unroll
+  for (int k = 1; k < 63; ++k) {
+    if (k >= 49 && k <= 54) continue;
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) f[k] += __shfl_down_sync(0xffffffffu, f[k], o, 8);
+  }
+  if (!ok || sub != 0) return;
+  v1[3 * i]     = ai[0] * f0 + ai[1] * f1 + ai[2] * f2;
+  v1[3 * i + 1] = ai[1] * f0 + ai[3] * f1 + ai[4] * f2;
+  v1[3 * i + 2] = ai[2] * f0 + ai[4] * f1 + ai[5] * f2;
   f[0]  = aiso6(ai) * 0.25f - 1.f;
   f[63] = (k1 - k0) * 0.01f;
   float* o = feats + (size_t)i * Mlp::IN;
 #pragma unroll
   for (int k = 0; k < Mlp::IN; ++k)
     if (k < 49 || k > 54) o[k] = f[k];
+}
+
+__device__ __forceinline__ void load_t6(const __half* t6, long k, float (&t)[6]) {
+  const __half2* h = reinterpret_cast<const __half2*>(t6 + 6 * k);  // 4-byte aligned
+  const float2 a = __half22float2(h[0]), b = __half22float2(h[1]), c = __half22float2(h[2]);
+  t[0] = a.x, t[1] = a.y, t[2] = b.x, t[3] = b.y, t[4] = c.x, t[5] = c.y;
 }
 
 // out_i = alpha_i sum_j T_ij in_j: eight lanes per site stride over its list
@@ -204,8 +222,9 @@ __global__ void k_near_T(NearListView nl, const T* __restrict__ a6, const T* __r
   T fx = 0, fy = 0, fz = 0;
   if (i < nl.n) {
     for (int k = nl.ptr[i] + sub; k < nl.ptr[i + 1]; k += 8) {
-      const int j    = nl.idx[k];
-      const float* t = nl.t6 + 6 * (size_t)k;
+      const int j = nl.idx[k];
+      float t[6];
+      load_t6(nl.t6, k, t);
       const T vx = in[3 * (size_t)j], vy = in[3 * (size_t)j + 1], vz = in[3 * (size_t)j + 2];
       fx += (T)t[0] * vx + (T)t[1] * vy + (T)t[2] * vz;
       fy += (T)t[1] * vx + (T)t[3] * vy + (T)t[4] * vz;
@@ -263,20 +282,44 @@ __global__ void k_guess(int n, const float* __restrict__ Y, const float* __restr
 }
 
 template <typename T>
-__global__ void k_precond_fix(int n, T* __restrict__ z, const T* __restrict__ w,
-                              const float* __restrict__ cw, const T* __restrict__ r,
-                              const T* __restrict__ r_old, T* __restrict__ p, int start,
-                              ReduceSlots rs, double* scal, const int* flags) {
+__global__ void k_precond_near(NearListView nl, const T* __restrict__ a6,
+                               const float* __restrict__ cw, const T* __restrict__ a,
+                               const T* __restrict__ r, const T* __restrict__ r_old,
+                               T* __restrict__ zc, T* __restrict__ p, int start, ReduceSlots rs,
+                               double* scal, const int* flags) {
   __shared__ double sh[64];
   if (!start && flags[0]) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = gid >> 3, sub = gid & 7;
+  T wx = 0, wy = 0, wz = 0;
+  if (i < nl.n) {
+    for (int k = nl.ptr[i] + sub; k < nl.ptr[i + 1]; k += 8) {
+      const int j = nl.idx[k];
+      float t[6];
+      load_t6(nl.t6, k, t);
+      const T vx = a[3 * (size_t)j], vy = a[3 * (size_t)j + 1], vz = a[3 * (size_t)j + 2];
+      wx += (T)t[0] * vx + (T)t[1] * vy + (T)t[2] * vz;
+      wy += (T)t[1] * vx + (T)t[3] * vy + (T)t[4] * vz;
+      wz += (T)t[2] * vx + (T)t[4] * vy + (T)t[5] * vz;
+    }
+  }
+#pragma unroll
+  for (int o = 4; o > 0; o >>= 1) {
+    wx += __shfl_down_sync(0xffffffffu, wx, o, 8);
+    wy += __shfl_down_sync(0xffffffffu, wy, o, 8);
+    wz += __shfl_down_sync(0xffffffffu, wz, o, 8);
+  }
   double v[2] = {0.0, 0.0};
-  if (i < n) {
-    const T c = (T)cw[i];
+  if (i < nl.n && sub == 0) {
+    const T* al = a6 + 6 * (size_t)i;
+    const T c   = (T)cw[i];
+    const T w[3] = {al[0] * wx + al[1] * wy + al[2] * wz, al[1] * wx + al[3] * wy + al[4] * wz,
+                    al[2] * wx + al[4] * wy + al[5] * wz};
+#pragma unroll
     for (int q = 0; q < 3; ++q) {
       const size_t k = 3 * (size_t)i + q;
-      const T zk     = z[k] + c * w[k];
-      z[k]           = zk;
+      const T zk     = a[k] + c * w[q];
+      zc[k]          = zk;
       if (start) p[k] = zk;
       v[0] += (double)zk * r[k];
       if (!start) v[1] += (double)zk * r_old[k];
@@ -290,7 +333,8 @@ __global__ void k_precond_fix(int n, T* __restrict__ z, const T* __restrict__ w,
 
 void learned_features(const NearListView& nl, const float* a6f, const double* F, float* feats,
                       float* v1, cudaStream_t s) {
-  k_features<<<(nl.n + 127) / 128, 128, 0, s>>>(nl, a6f, F, feats, v1);
+  const long threads = 8L * nl.n;
+  k_features<<<(unsigned)((threads + 127) / 128), 128, 0, s>>>(nl, a6f, F, feats, v1);
   CG_LAUNCH();
 }
 
@@ -318,19 +362,20 @@ void learned_guess(int n, const float* Y, const float* v1, const float* v2, cons
 }
 
 template <typename T>
-void precond_fix(int n, T* z, const T* w, const float* c, const T* r, const T* r_old, T* p,
-                 bool start, double* partials, unsigned* ticket, double* scal, const int* flags,
-                 cudaStream_t s) {
+void precond_near(const NearListView& nl, const T* a6, const float* c, const T* a, const T* r,
+                  const T* r_old, T* zc, T* p, bool start, double* partials, unsigned* ticket,
+                  double* scal, const int* flags, cudaStream_t s) {
   ReduceSlots rs{partials, ticket, scal + S_RED};
-  k_precond_fix<T><<<(n + 255) / 256, 256, 0, s>>>(n, z, w, c, r, r_old, p, start ? 1 : 0, rs,
-                                                   scal, flags);
+  const long threads = 8L * nl.n;
+  k_precond_near<T><<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
+        nl, a6, c, a, r, r_old, zc, p, start ? 1 : 0, rs, scal, flags);
   CG_LAUNCH();
 }
-template void precond_fix<float>(int, float*, const float*, const float*, const float*,
-                                 const float*, float*, bool, double*, unsigned*, double*,
-                                 const int*, cudaStream_t);
-template void precond_fix<double>(int, double*, const double*, const float*, const double*,
-                                  const double*, double*, bool, double*, unsigned*, double*,
-                                  const int*, cudaStream_t);
+template void precond_near<float>(const NearListView&, const float*, const float*, const float*,
+                                  const float*, const float*, float*, float*, bool, double*,
+                                  unsigned*, double*, const int*, cudaStream_t);
+template void precond_near<double>(const NearListView&, const double*, const float*,
+                                   const double*, const double*, const double*, double*, double*,
+                                   bool, double*, unsigned*, double*, const int*, cudaStream_t);
 
 }  // namespace cg

@@ -14,6 +14,8 @@
 // (Polak-Ribiere) beta.
 #pragma once
 
+#include <cuda_fp16.h>
+
 #include "engine.h"
 #include "mlp.h"
 
@@ -27,12 +29,13 @@ constexpr double LEARN_RC = 6.0 * 1.8897261246;  // 6 A in bohr
 // T_ij = G1 I + G2 r r^T (r = r_i - r_j; G1, G2 the radial factors of the
 // operator), so that (T v)_i = sum_j T_ij v_j is the field at i of dipoles v;
 // excluded pairs are listed (for the descriptors) with T_ij = 0.  Entry k of site i (ptr[i] <= k < ptr[i+1]) holds idx[k] = j,
-// t6[6k..6k+5] and d[k] = (r_j - r_i, |r_j - r_i|).
+// t6[6k..6k+5] (FP16: the tensors feed only the guess basis and the
+// preconditioner) and d[k] = (r_j - r_i, |r_j - r_i|).
 struct NearList {
   int n    = 0;
   long nnz = 0;
   DBuf<int> ptr, idx;
-  DBuf<float> t6;
+  DBuf<__half> t6;
   DBuf<float4> d;
   // exclusions in caller indices (CSR, may be null)
   void build(const Geometry& g, const int* caller_excl_ptr, const int* caller_excl_idx,
@@ -43,7 +46,7 @@ struct NearListView {
   int n;
   const int* ptr;
   const int* idx;
-  const float* t6;
+  const __half* t6;
   const float4* d;
 };
 
@@ -59,10 +62,12 @@ void learned_basis_features(int n, const float* v1, const float* v2, const float
                             float* feats, cudaStream_t s);
 void learned_guess(int n, const float* Y, const float* v1, const float* v2, const float* v3,
                    double* x, float* c, cudaStream_t s);
-// z += c w; with r_old: beta = (z.r - z.r_old) / rz_old (Polak-Ribiere), rz = z.r
+// Corrected preconditioner in one pass: zc = a + c alpha T_near a for a = alpha r
+// (the plain preconditioned residual); at a start p = zc; rz = zc.r and, after
+// a start, beta = (zc.r - zc.r_old) / rz_old (Polak-Ribiere).
 template <typename T>
-void precond_fix(int n, T* z, const T* w, const float* c, const T* r, const T* r_old, T* p,
-                 bool start, double* partials, unsigned* ticket, double* scal, const int* flags,
-                 cudaStream_t s);
+void precond_near(const NearListView& nl, const T* a6, const float* c, const T* a, const T* r,
+                  const T* r_old, T* zc, T* p, bool start, double* partials, unsigned* ticket,
+                  double* scal, const int* flags, cudaStream_t s);
 
 }  // namespace cg

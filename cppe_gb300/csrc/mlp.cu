@@ -255,6 +255,89 @@ void Mlp::reserve(int rows) {
   loss_part.alloc((rows + 255) / 256 + 1);
 }
 
+// Inference in one pass: a row per thread; the parameters and the
+// normalisation are staged in shared memory (read as float4 broadcasts), the
+// first hidden layer stays in registers and each second-layer unit is folded
+// into the output as soon as it is computed.
+constexpr int INFER_BLOCK = 128;
+constexpr int INFER_SMEM  = (Mlp::NPARAM + 3) / 4 * 4 + 2 * Mlp::IN;  // floats
+__global__ void __launch_bounds__(INFER_BLOCK)
+      k_mlp_infer(int rows, const float* __restrict__ raw, const float* __restrict__ params,
+                  const float* __restrict__ mean, const float* __restrict__ inv_std,
+                  float* __restrict__ Y) {
+  extern __shared__ float4 smem4[];
+  float* sm = reinterpret_cast<float*>(smem4);
+  constexpr int PPAD = (Mlp::NPARAM + 3) / 4 * 4;
+  for (int k = threadIdx.x; k < Mlp::NPARAM; k += blockDim.x) sm[k] = params[k];
+  for (int k = threadIdx.x; k < Mlp::IN; k += blockDim.x)
+    sm[PPAD + k] = mean[k], sm[PPAD + Mlp::IN + k] = inv_std[k];
+  __syncthreads();
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= rows) return;
+  const float* W1 = sm;
+  const float* b1 = W1 + Mlp::NW1;
+  const float* W2 = b1 + Mlp::NB1;
+  const float* b2 = W2 + Mlp::NW2;
+  const float* W3 = b2 + Mlp::NB2;
+  const float* b3 = W3 + Mlp::NW3;
+  float x[Mlp::IN];
+  const float4* xr = reinterpret_cast<const float4*>(raw + (size_t)row * Mlp::IN);
+#pragma unroll
+  for (int q = 0; q < Mlp::IN / 4; ++q) {
+    const float4 v = xr[q];
+    x[4 * q]       = (v.x - sm[PPAD + 4 * q]) * sm[PPAD + Mlp::IN + 4 * q];
+    x[4 * q + 1]   = (v.y - sm[PPAD + 4 * q + 1]) * sm[PPAD + Mlp::IN + 4 * q + 1];
+    x[4 * q + 2]   = (v.z - sm[PPAD + 4 * q + 2]) * sm[PPAD + Mlp::IN + 4 * q + 2];
+    x[4 * q + 3]   = (v.w - sm[PPAD + 4 * q + 3]) * sm[PPAD + Mlp::IN + 4 * q + 3];
+  }
+  float h[Mlp::H];
+#pragma unroll
+  for (int o = 0; o < Mlp::H; ++o) {
+    const float4* w = reinterpret_cast<const float4*>(W1 + o * Mlp::IN);
+    float a0 = b1[o], a1 = 0.f, a2 = 0.f, a3 = 0.f;  // four independent chains
+#pragma unroll
+    for (int q = 0; q < Mlp::IN / 4; ++q) {
+      const float4 v = w[q];
+      a0 = fmaf(v.x, x[4 * q], a0), a1 = fmaf(v.y, x[4 * q + 1], a1);
+      a2 = fmaf(v.z, x[4 * q + 2], a2), a3 = fmaf(v.w, x[4 * q + 3], a3);
+    }
+    h[o] = gelu((a0 + a1) + (a2 + a3));
+  }
+  float y[Mlp::OUT];
+#pragma unroll
+  for (int k = 0; k < Mlp::OUT; ++k) y[k] = b3[k];
+#pragma unroll 2
+  for (int o = 0; o < Mlp::H; ++o) {
+    const float4* w = reinterpret_cast<const float4*>(W2 + o * Mlp::H);
+    float a0 = b2[o], a1 = 0.f, a2 = 0.f, a3 = 0.f;
+#pragma unroll
+    for (int q = 0; q < Mlp::H / 4; ++q) {
+      const float4 v = w[q];
+      a0 = fmaf(v.x, h[4 * q], a0), a1 = fmaf(v.y, h[4 * q + 1], a1);
+      a2 = fmaf(v.z, h[4 * q + 2], a2), a3 = fmaf(v.w, h[4 * q + 3], a3);
+    }
+    const float g = gelu((a0 + a1) + (a2 + a3));
+#pragma unroll
+    for (int k = 0; k < Mlp::OUT; ++k) y[k] = fmaf(W3[k * Mlp::H + o], g, y[k]);
+  }
+#pragma unroll
+  for (int k = 0; k < Mlp::OUT; ++k) Y[(size_t)row * Mlp::OUT + k] = y[k];
+}
+
+void Mlp::infer(int rows, const float* raw, float* Y_out, cudaStream_t s) {
+  if (rows <= 0) return;
+  static int attr_device = -1;
+  if (attr_device != device) {
+    CG_CUDA(cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 INFER_SMEM * (int)sizeof(float)));
+    attr_device = device;
+  }
+  k_mlp_infer<<<(rows + INFER_BLOCK - 1) / INFER_BLOCK, INFER_BLOCK,
+                INFER_SMEM * sizeof(float), s>>>(rows, raw, params.p, feat_mean.p,
+                                                 feat_inv_std.p, Y_out);
+  CG_LAUNCH();
+}
+
 void Mlp::forward(int rows, const float* raw, float* Y_out, cudaStream_t s) {
   reserve(rows);
   const long nx = (long)rows * IN, nh = (long)rows * H;

@@ -36,7 +36,9 @@ struct Mlp {
   float* W3() { return params.p + NW1 + NB1 + NW2 + NB2; }
   float* b3() { return params.p + NW1 + NB1 + NW2 + NB2 + NW3; }
   // Y (rows x 4) for raw descriptors (rows x 64, device); normalises first.
+  // forward keeps the intermediate layers (training); infer is one fused pass.
   void forward(int rows, const float* raw, float* Y_out, cudaStream_t s);
+  void infer(int rows, const float* raw, float* Y_out, cudaStream_t s);
   // loss and parameter gradients (into grads) for one batch; returns loss.
   double loss_grad(int rows, const float* raw, const float* targets, float lam);
   void adam(float lr, float b1 = 0.9f, float b2 = 0.999f, float eps = 1e-8f);

@@ -379,8 +379,8 @@ int System::solve_fp64(bool zero_guess, double* hist_out, int hist_cap, int* ite
                                                slots(S_RED), scal.p, flags.p, hist.p, t,
                                                opt.maxiter, use_model ? lf_rold64.p : nullptr);
     CG_LAUNCH();
-    if (use_model) learned_precond<double>(z.p, r.p, p.p, false);
-    k_cg_dir<double><<<(n3 + VB - 1) / VB, VB, 0, stream>>>(n3, z.p, p.p, scal.p, flags.p);
+    const double* zd = use_model ? learned_precond<double>(z.p, r.p, p.p, false) : z.p;
+    k_cg_dir<double><<<(n3 + VB - 1) / VB, VB, 0, stream>>>(n3, zd, p.p, scal.p, flags.p);
     CG_LAUNCH();
     if (poll.after_iteration()) break;
   }
@@ -414,8 +414,8 @@ void System::inner_iteration_fp32(int nb, int nb3) {
                                             std::max(1, opt.maxiter),
                                             use_model ? lf_rold32.p : nullptr);
   CG_LAUNCH();
-  if (use_model) learned_precond<float>(z32.p, r32.p, p32.p, false);
-  k_cg_dir<float><<<nb3, VB, 0, stream>>>(3 * n, z32.p, p32.p, scal.p, flags.p);
+  const float* zd = use_model ? learned_precond<float>(z32.p, r32.p, p32.p, false) : z32.p;
+  k_cg_dir<float><<<nb3, VB, 0, stream>>>(3 * n, zd, p32.p, scal.p, flags.p);
   CG_LAUNCH();
 }
 
@@ -672,27 +672,25 @@ void System::learned_features_for_F() {
 
 void System::learned_start() {
   learned_features_for_F();
-  CG_CUDA(cudaStreamSynchronize(stream));
-  model->forward(n, lf_feats.p, lf_Y.p, model->stream);
-  CG_CUDA(cudaStreamSynchronize(model->stream));
+  model->infer(n, lf_feats.p, lf_Y.p, stream);
   learned_guess(n, lf_Y.p, lf_v1.p, lf_v2.p, lf_v3.p, x.p, lf_c.p, stream);
 }
 
 template <typename T>
-void System::learned_precond(T* zv, const T* rv, T* pv, bool start) {
+T* System::learned_precond(T* zv, const T* rv, T* pv, bool start) {
   const NearListView nl = view(*near);
   if constexpr (std::is_same<T, double>::value) {
-    near_T<double>(nl, alpha64.p, zv, lf_w64.p, stream);
-    precond_fix<double>(n, zv, lf_w64.p, lf_c.p, rv, lf_rold64.p, pv, start, partials.p, ticket.p,
-                        scal.p, flags.p, stream);
+    precond_near<double>(nl, alpha64.p, lf_c.p, zv, rv, lf_rold64.p, lf_w64.p, pv, start,
+                         partials.p, ticket.p, scal.p, flags.p, stream);
+    return lf_w64.p;
   } else {
-    near_T<float>(nl, alpha32.p, zv, lf_w32.p, stream);
-    precond_fix<float>(n, zv, lf_w32.p, lf_c.p, rv, lf_rold32.p, pv, start, partials.p, ticket.p,
-                       scal.p, flags.p, stream);
+    precond_near<float>(nl, alpha32.p, lf_c.p, zv, rv, lf_rold32.p, lf_w32.p, pv, start,
+                        partials.p, ticket.p, scal.p, flags.p, stream);
+    return lf_w32.p;
   }
 }
-template void System::learned_precond<double>(double*, const double*, double*, bool);
-template void System::learned_precond<float>(float*, const float*, float*, bool);
+template double* System::learned_precond<double>(double*, const double*, double*, bool);
+template float* System::learned_precond<float>(float*, const float*, float*, bool);
 
 void System::learned_rows(const double* mu_dev, std::vector<float>& feats, std::vector<float>& rows) {
   // F holds the rhs (device order); x0 = alpha F; r0 = F - B x0 (FP64)

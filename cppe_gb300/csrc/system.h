@@ -64,8 +64,9 @@ struct System {
   // x = learned guess, lf_c = preconditioner weights
   void learned_start();
   // z correction after a CG start/update (flexible CG)
+  // returns the corrected preconditioned residual (the z the CG continues with)
   template <typename T>
-  void learned_precond(T* z, const T* r, T* p, bool start);
+  T* learned_precond(T* z, const T* r, T* p, bool start);
   // training rows for rhs F (device order) and converged mu (device order)
   void learned_rows(const double* mu_star_dev, std::vector<float>& feats,
                     std::vector<float>& rows);
