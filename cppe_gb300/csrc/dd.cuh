@@ -103,4 +103,49 @@ __device__ __forceinline__ dd dd_exp_neg(dd v, const float2* tab) {
   return dd_mul({e.x, e.y}, et);
 }
 
+// ---------------------------------------------------------------------------
+// A value type over dd for generic code (the generated M2L translations):
+// +, -, * with dd accuracy, division by a Newton-corrected quotient.
+// ---------------------------------------------------------------------------
+struct ddv {
+  float h, l;
+  __device__ __forceinline__ ddv() : h(0.f), l(0.f) {}
+  __device__ __forceinline__ explicit ddv(int v) : h((float)v), l(0.f) {}
+  __device__ __forceinline__ ddv(float hh, float ll) : h(hh), l(ll) {}
+  __device__ __forceinline__ ddv(dd a) : h(a.h), l(a.l) {}
+  __device__ __forceinline__ operator dd() const { return dd{h, l}; }
+};
+__device__ __forceinline__ ddv operator+(ddv a, ddv b) { return dd_add(a, b); }
+__device__ __forceinline__ ddv operator-(ddv a) { return ddv(-a.h, -a.l); }
+__device__ __forceinline__ ddv operator-(ddv a, ddv b) { return dd_add(a, ddv(-b.h, -b.l)); }
+__device__ __forceinline__ ddv operator*(ddv a, ddv b) { return dd_mul(a, b); }
+__device__ __forceinline__ ddv fma(ddv a, ddv b, ddv c) { return dd_add(dd_mul(a, b), c); }
+// (the float and double overloads, visible next to the ddv one inside cg)
+__device__ __forceinline__ float fma(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fma(double a, double b, double c) { return ::fma(a, b, c); }
+__device__ __forceinline__ ddv operator/(ddv a, ddv b) {
+  const float q1 = a.h / b.h;
+  const dd r     = dd_add(a, dd_neg(dd_mul(b, dd{q1, 0.f})));
+  return dd_fast_two_sum(q1, r.h / b.h);
+}
+__device__ __forceinline__ ddv rsqrt_t(ddv a) { return dd_rsqrt(a); }
+
+// 1/o for a small positive integer o, in the precision of T (constant-folded)
+template <typename T>
+__device__ __forceinline__ T cinv(int o);
+template <>
+__device__ __forceinline__ float cinv<float>(int o) {
+  return 1.f / (float)o;
+}
+template <>
+__device__ __forceinline__ double cinv<double>(int o) {
+  return 1.0 / (double)o;
+}
+template <>
+__device__ __forceinline__ ddv cinv<ddv>(int o) {
+  const double v = 1.0 / (double)o;
+  const float hh = (float)v;
+  return ddv(hh, (float)(v - (double)hh));
+}
+
 }  // namespace cg

@@ -1326,6 +1326,14 @@ void SideStream::destroy() {
   s = nullptr, fork = join = nullptr;
 }
 
+__global__ void k_split_dd_vec(long n, const double* __restrict__ in, float2* __restrict__ out) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double v = in[i];
+  const float h  = (float)v;
+  out[i]         = make_float2(h, (float)(v - (double)h));
+}
+
 __global__ void k_split_dd(long n, const double* __restrict__ in, float2* __restrict__ out) {
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -1395,7 +1403,17 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
     }
     mark(1);
     w.Lpart.alloc((size_t)std::max<size_t>(1, g.h_m2l_chunks.size()) * ov.lsize);
-    if (launch_m2l_fixed<T>(tv, ov.m, ov.p, g.m2l_chunks.p, (int)g.h_m2l_chunks.size(),
+    bool m2l_done = false;
+    if constexpr (std::is_same<T, double>::value) {
+      if (near_mode == NEAR_DD) {
+        w.Mdd.alloc((size_t)std::max(1, tv.ncells) * ov.msize);
+        m2l_done = launch_m2l_dd(tv, ov.m, ov.p, g.m2l_chunks.p, (int)g.h_m2l_chunks.size(),
+                                 g.cell_chunk_ptr.p, w.M.p, ov.msize, w.Mdd.p, w.Lpart.p, w.L.p,
+                                 ov.lsize, fs);
+      }
+    }
+    if (m2l_done ||
+        launch_m2l_fixed<T>(tv, ov.m, ov.p, g.m2l_chunks.p, (int)g.h_m2l_chunks.size(),
                             g.cell_chunk_ptr.p, w.M.p, w.Lpart.p, w.L.p, ov.lsize, fs)) {
     } else {
       size_t smem = (size_t)(ov.nm2l_terms + 9 * ov.nt) * sizeof(int);

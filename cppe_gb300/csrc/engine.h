@@ -149,6 +149,7 @@ template <typename T>
 struct FieldWork {
   DBuf<T> M, L, Fnear, Mpart, Lleaf, Lpart;
   DBuf<float2> dd_src;  // double-float copy of the sources (double-float pass)
+  DBuf<float2> Mdd;     // double-float copy of the multipoles (double-float M2L)
 };
 
 // Output modes of the finishing pass.
@@ -188,7 +189,8 @@ struct SideStream {
 enum NearMode {
   NEAR_FP64     = 0,  // native FP64 throughout
   NEAR_FAST_EXP = 1,  // FP64, FP32 exponential where the damping argument is >= 20
-  NEAR_DD       = 2   // double-float on the FP32 pipe (dipole sources; others use FAST_EXP)
+  NEAR_DD       = 2   // double-float on the FP32 pipe (dipole sources; others use FAST_EXP);
+                      // the fixed-order M2L runs in double-float too
 };
 
 template <typename T>

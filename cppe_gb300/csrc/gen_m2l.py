@@ -12,7 +12,10 @@ y-power descending.  D is built from the recurrence
 
     |n| R^2 D_n = -(2|n|-1) sum_i n_i r_i D_{n-e_i} - (|n|-1) sum_i n_i (n_i-1) D_{n-2e_i}
 
-(differentiate R^2 d_i (1/R) = -r_i / R).  This file is run by the build
+(differentiate R^2 d_i (1/R) = -r_i / R).  The functions are templates over
+the arithmetic type: float, double, or the double-float pair `ddv` (dd.cuh),
+which supplies the operators, `fma`, `rsqrt_t` and `cinv<T>(o)` = 1/o.
+This file is run by the build
 (cppe_gb300/_build.py) and its output is not edited by hand.
 """
 import os
@@ -71,7 +74,7 @@ def emit(m, p):
         expr = f"T({2 * o - 1}) * ({e1})"
         if t2 and o > 1:
             expr += f" + T({o - 1}) * ({' + '.join(t2)})"
-        lines.append(f"  const T D{j} = -({expr}) * ir2 * (T(1) / T({o}));")
+        lines.append(f"  const T D{j} = -({expr}) * ir2 * cinv<T>({o});")
     for k in range(moff, nterms(p)):
         ka, kb, kc = mi[k]
         ko = ka + kb + kc

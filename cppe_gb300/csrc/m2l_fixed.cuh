@@ -10,6 +10,7 @@
 // warp shuffles in a fixed order at the end.
 #pragma once
 
+#include "dd.cuh"
 #include "engine.h"
 
 namespace cg {
@@ -49,6 +50,41 @@ namespace cg {
 CPPE_M2L_GENERATED(CPPE_DEF_M2L_KERNEL)
 #undef CPPE_DEF_M2L_KERNEL
 
+// Double-float variant for the mixed solver's FP64-accurate residual: the
+// same chunks, the source multipoles as double-float pairs (split once per
+// apply), the partial expansions written in FP64.
+#define CPPE_DEF_M2L_DD_KERNEL(M, P, NAME, LS, MS)                                          \
+  __global__ void __launch_bounds__(64)                                                     \
+        k_##NAME##_dd(TreeView tv, const int4* __restrict__ chunks, int nchunks,            \
+                      const float2* __restrict__ Mdd, double* __restrict__ Lpart) {         \
+    const int lane = threadIdx.x & 31;                                                      \
+    const int w    = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;                          \
+    if (w >= nchunks) return;                                                               \
+    const int4 ch = chunks[w];                                                              \
+    ddv acc[LS];                                                                            \
+    const double4_32a cA = tv.center[ch.x];                                                 \
+    for (int idx = ch.y + lane; idx < ch.z; idx += 32) {                                    \
+      const int B          = tv.m2l_src[idx];                                               \
+      const double4_32a cB = tv.center[B];                                                  \
+      NAME<ddv>(ddv(dd_from(cA.x - cB.x)), ddv(dd_from(cA.y - cB.y)),                       \
+                ddv(dd_from(cA.z - cB.z)),                                                  \
+                reinterpret_cast<const ddv*>(Mdd + (size_t)B * (MS)), acc);                 \
+    }                                                                                       \
+    double* LA = Lpart + (size_t)w * (LS);                                                  \
+    _Pragma("unroll") for (int q = 0; q < LS; ++q) {                                        \
+      dd v = acc[q];                                                                        \
+      _Pragma("unroll") for (int off = 16; off > 0; off >>= 1) {                            \
+        const dd o{__shfl_xor_sync(0xffffffffu, v.h, off),                                  \
+                   __shfl_xor_sync(0xffffffffu, v.l, off)};                                 \
+        v = dd_add(v, o);                                                                   \
+      }                                                                                     \
+      if ((q & 31) == lane) LA[q] = dd_to(v);                                               \
+    }                                                                                       \
+  }
+
+CPPE_M2L_GENERATED(CPPE_DEF_M2L_DD_KERNEL)
+#undef CPPE_DEF_M2L_DD_KERNEL
+
 // L of every cell: the sum of its chunk partials in order (0 without chunks).
 template <typename T>
 __global__ void k_lsum(int ncells, int lsize, const int* __restrict__ cell_chunk_ptr,
@@ -86,6 +122,38 @@ bool launch_m2l_fixed(const TreeView& tv, int m, int p, const int4* chunks, int 
   if (work > 0) {
     k_lsum<T><<<(unsigned)((work + 255) / 256), 256, 0, s>>>(tv.ncells, lsize, cell_chunk_ptr,
                                                              Lpart, L);
+    CG_LAUNCH();
+  }
+  return true;
+}
+
+// The double-float M2L for (m, p) when compiled: splits M into pairs, runs
+// the chunks, sums per cell in FP64.  Returns false otherwise.
+__global__ void k_split_dd_vec(long n, const double* __restrict__ in, float2* __restrict__ out);
+inline bool launch_m2l_dd(const TreeView& tv, int m, int p, const int4* chunks, int nchunks,
+                          const int* cell_chunk_ptr, const double* Mexp, int msize,
+                          float2* Mdd, double* Lpart, double* L, int lsize, cudaStream_t s) {
+  bool ok = false;
+  const long nm = (long)tv.ncells * msize;
+#define CPPE_LAUNCH_M2L_DD(MM, PP, NAME, LS, MS)                                           \
+  if (!ok && m == MM && p == PP) {                                                         \
+    if (nchunks > 0) {                                                                     \
+      k_split_dd_vec<<<(unsigned)((nm + 255) / 256), 256, 0, s>>>(nm, Mexp, Mdd);          \
+      CG_LAUNCH();                                                                         \
+      k_##NAME##_dd<<<(unsigned)(((long)nchunks * 32 + 63) / 64), 64, 0, s>>>(tv, chunks,  \
+                                                                             nchunks, Mdd, \
+                                                                             Lpart);       \
+      CG_LAUNCH();                                                                         \
+    }                                                                                      \
+    ok = true;                                                                             \
+  }
+  CPPE_M2L_GENERATED(CPPE_LAUNCH_M2L_DD)
+#undef CPPE_LAUNCH_M2L_DD
+  if (!ok) return false;
+  const long work = (long)tv.ncells * lsize;
+  if (work > 0) {
+    k_lsum<double><<<(unsigned)((work + 255) / 256), 256, 0, s>>>(tv.ncells, lsize,
+                                                                  cell_chunk_ptr, Lpart, L);
     CG_LAUNCH();
   }
   return true;

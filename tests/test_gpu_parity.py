@@ -158,14 +158,15 @@ def test_mixed_precision_solve(gpu, port, fmm):
     np.testing.assert_allclose(mumx, mu64, atol=1e-7)
 
 
-@pytest.mark.parametrize("fmm,damp", [(False, True), (True, True), (True, False)])
-def test_double_float_apply_matches_fp64(gpu, fmm, damp):
-    """The mixed solver's residual operator (double-float near field) equals
-    the FP64 operator to FP64-level accuracy."""
+@pytest.mark.parametrize("fmm,damp,order", [(False, True, 5), (True, True, 5),
+                                            (True, False, 5), (True, True, 6)])
+def test_double_float_apply_matches_fp64(gpu, fmm, damp, order):
+    """The mixed solver's residual operator (double-float near field and M2L)
+    equals the FP64 operator to FP64-level accuracy."""
     from cppe_gb300 import synthetic
     b = synthetic.water_box(1500, seed=31)
     s = cabi.System(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx,
-                    summation=cabi.FMM if fmm else cabi.DIRECT, damp=damp)
+                    summation=cabi.FMM if fmm else cabi.DIRECT, damp=damp, order=order)
     v = np.random.default_rng(5).normal(0, 0.1, size=3 * b.n)
     a64 = s.apply(v)
     add = s.apply(v, dd=True)
