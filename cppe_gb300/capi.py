@@ -394,6 +394,14 @@ class System:
         self._model = mlp
         check(lib().cppe_gpu_set_model(self.h, mlp.h if mlp is not None else None))
 
+    def autotune(self, reps=3):
+        """Picks the fastest near-field item size and M2L chunk; returns ms per apply."""
+        ms = ctypes.c_double(0)
+        lib().cppe_gpu_autotune.argtypes = [ctypes.c_void_p, ctypes.c_int,
+                                            ctypes.POINTER(ctypes.c_double)]
+        check(lib().cppe_gpu_autotune(self.h, reps, ctypes.byref(ms)))
+        return ms.value
+
     def kernel_timings(self, precision=FP64, reps=5):
         ms = np.zeros(6)
         npair, nm2l = ctypes.c_longlong(0), ctypes.c_longlong(0)

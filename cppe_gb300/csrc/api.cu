@@ -590,6 +590,15 @@ int cppe_gpu_kernel_timings(cppe_gpu_system* sys, int precision, int reps, doubl
   });
 }
 
+int cppe_gpu_autotune(cppe_gpu_system* sys, int reps, double* best_ms) {
+  return guard([&]() -> int {
+    need(sys && reps > 0, "null argument");
+    const double ms = sys->s.autotune(reps);
+    if (best_ms) *best_ms = ms;
+    return CPPE_GPU_OK;
+  });
+}
+
 int cppe_gpu_fma_peak(int device, int fp64, double* tflops) {
   return guard([&]() -> int {
     need(tflops, "null argument");

@@ -275,10 +275,11 @@ void Geometry::make_schedules() {
   // M2L chunks: at most M2L_CHUNK sources of one target cell each
   h_m2l_chunks.clear();
   h_cell_chunk_ptr.assign(L.ncells + 1, 0);
+  const int chunk = m2l_chunk > 0 ? m2l_chunk : M2L_CHUNK;
   if (fmm)
     for (int c = 0; c < L.ncells; ++c) {
-      for (int q = L.m2l_ptr[c]; q < L.m2l_ptr[c + 1]; q += M2L_CHUNK)
-        h_m2l_chunks.push_back(make_int4(c, q, std::min(q + M2L_CHUNK, L.m2l_ptr[c + 1]), 0));
+      for (int q = L.m2l_ptr[c]; q < L.m2l_ptr[c + 1]; q += chunk)
+        h_m2l_chunks.push_back(make_int4(c, q, std::min(q + chunk, L.m2l_ptr[c + 1]), 0));
       h_cell_chunk_ptr[c + 1] = (int)h_m2l_chunks.size();
     }
   if (h_lanc_cell.empty()) h_lanc_cell.push_back(0);
@@ -291,7 +292,7 @@ void Geometry::make_schedules() {
       total += na * (L.leaf_start[b + 1] - L.leaf_start[b]);
     }
   }
-  const long W = std::max<long>(8192, total / (32L * 152));
+  const long W = item_pairs > 0 ? item_pairs : std::max<long>(8192, total / (32L * 152));
   struct It {
     long w;
     int4 v;
@@ -321,6 +322,13 @@ void Geometry::make_schedules() {
     h_items[k] = its[k].v;
     nslot      = std::max(nslot, its[k].v.w + 1);
   }
+}
+
+void Geometry::upload_schedules(cudaStream_t s) {
+  items.upload(h_items, s);
+  leaf_nslot.upload(h_leaf_nslot, s);
+  if (!h_m2l_chunks.empty()) m2l_chunks.upload(h_m2l_chunks, s);
+  cell_chunk_ptr.upload(h_cell_chunk_ptr, s);
 }
 
 void Geometry::upload(cudaStream_t s) {

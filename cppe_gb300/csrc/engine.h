@@ -116,8 +116,13 @@ struct Geometry {
   DBuf<int4> p2m_tasks;
   DBuf<int> task_leaf, cell_task_ptr, lanc_ptr, lanc_cell, cell_ref;
   DBuf<float4> cell_off;
+  // tunable schedule parameters (0: the built-in choice)
+  long item_pairs = 0;  // target pairs per near-field work item
+  int m2l_chunk   = 0;  // sources per M2L warp
   // builds both schedules from `layout` and h_pos64
   void make_schedules();
+  // re-uploads what make_schedules changes (near-field items, M2L chunks)
+  void upload_schedules(cudaStream_t s);
 
   // host copies of the device arrays that are not part of `layout`
   std::vector<int> h_site_leaf, h_cptr, h_cidx;

@@ -2,6 +2,7 @@
 // (InducedMoments::compute, src/core/electric_fields.cc:191-239) and the
 // mixed-precision form (FP32 inner PCG, FP64 residual and refinement).
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <numeric>
@@ -308,6 +309,55 @@ void System::phase_timings(int precision, int reps, double* ms) {
   for (int k = 0; k < 6; ++k) ms[k] = acc[k] / std::max(1, reps);
 }
 
+double System::autotune(int reps) {
+  CG_CUDA(cudaSetDevice(device));
+  reps = std::max(1, reps);
+  // the built-in work-item size, for the candidates around it
+  long total = 0;
+  const TreeLayout& L = geo.layout;
+  for (int a = 0; a < L.nleaves; ++a)
+    for (int q = L.p2p_ptr[a]; q < L.p2p_ptr[a + 1]; ++q)
+      total += (long)(L.leaf_start[a + 1] - L.leaf_start[a]) *
+               (L.leaf_start[L.p2p_src[q] + 1] - L.leaf_start[L.p2p_src[q]]);
+  const long w0 = std::max<long>(8192, total / (32L * 152));
+  const long ws[3]  = {std::max<long>(4096, w0 / 2), w0, 2 * w0};
+  const int chs[3]  = {32, 64, 128};
+  const int nch     = geo.fmm ? 3 : 1;
+  cudaEvent_t e0, e1;
+  CG_CUDA(cudaEventCreate(&e0));
+  CG_CUDA(cudaEventCreate(&e1));
+  CG_CUDA(cudaMemsetAsync(p32.p, 0, sizeof(float) * 3 * (size_t)n, stream));
+  double best = 1e300;
+  long best_w = w0;
+  int best_c  = 64;
+  for (long w : ws)
+    for (int ci = 0; ci < nch; ++ci) {
+      geo.item_pairs = w;
+      geo.m2l_chunk  = chs[ci];
+      geo.make_schedules();
+      geo.upload_schedules(stream);
+      apply32(p32.p, Ap32.p, false);  // warm-up (sizes the work buffers)
+      CG_CUDA(cudaEventRecord(e0, stream));
+      for (int r = 0; r < reps; ++r) apply32(p32.p, Ap32.p, false);
+      CG_CUDA(cudaEventRecord(e1, stream));
+      CG_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      CG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      if (ms / reps < best) best = ms / reps, best_w = w, best_c = chs[ci];
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  geo.item_pairs = best_w;
+  geo.m2l_chunk  = best_c;
+  geo.make_schedules();
+  geo.upload_schedules(stream);
+  CG_CUDA(cudaStreamSynchronize(stream));
+  // captured inner loops hold the old schedule's buffers: rebuild on next use
+  for (auto& e : inner_exec)
+    if (e) cudaGraphExecDestroy(e), e = nullptr;
+  return best;
+}
+
 ReduceSlots System::slots(int k) const { return ReduceSlots{partials.p, ticket.p, scal.p + k}; }
 
 void System::apply64(const double* in, double* out, bool with_dot, int near_mode) {
@@ -427,6 +477,13 @@ void System::inner_iteration_fp32(int nb, int nb3) {
 // construction is refused, the iterations are launched from the host.
 void System::run_inner_fp32(int nb, int nb3) {
   const int v = use_model ? 1 : 0;
+  // CPPE_GPU_GRAPHS=0 launches the iterations from the host instead (same
+  // kernels; for profilers that do not descend into conditional graph nodes)
+  static const bool graphs = [] {
+    const char* e = std::getenv("CPPE_GPU_GRAPHS");
+    return !(e && e[0] == '0');
+  }();
+  if (!graphs) inner_graph_failed = true;
   if (!inner_exec[v] && !inner_graph_failed) {
     cudaGraph_t g = nullptr;
     bool ok       = cudaGraphCreate(&g, 0) == cudaSuccess;

@@ -88,6 +88,9 @@ struct System {
   // solves in device order: F holds the rhs, x the start vector
   int solve_fp64(bool zero_guess, double* hist_out, int hist_cap, int* iters);
   int solve_mixed(bool zero_guess, double* hist_out, int hist_cap, int* iters);
+  // Times the FP32 apply for a few near-field work-item sizes and M2L chunk
+  // sizes and keeps the fastest schedule; returns its apply time (ms).
+  double autotune(int reps);
   // inner FP32 PCG loop of the mixed solver (graph-launched when possible)
   void inner_iteration_fp32(int nb, int nb3);
   void run_inner_fp32(int nb, int nb3);

@@ -178,6 +178,24 @@ def test_double_float_apply_matches_fp64(gpu, fmm, damp, order):
     assert err_dd < 1e-3 * err_32
 
 
+def test_autotune_keeps_the_operator(gpu):
+    """The schedule autotuner changes the work partition, not the operator."""
+    from cppe_gb300 import synthetic
+    b = synthetic.water_box(1500, seed=32)
+    s = cabi.System(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, summation=cabi.FMM, damp=True,
+                    precision=cabi.MIXED)
+    v = np.random.default_rng(6).normal(0, 0.1, size=3 * b.n)
+    a64, a32 = s.apply(v), s.apply(v, fp32=True)
+    ms = s.autotune(2)
+    assert ms > 0
+    b64, b32 = s.apply(v), s.apply(v, fp32=True)
+    np.testing.assert_allclose(b64, a64, rtol=0, atol=1e-12 * np.abs(a64).max())
+    np.testing.assert_allclose(b32, a32, rtol=0, atol=2e-6 * np.abs(a32).max())
+    rhs = b.external_field()
+    mu, it, _, _ = s.solve(rhs)
+    assert np.linalg.norm(rhs - s.apply(mu)) < 1e-8
+
+
 def test_fmm_solve_matches_oracle(gpu, port):
     from cppe_gb300 import synthetic
     b = synthetic.water_box(1500, seed=4)
