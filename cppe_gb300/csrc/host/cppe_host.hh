@@ -119,6 +119,7 @@ class Potential {
   int index;
 
   void add_multipole(const Multipole& m) { m_multipoles.push_back(m); }
+  void add_multipole(Multipole&& m) { m_multipoles.push_back(std::move(m)); }
   void add_exclusion(int e) { m_exclusions.push_back(e); }
   bool excludes_site(int other) const;
   std::vector<int>& get_exclusions() { return m_exclusions; }

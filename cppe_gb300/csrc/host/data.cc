@@ -1,6 +1,9 @@
 // Data model, potfile reading, potential manipulation and math helpers of the
 // host layer (host-side setup code; no field arithmetic).
 #include <algorithm>
+#include <string_view>
+#include <cctype>
+#include <charconv>
 #include <cmath>
 #include <fstream>
 #include <iomanip>
@@ -95,21 +98,60 @@ std::vector<Potential> get_polarizable_sites(const std::vector<Potential>& poten
 }
 
 // --- PotfileReader (potfile_reader.cc:22-179) -------------------------------
+// The file is read into memory once and scanned line by line; tokens are
+// string views and numbers are parsed with std::from_chars (locale-free), so
+// a million-site file is read without per-token allocations.
 namespace {
 const double kAngToBohr = 1.8897261246;
 
-std::vector<std::string> tokens(const std::string& line) {
-  std::istringstream is(line);
-  std::vector<std::string> t;
-  std::string w;
-  while (is >> w) t.push_back(w);
-  return t;
+struct Scanner {
+  std::string buf;
+  size_t pos = 0;
+  bool next(std::string_view& line) {
+    if (pos >= buf.size()) return false;
+    size_t e = buf.find('\n', pos);
+    if (e == std::string::npos) e = buf.size();
+    line = std::string_view(buf).substr(pos, e - pos);
+    if (!line.empty() && line.back() == '\r') line.remove_suffix(1);
+    pos = e + 1;
+    return true;
+  }
+};
+
+// whitespace-separated tokens of a line (views into it)
+void tokens(std::string_view line, std::vector<std::string_view>& t) {
+  t.clear();
+  size_t i = 0;
+  const size_t n = line.size();
+  while (i < n) {
+    while (i < n && std::isspace((unsigned char)line[i])) ++i;
+    size_t j = i;
+    while (j < n && !std::isspace((unsigned char)line[j])) ++j;
+    if (j > i) t.push_back(line.substr(i, j - i));
+    i = j;
+  }
 }
-std::string trimmed(const std::string& s) {
-  auto t = tokens(s);
+std::string trimmed(std::string_view s) {
+  std::vector<std::string_view> t;
+  tokens(s, t);
   std::string out;
-  for (size_t i = 0; i < t.size(); ++i) out += (i ? " " : "") + t[i];
+  for (size_t i = 0; i < t.size(); ++i) out += (i ? " " : "") + std::string(t[i]);
   return out;
+}
+double num(std::string_view t) {
+  if (!t.empty() && t[0] == '+') t.remove_prefix(1);
+  double v      = 0.0;
+  const auto rc = std::from_chars(t.data(), t.data() + t.size(), v);
+  if (rc.ec != std::errc() || rc.ptr != t.data() + t.size())
+    throw std::invalid_argument("invalid number in potential file: " + std::string(t));
+  return v;
+}
+int inum(std::string_view t) {
+  if (!t.empty() && t[0] == '+') t.remove_prefix(1);
+  int v         = 0;
+  const auto rc = std::from_chars(t.data(), t.data() + t.size(), v);
+  if (rc.ec != std::errc()) throw std::invalid_argument("invalid integer in potential file");
+  return v;
 }
 }  // namespace
 
@@ -119,17 +161,25 @@ PotfileReader::PotfileReader(std::string name) : m_potfile(std::move(name)) {
 }
 
 std::vector<Potential> PotfileReader::read() {
-  std::ifstream in(m_potfile);
+  Scanner sc;
+  {
+    std::ifstream in(m_potfile, std::ios::binary);
+    std::ostringstream ss;
+    ss << in.rdbuf();
+    sc.buf = ss.str();
+  }
   std::vector<Potential> pots;
-  std::string line;
+  std::string_view line;
+  std::vector<std::string_view> t;
   int num_sites = 0;
   auto next     = [&]() {
-    if (!std::getline(in, line)) throw std::runtime_error("unexpected end of potential file");
+    if (!sc.next(line)) throw std::runtime_error("unexpected end of potential file");
     return line;
   };
-  while (std::getline(in, line)) {
-    if (line.find("@COORDINATES") != std::string::npos) {
-      num_sites        = std::stoi(tokens(next())[0]);
+  while (sc.next(line)) {
+    if (line.find("@COORDINATES") != std::string_view::npos) {
+      tokens(next(), t);
+      num_sites        = inum(t.at(0));
       std::string unit = trimmed(next());
       double conv;
       if (unit == "AA")
@@ -138,47 +188,51 @@ std::vector<Potential> PotfileReader::read() {
         conv = 1.0;
       else
         throw std::runtime_error("Invalid unit for potential file.");
+      pots.reserve(num_sites);
       for (int i = 0; i < num_sites; ++i) {
-        auto t = tokens(next());
+        tokens(next(), t);
         if (t.size() < 4) throw std::runtime_error("malformed coordinate line");
-        pots.emplace_back(std::stod(t[1]) * conv, std::stod(t[2]) * conv,
-                          std::stod(t[3]) * conv, t[0], i);
+        pots.emplace_back(num(t[1]) * conv, num(t[2]) * conv, num(t[3]) * conv,
+                          std::string(t[0]), i);
       }
     }
-    if (line.find("ORDER") != std::string::npos) {
-      auto t = tokens(line);
-      if (t.size() == 2) {
-        const int order = std::stoi(t[1]);
+    if (line.find("ORDER") != std::string_view::npos) {
+      std::vector<std::string_view> h;
+      tokens(line, h);
+      if (h.size() == 2) {
+        const int order = inum(h[1]);
         const int ncomp = multipole_components(order);
-        const int count = std::stoi(next());
+        tokens(next(), t);
+        const int count = inum(t.at(0));
         int before      = -1;
         auto zero_mul   = [&](int site) {
           Multipole m(order);
           for (int v = 0; v < ncomp; ++v) m.add_value(0.0);
-          pots.at(site).add_multipole(m);
+          pots.at(site).add_multipole(std::move(m));
         };
         for (int k = 0; k < count; ++k) {
-          auto r   = tokens(next());
-          int site = std::stoi(r.at(0)) - 1;
+          tokens(next(), t);
+          int site = inum(t.at(0)) - 1;
           for (int d = before + 1; d < site; ++d) zero_mul(d);  // sites without values
           Multipole m(order);
-          for (int v = 1; v <= ncomp; ++v) m.add_value(std::stod(r.at(v)));
+          for (int v = 1; v <= ncomp; ++v) m.add_value(num(t.at(v)));
           m.remove_trace();
-          pots.at(site).add_multipole(m);
+          pots.at(site).add_multipole(std::move(m));
           before = site;
           if (k == count - 1)
             for (int d = site + 1; d < num_sites; ++d) zero_mul(d);
         }
-      } else if (t.size() == 3) {
-        if (std::stoi(t[1]) != 1 || std::stoi(t[2]) != 1)
+      } else if (h.size() == 3) {
+        if (inum(h[1]) != 1 || inum(h[2]) != 1)
           throw std::runtime_error(
                 "Only dipole-dipole polarizabilities are currently supported.");
-        const int count = std::stoi(next());
+        tokens(next(), t);
+        const int count = inum(t.at(0));
         for (int k = 0; k < count; ++k) {
-          auto r   = tokens(next());
-          int site = std::stoi(r.at(0)) - 1;
-          std::vector<double> v;
-          for (int c = 1; c <= 6; ++c) v.push_back(std::stod(r.at(c)));
+          tokens(next(), t);
+          int site = inum(t.at(0)) - 1;
+          std::vector<double> v(6);
+          for (int c = 1; c <= 6; ++c) v[c - 1] = num(t.at(c));
           Polarizability p(v);
           if (pots.at(site).is_polarizable())
             throw std::runtime_error("Potential can only have one polarizability.");
@@ -188,13 +242,14 @@ std::vector<Potential> PotfileReader::read() {
         throw std::runtime_error("Invalid number in potfile ORDER.");
       }
     }
-    if (line.find("EXCLISTS") != std::string::npos) {
-      const int count = std::stoi(tokens(next())[0]);
+    if (line.find("EXCLISTS") != std::string_view::npos) {
+      tokens(next(), t);
+      const int count = inum(t.at(0));
       for (int k = 0; k < count; ++k) {
-        auto r   = tokens(next());
-        int site = std::stoi(r.at(0)) - 1;
-        for (size_t c = 1; c < r.size(); ++c) {
-          int e = std::stoi(r[c]) - 1;
+        tokens(next(), t);
+        int site = inum(t.at(0)) - 1;
+        for (size_t c = 1; c < t.size(); ++c) {
+          int e = inum(t[c]) - 1;
           if (e >= 0) pots.at(site).add_exclusion(e);
         }
       }

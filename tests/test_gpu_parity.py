@@ -248,6 +248,20 @@ def test_python_api_state_and_solver(gpu, unpacked, golden_vectors):
     assert abs(epol - (-0.5 * g["pna_mu_plain"] @ g["pna_mulfields"])) < 1e-12
     eef = state.induced_moments_eef()
     assert eef.shape == (54, 3)
+    # CppeState::induced_moments_eef (cppe_state.cc:111-128): three solves
+    # for unit fields along x, y, z at every polarizable site
+    from oracle import oracle as O
+    sites = O.read_potfile(unpacked["pna_6w.pot"])
+    pol = np.flatnonzero(sites.polarizable)
+    assert len(pol) == 18
+    port = O.PortOracle()
+    for a in range(3):
+        f = np.zeros(54)
+        f[a::3] = 1.0
+        mu_o, _, _, ok = port.solve(sites.xyz[pol], sites.alpha6[pol], sites.excl_ptr,
+                                    sites.excl_idx, f, thresh=1e-12)
+        assert ok
+        np.testing.assert_allclose(eef[:, a], mu_o, atol=1e-10)
     # warm start: a second call converges immediately from the previous moments
     state.update_induced_moments(np.zeros(54), False)
     np.testing.assert_allclose(state.get_induced_moments(), g["pna_mu_plain"], atol=1e-10)
