@@ -685,15 +685,18 @@ __device__ __forceinline__ void f32x2_pair_m1(const float2& nX, const float2& nY
   FZ = __ffma2_rn(z, nC, __ffma2_rn(mz, A, FZ));
 }
 
-template <bool DAMP>
+// NP packs of two targets per thread (NP = 1: two targets).
+constexpr int P2P32_NP = 1;
+template <bool DAMP, int NP>
 __global__ void __launch_bounds__(P2P_BLOCK)
       k_p2p32_m1(int n, const int* __restrict__ leaf_start, const int4* __restrict__ items,
                  const int* __restrict__ p2p_src, const float4* __restrict__ hi,
                  const float4* __restrict__ lo, const float* __restrict__ src, float damping,
                  float* __restrict__ Fnear) {
+  constexpr int TPT = 2 * NP;  // targets per thread
   __shared__ Src2 s_src[P2P_TILE];
   __shared__ TilePlan s_plan;
-  __shared__ float s_red[P2P_BLOCK * 6];
+  __shared__ float s_red[P2P_BLOCK * 3 * TPT];
 
   const int4 it = items[blockIdx.x];
   const int A = it.x, b0 = it.y, b1 = it.z, slot = it.w;
@@ -705,19 +708,23 @@ __global__ void __launch_bounds__(P2P_BLOCK)
                        (h.z - oh.z) + (l.z - ol.z), h.w > 0.f ? h.w : 1e15f);
   };
 
-  for (int tb = 0; tb < nA; tb += 2 * P2P_BLOCK) {
-    const int nT = min(2 * P2P_BLOCK, nA - tb);
-    const int T2 = (nT + 1) >> 1;
-    const int S  = P2P_BLOCK / T2;
-    const int t = threadIdx.x % T2, g = threadIdx.x / T2;
+  for (int tb = 0; tb < nA; tb += TPT * P2P_BLOCK) {
+    const int nT = min(TPT * P2P_BLOCK, nA - tb);
+    const int T  = (nT + TPT - 1) / TPT;  // threads per group
+    const int S  = P2P_BLOCK / T;         // groups
+    const int t = threadIdx.x % T, g = threadIdx.x / T;
     const bool active = g < S;
-    const bool has1   = t + T2 < nT;
-    const float4 me0 = rel(a0 + tb + t);
-    const float4 me1 = rel(a0 + tb + (has1 ? t + T2 : t));
-    const float2 nX = make_float2(-me0.x, -me1.x), nY = make_float2(-me0.y, -me1.y);
-    const float2 nZ = make_float2(-me0.z, -me1.z);
-    const float2 AI = make_float2(damping * me0.w, damping * me1.w);
-    Comp3<float> acc0, acc1;
+    float2 nX[NP], nY[NP], nZ[NP], AI[NP];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      const int k0 = t + 2 * p * T, k1 = t + (2 * p + 1) * T;
+      const float4 m0 = rel(a0 + tb + (k0 < nT ? k0 : t));
+      const float4 m1 = rel(a0 + tb + (k1 < nT ? k1 : t));
+      nX[p] = make_float2(-m0.x, -m1.x), nY[p] = make_float2(-m0.y, -m1.y);
+      nZ[p] = make_float2(-m0.z, -m1.z);
+      AI[p] = make_float2(damping * m0.w, damping * m1.w);
+    }
+    Comp3<float> acc[TPT];
     if (threadIdx.x == 0) s_plan.cur = b0, s_plan.coff = 0;
     __syncthreads();
     while (true) {
@@ -738,33 +745,44 @@ __global__ void __launch_bounds__(P2P_BLOCK)
       }
       __syncthreads();
       if (active) {
-        float2 FX = f2(0.f), FY = f2(0.f), FZ = f2(0.f);
+        float2 FX[NP], FY[NP], FZ[NP];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) FX[p] = FY[p] = FZ[p] = f2(0.f);
 #pragma unroll 4
         for (int jj = g; jj < total; jj += S) {
           const Src2 q = s_src[jj];
-          f32x2_pair_m1<DAMP>(nX, nY, nZ, AI, q, FX, FY, FZ);
+#pragma unroll
+          for (int p = 0; p < NP; ++p)
+            f32x2_pair_m1<DAMP>(nX[p], nY[p], nZ[p], AI[p], q, FX[p], FY[p], FZ[p]);
         }
-        acc0.add(FX.x, FY.x, FZ.x);
-        acc1.add(FX.y, FY.y, FZ.y);
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          acc[2 * p].add(FX[p].x, FY[p].x, FZ[p].x);
+          acc[2 * p + 1].add(FX[p].y, FY[p].y, FZ[p].y);
+        }
       }
       __syncthreads();
     }
     if (active) {
-      float* r = &s_red[(g * T2 + t) * 6];
-      r[0] = acc0.gx(), r[1] = acc0.gy(), r[2] = acc0.gz();
-      r[3] = acc1.gx(), r[4] = acc1.gy(), r[5] = acc1.gz();
+      float* r = &s_red[(g * T + t) * 3 * TPT];
+#pragma unroll
+      for (int k = 0; k < TPT; ++k)
+        r[3 * k] = acc[k].gx(), r[3 * k + 1] = acc[k].gy(), r[3 * k + 2] = acc[k].gz();
     }
     __syncthreads();
-    if (threadIdx.x < T2) {
-      float f[6] = {0, 0, 0, 0, 0, 0};
-      for (int gg = 0; gg < S; ++gg)
-#pragma unroll
-        for (int c = 0; c < 6; ++c) f[c] += s_red[(gg * T2 + threadIdx.x) * 6 + c];
-      float* o = Fnear + (size_t)slot * 3 * n + 3 * (size_t)(a0 + tb + threadIdx.x);
-      o[0] = f[0], o[1] = f[1], o[2] = f[2];
-      if (threadIdx.x + T2 < nT) {
-        float* o1 = Fnear + (size_t)slot * 3 * n + 3 * (size_t)(a0 + tb + threadIdx.x + T2);
-        o1[0] = f[3], o1[1] = f[4], o1[2] = f[5];
+    if (threadIdx.x < T) {
+      // target k of this thread is t + kk * T with kk the order of the packs'
+      // halves: (0, 1) for pack 0, (2, 3) for pack 1, ...
+      for (int k = 0; k < TPT; ++k) {
+        const int idx = threadIdx.x + k * T;
+        if (idx >= nT) continue;
+        float f0 = 0.f, f1 = 0.f, f2v = 0.f;
+        for (int gg = 0; gg < S; ++gg) {
+          const float* r = &s_red[(gg * T + threadIdx.x) * 3 * TPT + 3 * k];
+          f0 += r[0], f1 += r[1], f2v += r[2];
+        }
+        float* o = Fnear + (size_t)slot * 3 * n + 3 * (size_t)(a0 + tb + idx);
+        o[0] = f0, o[1] = f1, o[2] = f2v;
       }
     }
     __syncthreads();
@@ -1297,11 +1315,11 @@ static void launch_p2p(const Geometry& g, bool damp, bool fast, const T* src, T 
   const int grid = (int)g.h_items.size();
   if constexpr (std::is_same<T, float>::value && M == 1) {
     if (damp)
-      k_p2p32_m1<true><<<grid, P2P_BLOCK, 0, s>>>(g.n, g.leaf_start.p, g.items.p, g.p2p_src.p,
-                                                  g.hi32.p, g.lo32.p, src, damping, Fnear);
+      k_p2p32_m1<true, P2P32_NP><<<grid, P2P_BLOCK, 0, s>>>(
+            g.n, g.leaf_start.p, g.items.p, g.p2p_src.p, g.hi32.p, g.lo32.p, src, damping, Fnear);
     else
-      k_p2p32_m1<false><<<grid, P2P_BLOCK, 0, s>>>(g.n, g.leaf_start.p, g.items.p, g.p2p_src.p,
-                                                   g.hi32.p, g.lo32.p, src, damping, Fnear);
+      k_p2p32_m1<false, P2P32_NP><<<grid, P2P_BLOCK, 0, s>>>(
+            g.n, g.leaf_start.p, g.items.p, g.p2p_src.p, g.hi32.p, g.lo32.p, src, damping, Fnear);
     CG_LAUNCH();
     return;
   }
