@@ -89,3 +89,20 @@ def test_learned_guess_reduces_iterations(gpu):
             gained += it_p - it_l
             assert it_l <= it_p
     assert gained > 0
+
+
+def test_shipped_model_on_a_large_system(gpu):
+    """The shipped model drives a 75,000-site mixed solve (the learned
+    preconditioner's reductions span n/32 blocks) to the FP64 criterion."""
+    import os
+    from cppe_gb300 import learned, synthetic
+    path = os.path.join(os.path.dirname(__file__), "..", "cppe_gb300", "data", "learned_water.npz")
+    b = synthetic.water_box(25000, seed=41)
+    rhs = _rhs_for(b, 1, 5)[0]
+    s = cabi.System(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, summation=cabi.FMM, damp=True,
+                    precision=cabi.MIXED)
+    s.set_model(learned.load(path))
+    mu, it, _, _ = s.solve(rhs)
+    s.set_model(None)
+    s64 = cabi.System(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, summation=cabi.FMM, damp=True)
+    assert np.linalg.norm(rhs - s64.apply(mu)) < 1e-8
