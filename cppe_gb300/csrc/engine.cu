@@ -622,8 +622,9 @@ __global__ void __launch_bounds__(P2P_BLOCK)
 //    source - target (the dipole field is even in r).
 //  - Damped: 1/R is capped at 1e4 (real pairs have R > 1e-4 bohr), which
 //    turns the self pair (R = 0, v = 0, f_E = f_T = 0) into an exact zero
-//    without a branch; sources without a damping partner (s = 0) are staged
-//    with s = 1e15, i.e. e^-v = 0 and f = 1.
+//    without a branch; sites without a damping partner (s = 0) are staged
+//    with s = 1e15, i.e. e^-v = 0 and f = 1 (the exponent is clamped at
+//    2^-126 so that the damping polynomials stay finite).
 //  - Undamped: the self pair is removed by a select on R^2 > 0.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
@@ -632,6 +633,19 @@ __device__ __forceinline__ float ex2_approx(float x) {
   asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
   return y;
 }
+// 1/sqrt(x) as one MUFU operation (inputs are squared distances: never
+// subnormal; 0 gives +inf)
+__device__ __forceinline__ float rsqrt_approx(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+// ln 2 and the products of its powers that the damping polynomials take in
+// t = -v log2(e)
+constexpr float LN2       = 0.6931471805599453f;
+constexpr float LN2SQ_2   = 0.2402265069591007f;   // (ln 2)^2 / 2
+constexpr float LN2SQ_3_2 = 0.7206795208773021f;   // 3 (ln 2)^2 / 2
+constexpr float LN2CU_2   = 0.16651232599446472f;  // (ln 2)^3 / 2
 
 struct Src2 {
   float4 xy;  // x, x, y, y
@@ -651,27 +665,31 @@ __device__ __forceinline__ void f32x2_pair_m1(const float2& nX, const float2& nY
   const float2 r2 = __ffma2_rn(x, x, __ffma2_rn(y, y, __fmul2_rn(z, z)));
   float2 ir;
   if (DAMP) {
-    ir.x = fminf(rsqrtf(r2.x), 1e4f);
-    ir.y = fminf(rsqrtf(r2.y), 1e4f);
+    ir.x = fminf(rsqrt_approx(r2.x), 1e4f);
+    ir.y = fminf(rsqrt_approx(r2.y), 1e4f);
   } else {
-    ir.x = r2.x > 0.f ? rsqrtf(r2.x) : 0.f;
-    ir.y = r2.y > 0.f ? rsqrtf(r2.y) : 0.f;
+    ir.x = r2.x > 0.f ? rsqrt_approx(r2.x) : 0.f;
+    ir.y = r2.y > 0.f ? rsqrt_approx(r2.y) : 0.f;
   }
   const float2 ir2 = __fmul2_rn(ir, ir);
   const float2 ir3 = __fmul2_rn(ir2, ir);
   const float2 ir5 = __fmul2_rn(ir3, ir2);
   float2 A, Bn;  // field = mu A - r (mu.r) B, Bn = -B
   if (DAMP) {
-    const float2 a  = __fmul2_rn(AI, make_float2(q.zs.z, q.zs.w));
-    const float2 v  = __fmul2_rn(a, __fmul2_rn(r2, ir));
-    const float2 t  = __fmul2_rn(v, f2(-1.4426950408889634f));
+    // t = -v log2(e) with v = damping s_i s_j R (AI = -log2(e) damping s_i);
+    // with v = -t ln 2 the damping functions are
+    //   f_E = 1 - e^-v (1 + v + v^2/2)          = 1 + e np,
+    //   f_T = 1 - e^-v (1 + v + v^2/2 + v^3/6)  = 1 - e q3 / 3,
+    // np = -1 + t ln2 - t^2 ln2^2/2, q3 = 3 - 3 t ln2 + 3 t^2 ln2^2/2 - t^3 ln2^3/2
+    float2 t = __fmul2_rn(__fmul2_rn(AI, make_float2(q.zs.z, q.zs.w)), __fmul2_rn(r2, ir));
+    t.x = fmaxf(t.x, -126.f);
+    t.y = fmaxf(t.y, -126.f);
     const float2 e  = make_float2(ex2_approx(t.x), ex2_approx(t.y));
-    const float2 p  = __ffma2_rn(v, __ffma2_rn(v, f2(0.5f), f2(1.f)), f2(1.f));
-    const float2 d1 = __fmul2_rn(p, e);  // 1 - f_E
-    const float2 w  = __fmul2_rn(__fmul2_rn(__fmul2_rn(v, v), f2(1.f / 6.f)), v);
-    const float2 d2 = __ffma2_rn(w, e, d1);  // 1 - f_T
-    A  = __fmul2_rn(ir3, __ffma2_rn(d1, f2(-1.f), f2(1.f)));
-    Bn = __fmul2_rn(ir5, __ffma2_rn(d2, f2(3.f), f2(-3.f)));
+    const float2 np = __ffma2_rn(t, __ffma2_rn(t, f2(-LN2SQ_2), f2(LN2)), f2(-1.f));
+    const float2 q3 = __ffma2_rn(
+          t, __ffma2_rn(t, __ffma2_rn(t, f2(-LN2CU_2), f2(LN2SQ_3_2)), f2(-3.f * LN2)), f2(3.f));
+    A  = __fmul2_rn(ir3, __ffma2_rn(np, e, f2(1.f)));   // R^-3 f_E
+    Bn = __fmul2_rn(ir5, __ffma2_rn(q3, e, f2(-3.f)));  // -3 R^-5 f_T
   } else {
     A  = ir3;
     Bn = __fmul2_rn(ir5, f2(-3.f));
@@ -722,7 +740,8 @@ __global__ void __launch_bounds__(P2P_BLOCK)
       const float4 m1 = rel(a0 + tb + (k1 < nT ? k1 : t));
       nX[p] = make_float2(-m0.x, -m1.x), nY[p] = make_float2(-m0.y, -m1.y);
       nZ[p] = make_float2(-m0.z, -m1.z);
-      AI[p] = make_float2(damping * m0.w, damping * m1.w);
+      AI[p] = make_float2(-1.4426950408889634f * damping * m0.w,
+                          -1.4426950408889634f * damping * m1.w);
     }
     Comp3<float> acc[TPT];
     if (threadIdx.x == 0) s_plan.cur = b0, s_plan.coff = 0;
