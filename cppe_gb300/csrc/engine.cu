@@ -465,7 +465,7 @@ struct Comp3<float> {
 // Tile planning of the near-field pass.  An item covers positions [cur, b1)
 // of its target leaf's P2P list; each round warp 0 takes the next (up to) 32
 // source leaves, prefix-sums their sizes across the warp and keeps those that
-// start inside a tile of P2P_TILE sites, the last one possibly in part
+// start inside a tile of TILE sites, the last one possibly in part
 // (`coff` sites of the first leaf were taken by the previous round).
 // ---------------------------------------------------------------------------
 struct TilePlan {
@@ -474,6 +474,7 @@ struct TilePlan {
   int np, cur, coff;
 };
 
+template <int TILE = P2P_TILE>
 __device__ __forceinline__ void plan_tile(TilePlan& tp, int b1, const int* __restrict__ p2p_src,
                                           const int* __restrict__ leaf_start) {
   const int lane = threadIdx.x & 31;
@@ -493,8 +494,8 @@ __device__ __forceinline__ void plan_tile(TilePlan& tp, int b1, const int* __res
     if (lane >= o) incl += v;
   }
   const int excl     = incl - cnt;
-  const bool take    = e < b1 && excl < P2P_TILE;
-  const int takecnt  = take ? min(cnt, P2P_TILE - excl) : 0;
+  const bool take    = e < b1 && excl < TILE;
+  const int takecnt  = take ? min(cnt, TILE - excl) : 0;
   const unsigned msk = __ballot_sync(0xffffffffu, take);
   const int np       = __popc(msk);
   const int last     = max(np - 1, 0);
@@ -612,11 +613,12 @@ __global__ void __launch_bounds__(P2P_BLOCK)
 
 // ---------------------------------------------------------------------------
 // Near field, FP32, dipole sources: the inner pass of the mixed solver.
-// Each thread evaluates two targets of the leaf against one staged source
-// per step with packed FP32x2 arithmetic (__ffma2_rn / __fmul2_rn /
-// __fadd2_rn, sm_100 and later): the two targets occupy the two halves of
-// every float2, and the source is staged pre-broadcast ({x, x, y, y} ...), so
-// a pair costs about half the issue slots of scalar code.
+// Packed FP32x2 arithmetic (__ffma2_rn / __fmul2_rn / __fadd2_rn, sm_100 and
+// later) evaluates one target against two sources per instruction: sources
+// are staged in pairs ({x_j, x_j+1, y_j, y_j+1}, ... in four SoA arrays), the
+// target's coordinates are broadcast into both halves once, and each thread
+// serves two targets, so every pair of staged sources read from shared
+// memory feeds four pair evaluations.
 //  - Positions are relative to the first site of the target leaf, formed once
 //    per staged source from the hi/lo coordinates; separations are taken as
 //    source - target (the dipole field is even in r).
@@ -647,11 +649,12 @@ constexpr float LN2SQ_2   = 0.2402265069591007f;   // (ln 2)^2 / 2
 constexpr float LN2SQ_3_2 = 0.7206795208773021f;   // 3 (ln 2)^2 / 2
 constexpr float LN2CU_2   = 0.16651232599446472f;  // (ln 2)^3 / 2
 
+// two sources in the halves of packed operands
 struct Src2 {
-  float4 xy;  // x, x, y, y
-  float4 zs;  // z, z, s, s
-  float4 mxy; // mx, mx, my, my
-  float2 mz;  // mz, mz
+  float4 xy;   // x_j, x_j+1, y_j, y_j+1
+  float4 zs;   // z_j, z_j+1, s_j, s_j+1
+  float4 mxy;  // mx_j, mx_j+1, my_j, my_j+1
+  float2 mz;   // mz_j, mz_j+1
 };
 
 template <bool DAMP>
@@ -703,18 +706,20 @@ __device__ __forceinline__ void f32x2_pair_m1(const float2& nX, const float2& nY
   FZ = __ffma2_rn(z, nC, __ffma2_rn(mz, A, FZ));
 }
 
-// NP packs of two targets per thread (NP = 1: two targets).
-constexpr int P2P32_NP = 1;
-template <bool DAMP, int NP>
+constexpr int P2P32_PAIRS = 512;  // staged source pairs per tile (1,024 sources)
+template <bool DAMP>
 __global__ void __launch_bounds__(P2P_BLOCK)
       k_p2p32_m1(int n, const int* __restrict__ leaf_start, const int4* __restrict__ items,
                  const int* __restrict__ p2p_src, const float4* __restrict__ hi,
                  const float4* __restrict__ lo, const float* __restrict__ src, float damping,
                  float* __restrict__ Fnear) {
-  constexpr int TPT = 2 * NP;  // targets per thread
-  __shared__ Src2 s_src[P2P_TILE];
+  constexpr int TILE = 2 * P2P32_PAIRS;
+  __shared__ float4 s_xy[P2P32_PAIRS];   // x_j, x_j+1, y_j, y_j+1
+  __shared__ float4 s_zs[P2P32_PAIRS];   // z_j, z_j+1, s_j, s_j+1
+  __shared__ float4 s_mxy[P2P32_PAIRS];  // mx_j, mx_j+1, my_j, my_j+1
+  __shared__ float2 s_mz[P2P32_PAIRS];   // mz_j, mz_j+1
   __shared__ TilePlan s_plan;
-  __shared__ float s_red[P2P_BLOCK * 3 * TPT];
+  __shared__ float s_red[P2P_BLOCK * 6];
 
   const int4 it = items[blockIdx.x];
   const int A = it.x, b0 = it.y, b1 = it.z, slot = it.w;
@@ -726,78 +731,80 @@ __global__ void __launch_bounds__(P2P_BLOCK)
                        (h.z - oh.z) + (l.z - ol.z), h.w > 0.f ? h.w : 1e15f);
   };
 
-  for (int tb = 0; tb < nA; tb += TPT * P2P_BLOCK) {
-    const int nT = min(TPT * P2P_BLOCK, nA - tb);
-    const int T  = (nT + TPT - 1) / TPT;  // threads per group
-    const int S  = P2P_BLOCK / T;         // groups
+  for (int tb = 0; tb < nA; tb += 2 * P2P_BLOCK) {
+    const int nT = min(2 * P2P_BLOCK, nA - tb);
+    const int T  = (nT + 1) >> 1;  // threads per group
+    const int S  = P2P_BLOCK / T;  // groups
     const int t = threadIdx.x % T, g = threadIdx.x / T;
     const bool active = g < S;
-    float2 nX[NP], nY[NP], nZ[NP], AI[NP];
+    float2 nX[2], nY[2], nZ[2], AI[2];
 #pragma unroll
-    for (int p = 0; p < NP; ++p) {
-      const int k0 = t + 2 * p * T, k1 = t + (2 * p + 1) * T;
-      const float4 m0 = rel(a0 + tb + (k0 < nT ? k0 : t));
-      const float4 m1 = rel(a0 + tb + (k1 < nT ? k1 : t));
-      nX[p] = make_float2(-m0.x, -m1.x), nY[p] = make_float2(-m0.y, -m1.y);
-      nZ[p] = make_float2(-m0.z, -m1.z);
-      AI[p] = make_float2(-1.4426950408889634f * damping * m0.w,
-                          -1.4426950408889634f * damping * m1.w);
+    for (int p = 0; p < 2; ++p) {
+      const int k    = t + p * T;
+      const float4 m = rel(a0 + tb + (k < nT ? k : t));
+      nX[p] = f2(-m.x), nY[p] = f2(-m.y), nZ[p] = f2(-m.z);
+      AI[p] = f2(-1.4426950408889634f * damping * m.w);
     }
-    Comp3<float> acc[TPT];
+    Comp3<float> acc[2];
     if (threadIdx.x == 0) s_plan.cur = b0, s_plan.coff = 0;
     __syncthreads();
     while (true) {
-      if (threadIdx.x < 32) plan_tile(s_plan, b1, p2p_src, leaf_start);
+      if (threadIdx.x < 32) plan_tile<TILE>(s_plan, b1, p2p_src, leaf_start);
       __syncthreads();
       const int np = s_plan.np;
       if (np == 0) break;
-      const int total = s_plan.poff[np];
-      for (int q = threadIdx.x; q < total; q += P2P_BLOCK) {
-        const int j    = tile_site(s_plan, q);
-        const float4 r = rel(j);
-        const float mx = src[3 * (size_t)j], my = src[3 * (size_t)j + 1],
-                    mz = src[3 * (size_t)j + 2];
-        s_src[q].xy  = make_float4(r.x, r.x, r.y, r.y);
-        s_src[q].zs  = make_float4(r.z, r.z, r.w, r.w);
-        s_src[q].mxy = make_float4(mx, mx, my, my);
-        s_src[q].mz  = make_float2(mz, mz);
+      const int total  = s_plan.poff[np];
+      const int npairs = (total + 1) >> 1;
+      for (int q = threadIdx.x; q < npairs; q += P2P_BLOCK) {
+        const int j0 = tile_site(s_plan, 2 * q);
+        const float4 r0 = rel(j0);
+        const float mx0 = src[3 * (size_t)j0], my0 = src[3 * (size_t)j0 + 1],
+                    mz0 = src[3 * (size_t)j0 + 2];
+        // an odd tile ends with a source of zero moment far from the leaf
+        float4 r1 = make_float4(1e4f, 0.f, 0.f, 1.f);
+        float mx1 = 0.f, my1 = 0.f, mz1 = 0.f;
+        if (2 * q + 1 < total) {
+          const int j1 = tile_site(s_plan, 2 * q + 1);
+          r1 = rel(j1);
+          mx1 = src[3 * (size_t)j1], my1 = src[3 * (size_t)j1 + 1], mz1 = src[3 * (size_t)j1 + 2];
+        }
+        s_xy[q]  = make_float4(r0.x, r1.x, r0.y, r1.y);
+        s_zs[q]  = make_float4(r0.z, r1.z, r0.w, r1.w);
+        s_mxy[q] = make_float4(mx0, mx1, my0, my1);
+        s_mz[q]  = make_float2(mz0, mz1);
       }
       __syncthreads();
       if (active) {
-        float2 FX[NP], FY[NP], FZ[NP];
+        float2 FX[2], FY[2], FZ[2];
 #pragma unroll
-        for (int p = 0; p < NP; ++p) FX[p] = FY[p] = FZ[p] = f2(0.f);
-#pragma unroll 4
-        for (int jj = g; jj < total; jj += S) {
-          const Src2 q = s_src[jj];
+        for (int p = 0; p < 2; ++p) FX[p] = FY[p] = FZ[p] = f2(0.f);
+#pragma unroll 1
+        for (int jj = g; jj < npairs; jj += S) {
+          Src2 q;
+          q.xy = s_xy[jj], q.zs = s_zs[jj], q.mxy = s_mxy[jj], q.mz = s_mz[jj];
 #pragma unroll
-          for (int p = 0; p < NP; ++p)
+          for (int p = 0; p < 2; ++p)
             f32x2_pair_m1<DAMP>(nX[p], nY[p], nZ[p], AI[p], q, FX[p], FY[p], FZ[p]);
         }
 #pragma unroll
-        for (int p = 0; p < NP; ++p) {
-          acc[2 * p].add(FX[p].x, FY[p].x, FZ[p].x);
-          acc[2 * p + 1].add(FX[p].y, FY[p].y, FZ[p].y);
-        }
+        for (int p = 0; p < 2; ++p) acc[p].add(FX[p].x + FX[p].y, FY[p].x + FY[p].y, FZ[p].x + FZ[p].y);
       }
       __syncthreads();
     }
     if (active) {
-      float* r = &s_red[(g * T + t) * 3 * TPT];
+      float* r = &s_red[(g * T + t) * 6];
 #pragma unroll
-      for (int k = 0; k < TPT; ++k)
+      for (int k = 0; k < 2; ++k)
         r[3 * k] = acc[k].gx(), r[3 * k + 1] = acc[k].gy(), r[3 * k + 2] = acc[k].gz();
     }
     __syncthreads();
     if (threadIdx.x < T) {
-      // target k of this thread is t + kk * T with kk the order of the packs'
-      // halves: (0, 1) for pack 0, (2, 3) for pack 1, ...
-      for (int k = 0; k < TPT; ++k) {
+      for (int k = 0; k < 2; ++k) {
         const int idx = threadIdx.x + k * T;
         if (idx >= nT) continue;
         float f0 = 0.f, f1 = 0.f, f2v = 0.f;
         for (int gg = 0; gg < S; ++gg) {
-          const float* r = &s_red[(gg * T + threadIdx.x) * 3 * TPT + 3 * k];
+          const float* r = &s_red[(gg * T + threadIdx.x) * 6 + 3 * k];
           f0 += r[0], f1 += r[1], f2v += r[2];
         }
         float* o = Fnear + (size_t)slot * 3 * n + 3 * (size_t)(a0 + tb + idx);
@@ -1334,10 +1341,10 @@ static void launch_p2p(const Geometry& g, bool damp, bool fast, const T* src, T 
   const int grid = (int)g.h_items.size();
   if constexpr (std::is_same<T, float>::value && M == 1) {
     if (damp)
-      k_p2p32_m1<true, P2P32_NP><<<grid, P2P_BLOCK, 0, s>>>(
+      k_p2p32_m1<true><<<grid, P2P_BLOCK, 0, s>>>(
             g.n, g.leaf_start.p, g.items.p, g.p2p_src.p, g.hi32.p, g.lo32.p, src, damping, Fnear);
     else
-      k_p2p32_m1<false, P2P32_NP><<<grid, P2P_BLOCK, 0, s>>>(
+      k_p2p32_m1<false><<<grid, P2P_BLOCK, 0, s>>>(
             g.n, g.leaf_start.p, g.items.p, g.p2p_src.p, g.hi32.p, g.lo32.p, src, damping, Fnear);
     CG_LAUNCH();
     return;
