@@ -340,6 +340,8 @@ def large_section(cfg, dev, flush, model_path=None, zero_guess=True):
         out["plain_fp64_zero_guess"] = {"s": tz, "iterations": stz["fp64_applies"]}
     Bmu64 = s64.apply(mu64)
     smx = capi.System(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, precision=capi.MIXED, **kw)
+    t0 = time.perf_counter()
+    out["autotune"] = {"apply_ms": smx.autotune(2), "s": time.perf_counter() - t0}  # set-up
     timed(smx)  # warm-up (first-use allocations)
     variants = [("mixed", None)]
     if model_path and os.path.exists(model_path):

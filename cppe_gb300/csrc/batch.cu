@@ -506,7 +506,7 @@ int BatchSystem::solve_device(const double* d_rhs, double* d_mu, int* iters_out)
     bool exact = false;
     for (int outer = 0; outer < 12; ++outer) {
       // inner tolerances; segments already below the threshold stay put
-      for (int g = 0; g < nseg; ++g) tolv[g] = std::max(eta * rn[g], 0.25 * t);
+      for (int g = 0; g < nseg; ++g) tolv[g] = std::max(eta * rn[g], 0.5 * t);
       if (outer > 0) {
         if (std::all_of(rn.begin(), rn.end(), [&](double v) { return v < t; })) {
           status = CPPE_GPU_OK;

@@ -1363,19 +1363,28 @@ static void launch_p2p(const Geometry& g, bool damp, bool fast, const T* src, T 
 }
 
 void SideStream::create() {
-  // highest priority: the short far-field chain is scheduled ahead of the
-  // near-field pass's blocks instead of after them
+  // By default the far-field chain runs at the highest priority: where it is
+  // shorter than the near-field pass (a chain of small, latency-bound
+  // kernels) its blocks are scheduled ahead of the near field's instead of
+  // after them.  Where the chain is the longer part (high orders, large
+  // systems) the default priority lets the two share the GPU better; the
+  // schedule tuner picks between them by measurement.
   int least = 0, greatest = 0;
   CG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
-  CG_CUDA(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, greatest));
+  CG_CUDA(cudaStreamCreateWithPriority(&hi, cudaStreamNonBlocking, greatest));
+  CG_CUDA(cudaStreamCreateWithPriority(&lo, cudaStreamNonBlocking, least));
+  s = hi;
   CG_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
   CG_CUDA(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
 }
 void SideStream::destroy() {
+  if (hi) cudaStreamSynchronize(hi);
+  if (lo) cudaStreamSynchronize(lo);
   if (join) cudaEventDestroy(join);
   if (fork) cudaEventDestroy(fork);
-  if (s) cudaStreamDestroy(s);
-  s = nullptr, fork = join = nullptr;
+  if (hi) cudaStreamDestroy(hi);
+  if (lo) cudaStreamDestroy(lo);
+  s = hi = lo = nullptr, fork = join = nullptr;
 }
 
 __global__ void k_split_dd_vec(long n, const double* __restrict__ in, float2* __restrict__ out) {

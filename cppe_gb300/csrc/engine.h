@@ -183,11 +183,14 @@ struct PhaseEvents {
 // A second stream for the far-field passes (P2M, M2M, M2L, L2L), which run
 // concurrently with the near-field pass and join before the finishing pass.
 struct SideStream {
-  cudaStream_t s     = nullptr;
+  cudaStream_t s     = nullptr;  // the stream in use: hi (default) or lo
+  cudaStream_t hi    = nullptr;  // highest priority
+  cudaStream_t lo    = nullptr;  // lowest priority (that of the default stream)
   cudaEvent_t fork   = nullptr;
   cudaEvent_t join   = nullptr;
   void create();
   void destroy();
+  void use_high_priority(bool h) { s = h ? hi : lo; }
 };
 
 // Arithmetic of the near-field pass of an FP64 evaluation.

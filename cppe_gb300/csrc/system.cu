@@ -347,12 +347,29 @@ double System::autotune(int reps) {
       CG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
       if (ms / reps < best) best = ms / reps, best_w = w, best_c = chs[ci];
     }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   geo.item_pairs = best_w;
   geo.m2l_chunk  = best_c;
   geo.make_schedules();
   geo.upload_schedules(stream);
+  // priority of the far-field stream under the chosen schedule
+  if (geo.fmm) {
+    double t_side[2] = {0.0, 0.0};  // high, default priority
+    for (int k = 0; k < 2; ++k) {
+      side.use_high_priority(k == 0);
+      apply32(p32.p, Ap32.p, false);
+      CG_CUDA(cudaEventRecord(e0, stream));
+      for (int r = 0; r < reps; ++r) apply32(p32.p, Ap32.p, false);
+      CG_CUDA(cudaEventRecord(e1, stream));
+      CG_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      CG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      t_side[k] = ms / reps;
+    }
+    side.use_high_priority(t_side[0] <= t_side[1]);
+    best = std::min(t_side[0], t_side[1]);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
   CG_CUDA(cudaStreamSynchronize(stream));
   // captured inner loops hold the old schedule's buffers: rebuild on next use
   for (auto& e : inner_exec)
@@ -598,7 +615,10 @@ int System::solve_mixed(bool zero_guess, double* hist_out, int hist_cap, int* it
       rnorm = h_scal[S_RNORM];
     }
     have_inner_start = false;
-    const double tol = std::max(eta * rnorm, 0.25 * t);
+    // the last inner solve stops at half the threshold: the FP64 residual it
+    // leaves differs from the FP32 recursion's by ~1e-7 of the correction
+    // (far below the other half)
+    const double tol = std::max(eta * rnorm, 0.5 * t);
     // the threshold of this inner solve goes to the device; the loop itself
     // runs as one graph launch (device-side while loop)
     h_scal[S_TOL] = tol;

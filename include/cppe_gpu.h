@@ -243,8 +243,10 @@ int cppe_gpu_kernel_timings(cppe_gpu_system* sys, int precision, int reps, doubl
                             long long* near_pairs, long long* m2l_pairs);
 /* Schedule autotuning (no reference counterpart): times the FP32 operator for
  * three near-field work-item sizes and three M2L chunk sizes on this system
- * and keeps the fastest; best_ms (may be null) receives its apply time.  The
- * operator is unchanged; only the work partition differs. */
+ * and keeps the fastest, then the faster of the two priorities of the
+ * far-field stream (highest, default); best_ms (may be null) receives its
+ * apply time.  The operator is unchanged; only the work partition and the
+ * stream scheduling differ. */
 int cppe_gpu_autotune(cppe_gpu_system* sys, int reps, double* best_ms);
 /* Measured FMA throughput of the device in TFLOP/s (2 FLOP per FMA), FP32 or FP64. */
 int cppe_gpu_fma_peak(int device, int fp64, double* tflops);
