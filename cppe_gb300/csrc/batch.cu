@@ -253,14 +253,18 @@ __global__ void k_bcg_dir(int n, const int* __restrict__ site_seg, const T* __re
 
 __global__ void k_bres(int n, const double* __restrict__ F, const double* __restrict__ Ax,
                        const float* __restrict__ Bd, double* __restrict__ r,
-                       double* __restrict__ s_rr) {
-  // r = F - Ax (Ax given) or r -= Bd (Bd given); site values of r.r
+                       double* __restrict__ s_rr, const float* __restrict__ r32 = nullptr) {
+  // r = F - Ax (Ax given), r -= Bd (Bd given) or r = (r - fl(r)) + r32 (the
+  // inner solve's final residual r32 for the right-hand side fl(r)); site
+  // values of r.r
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double rr = 0;
   for (int c = 0; c < 3; ++c) {
     const size_t k = 3 * (size_t)i + c;
-    const double v = Ax ? F[k] - Ax[k] : r[k] - (double)Bd[k];
+    const double v = Ax   ? F[k] - Ax[k]
+                     : Bd ? r[k] - (double)Bd[k]
+                          : (r[k] - (double)(float)r[k]) + (double)r32[k];
     r[k]           = v;
     rr += v * v;
   }
@@ -529,7 +533,13 @@ int BatchSystem::solve_device(const double* d_rhs, double* d_mu, int* iters_out)
       CG_CUDA(cudaMemcpyAsync(it_h.data(), iters.p, nseg * sizeof(int), cudaMemcpyDeviceToHost,
                               stream));
       const double rmax = *std::max_element(rn.begin(), rn.end());
-      if (!(exact && rmax * 1e-4 < t)) {
+      if (exact && rmax * 1e-6 < 1e-3 * t) {
+        // residual from the inner recursion (as System::solve_mixed)
+        k_bres<<<nb, BB, 0, stream>>>(n, nullptr, nullptr, nullptr, r.p, site_b.p, r32.p);
+        CG_LAUNCH();
+        k_bacc<<<nb3, BB, 0, stream>>>(n3, x.p, d32.p);
+        CG_LAUNCH();
+      } else if (!(exact && rmax * 1e-4 < t)) {
         k_bacc<<<nb3, BB, 0, stream>>>(n3, x.p, d32.p);
         CG_LAUNCH();
         apply_seg<double>(x.p, Ap.p, NEAR_DD);

@@ -139,6 +139,22 @@ __global__ void k_residual_update(int n3, const float* __restrict__ Bd, double* 
   if (grid_sum_last<1>(v, sh, rs.partials, rs.ticket, rs.out)) scal[S_RNORM] = sqrt(rs.out[0]);
 }
 
+// r = (r - fl(r)) + r32: the FP64 residual after an inner solve whose
+// right-hand side was fl(r) (r rounded to FP32), from the inner solve's own
+// final residual r32; ||r||.
+__global__ void k_residual_inner(int n3, const float* __restrict__ r32, double* __restrict__ r,
+                                 ReduceSlots rs, double* scal) {
+  __shared__ double sh[32];
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  double v[1] = {0.0};
+  if (k < n3) {
+    const double d = (r[k] - (double)(float)r[k]) + (double)r32[k];
+    r[k]           = d;
+    v[0]           = d * d;
+  }
+  if (grid_sum_last<1>(v, sh, rs.partials, rs.ticket, rs.out)) scal[S_RNORM] = sqrt(rs.out[0]);
+}
+
 // x += d (FP64 += FP32); d is then cleared.
 __global__ void k_accumulate(int n3, double* __restrict__ x, float* __restrict__ d) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -629,10 +645,18 @@ int System::solve_mixed(bool zero_guess, double* hist_out, int hist_cap, int* it
     CG_CUDA(cudaStreamSynchronize(stream));
     total_inner += h_flags[1];
     last.fp32_applies += h_flags[1];
-    // An FP32 update of the residual errs by ~1e-7 ||B d|| ~ 1e-7 ||r||; it is
-    // used only on top of an exact residual small enough that this error is
-    // below 1e-3 of the threshold.
-    if (!(have_fp64_residual && rnorm * 1e-4 < t)) {
+    // After an exact residual r, the inner solve's B d = fl(r) - r32 is known
+    // from its own recursion to ~1e-6 ||r|| (FP32 operator and rounding of
+    // the updates); where that is below 1e-3 of the threshold the residual
+    // is formed from r32 without another apply.  Else an FP32 apply of d
+    // (error ~1e-7 ||B d|| ~ 1e-7 ||r||) where that is small enough, else the
+    // FP64 operator.
+    if (have_fp64_residual && rnorm * 1e-6 < 1e-3 * t) {
+      k_residual_inner<<<nb3, VB, 0, stream>>>(n3, r32.p, r.p, slots(S_RED), scal.p);
+      CG_LAUNCH();
+      k_accumulate<<<nb3, VB, 0, stream>>>(n3, x.p, d32.p);
+      CG_LAUNCH();
+    } else if (!(have_fp64_residual && rnorm * 1e-4 < t)) {
       // x += d; r = F - B64 x: the residual recomputed with the FP64 operator
       k_accumulate<<<nb3, VB, 0, stream>>>(n3, x.p, d32.p);
       CG_LAUNCH();
