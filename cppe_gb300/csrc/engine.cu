@@ -1131,6 +1131,125 @@ __global__ void __launch_bounds__(128)
   if (row < ov.lsize) Lleaf[(size_t)leaf * ov.lsize + row] = acc;
 }
 
+// ---------------------------------------------------------------------------
+// The same passes for dipole sources at the orders with straight-line
+// operators (m2l_gen.cuh): every thread applies a whole operator (all rows)
+// with the powers, monomials and accumulators in registers, instead of one
+// table-driven row per thread.
+//  - P2M: block per leaf; thread t takes sites t, t + 64, ...; the threads'
+//    expansions are added in thread order through shared memory.
+//  - M2M: eight tasks per block, a thread per task leaf; the leaves' shifts
+//    of a task are added in leaf order.
+//  - L2L: thread per leaf, its M2L-only ancestors in order.
+// ---------------------------------------------------------------------------
+constexpr int SHIFT_THREADS = 64;
+template <int P>
+struct Shifts;
+#define CPPE_DEF_SHIFTS(MM, PP, LS, MS)                                                          \
+  template <>                                                                                   \
+  struct Shifts<PP> {                                                                           \
+    static constexpr int ls = LS, ms = MS;                                                      \
+    template <typename T>                                                                       \
+    __device__ static void p2m(T x, T y, T z, T s0, T s1, T s2, T* acc) {                      \
+      p2m_m1_p##PP<T>(x, y, z, s0, s1, s2, acc);                                                \
+    }                                                                                           \
+    template <typename T>                                                                       \
+    __device__ static void m2m(T x, T y, T z, const T* Mc, T* acc) {                           \
+      m2m_m1_p##PP<T>(x, y, z, Mc, acc);                                                        \
+    }                                                                                           \
+    template <typename T>                                                                       \
+    __device__ static void l2l(T x, T y, T z, const T* Lc, T* acc) {                           \
+      l2l_m1_p##PP<T>(x, y, z, Lc, acc);                                                        \
+    }                                                                                           \
+    template <typename T>                                                                       \
+    __device__ static void l2p(T x, T y, T z, const T* Lc, T& f0, T& f1, T& f2) {              \
+      l2p_m1_p##PP<T>(x, y, z, Lc, f0, f1, f2);                                                 \
+    }                                                                                           \
+  };
+CPPE_SHIFTS_GENERATED(CPPE_DEF_SHIFTS)
+#undef CPPE_DEF_SHIFTS
+
+template <typename T, int P>
+__global__ void __launch_bounds__(SHIFT_THREADS)
+      k_p2m_leaf_fixed(TreeView tv, CellPos<T> cp, const T* __restrict__ src, T* __restrict__ M) {
+  constexpr int MS = Shifts<P>::ms;
+  __shared__ T s_part[SHIFT_THREADS * (MS + 1)];
+  const int leaf = blockIdx.x, cell = tv.leaf_cell[leaf];
+  const int a0 = tv.leaf_start[leaf], a1 = tv.leaf_start[leaf + 1];
+  T acc[MS];
+#pragma unroll
+  for (int r = 0; r < MS; ++r) acc[r] = T(0);
+  for (int q = a0 + (int)threadIdx.x; q < a1; q += SHIFT_THREADS) {
+    T x, y, z;
+    cp.d(cell, q, x, y, z);
+    const T* sq = src + 3 * (size_t)q;
+    Shifts<P>::p2m(x, y, z, sq[0], sq[1], sq[2], acc);
+  }
+#pragma unroll
+  for (int r = 0; r < MS; ++r) s_part[threadIdx.x * (MS + 1) + r] = acc[r];
+  __syncthreads();
+  for (int r = threadIdx.x; r < MS; r += SHIFT_THREADS) {
+    T v = T(0);
+    for (int t = 0; t < SHIFT_THREADS; ++t) v += s_part[t * (MS + 1) + r];
+    M[(size_t)cell * MS + r] = v;
+  }
+}
+
+template <typename T, int P>
+__global__ void __launch_bounds__(SHIFT_THREADS)
+      k_m2m_tasks_fixed(TreeView tv, const int4* __restrict__ tasks, int ntask,
+                        const int* __restrict__ task_leaf, CellPos<T> cp, const T* __restrict__ M,
+                        T* __restrict__ Mpart) {
+  constexpr int MS  = Shifts<P>::ms;
+  constexpr int TPB = SHIFT_THREADS / M2M_TASK_LEAVES;  // tasks per block
+  __shared__ T s_part[SHIFT_THREADS * (MS + 1)];
+  const int g = threadIdx.x / M2M_TASK_LEAVES, sl = threadIdx.x % M2M_TASK_LEAVES;
+  const int task = blockIdx.x * TPB + g;
+  T acc[MS];
+#pragma unroll
+  for (int r = 0; r < MS; ++r) acc[r] = T(0);
+  if (task < ntask) {
+    const int4 tk = tasks[task];
+    if (tk.y + sl < tk.z) {
+      const int lc = tv.leaf_cell[task_leaf[tk.y + sl]];
+      T x, y, z;
+      centre_diff<T>(tv, cp, tk.x, lc, x, y, z);
+      Shifts<P>::m2m(x, y, z, M + (size_t)lc * MS, acc);
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < MS; ++r) s_part[threadIdx.x * (MS + 1) + r] = acc[r];
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < TPB * MS; idx += SHIFT_THREADS) {
+    const int gg = idx / MS, r = idx - gg * MS, tsk = blockIdx.x * TPB + gg;
+    if (tsk >= ntask) continue;
+    T v = T(0);
+    for (int k = 0; k < M2M_TASK_LEAVES; ++k) v += s_part[(gg * M2M_TASK_LEAVES + k) * (MS + 1) + r];
+    Mpart[(size_t)tsk * MS + r] = v;
+  }
+}
+
+template <typename T, int P>
+__global__ void __launch_bounds__(SHIFT_THREADS)
+      k_l2l_leaf_fixed(TreeView tv, CellPos<T> cp, const T* __restrict__ L,
+                       T* __restrict__ Lleaf) {
+  constexpr int LS = Shifts<P>::ls;
+  const int leaf = blockIdx.x * SHIFT_THREADS + threadIdx.x;
+  if (leaf >= tv.nleaves) return;
+  const int lc = tv.leaf_cell[leaf];
+  T acc[LS];
+#pragma unroll
+  for (int r = 0; r < LS; ++r) acc[r] = T(0);
+  for (int u = tv.lanc_ptr[leaf]; u < tv.lanc_ptr[leaf + 1]; ++u) {
+    const int c = tv.lanc_cell[u];
+    T x, y, z;
+    centre_diff<T>(tv, cp, lc, c, x, y, z);
+    Shifts<P>::l2l(x, y, z, L + (size_t)c * LS, acc);
+  }
+#pragma unroll
+  for (int r = 0; r < LS; ++r) Lleaf[(size_t)leaf * LS + r] = acc[r];
+}
+
 // M of every cell with upward tasks: the sum of its task partials in order.
 template <typename T>
 __global__ void k_msum(int ncells, int msize, const int* __restrict__ cell_task_ptr,
@@ -1237,7 +1356,7 @@ __global__ void __launch_bounds__(32 * M2L_WARPS)
 // the far field (L2P of the site's leaf), removes excluded pairs, then either
 // adds alpha^-1 src (apply) or accumulates sign * F into an FP64 field.
 // ---------------------------------------------------------------------------
-template <typename T, int M, int MODE>
+template <typename T, int M, int MODE, int P = 0>
 __global__ void __launch_bounds__(FINISH_BLOCK) k_finish(int n, const int* __restrict__ leaf_nslot, const T* __restrict__ Fnear,
                          int use_fmm,
                          TreeView tv, OpsView ov, const T* __restrict__ L, PosArgs<T> pa,
@@ -1248,7 +1367,6 @@ __global__ void __launch_bounds__(FINISH_BLOCK) k_finish(int n, const int* __res
                          ReduceSlots dot) {
   constexpr int NS = ncomp(M);
   __shared__ double sh[32];
-  __shared__ T s_pw[FINISH_BLOCK * 3 * PW];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double dv[1] = {0.0};
   if (i < n) {
@@ -1261,17 +1379,22 @@ __global__ void __launch_bounds__(FINISH_BLOCK) k_finish(int n, const int* __res
     if (use_fmm) {
       // L2P of the leaf's accumulated local expansion
       const int leaf = tv.site_leaf[i];
-      T* pw          = s_pw + 3 * PW * threadIdx.x;
       T dx, dy, dz;
       cp.d(tv.leaf_cell[leaf], i, dx, dy, dz);
-      powers3<T>(-dx, -dy, -dz, ov.p - ov.m, pw);
       const T* Lc = L + (size_t)leaf * ov.lsize;
-      for (int w = 0; w < ov.nl2p; ++w) {
-        const T v   = mono3(pw, ov.exps[ov.l2p_j[w]]) * Lc[ov.l2p_n[w]];
-        const int c = ov.l2p_c[w];  // (no dynamic index into f: keeps it in registers)
-        f[0] -= c == 0 ? v : T(0);
-        f[1] -= c == 1 ? v : T(0);
-        f[2] -= c == 2 ? v : T(0);
+      if constexpr (P > 0) {
+        Shifts<P>::l2p(-dx, -dy, -dz, Lc, f[0], f[1], f[2]);
+      } else {
+        __shared__ T s_pw[FINISH_BLOCK * 3 * PW];
+        T* pw = s_pw + 3 * PW * threadIdx.x;
+        powers3<T>(-dx, -dy, -dz, ov.p - ov.m, pw);
+        for (int w = 0; w < ov.nl2p; ++w) {
+          const T v   = mono3(pw, ov.exps[ov.l2p_j[w]]) * Lc[ov.l2p_n[w]];
+          const int c = ov.l2p_c[w];  // (no dynamic index into f: keeps it in registers)
+          f[0] -= c == 0 ? v : T(0);
+          f[1] -= c == 1 ? v : T(0);
+          f[2] -= c == 2 ? v : T(0);
+        }
       }
     }
     const int e0 = corr_ptr[i], e1 = corr_ptr[i + 1];
@@ -1428,6 +1551,7 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
                 const PhaseEvents* pe, int near_mode, const SideStream* side) {
   const TreeView tv = g.view();
   OpsView ov{};
+  int fixedP  = 0;  // order of the straight-line expansion operators in use (0: tables)
   const int n = g.n;
   auto mark = [&](int k) {
     if (pe) CG_CUDA(cudaEventRecord(pe->ev[k], s));
@@ -1444,18 +1568,32 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
   if (g.fmm) {
     if (!ops || ops->host.m != m) fail(CPPE_GPU_INVALID_ARG, "FMM tables missing for order");
     ov = ops->view();
+    fixedP = (m == 1 && (ov.p == 5 || ov.p == 6)) ? ov.p : 0;
     w.M.alloc((size_t)tv.ncells * ov.msize);
     w.L.alloc((size_t)tv.ncells * ov.lsize);
     const int TB = 128;
     const int ntask = (int)g.h_p2m_tasks.size();
     if (tv.nleaves > 0) {
-      k_p2m_leaf<T><<<tv.nleaves, TB, 0, fs>>>(tv, ov, cell_pos<T>(g), src, w.M.p);
+      if (fixedP == 5)
+        k_p2m_leaf_fixed<T, 5><<<tv.nleaves, SHIFT_THREADS, 0, fs>>>(tv, cell_pos<T>(g), src, w.M.p);
+      else if (fixedP == 6)
+        k_p2m_leaf_fixed<T, 6><<<tv.nleaves, SHIFT_THREADS, 0, fs>>>(tv, cell_pos<T>(g), src, w.M.p);
+      else
+        k_p2m_leaf<T><<<tv.nleaves, TB, 0, fs>>>(tv, ov, cell_pos<T>(g), src, w.M.p);
       CG_LAUNCH();
     }
     if (ntask > 0) {
       w.Mpart.alloc((size_t)ntask * ov.msize);
-      k_m2m_tasks<T><<<ntask, TB, 0, fs>>>(tv, ov, g.p2m_tasks.p, g.task_leaf.p, cell_pos<T>(g),
-                                          w.M.p, w.Mpart.p);
+      const int tb = (ntask + SHIFT_THREADS / M2M_TASK_LEAVES - 1) / (SHIFT_THREADS / M2M_TASK_LEAVES);
+      if (fixedP == 5)
+        k_m2m_tasks_fixed<T, 5><<<tb, SHIFT_THREADS, 0, fs>>>(
+              tv, g.p2m_tasks.p, ntask, g.task_leaf.p, cell_pos<T>(g), w.M.p, w.Mpart.p);
+      else if (fixedP == 6)
+        k_m2m_tasks_fixed<T, 6><<<tb, SHIFT_THREADS, 0, fs>>>(
+              tv, g.p2m_tasks.p, ntask, g.task_leaf.p, cell_pos<T>(g), w.M.p, w.Mpart.p);
+      else
+        k_m2m_tasks<T><<<ntask, TB, 0, fs>>>(tv, ov, g.p2m_tasks.p, g.task_leaf.p,
+                                            cell_pos<T>(g), w.M.p, w.Mpart.p);
       CG_LAUNCH();
       const long work = (long)tv.ncells * ov.msize;
       k_msum<T><<<(unsigned)((work + 255) / 256), 256, 0, fs>>>(
@@ -1493,7 +1631,13 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
     mark(2);
     w.Lleaf.alloc((size_t)std::max(1, tv.nleaves) * ov.lsize);
     if (tv.nleaves > 0) {
-      k_l2l_leaf<T><<<tv.nleaves, 128, 0, fs>>>(tv, ov, cell_pos<T>(g), w.L.p, w.Lleaf.p);
+      const int lb = (tv.nleaves + SHIFT_THREADS - 1) / SHIFT_THREADS;
+      if (fixedP == 5)
+        k_l2l_leaf_fixed<T, 5><<<lb, SHIFT_THREADS, 0, fs>>>(tv, cell_pos<T>(g), w.L.p, w.Lleaf.p);
+      else if (fixedP == 6)
+        k_l2l_leaf_fixed<T, 6><<<lb, SHIFT_THREADS, 0, fs>>>(tv, cell_pos<T>(g), w.L.p, w.Lleaf.p);
+      else
+        k_l2l_leaf<T><<<tv.nleaves, 128, 0, fs>>>(tv, ov, cell_pos<T>(g), w.L.p, w.Lleaf.p);
       CG_LAUNCH();
     }
     mark(3);
@@ -1522,18 +1666,25 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
   ReduceSlots rs{nullptr, nullptr, nullptr};
   if (dot) rs = *dot;
   const T* Lp = g.fmm ? w.Lleaf.p : nullptr;
-#define CG_FINISH(TT, MM, MODE)                                                               \
-  k_finish<TT, MM, MODE><<<nb, FB, 0, s>>>(n, g.leaf_nslot.p, w.Fnear.p, g.fmm ? 1 : 0, tv, ov, Lp, \
+#define CG_FINISH(TT, MM, MODE, PP)                                                           \
+  k_finish<TT, MM, MODE, PP><<<nb, FB, 0, s>>>(n, g.leaf_nslot.p, w.Fnear.p, g.fmm ? 1 : 0, tv, ov, Lp, \
                                            pos_args<TT>(g), cell_pos<TT>(g), src, damp ? 1 : 0, \
                                            dampT, g.corr_ptr.p, g.corr_idx.p, ainv6, out,    \
                                            out64, sign, rs)
   if (mode == FINISH_APPLY) {
     if (m != 1) fail(CPPE_GPU_INVALID_ARG, "apply mode needs dipole sources");
-    CG_FINISH(T, 1, FINISH_APPLY);
+    if (fixedP == 5)
+      CG_FINISH(T, 1, FINISH_APPLY, 5);
+    else if (fixedP == 6)
+      CG_FINISH(T, 1, FINISH_APPLY, 6);
+    else
+      CG_FINISH(T, 1, FINISH_APPLY, 0);
   } else {
-    if (m == 0) CG_FINISH(T, 0, FINISH_FIELD);
-    if (m == 1) CG_FINISH(T, 1, FINISH_FIELD);
-    if (m == 2) CG_FINISH(T, 2, FINISH_FIELD);
+    if (m == 0) CG_FINISH(T, 0, FINISH_FIELD, 0);
+    if (m == 1 && fixedP == 5) CG_FINISH(T, 1, FINISH_FIELD, 5);
+    if (m == 1 && fixedP == 6) CG_FINISH(T, 1, FINISH_FIELD, 6);
+    if (m == 1 && fixedP == 0) CG_FINISH(T, 1, FINISH_FIELD, 0);
+    if (m == 2) CG_FINISH(T, 2, FINISH_FIELD, 0);
   }
 #undef CG_FINISH
   CG_LAUNCH();

@@ -1,6 +1,7 @@
 """Generates m2l_gen.cuh: straight-line M2L translations for fixed expansion
 orders, so that the derivative tensor and the local expansion live in
-registers.
+registers, and straight-line forms of the other expansion operators (P2M of
+a dipole, M2M and L2L shifts, L2P field evaluation) for the same orders.
 
 The operator is the reference's Cartesian M2L in the Dehnen/fmmgen
 convention (src/core/fmm/field_m*.cc, calculate.cc:186-203):
@@ -15,6 +16,16 @@ y-power descending.  D is built from the recurrence
 (differentiate R^2 d_i (1/R) = -r_i / R).  The functions are templates over
 the arithmetic type: float, double, or the double-float pair `ddv` (dd.cuh),
 which supplies the operators, `fma`, `rsqrt_t` and `cinv<T>(o)` = 1/o.
+The shifts are the index tables of fmm_ops.cc written out term by term
+(calculate.cc:129-260 with the field_m*.cc P2M/M2M/L2L/L2P kernels): with
+the scaled powers px_a = x^a / a! (and y, z alike) and the monomial
+mono(a, b, c) = px_a py_b pz_c,
+
+    P2M  M_n += sum_{|k| = 1, k <= n} mono(n - k) s_k        (s: the dipole)
+    M2M  M_n += sum_{k <= n} mono(n - k) M'_k
+    L2L  L_n += sum_{k >= n} mono(k - n) L'_k
+    L2P  f_c -= sum_{n_c >= 1} mono(n - e_c) L_n
+
 This file is run by the build
 (cppe_gb300/_build.py) and its output is not edited by hand.
 """
@@ -88,6 +99,121 @@ def emit(m, p):
     return "\n".join(lines), name, ls, nterms(p) - moff
 
 
+def powers_lines(q):
+    """Scaled powers px_a = x^a / a!, a = 1..q (px_0 = 1 is left out)."""
+    out = []
+    for v in "xyz":
+        for a in range(1, q + 1):
+            if a == 1:
+                out.append(f"  const T p{v}1 = {v};")
+            else:
+                out.append(f"  const T p{v}{a} = p{v}{a - 1} * {v} * cinv<T>({a});")
+    return out
+
+
+def mono(e):
+    """mono(a, b, c) as the product (px_a py_b) pz_c with unit factors left out
+    (the table-driven form multiplies by them: exact)."""
+    f = [f"p{v}{a}" for v, a in zip("xyz", e) if a > 0]
+    return " * ".join(f) if f else "T(1)"
+
+
+def emit_shifts(m, p):
+    mi = multi_indices(p + 1)
+    idx = {t: j for j, t in enumerate(mi)}
+    moff, nt, ls = nterms(m - 1), nterms(p), nterms(p - m)
+    ms = nt - moff
+    sub = lambda n, k: tuple(a - b for a, b in zip(mi[n], mi[k]))
+    ge = lambda d: all(v >= 0 for v in d)
+    out = []
+
+    def body(q, terms, used):
+        # terms: list of (input expression, [(output index, exponent)])
+        lines = powers_lines(q)
+        for e in sorted(used, key=lambda e: idx[e]):
+            if sum(e) > 1 and sum(1 for v in e if v) > 1:
+                lines.append(f"  const T m_{e[0]}_{e[1]}_{e[2]} = {mono(e)};")
+        for inp, outs in terms:
+            lines.append(f"  {{ const T v = {inp};")
+            for o, e in outs:
+                me = f"m_{e[0]}_{e[1]}_{e[2]}" if sum(e) > 1 and sum(1 for v in e if v) > 1 \
+                    else mono(e)
+                lines.append(f"    {o} = fma({me}, v, {o});")
+            lines.append("  }")
+        return lines
+
+    # P2M of a dipole (source order 1 only)
+    if m == 1:
+        terms, used = [], set()
+        for k in range(moff, nterms(m)):
+            outs = []
+            for n in range(moff, nt):
+                d = sub(n, k)
+                if ge(d):
+                    outs.append((f"acc[{n - moff}]", d))
+                    used.add(d)
+            terms.append((f"s{k - moff}", outs))
+        out.append(f"// P2M of a dipole (s0, s1, s2) at offset (x, y, z) = centre - site, order {p}")
+        out.append("template <typename T>")
+        out.append(f"__device__ __forceinline__ void p2m_m{m}_p{p}(T x, T y, T z, T s0, T s1, T s2, "
+                   "T* __restrict__ acc) {")
+        out += body(p - 1, terms, used)
+        out.append("}")
+    # M2M
+    terms, used = [], set()
+    for k in range(moff, nt):
+        outs = []
+        for n in range(k, nt):
+            d = sub(n, k)
+            if ge(d):
+                outs.append((f"acc[{n - moff}]", d))
+                used.add(d)
+        terms.append((f"Mc[{k - moff}]", outs))
+    out.append(f"// M2M: multipole Mc about a centre at (x, y, z) from this one, order {p}")
+    out.append("template <typename T>")
+    out.append(f"__device__ __forceinline__ void m2m_m{m}_p{p}(T x, T y, T z, const T* __restrict__ Mc, "
+               "T* __restrict__ acc) {")
+    out += body(p - 1, terms, used)
+    out.append("}")
+    # L2L
+    terms, used = [], set()
+    for k in range(ls):
+        outs = []
+        for n in range(0, k + 1):
+            d = sub(k, n)
+            if ge(d):
+                outs.append((f"acc[{n}]", d))
+                used.add(d)
+        terms.append((f"Lc[{k}]", outs))
+    out.append(f"// L2L: local expansion Lc about a centre at -(x, y, z) from this one, order {p}")
+    out.append("template <typename T>")
+    out.append(f"__device__ __forceinline__ void l2l_m{m}_p{p}(T x, T y, T z, const T* __restrict__ Lc, "
+               "T* __restrict__ acc) {")
+    out += body(p - m, terms, used)
+    out.append("}")
+    # L2P
+    terms, used = [], set()
+    for n in range(1, ls):
+        outs = []
+        for c in range(3):
+            e = list(mi[n])
+            if e[c] == 0:
+                continue
+            e[c] -= 1
+            e = tuple(e)
+            outs.append((f"f{c}", e))
+            used.add(e)
+        terms.append((f"-Lc[{n}]", outs))
+    out.append(f"// L2P: field -grad of the local expansion Lc at offset (x, y, z) = site - centre, "
+               f"order {p}")
+    out.append("template <typename T>")
+    out.append(f"__device__ __forceinline__ void l2p_m{m}_p{p}(T x, T y, T z, const T* __restrict__ Lc, "
+               "T& f0, T& f1, T& f2) {")
+    out += body(max(p - m - 1, 1), terms, used)
+    out.append("}")
+    return "\n".join(out), ls, ms
+
+
 def main(out_path):
     parts = ["// Generated by gen_m2l.py -- do not edit.", "#pragma once", ""]
     table = []
@@ -96,8 +222,16 @@ def main(out_path):
         parts.append(code)
         parts.append("")
         table.append((m, p, name, ls, ms))
+    for m, p in ORDERS:
+        code, ls, ms = emit_shifts(m, p)
+        parts.append(code)
+        parts.append("")
     parts.append("#define CPPE_M2L_GENERATED(X) \\")
     parts.append(" \\\n".join(f"  X({m}, {p}, {name}, {ls}, {ms})" for m, p, name, ls, ms in table))
+    parts.append("")
+    # (m, p, Lsize, Msize) of the straight-line shifts
+    parts.append("#define CPPE_SHIFTS_GENERATED(X) \\")
+    parts.append(" \\\n".join(f"  X({m}, {p}, {ls}, {ms})" for m, p, name, ls, ms in table))
     parts.append("")
     src = "\n".join(parts)
     if os.path.exists(out_path) and open(out_path).read() == src:

@@ -1677,6 +1677,3368 @@ __device__ __forceinline__ void m2l_m1_p6(T x, T y, T z, const T* __restrict__ M
   }
 }
 
+// P2M of a dipole (s0, s1, s2) at offset (x, y, z) = centre - site, order 5
+template <typename T>
+__device__ __forceinline__ void p2m_m1_p5(T x, T y, T z, T s0, T s1, T s2, T* __restrict__ acc) {
+  const T px1 = x;
+  const T px2 = px1 * x * cinv<T>(2);
+  const T px3 = px2 * x * cinv<T>(3);
+  const T px4 = px3 * x * cinv<T>(4);
+  const T py1 = y;
+  const T py2 = py1 * y * cinv<T>(2);
+  const T py3 = py2 * y * cinv<T>(3);
+  const T py4 = py3 * y * cinv<T>(4);
+  const T pz1 = z;
+  const T pz2 = pz1 * z * cinv<T>(2);
+  const T pz3 = pz2 * z * cinv<T>(3);
+  const T pz4 = pz3 * z * cinv<T>(4);
+  const T m_1_1_0 = px1 * py1;
+  const T m_1_0_1 = px1 * pz1;
+  const T m_0_1_1 = py1 * pz1;
+  const T m_2_1_0 = px2 * py1;
+  const T m_2_0_1 = px2 * pz1;
+  const T m_1_2_0 = px1 * py2;
+  const T m_1_1_1 = px1 * py1 * pz1;
+  const T m_1_0_2 = px1 * pz2;
+  const T m_0_2_1 = py2 * pz1;
+  const T m_0_1_2 = py1 * pz2;
+  const T m_3_1_0 = px3 * py1;
+  const T m_3_0_1 = px3 * pz1;
+  const T m_2_2_0 = px2 * py2;
+  const T m_2_1_1 = px2 * py1 * pz1;
+  const T m_2_0_2 = px2 * pz2;
+  const T m_1_3_0 = px1 * py3;
+  const T m_1_2_1 = px1 * py2 * pz1;
+  const T m_1_1_2 = px1 * py1 * pz2;
+  const T m_1_0_3 = px1 * pz3;
+  const T m_0_3_1 = py3 * pz1;
+  const T m_0_2_2 = py2 * pz2;
+  const T m_0_1_3 = py1 * pz3;
+  { const T v = s0;
+    acc[0] = fma(T(1), v, acc[0]);
+    acc[3] = fma(px1, v, acc[3]);
+    acc[4] = fma(py1, v, acc[4]);
+    acc[5] = fma(pz1, v, acc[5]);
+    acc[9] = fma(px2, v, acc[9]);
+    acc[10] = fma(m_1_1_0, v, acc[10]);
+    acc[11] = fma(m_1_0_1, v, acc[11]);
+    acc[12] = fma(py2, v, acc[12]);
+    acc[13] = fma(m_0_1_1, v, acc[13]);
+    acc[14] = fma(pz2, v, acc[14]);
+    acc[19] = fma(px3, v, acc[19]);
+    acc[20] = fma(m_2_1_0, v, acc[20]);
+    acc[21] = fma(m_2_0_1, v, acc[21]);
+    acc[22] = fma(m_1_2_0, v, acc[22]);
+    acc[23] = fma(m_1_1_1, v, acc[23]);
+    acc[24] = fma(m_1_0_2, v, acc[24]);
+    acc[25] = fma(py3, v, acc[25]);
+    acc[26] = fma(m_0_2_1, v, acc[26]);
+    acc[27] = fma(m_0_1_2, v, acc[27]);
+    acc[28] = fma(pz3, v, acc[28]);
+    acc[34] = fma(px4, v, acc[34]);
+    acc[35] = fma(m_3_1_0, v, acc[35]);
+    acc[36] = fma(m_3_0_1, v, acc[36]);
+    acc[37] = fma(m_2_2_0, v, acc[37]);
+    acc[38] = fma(m_2_1_1, v, acc[38]);
+    acc[39] = fma(m_2_0_2, v, acc[39]);
+    acc[40] = fma(m_1_3_0, v, acc[40]);
+    acc[41] = fma(m_1_2_1, v, acc[41]);
+    acc[42] = fma(m_1_1_2, v, acc[42]);
+    acc[43] = fma(m_1_0_3, v, acc[43]);
+    acc[44] = fma(py4, v, acc[44]);
+    acc[45] = fma(m_0_3_1, v, acc[45]);
+    acc[46] = fma(m_0_2_2, v, acc[46]);
+    acc[47] = fma(m_0_1_3, v, acc[47]);
+    acc[48] = fma(pz4, v, acc[48]);
+  }
+  { const T v = s1;
+    acc[1] = fma(T(1), v, acc[1]);
+    acc[4] = fma(px1, v, acc[4]);
+    acc[6] = fma(py1, v, acc[6]);
+    acc[7] = fma(pz1, v, acc[7]);
+    acc[10] = fma(px2, v, acc[10]);
+    acc[12] = fma(m_1_1_0, v, acc[12]);
+    acc[13] = fma(m_1_0_1, v, acc[13]);
+    acc[15] = fma(py2, v, acc[15]);
+    acc[16] = fma(m_0_1_1, v, acc[16]);
+    acc[17] = fma(pz2, v, acc[17]);
+    acc[20] = fma(px3, v, acc[20]);
+    acc[22] = fma(m_2_1_0, v, acc[22]);
+    acc[23] = fma(m_2_0_1, v, acc[23]);
+    acc[25] = fma(m_1_2_0, v, acc[25]);
+    acc[26] = fma(m_1_1_1, v, acc[26]);
+    acc[27] = fma(m_1_0_2, v, acc[27]);
+    acc[29] = fma(py3, v, acc[29]);
+    acc[30] = fma(m_0_2_1, v, acc[30]);
+    acc[31] = fma(m_0_1_2, v, acc[31]);
+    acc[32] = fma(pz3, v, acc[32]);
+    acc[35] = fma(px4, v, acc[35]);
+    acc[37] = fma(m_3_1_0, v, acc[37]);
+    acc[38] = fma(m_3_0_1, v, acc[38]);
+    acc[40] = fma(m_2_2_0, v, acc[40]);
+    acc[41] = fma(m_2_1_1, v, acc[41]);
+    acc[42] = fma(m_2_0_2, v, acc[42]);
+    acc[44] = fma(m_1_3_0, v, acc[44]);
+    acc[45] = fma(m_1_2_1, v, acc[45]);
+    acc[46] = fma(m_1_1_2, v, acc[46]);
+    acc[47] = fma(m_1_0_3, v, acc[47]);
+    acc[49] = fma(py4, v, acc[49]);
+    acc[50] = fma(m_0_3_1, v, acc[50]);
+    acc[51] = fma(m_0_2_2, v, acc[51]);
+    acc[52] = fma(m_0_1_3, v, acc[52]);
+    acc[53] = fma(pz4, v, acc[53]);
+  }
+  { const T v = s2;
+    acc[2] = fma(T(1), v, acc[2]);
+    acc[5] = fma(px1, v, acc[5]);
+    acc[7] = fma(py1, v, acc[7]);
+    acc[8] = fma(pz1, v, acc[8]);
+    acc[11] = fma(px2, v, acc[11]);
+    acc[13] = fma(m_1_1_0, v, acc[13]);
+    acc[14] = fma(m_1_0_1, v, acc[14]);
+    acc[16] = fma(py2, v, acc[16]);
+    acc[17] = fma(m_0_1_1, v, acc[17]);
+    acc[18] = fma(pz2, v, acc[18]);
+    acc[21] = fma(px3, v, acc[21]);
+    acc[23] = fma(m_2_1_0, v, acc[23]);
+    acc[24] = fma(m_2_0_1, v, acc[24]);
+    acc[26] = fma(m_1_2_0, v, acc[26]);
+    acc[27] = fma(m_1_1_1, v, acc[27]);
+    acc[28] = fma(m_1_0_2, v, acc[28]);
+    acc[30] = fma(py3, v, acc[30]);
+    acc[31] = fma(m_0_2_1, v, acc[31]);
+    acc[32] = fma(m_0_1_2, v, acc[32]);
+    acc[33] = fma(pz3, v, acc[33]);
+    acc[36] = fma(px4, v, acc[36]);
+    acc[38] = fma(m_3_1_0, v, acc[38]);
+    acc[39] = fma(m_3_0_1, v, acc[39]);
+    acc[41] = fma(m_2_2_0, v, acc[41]);
+    acc[42] = fma(m_2_1_1, v, acc[42]);
+    acc[43] = fma(m_2_0_2, v, acc[43]);
+    acc[45] = fma(m_1_3_0, v, acc[45]);
+    acc[46] = fma(m_1_2_1, v, acc[46]);
+    acc[47] = fma(m_1_1_2, v, acc[47]);
+    acc[48] = fma(m_1_0_3, v, acc[48]);
+    acc[50] = fma(py4, v, acc[50]);
+    acc[51] = fma(m_0_3_1, v, acc[51]);
+    acc[52] = fma(m_0_2_2, v, acc[52]);
+    acc[53] = fma(m_0_1_3, v, acc[53]);
+    acc[54] = fma(pz4, v, acc[54]);
+  }
+}
+// M2M: multipole Mc about a centre at (x, y, z) from this one, order 5
+template <typename T>
+__device__ __forceinline__ void m2m_m1_p5(T x, T y, T z, const T* __restrict__ Mc, T* __restrict__ acc) {
+  const T px1 = x;
+  const T px2 = px1 * x * cinv<T>(2);
+  const T px3 = px2 * x * cinv<T>(3);
+  const T px4 = px3 * x * cinv<T>(4);
+  const T py1 = y;
+  const T py2 = py1 * y * cinv<T>(2);
+  const T py3 = py2 * y * cinv<T>(3);
+  const T py4 = py3 * y * cinv<T>(4);
+  const T pz1 = z;
+  const T pz2 = pz1 * z * cinv<T>(2);
+  const T pz3 = pz2 * z * cinv<T>(3);
+  const T pz4 = pz3 * z * cinv<T>(4);
+  const T m_1_1_0 = px1 * py1;
+  const T m_1_0_1 = px1 * pz1;
+  const T m_0_1_1 = py1 * pz1;
+  const T m_2_1_0 = px2 * py1;
+  const T m_2_0_1 = px2 * pz1;
+  const T m_1_2_0 = px1 * py2;
+  const T m_1_1_1 = px1 * py1 * pz1;
+  const T m_1_0_2 = px1 * pz2;
+  const T m_0_2_1 = py2 * pz1;
+  const T m_0_1_2 = py1 * pz2;
+  const T m_3_1_0 = px3 * py1;
+  const T m_3_0_1 = px3 * pz1;
+  const T m_2_2_0 = px2 * py2;
+  const T m_2_1_1 = px2 * py1 * pz1;
+  const T m_2_0_2 = px2 * pz2;
+  const T m_1_3_0 = px1 * py3;
+  const T m_1_2_1 = px1 * py2 * pz1;
+  const T m_1_1_2 = px1 * py1 * pz2;
+  const T m_1_0_3 = px1 * pz3;
+  const T m_0_3_1 = py3 * pz1;
+  const T m_0_2_2 = py2 * pz2;
+  const T m_0_1_3 = py1 * pz3;
+  { const T v = Mc[0];
+    acc[0] = fma(T(1), v, acc[0]);
+    acc[3] = fma(px1, v, acc[3]);
+    acc[4] = fma(py1, v, acc[4]);
+    acc[5] = fma(pz1, v, acc[5]);
+    acc[9] = fma(px2, v, acc[9]);
+    acc[10] = fma(m_1_1_0, v, acc[10]);
+    acc[11] = fma(m_1_0_1, v, acc[11]);
+    acc[12] = fma(py2, v, acc[12]);
+    acc[13] = fma(m_0_1_1, v, acc[13]);
+    acc[14] = fma(pz2, v, acc[14]);
+    acc[19] = fma(px3, v, acc[19]);
+    acc[20] = fma(m_2_1_0, v, acc[20]);
+    acc[21] = fma(m_2_0_1, v, acc[21]);
+    acc[22] = fma(m_1_2_0, v, acc[22]);
+    acc[23] = fma(m_1_1_1, v, acc[23]);
+    acc[24] = fma(m_1_0_2, v, acc[24]);
+    acc[25] = fma(py3, v, acc[25]);
+    acc[26] = fma(m_0_2_1, v, acc[26]);
+    acc[27] = fma(m_0_1_2, v, acc[27]);
+    acc[28] = fma(pz3, v, acc[28]);
+    acc[34] = fma(px4, v, acc[34]);
+    acc[35] = fma(m_3_1_0, v, acc[35]);
+    acc[36] = fma(m_3_0_1, v, acc[36]);
+    acc[37] = fma(m_2_2_0, v, acc[37]);
+    acc[38] = fma(m_2_1_1, v, acc[38]);
+    acc[39] = fma(m_2_0_2, v, acc[39]);
+    acc[40] = fma(m_1_3_0, v, acc[40]);
+    acc[41] = fma(m_1_2_1, v, acc[41]);
+    acc[42] = fma(m_1_1_2, v, acc[42]);
+    acc[43] = fma(m_1_0_3, v, acc[43]);
+    acc[44] = fma(py4, v, acc[44]);
+    acc[45] = fma(m_0_3_1, v, acc[45]);
+    acc[46] = fma(m_0_2_2, v, acc[46]);
+    acc[47] = fma(m_0_1_3, v, acc[47]);
+    acc[48] = fma(pz4, v, acc[48]);
+  }
+  { const T v = Mc[1];
+    acc[1] = fma(T(1), v, acc[1]);
+    acc[4] = fma(px1, v, acc[4]);
+    acc[6] = fma(py1, v, acc[6]);
+    acc[7] = fma(pz1, v, acc[7]);
+    acc[10] = fma(px2, v, acc[10]);
+    acc[12] = fma(m_1_1_0, v, acc[12]);
+    acc[13] = fma(m_1_0_1, v, acc[13]);
+    acc[15] = fma(py2, v, acc[15]);
+    acc[16] = fma(m_0_1_1, v, acc[16]);
+    acc[17] = fma(pz2, v, acc[17]);
+    acc[20] = fma(px3, v, acc[20]);
+    acc[22] = fma(m_2_1_0, v, acc[22]);
+    acc[23] = fma(m_2_0_1, v, acc[23]);
+    acc[25] = fma(m_1_2_0, v, acc[25]);
+    acc[26] = fma(m_1_1_1, v, acc[26]);
+    acc[27] = fma(m_1_0_2, v, acc[27]);
+    acc[29] = fma(py3, v, acc[29]);
+    acc[30] = fma(m_0_2_1, v, acc[30]);
+    acc[31] = fma(m_0_1_2, v, acc[31]);
+    acc[32] = fma(pz3, v, acc[32]);
+    acc[35] = fma(px4, v, acc[35]);
+    acc[37] = fma(m_3_1_0, v, acc[37]);
+    acc[38] = fma(m_3_0_1, v, acc[38]);
+    acc[40] = fma(m_2_2_0, v, acc[40]);
+    acc[41] = fma(m_2_1_1, v, acc[41]);
+    acc[42] = fma(m_2_0_2, v, acc[42]);
+    acc[44] = fma(m_1_3_0, v, acc[44]);
+    acc[45] = fma(m_1_2_1, v, acc[45]);
+    acc[46] = fma(m_1_1_2, v, acc[46]);
+    acc[47] = fma(m_1_0_3, v, acc[47]);
+    acc[49] = fma(py4, v, acc[49]);
+    acc[50] = fma(m_0_3_1, v, acc[50]);
+    acc[51] = fma(m_0_2_2, v, acc[51]);
+    acc[52] = fma(m_0_1_3, v, acc[52]);
+    acc[53] = fma(pz4, v, acc[53]);
+  }
+  { const T v = Mc[2];
+    acc[2] = fma(T(1), v, acc[2]);
+    acc[5] = fma(px1, v, acc[5]);
+    acc[7] = fma(py1, v, acc[7]);
+    acc[8] = fma(pz1, v, acc[8]);
+    acc[11] = fma(px2, v, acc[11]);
+    acc[13] = fma(m_1_1_0, v, acc[13]);
+    acc[14] = fma(m_1_0_1, v, acc[14]);
+    acc[16] = fma(py2, v, acc[16]);
+    acc[17] = fma(m_0_1_1, v, acc[17]);
+    acc[18] = fma(pz2, v, acc[18]);
+    acc[21] = fma(px3, v, acc[21]);
+    acc[23] = fma(m_2_1_0, v, acc[23]);
+    acc[24] = fma(m_2_0_1, v, acc[24]);
+    acc[26] = fma(m_1_2_0, v, acc[26]);
+    acc[27] = fma(m_1_1_1, v, acc[27]);
+    acc[28] = fma(m_1_0_2, v, acc[28]);
+    acc[30] = fma(py3, v, acc[30]);
+    acc[31] = fma(m_0_2_1, v, acc[31]);
+    acc[32] = fma(m_0_1_2, v, acc[32]);
+    acc[33] = fma(pz3, v, acc[33]);
+    acc[36] = fma(px4, v, acc[36]);
+    acc[38] = fma(m_3_1_0, v, acc[38]);
+    acc[39] = fma(m_3_0_1, v, acc[39]);
+    acc[41] = fma(m_2_2_0, v, acc[41]);
+    acc[42] = fma(m_2_1_1, v, acc[42]);
+    acc[43] = fma(m_2_0_2, v, acc[43]);
+    acc[45] = fma(m_1_3_0, v, acc[45]);
+    acc[46] = fma(m_1_2_1, v, acc[46]);
+    acc[47] = fma(m_1_1_2, v, acc[47]);
+    acc[48] = fma(m_1_0_3, v, acc[48]);
+    acc[50] = fma(py4, v, acc[50]);
+    acc[51] = fma(m_0_3_1, v, acc[51]);
+    acc[52] = fma(m_0_2_2, v, acc[52]);
+    acc[53] = fma(m_0_1_3, v, acc[53]);
+    acc[54] = fma(pz4, v, acc[54]);
+  }
+  { const T v = Mc[3];
+    acc[3] = fma(T(1), v, acc[3]);
+    acc[9] = fma(px1, v, acc[9]);
+    acc[10] = fma(py1, v, acc[10]);
+    acc[11] = fma(pz1, v, acc[11]);
+    acc[19] = fma(px2, v, acc[19]);
+    acc[20] = fma(m_1_1_0, v, acc[20]);
+    acc[21] = fma(m_1_0_1, v, acc[21]);
+    acc[22] = fma(py2, v, acc[22]);
+    acc[23] = fma(m_0_1_1, v, acc[23]);
+    acc[24] = fma(pz2, v, acc[24]);
+    acc[34] = fma(px3, v, acc[34]);
+    acc[35] = fma(m_2_1_0, v, acc[35]);
+    acc[36] = fma(m_2_0_1, v, acc[36]);
+    acc[37] = fma(m_1_2_0, v, acc[37]);
+    acc[38] = fma(m_1_1_1, v, acc[38]);
+    acc[39] = fma(m_1_0_2, v, acc[39]);
+    acc[40] = fma(py3, v, acc[40]);
+    acc[41] = fma(m_0_2_1, v, acc[41]);
+    acc[42] = fma(m_0_1_2, v, acc[42]);
+    acc[43] = fma(pz3, v, acc[43]);
+  }
+  { const T v = Mc[4];
+    acc[4] = fma(T(1), v, acc[4]);
+    acc[10] = fma(px1, v, acc[10]);
+    acc[12] = fma(py1, v, acc[12]);
+    acc[13] = fma(pz1, v, acc[13]);
+    acc[20] = fma(px2, v, acc[20]);
+    acc[22] = fma(m_1_1_0, v, acc[22]);
+    acc[23] = fma(m_1_0_1, v, acc[23]);
+    acc[25] = fma(py2, v, acc[25]);
+    acc[26] = fma(m_0_1_1, v, acc[26]);
+    acc[27] = fma(pz2, v, acc[27]);
+    acc[35] = fma(px3, v, acc[35]);
+    acc[37] = fma(m_2_1_0, v, acc[37]);
+    acc[38] = fma(m_2_0_1, v, acc[38]);
+    acc[40] = fma(m_1_2_0, v, acc[40]);
+    acc[41] = fma(m_1_1_1, v, acc[41]);
+    acc[42] = fma(m_1_0_2, v, acc[42]);
+    acc[44] = fma(py3, v, acc[44]);
+    acc[45] = fma(m_0_2_1, v, acc[45]);
+    acc[46] = fma(m_0_1_2, v, acc[46]);
+    acc[47] = fma(pz3, v, acc[47]);
+  }
+  { const T v = Mc[5];
+    acc[5] = fma(T(1), v, acc[5]);
+    acc[11] = fma(px1, v, acc[11]);
+    acc[13] = fma(py1, v, acc[13]);
+    acc[14] = fma(pz1, v, acc[14]);
+    acc[21] = fma(px2, v, acc[21]);
+    acc[23] = fma(m_1_1_0, v, acc[23]);
+    acc[24] = fma(m_1_0_1, v, acc[24]);
+    acc[26] = fma(py2, v, acc[26]);
+    acc[27] = fma(m_0_1_1, v, acc[27]);
+    acc[28] = fma(pz2, v, acc[28]);
+    acc[36] = fma(px3, v, acc[36]);
+    acc[38] = fma(m_2_1_0, v, acc[38]);
+    acc[39] = fma(m_2_0_1, v, acc[39]);
+    acc[41] = fma(m_1_2_0, v, acc[41]);
+    acc[42] = fma(m_1_1_1, v, acc[42]);
+    acc[43] = fma(m_1_0_2, v, acc[43]);
+    acc[45] = fma(py3, v, acc[45]);
+    acc[46] = fma(m_0_2_1, v, acc[46]);
+    acc[47] = fma(m_0_1_2, v, acc[47]);
+    acc[48] = fma(pz3, v, acc[48]);
+  }
+  { const T v = Mc[6];
+    acc[6] = fma(T(1), v, acc[6]);
+    acc[12] = fma(px1, v, acc[12]);
+    acc[15] = fma(py1, v, acc[15]);
+    acc[16] = fma(pz1, v, acc[16]);
+    acc[22] = fma(px2, v, acc[22]);
+    acc[25] = fma(m_1_1_0, v, acc[25]);
+    acc[26] = fma(m_1_0_1, v, acc[26]);
+    acc[29] = fma(py2, v, acc[29]);
+    acc[30] = fma(m_0_1_1, v, acc[30]);
+    acc[31] = fma(pz2, v, acc[31]);
+    acc[37] = fma(px3, v, acc[37]);
+    acc[40] = fma(m_2_1_0, v, acc[40]);
+    acc[41] = fma(m_2_0_1, v, acc[41]);
+    acc[44] = fma(m_1_2_0, v, acc[44]);
+    acc[45] = fma(m_1_1_1, v, acc[45]);
+    acc[46] = fma(m_1_0_2, v, acc[46]);
+    acc[49] = fma(py3, v, acc[49]);
+    acc[50] = fma(m_0_2_1, v, acc[50]);
+    acc[51] = fma(m_0_1_2, v, acc[51]);
+    acc[52] = fma(pz3, v, acc[52]);
+  }
+  { const T v = Mc[7];
+    acc[7] = fma(T(1), v, acc[7]);
+    acc[13] = fma(px1, v, acc[13]);
+    acc[16] = fma(py1, v, acc[16]);
+    acc[17] = fma(pz1, v, acc[17]);
+    acc[23] = fma(px2, v, acc[23]);
+    acc[26] = fma(m_1_1_0, v, acc[26]);
+    acc[27] = fma(m_1_0_1, v, acc[27]);
+    acc[30] = fma(py2, v, acc[30]);
+    acc[31] = fma(m_0_1_1, v, acc[31]);
+    acc[32] = fma(pz2, v, acc[32]);
+    acc[38] = fma(px3, v, acc[38]);
+    acc[41] = fma(m_2_1_0, v, acc[41]);
+    acc[42] = fma(m_2_0_1, v, acc[42]);
+    acc[45] = fma(m_1_2_0, v, acc[45]);
+    acc[46] = fma(m_1_1_1, v, acc[46]);
+    acc[47] = fma(m_1_0_2, v, acc[47]);
+    acc[50] = fma(py3, v, acc[50]);
+    acc[51] = fma(m_0_2_1, v, acc[51]);
+    acc[52] = fma(m_0_1_2, v, acc[52]);
+    acc[53] = fma(pz3, v, acc[53]);
+  }
+  { const T v = Mc[8];
+    acc[8] = fma(T(1), v, acc[8]);
+    acc[14] = fma(px1, v, acc[14]);
+    acc[17] = fma(py1, v, acc[17]);
+    acc[18] = fma(pz1, v, acc[18]);
+    acc[24] = fma(px2, v, acc[24]);
+    acc[27] = fma(m_1_1_0, v, acc[27]);
+    acc[28] = fma(m_1_0_1, v, acc[28]);
+    acc[31] = fma(py2, v, acc[31]);
+    acc[32] = fma(m_0_1_1, v, acc[32]);
+    acc[33] = fma(pz2, v, acc[33]);
+    acc[39] = fma(px3, v, acc[39]);
+    acc[42] = fma(m_2_1_0, v, acc[42]);
+    acc[43] = fma(m_2_0_1, v, acc[43]);
+    acc[46] = fma(m_1_2_0, v, acc[46]);
+    acc[47] = fma(m_1_1_1, v, acc[47]);
+    acc[48] = fma(m_1_0_2, v, acc[48]);
+    acc[51] = fma(py3, v, acc[51]);
+    acc[52] = fma(m_0_2_1, v, acc[52]);
+    acc[53] = fma(m_0_1_2, v, acc[53]);
+    acc[54] = fma(pz3, v, acc[54]);
+  }
+  { const T v = Mc[9];
+    acc[9] = fma(T(1), v, acc[9]);
+    acc[19] = fma(px1, v, acc[19]);
+    acc[20] = fma(py1, v, acc[20]);
+    acc[21] = fma(pz1, v, acc[21]);
+    acc[34] = fma(px2, v, acc[34]);
+    acc[35] = fma(m_1_1_0, v, acc[35]);
+    acc[36] = fma(m_1_0_1, v, acc[36]);
+    acc[37] = fma(py2, v, acc[37]);
+    acc[38] = fma(m_0_1_1, v, acc[38]);
+    acc[39] = fma(pz2, v, acc[39]);
+  }
+  { const T v = Mc[10];
+    acc[10] = fma(T(1), v, acc[10]);
+    acc[20] = fma(px1, v, acc[20]);
+    acc[22] = fma(py1, v, acc[22]);
+    acc[23] = fma(pz1, v, acc[23]);
+    acc[35] = fma(px2, v, acc[35]);
+    acc[37] = fma(m_1_1_0, v, acc[37]);
+    acc[38] = fma(m_1_0_1, v, acc[38]);
+    acc[40] = fma(py2, v, acc[40]);
+    acc[41] = fma(m_0_1_1, v, acc[41]);
+    acc[42] = fma(pz2, v, acc[42]);
+  }
+  { const T v = Mc[11];
+    acc[11] = fma(T(1), v, acc[11]);
+    acc[21] = fma(px1, v, acc[21]);
+    acc[23] = fma(py1, v, acc[23]);
+    acc[24] = fma(pz1, v, acc[24]);
+    acc[36] = fma(px2, v, acc[36]);
+    acc[38] = fma(m_1_1_0, v, acc[38]);
+    acc[39] = fma(m_1_0_1, v, acc[39]);
+    acc[41] = fma(py2, v, acc[41]);
+    acc[42] = fma(m_0_1_1, v, acc[42]);
+    acc[43] = fma(pz2, v, acc[43]);
+  }
+  { const T v = Mc[12];
+    acc[12] = fma(T(1), v, acc[12]);
+    acc[22] = fma(px1, v, acc[22]);
+    acc[25] = fma(py1, v, acc[25]);
+    acc[26] = fma(pz1, v, acc[26]);
+    acc[37] = fma(px2, v, acc[37]);
+    acc[40] = fma(m_1_1_0, v, acc[40]);
+    acc[41] = fma(m_1_0_1, v, acc[41]);
+    acc[44] = fma(py2, v, acc[44]);
+    acc[45] = fma(m_0_1_1, v, acc[45]);
+    acc[46] = fma(pz2, v, acc[46]);
+  }
+  { const T v = Mc[13];
+    acc[13] = fma(T(1), v, acc[13]);
+    acc[23] = fma(px1, v, acc[23]);
+    acc[26] = fma(py1, v, acc[26]);
+    acc[27] = fma(pz1, v, acc[27]);
+    acc[38] = fma(px2, v, acc[38]);
+    acc[41] = fma(m_1_1_0, v, acc[41]);
+    acc[42] = fma(m_1_0_1, v, acc[42]);
+    acc[45] = fma(py2, v, acc[45]);
+    acc[46] = fma(m_0_1_1, v, acc[46]);
+    acc[47] = fma(pz2, v, acc[47]);
+  }
+  { const T v = Mc[14];
+    acc[14] = fma(T(1), v, acc[14]);
+    acc[24] = fma(px1, v, acc[24]);
+    acc[27] = fma(py1, v, acc[27]);
+    acc[28] = fma(pz1, v, acc[28]);
+    acc[39] = fma(px2, v, acc[39]);
+    acc[42] = fma(m_1_1_0, v, acc[42]);
+    acc[43] = fma(m_1_0_1, v, acc[43]);
+    acc[46] = fma(py2, v, acc[46]);
+    acc[47] = fma(m_0_1_1, v, acc[47]);
+    acc[48] = fma(pz2, v, acc[48]);
+  }
+  { const T v = Mc[15];
+    acc[15] = fma(T(1), v, acc[15]);
+    acc[25] = fma(px1, v, acc[25]);
+    acc[29] = fma(py1, v, acc[29]);
+    acc[30] = fma(pz1, v, acc[30]);
+    acc[40] = fma(px2, v, acc[40]);
+    acc[44] = fma(m_1_1_0, v, acc[44]);
+    acc[45] = fma(m_1_0_1, v, acc[45]);
+    acc[49] = fma(py2, v, acc[49]);
+    acc[50] = fma(m_0_1_1, v, acc[50]);
+    acc[51] = fma(pz2, v, acc[51]);
+  }
+  { const T v = Mc[16];
+    acc[16] = fma(T(1), v, acc[16]);
+    acc[26] = fma(px1, v, acc[26]);
+    acc[30] = fma(py1, v, acc[30]);
+    acc[31] = fma(pz1, v, acc[31]);
+    acc[41] = fma(px2, v, acc[41]);
+    acc[45] = fma(m_1_1_0, v, acc[45]);
+    acc[46] = fma(m_1_0_1, v, acc[46]);
+    acc[50] = fma(py2, v, acc[50]);
+    acc[51] = fma(m_0_1_1, v, acc[51]);
+    acc[52] = fma(pz2, v, acc[52]);
+  }
+  { const T v = Mc[17];
+    acc[17] = fma(T(1), v, acc[17]);
+    acc[27] = fma(px1, v, acc[27]);
+    acc[31] = fma(py1, v, acc[31]);
+    acc[32] = fma(pz1, v, acc[32]);
+    acc[42] = fma(px2, v, acc[42]);
+    acc[46] = fma(m_1_1_0, v, acc[46]);
+    acc[47] = fma(m_1_0_1, v, acc[47]);
+    acc[51] = fma(py2, v, acc[51]);
+    acc[52] = fma(m_0_1_1, v, acc[52]);
+    acc[53] = fma(pz2, v, acc[53]);
+  }
+  { const T v = Mc[18];
+    acc[18] = fma(T(1), v, acc[18]);
+    acc[28] = fma(px1, v, acc[28]);
+    acc[32] = fma(py1, v, acc[32]);
+    acc[33] = fma(pz1, v, acc[33]);
+    acc[43] = fma(px2, v, acc[43]);
+    acc[47] = fma(m_1_1_0, v, acc[47]);
+    acc[48] = fma(m_1_0_1, v, acc[48]);
+    acc[52] = fma(py2, v, acc[52]);
+    acc[53] = fma(m_0_1_1, v, acc[53]);
+    acc[54] = fma(pz2, v, acc[54]);
+  }
+  { const T v = Mc[19];
+    acc[19] = fma(T(1), v, acc[19]);
+    acc[34] = fma(px1, v, acc[34]);
+    acc[35] = fma(py1, v, acc[35]);
+    acc[36] = fma(pz1, v, acc[36]);
+  }
+  { const T v = Mc[20];
+    acc[20] = fma(T(1), v, acc[20]);
+    acc[35] = fma(px1, v, acc[35]);
+    acc[37] = fma(py1, v, acc[37]);
+    acc[38] = fma(pz1, v, acc[38]);
+  }
+  { const T v = Mc[21];
+    acc[21] = fma(T(1), v, acc[21]);
+    acc[36] = fma(px1, v, acc[36]);
+    acc[38] = fma(py1, v, acc[38]);
+    acc[39] = fma(pz1, v, acc[39]);
+  }
+  { const T v = Mc[22];
+    acc[22] = fma(T(1), v, acc[22]);
+    acc[37] = fma(px1, v, acc[37]);
+    acc[40] = fma(py1, v, acc[40]);
+    acc[41] = fma(pz1, v, acc[41]);
+  }
+  { const T v = Mc[23];
+    acc[23] = fma(T(1), v, acc[23]);
+    acc[38] = fma(px1, v, acc[38]);
+    acc[41] = fma(py1, v, acc[41]);
+    acc[42] = fma(pz1, v, acc[42]);
+  }
+  { const T v = Mc[24];
+    acc[24] = fma(T(1), v, acc[24]);
+    acc[39] = fma(px1, v, acc[39]);
+    acc[42] = fma(py1, v, acc[42]);
+    acc[43] = fma(pz1, v, acc[43]);
+  }
+  { const T v = Mc[25];
+    acc[25] = fma(T(1), v, acc[25]);
+    acc[40] = fma(px1, v, acc[40]);
+    acc[44] = fma(py1, v, acc[44]);
+    acc[45] = fma(pz1, v, acc[45]);
+  }
+  { const T v = Mc[26];
+    acc[26] = fma(T(1), v, acc[26]);
+    acc[41] = fma(px1, v, acc[41]);
+    acc[45] = fma(py1, v, acc[45]);
+    acc[46] = fma(pz1, v, acc[46]);
+  }
+  { const T v = Mc[27];
+    acc[27] = fma(T(1), v, acc[27]);
+    acc[42] = fma(px1, v, acc[42]);
+    acc[46] = fma(py1, v, acc[46]);
+    acc[47] = fma(pz1, v, acc[47]);
+  }
+  { const T v = Mc[28];
+    acc[28] = fma(T(1), v, acc[28]);
+    acc[43] = fma(px1, v, acc[43]);
+    acc[47] = fma(py1, v, acc[47]);
+    acc[48] = fma(pz1, v, acc[48]);
+  }
+  { const T v = Mc[29];
+    acc[29] = fma(T(1), v, acc[29]);
+    acc[44] = fma(px1, v, acc[44]);
+    acc[49] = fma(py1, v, acc[49]);
+    acc[50] = fma(pz1, v, acc[50]);
+  }
+  { const T v = Mc[30];
+    acc[30] = fma(T(1), v, acc[30]);
+    acc[45] = fma(px1, v, acc[45]);
+    acc[50] = fma(py1, v, acc[50]);
+    acc[51] = fma(pz1, v, acc[51]);
+  }
+  { const T v = Mc[31];
+    acc[31] = fma(T(1), v, acc[31]);
+    acc[46] = fma(px1, v, acc[46]);
+    acc[51] = fma(py1, v, acc[51]);
+    acc[52] = fma(pz1, v, acc[52]);
+  }
+  { const T v = Mc[32];
+    acc[32] = fma(T(1), v, acc[32]);
+    acc[47] = fma(px1, v, acc[47]);
+    acc[52] = fma(py1, v, acc[52]);
+    acc[53] = fma(pz1, v, acc[53]);
+  }
+  { const T v = Mc[33];
+    acc[33] = fma(T(1), v, acc[33]);
+    acc[48] = fma(px1, v, acc[48]);
+    acc[53] = fma(py1, v, acc[53]);
+    acc[54] = fma(pz1, v, acc[54]);
+  }
+  { const T v = Mc[34];
+    acc[34] = fma(T(1), v, acc[34]);
+  }
+  { const T v = Mc[35];
+    acc[35] = fma(T(1), v, acc[35]);
+  }
+  { const T v = Mc[36];
+    acc[36] = fma(T(1), v, acc[36]);
+  }
+  { const T v = Mc[37];
+    acc[37] = fma(T(1), v, acc[37]);
+  }
+  { const T v = Mc[38];
+    acc[38] = fma(T(1), v, acc[38]);
+  }
+  { const T v = Mc[39];
+    acc[39] = fma(T(1), v, acc[39]);
+  }
+  { const T v = Mc[40];
+    acc[40] = fma(T(1), v, acc[40]);
+  }
+  { const T v = Mc[41];
+    acc[41] = fma(T(1), v, acc[41]);
+  }
+  { const T v = Mc[42];
+    acc[42] = fma(T(1), v, acc[42]);
+  }
+  { const T v = Mc[43];
+    acc[43] = fma(T(1), v, acc[43]);
+  }
+  { const T v = Mc[44];
+    acc[44] = fma(T(1), v, acc[44]);
+  }
+  { const T v = Mc[45];
+    acc[45] = fma(T(1), v, acc[45]);
+  }
+  { const T v = Mc[46];
+    acc[46] = fma(T(1), v, acc[46]);
+  }
+  { const T v = Mc[47];
+    acc[47] = fma(T(1), v, acc[47]);
+  }
+  { const T v = Mc[48];
+    acc[48] = fma(T(1), v, acc[48]);
+  }
+  { const T v = Mc[49];
+    acc[49] = fma(T(1), v, acc[49]);
+  }
+  { const T v = Mc[50];
+    acc[50] = fma(T(1), v, acc[50]);
+  }
+  { const T v = Mc[51];
+    acc[51] = fma(T(1), v, acc[51]);
+  }
+  { const T v = Mc[52];
+    acc[52] = fma(T(1), v, acc[52]);
+  }
+  { const T v = Mc[53];
+    acc[53] = fma(T(1), v, acc[53]);
+  }
+  { const T v = Mc[54];
+    acc[54] = fma(T(1), v, acc[54]);
+  }
+}
+// L2L: local expansion Lc about a centre at -(x, y, z) from this one, order 5
+template <typename T>
+__device__ __forceinline__ void l2l_m1_p5(T x, T y, T z, const T* __restrict__ Lc, T* __restrict__ acc) {
+  const T px1 = x;
+  const T px2 = px1 * x * cinv<T>(2);
+  const T px3 = px2 * x * cinv<T>(3);
+  const T px4 = px3 * x * cinv<T>(4);
+  const T py1 = y;
+  const T py2 = py1 * y * cinv<T>(2);
+  const T py3 = py2 * y * cinv<T>(3);
+  const T py4 = py3 * y * cinv<T>(4);
+  const T pz1 = z;
+  const T pz2 = pz1 * z * cinv<T>(2);
+  const T pz3 = pz2 * z * cinv<T>(3);
+  const T pz4 = pz3 * z * cinv<T>(4);
+  const T m_1_1_0 = px1 * py1;
+  const T m_1_0_1 = px1 * pz1;
+  const T m_0_1_1 = py1 * pz1;
+  const T m_2_1_0 = px2 * py1;
+  const T m_2_0_1 = px2 * pz1;
+  const T m_1_2_0 = px1 * py2;
+  const T m_1_1_1 = px1 * py1 * pz1;
+  const T m_1_0_2 = px1 * pz2;
+  const T m_0_2_1 = py2 * pz1;
+  const T m_0_1_2 = py1 * pz2;
+  const T m_3_1_0 = px3 * py1;
+  const T m_3_0_1 = px3 * pz1;
+  const T m_2_2_0 = px2 * py2;
+  const T m_2_1_1 = px2 * py1 * pz1;
+  const T m_2_0_2 = px2 * pz2;
+  const T m_1_3_0 = px1 * py3;
+  const T m_1_2_1 = px1 * py2 * pz1;
+  const T m_1_1_2 = px1 * py1 * pz2;
+  const T m_1_0_3 = px1 * pz3;
+  const T m_0_3_1 = py3 * pz1;
+  const T m_0_2_2 = py2 * pz2;
+  const T m_0_1_3 = py1 * pz3;
+  { const T v = Lc[0];
+    acc[0] = fma(T(1), v, acc[0]);
+  }
+  { const T v = Lc[1];
+    acc[0] = fma(px1, v, acc[0]);
+    acc[1] = fma(T(1), v, acc[1]);
+  }
+  { const T v = Lc[2];
+    acc[0] = fma(py1, v, acc[0]);
+    acc[2] = fma(T(1), v, acc[2]);
+  }
+  { const T v = Lc[3];
+    acc[0] = fma(pz1, v, acc[0]);
+    acc[3] = fma(T(1), v, acc[3]);
+  }
+  { const T v = Lc[4];
+    acc[0] = fma(px2, v, acc[0]);
+    acc[1] = fma(px1, v, acc[1]);
+    acc[4] = fma(T(1), v, acc[4]);
+  }
+  { const T v = Lc[5];
+    acc[0] = fma(m_1_1_0, v, acc[0]);
+    acc[1] = fma(py1, v, acc[1]);
+    acc[2] = fma(px1, v, acc[2]);
+    acc[5] = fma(T(1), v, acc[5]);
+  }
+  { const T v = Lc[6];
+    acc[0] = fma(m_1_0_1, v, acc[0]);
+    acc[1] = fma(pz1, v, acc[1]);
+    acc[3] = fma(px1, v, acc[3]);
+    acc[6] = fma(T(1), v, acc[6]);
+  }
+  { const T v = Lc[7];
+    acc[0] = fma(py2, v, acc[0]);
+    acc[2] = fma(py1, v, acc[2]);
+    acc[7] = fma(T(1), v, acc[7]);
+  }
+  { const T v = Lc[8];
+    acc[0] = fma(m_0_1_1, v, acc[0]);
+    acc[2] = fma(pz1, v, acc[2]);
+    acc[3] = fma(py1, v, acc[3]);
+    acc[8] = fma(T(1), v, acc[8]);
+  }
+  { const T v = Lc[9];
+    acc[0] = fma(pz2, v, acc[0]);
+    acc[3] = fma(pz1, v, acc[3]);
+    acc[9] = fma(T(1), v, acc[9]);
+  }
+  { const T v = Lc[10];
+    acc[0] = fma(px3, v, acc[0]);
+    acc[1] = fma(px2, v, acc[1]);
+    acc[4] = fma(px1, v, acc[4]);
+    acc[10] = fma(T(1), v, acc[10]);
+  }
+  { const T v = Lc[11];
+    acc[0] = fma(m_2_1_0, v, acc[0]);
+    acc[1] = fma(m_1_1_0, v, acc[1]);
+    acc[2] = fma(px2, v, acc[2]);
+    acc[4] = fma(py1, v, acc[4]);
+    acc[5] = fma(px1, v, acc[5]);
+    acc[11] = fma(T(1), v, acc[11]);
+  }
+  { const T v = Lc[12];
+    acc[0] = fma(m_2_0_1, v, acc[0]);
+    acc[1] = fma(m_1_0_1, v, acc[1]);
+    acc[3] = fma(px2, v, acc[3]);
+    acc[4] = fma(pz1, v, acc[4]);
+    acc[6] = fma(px1, v, acc[6]);
+    acc[12] = fma(T(1), v, acc[12]);
+  }
+  { const T v = Lc[13];
+    acc[0] = fma(m_1_2_0, v, acc[0]);
+    acc[1] = fma(py2, v, acc[1]);
+    acc[2] = fma(m_1_1_0, v, acc[2]);
+    acc[5] = fma(py1, v, acc[5]);
+    acc[7] = fma(px1, v, acc[7]);
+    acc[13] = fma(T(1), v, acc[13]);
+  }
+  { const T v = Lc[14];
+    acc[0] = fma(m_1_1_1, v, acc[0]);
+    acc[1] = fma(m_0_1_1, v, acc[1]);
+    acc[2] = fma(m_1_0_1, v, acc[2]);
+    acc[3] = fma(m_1_1_0, v, acc[3]);
+    acc[5] = fma(pz1, v, acc[5]);
+    acc[6] = fma(py1, v, acc[6]);
+    acc[8] = fma(px1, v, acc[8]);
+    acc[14] = fma(T(1), v, acc[14]);
+  }
+  { const T v = Lc[15];
+    acc[0] = fma(m_1_0_2, v, acc[0]);
+    acc[1] = fma(pz2, v, acc[1]);
+    acc[3] = fma(m_1_0_1, v, acc[3]);
+    acc[6] = fma(pz1, v, acc[6]);
+    acc[9] = fma(px1, v, acc[9]);
+    acc[15] = fma(T(1), v, acc[15]);
+  }
+  { const T v = Lc[16];
+    acc[0] = fma(py3, v, acc[0]);
+    acc[2] = fma(py2, v, acc[2]);
+    acc[7] = fma(py1, v, acc[7]);
+    acc[16] = fma(T(1), v, acc[16]);
+  }
+  { const T v = Lc[17];
+    acc[0] = fma(m_0_2_1, v, acc[0]);
+    acc[2] = fma(m_0_1_1, v, acc[2]);
+    acc[3] = fma(py2, v, acc[3]);
+    acc[7] = fma(pz1, v, acc[7]);
+    acc[8] = fma(py1, v, acc[8]);
+    acc[17] = fma(T(1), v, acc[17]);
+  }
+  { const T v = Lc[18];
+    acc[0] = fma(m_0_1_2, v, acc[0]);
+    acc[2] = fma(pz2, v, acc[2]);
+    acc[3] = fma(m_0_1_1, v, acc[3]);
+    acc[8] = fma(pz1, v, acc[8]);
+    acc[9] = fma(py1, v, acc[9]);
+    acc[18] = fma(T(1), v, acc[18]);
+  }
+  { const T v = Lc[19];
+    acc[0] = fma(pz3, v, acc[0]);
+    acc[3] = fma(pz2, v, acc[3]);
+    acc[9] = fma(pz1, v, acc[9]);
+    acc[19] = fma(T(1), v, acc[19]);
+  }
+  { const T v = Lc[20];
+    acc[0] = fma(px4, v, acc[0]);
+    acc[1] = fma(px3, v, acc[1]);
+    acc[4] = fma(px2, v, acc[4]);
+    acc[10] = fma(px1, v, acc[10]);
+    acc[20] = fma(T(1), v, acc[20]);
+  }
+  { const T v = Lc[21];
+    acc[0] = fma(m_3_1_0, v, acc[0]);
+    acc[1] = fma(m_2_1_0, v, acc[1]);
+    acc[2] = fma(px3, v, acc[2]);
+    acc[4] = fma(m_1_1_0, v, acc[4]);
+    acc[5] = fma(px2, v, acc[5]);
+    acc[10] = fma(py1, v, acc[10]);
+    acc[11] = fma(px1, v, acc[11]);
+    acc[21] = fma(T(1), v, acc[21]);
+  }
+  { const T v = Lc[22];
+    acc[0] = fma(m_3_0_1, v, acc[0]);
+    acc[1] = fma(m_2_0_1, v, acc[1]);
+    acc[3] = fma(px3, v, acc[3]);
+    acc[4] = fma(m_1_0_1, v, acc[4]);
+    acc[6] = fma(px2, v, acc[6]);
+    acc[10] = fma(pz1, v, acc[10]);
+    acc[12] = fma(px1, v, acc[12]);
+    acc[22] = fma(T(1), v, acc[22]);
+  }
+  { const T v = Lc[23];
+    acc[0] = fma(m_2_2_0, v, acc[0]);
+    acc[1] = fma(m_1_2_0, v, acc[1]);
+    acc[2] = fma(m_2_1_0, v, acc[2]);
+    acc[4] = fma(py2, v, acc[4]);
+    acc[5] = fma(m_1_1_0, v, acc[5]);
+    acc[7] = fma(px2, v, acc[7]);
+    acc[11] = fma(py1, v, acc[11]);
+    acc[13] = fma(px1, v, acc[13]);
+    acc[23] = fma(T(1), v, acc[23]);
+  }
+  { const T v = Lc[24];
+    acc[0] = fma(m_2_1_1, v, acc[0]);
+    acc[1] = fma(m_1_1_1, v, acc[1]);
+    acc[2] = fma(m_2_0_1, v, acc[2]);
+    acc[3] = fma(m_2_1_0, v, acc[3]);
+    acc[4] = fma(m_0_1_1, v, acc[4]);
+    acc[5] = fma(m_1_0_1, v, acc[5]);
+    acc[6] = fma(m_1_1_0, v, acc[6]);
+    acc[8] = fma(px2, v, acc[8]);
+    acc[11] = fma(pz1, v, acc[11]);
+    acc[12] = fma(py1, v, acc[12]);
+    acc[14] = fma(px1, v, acc[14]);
+    acc[24] = fma(T(1), v, acc[24]);
+  }
+  { const T v = Lc[25];
+    acc[0] = fma(m_2_0_2, v, acc[0]);
+    acc[1] = fma(m_1_0_2, v, acc[1]);
+    acc[3] = fma(m_2_0_1, v, acc[3]);
+    acc[4] = fma(pz2, v, acc[4]);
+    acc[6] = fma(m_1_0_1, v, acc[6]);
+    acc[9] = fma(px2, v, acc[9]);
+    acc[12] = fma(pz1, v, acc[12]);
+    acc[15] = fma(px1, v, acc[15]);
+    acc[25] = fma(T(1), v, acc[25]);
+  }
+  { const T v = Lc[26];
+    acc[0] = fma(m_1_3_0, v, acc[0]);
+    acc[1] = fma(py3, v, acc[1]);
+    acc[2] = fma(m_1_2_0, v, acc[2]);
+    acc[5] = fma(py2, v, acc[5]);
+    acc[7] = fma(m_1_1_0, v, acc[7]);
+    acc[13] = fma(py1, v, acc[13]);
+    acc[16] = fma(px1, v, acc[16]);
+    acc[26] = fma(T(1), v, acc[26]);
+  }
+  { const T v = Lc[27];
+    acc[0] = fma(m_1_2_1, v, acc[0]);
+    acc[1] = fma(m_0_2_1, v, acc[1]);
+    acc[2] = fma(m_1_1_1, v, acc[2]);
+    acc[3] = fma(m_1_2_0, v, acc[3]);
+    acc[5] = fma(m_0_1_1, v, acc[5]);
+    acc[6] = fma(py2, v, acc[6]);
+    acc[7] = fma(m_1_0_1, v, acc[7]);
+    acc[8] = fma(m_1_1_0, v, acc[8]);
+    acc[13] = fma(pz1, v, acc[13]);
+    acc[14] = fma(py1, v, acc[14]);
+    acc[17] = fma(px1, v, acc[17]);
+    acc[27] = fma(T(1), v, acc[27]);
+  }
+  { const T v = Lc[28];
+    acc[0] = fma(m_1_1_2, v, acc[0]);
+    acc[1] = fma(m_0_1_2, v, acc[1]);
+    acc[2] = fma(m_1_0_2, v, acc[2]);
+    acc[3] = fma(m_1_1_1, v, acc[3]);
+    acc[5] = fma(pz2, v, acc[5]);
+    acc[6] = fma(m_0_1_1, v, acc[6]);
+    acc[8] = fma(m_1_0_1, v, acc[8]);
+    acc[9] = fma(m_1_1_0, v, acc[9]);
+    acc[14] = fma(pz1, v, acc[14]);
+    acc[15] = fma(py1, v, acc[15]);
+    acc[18] = fma(px1, v, acc[18]);
+    acc[28] = fma(T(1), v, acc[28]);
+  }
+  { const T v = Lc[29];
+    acc[0] = fma(m_1_0_3, v, acc[0]);
+    acc[1] = fma(pz3, v, acc[1]);
+    acc[3] = fma(m_1_0_2, v, acc[3]);
+    acc[6] = fma(pz2, v, acc[6]);
+    acc[9] = fma(m_1_0_1, v, acc[9]);
+    acc[15] = fma(pz1, v, acc[15]);
+    acc[19] = fma(px1, v, acc[19]);
+    acc[29] = fma(T(1), v, acc[29]);
+  }
+  { const T v = Lc[30];
+    acc[0] = fma(py4, v, acc[0]);
+    acc[2] = fma(py3, v, acc[2]);
+    acc[7] = fma(py2, v, acc[7]);
+    acc[16] = fma(py1, v, acc[16]);
+    acc[30] = fma(T(1), v, acc[30]);
+  }
+  { const T v = Lc[31];
+    acc[0] = fma(m_0_3_1, v, acc[0]);
+    acc[2] = fma(m_0_2_1, v, acc[2]);
+    acc[3] = fma(py3, v, acc[3]);
+    acc[7] = fma(m_0_1_1, v, acc[7]);
+    acc[8] = fma(py2, v, acc[8]);
+    acc[16] = fma(pz1, v, acc[16]);
+    acc[17] = fma(py1, v, acc[17]);
+    acc[31] = fma(T(1), v, acc[31]);
+  }
+  { const T v = Lc[32];
+    acc[0] = fma(m_0_2_2, v, acc[0]);
+    acc[2] = fma(m_0_1_2, v, acc[2]);
+    acc[3] = fma(m_0_2_1, v, acc[3]);
+    acc[7] = fma(pz2, v, acc[7]);
+    acc[8] = fma(m_0_1_1, v, acc[8]);
+    acc[9] = fma(py2, v, acc[9]);
+    acc[17] = fma(pz1, v, acc[17]);
+    acc[18] = fma(py1, v, acc[18]);
+    acc[32] = fma(T(1), v, acc[32]);
+  }
+  { const T v = Lc[33];
+    acc[0] = fma(m_0_1_3, v, acc[0]);
+    acc[2] = fma(pz3, v, acc[2]);
+    acc[3] = fma(m_0_1_2, v, acc[3]);
+    acc[8] = fma(pz2, v, acc[8]);
+    acc[9] = fma(m_0_1_1, v, acc[9]);
+    acc[18] = fma(pz1, v, acc[18]);
+    acc[19] = fma(py1, v, acc[19]);
+    acc[33] = fma(T(1), v, acc[33]);
+  }
+  { const T v = Lc[34];
+    acc[0] = fma(pz4, v, acc[0]);
+    acc[3] = fma(pz3, v, acc[3]);
+    acc[9] = fma(pz2, v, acc[9]);
+    acc[19] = fma(pz1, v, acc[19]);
+    acc[34] = fma(T(1), v, acc[34]);
+  }
+}
+// L2P: field -grad of the local expansion Lc at offset (x, y, z) = site - centre, order 5
+template <typename T>
+__device__ __forceinline__ void l2p_m1_p5(T x, T y, T z, const T* __restrict__ Lc, T& f0, T& f1, T& f2) {
+  const T px1 = x;
+  const T px2 = px1 * x * cinv<T>(2);
+  const T px3 = px2 * x * cinv<T>(3);
+  const T py1 = y;
+  const T py2 = py1 * y * cinv<T>(2);
+  const T py3 = py2 * y * cinv<T>(3);
+  const T pz1 = z;
+  const T pz2 = pz1 * z * cinv<T>(2);
+  const T pz3 = pz2 * z * cinv<T>(3);
+  const T m_1_1_0 = px1 * py1;
+  const T m_1_0_1 = px1 * pz1;
+  const T m_0_1_1 = py1 * pz1;
+  const T m_2_1_0 = px2 * py1;
+  const T m_2_0_1 = px2 * pz1;
+  const T m_1_2_0 = px1 * py2;
+  const T m_1_1_1 = px1 * py1 * pz1;
+  const T m_1_0_2 = px1 * pz2;
+  const T m_0_2_1 = py2 * pz1;
+  const T m_0_1_2 = py1 * pz2;
+  { const T v = -Lc[1];
+    f0 = fma(T(1), v, f0);
+  }
+  { const T v = -Lc[2];
+    f1 = fma(T(1), v, f1);
+  }
+  { const T v = -Lc[3];
+    f2 = fma(T(1), v, f2);
+  }
+  { const T v = -Lc[4];
+    f0 = fma(px1, v, f0);
+  }
+  { const T v = -Lc[5];
+    f0 = fma(py1, v, f0);
+    f1 = fma(px1, v, f1);
+  }
+  { const T v = -Lc[6];
+    f0 = fma(pz1, v, f0);
+    f2 = fma(px1, v, f2);
+  }
+  { const T v = -Lc[7];
+    f1 = fma(py1, v, f1);
+  }
+  { const T v = -Lc[8];
+    f1 = fma(pz1, v, f1);
+    f2 = fma(py1, v, f2);
+  }
+  { const T v = -Lc[9];
+    f2 = fma(pz1, v, f2);
+  }
+  { const T v = -Lc[10];
+    f0 = fma(px2, v, f0);
+  }
+  { const T v = -Lc[11];
+    f0 = fma(m_1_1_0, v, f0);
+    f1 = fma(px2, v, f1);
+  }
+  { const T v = -Lc[12];
+    f0 = fma(m_1_0_1, v, f0);
+    f2 = fma(px2, v, f2);
+  }
+  { const T v = -Lc[13];
+    f0 = fma(py2, v, f0);
+    f1 = fma(m_1_1_0, v, f1);
+  }
+  { const T v = -Lc[14];
+    f0 = fma(m_0_1_1, v, f0);
+    f1 = fma(m_1_0_1, v, f1);
+    f2 = fma(m_1_1_0, v, f2);
+  }
+  { const T v = -Lc[15];
+    f0 = fma(pz2, v, f0);
+    f2 = fma(m_1_0_1, v, f2);
+  }
+  { const T v = -Lc[16];
+    f1 = fma(py2, v, f1);
+  }
+  { const T v = -Lc[17];
+    f1 = fma(m_0_1_1, v, f1);
+    f2 = fma(py2, v, f2);
+  }
+  { const T v = -Lc[18];
+    f1 = fma(pz2, v, f1);
+    f2 = fma(m_0_1_1, v, f2);
+  }
+  { const T v = -Lc[19];
+    f2 = fma(pz2, v, f2);
+  }
+  { const T v = -Lc[20];
+    f0 = fma(px3, v, f0);
+  }
+  { const T v = -Lc[21];
+    f0 = fma(m_2_1_0, v, f0);
+    f1 = fma(px3, v, f1);
+  }
+  { const T v = -Lc[22];
+    f0 = fma(m_2_0_1, v, f0);
+    f2 = fma(px3, v, f2);
+  }
+  { const T v = -Lc[23];
+    f0 = fma(m_1_2_0, v, f0);
+    f1 = fma(m_2_1_0, v, f1);
+  }
+  { const T v = -Lc[24];
+    f0 = fma(m_1_1_1, v, f0);
+    f1 = fma(m_2_0_1, v, f1);
+    f2 = fma(m_2_1_0, v, f2);
+  }
+  { const T v = -Lc[25];
+    f0 = fma(m_1_0_2, v, f0);
+    f2 = fma(m_2_0_1, v, f2);
+  }
+  { const T v = -Lc[26];
+    f0 = fma(py3, v, f0);
+    f1 = fma(m_1_2_0, v, f1);
+  }
+  { const T v = -Lc[27];
+    f0 = fma(m_0_2_1, v, f0);
+    f1 = fma(m_1_1_1, v, f1);
+    f2 = fma(m_1_2_0, v, f2);
+  }
+  { const T v = -Lc[28];
+    f0 = fma(m_0_1_2, v, f0);
+    f1 = fma(m_1_0_2, v, f1);
+    f2 = fma(m_1_1_1, v, f2);
+  }
+  { const T v = -Lc[29];
+    f0 = fma(pz3, v, f0);
+    f2 = fma(m_1_0_2, v, f2);
+  }
+  { const T v = -Lc[30];
+    f1 = fma(py3, v, f1);
+  }
+  { const T v = -Lc[31];
+    f1 = fma(m_0_2_1, v, f1);
+    f2 = fma(py3, v, f2);
+  }
+  { const T v = -Lc[32];
+    f1 = fma(m_0_1_2, v, f1);
+    f2 = fma(m_0_2_1, v, f2);
+  }
+  { const T v = -Lc[33];
+    f1 = fma(pz3, v, f1);
+    f2 = fma(m_0_1_2, v, f2);
+  }
+  { const T v = -Lc[34];
+    f2 = fma(pz3, v, f2);
+  }
+}
+
+// P2M of a dipole (s0, s1, s2) at offset (x, y, z) = centre - site, order 6
+template <typename T>
+__device__ __forceinline__ void p2m_m1_p6(T x, T y, T z, T s0, T s1, T s2, T* __restrict__ acc) {
+  const T px1 = x;
+  const T px2 = px1 * x * cinv<T>(2);
+  const T px3 = px2 * x * cinv<T>(3);
+  const T px4 = px3 * x * cinv<T>(4);
+  const T px5 = px4 * x * cinv<T>(5);
+  const T py1 = y;
+  const T py2 = py1 * y * cinv<T>(2);
+  const T py3 = py2 * y * cinv<T>(3);
+  const T py4 = py3 * y * cinv<T>(4);
+  const T py5 = py4 * y * cinv<T>(5);
+  const T pz1 = z;
+  const T pz2 = pz1 * z * cinv<T>(2);
+  const T pz3 = pz2 * z * cinv<T>(3);
+  const T pz4 = pz3 * z * cinv<T>(4);
+  const T pz5 = pz4 * z * cinv<T>(5);
+  const T m_1_1_0 = px1 * py1;
+  const T m_1_0_1 = px1 * pz1;
+  const T m_0_1_1 = py1 * pz1;
+  const T m_2_1_0 = px2 * py1;
+  const T m_2_0_1 = px2 * pz1;
+  const T m_1_2_0 = px1 * py2;
+  const T m_1_1_1 = px1 * py1 * pz1;
+  const T m_1_0_2 = px1 * pz2;
+  const T m_0_2_1 = py2 * pz1;
+  const T m_0_1_2 = py1 * pz2;
+  const T m_3_1_0 = px3 * py1;
+  const T m_3_0_1 = px3 * pz1;
+  const T m_2_2_0 = px2 * py2;
+  const T m_2_1_1 = px2 * py1 * pz1;
+  const T m_2_0_2 = px2 * pz2;
+  const T m_1_3_0 = px1 * py3;
+  const T m_1_2_1 = px1 * py2 * pz1;
+  const T m_1_1_2 = px1 * py1 * pz2;
+  const T m_1_0_3 = px1 * pz3;
+  const T m_0_3_1 = py3 * pz1;
+  const T m_0_2_2 = py2 * pz2;
+  const T m_0_1_3 = py1 * pz3;
+  const T m_4_1_0 = px4 * py1;
+  const T m_4_0_1 = px4 * pz1;
+  const T m_3_2_0 = px3 * py2;
+  const T m_3_1_1 = px3 * py1 * pz1;
+  const T m_3_0_2 = px3 * pz2;
+  const T m_2_3_0 = px2 * py3;
+  const T m_2_2_1 = px2 * py2 * pz1;
+  const T m_2_1_2 = px2 * py1 * pz2;
+  const T m_2_0_3 = px2 * pz3;
+  const T m_1_4_0 = px1 * py4;
+  const T m_1_3_1 = px1 * py3 * pz1;
+  const T m_1_2_2 = px1 * py2 * pz2;
+  const T m_1_1_3 = px1 * py1 * pz3;
+  const T m_1_0_4 = px1 * pz4;
+  const T m_0_4_1 = py4 * pz1;
+  const T m_0_3_2 = py3 * pz2;
+  const T m_0_2_3 = py2 * pz3;
+  const T m_0_1_4 = py1 * pz4;
+  { const T v = s0;
+    acc[0] = fma(T(1), v, acc[0]);
+    acc[3] = fma(px1, v, acc[3]);
+    acc[4] = fma(py1, v, acc[4]);
+    acc[5] = fma(pz1, v, acc[5]);
+    acc[9] = fma(px2, v, acc[9]);
+    acc[10] = fma(m_1_1_0, v, acc[10]);
+    acc[11] = fma(m_1_0_1, v, acc[11]);
+    acc[12] = fma(py2, v, acc[12]);
+    acc[13] = fma(m_0_1_1, v, acc[13]);
+    acc[14] = fma(pz2, v, acc[14]);
+    acc[19] = fma(px3, v, acc[19]);
+    acc[20] = fma(m_2_1_0, v, acc[20]);
+    acc[21] = fma(m_2_0_1, v, acc[21]);
+    acc[22] = fma(m_1_2_0, v, acc[22]);
+    acc[23] = fma(m_1_1_1, v, acc[23]);
+    acc[24] = fma(m_1_0_2, v, acc[24]);
+    acc[25] = fma(py3, v, acc[25]);
+    acc[26] = fma(m_0_2_1, v, acc[26]);
+    acc[27] = fma(m_0_1_2, v, acc[27]);
+    acc[28] = fma(pz3, v, acc[28]);
+    acc[34] = fma(px4, v, acc[34]);
+    acc[35] = fma(m_3_1_0, v, acc[35]);
+    acc[36] = fma(m_3_0_1, v, acc[36]);
+    acc[37] = fma(m_2_2_0, v, acc[37]);
+    acc[38] = fma(m_2_1_1, v, acc[38]);
+    acc[39] = fma(m_2_0_2, v, acc[39]);
+    acc[40] = fma(m_1_3_0, v, acc[40]);
+    acc[41] = fma(m_1_2_1, v, acc[41]);
+    acc[42] = fma(m_1_1_2, v, acc[42]);
+    acc[43] = fma(m_1_0_3, v, acc[43]);
+    acc[44] = fma(py4, v, acc[44]);
+    acc[45] = fma(m_0_3_1, v, acc[45]);
+    acc[46] = fma(m_0_2_2, v, acc[46]);
+    acc[47] = fma(m_0_1_3, v, acc[47]);
+    acc[48] = fma(pz4, v, acc[48]);
+    acc[55] = fma(px5, v, acc[55]);
+    acc[56] = fma(m_4_1_0, v, acc[56]);
+    acc[57] = fma(m_4_0_1, v, acc[57]);
+    acc[58] = fma(m_3_2_0, v, acc[58]);
+    acc[59] = fma(m_3_1_1, v, acc[59]);
+    acc[60] = fma(m_3_0_2, v, acc[60]);
+    acc[61] = fma(m_2_3_0, v, acc[61]);
+    acc[62] = fma(m_2_2_1, v, acc[62]);
+    acc[63] = fma(m_2_1_2, v, acc[63]);
+    acc[64] = fma(m_2_0_3, v, acc[64]);
+    acc[65] = fma(m_1_4_0, v, acc[65]);
+    acc[66] = fma(m_1_3_1, v, acc[66]);
+    acc[67] = fma(m_1_2_2, v, acc[67]);
+    acc[68] = fma(m_1_1_3, v, acc[68]);
+    acc[69] = fma(m_1_0_4, v, acc[69]);
+    acc[70] = fma(py5, v, acc[70]);
+    acc[71] = fma(m_0_4_1, v, acc[71]);
+    acc[72] = fma(m_0_3_2, v, acc[72]);
+    acc[73] = fma(m_0_2_3, v, acc[73]);
+    acc[74] = fma(m_0_1_4, v, acc[74]);
+    acc[75] = fma(pz5, v, acc[75]);
+  }
+  { const T v = s1;
+    acc[1] = fma(T(1), v, acc[1]);
+    acc[4] = fma(px1, v, acc[4]);
+    acc[6] = fma(py1, v, acc[6]);
+    acc[7] = fma(pz1, v, acc[7]);
+    acc[10] = fma(px2, v, acc[10]);
+    acc[12] = fma(m_1_1_0, v, acc[12]);
+    acc[13] = fma(m_1_0_1, v, acc[13]);
+    acc[15] = fma(py2, v, acc[15]);
+    acc[16] = fma(m_0_1_1, v, acc[16]);
+    acc[17] = fma(pz2, v, acc[17]);
+    acc[20] = fma(px3, v, acc[20]);
+    acc[22] = fma(m_2_1_0, v, acc[22]);
+    acc[23] = fma(m_2_0_1, v, acc[23]);
+    acc[25] = fma(m_1_2_0, v, acc[25]);
+    acc[26] = fma(m_1_1_1, v, acc[26]);
+    acc[27] = fma(m_1_0_2, v, acc[27]);
+    acc[29] = fma(py3, v, acc[29]);
+    acc[30] = fma(m_0_2_1, v, acc[30]);
+    acc[31] = fma(m_0_1_2, v, acc[31]);
+    acc[32] = fma(pz3, v, acc[32]);
+    acc[35] = fma(px4, v, acc[35]);
+    acc[37] = fma(m_3_1_0, v, acc[37]);
+    acc[38] = fma(m_3_0_1, v, acc[38]);
+    acc[40] = fma(m_2_2_0, v, acc[40]);
+    acc[41] = fma(m_2_1_1, v, acc[41]);
+    acc[42] = fma(m_2_0_2, v, acc[42]);
+    acc[44] = fma(m_1_3_0, v, acc[44]);
+    acc[45] = fma(m_1_2_1, v, acc[45]);
+    acc[46] = fma(m_1_1_2, v, acc[46]);
+    acc[47] = fma(m_1_0_3, v, acc[47]);
+    acc[49] = fma(py4, v, acc[49]);
+    acc[50] = fma(m_0_3_1, v, acc[50]);
+    acc[51] = fma(m_0_2_2, v, acc[51]);
+    acc[52] = fma(m_0_1_3, v, acc[52]);
+    acc[53] = fma(pz4, v, acc[53]);
+    acc[56] = fma(px5, v, acc[56]);
+    acc[58] = fma(m_4_1_0, v, acc[58]);
+    acc[59] = fma(m_4_0_1, v, acc[59]);
+    acc[61] = fma(m_3_2_0, v, acc[61]);
+    acc[62] = fma(m_3_1_1, v, acc[62]);
+    acc[63] = fma(m_3_0_2, v, acc[63]);
+    acc[65] = fma(m_2_3_0, v, acc[65]);
+    acc[66] = fma(m_2_2_1, v, acc[66]);
+    acc[67] = fma(m_2_1_2, v, acc[67]);
+    acc[68] = fma(m_2_0_3, v, acc[68]);
+    acc[70] = fma(m_1_4_0, v, acc[70]);
+    acc[71] = fma(m_1_3_1, v, acc[71]);
+    acc[72] = fma(m_1_2_2, v, acc[72]);
+    acc[73] = fma(m_1_1_3, v, acc[73]);
+    acc[74] = fma(m_1_0_4, v, acc[74]);
+    acc[76] = fma(py5, v, acc[76]);
+    acc[77] = fma(m_0_4_1, v, acc[77]);
+    acc[78] = fma(m_0_3_2, v, acc[78]);
+    acc[79] = fma(m_0_2_3, v, acc[79]);
+    acc[80] = fma(m_0_1_4, v, acc[80]);
+    acc[81] = fma(pz5, v, acc[81]);
+  }
+  { const T v = s2;
+    acc[2] = fma(T(1), v, acc[2]);
+    acc[5] = fma(px1, v, acc[5]);
+    acc[7] = fma(py1, v, acc[7]);
+    acc[8] = fma(pz1, v, acc[8]);
+    acc[11] = fma(px2, v, acc[11]);
+    acc[13] = fma(m_1_1_0, v, acc[13]);
+    acc[14] = fma(m_1_0_1, v, acc[14]);
+    acc[16] = fma(py2, v, acc[16]);
+    acc[17] = fma(m_0_1_1, v, acc[17]);
+    acc[18] = fma(pz2, v, acc[18]);
+    acc[21] = fma(px3, v, acc[21]);
+    acc[23] = fma(m_2_1_0, v, acc[23]);
+    acc[24] = fma(m_2_0_1, v, acc[24]);
+    acc[26] = fma(m_1_2_0, v, acc[26]);
+    acc[27] = fma(m_1_1_1, v, acc[27]);
+    acc[28] = fma(m_1_0_2, v, acc[28]);
+    acc[30] = fma(py3, v, acc[30]);
+    acc[31] = fma(m_0_2_1, v, acc[31]);
+    acc[32] = fma(m_0_1_2, v, acc[32]);
+    acc[33] = fma(pz3, v, acc[33]);
+    acc[36] = fma(px4, v, acc[36]);
+    acc[38] = fma(m_3_1_0, v, acc[38]);
+    acc[39] = fma(m_3_0_1, v, acc[39]);
+    acc[41] = fma(m_2_2_0, v, acc[41]);
+    acc[42] = fma(m_2_1_1, v, acc[42]);
+    acc[43] = fma(m_2_0_2, v, acc[43]);
+    acc[45] = fma(m_1_3_0, v, acc[45]);
+    acc[46] = fma(m_1_2_1, v, acc[46]);
+    acc[47] = fma(m_1_1_2, v, acc[47]);
+    acc[48] = fma(m_1_0_3, v, acc[48]);
+    acc[50] = fma(py4, v, acc[50]);
+    acc[51] = fma(m_0_3_1, v, acc[51]);
+    acc[52] = fma(m_0_2_2, v, acc[52]);
+    acc[53] = fma(m_0_1_3, v, acc[53]);
+    acc[54] = fma(pz4, v, acc[54]);
+    acc[57] = fma(px5, v, acc[57]);
+    acc[59] = fma(m_4_1_0, v, acc[59]);
+    acc[60] = fma(m_4_0_1, v, acc[60]);
+    acc[62] = fma(m_3_2_0, v, acc[62]);
+    acc[63] = fma(m_3_1_1, v, acc[63]);
+    acc[64] = fma(m_3_0_2, v, acc[64]);
+    acc[66] = fma(m_2_3_0, v, acc[66]);
+    acc[67] = fma(m_2_2_1, v, acc[67]);
+    acc[68] = fma(m_2_1_2, v, acc[68]);
+    acc[69] = fma(m_2_0_3, v, acc[69]);
+    acc[71] = fma(m_1_4_0, v, acc[71]);
+    acc[72] = fma(m_1_3_1, v, acc[72]);
+    acc[73] = fma(m_1_2_2, v, acc[73]);
+    acc[74] = fma(m_1_1_3, v, acc[74]);
+    acc[75] = fma(m_1_0_4, v, acc[75]);
+    acc[77] = fma(py5, v, acc[77]);
+    acc[78] = fma(m_0_4_1, v, acc[78]);
+    acc[79] = fma(m_0_3_2, v, acc[79]);
+    acc[80] = fma(m_0_2_3, v, acc[80]);
+    acc[81] = fma(m_0_1_4, v, acc[81]);
+    acc[82] = fma(pz5, v, acc[82]);
+  }
+}
+// M2M: multipole Mc about a centre at (x, y, z) from this one, order 6
+template <typename T>
+__device__ __forceinline__ void m2m_m1_p6(T x, T y, T z, const T* __restrict__ Mc, T* __restrict__ acc) {
+  const T px1 = x;
+  const T px2 = px1 * x * cinv<T>(2);
+  const T px3 = px2 * x * cinv<T>(3);
+  const T px4 = px3 * x * cinv<T>(4);
+  const T px5 = px4 * x * cinv<T>(5);
+  const T py1 = y;
+  const T py2 = py1 * y * cinv<T>(2);
+  const T py3 = py2 * y * cinv<T>(3);
+  const T py4 = py3 * y * cinv<T>(4);
+  const T py5 = py4 * y * cinv<T>(5);
+  const T pz1 = z;
+  const T pz2 = pz1 * z * cinv<T>(2);
+  const T pz3 = pz2 * z * cinv<T>(3);
+  const T pz4 = pz3 * z * cinv<T>(4);
+  const T pz5 = pz4 * z * cinv<T>(5);
+  const T m_1_1_0 = px1 * py1;
+  const T m_1_0_1 = px1 * pz1;
+  const T m_0_1_1 = py1 * pz1;
+  const T m_2_1_0 = px2 * py1;
+  const T m_2_0_1 = px2 * pz1;
+  const T m_1_2_0 = px1 * py2;
+  const T m_1_1_1 = px1 * py1 * pz1;
+  const T m_1_0_2 = px1 * pz2;
+  const T m_0_2_1 = py2 * pz1;
+  const T m_0_1_2 = py1 * pz2;
+  const T m_3_1_0 = px3 * py1;
+  const T m_3_0_1 = px3 * pz1;
+  const T m_2_2_0 = px2 * py2;
+  const T m_2_1_1 = px2 * py1 * pz1;
+  const T m_2_0_2 = px2 * pz2;
+  const T m_1_3_0 = px1 * py3;
+  const T m_1_2_1 = px1 * py2 * pz1;
+  const T m_1_1_2 = px1 * py1 * pz2;
+  const T m_1_0_3 = px1 * pz3;
+  const T m_0_3_1 = py3 * pz1;
+  const T m_0_2_2 = py2 * pz2;
+  const T m_0_1_3 = py1 * pz3;
+  const T m_4_1_0 = px4 * py1;
+  const T m_4_0_1 = px4 * pz1;
+  const T m_3_2_0 = px3 * py2;
+  const T m_3_1_1 = px3 * py1 * pz1;
+  const T m_3_0_2 = px3 * pz2;
+  const T m_2_3_0 = px2 * py3;
+  const T m_2_2_1 = px2 * py2 * pz1;
+  const T m_2_1_2 = px2 * py1 * pz2;
+  const T m_2_0_3 = px2 * pz3;
+  const T m_1_4_0 = px1 * py4;
+  const T m_1_3_1 = px1 * py3 * pz1;
+  const T m_1_2_2 = px1 * py2 * pz2;
+  const T m_1_1_3 = px1 * py1 * pz3;
+  const T m_1_0_4 = px1 * pz4;
+  const T m_0_4_1 = py4 * pz1;
+  const T m_0_3_2 = py3 * pz2;
+  const T m_0_2_3 = py2 * pz3;
+  const T m_0_1_4 = py1 * pz4;
+  { const T v = Mc[0];
+    acc[0] = fma(T(1), v, acc[0]);
+    acc[3] = fma(px1, v, acc[3]);
+    acc[4] = fma(py1, v, acc[4]);
+    acc[5] = fma(pz1, v, acc[5]);
+    acc[9] = fma(px2, v, acc[9]);
+    acc[10] = fma(m_1_1_0, v, acc[10]);
+    acc[11] = fma(m_1_0_1, v, acc[11]);
+    acc[12] = fma(py2, v, acc[12]);
+    acc[13] = fma(m_0_1_1, v, acc[13]);
+    acc[14] = fma(pz2, v, acc[14]);
+    acc[19] = fma(px3, v, acc[19]);
+    acc[20] = fma(m_2_1_0, v, acc[20]);
+    acc[21] = fma(m_2_0_1, v, acc[21]);
+    acc[22] = fma(m_1_2_0, v, acc[22]);
+    acc[23] = fma(m_1_1_1, v, acc[23]);
+    acc[24] = fma(m_1_0_2, v, acc[24]);
+    acc[25] = fma(py3, v, acc[25]);
+    acc[26] = fma(m_0_2_1, v, acc[26]);
+    acc[27] = fma(m_0_1_2, v, acc[27]);
+    acc[28] = fma(pz3, v, acc[28]);
+    acc[34] = fma(px4, v, acc[34]);
+    acc[35] = fma(m_3_1_0, v, acc[35]);
+    acc[36] = fma(m_3_0_1, v, acc[36]);
+    acc[37] = fma(m_2_2_0, v, acc[37]);
+    acc[38] = fma(m_2_1_1, v, acc[38]);
+    acc[39] = fma(m_2_0_2, v, acc[39]);
+    acc[40] = fma(m_1_3_0, v, acc[40]);
+    acc[41] = fma(m_1_2_1, v, acc[41]);
+    acc[42] = fma(m_1_1_2, v, acc[42]);
+    acc[43] = fma(m_1_0_3, v, acc[43]);
+    acc[44] = fma(py4, v, acc[44]);
+    acc[45] = fma(m_0_3_1, v, acc[45]);
+    acc[46] = fma(m_0_2_2, v, acc[46]);
+    acc[47] = fma(m_0_1_3, v, acc[47]);
+    acc[48] = fma(pz4, v, acc[48]);
+    acc[55] = fma(px5, v, acc[55]);
+    acc[56] = fma(m_4_1_0, v, acc[56]);
+    acc[57] = fma(m_4_0_1, v, acc[57]);
+    acc[58] = fma(m_3_2_0, v, acc[58]);
+    acc[59] = fma(m_3_1_1, v, acc[59]);
+    acc[60] = fma(m_3_0_2, v, acc[60]);
+    acc[61] = fma(m_2_3_0, v, acc[61]);
+    acc[62] = fma(m_2_2_1, v, acc[62]);
+    acc[63] = fma(m_2_1_2, v, acc[63]);
+    acc[64] = fma(m_2_0_3, v, acc[64]);
+    acc[65] = fma(m_1_4_0, v, acc[65]);
+    acc[66] = fma(m_1_3_1, v, acc[66]);
+    acc[67] = fma(m_1_2_2, v, acc[67]);
+    acc[68] = fma(m_1_1_3, v, acc[68]);
+    acc[69] = fma(m_1_0_4, v, acc[69]);
+    acc[70] = fma(py5, v, acc[70]);
+    acc[71] = fma(m_0_4_1, v, acc[71]);
+    acc[72] = fma(m_0_3_2, v, acc[72]);
+    acc[73] = fma(m_0_2_3, v, acc[73]);
+    acc[74] = fma(m_0_1_4, v, acc[74]);
+    acc[75] = fma(pz5, v, acc[75]);
+  }
+  { const T v = Mc[1];
+    acc[1] = fma(T(1), v, acc[1]);
+    acc[4] = fma(px1, v, acc[4]);
+    acc[6] = fma(py1, v, acc[6]);
+    acc[7] = fma(pz1, v, acc[7]);
+    acc[10] = fma(px2, v, acc[10]);
+    acc[12] = fma(m_1_1_0, v, acc[12]);
+    acc[13] = fma(m_1_0_1, v, acc[13]);
+    acc[15] = fma(py2, v, acc[15]);
+    acc[16] = fma(m_0_1_1, v, acc[16]);
+    acc[17] = fma(pz2, v, acc[17]);
+    acc[20] = fma(px3, v, acc[20]);
+    acc[22] = fma(m_2_1_0, v, acc[22]);
+    acc[23] = fma(m_2_0_1, v, acc[23]);
+    acc[25] = fma(m_1_2_0, v, acc[25]);
+    acc[26] = fma(m_1_1_1, v, acc[26]);
+    acc[27] = fma(m_1_0_2, v, acc[27]);
+    acc[29] = fma(py3, v, acc[29]);
+    acc[30] = fma(m_0_2_1, v, acc[30]);
+    acc[31] = fma(m_0_1_2, v, acc[31]);
+    acc[32] = fma(pz3, v, acc[32]);
+    acc[35] = fma(px4, v, acc[35]);
+    acc[37] = fma(m_3_1_0, v, acc[37]);
+    acc[38] = fma(m_3_0_1, v, acc[38]);
+    acc[40] = fma(m_2_2_0, v, acc[40]);
+    acc[41] = fma(m_2_1_1, v, acc[41]);
+    acc[42] = fma(m_2_0_2, v, acc[42]);
+    acc[44] = fma(m_1_3_0, v, acc[44]);
+    acc[45] = fma(m_1_2_1, v, acc[45]);
+    acc[46] = fma(m_1_1_2, v, acc[46]);
+    acc[47] = fma(m_1_0_3, v, acc[47]);
+    acc[49] = fma(py4, v, acc[49]);
+    acc[50] = fma(m_0_3_1, v, acc[50]);
+    acc[51] = fma(m_0_2_2, v, acc[51]);
+    acc[52] = fma(m_0_1_3, v, acc[52]);
+    acc[53] = fma(pz4, v, acc[53]);
+    acc[56] = fma(px5, v, acc[56]);
+    acc[58] = fma(m_4_1_0, v, acc[58]);
+    acc[59] = fma(m_4_0_1, v, acc[59]);
+    acc[61] = fma(m_3_2_0, v, acc[61]);
+    acc[62] = fma(m_3_1_1, v, acc[62]);
+    acc[63] = fma(m_3_0_2, v, acc[63]);
+    acc[65] = fma(m_2_3_0, v, acc[65]);
+    acc[66] = fma(m_2_2_1, v, acc[66]);
+    acc[67] = fma(m_2_1_2, v, acc[67]);
+    acc[68] = fma(m_2_0_3, v, acc[68]);
+    acc[70] = fma(m_1_4_0, v, acc[70]);
+    acc[71] = fma(m_1_3_1, v, acc[71]);
+    acc[72] = fma(m_1_2_2, v, acc[72]);
+    acc[73] = fma(m_1_1_3, v, acc[73]);
+    acc[74] = fma(m_1_0_4, v, acc[74]);
+    acc[76] = fma(py5, v, acc[76]);
+    acc[77] = fma(m_0_4_1, v, acc[77]);
+    acc[78] = fma(m_0_3_2, v, acc[78]);
+    acc[79] = fma(m_0_2_3, v, acc[79]);
+    acc[80] = fma(m_0_1_4, v, acc[80]);
+    acc[81] = fma(pz5, v, acc[81]);
+  }
+  { const T v = Mc[2];
+    acc[2] = fma(T(1), v, acc[2]);
+    acc[5] = fma(px1, v, acc[5]);
+    acc[7] = fma(py1, v, acc[7]);
+    acc[8] = fma(pz1, v, acc[8]);
+    acc[11] = fma(px2, v, acc[11]);
+    acc[13] = fma(m_1_1_0, v, acc[13]);
+    acc[14] = fma(m_1_0_1, v, acc[14]);
+    acc[16] = fma(py2, v, acc[16]);
+    acc[17] = fma(m_0_1_1, v, acc[17]);
+    acc[18] = fma(pz2, v, acc[18]);
+    acc[21] = fma(px3, v, acc[21]);
+    acc[23] = fma(m_2_1_0, v, acc[23]);
+    acc[24] = fma(m_2_0_1, v, acc[24]);
+    acc[26] = fma(m_1_2_0, v, acc[26]);
+    acc[27] = fma(m_1_1_1, v, acc[27]);
+    acc[28] = fma(m_1_0_2, v, acc[28]);
+    acc[30] = fma(py3, v, acc[30]);
+    acc[31] = fma(m_0_2_1, v, acc[31]);
+    acc[32] = fma(m_0_1_2, v, acc[32]);
+    acc[33] = fma(pz3, v, acc[33]);
+    acc[36] = fma(px4, v, acc[36]);
+    acc[38] = fma(m_3_1_0, v, acc[38]);
+    acc[39] = fma(m_3_0_1, v, acc[39]);
+    acc[41] = fma(m_2_2_0, v, acc[41]);
+    acc[42] = fma(m_2_1_1, v, acc[42]);
+    acc[43] = fma(m_2_0_2, v, acc[43]);
+    acc[45] = fma(m_1_3_0, v, acc[45]);
+    acc[46] = fma(m_1_2_1, v, acc[46]);
+    acc[47] = fma(m_1_1_2, v, acc[47]);
+    acc[48] = fma(m_1_0_3, v, acc[48]);
+    acc[50] = fma(py4, v, acc[50]);
+    acc[51] = fma(m_0_3_1, v, acc[51]);
+    acc[52] = fma(m_0_2_2, v, acc[52]);
+    acc[53] = fma(m_0_1_3, v, acc[53]);
+    acc[54] = fma(pz4, v, acc[54]);
+    acc[57] = fma(px5, v, acc[57]);
+    acc[59] = fma(m_4_1_0, v, acc[59]);
+    acc[60] = fma(m_4_0_1, v, acc[60]);
+    acc[62] = fma(m_3_2_0, v, acc[62]);
+    acc[63] = fma(m_3_1_1, v, acc[63]);
+    acc[64] = fma(m_3_0_2, v, acc[64]);
+    acc[66] = fma(m_2_3_0, v, acc[66]);
+    acc[67] = fma(m_2_2_1, v, acc[67]);
+    acc[68] = fma(m_2_1_2, v, acc[68]);
+    acc[69] = fma(m_2_0_3, v, acc[69]);
+    acc[71] = fma(m_1_4_0, v, acc[71]);
+    acc[72] = fma(m_1_3_1, v, acc[72]);
+    acc[73] = fma(m_1_2_2, v, acc[73]);
+    acc[74] = fma(m_1_1_3, v, acc[74]);
+    acc[75] = fma(m_1_0_4, v, acc[75]);
+    acc[77] = fma(py5, v, acc[77]);
+    acc[78] = fma(m_0_4_1, v, acc[78]);
+    acc[79] = fma(m_0_3_2, v, acc[79]);
+    acc[80] = fma(m_0_2_3, v, acc[80]);
+    acc[81] = fma(m_0_1_4, v, acc[81]);
+    acc[82] = fma(pz5, v, acc[82]);
+  }
+  { const T v = Mc[3];
+    acc[3] = fma(T(1), v, acc[3]);
+    acc[9] = fma(px1, v, acc[9]);
+    acc[10] = fma(py1, v, acc[10]);
+    acc[11] = fma(pz1, v, acc[11]);
+    acc[19] = fma(px2, v, acc[19]);
+    acc[20] = fma(m_1_1_0, v, acc[20]);
+    acc[21] = fma(m_1_0_1, v, acc[21]);
+    acc[22] = fma(py2, v, acc[22]);
+    acc[23] = fma(m_0_1_1, v, acc[23]);
+    acc[24] = fma(pz2, v, acc[24]);
+    acc[34] = fma(px3, v, acc[34]);
+    acc[35] = fma(m_2_1_0, v, acc[35]);
+    acc[36] = fma(m_2_0_1, v, acc[36]);
+    acc[37] = fma(m_1_2_0, v, acc[37]);
+    acc[38] = fma(m_1_1_1, v, acc[38]);
+    acc[39] = fma(m_1_0_2, v, acc[39]);
+    acc[40] = fma(py3, v, acc[40]);
+    acc[41] = fma(m_0_2_1, v, acc[41]);
+    acc[42] = fma(m_0_1_2, v, acc[42]);
+    acc[43] = fma(pz3, v, acc[43]);
+    acc[55] = fma(px4, v, acc[55]);
+    acc[56] = fma(m_3_1_0, v, acc[56]);
+    acc[57] = fma(m_3_0_1, v, acc[57]);
+    acc[58] = fma(m_2_2_0, v, acc[58]);
+    acc[59] = fma(m_2_1_1, v, acc[59]);
+    acc[60] = fma(m_2_0_2, v, acc[60]);
+    acc[61] = fma(m_1_3_0, v, acc[61]);
+    acc[62] = fma(m_1_2_1, v, acc[62]);
+    acc[63] = fma(m_1_1_2, v, acc[63]);
+    acc[64] = fma(m_1_0_3, v, acc[64]);
+    acc[65] = fma(py4, v, acc[65]);
+    acc[66] = fma(m_0_3_1, v, acc[66]);
+    acc[67] = fma(m_0_2_2, v, acc[67]);
+    acc[68] = fma(m_0_1_3, v, acc[68]);
+    acc[69] = fma(pz4, v, acc[69]);
+  }
+  { const T v = Mc[4];
+    acc[4] = fma(T(1), v, acc[4]);
+    acc[10] = fma(px1, v, acc[10]);
+    acc[12] = fma(py1, v, acc[12]);
+    acc[13] = fma(pz1, v, acc[13]);
+    acc[20] = fma(px2, v, acc[20]);
+    acc[22] = fma(m_1_1_0, v, acc[22]);
+    acc[23] = fma(m_1_0_1, v, acc[23]);
+    acc[25] = fma(py2, v, acc[25]);
+    acc[26] = fma(m_0_1_1, v, acc[26]);
+    acc[27] = fma(pz2, v, acc[27]);
+    acc[35] = fma(px3, v, acc[35]);
+    acc[37] = fma(m_2_1_0, v, acc[37]);
+    acc[38] = fma(m_2_0_1, v, acc[38]);
+    acc[40] = fma(m_1_2_0, v, acc[40]);
+    acc[41] = fma(m_1_1_1, v, acc[41]);
+    acc[42] = fma(m_1_0_2, v, acc[42]);
+    acc[44] = fma(py3, v, acc[44]);
+    acc[45] = fma(m_0_2_1, v, acc[45]);
+    acc[46] = fma(m_0_1_2, v, acc[46]);
+    acc[47] = fma(pz3, v, acc[47]);
+    acc[56] = fma(px4, v, acc[56]);
+    acc[58] = fma(m_3_1_0, v, acc[58]);
+    acc[59] = fma(m_3_0_1, v, acc[59]);
+    acc[61] = fma(m_2_2_0, v, acc[61]);
+    acc[62] = fma(m_2_1_1, v, acc[62]);
+    acc[63] = fma(m_2_0_2, v, acc[63]);
+    acc[65] = fma(m_1_3_0, v, acc[65]);
+    acc[66] = fma(m_1_2_1, v, acc[66]);
+    acc[67] = fma(m_1_1_2, v, acc[67]);
+    acc[68] = fma(m_1_0_3, v, acc[68]);
+    acc[70] = fma(py4, v, acc[70]);
+    acc[71] = fma(m_0_3_1, v, acc[71]);
+    acc[72] = fma(m_0_2_2, v, acc[72]);
+    acc[73] = fma(m_0_1_3, v, acc[73]);
+    acc[74] = fma(pz4, v, acc[74]);
+  }
+  { const T v = Mc[5];
+    acc[5] = fma(T(1), v, acc[5]);
+    acc[11] = fma(px1, v, acc[11]);
+    acc[13] = fma(py1, v, acc[13]);
+    acc[14] = fma(pz1, v, acc[14]);
+    acc[21] = fma(px2, v, acc[21]);
+    acc[23] = fma(m_1_1_0, v, acc[23]);
+    acc[24] = fma(m_1_0_1, v, acc[24]);
+    acc[26] = fma(py2, v, acc[26]);
+    acc[27] = fma(m_0_1_1, v, acc[27]);
+    acc[28] = fma(pz2, v, acc[28]);
+    acc[36] = fma(px3, v, acc[36]);
+    acc[38] = fma(m_2_1_0, v, acc[38]);
+    acc[39] = fma(m_2_0_1, v, acc[39]);
+    acc[41] = fma(m_1_2_0, v, acc[41]);
+    acc[42] = fma(m_1_1_1, v, acc[42]);
+    acc[43] = fma(m_1_0_2, v, acc[43]);
+    acc[45] = fma(py3, v, acc[45]);
+    acc[46] = fma(m_0_2_1, v, acc[46]);
+    acc[47] = fma(m_0_1_2, v, acc[47]);
+    acc[48] = fma(pz3, v, acc[48]);
+    acc[57] = fma(px4, v, acc[57]);
+    acc[59] = fma(m_3_1_0, v, acc[59]);
+    acc[60] = fma(m_3_0_1, v, acc[60]);
+    acc[62] = fma(m_2_2_0, v, acc[62]);
+    acc[63] = fma(m_2_1_1, v, acc[63]);
+    acc[64] = fma(m_2_0_2, v, acc[64]);
+    acc[66] = fma(m_1_3_0, v, acc[66]);
+    acc[67] = fma(m_1_2_1, v, acc[67]);
+    acc[68] = fma(m_1_1_2, v, acc[68]);
+    acc[69] = fma(m_1_0_3, v, acc[69]);
+    acc[71] = fma(py4, v, acc[71]);
+    acc[72] = fma(m_0_3_1, v, acc[72]);
+    acc[73] = fma(m_0_2_2, v, acc[73]);
+    acc[74] = fma(m_0_1_3, v, acc[74]);
+    acc[75] = fma(pz4, v, acc[75]);
+  }
+  { const T v = Mc[6];
+    acc[6] = fma(T(1), v, acc[6]);
+    acc[12] = fma(px1, v, acc[12]);
+    acc[15] = fma(py1, v, acc[15]);
+    acc[16] = fma(pz1, v, acc[16]);
+    acc[22] = fma(px2, v, acc[22]);
+    acc[25] = fma(m_1_1_0, v, acc[25]);
+    acc[26] = fma(m_1_0_1, v, acc[26]);
+    acc[29] = fma(py2, v, acc[29]);
+    acc[30] = fma(m_0_1_1, v, acc[30]);
+    acc[31] = fma(pz2, v, acc[31]);
+    acc[37] = fma(px3, v, acc[37]);
+    acc[40] = fma(m_2_1_0, v, acc[40]);
+    acc[41] = fma(m_2_0_1, v, acc[41]);
+    acc[44] = fma(m_1_2_0, v, acc[44]);
+    acc[45] = fma(m_1_1_1, v, acc[45]);
+    acc[46] = fma(m_1_0_2, v, acc[46]);
+    acc[49] = fma(py3, v, acc[49]);
+    acc[50] = fma(m_0_2_1, v, acc[50]);
+    acc[51] = fma(m_0_1_2, v, acc[51]);
+    acc[52] = fma(pz3, v, acc[52]);
+    acc[58] = fma(px4, v, acc[58]);
+    acc[61] = fma(m_3_1_0, v, acc[61]);
+    acc[62] = fma(m_3_0_1, v, acc[62]);
+    acc[65] = fma(m_2_2_0, v, acc[65]);
+    acc[66] = fma(m_2_1_1, v, acc[66]);
+    acc[67] = fma(m_2_0_2, v, acc[67]);
+    acc[70] = fma(m_1_3_0, v, acc[70]);
+    acc[71] = fma(m_1_2_1, v, acc[71]);
+    acc[72] = fma(m_1_1_2, v, acc[72]);
+    acc[73] = fma(m_1_0_3, v, acc[73]);
+    acc[76] = fma(py4, v, acc[76]);
+    acc[77] = fma(m_0_3_1, v, acc[77]);
+    acc[78] = fma(m_0_2_2, v, acc[78]);
+    acc[79] = fma(m_0_1_3, v, acc[79]);
+    acc[80] = fma(pz4, v, acc[80]);
+  }
+  { const T v = Mc[7];
+    acc[7] = fma(T(1), v, acc[7]);
+    acc[13] = fma(px1, v, acc[13]);
+    acc[16] = fma(py1, v, acc[16]);
+    acc[17] = fma(pz1, v, acc[17]);
+    acc[23] = fma(px2, v, acc[23]);
+    acc[26] = fma(m_1_1_0, v, acc[26]);
+    acc[27] = fma(m_1_0_1, v, acc[27]);
+    acc[30] = fma(py2, v, acc[30]);
+    acc[31] = fma(m_0_1_1, v, acc[31]);
+    acc[32] = fma(pz2, v, acc[32]);
+    acc[38] = fma(px3, v, acc[38]);
+    acc[41] = fma(m_2_1_0, v, acc[41]);
+    acc[42] = fma(m_2_0_1, v, acc[42]);
+    acc[45] = fma(m_1_2_0, v, acc[45]);
+    acc[46] = fma(m_1_1_1, v, acc[46]);
+    acc[47] = fma(m_1_0_2, v, acc[47]);
+    acc[50] = fma(py3, v, acc[50]);
+    acc[51] = fma(m_0_2_1, v, acc[51]);
+    acc[52] = fma(m_0_1_2, v, acc[52]);
+    acc[53] = fma(pz3, v, acc[53]);
+    acc[59] = fma(px4, v, acc[59]);
+    acc[62] = fma(m_3_1_0, v, acc[62]);
+    acc[63] = fma(m_3_0_1, v, acc[63]);
+    acc[66] = fma(m_2_2_0, v, acc[66]);
+    acc[67] = fma(m_2_1_1, v, acc[67]);
+    acc[68] = fma(m_2_0_2, v, acc[68]);
+    acc[71] = fma(m_1_3_0, v, acc[71]);
+    acc[72] = fma(m_1_2_1, v, acc[72]);
+    acc[73] = fma(m_1_1_2, v, acc[73]);
+    acc[74] = fma(m_1_0_3, v, acc[74]);
+    acc[77] = fma(py4, v, acc[77]);
+    acc[78] = fma(m_0_3_1, v, acc[78]);
+    acc[79] = fma(m_0_2_2, v, acc[79]);
+    acc[80] = fma(m_0_1_3, v, acc[80]);
+    acc[81] = fma(pz4, v, acc[81]);
+  }
+  { const T v = Mc[8];
+    acc[8] = fma(T(1), v, acc[8]);
+    acc[14] = fma(px1, v, acc[14]);
+    acc[17] = fma(py1, v, acc[17]);
+    acc[18] = fma(pz1, v, acc[18]);
+    acc[24] = fma(px2, v, acc[24]);
+    acc[27] = fma(m_1_1_0, v, acc[27]);
+    acc[28] = fma(m_1_0_1, v, acc[28]);
+    acc[31] = fma(py2, v, acc[31]);
+    acc[32] = fma(m_0_1_1, v, acc[32]);
+    acc[33] = fma(pz2, v, acc[33]);
+    acc[39] = fma(px3, v, acc[39]);
+    acc[42] = fma(m_2_1_0, v, acc[42]);
+    acc[43] = fma(m_2_0_1, v, acc[43]);
+    acc[46] = fma(m_1_2_0, v, acc[46]);
+    acc[47] = fma(m_1_1_1, v, acc[47]);
+    acc[48] = fma(m_1_0_2, v, acc[48]);
+    acc[51] = fma(py3, v, acc[51]);
+    acc[52] = fma(m_0_2_1, v, acc[52]);
+    acc[53] = fma(m_0_1_2, v, acc[53]);
+    acc[54] = fma(pz3, v, acc[54]);
+    acc[60] = fma(px4, v, acc[60]);
+    acc[63] = fma(m_3_1_0, v, acc[63]);
+    acc[64] = fma(m_3_0_1, v, acc[64]);
+    acc[67] = fma(m_2_2_0, v, acc[67]);
+    acc[68] = fma(m_2_1_1, v, acc[68]);
+    acc[69] = fma(m_2_0_2, v, acc[69]);
+    acc[72] = fma(m_1_3_0, v, acc[72]);
+    acc[73] = fma(m_1_2_1, v, acc[73]);
+    acc[74] = fma(m_1_1_2, v, acc[74]);
+    acc[75] = fma(m_1_0_3, v, acc[75]);
+    acc[78] = fma(py4, v, acc[78]);
+    acc[79] = fma(m_0_3_1, v, acc[79]);
+    acc[80] = fma(m_0_2_2, v, acc[80]);
+    acc[81] = fma(m_0_1_3, v, acc[81]);
+    acc[82] = fma(pz4, v, acc[82]);
+  }
+  { const T v = Mc[9];
+    acc[9] = fma(T(1), v, acc[9]);
+    acc[19] = fma(px1, v, acc[19]);
+    acc[20] = fma(py1, v, acc[20]);
+    acc[21] = fma(pz1, v, acc[21]);
+    acc[34] = fma(px2, v, acc[34]);
+    acc[35] = fma(m_1_1_0, v, acc[35]);
+    acc[36] = fma(m_1_0_1, v, acc[36]);
+    acc[37] = fma(py2, v, acc[37]);
+    acc[38] = fma(m_0_1_1, v, acc[38]);
+    acc[39] = fma(pz2, v, acc[39]);
+    acc[55] = fma(px3, v, acc[55]);
+    acc[56] = fma(m_2_1_0, v, acc[56]);
+    acc[57] = fma(m_2_0_1, v, acc[57]);
+    acc[58] = fma(m_1_2_0, v, acc[58]);
+    acc[59] = fma(m_1_1_1, v, acc[59]);
+    acc[60] = fma(m_1_0_2, v, acc[60]);
+    acc[61] = fma(py3, v, acc[61]);
+    acc[62] = fma(m_0_2_1, v, acc[62]);
+    acc[63] = fma(m_0_1_2, v, acc[63]);
+    acc[64] = fma(pz3, v, acc[64]);
+  }
+  { const T v = Mc[10];
+    acc[10] = fma(T(1), v, acc[10]);
+    acc[20] = fma(px1, v, acc[20]);
+    acc[22] = fma(py1, v, acc[22]);
+    acc[23] = fma(pz1, v, acc[23]);
+    acc[35] = fma(px2, v, acc[35]);
+    acc[37] = fma(m_1_1_0, v, acc[37]);
+    acc[38] = fma(m_1_0_1, v, acc[38]);
+    acc[40] = fma(py2, v, acc[40]);
+    acc[41] = fma(m_0_1_1, v, acc[41]);
+    acc[42] = fma(pz2, v, acc[42]);
+    acc[56] = fma(px3, v, acc[56]);
+    acc[58] = fma(m_2_1_0, v, acc[58]);
+    acc[59] = fma(m_2_0_1, v, acc[59]);
+    acc[61] = fma(m_1_2_0, v, acc[61]);
+    acc[62] = fma(m_1_1_1, v, acc[62]);
+    acc[63] = fma(m_1_0_2, v, acc[63]);
+    acc[65] = fma(py3, v, acc[65]);
+    acc[66] = fma(m_0_2_1, v, acc[66]);
+    acc[67] = fma(m_0_1_2, v, acc[67]);
+    acc[68] = fma(pz3, v, acc[68]);
+  }
+  { const T v = Mc[11];
+    acc[11] = fma(T(1), v, acc[11]);
+    acc[21] = fma(px1, v, acc[21]);
+    acc[23] = fma(py1, v, acc[23]);
+    acc[24] = fma(pz1, v, acc[24]);
+    acc[36] = fma(px2, v, acc[36]);
+    acc[38] = fma(m_1_1_0, v, acc[38]);
+    acc[39] = fma(m_1_0_1, v, acc[39]);
+    acc[41] = fma(py2, v, acc[41]);
+    acc[42] = fma(m_0_1_1, v, acc[42]);
+    acc[43] = fma(pz2, v, acc[43]);
+    acc[57] = fma(px3, v, acc[57]);
+    acc[59] = fma(m_2_1_0, v, acc[59]);
+    acc[60] = fma(m_2_0_1, v, acc[60]);
+    acc[62] = fma(m_1_2_0, v, acc[62]);
+    acc[63] = fma(m_1_1_1, v, acc[63]);
+    acc[64] = fma(m_1_0_2, v, acc[64]);
+    acc[66] = fma(py3, v, acc[66]);
+    acc[67] = fma(m_0_2_1, v, acc[67]);
+    acc[68] = fma(m_0_1_2, v, acc[68]);
+    acc[69] = fma(pz3, v, acc[69]);
+  }
+  { const T v = Mc[12];
+    acc[12] = fma(T(1), v, acc[12]);
+    acc[22] = fma(px1, v, acc[22]);
+    acc[25] = fma(py1, v, acc[25]);
+    acc[26] = fma(pz1, v, acc[26]);
+    acc[37] = fma(px2, v, acc[37]);
+    acc[40] = fma(m_1_1_0, v, acc[40]);
+    acc[41] = fma(m_1_0_1, v, acc[41]);
+    acc[44] = fma(py2, v, acc[44]);
+    acc[45] = fma(m_0_1_1, v, acc[45]);
+    acc[46] = fma(pz2, v, acc[46]);
+    acc[58] = fma(px3, v, acc[58]);
+    acc[61] = fma(m_2_1_0, v, acc[61]);
+    acc[62] = fma(m_2_0_1, v, acc[62]);
+    acc[65] = fma(m_1_2_0, v, acc[65]);
+    acc[66] = fma(m_1_1_1, v, acc[66]);
+    acc[67] = fma(m_1_0_2, v, acc[67]);
+    acc[70] = fma(py3, v, acc[70]);
+    acc[71] = fma(m_0_2_1, v, acc[71]);
+    acc[72] = fma(m_0_1_2, v, acc[72]);
+    acc[73] = fma(pz3, v, acc[73]);
+  }
+  { const T v = Mc[13];
+    acc[13] = fma(T(1), v, acc[13]);
+    acc[23] = fma(px1, v, acc[23]);
+    acc[26] = fma(py1, v, acc[26]);
+    acc[27] = fma(pz1, v, acc[27]);
+    acc[38] = fma(px2, v, acc[38]);
+    acc[41] = fma(m_1_1_0, v, acc[41]);
+    acc[42] = fma(m_1_0_1, v, acc[42]);
+    acc[45] = fma(py2, v, acc[45]);
+    acc[46] = fma(m_0_1_1, v, acc[46]);
+    acc[47] = fma(pz2, v, acc[47]);
+    acc[59] = fma(px3, v, acc[59]);
+    acc[62] = fma(m_2_1_0, v, acc[62]);
+    acc[63] = fma(m_2_0_1, v, acc[63]);
+    acc[66] = fma(m_1_2_0, v, acc[66]);
+    acc[67] = fma(m_1_1_1, v, acc[67]);
+    acc[68] = fma(m_1_0_2, v, acc[68]);
+    acc[71] = fma(py3, v, acc[71]);
+    acc[72] = fma(m_0_2_1, v, acc[72]);
+    acc[73] = fma(m_0_1_2, v, acc[73]);
+    acc[74] = fma(pz3, v, acc[74]);
+  }
+  { const T v = Mc[14];
+    acc[14] = fma(T(1), v, acc[14]);
+    acc[24] = fma(px1, v, acc[24]);
+    acc[27] = fma(py1, v, acc[27]);
+    acc[28] = fma(pz1, v, acc[28]);
+    acc[39] = fma(px2, v, acc[39]);
+    acc[42] = fma(m_1_1_0, v, acc[42]);
+    acc[43] = fma(m_1_0_1, v, acc[43]);
+    acc[46] = fma(py2, v, acc[46]);
+    acc[47] = fma(m_0_1_1, v, acc[47]);
+    acc[48] = fma(pz2, v, acc[48]);
+    acc[60] = fma(px3, v, acc[60]);
+    acc[63] = fma(m_2_1_0, v, acc[63]);
+    acc[64] = fma(m_2_0_1, v, acc[64]);
+    acc[67] = fma(m_1_2_0, v, acc[67]);
+    acc[68] = fma(m_1_1_1, v, acc[68]);
+    acc[69] = fma(m_1_0_2, v, acc[69]);
+    acc[72] = fma(py3, v, acc[72]);
+    acc[73] = fma(m_0_2_1, v, acc[73]);
+    acc[74] = fma(m_0_1_2, v, acc[74]);
+    acc[75] = fma(pz3, v, acc[75]);
+  }
+  { const T v = Mc[15];
+    acc[15] = fma(T(1), v, acc[15]);
+    acc[25] = fma(px1, v, acc[25]);
+    acc[29] = fma(py1, v, acc[29]);
+    acc[30] = fma(pz1, v, acc[30]);
+    acc[40] = fma(px2, v, acc[40]);
+    acc[44] = fma(m_1_1_0, v, acc[44]);
+    acc[45] = fma(m_1_0_1, v, acc[45]);
+    acc[49] = fma(py2, v, acc[49]);
+    acc[50] = fma(m_0_1_1, v, acc[50]);
+    acc[51] = fma(pz2, v, acc[51]);
+    acc[61] = fma(px3, v, acc[61]);
+    acc[65] = fma(m_2_1_0, v, acc[65]);
+    acc[66] = fma(m_2_0_1, v, acc[66]);
+    acc[70] = fma(m_1_2_0, v, acc[70]);
+    acc[71] = fma(m_1_1_1, v, acc[71]);
+    acc[72] = fma(m_1_0_2, v, acc[72]);
+    acc[76] = fma(py3, v, acc[76]);
+    acc[77] = fma(m_0_2_1, v, acc[77]);
+    acc[78] = fma(m_0_1_2, v, acc[78]);
+    acc[79] = fma(pz3, v, acc[79]);
+  }
+  { const T v = Mc[16];
+    acc[16] = fma(T(1), v, acc[16]);
+    acc[26] = fma(px1, v, acc[26]);
+    acc[30] = fma(py1, v, acc[30]);
+    acc[31] = fma(pz1, v, acc[31]);
+    acc[41] = fma(px2, v, acc[41]);
+    acc[45] = fma(m_1_1_0, v, acc[45]);
+    acc[46] = fma(m_1_0_1, v, acc[46]);
+    acc[50] = fma(py2, v, acc[50]);
+    acc[51] = fma(m_0_1_1, v, acc[51]);
+    acc[52] = fma(pz2, v, acc[52]);
+    acc[62] = fma(px3, v, acc[62]);
+    acc[66] = fma(m_2_1_0, v, acc[66]);
+    acc[67] = fma(m_2_0_1, v, acc[67]);
+    acc[71] = fma(m_1_2_0, v, acc[71]);
+    acc[72] = fma(m_1_1_1, v, acc[72]);
+    acc[73] = fma(m_1_0_2, v, acc[73]);
+    acc[77] = fma(py3, v, acc[77]);
+    acc[78] = fma(m_0_2_1, v, acc[78]);
+    acc[79] = fma(m_0_1_2, v, acc[79]);
+    acc[80] = fma(pz3, v, acc[80]);
+  }
+  { const T v = Mc[17];
+    acc[17] = fma(T(1), v, acc[17]);
+    acc[27] = fma(px1, v, acc[27]);
+    acc[31] = fma(py1, v, acc[31]);
+    acc[32] = fma(pz1, v, acc[32]);
+    acc[42] = fma(px2, v, acc[42]);
+    acc[46] = fma(m_1_1_0, v, acc[46]);
+    acc[47] = fma(m_1_0_1, v, acc[47]);
+    acc[51] = fma(py2, v, acc[51]);
+    acc[52] = fma(m_0_1_1, v, acc[52]);
+    acc[53] = fma(pz2, v, acc[53]);
+    acc[63] = fma(px3, v, acc[63]);
+    acc[67] = fma(m_2_1_0, v, acc[67]);
+    acc[68] = fma(m_2_0_1, v, acc[68]);
+    acc[72] = fma(m_1_2_0, v, acc[72]);
+    acc[73] = fma(m_1_1_1, v, acc[73]);
+    acc[74] = fma(m_1_0_2, v, acc[74]);
+    acc[78] = fma(py3, v, acc[78]);
+    acc[79] = fma(m_0_2_1, v, acc[79]);
+    acc[80] = fma(m_0_1_2, v, acc[80]);
+    acc[81] = fma(pz3, v, acc[81]);
+  }
+  { const T v = Mc[18];
+    acc[18] = fma(T(1), v, acc[18]);
+    acc[28] = fma(px1, v, acc[28]);
+    acc[32] = fma(py1, v, acc[32]);
+    acc[33] = fma(pz1, v, acc[33]);
+    acc[43] = fma(px2, v, acc[43]);
+    acc[47] = fma(m_1_1_0, v, acc[47]);
+    acc[48] = fma(m_1_0_1, v, acc[48]);
+    acc[52] = fma(py2, v, acc[52]);
+    acc[53] = fma(m_0_1_1, v, acc[53]);
+    acc[54] = fma(pz2, v, acc[54]);
+    acc[64] = fma(px3, v, acc[64]);
+    acc[68] = fma(m_2_1_0, v, acc[68]);
+    acc[69] = fma(m_2_0_1, v, acc[69]);
+    acc[73] = fma(m_1_2_0, v, acc[73]);
+    acc[74] = fma(m_1_1_1, v, acc[74]);
+    acc[75] = fma(m_1_0_2, v, acc[75]);
+    acc[79] = fma(py3, v, acc[79]);
+    acc[80] = fma(m_0_2_1, v, acc[80]);
+    acc[81] = fma(m_0_1_2, v, acc[81]);
+    acc[82] = fma(pz3, v, acc[82]);
+  }
+  { const T v = Mc[19];
+    acc[19] = fma(T(1), v, acc[19]);
+    acc[34] = fma(px1, v, acc[34]);
+    acc[35] = fma(py1, v, acc[35]);
+    acc[36] = fma(pz1, v, acc[36]);
+    acc[55] = fma(px2, v, acc[55]);
+    acc[56] = fma(m_1_1_0, v, acc[56]);
+    acc[57] = fma(m_1_0_1, v, acc[57]);
+    acc[58] = fma(py2, v, acc[58]);
+    acc[59] = fma(m_0_1_1, v, acc[59]);
+    acc[60] = fma(pz2, v, acc[60]);
+  }
+  { const T v = Mc[20];
+    acc[20] = fma(T(1), v, acc[20]);
+    acc[35] = fma(px1, v, acc[35]);
+    acc[37] = fma(py1, v, acc[37]);
+    acc[38] = fma(pz1, v, acc[38]);
+    acc[56] = fma(px2, v, acc[56]);
+    acc[58] = fma(m_1_1_0, v, acc[58]);
+    acc[59] = fma(m_1_0_1, v, acc[59]);
+    acc[61] = fma(py2, v, acc[61]);
+    acc[62] = fma(m_0_1_1, v, acc[62]);
+    acc[63] = fma(pz2, v, acc[63]);
+  }
+  { const T v = Mc[21];
+    acc[21] = fma(T(1), v, acc[21]);
+    acc[36] = fma(px1, v, acc[36]);
+    acc[38] = fma(py1, v, acc[38]);
+    acc[39] = fma(pz1, v, acc[39]);
+    acc[57] = fma(px2, v, acc[57]);
+    acc[59] = fma(m_1_1_0, v, acc[59]);
+    acc[60] = fma(m_1_0_1, v, acc[60]);
+    acc[62] = fma(py2, v, acc[62]);
+    acc[63] = fma(m_0_1_1, v, acc[63]);
+    acc[64] = fma(pz2, v, acc[64]);
+  }
+  { const T v = Mc[22];
+    acc[22] = fma(T(1), v, acc[22]);
+    acc[37] = fma(px1, v, acc[37]);
+    acc[40] = fma(py1, v, acc[40]);
+    acc[41] = fma(pz1, v, acc[41]);
+    acc[58] = fma(px2, v, acc[58]);
+    acc[61] = fma(m_1_1_0, v, acc[61]);
+    acc[62] = fma(m_1_0_1, v, acc[62]);
+    acc[65] = fma(py2, v, acc[65]);
+    acc[66] = fma(m_0_1_1, v, acc[66]);
+    acc[67] = fma(pz2, v, acc[67]);
+  }
+  { const T v = Mc[23];
+    acc[23] = fma(T(1), v, acc[23]);
+    acc[38] = fma(px1, v, acc[38]);
+    acc[41] = fma(py1, v, acc[41]);
+    acc[42] = fma(pz1, v, acc[42]);
+    acc[59] = fma(px2, v, acc[59]);
+    acc[62] = fma(m_1_1_0, v, acc[62]);
+    acc[63] = fma(m_1_0_1, v, acc[63]);
+    acc[66] = fma(py2, v, acc[66]);
+    acc[67] = fma(m_0_1_1, v, acc[67]);
+    acc[68] = fma(pz2, v, acc[68]);
+  }
+  { const T v = Mc[24];
+    acc[24] = fma(T(1), v, acc[24]);
+    acc[39] = fma(px1, v, acc[39]);
+    acc[42] = fma(py1, v, acc[42]);
+    acc[43] = fma(pz1, v, acc[43]);
+    acc[60] = fma(px2, v, acc[60]);
+    acc[63] = fma(m_1_1_0, v, acc[63]);
+    acc[64] = fma(m_1_0_1, v, acc[64]);
+    acc[67] = fma(py2, v, acc[67]);
+    acc[68] = fma(m_0_1_1, v, acc[68]);
+    acc[69] = fma(pz2, v, acc[69]);
+  }
+  { const T v = Mc[25];
+    acc[25] = fma(T(1), v, acc[25]);
+    acc[40] = fma(px1, v, acc[40]);
+    acc[44] = fma(py1, v, acc[44]);
+    acc[45] = fma(pz1, v, acc[45]);
+    acc[61] = fma(px2, v, acc[61]);
+    acc[65] = fma(m_1_1_0, v, acc[65]);
+    acc[66] = fma(m_1_0_1, v, acc[66]);
+    acc[70] = fma(py2, v, acc[70]);
+    acc[71] = fma(m_0_1_1, v, acc[71]);
+    acc[72] = fma(pz2, v, acc[72]);
+  }
+  { const T v = Mc[26];
+    acc[26] = fma(T(1), v, acc[26]);
+    acc[41] = fma(px1, v, acc[41]);
+    acc[45] = fma(py1, v, acc[45]);
+    acc[46] = fma(pz1, v, acc[46]);
+    acc[62] = fma(px2, v, acc[62]);
+    acc[66] = fma(m_1_1_0, v, acc[66]);
+    acc[67] = fma(m_1_0_1, v, acc[67]);
+    acc[71] = fma(py2, v, acc[71]);
+    acc[72] = fma(m_0_1_1, v, acc[72]);
+    acc[73] = fma(pz2, v, acc[73]);
+  }
+  { const T v = Mc[27];
+    acc[27] = fma(T(1), v, acc[27]);
+    acc[42] = fma(px1, v, acc[42]);
+    acc[46] = fma(py1, v, acc[46]);
+    acc[47] = fma(pz1, v, acc[47]);
+    acc[63] = fma(px2, v, acc[63]);
+    acc[67] = fma(m_1_1_0, v, acc[67]);
+    acc[68] = fma(m_1_0_1, v, acc[68]);
+    acc[72] = fma(py2, v, acc[72]);
+    acc[73] = fma(m_0_1_1, v, acc[73]);
+    acc[74] = fma(pz2, v, acc[74]);
+  }
+  { const T v = Mc[28];
+    acc[28] = fma(T(1), v, acc[28]);
+    acc[43] = fma(px1, v, acc[43]);
+    acc[47] = fma(py1, v, acc[47]);
+    acc[48] = fma(pz1, v, acc[48]);
+    acc[64] = fma(px2, v, acc[64]);
+    acc[68] = fma(m_1_1_0, v, acc[68]);
+    acc[69] = fma(m_1_0_1, v, acc[69]);
+    acc[73] = fma(py2, v, acc[73]);
+    acc[74] = fma(m_0_1_1, v, acc[74]);
+    acc[75] = fma(pz2, v, acc[75]);
+  }
+  { const T v = Mc[29];
+    acc[29] = fma(T(1), v, acc[29]);
+    acc[44] = fma(px1, v, acc[44]);
+    acc[49] = fma(py1, v, acc[49]);
+    acc[50] = fma(pz1, v, acc[50]);
+    acc[65] = fma(px2, v, acc[65]);
+    acc[70] = fma(m_1_1_0, v, acc[70]);
+    acc[71] = fma(m_1_0_1, v, acc[71]);
+    acc[76] = fma(py2, v, acc[76]);
+    acc[77] = fma(m_0_1_1, v, acc[77]);
+    acc[78] = fma(pz2, v, acc[78]);
+  }
+  { const T v = Mc[30];
+    acc[30] = fma(T(1), v, acc[30]);
+    acc[45] = fma(px1, v, acc[45]);
+    acc[50] = fma(py1, v, acc[50]);
+    acc[51] = fma(pz1, v, acc[51]);
+    acc[66] = fma(px2, v, acc[66]);
+    acc[71] = fma(m_1_1_0, v, acc[71]);
+    acc[72] = fma(m_1_0_1, v, acc[72]);
+    acc[77] = fma(py2, v, acc[77]);
+    acc[78] = fma(m_0_1_1, v, acc[78]);
+    acc[79] = fma(pz2, v, acc[79]);
+  }
+  { const T v = Mc[31];
+    acc[31] = fma(T(1), v, acc[31]);
+    acc[46] = fma(px1, v, acc[46]);
+    acc[51] = fma(py1, v, acc[51]);
+    acc[52] = fma(pz1, v, acc[52]);
+    acc[67] = fma(px2, v, acc[67]);
+    acc[72] = fma(m_1_1_0, v, acc[72]);
+    acc[73] = fma(m_1_0_1, v, acc[73]);
+    acc[78] = fma(py2, v, acc[78]);
+    acc[79] = fma(m_0_1_1, v, acc[79]);
+    acc[80] = fma(pz2, v, acc[80]);
+  }
+  { const T v = Mc[32];
+    acc[32] = fma(T(1), v, acc[32]);
+    acc[47] = fma(px1, v, acc[47]);
+    acc[52] = fma(py1, v, acc[52]);
+    acc[53] = fma(pz1, v, acc[53]);
+    acc[68] = fma(px2, v, acc[68]);
+    acc[73] = fma(m_1_1_0, v, acc[73]);
+    acc[74] = fma(m_1_0_1, v, acc[74]);
+    acc[79] = fma(py2, v, acc[79]);
+    acc[80] = fma(m_0_1_1, v, acc[80]);
+    acc[81] = fma(pz2, v, acc[81]);
+  }
+  { const T v = Mc[33];
+    acc[33] = fma(T(1), v, acc[33]);
+    acc[48] = fma(px1, v, acc[48]);
+    acc[53] = fma(py1, v, acc[53]);
+    acc[54] = fma(pz1, v, acc[54]);
+    acc[69] = fma(px2, v, acc[69]);
+    acc[74] = fma(m_1_1_0, v, acc[74]);
+    acc[75] = fma(m_1_0_1, v, acc[75]);
+    acc[80] = fma(py2, v, acc[80]);
+    acc[81] = fma(m_0_1_1, v, acc[81]);
+    acc[82] = fma(pz2, v, acc[82]);
+  }
+  { const T v = Mc[34];
+    acc[34] = fma(T(1), v, acc[34]);
+    acc[55] = fma(px1, v, acc[55]);
+    acc[56] = fma(py1, v, acc[56]);
+    acc[57] = fma(pz1, v, acc[57]);
+  }
+  { const T v = Mc[35];
+    acc[35] = fma(T(1), v, acc[35]);
+    acc[56] = fma(px1, v, acc[56]);
+    acc[58] = fma(py1, v, acc[58]);
+    acc[59] = fma(pz1, v, acc[59]);
+  }
+  { const T v = Mc[36];
+    acc[36] = fma(T(1), v, acc[36]);
+    acc[57] = fma(px1, v, acc[57]);
+    acc[59] = fma(py1, v, acc[59]);
+    acc[60] = fma(pz1, v, acc[60]);
+  }
+  { const T v = Mc[37];
+    acc[37] = fma(T(1), v, acc[37]);
+    acc[58] = fma(px1, v, acc[58]);
+    acc[61] = fma(py1, v, acc[61]);
+    acc[62] = fma(pz1, v, acc[62]);
+  }
+  { const T v = Mc[38];
+    acc[38] = fma(T(1), v, acc[38]);
+    acc[59] = fma(px1, v, acc[59]);
+    acc[62] = fma(py1, v, acc[62]);
+    acc[63] = fma(pz1, v, acc[63]);
+  }
+  { const T v = Mc[39];
+    acc[39] = fma(T(1), v, acc[39]);
+    acc[60] = fma(px1, v, acc[60]);
+    acc[63] = fma(py1, v, acc[63]);
+    acc[64] = fma(pz1, v, acc[64]);
+  }
+  { const T v = Mc[40];
+    acc[40] = fma(T(1), v, acc[40]);
+    acc[61] = fma(px1, v, acc[61]);
+    acc[65] = fma(py1, v, acc[65]);
+    acc[66] = fma(pz1, v, acc[66]);
+  }
+  { const T v = Mc[41];
+    acc[41] = fma(T(1), v, acc[41]);
+    acc[62] = fma(px1, v, acc[62]);
+    acc[66] = fma(py1, v, acc[66]);
+    acc[67] = fma(pz1, v, acc[67]);
+  }
+  { const T v = Mc[42];
+    acc[42] = fma(T(1), v, acc[42]);
+    acc[63] = fma(px1, v, acc[63]);
+    acc[67] = fma(py1, v, acc[67]);
+    acc[68] = fma(pz1, v, acc[68]);
+  }
+  { const T v = Mc[43];
+    acc[43] = fma(T(1), v, acc[43]);
+    acc[64] = fma(px1, v, acc[64]);
+    acc[68] = fma(py1, v, acc[68]);
+    acc[69] = fma(pz1, v, acc[69]);
+  }
+  { const T v = Mc[44];
+    acc[44] = fma(T(1), v, acc[44]);
+    acc[65] = fma(px1, v, acc[65]);
+    acc[70] = fma(py1, v, acc[70]);
+    acc[71] = fma(pz1, v, acc[71]);
+  }
+  { const T v = Mc[45];
+    acc[45] = fma(T(1), v, acc[45]);
+    acc[66] = fma(px1, v, acc[66]);
+    acc[71] = fma(py1, v, acc[71]);
+    acc[72] = fma(pz1, v, acc[72]);
+  }
+  { const T v = Mc[46];
+    acc[46] = fma(T(1), v, acc[46]);
+    acc[67] = fma(px1, v, acc[67]);
+    acc[72] = fma(py1, v, acc[72]);
+    acc[73] = fma(pz1, v, acc[73]);
+  }
+  { const T v = Mc[47];
+    acc[47] = fma(T(1), v, acc[47]);
+    acc[68] = fma(px1, v, acc[68]);
+    acc[73] = fma(py1, v, acc[73]);
+    acc[74] = fma(pz1, v, acc[74]);
+  }
+  { const T v = Mc[48];
+    acc[48] = fma(T(1), v, acc[48]);
+    acc[69] = fma(px1, v, acc[69]);
+    acc[74] = fma(py1, v, acc[74]);
+    acc[75] = fma(pz1, v, acc[75]);
+  }
+  { const T v = Mc[49];
+    acc[49] = fma(T(1), v, acc[49]);
+    acc[70] = fma(px1, v, acc[70]);
+    acc[76] = fma(py1, v, acc[76]);
+    acc[77] = fma(pz1, v, acc[77]);
+  }
+  { const T v = Mc[50];
+    acc[50] = fma(T(1), v, acc[50]);
+    acc[71] = fma(px1, v, acc[71]);
+    acc[77] = fma(py1, v, acc[77]);
+    acc[78] = fma(pz1, v, acc[78]);
+  }
+  { const T v = Mc[51];
+    acc[51] = fma(T(1), v, acc[51]);
+    acc[72] = fma(px1, v, acc[72]);
+    acc[78] = fma(py1, v, acc[78]);
+    acc[79] = fma(pz1, v, acc[79]);
+  }
+  { const T v = Mc[52];
+    acc[52] = fma(T(1), v, acc[52]);
+    acc[73] = fma(px1, v, acc[73]);
+    acc[79] = fma(py1, v, acc[79]);
+    acc[80] = fma(pz1, v, acc[80]);
+  }
+  { const T v = Mc[53];
+    acc[53] = fma(T(1), v, acc[53]);
+    acc[74] = fma(px1, v, acc[74]);
+    acc[80] = fma(py1, v, acc[80]);
+    acc[81] = fma(pz1, v, acc[81]);
+  }
+  { const T v = Mc[54];
+    acc[54] = fma(T(1), v, acc[54]);
+    acc[75] = fma(px1, v, acc[75]);
+    acc[81] = fma(py1, v, acc[81]);
+    acc[82] = fma(pz1, v, acc[82]);
+  }
+  { const T v = Mc[55];
+    acc[55] = fma(T(1), v, acc[55]);
+  }
+  { const T v = Mc[56];
+    acc[56] = fma(T(1), v, acc[56]);
+  }
+  { const T v = Mc[57];
+    acc[57] = fma(T(1), v, acc[57]);
+  }
+  { const T v = Mc[58];
+    acc[58] = fma(T(1), v, acc[58]);
+  }
+  { const T v = Mc[59];
+    acc[59] = fma(T(1), v, acc[59]);
+  }
+  { const T v = Mc[60];
+    acc[60] = fma(T(1), v, acc[60]);
+  }
+  { const T v = Mc[61];
+    acc[61] = fma(T(1), v, acc[61]);
+  }
+  { const T v = Mc[62];
+    acc[62] = fma(T(1), v, acc[62]);
+  }
+  { const T v = Mc[63];
+    acc[63] = fma(T(1), v, acc[63]);
+  }
+  { const T v = Mc[64];
+    acc[64] = fma(T(1), v, acc[64]);
+  }
+  { const T v = Mc[65];
+    acc[65] = fma(T(1), v, acc[65]);
+  }
+  { const T v = Mc[66];
+    acc[66] = fma(T(1), v, acc[66]);
+  }
+  { const T v = Mc[67];
+    acc[67] = fma(T(1), v, acc[67]);
+  }
+  { const T v = Mc[68];
+    acc[68] = fma(T(1), v, acc[68]);
+  }
+  { const T v = Mc[69];
+    acc[69] = fma(T(1), v, acc[69]);
+  }
+  { const T v = Mc[70];
+    acc[70] = fma(T(1), v, acc[70]);
+  }
+  { const T v = Mc[71];
+    acc[71] = fma(T(1), v, acc[71]);
+  }
+  { const T v = Mc[72];
+    acc[72] = fma(T(1), v, acc[72]);
+  }
+  { const T v = Mc[73];
+    acc[73] = fma(T(1), v, acc[73]);
+  }
+  { const T v = Mc[74];
+    acc[74] = fma(T(1), v, acc[74]);
+  }
+  { const T v = Mc[75];
+    acc[75] = fma(T(1), v, acc[75]);
+  }
+  { const T v = Mc[76];
+    acc[76] = fma(T(1), v, acc[76]);
+  }
+  { const T v = Mc[77];
+    acc[77] = fma(T(1), v, acc[77]);
+  }
+  { const T v = Mc[78];
+    acc[78] = fma(T(1), v, acc[78]);
+  }
+  { const T v = Mc[79];
+    acc[79] = fma(T(1), v, acc[79]);
+  }
+  { const T v = Mc[80];
+    acc[80] = fma(T(1), v, acc[80]);
+  }
+  { const T v = Mc[81];
+    acc[81] = fma(T(1), v, acc[81]);
+  }
+  { const T v = Mc[82];
+    acc[82] = fma(T(1), v, acc[82]);
+  }
+}
+// L2L: local expansion Lc about a centre at -(x, y, z) from this one, order 6
+template <typename T>
+__device__ __forceinline__ void l2l_m1_p6(T x, T y, T z, const T* __restrict__ Lc, T* __restrict__ acc) {
+  const T px1 = x;
+  const T px2 = px1 * x * cinv<T>(2);
+  const T px3 = px2 * x * cinv<T>(3);
+  const T px4 = px3 * x * cinv<T>(4);
+  const T px5 = px4 * x * cinv<T>(5);
+  const T py1 = y;
+  const T py2 = py1 * y * cinv<T>(2);
+  const T py3 = py2 * y * cinv<T>(3);
+  const T py4 = py3 * y * cinv<T>(4);
+  const T py5 = py4 * y * cinv<T>(5);
+  const T pz1 = z;
+  const T pz2 = pz1 * z * cinv<T>(2);
+  const T pz3 = pz2 * z * cinv<T>(3);
+  const T pz4 = pz3 * z * cinv<T>(4);
+  const T pz5 = pz4 * z * cinv<T>(5);
+  const T m_1_1_0 = px1 * py1;
+  const T m_1_0_1 = px1 * pz1;
+  const T m_0_1_1 = py1 * pz1;
+  const T m_2_1_0 = px2 * py1;
+  const T m_2_0_1 = px2 * pz1;
+  const T m_1_2_0 = px1 * py2;
+  const T m_1_1_1 = px1 * py1 * pz1;
+  const T m_1_0_2 = px1 * pz2;
+  const T m_0_2_1 = py2 * pz1;
+  const T m_0_1_2 = py1 * pz2;
+  const T m_3_1_0 = px3 * py1;
+  const T m_3_0_1 = px3 * pz1;
+  const T m_2_2_0 = px2 * py2;
+  const T m_2_1_1 = px2 * py1 * pz1;
+  const T m_2_0_2 = px2 * pz2;
+  const T m_1_3_0 = px1 * py3;
+  const T m_1_2_1 = px1 * py2 * pz1;
+  const T m_1_1_2 = px1 * py1 * pz2;
+  const T m_1_0_3 = px1 * pz3;
+  const T m_0_3_1 = py3 * pz1;
+  const T m_0_2_2 = py2 * pz2;
+  const T m_0_1_3 = py1 * pz3;
+  const T m_4_1_0 = px4 * py1;
+  const T m_4_0_1 = px4 * pz1;
+  const T m_3_2_0 = px3 * py2;
+  const T m_3_1_1 = px3 * py1 * pz1;
+  const T m_3_0_2 = px3 * pz2;
+  const T m_2_3_0 = px2 * py3;
+  const T m_2_2_1 = px2 * py2 * pz1;
+  const T m_2_1_2 = px2 * py1 * pz2;
+  const T m_2_0_3 = px2 * pz3;
+  const T m_1_4_0 = px1 * py4;
+  const T m_1_3_1 = px1 * py3 * pz1;
+  const T m_1_2_2 = px1 * py2 * pz2;
+  const T m_1_1_3 = px1 * py1 * pz3;
+  const T m_1_0_4 = px1 * pz4;
+  const T m_0_4_1 = py4 * pz1;
+  const T m_0_3_2 = py3 * pz2;
+  const T m_0_2_3 = py2 * pz3;
+  const T m_0_1_4 = py1 * pz4;
+  { const T v = Lc[0];
+    acc[0] = fma(T(1), v, acc[0]);
+  }
+  { const T v = Lc[1];
+    acc[0] = fma(px1, v, acc[0]);
+    acc[1] = fma(T(1), v, acc[1]);
+  }
+  { const T v = Lc[2];
+    acc[0] = fma(py1, v, acc[0]);
+    acc[2] = fma(T(1), v, acc[2]);
+  }
+  { const T v = Lc[3];
+    acc[0] = fma(pz1, v, acc[0]);
+    acc[3] = fma(T(1), v, acc[3]);
+  }
+  { const T v = Lc[4];
+    acc[0] = fma(px2, v, acc[0]);
+    acc[1] = fma(px1, v, acc[1]);
+    acc[4] = fma(T(1), v, acc[4]);
+  }
+  { const T v = Lc[5];
+    acc[0] = fma(m_1_1_0, v, acc[0]);
+    acc[1] = fma(py1, v, acc[1]);
+    acc[2] = fma(px1, v, acc[2]);
+    acc[5] = fma(T(1), v, acc[5]);
+  }
+  { const T v = Lc[6];
+    acc[0] = fma(m_1_0_1, v, acc[0]);
+    acc[1] = fma(pz1, v, acc[1]);
+    acc[3] = fma(px1, v, acc[3]);
+    acc[6] = fma(T(1), v, acc[6]);
+  }
+  { const T v = Lc[7];
+    acc[0] = fma(py2, v, acc[0]);
+    acc[2] = fma(py1, v, acc[2]);
+    acc[7] = fma(T(1), v, acc[7]);
+  }
+  { const T v = Lc[8];
+    acc[0] = fma(m_0_1_1, v, acc[0]);
+    acc[2] = fma(pz1, v, acc[2]);
+    acc[3] = fma(py1, v, acc[3]);
+    acc[8] = fma(T(1), v, acc[8]);
+  }
+  { const T v = Lc[9];
+    acc[0] = fma(pz2, v, acc[0]);
+    acc[3] = fma(pz1, v, acc[3]);
+    acc[9] = fma(T(1), v, acc[9]);
+  }
+  { const T v = Lc[10];
+    acc[0] = fma(px3, v, acc[0]);
+    acc[1] = fma(px2, v, acc[1]);
+    acc[4] = fma(px1, v, acc[4]);
+    acc[10] = fma(T(1), v, acc[10]);
+  }
+  { const T v = Lc[11];
+    acc[0] = fma(m_2_1_0, v, acc[0]);
+    acc[1] = fma(m_1_1_0, v, acc[1]);
+    acc[2] = fma(px2, v, acc[2]);
+    acc[4] = fma(py1, v, acc[4]);
+    acc[5] = fma(px1, v, acc[5]);
+    acc[11] = fma(T(1), v, acc[11]);
+  }
+  { const T v = Lc[12];
+    acc[0] = fma(m_2_0_1, v, acc[0]);
+    acc[1] = fma(m_1_0_1, v, acc[1]);
+    acc[3] = fma(px2, v, acc[3]);
+    acc[4] = fma(pz1, v, acc[4]);
+    acc[6] = fma(px1, v, acc[6]);
+    acc[12] = fma(T(1), v, acc[12]);
+  }
+  { const T v = Lc[13];
+    acc[0] = fma(m_1_2_0, v, acc[0]);
+    acc[1] = fma(py2, v, acc[1]);
+    acc[2] = fma(m_1_1_0, v, acc[2]);
+    acc[5] = fma(py1, v, acc[5]);
+    acc[7] = fma(px1, v, acc[7]);
+    acc[13] = fma(T(1), v, acc[13]);
+  }
+  { const T v = Lc[14];
+    acc[0] = fma(m_1_1_1, v, acc[0]);
+    acc[1] = fma(m_0_1_1, v, acc[1]);
+    acc[2] = fma(m_1_0_1, v, acc[2]);
+    acc[3] = fma(m_1_1_0, v, acc[3]);
+    acc[5] = fma(pz1, v, acc[5]);
+    acc[6] = fma(py1, v, acc[6]);
+    acc[8] = fma(px1, v, acc[8]);
+    acc[14] = fma(T(1), v, acc[14]);
+  }
+  { const T v = Lc[15];
+    acc[0] = fma(m_1_0_2, v, acc[0]);
+    acc[1] = fma(pz2, v, acc[1]);
+    acc[3] = fma(m_1_0_1, v, acc[3]);
+    acc[6] = fma(pz1, v, acc[6]);
+    acc[9] = fma(px1, v, acc[9]);
+    acc[15] = fma(T(1), v, acc[15]);
+  }
+  { const T v = Lc[16];
+    acc[0] = fma(py3, v, acc[0]);
+    acc[2] = fma(py2, v, acc[2]);
+    acc[7] = fma(py1, v, acc[7]);
+    acc[16] = fma(T(1), v, acc[16]);
+  }
+  { const T v = Lc[17];
+    acc[0] = fma(m_0_2_1, v, acc[0]);
+    acc[2] = fma(m_0_1_1, v, acc[2]);
+    acc[3] = fma(py2, v, acc[3]);
+    acc[7] = fma(pz1, v, acc[7]);
+    acc[8] = fma(py1, v, acc[8]);
+    acc[17] = fma(T(1), v, acc[17]);
+  }
+  { const T v = Lc[18];
+    acc[0] = fma(m_0_1_2, v, acc[0]);
+    acc[2] = fma(pz2, v, acc[2]);
+    acc[3] = fma(m_0_1_1, v, acc[3]);
+    acc[8] = fma(pz1, v, acc[8]);
+    acc[9] = fma(py1, v, acc[9]);
+    acc[18] = fma(T(1), v, acc[18]);
+  }
+  { const T v = Lc[19];
+    acc[0] = fma(pz3, v, acc[0]);
+    acc[3] = fma(pz2, v, acc[3]);
+    acc[9] = fma(pz1, v, acc[9]);
+    acc[19] = fma(T(1), v, acc[19]);
+  }
+  { const T v = Lc[20];
+    acc[0] = fma(px4, v, acc[0]);
+    acc[1] = fma(px3, v, acc[1]);
+    acc[4] = fma(px2, v, acc[4]);
+    acc[10] = fma(px1, v, acc[10]);
+    acc[20] = fma(T(1), v, acc[20]);
+  }
+  { const T v = Lc[21];
+    acc[0] = fma(m_3_1_0, v, acc[0]);
+    acc[1] = fma(m_2_1_0, v, acc[1]);
+    acc[2] = fma(px3, v, acc[2]);
+    acc[4] = fma(m_1_1_0, v, acc[4]);
+    acc[5] = fma(px2, v, acc[5]);
+    acc[10] = fma(py1, v, acc[10]);
+    acc[11] = fma(px1, v, acc[11]);
+    acc[21] = fma(T(1), v, acc[21]);
+  }
+  { const T v = Lc[22];
+    acc[0] = fma(m_3_0_1, v, acc[0]);
+    acc[1] = fma(m_2_0_1, v, acc[1]);
+    acc[3] = fma(px3, v, acc[3]);
+    acc[4] = fma(m_1_0_1, v, acc[4]);
+    acc[6] = fma(px2, v, acc[6]);
+    acc[10] = fma(pz1, v, acc[10]);
+    acc[12] = fma(px1, v, acc[12]);
+    acc[22] = fma(T(1), v, acc[22]);
+  }
+  { const T v = Lc[23];
+    acc[0] = fma(m_2_2_0, v, acc[0]);
+    acc[1] = fma(m_1_2_0, v, acc[1]);
+    acc[2] = fma(m_2_1_0, v, acc[2]);
+    acc[4] = fma(py2, v, acc[4]);
+    acc[5] = fma(m_1_1_0, v, acc[5]);
+    acc[7] = fma(px2, v, acc[7]);
+    acc[11] = fma(py1, v, acc[11]);
+    acc[13] = fma(px1, v, acc[13]);
+    acc[23] = fma(T(1), v, acc[23]);
+  }
+  { const T v = Lc[24];
+    acc[0] = fma(m_2_1_1, v, acc[0]);
+    acc[1] = fma(m_1_1_1, v, acc[1]);
+    acc[2] = fma(m_2_0_1, v, acc[2]);
+    acc[3] = fma(m_2_1_0, v, acc[3]);
+    acc[4] = fma(m_0_1_1, v, acc[4]);
+    acc[5] = fma(m_1_0_1, v, acc[5]);
+    acc[6] = fma(m_1_1_0, v, acc[6]);
+    acc[8] = fma(px2, v, acc[8]);
+    acc[11] = fma(pz1, v, acc[11]);
+    acc[12] = fma(py1, v, acc[12]);
+    acc[14] = fma(px1, v, acc[14]);
+    acc[24] = fma(T(1), v, acc[24]);
+  }
+  { const T v = Lc[25];
+    acc[0] = fma(m_2_0_2, v, acc[0]);
+    acc[1] = fma(m_1_0_2, v, acc[1]);
+    acc[3] = fma(m_2_0_1, v, acc[3]);
+    acc[4] = fma(pz2, v, acc[4]);
+    acc[6] = fma(m_1_0_1, v, acc[6]);
+    acc[9] = fma(px2, v, acc[9]);
+    acc[12] = fma(pz1, v, acc[12]);
+    acc[15] = fma(px1, v, acc[15]);
+    acc[25] = fma(T(1), v, acc[25]);
+  }
+  { const T v = Lc[26];
+    acc[0] = fma(m_1_3_0, v, acc[0]);
+    acc[1] = fma(py3, v, acc[1]);
+    acc[2] = fma(m_1_2_0, v, acc[2]);
+    acc[5] = fma(py2, v, acc[5]);
+    acc[7] = fma(m_1_1_0, v, acc[7]);
+    acc[13] = fma(py1, v, acc[13]);
+    acc[16] = fma(px1, v, acc[16]);
+    acc[26] = fma(T(1), v, acc[26]);
+  }
+  { const T v = Lc[27];
+    acc[0] = fma(m_1_2_1, v, acc[0]);
+    acc[1] = fma(m_0_2_1, v, acc[1]);
+    acc[2] = fma(m_1_1_1, v, acc[2]);
+    acc[3] = fma(m_1_2_0, v, acc[3]);
+    acc[5] = fma(m_0_1_1, v, acc[5]);
+    acc[6] = fma(py2, v, acc[6]);
+    acc[7] = fma(m_1_0_1, v, acc[7]);
+    acc[8] = fma(m_1_1_0, v, acc[8]);
+    acc[13] = fma(pz1, v, acc[13]);
+    acc[14] = fma(py1, v, acc[14]);
+    acc[17] = fma(px1, v, acc[17]);
+    acc[27] = fma(T(1), v, acc[27]);
+  }
+  { const T v = Lc[28];
+    acc[0] = fma(m_1_1_2, v, acc[0]);
+    acc[1] = fma(m_0_1_2, v, acc[1]);
+    acc[2] = fma(m_1_0_2, v, acc[2]);
+    acc[3] = fma(m_1_1_1, v, acc[3]);
+    acc[5] = fma(pz2, v, acc[5]);
+    acc[6] = fma(m_0_1_1, v, acc[6]);
+    acc[8] = fma(m_1_0_1, v, acc[8]);
+    acc[9] = fma(m_1_1_0, v, acc[9]);
+    acc[14] = fma(pz1, v, acc[14]);
+    acc[15] = fma(py1, v, acc[15]);
+    acc[18] = fma(px1, v, acc[18]);
+    acc[28] = fma(T(1), v, acc[28]);
+  }
+  { const T v = Lc[29];
+    acc[0] = fma(m_1_0_3, v, acc[0]);
+    acc[1] = fma(pz3, v, acc[1]);
+    acc[3] = fma(m_1_0_2, v, acc[3]);
+    acc[6] = fma(pz2, v, acc[6]);
+    acc[9] = fma(m_1_0_1, v, acc[9]);
+    acc[15] = fma(pz1, v, acc[15]);
+    acc[19] = fma(px1, v, acc[19]);
+    acc[29] = fma(T(1), v, acc[29]);
+  }
+  { const T v = Lc[30];
+    acc[0] = fma(py4, v, acc[0]);
+    acc[2] = fma(py3, v, acc[2]);
+    acc[7] = fma(py2, v, acc[7]);
+    acc[16] = fma(py1, v, acc[16]);
+    acc[30] = fma(T(1), v, acc[30]);
+  }
+  { const T v = Lc[31];
+    acc[0] = fma(m_0_3_1, v, acc[0]);
+    acc[2] = fma(m_0_2_1, v, acc[2]);
+    acc[3] = fma(py3, v, acc[3]);
+    acc[7] = fma(m_0_1_1, v, acc[7]);
+    acc[8] = fma(py2, v, acc[8]);
+    acc[16] = fma(pz1, v, acc[16]);
+    acc[17] = fma(py1, v, acc[17]);
+    acc[31] = fma(T(1), v, acc[31]);
+  }
+  { const T v = Lc[32];
+    acc[0] = fma(m_0_2_2, v, acc[0]);
+    acc[2] = fma(m_0_1_2, v, acc[2]);
+    acc[3] = fma(m_0_2_1, v, acc[3]);
+    acc[7] = fma(pz2, v, acc[7]);
+    acc[8] = fma(m_0_1_1, v, acc[8]);
+    acc[9] = fma(py2, v, acc[9]);
+    acc[17] = fma(pz1, v, acc[17]);
+    acc[18] = fma(py1, v, acc[18]);
+    acc[32] = fma(T(1), v, acc[32]);
+  }
+  { const T v = Lc[33];
+    acc[0] = fma(m_0_1_3, v, acc[0]);
+    acc[2] = fma(pz3, v, acc[2]);
+    acc[3] = fma(m_0_1_2, v, acc[3]);
+    acc[8] = fma(pz2, v, acc[8]);
+    acc[9] = fma(m_0_1_1, v, acc[9]);
+    acc[18] = fma(pz1, v, acc[18]);
+    acc[19] = fma(py1, v, acc[19]);
+    acc[33] = fma(T(1), v, acc[33]);
+  }
+  { const T v = Lc[34];
+    acc[0] = fma(pz4, v, acc[0]);
+    acc[3] = fma(pz3, v, acc[3]);
+    acc[9] = fma(pz2, v, acc[9]);
+    acc[19] = fma(pz1, v, acc[19]);
+    acc[34] = fma(T(1), v, acc[34]);
+  }
+  { const T v = Lc[35];
+    acc[0] = fma(px5, v, acc[0]);
+    acc[1] = fma(px4, v, acc[1]);
+    acc[4] = fma(px3, v, acc[4]);
+    acc[10] = fma(px2, v, acc[10]);
+    acc[20] = fma(px1, v, acc[20]);
+    acc[35] = fma(T(1), v, acc[35]);
+  }
+  { const T v = Lc[36];
+    acc[0] = fma(m_4_1_0, v, acc[0]);
+    acc[1] = fma(m_3_1_0, v, acc[1]);
+    acc[2] = fma(px4, v, acc[2]);
+    acc[4] = fma(m_2_1_0, v, acc[4]);
+    acc[5] = fma(px3, v, acc[5]);
+    acc[10] = fma(m_1_1_0, v, acc[10]);
+    acc[11] = fma(px2, v, acc[11]);
+    acc[20] = fma(py1, v, acc[20]);
+    acc[21] = fma(px1, v, acc[21]);
+    acc[36] = fma(T(1), v, acc[36]);
+  }
+  { const T v = Lc[37];
+    acc[0] = fma(m_4_0_1, v, acc[0]);
+    acc[1] = fma(m_3_0_1, v, acc[1]);
+    acc[3] = fma(px4, v, acc[3]);
+    acc[4] = fma(m_2_0_1, v, acc[4]);
+    acc[6] = fma(px3, v, acc[6]);
+    acc[10] = fma(m_1_0_1, v, acc[10]);
+    acc[12] = fma(px2, v, acc[12]);
+    acc[20] = fma(pz1, v, acc[20]);
+    acc[22] = fma(px1, v, acc[22]);
+    acc[37] = fma(T(1), v, acc[37]);
+  }
+  { const T v = Lc[38];
+    acc[0] = fma(m_3_2_0, v, acc[0]);
+    acc[1] = fma(m_2_2_0, v, acc[1]);
+    acc[2] = fma(m_3_1_0, v, acc[2]);
+    acc[4] = fma(m_1_2_0, v, acc[4]);
+    acc[5] = fma(m_2_1_0, v, acc[5]);
+    acc[7] = fma(px3, v, acc[7]);
+    acc[10] = fma(py2, v, acc[10]);
+    acc[11] = fma(m_1_1_0, v, acc[11]);
+    acc[13] = fma(px2, v, acc[13]);
+    acc[21] = fma(py1, v, acc[21]);
+    acc[23] = fma(px1, v, acc[23]);
+    acc[38] = fma(T(1), v, acc[38]);
+  }
+  { const T v = Lc[39];
+    acc[0] = fma(m_3_1_1, v, acc[0]);
+    acc[1] = fma(m_2_1_1, v, acc[1]);
+    acc[2] = fma(m_3_0_1, v, acc[2]);
+    acc[3] = fma(m_3_1_0, v, acc[3]);
+    acc[4] = fma(m_1_1_1, v, acc[4]);
+    acc[5] = fma(m_2_0_1, v, acc[5]);
+    acc[6] = fma(m_2_1_0, v, acc[6]);
+    acc[8] = fma(px3, v, acc[8]);
+    acc[10] = fma(m_0_1_1, v, acc[10]);
+    acc[11] = fma(m_1_0_1, v, acc[11]);
+    acc[12] = fma(m_1_1_0, v, acc[12]);
+    acc[14] = fma(px2, v, acc[14]);
+    acc[21] = fma(pz1, v, acc[21]);
+    acc[22] = fma(py1, v, acc[22]);
+    acc[24] = fma(px1, v, acc[24]);
+    acc[39] = fma(T(1), v, acc[39]);
+  }
+  { const T v = Lc[40];
+    acc[0] = fma(m_3_0_2, v, acc[0]);
+    acc[1] = fma(m_2_0_2, v, acc[1]);
+    acc[3] = fma(m_3_0_1, v, acc[3]);
+    acc[4] = fma(m_1_0_2, v, acc[4]);
+    acc[6] = fma(m_2_0_1, v, acc[6]);
+    acc[9] = fma(px3, v, acc[9]);
+    acc[10] = fma(pz2, v, acc[10]);
+    acc[12] = fma(m_1_0_1, v, acc[12]);
+    acc[15] = fma(px2, v, acc[15]);
+    acc[22] = fma(pz1, v, acc[22]);
+    acc[25] = fma(px1, v, acc[25]);
+    acc[40] = fma(T(1), v, acc[40]);
+  }
+  { const T v = Lc[41];
+    acc[0] = fma(m_2_3_0, v, acc[0]);
+    acc[1] = fma(m_1_3_0, v, acc[1]);
+    acc[2] = fma(m_2_2_0, v, acc[2]);
+    acc[4] = fma(py3, v, acc[4]);
+    acc[5] = fma(m_1_2_0, v, acc[5]);
+    acc[7] = fma(m_2_1_0, v, acc[7]);
+    acc[11] = fma(py2, v, acc[11]);
+    acc[13] = fma(m_1_1_0, v, acc[13]);
+    acc[16] = fma(px2, v, acc[16]);
+    acc[23] = fma(py1, v, acc[23]);
+    acc[26] = fma(px1, v, acc[26]);
+    acc[41] = fma(T(1), v, acc[41]);
+  }
+  { const T v = Lc[42];
+    acc[0] = fma(m_2_2_1, v, acc[0]);
+    acc[1] = fma(m_1_2_1, v, acc[1]);
+    acc[2] = fma(m_2_1_1, v, acc[2]);
+    acc[3] = fma(m_2_2_0, v, acc[3]);
+    acc[4] = fma(m_0_2_1, v, acc[4]);
+    acc[5] = fma(m_1_1_1, v, acc[5]);
+    acc[6] = fma(m_1_2_0, v, acc[6]);
+    acc[7] = fma(m_2_0_1, v, acc[7]);
+    acc[8] = fma(m_2_1_0, v, acc[8]);
+    acc[11] = fma(m_0_1_1, v, acc[11]);
+    acc[12] = fma(py2, v, acc[12]);
+    acc[13] = fma(m_1_0_1, v, acc[13]);
+    acc[14] = fma(m_1_1_0, v, acc[14]);
+    acc[17] = fma(px2, v, acc[17]);
+    acc[23] = fma(pz1, v, acc[23]);
+    acc[24] = fma(py1, v, acc[24]);
+    acc[27] = fma(px1, v, acc[27]);
+    acc[42] = fma(T(1), v, acc[42]);
+  }
+  { const T v = Lc[43];
+    acc[0] = fma(m_2_1_2, v, acc[0]);
+    acc[1] = fma(m_1_1_2, v, acc[1]);
+    acc[2] = fma(m_2_0_2, v, acc[2]);
+    acc[3] = fma(m_2_1_1, v, acc[3]);
+    acc[4] = fma(m_0_1_2, v, acc[4]);
+    acc[5] = fma(m_1_0_2, v, acc[5]);
+    acc[6] = fma(m_1_1_1, v, acc[6]);
+    acc[8] = fma(m_2_0_1, v, acc[8]);
+    acc[9] = fma(m_2_1_0, v, acc[9]);
+    acc[11] = fma(pz2, v, acc[11]);
+    acc[12] = fma(m_0_1_1, v, acc[12]);
+    acc[14] = fma(m_1_0_1, v, acc[14]);
+    acc[15] = fma(m_1_1_0, v, acc[15]);
+    acc[18] = fma(px2, v, acc[18]);
+    acc[24] = fma(pz1, v, acc[24]);
+    acc[25] = fma(py1, v, acc[25]);
+    acc[28] = fma(px1, v, acc[28]);
+    acc[43] = fma(T(1), v, acc[43]);
+  }
+  { const T v = Lc[44];
+    acc[0] = fma(m_2_0_3, v, acc[0]);
+    acc[1] = fma(m_1_0_3, v, acc[1]);
+    acc[3] = fma(m_2_0_2, v, acc[3]);
+    acc[4] = fma(pz3, v, acc[4]);
+    acc[6] = fma(m_1_0_2, v, acc[6]);
+    acc[9] = fma(m_2_0_1, v, acc[9]);
+    acc[12] = fma(pz2, v, acc[12]);
+    acc[15] = fma(m_1_0_1, v, acc[15]);
+    acc[19] = fma(px2, v, acc[19]);
+    acc[25] = fma(pz1, v, acc[25]);
+    acc[29] = fma(px1, v, acc[29]);
+    acc[44] = fma(T(1), v, acc[44]);
+  }
+  { const T v = Lc[45];
+    acc[0] = fma(m_1_4_0, v, acc[0]);
+    acc[1] = fma(py4, v, acc[1]);
+    acc[2] = fma(m_1_3_0, v, acc[2]);
+    acc[5] = fma(py3, v, acc[5]);
+    acc[7] = fma(m_1_2_0, v, acc[7]);
+    acc[13] = fma(py2, v, acc[13]);
+    acc[16] = fma(m_1_1_0, v, acc[16]);
+    acc[26] = fma(py1, v, acc[26]);
+    acc[30] = fma(px1, v, acc[30]);
+    acc[45] = fma(T(1), v, acc[45]);
+  }
+  { const T v = Lc[46];
+    acc[0] = fma(m_1_3_1, v, acc[0]);
+    acc[1] = fma(m_0_3_1, v, acc[1]);
+    acc[2] = fma(m_1_2_1, v, acc[2]);
+    acc[3] = fma(m_1_3_0, v, acc[3]);
+    acc[5] = fma(m_0_2_1, v, acc[5]);
+    acc[6] = fma(py3, v, acc[6]);
+    acc[7] = fma(m_1_1_1, v, acc[7]);
+    acc[8] = fma(m_1_2_0, v, acc[8]);
+    acc[13] = fma(m_0_1_1, v, acc[13]);
+    acc[14] = fma(py2, v, acc[14]);
+    acc[16] = fma(m_1_0_1, v, acc[16]);
+    acc[17] = fma(m_1_1_0, v, acc[17]);
+    acc[26] = fma(pz1, v, acc[26]);
+    acc[27] = fma(py1, v, acc[27]);
+    acc[31] = fma(px1, v, acc[31]);
+    acc[46] = fma(T(1), v, acc[46]);
+  }
+  { const T v = Lc[47];
+    acc[0] = fma(m_1_2_2, v, acc[0]);
+    acc[1] = fma(m_0_2_2, v, acc[1]);
+    acc[2] = fma(m_1_1_2, v, acc[2]);
+    acc[3] = fma(m_1_2_1, v, acc[3]);
+    acc[5] = fma(m_0_1_2, v, acc[5]);
+    acc[6] = fma(m_0_2_1, v, acc[6]);
+    acc[7] = fma(m_1_0_2, v, acc[7]);
+    acc[8] = fma(m_1_1_1, v, acc[8]);
+    acc[9] = fma(m_1_2_0, v, acc[9]);
+    acc[13] = fma(pz2, v, acc[13]);
+    acc[14] = fma(m_0_1_1, v, acc[14]);
+    acc[15] = fma(py2, v, acc[15]);
+    acc[17] = fma(m_1_0_1, v, acc[17]);
+    acc[18] = fma(m_1_1_0, v, acc[18]);
+    acc[27] = fma(pz1, v, acc[27]);
+    acc[28] = fma(py1, v, acc[28]);
+    acc[32] = fma(px1, v, acc[32]);
+    acc[47] = fma(T(1), v, acc[47]);
+  }
+  { const T v = Lc[48];
+    acc[0] = fma(m_1_1_3, v, acc[0]);
+    acc[1] = fma(m_0_1_3, v, acc[1]);
+    acc[2] = fma(m_1_0_3, v, acc[2]);
+    acc[3] = fma(m_1_1_2, v, acc[3]);
+    acc[5] = fma(pz3, v, acc[5]);
+    acc[6] = fma(m_0_1_2, v, acc[6]);
+    acc[8] = fma(m_1_0_2, v, acc[8]);
+    acc[9] = fma(m_1_1_1, v, acc[9]);
+    acc[14] = fma(pz2, v, acc[14]);
+    acc[15] = fma(m_0_1_1, v, acc[15]);
+    acc[18] = fma(m_1_0_1, v, acc[18]);
+    acc[19] = fma(m_1_1_0, v, acc[19]);
+    acc[28] = fma(pz1, v, acc[28]);
+    acc[29] = fma(py1, v, acc[29]);
+    acc[33] = fma(px1, v, acc[33]);
+    acc[48] = fma(T(1), v, acc[48]);
+  }
+  { const T v = Lc[49];
+    acc[0] = fma(m_1_0_4, v, acc[0]);
+    acc[1] = fma(pz4, v, acc[1]);
+    acc[3] = fma(m_1_0_3, v, acc[3]);
+    acc[6] = fma(pz3, v, acc[6]);
+    acc[9] = fma(m_1_0_2, v, acc[9]);
+    acc[15] = fma(pz2, v, acc[15]);
+    acc[19] = fma(m_1_0_1, v, acc[19]);
+    acc[29] = fma(pz1, v, acc[29]);
+    acc[34] = fma(px1, v, acc[34]);
+    acc[49] = fma(T(1), v, acc[49]);
+  }
+  { const T v = Lc[50];
+    acc[0] = fma(py5, v, acc[0]);
+    acc[2] = fma(py4, v, acc[2]);
+    acc[7] = fma(py3, v, acc[7]);
+    acc[16] = fma(py2, v, acc[16]);
+    acc[30] = fma(py1, v, acc[30]);
+    acc[50] = fma(T(1), v, acc[50]);
+  }
+  { const T v = Lc[51];
+    acc[0] = fma(m_0_4_1, v, acc[0]);
+    acc[2] = fma(m_0_3_1, v, acc[2]);
+    acc[3] = fma(py4, v, acc[3]);
+    acc[7] = fma(m_0_2_1, v, acc[7]);
+    acc[8] = fma(py3, v, acc[8]);
+    acc[16] = fma(m_0_1_1, v, acc[16]);
+    acc[17] = fma(py2, v, acc[17]);
+    acc[30] = fma(pz1, v, acc[30]);
+    acc[31] = fma(py1, v, acc[31]);
+    acc[51] = fma(T(1), v, acc[51]);
+  }
+  { const T v = Lc[52];
+    acc[0] = fma(m_0_3_2, v, acc[0]);
+    acc[2] = fma(m_0_2_2, v, acc[2]);
+    acc[3] = fma(m_0_3_1, v, acc[3]);
+    acc[7] = fma(m_0_1_2, v, acc[7]);
+    acc[8] = fma(m_0_2_1, v, acc[8]);
+    acc[9] = fma(py3, v, acc[9]);
+    acc[16] = fma(pz2, v, acc[16]);
+    acc[17] = fma(m_0_1_1, v, acc[17]);
+    acc[18] = fma(py2, v, acc[18]);
+    acc[31] = fma(pz1, v, acc[31]);
+    acc[32] = fma(py1, v, acc[32]);
+    acc[52] = fma(T(1), v, acc[52]);
+  }
+  { const T v = Lc[53];
+    acc[0] = fma(m_0_2_3, v, acc[0]);
+    acc[2] = fma(m_0_1_3, v, acc[2]);
+    acc[3] = fma(m_0_2_2, v, acc[3]);
+    acc[7] = fma(pz3, v, acc[7]);
+    acc[8] = fma(m_0_1_2, v, acc[8]);
+    acc[9] = fma(m_0_2_1, v, acc[9]);
+    acc[17] = fma(pz2, v, acc[17]);
+    acc[18] = fma(m_0_1_1, v, acc[18]);
+    acc[19] = fma(py2, v, acc[19]);
+    acc[32] = fma(pz1, v, acc[32]);
+    acc[33] = fma(py1, v, acc[33]);
+    acc[53] = fma(T(1), v, acc[53]);
+  }
+  { const T v = Lc[54];
+    acc[0] = fma(m_0_1_4, v, acc[0]);
+    acc[2] = fma(pz4, v, acc[2]);
+    acc[3] = fma(m_0_1_3, v, acc[3]);
+    acc[8] = fma(pz3, v, acc[8]);
+    acc[9] = fma(m_0_1_2, v, acc[9]);
+    acc[18] = fma(pz2, v, acc[18]);
+    acc[19] = fma(m_0_1_1, v, acc[19]);
+    acc[33] = fma(pz1, v, acc[33]);
+    acc[34] = fma(py1, v, acc[34]);
+    acc[54] = fma(T(1), v, acc[54]);
+  }
+  { const T v = Lc[55];
+    acc[0] = fma(pz5, v, acc[0]);
+    acc[3] = fma(pz4, v, acc[3]);
+    acc[9] = fma(pz3, v, acc[9]);
+    acc[19] = fma(pz2, v, acc[19]);
+    acc[34] = fma(pz1, v, acc[34]);
+    acc[55] = fma(T(1), v, acc[55]);
+  }
+}
+// L2P: field -grad of the local expansion Lc at offset (x, y, z) = site - centre, order 6
+template <typename T>
+__device__ __forceinline__ void l2p_m1_p6(T x, T y, T z, const T* __restrict__ Lc, T& f0, T& f1, T& f2) {
+  const T px1 = x;
+  const T px2 = px1 * x * cinv<T>(2);
+  const T px3 = px2 * x * cinv<T>(3);
+  const T px4 = px3 * x * cinv<T>(4);
+  const T py1 = y;
+  const T py2 = py1 * y * cinv<T>(2);
+  const T py3 = py2 * y * cinv<T>(3);
+  const T py4 = py3 * y * cinv<T>(4);
+  const T pz1 = z;
+  const T pz2 = pz1 * z * cinv<T>(2);
+  const T pz3 = pz2 * z * cinv<T>(3);
+  const T pz4 = pz3 * z * cinv<T>(4);
+  const T m_1_1_0 = px1 * py1;
+  const T m_1_0_1 = px1 * pz1;
+  const T m_0_1_1 = py1 * pz1;
+  const T m_2_1_0 = px2 * py1;
+  const T m_2_0_1 = px2 * pz1;
+  const T m_1_2_0 = px1 * py2;
+  const T m_1_1_1 = px1 * py1 * pz1;
+  const T m_1_0_2 = px1 * pz2;
+  const T m_0_2_1 = py2 * pz1;
+  const T m_0_1_2 = py1 * pz2;
+  const T m_3_1_0 = px3 * py1;
+  const T m_3_0_1 = px3 * pz1;
+  const T m_2_2_0 = px2 * py2;
+  const T m_2_1_1 = px2 * py1 * pz1;
+  const T m_2_0_2 = px2 * pz2;
+  const T m_1_3_0 = px1 * py3;
+  const T m_1_2_1 = px1 * py2 * pz1;
+  const T m_1_1_2 = px1 * py1 * pz2;
+  const T m_1_0_3 = px1 * pz3;
+  const T m_0_3_1 = py3 * pz1;
+  const T m_0_2_2 = py2 * pz2;
+  const T m_0_1_3 = py1 * pz3;
+  { const T v = -Lc[1];
+    f0 = fma(T(1), v, f0);
+  }
+  { const T v = -Lc[2];
+    f1 = fma(T(1), v, f1);
+  }
+  { const T v = -Lc[3];
+    f2 = fma(T(1), v, f2);
+  }
+  { const T v = -Lc[4];
+    f0 = fma(px1, v, f0);
+  }
+  { const T v = -Lc[5];
+    f0 = fma(py1, v, f0);
+    f1 = fma(px1, v, f1);
+  }
+  { const T v = -Lc[6];
+    f0 = fma(pz1, v, f0);
+    f2 = fma(px1, v, f2);
+  }
+  { const T v = -Lc[7];
+    f1 = fma(py1, v, f1);
+  }
+  { const T v = -Lc[8];
+    f1 = fma(pz1, v, f1);
+    f2 = fma(py1, v, f2);
+  }
+  { const T v = -Lc[9];
+    f2 = fma(pz1, v, f2);
+  }
+  { const T v = -Lc[10];
+    f0 = fma(px2, v, f0);
+  }
+  { const T v = -Lc[11];
+    f0 = fma(m_1_1_0, v, f0);
+    f1 = fma(px2, v, f1);
+  }
+  { const T v = -Lc[12];
+    f0 = fma(m_1_0_1, v, f0);
+    f2 = fma(px2, v, f2);
+  }
+  { const T v = -Lc[13];
+    f0 = fma(py2, v, f0);
+    f1 = fma(m_1_1_0, v, f1);
+  }
+  { const T v = -Lc[14];
+    f0 = fma(m_0_1_1, v, f0);
+    f1 = fma(m_1_0_1, v, f1);
+    f2 = fma(m_1_1_0, v, f2);
+  }
+  { const T v = -Lc[15];
+    f0 = fma(pz2, v, f0);
+    f2 = fma(m_1_0_1, v, f2);
+  }
+  { const T v = -Lc[16];
+    f1 = fma(py2, v, f1);
+  }
+  { const T v = -Lc[17];
+    f1 = fma(m_0_1_1, v, f1);
+    f2 = fma(py2, v, f2);
+  }
+  { const T v = -Lc[18];
+    f1 = fma(pz2, v, f1);
+    f2 = fma(m_0_1_1, v, f2);
+  }
+  { const T v = -Lc[19];
+    f2 = fma(pz2, v, f2);
+  }
+  { const T v = -Lc[20];
+    f0 = fma(px3, v, f0);
+  }
+  { const T v = -Lc[21];
+    f0 = fma(m_2_1_0, v, f0);
+    f1 = fma(px3, v, f1);
+  }
+  { const T v = -Lc[22];
+    f0 = fma(m_2_0_1, v, f0);
+    f2 = fma(px3, v, f2);
+  }
+  { const T v = -Lc[23];
+    f0 = fma(m_1_2_0, v, f0);
+    f1 = fma(m_2_1_0, v, f1);
+  }
+  { const T v = -Lc[24];
+    f0 = fma(m_1_1_1, v, f0);
+    f1 = fma(m_2_0_1, v, f1);
+    f2 = fma(m_2_1_0, v, f2);
+  }
+  { const T v = -Lc[25];
+    f0 = fma(m_1_0_2, v, f0);
+    f2 = fma(m_2_0_1, v, f2);
+  }
+  { const T v = -Lc[26];
+    f0 = fma(py3, v, f0);
+    f1 = fma(m_1_2_0, v, f1);
+  }
+  { const T v = -Lc[27];
+    f0 = fma(m_0_2_1, v, f0);
+    f1 = fma(m_1_1_1, v, f1);
+    f2 = fma(m_1_2_0, v, f2);
+  }
+  { const T v = -Lc[28];
+    f0 = fma(m_0_1_2, v, f0);
+    f1 = fma(m_1_0_2, v, f1);
+    f2 = fma(m_1_1_1, v, f2);
+  }
+  { const T v = -Lc[29];
+    f0 = fma(pz3, v, f0);
+    f2 = fma(m_1_0_2, v, f2);
+  }
+  { const T v = -Lc[30];
+    f1 = fma(py3, v, f1);
+  }
+  { const T v = -Lc[31];
+    f1 = fma(m_0_2_1, v, f1);
+    f2 = fma(py3, v, f2);
+  }
+  { const T v = -Lc[32];
+    f1 = fma(m_0_1_2, v, f1);
+    f2 = fma(m_0_2_1, v, f2);
+  }
+  { const T v = -Lc[33];
+    f1 = fma(pz3, v, f1);
+    f2 = fma(m_0_1_2, v, f2);
+  }
+  { const T v = -Lc[34];
+    f2 = fma(pz3, v, f2);
+  }
+  { const T v = -Lc[35];
+    f0 = fma(px4, v, f0);
+  }
+  { const T v = -Lc[36];
+    f0 = fma(m_3_1_0, v, f0);
+    f1 = fma(px4, v, f1);
+  }
+  { const T v = -Lc[37];
+    f0 = fma(m_3_0_1, v, f0);
+    f2 = fma(px4, v, f2);
+  }
+  { const T v = -Lc[38];
+    f0 = fma(m_2_2_0, v, f0);
+    f1 = fma(m_3_1_0, v, f1);
+  }
+  { const T v = -Lc[39];
+    f0 = fma(m_2_1_1, v, f0);
+    f1 = fma(m_3_0_1, v, f1);
+    f2 = fma(m_3_1_0, v, f2);
+  }
+  { const T v = -Lc[40];
+    f0 = fma(m_2_0_2, v, f0);
+    f2 = fma(m_3_0_1, v, f2);
+  }
+  { const T v = -Lc[41];
+    f0 = fma(m_1_3_0, v, f0);
+    f1 = fma(m_2_2_0, v, f1);
+  }
+  { const T v = -Lc[42];
+    f0 = fma(m_1_2_1, v, f0);
+    f1 = fma(m_2_1_1, v, f1);
+    f2 = fma(m_2_2_0, v, f2);
+  }
+  { const T v = -Lc[43];
+    f0 = fma(m_1_1_2, v, f0);
+    f1 = fma(m_2_0_2, v, f1);
+    f2 = fma(m_2_1_1, v, f2);
+  }
+  { const T v = -Lc[44];
+    f0 = fma(m_1_0_3, v, f0);
+    f2 = fma(m_2_0_2, v, f2);
+  }
+  { const T v = -Lc[45];
+    f0 = fma(py4, v, f0);
+    f1 = fma(m_1_3_0, v, f1);
+  }
+  { const T v = -Lc[46];
+    f0 = fma(m_0_3_1, v, f0);
+    f1 = fma(m_1_2_1, v, f1);
+    f2 = fma(m_1_3_0, v, f2);
+  }
+  { const T v = -Lc[47];
+    f0 = fma(m_0_2_2, v, f0);
+    f1 = fma(m_1_1_2, v, f1);
+    f2 = fma(m_1_2_1, v, f2);
+  }
+  { const T v = -Lc[48];
+    f0 = fma(m_0_1_3, v, f0);
+    f1 = fma(m_1_0_3, v, f1);
+    f2 = fma(m_1_1_2, v, f2);
+  }
+  { const T v = -Lc[49];
+    f0 = fma(pz4, v, f0);
+    f2 = fma(m_1_0_3, v, f2);
+  }
+  { const T v = -Lc[50];
+    f1 = fma(py4, v, f1);
+  }
+  { const T v = -Lc[51];
+    f1 = fma(m_0_3_1, v, f1);
+    f2 = fma(py4, v, f2);
+  }
+  { const T v = -Lc[52];
+    f1 = fma(m_0_2_2, v, f1);
+    f2 = fma(m_0_3_1, v, f2);
+  }
+  { const T v = -Lc[53];
+    f1 = fma(m_0_1_3, v, f1);
+    f2 = fma(m_0_2_2, v, f2);
+  }
+  { const T v = -Lc[54];
+    f1 = fma(pz4, v, f1);
+    f2 = fma(m_0_1_3, v, f2);
+  }
+  { const T v = -Lc[55];
+    f2 = fma(pz4, v, f2);
+  }
+}
+
 #define CPPE_M2L_GENERATED(X) \
   X(1, 5, m2l_m1_p5, 35, 55) \
   X(1, 6, m2l_m1_p6, 56, 83)
+
+#define CPPE_SHIFTS_GENERATED(X) \
+  X(1, 5, 35, 55) \
+  X(1, 6, 56, 83)
