@@ -36,6 +36,7 @@ void Geometry::combine(const std::vector<const Geometry*>& parts, int copies, Ge
   TreeLayout& L = out.layout;
   out.fmm       = any_fmm;
   out.ncrit     = parts[0]->ncrit;
+  out.damping   = parts[0]->damping;
   out.theta     = parts[0]->theta;
   // cells: by (level, segment, cell)
   std::vector<std::vector<int>> cmap(nseg);
@@ -341,6 +342,7 @@ void BatchSystem::init(int nsys, const int* site_offset, const double* xyz, cons
       ei.assign(excl_idx + excl_ptr[o0], excl_idx + excl_ptr[o0 + ns]);
     }
     const bool fmm = ns >= direct_below;
+    parts[s].damping = o.damp ? o.damping_factor : 0.0;
     parts[s].prepare(ns, xyz + 3 * (size_t)o0, sd.data(), excl_ptr ? ep.data() : nullptr,
                      ei.empty() ? nullptr : ei.data(), fmm, o.tree_ncrit, o.theta);
     pp.push_back(&parts[s]);

@@ -31,6 +31,10 @@ namespace cg {
 
 constexpr int P2P_BLOCK  = 128;
 constexpr int P2P_TILE   = 512;  // source sites staged in shared memory per tile
+// lower bound of the Thole argument v from which a near-field pair is
+// evaluated without damping in FP32 (1 - f_T < 2e-9 there) and without the
+// double-float exponential in the residual pass
+constexpr double P2P_UNDAMPED_V = 27.0;
 constexpr int M2L_WARPS  = 4;
 constexpr int P2M_LEAF_SITES  = 128;  // sites staged per round of the leaf P2M
 constexpr int M2M_TASK_LEAVES = 8;    // leaf multipoles shifted per upward-pass task
@@ -283,6 +287,52 @@ void Geometry::make_schedules() {
       h_cell_chunk_ptr[c + 1] = (int)h_m2l_chunks.size();
     }
   if (h_lanc_cell.empty()) h_lanc_cell.push_back(0);
+  // ---- damping split of every target's source list, from a lower bound of
+  // the Thole argument v = damping s_i s_j R over the two leaves (box
+  // distance, smallest s; a site without damping partner counts as
+  // s = infinity): leaves with v >= 27 for every pair (Thole factors 1 to
+  // FP32 rounding, and the double-float exponential not needed) are moved to
+  // the end of the list (stable, so a second call changes nothing), from
+  // position h_leaf_split[a] on.
+  if ((int)h_leaf_split.size() != L.nleaves) {
+    h_leaf_split.assign(L.nleaves, 0);
+    for (int a = 0; a < L.nleaves; ++a) h_leaf_split[a] = L.p2p_ptr[a + 1];
+    if (damping > 0.0 && L.nleaves > 0) {
+      std::vector<double> box(6 * (size_t)L.nleaves), smin(L.nleaves);
+      for (int a = 0; a < L.nleaves; ++a) {
+        double* bx = &box[6 * (size_t)a];
+        bx[0] = bx[1] = bx[2] = 1e300;
+        bx[3] = bx[4] = bx[5] = -1e300;
+        smin[a] = 1e300;
+        for (int k = L.leaf_start[a]; k < L.leaf_start[a + 1]; ++k) {
+          const double4_32a& q = h_pos64[k];
+          bx[0] = std::min(bx[0], q.x), bx[1] = std::min(bx[1], q.y), bx[2] = std::min(bx[2], q.z);
+          bx[3] = std::max(bx[3], q.x), bx[4] = std::max(bx[4], q.y), bx[5] = std::max(bx[5], q.z);
+          smin[a] = std::min(smin[a], q.w > 0.0 ? q.w : 1e300);
+        }
+      }
+      std::vector<int> nearer, farther;
+      for (int a = 0; a < L.nleaves; ++a) {
+        const double* ba = &box[6 * (size_t)a];
+        nearer.clear(), farther.clear();
+        for (int q = L.p2p_ptr[a]; q < L.p2p_ptr[a + 1]; ++q) {
+          const int b      = L.p2p_src[q];
+          const double* bb = &box[6 * (size_t)b];
+          double r2 = 0.0;
+          for (int c = 0; c < 3; ++c) {
+            const double d = std::max(0.0, std::max(ba[c] - bb[c + 3], bb[c] - ba[c + 3]));
+            r2 += d * d;
+          }
+          const double v = 0.999 * damping * smin[a] * smin[b] * std::sqrt(r2);
+          (v >= P2P_UNDAMPED_V ? farther : nearer).push_back(b);
+        }
+        int q = L.p2p_ptr[a];
+        for (int b : nearer) layout.p2p_src[q++] = b;
+        h_leaf_split[a] = q;
+        for (int b : farther) layout.p2p_src[q++] = b;
+      }
+    }
+  }
   // ---- near-field work items
   long total          = 0;
   for (int a = 0; a < L.nleaves; ++a) {
@@ -317,15 +367,19 @@ void Geometry::make_schedules() {
   }
   std::stable_sort(its.begin(), its.end(), [](const It& x, const It& y) { return x.w > y.w; });
   h_items.resize(its.size());
+  h_item_split.resize(its.size());
   nslot = 1;
   for (size_t k = 0; k < its.size(); ++k) {
-    h_items[k] = its[k].v;
-    nslot      = std::max(nslot, its[k].v.w + 1);
+    const int4 v    = its[k].v;
+    h_items[k]      = v;
+    h_item_split[k] = std::max(v.y, std::min(v.z, h_leaf_split[v.x]));
+    nslot           = std::max(nslot, v.w + 1);
   }
 }
 
 void Geometry::upload_schedules(cudaStream_t s) {
   items.upload(h_items, s);
+  item_split.upload(h_item_split, s);
   leaf_nslot.upload(h_leaf_nslot, s);
   if (!h_m2l_chunks.empty()) m2l_chunks.upload(h_m2l_chunks, s);
   cell_chunk_ptr.upload(h_cell_chunk_ptr, s);
@@ -341,6 +395,7 @@ void Geometry::upload(cudaStream_t s) {
     dd_exp.upload(tab, s);
   }
   items.upload(h_items, s);
+  item_split.upload(h_item_split, s);
   leaf_nslot.upload(h_leaf_nslot, s);
   if (!h_p2m_tasks.empty()) p2m_tasks.upload(h_p2m_tasks, s);
   task_leaf.upload(h_task_leaf, s);
@@ -710,7 +765,7 @@ constexpr int P2P32_PAIRS = 512;  // staged source pairs per tile (1,024 sources
 template <bool DAMP>
 __global__ void __launch_bounds__(P2P_BLOCK)
       k_p2p32_m1(int n, const int* __restrict__ leaf_start, const int4* __restrict__ items,
-                 const int* __restrict__ p2p_src, const float4* __restrict__ hi,
+                 const int* __restrict__ item_split, const int* __restrict__ p2p_src, const float4* __restrict__ hi,
                  const float4* __restrict__ lo, const float* __restrict__ src, float damping,
                  float* __restrict__ Fnear) {
   constexpr int TILE = 2 * P2P32_PAIRS;
@@ -723,6 +778,7 @@ __global__ void __launch_bounds__(P2P_BLOCK)
 
   const int4 it = items[blockIdx.x];
   const int A = it.x, b0 = it.y, b1 = it.z, slot = it.w;
+  const int sp = item_split[blockIdx.x];
   const int a0 = leaf_start[A], nA = leaf_start[A + 1] - a0;
   const float4 oh = hi[a0], ol = lo[a0];
   auto rel = [&](int k) {
@@ -746,10 +802,14 @@ __global__ void __launch_bounds__(P2P_BLOCK)
       AI[p] = f2(-1.4426950408889634f * damping * m.w);
     }
     Comp3<float> acc[2];
-    if (threadIdx.x == 0) s_plan.cur = b0, s_plan.coff = 0;
+    // phase 0: sources [b0, sp) with the Thole factors; phase 1: [sp, b1),
+    // every pair with v >= 27 (the factors equal 1 to FP32 rounding)
+    for (int ph = 0; ph < 2; ++ph) {
+    const int pend = ph == 0 ? sp : b1;
+    if (threadIdx.x == 0) s_plan.cur = ph == 0 ? b0 : sp, s_plan.coff = 0;
     __syncthreads();
     while (true) {
-      if (threadIdx.x < 32) plan_tile<TILE>(s_plan, b1, p2p_src, leaf_start);
+      if (threadIdx.x < 32) plan_tile<TILE>(s_plan, pend, p2p_src, leaf_start);
       __syncthreads();
       const int np = s_plan.np;
       if (np == 0) break;
@@ -778,18 +838,26 @@ __global__ void __launch_bounds__(P2P_BLOCK)
         float2 FX[2], FY[2], FZ[2];
 #pragma unroll
         for (int p = 0; p < 2; ++p) FX[p] = FY[p] = FZ[p] = f2(0.f);
+        auto sweep = [&](auto damped) {
+          constexpr bool D = decltype(damped)::value;
 #pragma unroll 1
-        for (int jj = g; jj < npairs; jj += S) {
-          Src2 q;
-          q.xy = s_xy[jj], q.zs = s_zs[jj], q.mxy = s_mxy[jj], q.mz = s_mz[jj];
+          for (int jj = g; jj < npairs; jj += S) {
+            Src2 q;
+            q.xy = s_xy[jj], q.zs = s_zs[jj], q.mxy = s_mxy[jj], q.mz = s_mz[jj];
 #pragma unroll
-          for (int p = 0; p < 2; ++p)
-            f32x2_pair_m1<DAMP>(nX[p], nY[p], nZ[p], AI[p], q, FX[p], FY[p], FZ[p]);
-        }
+            for (int p = 0; p < 2; ++p)
+              f32x2_pair_m1<D>(nX[p], nY[p], nZ[p], AI[p], q, FX[p], FY[p], FZ[p]);
+          }
+        };
+        if (DAMP && ph == 0)
+          sweep(std::true_type{});
+        else
+          sweep(std::false_type{});
 #pragma unroll
         for (int p = 0; p < 2; ++p) acc[p].add(FX[p].x + FX[p].y, FY[p].x + FY[p].y, FZ[p].x + FZ[p].y);
       }
       __syncthreads();
+    }
     }
     if (active) {
       float* r = &s_red[(g * T + t) * 6];
@@ -822,7 +890,9 @@ __global__ void __launch_bounds__(P2P_BLOCK)
 // term), accumulated in DD and written in FP64.  Separations are exact in
 // their high parts because the FP32 coordinates are snapped to a common grid.
 // ---------------------------------------------------------------------------
-template <bool DAMP>
+// MODE 0: any v; 1: every v >= 20 (the double-float exponential is never
+// needed); 2: every v >= 50 (no damping).
+template <bool DAMP, int MODE = 0>
 __device__ __forceinline__ void dd_pair_m1(const SiteRec<float>& ti, dd ai,
                                            const SiteRec<float>& sj, const float* mu,
                                            const float2* etab, dd (&f)[3]) {
@@ -836,13 +906,13 @@ __device__ __forceinline__ void dd_pair_m1(const SiteRec<float>& ti, dd ai,
   const dd ir3 = dd_mul(ir2, ir);
   dd G1        = dd_neg(ir3);
   dd G2        = dd_mul_f(dd_mul(ir3, ir2), 3.f);
-  if (DAMP) {
+  if (DAMP && MODE < 2) {
     const dd a = dd_mul(ai, dd{sj.s, sj.ls});
     if (a.h > 0.f) {
       const dd v = dd_mul(a, dd_mul(r2, ir));
       if (v.h < 50.f) {
         dd fE, fT;
-        if (v.h < 20.f) {
+        if (MODE == 0 && v.h < 20.f) {
           const dd e  = dd_exp_neg(v, etab);
           const dd v2 = dd_sqr(v);
           const dd u  = dd_add(dd_two_sum(1.f, v.h), dd{0.5f * v2.h, v.l + 0.5f * v2.l});
@@ -873,7 +943,7 @@ __device__ __forceinline__ void dd_pair_m1(const SiteRec<float>& ti, dd ai,
 template <bool DAMP>
 __global__ void __launch_bounds__(P2P_BLOCK)
       k_p2p_dd(int n, const int* __restrict__ leaf_start, const int4* __restrict__ items,
-               const int* __restrict__ p2p_src, PosArgs<float> pa,
+               const int* __restrict__ item_split, const int* __restrict__ p2p_src, PosArgs<float> pa,
                const float2* __restrict__ src, const float2* __restrict__ etab,
                double damping, double* __restrict__ Fnear) {
   __shared__ SiteRec<float> s_rec[P2P_TILE];
@@ -885,6 +955,7 @@ __global__ void __launch_bounds__(P2P_BLOCK)
   for (int k = threadIdx.x; k < DD_EXP_TAB; k += P2P_BLOCK) s_etab[k] = etab[k];
   const int4 it = items[blockIdx.x];
   const int A = it.x, b0 = it.y, b1 = it.z, slot = it.w;
+  const int sp = item_split[blockIdx.x];
   const int a0 = leaf_start[A], nA = leaf_start[A + 1] - a0;
   const dd dmp = dd_from(damping);
 
@@ -900,10 +971,14 @@ __global__ void __launch_bounds__(P2P_BLOCK)
     const dd ai0 = dd_mul(dmp, dd{me0.s, me0.ls}), ai1 = dd_mul(dmp, dd{me1.s, me1.ls});
     dd f0[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
     dd f1[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-    if (threadIdx.x == 0) s_plan.cur = b0, s_plan.coff = 0;
+    // phase 0: sources [b0, sp); phase 1: [sp, b1), every pair with v >= 27
+    // (never the double-float exponential)
+    for (int ph = 0; ph < 2; ++ph) {
+    const int pend = ph == 0 ? sp : b1;
+    if (threadIdx.x == 0) s_plan.cur = ph == 0 ? b0 : sp, s_plan.coff = 0;
     __syncthreads();
     while (true) {
-      if (threadIdx.x < 32) plan_tile(s_plan, b1, p2p_src, leaf_start);
+      if (threadIdx.x < 32) plan_tile(s_plan, pend, p2p_src, leaf_start);
       __syncthreads();
       const int np = s_plan.np;
       if (np == 0) break;
@@ -919,14 +994,22 @@ __global__ void __launch_bounds__(P2P_BLOCK)
       }
       __syncthreads();
       if (active) {
-        for (int jj = g; jj < total; jj += S) {
-          const SiteRec<float> sj = s_rec[jj];
-          const float* mu         = &s_mu[jj * 6];
-          dd_pair_m1<DAMP>(me0, ai0, sj, mu, s_etab, f0);
-          dd_pair_m1<DAMP>(me1, ai1, sj, mu, s_etab, f1);
-        }
+        auto sweep = [&](auto mode) {
+          constexpr int MD = decltype(mode)::value;
+          for (int jj = g; jj < total; jj += S) {
+            const SiteRec<float> sj = s_rec[jj];
+            const float* mu         = &s_mu[jj * 6];
+            dd_pair_m1<DAMP, MD>(me0, ai0, sj, mu, s_etab, f0);
+            dd_pair_m1<DAMP, MD>(me1, ai1, sj, mu, s_etab, f1);
+          }
+        };
+        if (!DAMP || ph == 0)
+          sweep(std::integral_constant<int, 0>{});
+        else
+          sweep(std::integral_constant<int, 1>{});
       }
       __syncthreads();
+    }
     }
     if (active) {
       double* r = &s_red[(g * T2 + t) * 6];
@@ -1465,10 +1548,10 @@ static void launch_p2p(const Geometry& g, bool damp, bool fast, const T* src, T 
   if constexpr (std::is_same<T, float>::value && M == 1) {
     if (damp)
       k_p2p32_m1<true><<<grid, P2P_BLOCK, 0, s>>>(
-            g.n, g.leaf_start.p, g.items.p, g.p2p_src.p, g.hi32.p, g.lo32.p, src, damping, Fnear);
+            g.n, g.leaf_start.p, g.items.p, g.item_split.p, g.p2p_src.p, g.hi32.p, g.lo32.p, src, damping, Fnear);
     else
       k_p2p32_m1<false><<<grid, P2P_BLOCK, 0, s>>>(
-            g.n, g.leaf_start.p, g.items.p, g.p2p_src.p, g.hi32.p, g.lo32.p, src, damping, Fnear);
+            g.n, g.leaf_start.p, g.items.p, g.item_split.p, g.p2p_src.p, g.hi32.p, g.lo32.p, src, damping, Fnear);
     CG_LAUNCH();
     return;
   }
@@ -1534,11 +1617,11 @@ static void launch_p2p_dd(const Geometry& g, bool damp, const double* src, doubl
   CG_LAUNCH();
   const int grid = (int)g.h_items.size();
   if (damp)
-    k_p2p_dd<true><<<grid, P2P_BLOCK, 0, s>>>(g.n, g.leaf_start.p, g.items.p, g.p2p_src.p,
+    k_p2p_dd<true><<<grid, P2P_BLOCK, 0, s>>>(g.n, g.leaf_start.p, g.items.p, g.item_split.p, g.p2p_src.p,
                                               pos_args<float>(g), w.dd_src.p, g.dd_exp.p,
                                               damping, w.Fnear.p);
   else
-    k_p2p_dd<false><<<grid, P2P_BLOCK, 0, s>>>(g.n, g.leaf_start.p, g.items.p, g.p2p_src.p,
+    k_p2p_dd<false><<<grid, P2P_BLOCK, 0, s>>>(g.n, g.leaf_start.p, g.items.p, g.item_split.p, g.p2p_src.p,
                                                pos_args<float>(g), w.dd_src.p, g.dd_exp.p,
                                                damping, w.Fnear.p);
   CG_LAUNCH();

@@ -89,12 +89,15 @@ struct Geometry {
 
   // Near-field work items (target leaf, first and last+1 position in its
   // P2P list, output slot), largest first; a leaf's items write slots
-  // 0..leaf_nslot-1 of the near-field buffer.
+  // 0..leaf_nslot-1 of the near-field buffer.  A leaf's P2P list holds the
+  // source leaves that may need Thole damping first and those that do not
+  // (every pair with v >= 27) from h_leaf_split[leaf] on; item_split is
+  // that position clamped to each item's range.
   int nslot = 1;
   std::vector<int4> h_items;
-  std::vector<int> h_leaf_nslot;
+  std::vector<int> h_leaf_nslot, h_leaf_split, h_item_split;
   DBuf<int4> items;
-  DBuf<int> leaf_nslot;
+  DBuf<int> leaf_nslot, item_split;
 
   // Upward pass without level-by-level M2M: leaf multipoles (P2M), then the
   // multipole of every non-leaf cell that is an M2L source from M2M shifts of
@@ -116,6 +119,9 @@ struct Geometry {
   DBuf<int4> p2m_tasks;
   DBuf<int> task_leaf, cell_task_ptr, lanc_ptr, lanc_cell, cell_ref;
   DBuf<float4> cell_off;
+  // Thole damping factor of the operator (0: undamped), for the damping
+  // split of the P2P lists
+  double damping = 0.0;
   // tunable schedule parameters (0: the built-in choice)
   long item_pairs = 0;  // target pairs per near-field work item
   int m2l_chunk   = 0;  // sources per M2L warp

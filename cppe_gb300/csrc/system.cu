@@ -253,6 +253,7 @@ void System::init(int n_, const double* xyz, const double* alpha6, const int* ex
     const double iso = (a[0] + a[3] + a[5]) / 3.0;
     if (o.damp && iso > 0.0) sd[i] = std::pow(iso, -1.0 / 6.0);
   }
+  geo.damping = o.damp ? o.damping_factor : 0.0;
   geo.build(n, xyz, sd.data(), excl_ptr, excl_idx, fmm, o.tree_ncrit, o.theta, stream);
   if (fmm) {
     ops = std::make_unique<DeviceOps>();
