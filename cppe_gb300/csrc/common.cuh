@@ -194,6 +194,45 @@ __device__ __forceinline__ void block_sum(double (&v)[K], double* sh /* >= 32*K 
   __syncthreads();
 }
 
+// The same block sum from FP32 per-thread values (GB300's FP64 pipe runs at
+// about 1/75 of its FP32 rate, so the per-thread products and the warp
+// reduction stay in FP32): a compensated warp reduction (two-sum, the error
+// terms carried along), then the warps' sums in FP64 in thread 0.
+template <int K>
+__device__ __forceinline__ void block_sum(const float (&vf)[K], double (&v)[K],
+                                          double* sh /* >= 32*K */) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    float x = vf[k], e = 0.f;
+    for (int o = 16; o > 0; o >>= 1) {
+      const float xo = __shfl_down_sync(0xffffffffu, x, o);
+      const float eo = __shfl_down_sync(0xffffffffu, e, o);
+      float t, te;
+      two_sum(x, xo, t, te);
+      x = t;
+      e += eo + te;
+    }
+    if (lane == 0) sh[wid * K + k] = (double)x + (double)e;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      double s = 0.0;
+      for (int w = 0; w < nw; ++w) s += sh[w * K + k];
+      v[k] = s;
+    }
+  }
+  __syncthreads();
+}
+
+// Last-block part of grid_sum_last, after the block sum is in thread 0.
+template <int K>
+__device__ __forceinline__ bool grid_finish_last(double (&v)[K], double* sh, double* partials,
+                                                 unsigned* ticket, double* out);
+
 // Returns true in thread 0 of the last block; partials[b*K + k] hold the
 // per-block sums, and `out` receives the totals.  The last block adds the
 // partials with all its threads (thread t takes blocks t, t + blockDim, ...,
@@ -203,6 +242,20 @@ template <int K>
 __device__ __forceinline__ bool grid_sum_last(double (&v)[K], double* sh, double* partials,
                                               unsigned* ticket, double* out) {
   block_sum<K>(v, sh);
+  return grid_finish_last<K>(v, sh, partials, ticket, out);
+}
+// FP32 per-thread values (see block_sum above).
+template <int K>
+__device__ __forceinline__ bool grid_sum_last(const float (&vf)[K], double* sh, double* partials,
+                                              unsigned* ticket, double* out) {
+  double v[K];
+  block_sum<K>(vf, v, sh);
+  return grid_finish_last<K>(v, sh, partials, ticket, out);
+}
+
+template <int K>
+__device__ __forceinline__ bool grid_finish_last(double (&v)[K], double* sh, double* partials,
+                                                 unsigned* ticket, double* out) {
   __shared__ bool last;
   if (threadIdx.x == 0) {
 #pragma unroll

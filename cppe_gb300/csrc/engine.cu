@@ -1451,7 +1451,7 @@ __global__ void __launch_bounds__(FINISH_BLOCK) k_finish(int n, const int* __res
   constexpr int NS = ncomp(M);
   __shared__ double sh[32];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  double dv[1] = {0.0};
+  T dv[1]     = {T(0)};  // (FP32 products for the FP32 apply: see block_sum)
   if (i < n) {
     T f[3] = {0, 0, 0};
     const int nsl = leaf_nslot[tv.site_leaf[i]];
@@ -1503,7 +1503,7 @@ __global__ void __launch_bounds__(FINISH_BLOCK) k_finish(int n, const int* __res
       out[3 * (size_t)i]     = o0;
       out[3 * (size_t)i + 1] = o1;
       out[3 * (size_t)i + 2] = o2;
-      dv[0] = (double)sv[0] * o0 + (double)sv[1] * o1 + (double)sv[2] * o2;
+      dv[0] = sv[0] * o0 + sv[1] * o1 + sv[2] * o2;
     } else {
       out64[3 * (size_t)i] += sign * (double)f[0];
       out64[3 * (size_t)i + 1] += sign * (double)f[1];

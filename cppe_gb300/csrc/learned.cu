@@ -2,6 +2,8 @@
 #include <algorithm>
 #include <cmath>
 
+#include <cub/device/device_segmented_sort.cuh>
+
 #include "learned.h"
 #include "system.h"
 
@@ -69,6 +71,33 @@ __global__ void k_near_build(int n, CellGridView cgv, const float4* __restrict__
   if (!FILL) count[i] = k;
 }
 
+__global__ void k_iota(long n, int* __restrict__ v) {
+  const long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) v[k] = (int)k;
+}
+
+// Entry k of the sorted lists from entry perm[k] of the scan order; the
+// packed operator entries alongside.
+__global__ void k_near_permute(long nnz, const int* __restrict__ perm, const int* __restrict__ idx,
+                               const __half* __restrict__ t6_in, const float4* __restrict__ d_in,
+                               __half* __restrict__ t6, float4* __restrict__ d,
+                               int4* __restrict__ ent) {
+  const long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nnz) return;
+  const long q = perm[k];
+  const __half2* h = reinterpret_cast<const __half2*>(t6_in + 6 * q);
+  __half2* o       = reinterpret_cast<__half2*>(t6 + 6 * k);
+  const __half2 a = h[0], b = h[1], c = h[2];
+  o[0] = a, o[1] = b, o[2] = c;
+  d[k] = d_in[q];
+  int4 e;
+  e.x    = idx[k];
+  e.y    = *reinterpret_cast<const int*>(&a);
+  e.z    = *reinterpret_cast<const int*>(&b);
+  e.w    = *reinterpret_cast<const int*>(&c);
+  ent[k] = e;
+}
+
 void NearList::build(const Geometry& g, const int* cep, const int* cei, int damp,
                      double damping, cudaStream_t s) {
   n = g.n;
@@ -132,15 +161,43 @@ void NearList::build(const Geometry& g, const int* cep, const int* cei, int damp
   idx.alloc(std::max(1L, nnz));
   t6.alloc(6 * std::max(1L, nnz));
   d.alloc(std::max(1L, nnz));
+  DBuf<int> idx0, perm0, perm;
+  DBuf<__half> t60;
+  DBuf<float4> d0;
+  idx0.alloc(std::max(1L, nnz));
+  t60.alloc(6 * std::max(1L, nnz));
+  d0.alloc(std::max(1L, nnz));
+  ent.alloc(std::max(1L, nnz));
   if (n > 0) {
     k_near_build<true><<<nb, 128, 0, s>>>(n, cv, g.hi32.p, g.lo32.p, rc2, damp, (float)damping,
-                                          nullptr, ptr.p, idx.p, t6.p, d.p);
+                                          nullptr, ptr.p, idx0.p, t60.p, d0.p);
     CG_LAUNCH();
   }
-  CG_CUDA(cudaStreamSynchronize(s));  // the temporaries above are freed on return
+  if (nnz > 0) {
+    // every site's entries in ascending partner order, so that the eight
+    // lanes serving a site gather neighbouring partners (shared cache lines)
+    perm0.alloc(nnz);
+    perm.alloc(nnz);
+    k_iota<<<(unsigned)((nnz + 255) / 256), 256, 0, s>>>(nnz, perm0.p);
+    CG_LAUNCH();
+    size_t tmp_bytes = 0;
+    CG_CUDA(cub::DeviceSegmentedSort::SortPairs(nullptr, tmp_bytes, idx0.p, idx.p, perm0.p, perm.p,
+                                                nnz, n, ptr.p, ptr.p + 1, s));
+    DBuf<unsigned char> tmp;
+    tmp.alloc(std::max<size_t>(1, tmp_bytes));
+    CG_CUDA(cub::DeviceSegmentedSort::SortPairs(tmp.p, tmp_bytes, idx0.p, idx.p, perm0.p, perm.p,
+                                                nnz, n, ptr.p, ptr.p + 1, s));
+    k_near_permute<<<(unsigned)((nnz + 255) / 256), 256, 0, s>>>(nnz, perm.p, idx.p, t60.p, d0.p,
+                                                                 t6.p, d.p, ent.p);
+    CG_LAUNCH();
+    CG_CUDA(cudaStreamSynchronize(s));  // the temporaries above are freed on return
+  }
+  CG_CUDA(cudaStreamSynchronize(s));
 }
 
-NearListView view(const NearList& g) { return NearListView{g.n, g.ptr.p, g.idx.p, g.t6.p, g.d.p}; }
+NearListView view(const NearList& g) {
+  return NearListView{g.n, g.ptr.p, g.idx.p, g.t6.p, g.d.p, g.ent.p};
+}
 
 __device__ __forceinline__ float aiso6(const float* a) { return (a[0] + a[3] + a[5]) / 3.f; }
 
@@ -206,10 +263,41 @@ __global__ void k_features(NearListView nl, const float* __restrict__ a6,
     if (k < 49 || k > 54) o[k] = f[k];
 }
 
-__device__ __forceinline__ void load_t6(const __half* t6, long k, float (&t)[6]) {
-  const __half2* h = reinterpret_cast<const __half2*>(t6 + 6 * k);  // 4-byte aligned
-  const float2 a = __half22float2(h[0]), b = __half22float2(h[1]), c = __half22float2(h[2]);
-  t[0] = a.x, t[1] = a.y, t[2] = b.x, t[3] = b.y, t[4] = c.x, t[5] = c.y;
+// Lane `sub` of eight: its share of sum_j T_ij in_j over site i's entries,
+// four entries per step with their loads issued together (the loop is
+// bound by the latency of the entry load and the dependent gather).
+template <typename T>
+__device__ __forceinline__ void near_T_lane(const NearListView& nl, int i, int sub,
+                                            const T* __restrict__ in, T& wx, T& wy, T& wz,
+                                            const float4* __restrict__ in4 = nullptr) {
+  const int k0 = nl.ptr[i] + sub, k1 = nl.ptr[i + 1];
+  for (int k = k0; k < k1; k += 32) {
+    int4 e[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) e[u] = k + 8 * u < k1 ? nl.ent[k + 8 * u] : make_int4(-1, 0, 0, 0);
+    T v[4][3];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int j = e[u].x;
+      if (in4) {
+        const float4 q = j >= 0 ? in4[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        v[u][0] = (T)q.x, v[u][1] = (T)q.y, v[u][2] = (T)q.z;
+      } else {
+        v[u][0] = j >= 0 ? in[3 * (size_t)j] : T(0);
+        v[u][1] = j >= 0 ? in[3 * (size_t)j + 1] : T(0);
+        v[u][2] = j >= 0 ? in[3 * (size_t)j + 2] : T(0);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&e[u].y));
+      const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&e[u].z));
+      const float2 c = __half22float2(*reinterpret_cast<const __half2*>(&e[u].w));
+      wx += (T)a.x * v[u][0] + (T)a.y * v[u][1] + (T)b.x * v[u][2];
+      wy += (T)a.y * v[u][0] + (T)b.y * v[u][1] + (T)c.x * v[u][2];
+      wz += (T)b.x * v[u][0] + (T)c.x * v[u][1] + (T)c.y * v[u][2];
+    }
+  }
 }
 
 // out_i = alpha_i sum_j T_ij in_j: eight lanes per site stride over its list
@@ -221,15 +309,7 @@ __global__ void k_near_T(NearListView nl, const T* __restrict__ a6, const T* __r
   const int i = gid >> 3, sub = gid & 7;
   T fx = 0, fy = 0, fz = 0;
   if (i < nl.n) {
-    for (int k = nl.ptr[i] + sub; k < nl.ptr[i + 1]; k += 8) {
-      const int j = nl.idx[k];
-      float t[6];
-      load_t6(nl.t6, k, t);
-      const T vx = in[3 * (size_t)j], vy = in[3 * (size_t)j + 1], vz = in[3 * (size_t)j + 2];
-      fx += (T)t[0] * vx + (T)t[1] * vy + (T)t[2] * vz;
-      fy += (T)t[1] * vx + (T)t[3] * vy + (T)t[4] * vz;
-      fz += (T)t[2] * vx + (T)t[4] * vy + (T)t[5] * vz;
-    }
+    near_T_lane<T>(nl, i, sub, in, fx, fy, fz);
   }
 #pragma unroll
   for (int o = 4; o > 0; o >>= 1) {
@@ -286,22 +366,14 @@ __global__ void k_precond_near(NearListView nl, const T* __restrict__ a6,
                                const float* __restrict__ cw, const T* __restrict__ a,
                                const T* __restrict__ r, const T* __restrict__ r_old,
                                T* __restrict__ zc, T* __restrict__ p, int start, ReduceSlots rs,
-                               double* scal, const int* flags) {
+                               double* scal, const int* flags, const float4* __restrict__ a4) {
   __shared__ double sh[64];
   if (!start && flags[0]) return;
   const int gid = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = gid >> 3, sub = gid & 7;
   T wx = 0, wy = 0, wz = 0;
   if (i < nl.n) {
-    for (int k = nl.ptr[i] + sub; k < nl.ptr[i + 1]; k += 8) {
-      const int j = nl.idx[k];
-      float t[6];
-      load_t6(nl.t6, k, t);
-      const T vx = a[3 * (size_t)j], vy = a[3 * (size_t)j + 1], vz = a[3 * (size_t)j + 2];
-      wx += (T)t[0] * vx + (T)t[1] * vy + (T)t[2] * vz;
-      wy += (T)t[1] * vx + (T)t[3] * vy + (T)t[4] * vz;
-      wz += (T)t[2] * vx + (T)t[4] * vy + (T)t[5] * vz;
-    }
+    near_T_lane<T>(nl, i, sub, a, wx, wy, wz, a4);
   }
 #pragma unroll
   for (int o = 4; o > 0; o >>= 1) {
@@ -309,7 +381,7 @@ __global__ void k_precond_near(NearListView nl, const T* __restrict__ a6,
     wy += __shfl_down_sync(0xffffffffu, wy, o, 8);
     wz += __shfl_down_sync(0xffffffffu, wz, o, 8);
   }
-  double v[2] = {0.0, 0.0};
+  T v[2] = {T(0), T(0)};  // (FP32 products for the FP32 solve: see block_sum)
   if (i < nl.n && sub == 0) {
     const T* al = a6 + 6 * (size_t)i;
     const T c   = (T)cw[i];
@@ -321,8 +393,8 @@ __global__ void k_precond_near(NearListView nl, const T* __restrict__ a6,
       const T zk     = a[k] + c * w[q];
       zc[k]          = zk;
       if (start) p[k] = zk;
-      v[0] += (double)zk * r[k];
-      if (!start) v[1] += (double)zk * r_old[k];
+      v[0] += zk * r[k];
+      if (!start) v[1] += zk * r_old[k];
     }
   }
   if (grid_sum_last<2>(v, sh, rs.partials, rs.ticket, rs.out)) {
@@ -364,18 +436,19 @@ void learned_guess(int n, const float* Y, const float* v1, const float* v2, cons
 template <typename T>
 void precond_near(const NearListView& nl, const T* a6, const float* c, const T* a, const T* r,
                   const T* r_old, T* zc, T* p, bool start, double* partials, unsigned* ticket,
-                  double* scal, const int* flags, cudaStream_t s) {
+                  double* scal, const int* flags, cudaStream_t s, const float4* a4) {
   ReduceSlots rs{partials, ticket, scal + S_RED};
   const long threads = 8L * nl.n;
   k_precond_near<T><<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
-        nl, a6, c, a, r, r_old, zc, p, start ? 1 : 0, rs, scal, flags);
+        nl, a6, c, a, r, r_old, zc, p, start ? 1 : 0, rs, scal, flags, a4);
   CG_LAUNCH();
 }
 template void precond_near<float>(const NearListView&, const float*, const float*, const float*,
                                   const float*, const float*, float*, float*, bool, double*,
-                                  unsigned*, double*, const int*, cudaStream_t);
+                                  unsigned*, double*, const int*, cudaStream_t, const float4*);
 template void precond_near<double>(const NearListView&, const double*, const float*,
                                    const double*, const double*, const double*, double*, double*,
-                                   bool, double*, unsigned*, double*, const int*, cudaStream_t);
+                                   bool, double*, unsigned*, double*, const int*, cudaStream_t,
+                                   const float4*);
 
 }  // namespace cg

@@ -37,6 +37,9 @@ struct NearList {
   DBuf<int> ptr, idx;
   DBuf<__half> t6;
   DBuf<float4> d;
+  // the operator's entries packed for one 16-byte load each:
+  // {j, half2(t0, t1), half2(t2, t3), half2(t4, t5)}
+  DBuf<int4> ent;
   // exclusions in caller indices (CSR, may be null)
   void build(const Geometry& g, const int* caller_excl_ptr, const int* caller_excl_idx,
              int damp, double damping, cudaStream_t s);
@@ -48,6 +51,7 @@ struct NearListView {
   const int* idx;
   const __half* t6;
   const float4* d;
+  const int4* ent;
 };
 
 NearListView view(const NearList& g);
@@ -65,9 +69,11 @@ void learned_guess(int n, const float* Y, const float* v1, const float* v2, cons
 // Corrected preconditioner in one pass: zc = a + c alpha T_near a for a = alpha r
 // (the plain preconditioned residual); at a start p = zc; rz = zc.r and, after
 // a start, beta = (zc.r - zc.r_old) / rz_old (Polak-Ribiere).
+// a4 (may be null): a as one float4 per site, read by the gathers instead.
 template <typename T>
 void precond_near(const NearListView& nl, const T* a6, const float* c, const T* a, const T* r,
                   const T* r_old, T* zc, T* p, bool start, double* partials, unsigned* ticket,
-                  double* scal, const int* flags, cudaStream_t s);
+                  double* scal, const int* flags, cudaStream_t s,
+                  const float4* a4 = nullptr);
 
 }  // namespace cg

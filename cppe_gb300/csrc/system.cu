@@ -26,13 +26,16 @@ __device__ __forceinline__ void sym3(const A* a, const B* v, B* o) {
 }
 
 // r = F - Ax (Ax may be null: zero start), z = alpha r, p = z; rz, rr.
+// z4 (may be null): z again as one float4 per site, for the gathers of the
+// learned preconditioner.
 template <typename T>
 __global__ void k_cg_start(int n, const double* __restrict__ F, const T* __restrict__ Ax,
                            const T* __restrict__ a6, T* __restrict__ r, T* __restrict__ z,
-                           T* __restrict__ p, ReduceSlots rs, double* scal, int* flags) {
+                           T* __restrict__ p, ReduceSlots rs, double* scal, int* flags,
+                           float4* __restrict__ z4 = nullptr) {
   __shared__ double sh[64];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  double v[2] = {0.0, 0.0};
+  T v[2] = {T(0), T(0)};  // (FP32 products for the FP32 solve: see block_sum)
   if (i < n) {
     T rv[3], zv[3];
 #pragma unroll
@@ -41,9 +44,10 @@ __global__ void k_cg_start(int n, const double* __restrict__ F, const T* __restr
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       r[3 * i + c] = rv[c], z[3 * i + c] = zv[c], p[3 * i + c] = zv[c];
-      v[0] += (double)rv[c] * zv[c];
-      v[1] += (double)rv[c] * rv[c];
+      v[0] += rv[c] * zv[c];
+      v[1] += rv[c] * rv[c];
     }
+    if (z4) z4[i] = make_float4((float)zv[0], (float)zv[1], (float)zv[2], 0.f);
   }
   if (grid_sum_last<2>(v, sh, rs.partials, rs.ticket, rs.out)) {
     scal[S_RZ]    = rs.out[0];
@@ -61,13 +65,14 @@ template <typename T>
 __global__ void k_cg_update(int n, const T* __restrict__ p, const T* __restrict__ Ap,
                             const T* __restrict__ a6, T* __restrict__ x, T* __restrict__ r,
                             T* __restrict__ z, ReduceSlots rs, double* scal, int* flags,
-                            double* hist, double thresh, int maxiter, T* __restrict__ r_old) {
+                            double* hist, double thresh, int maxiter, T* __restrict__ r_old,
+                            float4* __restrict__ z4 = nullptr) {
   __shared__ double sh[64];
   if (flags[0]) return;
   const double a = scal[S_RZ] / scal[S_PAP];
   const T aT     = (T)a;
   const int i    = blockIdx.x * blockDim.x + threadIdx.x;
-  double v[2]    = {0.0, 0.0};
+  T v[2]         = {T(0), T(0)};
   if (i < n) {
     T rv[3], zv[3];
 #pragma unroll
@@ -82,9 +87,10 @@ __global__ void k_cg_update(int n, const T* __restrict__ p, const T* __restrict_
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       z[3 * (size_t)i + c] = zv[c];
-      v[0] += (double)rv[c] * rv[c];
-      v[1] += (double)rv[c] * zv[c];
+      v[0] += rv[c] * rv[c];
+      v[1] += rv[c] * zv[c];
     }
+    if (z4) z4[i] = make_float4((float)zv[0], (float)zv[1], (float)zv[2], 0.f);
   }
   if (grid_sum_last<2>(v, sh, rs.partials, rs.ticket, rs.out)) {
     const double rn = sqrt(rs.out[0]);
@@ -498,7 +504,8 @@ void System::inner_iteration_fp32(int nb, int nb3) {
   k_cg_update<float><<<nb, VB, 0, stream>>>(n, p32.p, Ap32.p, alpha32.p, d32.p, r32.p, z32.p,
                                             slots(S_RED), scal.p, flags.p, nullptr, -1.0,
                                             std::max(1, opt.maxiter),
-                                            use_model ? lf_rold32.p : nullptr);
+                                            use_model ? lf_rold32.p : nullptr,
+                                            use_model ? lf_z4.p : nullptr);
   CG_LAUNCH();
   const float* zd = use_model ? learned_precond<float>(z32.p, r32.p, p32.p, false) : z32.p;
   k_cg_dir<float><<<nb3, VB, 0, stream>>>(3 * n, zd, p32.p, scal.p, flags.p);
@@ -600,7 +607,8 @@ int System::solve_mixed(bool zero_guess, double* hist_out, int hist_cap, int* it
     apply32(p32.p, Ap32.p, false);
     last.fp32_applies++;
     k_cg_start<float><<<nb, VB, 0, stream>>>(n, F.p, Ap32.p, alpha32.p, r32.p, z32.p, p32.p,
-                                             slots(S_RED), scal.p, flags.p);
+                                             slots(S_RED), scal.p, flags.p,
+                                             use_model ? lf_z4.p : nullptr);
     CG_LAUNCH();
     if (use_model) learned_precond<float>(z32.p, r32.p, p32.p, true);
   }
@@ -622,7 +630,8 @@ int System::solve_mixed(bool zero_guess, double* hist_out, int hist_cap, int* it
       }
       // inner right-hand side: the FP64 residual
       k_cg_start<float><<<nb, VB, 0, stream>>>(n, r.p, nullptr, alpha32.p, r32.p, z32.p,
-                                               p32.p, slots(S_RED), scal.p, flags.p);
+                                               p32.p, slots(S_RED), scal.p, flags.p,
+                                               use_model ? lf_z4.p : nullptr);
       CG_LAUNCH();
       if (use_model) learned_precond<float>(z32.p, r32.p, p32.p, true);
     } else {
@@ -763,6 +772,7 @@ void System::learned_setup() {
   lf_c.alloc(n);
   lf_w64.alloc(n3);
   lf_rold64.alloc(n3);
+  lf_z4.alloc(n);
 }
 
 void System::learned_features_for_F() {
@@ -791,7 +801,7 @@ T* System::learned_precond(T* zv, const T* rv, T* pv, bool start) {
     return lf_w64.p;
   } else {
     precond_near<float>(nl, alpha32.p, lf_c.p, zv, rv, lf_rold32.p, lf_w32.p, pv, start,
-                        partials.p, ticket.p, scal.p, flags.p, stream);
+                        partials.p, ticket.p, scal.p, flags.p, stream, lf_z4.p);
     return lf_w32.p;
   }
 }

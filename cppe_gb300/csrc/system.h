@@ -58,6 +58,7 @@ struct System {
   std::unique_ptr<NearList> near;
   DBuf<float> lf_feats, lf_v1, lf_v2, lf_v3, lf_Y, lf_c, lf_w32, lf_rold32;
   DBuf<double> lf_w64, lf_rold64;
+  DBuf<float4> lf_z4;  // z of the FP32 inner solve as float4 per site (gathers)
   void learned_setup();
   // descriptors and basis vectors for the current F (device order)
   void learned_features_for_F();
