@@ -510,16 +510,20 @@ int BatchSystem::solve_device(const double* d_rhs, double* d_mu, int* iters_out)
                             stream));
     CG_CUDA(cudaStreamSynchronize(stream));
     bool exact = false;
+    // bound of the residual norms' error where they were not recomputed with
+    // the FP64 operator (as in System::solve_mixed, over the largest norm)
+    constexpr double REC_ERR = 3e-6, CORR_ERR = 3e-7;
+    double rerr = 0.0;
     for (int outer = 0; outer < 12; ++outer) {
       // inner tolerances; segments already below the threshold stay put
       for (int g = 0; g < nseg; ++g) tolv[g] = std::max(eta * rn[g], 0.5 * t);
       if (outer > 0) {
-        if (std::all_of(rn.begin(), rn.end(), [&](double v) { return v < t; })) {
+        if (std::all_of(rn.begin(), rn.end(), [&](double v) { return v + rerr < t; })) {
           status = CPPE_GPU_OK;
           break;
         }
         for (int g = 0; g < nseg; ++g)
-          if (rn[g] < t) tolv[g] = 1e300;  // done at once
+          if (rn[g] + rerr < t) tolv[g] = 1e300;  // done at once
         k_bcg_start<float><<<nb, BB, 0, stream>>>(n, r.p, nullptr, alpha32.p, r32.p, z32.p,
                                                   p32.p, site_a.p, site_b.p);
         CG_LAUNCH();
@@ -535,13 +539,14 @@ int BatchSystem::solve_device(const double* d_rhs, double* d_mu, int* iters_out)
       CG_CUDA(cudaMemcpyAsync(it_h.data(), iters.p, nseg * sizeof(int), cudaMemcpyDeviceToHost,
                               stream));
       const double rmax = *std::max_element(rn.begin(), rn.end());
-      if (exact && rmax * 1e-6 < 1e-3 * t) {
+      if (exact && rerr + REC_ERR * rmax < 0.1 * t) {
         // residual from the inner recursion (as System::solve_mixed)
         k_bres<<<nb, BB, 0, stream>>>(n, nullptr, nullptr, nullptr, r.p, site_b.p, r32.p);
         CG_LAUNCH();
         k_bacc<<<nb3, BB, 0, stream>>>(n3, x.p, d32.p);
         CG_LAUNCH();
-      } else if (!(exact && rmax * 1e-4 < t)) {
+        rerr += REC_ERR * rmax;
+      } else if (!(exact && rerr + CORR_ERR * rmax < 0.1 * t)) {
         k_bacc<<<nb3, BB, 0, stream>>>(n3, x.p, d32.p);
         CG_LAUNCH();
         apply_seg<double>(x.p, Ap.p, NEAR_DD);
@@ -549,6 +554,7 @@ int BatchSystem::solve_device(const double* d_rhs, double* d_mu, int* iters_out)
         k_bres<<<nb, BB, 0, stream>>>(n, F.p, Ap.p, nullptr, r.p, site_b.p);
         CG_LAUNCH();
         exact = true;
+        rerr  = 0.0;
       } else {
         apply_seg<float>(d32.p, Ap32.p);
         stats.fp32_applies++;
@@ -556,6 +562,7 @@ int BatchSystem::solve_device(const double* d_rhs, double* d_mu, int* iters_out)
         CG_LAUNCH();
         k_bacc<<<nb3, BB, 0, stream>>>(n3, x.p, d32.p);
         CG_LAUNCH();
+        rerr += CORR_ERR * rmax;
       }
       seg_norms_from_site_b();
       CG_CUDA(cudaMemcpyAsync(rn.data(), seg_rnorm.p, nseg * sizeof(double),
@@ -563,7 +570,8 @@ int BatchSystem::solve_device(const double* d_rhs, double* d_mu, int* iters_out)
       CG_CUDA(cudaStreamSynchronize(stream));
       for (int g = 0; g < nseg; ++g) total[g] += it_h[g];
     }
-    if (status != CPPE_GPU_OK && std::all_of(rn.begin(), rn.end(), [&](double v) { return v < t; }))
+    if (status != CPPE_GPU_OK &&
+        std::all_of(rn.begin(), rn.end(), [&](double v) { return v + rerr < t; }))
       status = CPPE_GPU_OK;
     last_rnorm = rn;
   }

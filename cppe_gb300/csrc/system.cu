@@ -32,7 +32,7 @@ template <typename T>
 __global__ void k_cg_start(int n, const double* __restrict__ F, const T* __restrict__ Ax,
                            const T* __restrict__ a6, T* __restrict__ r, T* __restrict__ z,
                            T* __restrict__ p, ReduceSlots rs, double* scal, int* flags,
-                           float4* __restrict__ z4 = nullptr) {
+                           float4* __restrict__ z4 = nullptr, const int* skip = nullptr) {
   __shared__ double sh[64];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   T v[2] = {T(0), T(0)};  // (FP32 products for the FP32 solve: see block_sum)
@@ -53,7 +53,7 @@ __global__ void k_cg_start(int n, const double* __restrict__ F, const T* __restr
     scal[S_RZ]    = rs.out[0];
     scal[S_RR]    = rs.out[1];
     scal[S_RNORM] = sqrt(rs.out[1]);
-    flags[0]      = 0;
+    flags[0]      = skip ? *skip : 0;
     flags[1]      = 0;
   }
 }
@@ -492,6 +492,19 @@ int System::solve_fp64(bool zero_guess, double* hist_out, int hist_cap, int* ite
   return h_flags[0] == 1 ? CPPE_GPU_OK : CPPE_GPU_NOT_CONVERGED;
 }
 
+// Set-up of an inner FP32 solve on the device (no host round trip): its
+// threshold max(eta ||r||, 0.5 t) from the residual norm in scal[S_RNORM],
+// which is also kept (S_RSTAGE); the iterations of the previous inner solve
+// are added to flags[3] (stage 0 clears it); flags[2] = 1 when the residual
+// already meets t, which makes the following k_cg_start start a finished solve.
+__global__ void k_inner_stage(double* scal, int* flags, double t, double eta, int stage) {
+  const double rn = scal[S_RNORM];
+  scal[S_TOL]     = fmax(eta * rn, 0.5 * t);
+  scal[S_RSTAGE]  = rn;
+  flags[3]        = stage == 0 ? 0 : flags[3] + flags[1];
+  flags[2]        = stage > 0 && rn < t ? 1 : 0;
+}
+
 // Continues the inner graph's while loop until the solve has stopped.
 __global__ void k_while_running(cudaGraphConditionalHandle h, const int* flags) {
   cudaGraphSetConditional(h, flags[0] == 0 ? 1u : 0u);
@@ -518,7 +531,7 @@ void System::inner_iteration_fp32(int nb, int nb3) {
 // flags[0] (converged, or the iteration limit).  Built once per system and
 // learned/plain variant, after the buffers it uses exist.  Where graph
 // construction is refused, the iterations are launched from the host.
-void System::run_inner_fp32(int nb, int nb3) {
+bool System::inner_graph_ready(int nb, int nb3) {
   const int v = use_model ? 1 : 0;
   // CPPE_GPU_GRAPHS=0 launches the iterations from the host instead (same
   // kernels; for profilers that do not descend into conditional graph nodes)
@@ -570,7 +583,12 @@ void System::run_inner_fp32(int nb, int nb3) {
       inner_graph_failed = true;
     }
   }
-  if (inner_exec[v]) {
+  return inner_exec[v] != nullptr;
+}
+
+void System::run_inner_fp32(int nb, int nb3) {
+  const int v = use_model ? 1 : 0;
+  if (inner_graph_ready(nb, nb3)) {
     CG_CUDA(cudaGraphLaunch(inner_exec[v], stream));
     CG_CUDA(cudaMemcpyAsync(h_flags, flags.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream));
     CG_CUDA(cudaStreamSynchronize(stream));
@@ -615,7 +633,70 @@ int System::solve_mixed(bool zero_guess, double* hist_out, int hist_cap, int* it
   bool have_inner_start   = !zero_guess;
   bool have_fp64_residual = zero_guess;  // r = F is exact for a zero start
   int status              = CPPE_GPU_NOT_CONVERGED;
-  for (int outer = 0; outer < max_outer; ++outer) {
+  // Bound of |computed - true| of the FP64 residual's norm where it was not
+  // recomputed with the FP64 operator: after an inner solve started from a
+  // residual of norm rs, forming the new residual from the FP32 recursion
+  // errs by < REC_ERR rs (the recursion's rounding, ~1e-7 per update and
+  // FP32 operator error ~1e-7 of ||B d|| ~ rs, times a condition-number
+  // margin), an FP32 apply of the correction by < CORR_ERR rs.  A residual is
+  // accepted when its norm plus the bound is below t; the cheaper forms are
+  // used where their bound stays below t / 10.
+  constexpr double REC_ERR = 3e-6, CORR_ERR = 3e-7;
+  double rerr = 0.0;
+  // The usual course -- FP32 solve, FP64 residual, FP32 solve, residual from
+  // the recursion -- queued at once with the decisions on the device and one
+  // host synchronisation; the loop below takes over where it does not end
+  // the solve (or where the inner iterations cannot run as a graph).
+  if (!zero_guess && inner_graph_ready(nb, nb3)) {
+    const int v = use_model ? 1 : 0;
+    k_inner_stage<<<1, 1, 0, stream>>>(scal.p, flags.p, t, eta, 0);
+    CG_LAUNCH();
+    CG_CUDA(cudaGraphLaunch(inner_exec[v], stream));
+    k_accumulate<<<nb3, VB, 0, stream>>>(n3, x.p, d32.p);
+    CG_LAUNCH();
+    apply64(x.p, Ap.p, false, NEAR_DD);
+    k_residual<<<nb3, VB, 0, stream>>>(n3, F.p, Ap.p, r.p, slots(S_RED), scal.p);
+    CG_LAUNCH();
+    k_inner_stage<<<1, 1, 0, stream>>>(scal.p, flags.p, t, eta, 1);
+    CG_LAUNCH();
+    k_cg_start<float><<<nb, VB, 0, stream>>>(n, r.p, nullptr, alpha32.p, r32.p, z32.p, p32.p,
+                                             slots(S_RED), scal.p, flags.p,
+                                             use_model ? lf_z4.p : nullptr, flags.p + 2);
+    CG_LAUNCH();
+    if (use_model) learned_precond<float>(z32.p, r32.p, p32.p, true);
+    CG_CUDA(cudaGraphLaunch(inner_exec[v], stream));
+    k_residual_inner<<<nb3, VB, 0, stream>>>(n3, r32.p, r.p, slots(S_RED), scal.p);
+    CG_LAUNCH();
+    k_accumulate<<<nb3, VB, 0, stream>>>(n3, x.p, d32.p);
+    CG_LAUNCH();
+    CG_CUDA(cudaMemcpyAsync(h_flags, flags.p, 4 * sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CG_CUDA(cudaMemcpyAsync(h_scal, scal.p, S_NSCAL * sizeof(double), cudaMemcpyDeviceToHost,
+                            stream));
+    CG_CUDA(cudaStreamSynchronize(stream));
+    const int it1 = h_flags[3], it2 = h_flags[1];
+    total_inner += it1 + it2;
+    last.fp32_applies += it1 + it2;
+    last.fp64_applies++;
+    launch_counter() += inner_body_launches[v] * (std::max(1, it1) + std::max(1, it2));
+    const double r1 = h_scal[S_RSTAGE];  // FP64 residual after the first inner solve
+    outer_hist.push_back(r1);
+    have_fp64_residual = true;
+    have_inner_start   = false;
+    // the residual from the recursion stands where its error is below 1e-3 t
+    const bool recursion_ok = r1 < t || REC_ERR * r1 < 0.1 * t;
+    if (recursion_ok && r1 >= t) rerr = REC_ERR * r1;
+    if (recursion_ok && h_scal[S_RNORM] + rerr < t) {
+      if (r1 >= t) outer_hist.push_back(h_scal[S_RNORM]);
+      status = CPPE_GPU_OK;
+    } else if (!recursion_ok) {
+      // recompute the residual of the accumulated x with the FP64 operator
+      apply64(x.p, Ap.p, false, NEAR_DD);
+      last.fp64_applies++;
+      k_residual<<<nb3, VB, 0, stream>>>(n3, F.p, Ap.p, r.p, slots(S_RED), scal.p);
+      CG_LAUNCH();
+    }
+  }
+  for (int outer = (int)outer_hist.size(); outer < max_outer && status != CPPE_GPU_OK; ++outer) {
     double rnorm;
     if (!have_inner_start) {
       // r holds the FP64 residual; read its norm and set up the inner solve.
@@ -624,7 +705,7 @@ int System::solve_mixed(bool zero_guess, double* hist_out, int hist_cap, int* it
       CG_CUDA(cudaStreamSynchronize(stream));
       rnorm = h_scal[S_RNORM];
       outer_hist.push_back(rnorm);
-      if (rnorm < t) {
+      if (rnorm + rerr < t) {
         status = CPPE_GPU_OK;
         break;
       }
@@ -655,18 +736,18 @@ int System::solve_mixed(bool zero_guess, double* hist_out, int hist_cap, int* it
     CG_CUDA(cudaStreamSynchronize(stream));
     total_inner += h_flags[1];
     last.fp32_applies += h_flags[1];
-    // After an exact residual r, the inner solve's B d = fl(r) - r32 is known
-    // from its own recursion to ~1e-6 ||r|| (FP32 operator and rounding of
-    // the updates); where that is below 1e-3 of the threshold the residual
-    // is formed from r32 without another apply.  Else an FP32 apply of d
-    // (error ~1e-7 ||B d|| ~ 1e-7 ||r||) where that is small enough, else the
-    // FP64 operator.
-    if (have_fp64_residual && rnorm * 1e-6 < 1e-3 * t) {
+    // After a residual r (exact or within rerr), the inner solve's
+    // B d = fl(r) - r32 is known from its own recursion (bound REC_ERR ||r||);
+    // where the bounds stay below t / 10 the residual is formed from r32
+    // without another apply, else from an FP32 apply of d (CORR_ERR), else
+    // with the FP64 operator.
+    if (have_fp64_residual && rerr + REC_ERR * rnorm < 0.1 * t) {
       k_residual_inner<<<nb3, VB, 0, stream>>>(n3, r32.p, r.p, slots(S_RED), scal.p);
       CG_LAUNCH();
       k_accumulate<<<nb3, VB, 0, stream>>>(n3, x.p, d32.p);
       CG_LAUNCH();
-    } else if (!(have_fp64_residual && rnorm * 1e-4 < t)) {
+      rerr += REC_ERR * rnorm;
+    } else if (!(have_fp64_residual && rerr + CORR_ERR * rnorm < 0.1 * t)) {
       // x += d; r = F - B64 x: the residual recomputed with the FP64 operator
       k_accumulate<<<nb3, VB, 0, stream>>>(n3, x.p, d32.p);
       CG_LAUNCH();
@@ -675,6 +756,7 @@ int System::solve_mixed(bool zero_guess, double* hist_out, int hist_cap, int* it
       k_residual<<<nb3, VB, 0, stream>>>(n3, F.p, Ap.p, r.p, slots(S_RED), scal.p);
       CG_LAUNCH();
       have_fp64_residual = true;
+      rerr               = 0.0;
     } else {
       // Later corrections are small: r -= B d with B d in FP32 (its error is
       // ~1e-7 of ||B d|| ~ ||r||, far below the threshold), accumulated into
@@ -685,13 +767,14 @@ int System::solve_mixed(bool zero_guess, double* hist_out, int hist_cap, int* it
       CG_LAUNCH();
       k_accumulate<<<nb3, VB, 0, stream>>>(n3, x.p, d32.p);
       CG_LAUNCH();
+      rerr += CORR_ERR * rnorm;
     }
   }
   if (status != CPPE_GPU_OK) {
     CG_CUDA(cudaMemcpyAsync(h_scal, scal.p, S_NSCAL * sizeof(double), cudaMemcpyDeviceToHost,
                             stream));
     CG_CUDA(cudaStreamSynchronize(stream));
-    if (h_scal[S_RNORM] < t) status = CPPE_GPU_OK;
+    if (h_scal[S_RNORM] + rerr < t) status = CPPE_GPU_OK;
     outer_hist.push_back(h_scal[S_RNORM]);
   }
   last.iterations  = total_inner;

@@ -19,6 +19,7 @@ enum Scalar {
   S_RNORM,    // ||r||_2 after the last update
   S_TOL,      // stopping threshold of the running loop
   S_RZOLD,    // r . z before the last update (flexible CG)
+  S_RSTAGE = 12,  // ||r|| at the set-up of the running inner solve
   S_RED = 8,  // 4 slots receiving grid reductions
   S_NSCAL = 16
 };
@@ -95,6 +96,8 @@ struct System {
   // inner FP32 PCG loop of the mixed solver (graph-launched when possible)
   void inner_iteration_fp32(int nb, int nb3);
   void run_inner_fp32(int nb, int nb3);
+  // builds the inner loop's graph on first use; false where graphs are off
+  bool inner_graph_ready(int nb, int nb3);
   cudaGraphExec_t inner_exec[2] = {nullptr, nullptr};  // plain / learned body
   long long inner_body_launches[2] = {0, 0};
   bool inner_graph_failed = false;
