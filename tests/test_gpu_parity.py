@@ -178,6 +178,27 @@ def test_double_float_apply_matches_fp64(gpu, fmm, damp, order):
     assert err_dd < 1e-3 * err_32
 
 
+@pytest.mark.parametrize("thresh", [1e-8, 1e-11])
+def test_mixed_solve_meets_the_threshold(gpu, thresh):
+    """The mixed solver's answer meets the threshold with the FP64 operator,
+    both where its residuals come from the inner recursion (1e-8) and where
+    the first inner solve leaves too large a residual for that, so that the
+    solver recomputes them with the FP64 operator (1e-11)."""
+    from cppe_gb300 import synthetic
+    b = synthetic.water_box(2000, seed=33)
+    kw = dict(summation=cabi.FMM, damp=True, thresh=thresh, maxiter=80)
+    s64 = cabi.System(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, precision=cabi.FP64, **kw)
+    smx = cabi.System(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, precision=cabi.MIXED, **kw)
+    rhs = b.external_field() + 0.05 * np.random.default_rng(7).normal(size=3 * b.n)
+    mu, _, hist, rc = smx.solve(rhs)
+    st = smx.stats()
+    res = np.linalg.norm(rhs - s64.apply(mu))
+    assert res < thresh, (res, hist)
+    assert st["rnorm"] < thresh and abs(st["rnorm"] - res) < 0.1 * thresh
+    if thresh < 1e-10:
+        assert st["fp64_applies"] >= 2  # the residual was recomputed
+
+
 def test_autotune_keeps_the_operator(gpu):
     """The schedule autotuner changes the work partition, not the operator."""
     from cppe_gb300 import synthetic
