@@ -410,13 +410,13 @@ int cppe_gpu_solve(cppe_gpu_system* sys, const double* rhs, const double* guess,
     System& S = sys->s;
     CG_CUDA(cudaSetDevice(S.device));
     const size_t n3 = 3 * (size_t)S.n;
-    DBuf<double> drhs, dg, dmu;
-    drhs.upload(rhs, n3, S.stream);
-    if (guess && !make_guess) dg.upload(guess, n3, S.stream);
-    dmu.alloc(n3);
-    int st = S.solve_device(drhs.p, (guess && !make_guess) ? dg.p : nullptr, make_guess,
-                            dmu.p, iters, rnorm_hist, hist_cap);
-    CG_CUDA(cudaMemcpyAsync(mu, dmu.p, n3 * sizeof(double), cudaMemcpyDeviceToHost, S.stream));
+    S.io_rhs.upload(rhs, n3, S.stream);
+    if (guess && !make_guess) S.io_guess.upload(guess, n3, S.stream);
+    S.io_mu.alloc(n3);
+    int st = S.solve_device(S.io_rhs.p, (guess && !make_guess) ? S.io_guess.p : nullptr,
+                            make_guess, S.io_mu.p, iters, rnorm_hist, hist_cap);
+    CG_CUDA(cudaMemcpyAsync(mu, S.io_mu.p, n3 * sizeof(double), cudaMemcpyDeviceToHost,
+                            S.stream));
     CG_CUDA(cudaStreamSynchronize(S.stream));
     return st;
   });

@@ -221,12 +221,23 @@ __global__ void k_features(NearListView nl, const float* __restrict__ a6,
   const float rc = (float)LEARN_RC;
   const float w16 = (rc - 1.f) / 15.f, w8 = (rc - 1.f) / 7.f;
   const int k0 = ok ? nl.ptr[ii] : 0, k1 = ok ? nl.ptr[ii + 1] : 0;
+  // the next entry's loads (and its dependent polarizability gather) are
+  // issued before this entry's arithmetic, which hides their latency
+  float4 dv_n = make_float4(0.f, 0.f, 0.f, 1.f);
+  float aj_n  = 0.f;
+  if (k0 + sub < k1) {
+    dv_n = nl.d[k0 + sub];
+    aj_n = aiso6(a6 + 6 * (size_t)nl.idx[k0 + sub]);
+  }
   for (int k = k0 + sub; k < k1; k += 8) {
-    const float4 dv = nl.d[k];
-    const int j     = nl.idx[k];
+    const float4 dv = dv_n;
+    const float aj  = aj_n * 0.25f;
+    if (k + 8 < k1) {
+      dv_n = nl.d[k + 8];
+      aj_n = aiso6(a6 + 6 * (size_t)nl.idx[k + 8]);
+    }
     const float r   = dv.w;
     const float fc  = 0.5f * (__cosf(3.14159265f * r / rc) + 1.f);
-    const float aj  = aiso6(a6 + 6 * (size_t)j) * 0.25f;
 #pragma unroll
     for (int q = 0; q < 16; ++q) {
       const float t = (r - (1.f + q * w16)) / w16;

@@ -292,6 +292,55 @@ void System::init(int n_, const double* xyz, const double* alpha6, const int* ex
   CG_CUDA(cudaMallocHost(&h_flags, 4 * sizeof(int)));
   CG_CUDA(cudaMallocHost(&h_scal, S_NSCAL * sizeof(double)));
   CG_CUDA(cudaStreamSynchronize(stream));
+  setup_inexact(xyz, sd.data());
+}
+
+// Opening angle of the inexact inner operator.  At 30,000 water sites it
+// moves 42 % of the near-field pairs into M2L (FP32 apply 0.146 ms against
+// 0.212 ms) and differs from the operator by 2e-4 - 3e-4 relative.
+constexpr double INEXACT_THETA = 0.6;
+
+void System::setup_inexact(const double* xyz, const double* sd) {
+  have_inexact = false;
+  if (!geo.fmm || opt.precision != CPPE_GPU_MIXED || opt.theta >= INEXACT_THETA) return;
+  geo2.damping = geo.damping;
+  geo2.build(n, xyz, sd, excl_ptr_h.empty() ? nullptr : excl_ptr_h.data(),
+             excl_idx_h.empty() ? nullptr : excl_idx_h.data(), true, opt.tree_ncrit,
+             INEXACT_THETA, stream);
+  // the opening angle changes the lists, not the tree: same site order
+  if (geo2.layout.perm != geo.layout.perm) return;
+  // relative difference from the FP64 operator on a random vector and on a
+  // smooth one (the response of every site to one uniform field)
+  const size_t n3 = 3 * (size_t)n;
+  std::vector<double> v(n3), a64(n3), a32(n3);
+  double worst = 0.0;
+  unsigned long long st = 0x9e3779b97f4a7c15ull;
+  for (int trial = 0; trial < 2; ++trial) {
+    for (size_t k = 0; k < n3; ++k) {
+      if (trial == 0) {
+        st ^= st << 13, st ^= st >> 7, st ^= st << 17;
+        v[k] = (double)(st >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+      } else {
+        v[k] = (k % 3 == 0) ? 1.0 : (k % 3 == 1 ? 0.5 : 0.25);
+      }
+    }
+    CG_CUDA(cudaMemcpyAsync(tmp_in.p, v.data(), n3 * sizeof(double), cudaMemcpyHostToDevice,
+                            stream));
+    apply64(tmp_in.p, tmp_out.p, false, NEAR_DD);
+    CG_CUDA(cudaMemcpyAsync(a64.data(), tmp_out.p, n3 * sizeof(double), cudaMemcpyDeviceToHost,
+                            stream));
+    apply_inexact = true, have_inexact = true;
+    apply32_widen(tmp_in.p, tmp_out.p);
+    apply_inexact = false, have_inexact = false;
+    CG_CUDA(cudaMemcpyAsync(a32.data(), tmp_out.p, n3 * sizeof(double), cudaMemcpyDeviceToHost,
+                            stream));
+    CG_CUDA(cudaStreamSynchronize(stream));
+    double num = 0.0, den = 0.0;
+    for (size_t k = 0; k < n3; ++k) num += (a32[k] - a64[k]) * (a32[k] - a64[k]), den += a64[k] * a64[k];
+    if (den > 0.0) worst = std::max(worst, std::sqrt(num / den));
+  }
+  inexact_delta = 3.0 * worst;
+  have_inexact  = worst > 0.0 && inexact_delta < 1e-2;
 }
 
 void System::apply32_widen(const double* in, double* out) {
@@ -411,9 +460,10 @@ void System::apply64(const double* in, double* out, bool with_dot, int near_mode
 
 void System::apply32(const float* in, float* out, bool with_dot) {
   ReduceSlots rs = slots(S_PAP);
-  eval_field<float>(geo, ops.get(), w32, 1, in, opt.damp != 0, opt.damping_factor,
-                    FINISH_APPLY, ainv32.p, out, nullptr, 1.0, with_dot ? &rs : nullptr,
-                    stream, nullptr, NEAR_FP64, &side);
+  const bool inexact = apply_inexact && have_inexact;
+  eval_field<float>(inexact ? geo2 : geo, ops.get(), inexact ? w32b : w32, 1, in,
+                    opt.damp != 0, opt.damping_factor, FINISH_APPLY, ainv32.p, out, nullptr, 1.0,
+                    with_dot ? &rs : nullptr, stream, nullptr, NEAR_FP64, &side);
 }
 
 namespace {
@@ -497,12 +547,48 @@ int System::solve_fp64(bool zero_guess, double* hist_out, int hist_cap, int* ite
 // which is also kept (S_RSTAGE); the iterations of the previous inner solve
 // are added to flags[3] (stage 0 clears it); flags[2] = 1 when the residual
 // already meets t, which makes the following k_cg_start start a finished solve.
-__global__ void k_inner_stage(double* scal, int* flags, double t, double eta, int stage) {
+// With an inexact operator (delta > 0) the solve runs with the operator
+// down to S_TOL = max(threshold, switch point) and then with the inexact one
+// down to S_TOL2 = the threshold.  Switch points: where the inexact
+// operator's effect on the residual, ~delta ||r||, stays below 0.3 of the
+// stage's target (stage 0: eta ||r0||), or, for the last stage, where
+// 1.5 delta ||r|| stays below 0.4 t (the residual is then formed from the
+// recursion, which carries that difference).
+__global__ void k_inner_stage(double* scal, int* flags, double t, double eta, int stage,
+                              double delta) {
+  const double rn  = scal[S_RNORM];
+  const double tol = fmax(eta * rn, 0.5 * t);
+  double sw        = tol;
+  if (delta > 0.0) sw = stage == 0 ? 0.3 * eta * rn / delta : 0.4 * t / (1.5 * delta);
+  scal[S_TOL2]     = tol;
+  scal[S_TOL]      = fmax(tol, sw);
+  scal[S_RSTAGE]   = rn;
+  scal[S_RSWITCH]  = 0.0;
+  flags[3]         = stage == 0 ? 0 : flags[3] + flags[1];
+  flags[2]         = 0;
+  // flags[2] = 1 makes the following k_cg_start start a finished solve
+  if (stage > 0 && rn < t) {
+    flags[2]     = 1;  // nothing left to do: neither part runs
+    scal[S_TOL2] = 1e300;
+  } else if (stage > 0 && rn < scal[S_TOL]) {
+    flags[2] = 1;  // the operator's part has nothing to do
+  }
+}
+
+// Hand-over from the operator to the inexact one inside an inner solve: the
+// solve continues (same direction and scalars) unless it has reached its
+// final threshold or the iteration limit.
+// flags[0] = 0 lets the stopping iteration's skipped direction update run
+// before the inexact part; 3 (no iteration ran) skips it, k_inner_resume
+// then clears it.
+__global__ void k_inner_switch(double* scal, int* flags) {
   const double rn = scal[S_RNORM];
-  scal[S_TOL]     = fmax(eta * rn, 0.5 * t);
-  scal[S_RSTAGE]  = rn;
-  flags[3]        = stage == 0 ? 0 : flags[3] + flags[1];
-  flags[2]        = stage > 0 && rn < t ? 1 : 0;
+  scal[S_RSWITCH] = rn;
+  scal[S_TOL]     = scal[S_TOL2];
+  if (flags[0] == 1 && rn >= scal[S_TOL2]) flags[0] = flags[1] > 0 ? 0 : 3;
+}
+__global__ void k_inner_resume(int* flags) {
+  if (flags[0] == 3) flags[0] = 0;
 }
 
 // Continues the inner graph's while loop until the solve has stopped.
@@ -528,11 +614,13 @@ void System::inner_iteration_fp32(int nb, int nb3) {
 // The inner loop as a CUDA graph with a conditional while node: the body is
 // one iteration captured from the stream (including the far-field side
 // stream's fork and join), repeated on the device until k_cg_update sets
-// flags[0] (converged, or the iteration limit).  Built once per system and
-// learned/plain variant, after the buffers it uses exist.  Where graph
-// construction is refused, the iterations are launched from the host.
-bool System::inner_graph_ready(int nb, int nb3) {
-  const int v = use_model ? 1 : 0;
+// flags[0] (converged, or the iteration limit); a kernel ahead of the loop
+// sets its condition, so a solve that is already finished runs no
+// iteration.  Built once per system and learned/plain variant and operator,
+// after the buffers it uses exist.  Where graph construction is refused, the
+// iterations are launched from the host.
+bool System::inner_graph_ready(int nb, int nb3, bool inexact) {
+  const int v = (use_model ? 1 : 0) + (inexact && have_inexact ? 2 : 0);
   // CPPE_GPU_GRAPHS=0 launches the iterations from the host instead (same
   // kernels; for profilers that do not descend into conditional graph nodes)
   static const bool graphs = [] {
@@ -546,14 +634,28 @@ bool System::inner_graph_ready(int nb, int nb3) {
     cudaGraphConditionalHandle h{};
     cudaGraphNode_t node{};
     cudaGraphNodeParams np{};
-    ok = ok && cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) ==
+    ok = ok && cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault) ==
                      cudaSuccess;
+    // the kernel that sets the loop's first condition, captured into g
+    cudaGraphNode_t pre{};
+    if (ok) {
+      ok = cudaStreamBeginCaptureToGraph(stream, g, nullptr, nullptr, 0,
+                                         cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+      if (ok) {
+        k_while_running<<<1, 1, 0, stream>>>(h, flags.p);
+        ok = cudaGetLastError() == cudaSuccess;
+        cudaGraph_t captured = nullptr;
+        ok = (cudaStreamEndCapture(stream, &captured) == cudaSuccess) && ok;
+      }
+      size_t nn = 1;
+      ok = ok && cudaGraphGetNodes(g, &pre, &nn) == cudaSuccess && nn == 1;
+    }
     if (ok) {
       np.type                 = cudaGraphNodeTypeConditional;
       np.conditional.handle   = h;
       np.conditional.type     = cudaGraphCondTypeWhile;
       np.conditional.size     = 1;
-      ok = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np) == cudaSuccess;
+      ok = cudaGraphAddNode(&node, g, &pre, nullptr, 1, &np) == cudaSuccess;
     }
     if (ok) {
       cudaGraph_t body = np.conditional.phGraph_out[0];
@@ -561,6 +663,7 @@ bool System::inner_graph_ready(int nb, int nb3) {
                                          cudaStreamCaptureModeThreadLocal) == cudaSuccess;
       if (ok) {
         const long long c0 = launch_counter();
+        apply_inexact      = inexact && have_inexact;
         try {
           inner_iteration_fp32(nb, nb3);
           k_while_running<<<1, 1, 0, stream>>>(h, flags.p);
@@ -568,6 +671,7 @@ bool System::inner_graph_ready(int nb, int nb3) {
         } catch (const Failure&) {
           ok = false;
         }
+        apply_inexact = false;
         inner_body_launches[v] = launch_counter() - c0;
         launch_counter()       = c0;
         cudaGraph_t captured   = nullptr;
@@ -647,24 +751,43 @@ int System::solve_mixed(bool zero_guess, double* hist_out, int hist_cap, int* it
   // the recursion -- queued at once with the decisions on the device and one
   // host synchronisation; the loop below takes over where it does not end
   // the solve (or where the inner iterations cannot run as a graph).
-  if (!zero_guess && inner_graph_ready(nb, nb3)) {
-    const int v = use_model ? 1 : 0;
-    k_inner_stage<<<1, 1, 0, stream>>>(scal.p, flags.p, t, eta, 0);
+  if (!zero_guess && inner_graph_ready(nb, nb3) &&
+      (!have_inexact || inner_graph_ready(nb, nb3, true))) {
+    const int v      = use_model ? 1 : 0;
+    const bool inex  = have_inexact;
+    const double dlt = inex ? inexact_delta : 0.0;
+    // one inner solve: the operator's graph, then (with an inexact operator)
+    // the hand-over and the inexact graph
+    auto inner = [&]() {
+      CG_CUDA(cudaGraphLaunch(inner_exec[v], stream));
+      if (!inex) return;
+      k_inner_switch<<<1, 1, 0, stream>>>(scal.p, flags.p);
+      CG_LAUNCH();
+      // the direction update the stopping iteration skipped (no-ops if the
+      // solve stays finished)
+      const float* zd = use_model ? learned_precond<float>(z32.p, r32.p, p32.p, false) : z32.p;
+      k_cg_dir<float><<<nb3, VB, 0, stream>>>(3 * n, zd, p32.p, scal.p, flags.p);
+      CG_LAUNCH();
+      k_inner_resume<<<1, 1, 0, stream>>>(flags.p);
+      CG_LAUNCH();
+      CG_CUDA(cudaGraphLaunch(inner_exec[v + 2], stream));
+    };
+    k_inner_stage<<<1, 1, 0, stream>>>(scal.p, flags.p, t, eta, 0, dlt);
     CG_LAUNCH();
-    CG_CUDA(cudaGraphLaunch(inner_exec[v], stream));
+    inner();
     k_accumulate<<<nb3, VB, 0, stream>>>(n3, x.p, d32.p);
     CG_LAUNCH();
     apply64(x.p, Ap.p, false, NEAR_DD);
     k_residual<<<nb3, VB, 0, stream>>>(n3, F.p, Ap.p, r.p, slots(S_RED), scal.p);
     CG_LAUNCH();
-    k_inner_stage<<<1, 1, 0, stream>>>(scal.p, flags.p, t, eta, 1);
+    k_inner_stage<<<1, 1, 0, stream>>>(scal.p, flags.p, t, eta, 1, dlt);
     CG_LAUNCH();
     k_cg_start<float><<<nb, VB, 0, stream>>>(n, r.p, nullptr, alpha32.p, r32.p, z32.p, p32.p,
                                              slots(S_RED), scal.p, flags.p,
                                              use_model ? lf_z4.p : nullptr, flags.p + 2);
     CG_LAUNCH();
     if (use_model) learned_precond<float>(z32.p, r32.p, p32.p, true);
-    CG_CUDA(cudaGraphLaunch(inner_exec[v], stream));
+    inner();
     k_residual_inner<<<nb3, VB, 0, stream>>>(n3, r32.p, r.p, slots(S_RED), scal.p);
     CG_LAUNCH();
     k_accumulate<<<nb3, VB, 0, stream>>>(n3, x.p, d32.p);
@@ -677,14 +800,17 @@ int System::solve_mixed(bool zero_guess, double* hist_out, int hist_cap, int* it
     total_inner += it1 + it2;
     last.fp32_applies += it1 + it2;
     last.fp64_applies++;
-    launch_counter() += inner_body_launches[v] * (std::max(1, it1) + std::max(1, it2));
+    launch_counter() += inner_body_launches[v] * (it1 + it2) + (inex ? 8 : 2);
     const double r1 = h_scal[S_RSTAGE];  // FP64 residual after the first inner solve
     outer_hist.push_back(r1);
     have_fp64_residual = true;
     have_inner_start   = false;
-    // the residual from the recursion stands where its error is below 1e-3 t
-    const bool recursion_ok = r1 < t || REC_ERR * r1 < 0.1 * t;
-    if (recursion_ok && r1 >= t) rerr = REC_ERR * r1;
+    // the residual from the recursion stands where its error bound is below
+    // t / 10 (the inexact operator adds ~1.5 delta ||r|| from the hand-over on)
+    const double rsw = inex ? std::min(r1, h_scal[S_RSWITCH]) : 0.0;
+    const double bound = REC_ERR * r1 + 1.5 * dlt * rsw;
+    const bool recursion_ok = r1 < t || bound < 0.4 * t;
+    if (recursion_ok && r1 >= t) rerr = bound;
     if (recursion_ok && h_scal[S_RNORM] + rerr < t) {
       if (r1 >= t) outer_hist.push_back(h_scal[S_RNORM]);
       status = CPPE_GPU_OK;

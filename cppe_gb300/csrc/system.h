@@ -20,6 +20,8 @@ enum Scalar {
   S_TOL,      // stopping threshold of the running loop
   S_RZOLD,    // r . z before the last update (flexible CG)
   S_RSTAGE = 12,  // ||r|| at the set-up of the running inner solve
+  S_TOL2   = 13,  // threshold of the inner solve's inexact part
+  S_RSWITCH = 14, // ||r|| where the inner solve went over to the inexact operator
   S_RED = 8,  // 4 slots receiving grid reductions
   S_NSCAL = 16
 };
@@ -39,6 +41,17 @@ struct System {
   std::unique_ptr<DeviceOps> ops;  // m = 1, p = order (FMM only)
   FieldWork<double> w64;
   FieldWork<float> w32;
+  // The inexact inner operator of the mixed solver: the same tree walked with
+  // a larger opening angle (fewer near pairs), in FP32; `inexact_delta`
+  // bounds its relative difference from the operator (measured at set-up,
+  // times 3).  Used by the inner solves once their residual is small enough
+  // that the difference stays below what they must resolve.
+  Geometry geo2;
+  FieldWork<float> w32b;
+  bool have_inexact    = false;
+  double inexact_delta = 0.0;
+  bool apply_inexact   = false;  // apply32 uses geo2 (set while capturing)
+  void setup_inexact(const double* xyz, const double* sd);
   // operator data in device order
   DBuf<double> ainv64, alpha64;  // 6 per site
   DBuf<float> ainv32, alpha32;
@@ -60,6 +73,9 @@ struct System {
   DBuf<float> lf_feats, lf_v1, lf_v2, lf_v3, lf_Y, lf_c, lf_w32, lf_rold32;
   DBuf<double> lf_w64, lf_rold64;
   DBuf<float4> lf_z4;  // z of the FP32 inner solve as float4 per site (gathers)
+  // device copies for the host-buffer solve entry point (kept between calls:
+  // a cudaMalloc/cudaFree pair per solve costs about as much as the copies)
+  DBuf<double> io_rhs, io_guess, io_mu;
   void learned_setup();
   // descriptors and basis vectors for the current F (device order)
   void learned_features_for_F();
@@ -97,9 +113,10 @@ struct System {
   void inner_iteration_fp32(int nb, int nb3);
   void run_inner_fp32(int nb, int nb3);
   // builds the inner loop's graph on first use; false where graphs are off
-  bool inner_graph_ready(int nb, int nb3);
-  cudaGraphExec_t inner_exec[2] = {nullptr, nullptr};  // plain / learned body
-  long long inner_body_launches[2] = {0, 0};
+  bool inner_graph_ready(int nb, int nb3, bool inexact = false);
+  // plain / learned body, with the operator / the inexact operator
+  cudaGraphExec_t inner_exec[4] = {nullptr, nullptr, nullptr, nullptr};
+  long long inner_body_launches[4] = {0, 0, 0, 0};
   bool inner_graph_failed = false;
   int solve_device(const double* d_rhs, const double* d_guess, int make_guess, double* d_mu,
                    int* iters, double* hist_out, int hist_cap);
