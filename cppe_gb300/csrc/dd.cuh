@@ -104,6 +104,101 @@ __device__ __forceinline__ dd dd_exp_neg(dd v, const float2* tab) {
 }
 
 // ---------------------------------------------------------------------------
+// Packed double-float: two independent dd values in the halves of float2
+// registers, so that one FFMA2/FMUL2/FADD2 (sm_100 and later) advances both.
+// Same algorithms as the scalar functions above.
+// ---------------------------------------------------------------------------
+struct dd2 {
+  float2 h, l;
+};
+__device__ __forceinline__ float2 p2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 pneg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 padd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 psub(float2 a, float2 b) { return __fadd2_rn(a, pneg(b)); }
+__device__ __forceinline__ float2 pmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 pfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 psel(bool cx, bool cy, float2 a, float2 b) {
+  return make_float2(cx ? a.x : b.x, cy ? a.y : b.y);
+}
+__device__ __forceinline__ dd2 dd2_sel(bool cx, bool cy, dd2 a, dd2 b) {
+  return {psel(cx, cy, a.h, b.h), psel(cx, cy, a.l, b.l)};
+}
+__device__ __forceinline__ dd2 dd2_two_sum(float2 a, float2 b) {
+  const float2 s  = padd(a, b);
+  const float2 bb = psub(s, a);
+  return {s, padd(psub(a, psub(s, bb)), psub(b, bb))};
+}
+__device__ __forceinline__ dd2 dd2_fast_two_sum(float2 a, float2 b) {
+  const float2 s = padd(a, b);
+  return {s, psub(b, psub(s, a))};
+}
+__device__ __forceinline__ dd2 dd2_add(dd2 a, dd2 b) {
+  const dd2 s = dd2_two_sum(a.h, b.h);
+  return dd2_fast_two_sum(s.h, padd(s.l, padd(a.l, b.l)));
+}
+__device__ __forceinline__ dd2 dd2_add_lazy(dd2 a, dd2 b) {
+  const dd2 s = dd2_two_sum(a.h, b.h);
+  return {s.h, padd(s.l, padd(a.l, b.l))};
+}
+__device__ __forceinline__ dd2 dd2_neg(dd2 a) { return {pneg(a.h), pneg(a.l)}; }
+__device__ __forceinline__ dd2 dd2_mul(dd2 a, dd2 b) {
+  const float2 p = pmul(a.h, b.h);
+  float2 e       = pfma(a.h, b.h, pneg(p));
+  e              = pfma(a.h, b.l, e);
+  e              = pfma(a.l, b.h, e);
+  return {p, e};
+}
+__device__ __forceinline__ dd2 dd2_sqr(dd2 a) {
+  const float2 p = pmul(a.h, a.h);
+  float2 e       = pfma(a.h, a.h, pneg(p));
+  e              = pfma(padd(a.h, a.h), a.l, e);
+  return {p, e};
+}
+__device__ __forceinline__ dd2 dd2_sqr_full(dd2 a) {
+  const float2 p = pmul(a.h, a.h);
+  float2 e       = pfma(a.h, a.h, pneg(p));
+  e              = pfma(padd(a.h, a.h), a.l, e);
+  e              = pfma(a.l, a.l, e);
+  return {p, e};
+}
+__device__ __forceinline__ dd2 dd2_mul_f(dd2 a, float2 b) {
+  const float2 p = pmul(a.h, b);
+  return {p, pfma(a.l, b, pfma(a.h, b, pneg(p)))};
+}
+// 1/sqrt(a) for a > 0 (as dd_rsqrt); the estimate is one MUFU operation per
+// half (`rsqrt.approx.ftz`: the inputs are squared distances, never subnormal)
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ dd2 dd2_rsqrt(dd2 a) {
+  const float2 y  = make_float2(rsqrt_ftz(a.h.x), rsqrt_ftz(a.h.y));
+  const float2 q  = pmul(y, y);
+  const float2 qe = pfma(y, y, pneg(q));
+  float2 h        = pfma(a.h, q, p2(-1.f));
+  h               = pfma(a.h, qe, pfma(a.l, q, h));
+  return {y, pmul(pmul(y, h), pfma(p2(0.375f), h, p2(-0.5f)))};
+}
+// e^-v as dd_exp_neg, each half with its own table entry; v.h < 20 (callers
+// clamp the halves they do not use)
+__device__ __forceinline__ dd2 dd2_exp_neg(dd2 v, const float* tab_h, const float* tab_l) {
+  const int kx    = __float2int_rn(v.h.x * 16.f), ky = __float2int_rn(v.h.y * 16.f);
+  const float2 th = pfma(make_float2((float)kx, (float)ky), p2(-0.0625f), v.h);
+  const dd2 t     = dd2_two_sum(th, v.l);
+  const dd2 t2    = dd2_sqr(t);
+  float2 c        = pfma(t.h, p2(1.f / 720.f), p2(-1.f / 120.f));
+  c               = pfma(t.h, c, p2(1.f / 24.f));
+  c               = pfma(t.h, c, p2(-1.f / 6.f));
+  const float2 r3 = pmul(pmul(t2.h, t.h), c);
+  const dd2 s     = dd2_fast_two_sum(p2(1.f), pneg(t.h));
+  const dd2 s2    = dd2_fast_two_sum(s.h, pmul(p2(0.5f), t2.h));
+  const float2 el = padd(pfma(p2(0.5f), t2.l, psub(padd(s.l, s2.l), t.l)), r3);
+  const dd2 e     = {make_float2(tab_h[kx], tab_h[ky]), make_float2(tab_l[kx], tab_l[ky])};
+  return dd2_mul(e, {s2.h, el});
+}
+
+// ---------------------------------------------------------------------------
 // A value type over dd for generic code (the generated M2L translations):
 // +, -, * with dd accuracy, division by a Newton-corrected quotient.
 // ---------------------------------------------------------------------------

@@ -2,7 +2,7 @@
 // the FMM passes and the finishing pass.
 //
 // Reference counterparts (maxscheurer/cppe, src/core/fmm/):
-//   k_p2p, k_p2p32_m1, k_p2p_dd
+//   k_p2p, k_p2p32_m1, k_p2p_dd2
 //              evaluate_direct{,_damping} calculate.cc:262-300,
 //              evaluate_P2P_lazy + P2P_Cells{,_damping} calculate.cc:29-72,205-225
 //   k_p2m_tasks + k_msum
@@ -885,149 +885,185 @@ __global__ void __launch_bounds__(P2P_BLOCK)
 
 // ---------------------------------------------------------------------------
 // Near field in double-float arithmetic (dipole sources): the FP64-accurate
-// pass of the mixed solver's residual B x, on the FP32 pipe.  Same items and
-// tiles as k_p2p; each pair is evaluated in DD (about 1e-13 relative per
-// term), accumulated in DD and written in FP64.  Separations are exact in
-// their high parts because the FP32 coordinates are snapped to a common grid.
+// pass of the mixed solver's residual B x, on the FP32 pipe.  Same items,
+// tiles and damping split as the FP32 pass; each pair is evaluated in
+// double-float (about 1e-13 relative per term), accumulated in double-float
+// and written in FP64.  Separations are exact in their high parts because
+// the FP32 coordinates are snapped to a common grid.  Packed FP32x2
+// arithmetic evaluates one target against two staged sources per operation
+// (the dd2 helpers of dd.cuh); the per-pair branches become per-half
+// selects: the self pair (R = 0), sites without a damping partner
+// (a = 0) and v >= 50 keep the undamped tensor; with MODE 0 the damping
+// factors come from the double-float exponential where v < 20 and from the
+// FP32 deficit (< 5e-7 there) elsewhere; with MODE 1 (every v >= 20) from
+// the FP32 deficit only.
 // ---------------------------------------------------------------------------
-// MODE 0: any v; 1: every v >= 20 (the double-float exponential is never
-// needed); 2: every v >= 50 (no damping).
-template <bool DAMP, int MODE = 0>
-__device__ __forceinline__ void dd_pair_m1(const SiteRec<float>& ti, dd ai,
-                                           const SiteRec<float>& sj, const float* mu,
-                                           const float2* etab, dd (&f)[3]) {
-  const dd x = {ti.x - sj.x, ti.lx - sj.lx};
-  const dd y = {ti.y - sj.y, ti.ly - sj.ly};
-  const dd z = {ti.z - sj.z, ti.lz - sj.lz};
-  const dd r2 = dd_add(dd_add_lazy(dd_sqr_full(x), dd_sqr_full(y)), dd_sqr_full(z));
-  if (r2.h == 0.f) return;  // a site paired with itself (direct summation)
-  const dd ir  = dd_rsqrt(r2);
-  const dd ir2 = dd_sqr(ir);
-  const dd ir3 = dd_mul(ir2, ir);
-  dd G1        = dd_neg(ir3);
-  dd G2        = dd_mul_f(dd_mul(ir3, ir2), 3.f);
+struct DDSrc2 {
+  dd2 x, y, z, s, mx, my, mz;
+};
+template <bool DAMP, int MODE>
+__device__ __forceinline__ void dd2_pair_m1(const dd2& tx, const dd2& ty, const dd2& tz,
+                                            const dd2& ai, const DDSrc2& q, const float* eh,
+                                            const float* el, dd2 (&f)[3]) {
+  const dd2 x  = {psub(tx.h, q.x.h), psub(tx.l, q.x.l)};
+  const dd2 y  = {psub(ty.h, q.y.h), psub(ty.l, q.y.l)};
+  const dd2 z  = {psub(tz.h, q.z.h), psub(tz.l, q.z.l)};
+  const dd2 r2 = dd2_add(dd2_add_lazy(dd2_sqr_full(x), dd2_sqr_full(y)), dd2_sqr_full(z));
+  const bool okx = r2.h.x > 0.f, oky = r2.h.y > 0.f;  // false: a site paired with itself
+  const dd2 zero = {p2(0.f), p2(0.f)};
+  const dd2 ir   = dd2_sel(okx, oky, dd2_rsqrt(dd2_sel(okx, oky, r2, {p2(1.f), p2(0.f)})), zero);
+  const dd2 ir2  = dd2_sqr(ir);
+  const dd2 ir3  = dd2_mul(ir2, ir);
+  dd2 G1         = dd2_neg(ir3);
+  dd2 G2         = dd2_mul_f(dd2_mul(ir3, ir2), p2(3.f));
   if (DAMP && MODE < 2) {
-    const dd a = dd_mul(ai, dd{sj.s, sj.ls});
-    if (a.h > 0.f) {
-      const dd v = dd_mul(a, dd_mul(r2, ir));
-      if (v.h < 50.f) {
-        dd fE, fT;
-        if (MODE == 0 && v.h < 20.f) {
-          const dd e  = dd_exp_neg(v, etab);
-          const dd v2 = dd_sqr(v);
-          const dd u  = dd_add(dd_two_sum(1.f, v.h), dd{0.5f * v2.h, v.l + 0.5f * v2.l});
-          const dd w  = dd_mul(dd_mul(v2, v), dd{1.f / 6.f, DD_SIXTH_LO});
-          fE          = dd_sub(dd{1.f, 0.f}, dd_mul(u, e));
-          fT          = dd_sub(fE, dd_mul(w, e));
-        } else {
-          // (1 + v + v^2/2) e^-v < 5e-7 here: FP32 suffices for the deficit
-          const float e = expf(-v.h);
-          const float u = fmaf(v.h, fmaf(v.h, 0.5f, 1.f), 1.f) * e;
-          const float w = v.h * v.h * v.h * (1.f / 6.f) * e;
-          fE            = dd_fast_two_sum(1.f, -u);
-          fT            = dd_fast_two_sum(1.f, -(u + w));
-        }
-        G1 = dd_mul(G1, fE);
-        G2 = dd_mul(G2, fT);
-      }
+    const dd2 a  = dd2_mul(ai, q.s);
+    const dd2 v  = dd2_mul(a, dd2_mul(r2, ir));
+    const bool dx = a.h.x > 0.f && v.h.x < 50.f, dy = a.h.y > 0.f && v.h.y < 50.f;
+    // FP32 deficit (used where v >= 20)
+    const float2 e32 = make_float2(expf(-v.h.x), expf(-v.h.y));
+    const float2 u32 = pmul(pfma(v.h, pfma(v.h, p2(0.5f), p2(1.f)), p2(1.f)), e32);
+    const float2 w32 = pmul(pmul(pmul(pmul(v.h, v.h), v.h), p2(1.f / 6.f)), e32);
+    dd2 fE           = dd2_fast_two_sum(p2(1.f), pneg(u32));
+    dd2 fT           = dd2_fast_two_sum(p2(1.f), pneg(padd(u32, w32)));
+    const bool sx = MODE == 0 && v.h.x < 20.f, sy = MODE == 0 && v.h.y < 20.f;
+    if (sx || sy) {
+      const dd2 vc  = dd2_sel(sx, sy, v, zero);  // in range of the exponential's table
+      const dd2 e   = dd2_exp_neg(vc, eh, el);
+      const dd2 v2  = dd2_sqr(vc);
+      const dd2 u   = dd2_add(dd2_two_sum(p2(1.f), vc.h),
+                              {pmul(p2(0.5f), v2.h), pfma(p2(0.5f), v2.l, vc.l)});
+      const dd2 w   = dd2_mul(dd2_mul(v2, vc), {p2(1.f / 6.f), p2(DD_SIXTH_LO)});
+      const dd2 fEd = dd2_add(dd2{p2(1.f), p2(0.f)}, dd2_neg(dd2_mul(u, e)));
+      const dd2 fTd = dd2_add(fEd, dd2_neg(dd2_mul(w, e)));
+      fE = dd2_sel(sx, sy, fEd, fE);
+      fT = dd2_sel(sx, sy, fTd, fT);
     }
+    G1 = dd2_sel(dx, dy, dd2_mul(G1, fE), G1);
+    G2 = dd2_sel(dx, dy, dd2_mul(G2, fT), G2);
   }
-  const dd mx = {mu[0], mu[3]}, my = {mu[1], mu[4]}, mz = {mu[2], mu[5]};
-  const dd mr = dd_add(dd_add_lazy(dd_mul(mx, x), dd_mul(my, y)), dd_mul(mz, z));
-  const dd sg = dd_mul(mr, G2);
-  f[0] = dd_add_lazy(f[0], dd_neg(dd_add_lazy(dd_mul(mx, G1), dd_mul(sg, x))));
-  f[1] = dd_add_lazy(f[1], dd_neg(dd_add_lazy(dd_mul(my, G1), dd_mul(sg, y))));
-  f[2] = dd_add_lazy(f[2], dd_neg(dd_add_lazy(dd_mul(mz, G1), dd_mul(sg, z))));
+  const dd2 mr = dd2_add(dd2_add_lazy(dd2_mul(q.mx, x), dd2_mul(q.my, y)), dd2_mul(q.mz, z));
+  const dd2 sg = dd2_mul(mr, G2);
+  f[0] = dd2_add_lazy(f[0], dd2_neg(dd2_add_lazy(dd2_mul(q.mx, G1), dd2_mul(sg, x))));
+  f[1] = dd2_add_lazy(f[1], dd2_neg(dd2_add_lazy(dd2_mul(q.my, G1), dd2_mul(sg, y))));
+  f[2] = dd2_add_lazy(f[2], dd2_neg(dd2_add_lazy(dd2_mul(q.mz, G1), dd2_mul(sg, z))));
 }
 
+// One target per thread (its packed accumulators are already 4 x 3 floats),
+// sources staged in pairs: positions (high and low parts), s and the
+// double-float moments in seven float4 columns per source pair.
+constexpr int P2P_DD_PAIRS = 256;  // staged source pairs per tile (512 sources)
 template <bool DAMP>
 __global__ void __launch_bounds__(P2P_BLOCK)
-      k_p2p_dd(int n, const int* __restrict__ leaf_start, const int4* __restrict__ items,
-               const int* __restrict__ item_split, const int* __restrict__ p2p_src, PosArgs<float> pa,
-               const float2* __restrict__ src, const float2* __restrict__ etab,
-               double damping, double* __restrict__ Fnear) {
-  __shared__ SiteRec<float> s_rec[P2P_TILE];
-  __shared__ float s_mu[P2P_TILE * 6];
-  __shared__ float2 s_etab[DD_EXP_TAB];
+      k_p2p_dd2(int n, const int* __restrict__ leaf_start, const int4* __restrict__ items,
+                const int* __restrict__ item_split, const int* __restrict__ p2p_src,
+                PosArgs<float> pa, const float2* __restrict__ src,
+                const float2* __restrict__ etab, double damping, double* __restrict__ Fnear) {
+  constexpr int TILE = 2 * P2P_DD_PAIRS;
+  __shared__ float4 s_q[7][P2P_DD_PAIRS];
+  __shared__ float s_eh[DD_EXP_TAB], s_el[DD_EXP_TAB];
   __shared__ TilePlan s_plan;
-  __shared__ double s_red[P2P_BLOCK * 6];
+  __shared__ double s_red[P2P_BLOCK * 3];
 
-  for (int k = threadIdx.x; k < DD_EXP_TAB; k += P2P_BLOCK) s_etab[k] = etab[k];
+  for (int k = threadIdx.x; k < DD_EXP_TAB; k += P2P_BLOCK) {
+    const float2 e = etab[k];
+    s_eh[k] = e.x, s_el[k] = e.y;
+  }
   const int4 it = items[blockIdx.x];
   const int A = it.x, b0 = it.y, b1 = it.z, slot = it.w;
   const int sp = item_split[blockIdx.x];
   const int a0 = leaf_start[A], nA = leaf_start[A + 1] - a0;
   const dd dmp = dd_from(damping);
 
-  for (int tb = 0; tb < nA; tb += 2 * P2P_BLOCK) {
-    const int nT = min(2 * P2P_BLOCK, nA - tb);
-    const int T2 = (nT + 1) >> 1;
-    const int S  = P2P_BLOCK / T2;
-    const int t = threadIdx.x % T2, g = threadIdx.x / T2;
+  for (int tb = 0; tb < nA; tb += P2P_BLOCK) {
+    const int nT = min(P2P_BLOCK, nA - tb);
+    const int S  = P2P_BLOCK / nT;
+    const int t = threadIdx.x % nT, g = threadIdx.x / nT;
     const bool active = g < S;
-    const bool has1   = t + T2 < nT;
-    const SiteRec<float> me0 = pa.load(a0 + tb + t);
-    const SiteRec<float> me1 = pa.load(a0 + tb + (has1 ? t + T2 : t));
-    const dd ai0 = dd_mul(dmp, dd{me0.s, me0.ls}), ai1 = dd_mul(dmp, dd{me1.s, me1.ls});
-    dd f0[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-    dd f1[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    const SiteRec<float> me = pa.load(a0 + tb + t);
+    const dd2 tx = {p2(me.x), p2(me.lx)}, ty = {p2(me.y), p2(me.ly)}, tz = {p2(me.z), p2(me.lz)};
+    const dd ai1 = dd_mul(dmp, dd{me.s, me.ls});
+    const dd2 ai = {p2(ai1.h), p2(ai1.l)};
+    const dd2 zero = {p2(0.f), p2(0.f)};
+    dd2 f[3] = {zero, zero, zero};
     // phase 0: sources [b0, sp); phase 1: [sp, b1), every pair with v >= 27
-    // (never the double-float exponential)
     for (int ph = 0; ph < 2; ++ph) {
-    const int pend = ph == 0 ? sp : b1;
-    if (threadIdx.x == 0) s_plan.cur = ph == 0 ? b0 : sp, s_plan.coff = 0;
-    __syncthreads();
-    while (true) {
-      if (threadIdx.x < 32) plan_tile(s_plan, pend, p2p_src, leaf_start);
+      const int pend = ph == 0 ? sp : b1;
+      if (threadIdx.x == 0) s_plan.cur = ph == 0 ? b0 : sp, s_plan.coff = 0;
       __syncthreads();
-      const int np = s_plan.np;
-      if (np == 0) break;
-      const int total = s_plan.poff[np];
-      for (int q = threadIdx.x; q < total; q += P2P_BLOCK) {
-        const int j = tile_site(s_plan, q);
-        s_rec[q]    = pa.load(j);
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          const float2 m = src[3 * (size_t)j + c];
-          s_mu[q * 6 + c] = m.x, s_mu[q * 6 + 3 + c] = m.y;
-        }
-      }
-      __syncthreads();
-      if (active) {
-        auto sweep = [&](auto mode) {
-          constexpr int MD = decltype(mode)::value;
-          for (int jj = g; jj < total; jj += S) {
-            const SiteRec<float> sj = s_rec[jj];
-            const float* mu         = &s_mu[jj * 6];
-            dd_pair_m1<DAMP, MD>(me0, ai0, sj, mu, s_etab, f0);
-            dd_pair_m1<DAMP, MD>(me1, ai1, sj, mu, s_etab, f1);
+      while (true) {
+        if (threadIdx.x < 32) plan_tile<TILE>(s_plan, pend, p2p_src, leaf_start);
+        __syncthreads();
+        const int np = s_plan.np;
+        if (np == 0) break;
+        const int total  = s_plan.poff[np];
+        const int npairs = (total + 1) >> 1;
+        for (int q = threadIdx.x; q < npairs; q += P2P_BLOCK) {
+          const int j0 = tile_site(s_plan, 2 * q);
+          const SiteRec<float> r0 = pa.load(j0);
+          const float2 m0x = src[3 * (size_t)j0], m0y = src[3 * (size_t)j0 + 1],
+                       m0z = src[3 * (size_t)j0 + 2];
+          // an odd tile ends with a source of zero moment far from the leaf
+          SiteRec<float> r1 = r0;
+          r1.x += 1e4f, r1.s = 1.f, r1.ls = 0.f;
+          float2 m1x = make_float2(0.f, 0.f), m1y = m1x, m1z = m1x;
+          if (2 * q + 1 < total) {
+            const int j1 = tile_site(s_plan, 2 * q + 1);
+            r1  = pa.load(j1);
+            m1x = src[3 * (size_t)j1], m1y = src[3 * (size_t)j1 + 1], m1z = src[3 * (size_t)j1 + 2];
           }
-        };
-        if (!DAMP || ph == 0)
-          sweep(std::integral_constant<int, 0>{});
-        else
-          sweep(std::integral_constant<int, 1>{});
+          s_q[0][q] = make_float4(r0.x, r1.x, r0.y, r1.y);
+          s_q[1][q] = make_float4(r0.z, r1.z, r0.s, r1.s);
+          s_q[2][q] = make_float4(r0.lx, r1.lx, r0.ly, r1.ly);
+          s_q[3][q] = make_float4(r0.lz, r1.lz, r0.ls, r1.ls);
+          s_q[4][q] = make_float4(m0x.x, m1x.x, m0y.x, m1y.x);
+          s_q[5][q] = make_float4(m0z.x, m1z.x, m0x.y, m1x.y);
+          s_q[6][q] = make_float4(m0y.y, m1y.y, m0z.y, m1z.y);
+        }
+        __syncthreads();
+        if (active) {
+          auto sweep = [&](auto mode) {
+            constexpr int MD = decltype(mode)::value;
+#pragma unroll 1
+            for (int jj = g; jj < npairs; jj += S) {
+              const float4 A0 = s_q[0][jj], B0 = s_q[1][jj], C0 = s_q[2][jj], D0 = s_q[3][jj];
+              const float4 E0 = s_q[4][jj], F0 = s_q[5][jj], G0 = s_q[6][jj];
+              DDSrc2 q;
+              q.x  = {make_float2(A0.x, A0.y), make_float2(C0.x, C0.y)};
+              q.y  = {make_float2(A0.z, A0.w), make_float2(C0.z, C0.w)};
+              q.z  = {make_float2(B0.x, B0.y), make_float2(D0.x, D0.y)};
+              q.s  = {make_float2(B0.z, B0.w), make_float2(D0.z, D0.w)};
+              q.mx = {make_float2(E0.x, E0.y), make_float2(F0.z, F0.w)};
+              q.my = {make_float2(E0.z, E0.w), make_float2(G0.x, G0.y)};
+              q.mz = {make_float2(F0.x, F0.y), make_float2(G0.z, G0.w)};
+              dd2_pair_m1<DAMP, MD>(tx, ty, tz, ai, q, s_eh, s_el, f);
+            }
+          };
+          if (!DAMP || ph == 0)
+            sweep(std::integral_constant<int, 0>{});
+          else
+            sweep(std::integral_constant<int, 1>{});
+        }
+        __syncthreads();
       }
-      __syncthreads();
-    }
     }
     if (active) {
-      double* r = &s_red[(g * T2 + t) * 6];
-      r[0] = dd_to(f0[0]), r[1] = dd_to(f0[1]), r[2] = dd_to(f0[2]);
-      r[3] = dd_to(f1[0]), r[4] = dd_to(f1[1]), r[5] = dd_to(f1[2]);
+      double* r = &s_red[(g * nT + t) * 3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        // the two halves' sums, added in double-float, then widened
+        const dd h0 = {f[c].h.x, f[c].l.x}, h1 = {f[c].h.y, f[c].l.y};
+        r[c] = dd_to(dd_add(h0, h1));
+      }
     }
     __syncthreads();
-    if (threadIdx.x < T2) {
-      double f[6] = {0, 0, 0, 0, 0, 0};
+    if (threadIdx.x < nT) {
+      double o3[3] = {0, 0, 0};
       for (int gg = 0; gg < S; ++gg)
 #pragma unroll
-        for (int c = 0; c < 6; ++c) f[c] += s_red[(gg * T2 + threadIdx.x) * 6 + c];
+        for (int c = 0; c < 3; ++c) o3[c] += s_red[(gg * nT + threadIdx.x) * 3 + c];
       double* o = Fnear + (size_t)slot * 3 * n + 3 * (size_t)(a0 + tb + threadIdx.x);
-      o[0] = f[0], o[1] = f[1], o[2] = f[2];
-      if (threadIdx.x + T2 < nT) {
-        double* o1 = Fnear + (size_t)slot * 3 * n + 3 * (size_t)(a0 + tb + threadIdx.x + T2);
-        o1[0] = f[3], o1[1] = f[4], o1[2] = f[5];
-      }
+      o[0] = o3[0], o[1] = o3[1], o[2] = o3[2];
     }
     __syncthreads();
   }
@@ -1617,13 +1653,13 @@ static void launch_p2p_dd(const Geometry& g, bool damp, const double* src, doubl
   CG_LAUNCH();
   const int grid = (int)g.h_items.size();
   if (damp)
-    k_p2p_dd<true><<<grid, P2P_BLOCK, 0, s>>>(g.n, g.leaf_start.p, g.items.p, g.item_split.p, g.p2p_src.p,
-                                              pos_args<float>(g), w.dd_src.p, g.dd_exp.p,
-                                              damping, w.Fnear.p);
+    k_p2p_dd2<true><<<grid, P2P_BLOCK, 0, s>>>(g.n, g.leaf_start.p, g.items.p, g.item_split.p,
+                                               g.p2p_src.p, pos_args<float>(g), w.dd_src.p,
+                                               g.dd_exp.p, damping, w.Fnear.p);
   else
-    k_p2p_dd<false><<<grid, P2P_BLOCK, 0, s>>>(g.n, g.leaf_start.p, g.items.p, g.item_split.p, g.p2p_src.p,
-                                               pos_args<float>(g), w.dd_src.p, g.dd_exp.p,
-                                               damping, w.Fnear.p);
+    k_p2p_dd2<false><<<grid, P2P_BLOCK, 0, s>>>(g.n, g.leaf_start.p, g.items.p, g.item_split.p,
+                                                g.p2p_src.p, pos_args<float>(g), w.dd_src.p,
+                                                g.dd_exp.p, damping, w.Fnear.p);
   CG_LAUNCH();
 }
 
