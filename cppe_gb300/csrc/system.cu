@@ -193,8 +193,9 @@ System::~System() {
   if (stream) {
     cudaSetDevice(device);
     cudaStreamSynchronize(stream);
-    for (auto& e : inner_exec)
-      if (e) cudaGraphExecDestroy(e);
+    for (auto& row : inner_exec)
+      for (auto& e : row)
+        if (e) cudaGraphExecDestroy(e);
     if (side.s) cudaStreamSynchronize(side.s);
     side.destroy();
     cudaStreamDestroy(stream);
@@ -295,52 +296,67 @@ void System::init(int n_, const double* xyz, const double* alpha6, const int* ex
   setup_inexact(xyz, sd.data());
 }
 
-// Opening angle of the inexact inner operator.  At 30,000 water sites it
-// moves 42 % of the near-field pairs into M2L (FP32 apply 0.146 ms against
-// 0.212 ms) and differs from the operator by 2e-4 - 3e-4 relative.
-constexpr double INEXACT_THETA = 0.6;
+// Opening angles of the inexact inner operators.  At 30,000 water sites
+// (FP32 apply 0.212 ms with the operator's 0.5): 0.6 moves 42 % of the
+// near-field pairs into M2L (0.146 ms) and differs from the operator by
+// 2e-4 - 3e-4 relative; 0.8 moves 75 % (0.089 ms) at 1.2e-3 - 1.9e-3.
+constexpr double INEXACT_THETA[System::NINEXACT] = {0.6, 0.8};
 
 void System::setup_inexact(const double* xyz, const double* sd) {
-  have_inexact = false;
-  if (!geo.fmm || opt.precision != CPPE_GPU_MIXED || opt.theta >= INEXACT_THETA) return;
-  geo2.damping = geo.damping;
-  geo2.build(n, xyz, sd, excl_ptr_h.empty() ? nullptr : excl_ptr_h.data(),
-             excl_idx_h.empty() ? nullptr : excl_idx_h.data(), true, opt.tree_ncrit,
-             INEXACT_THETA, stream);
-  // the opening angle changes the lists, not the tree: same site order
-  if (geo2.layout.perm != geo.layout.perm) return;
-  // relative difference from the FP64 operator on a random vector and on a
-  // smooth one (the response of every site to one uniform field)
+  n_inexact = 0;
+  if (!geo.fmm || opt.precision != CPPE_GPU_MIXED) return;
   const size_t n3 = 3 * (size_t)n;
-  std::vector<double> v(n3), a64(n3), a32(n3);
-  double worst = 0.0;
+  // a random vector and a smooth one (the response of every site to one
+  // uniform field), and the operator on them in FP64 accuracy
+  std::vector<double> vin[2] = {std::vector<double>(n3), std::vector<double>(n3)};
+  std::vector<double> a64[2] = {std::vector<double>(n3), std::vector<double>(n3)};
   unsigned long long st = 0x9e3779b97f4a7c15ull;
-  for (int trial = 0; trial < 2; ++trial) {
-    for (size_t k = 0; k < n3; ++k) {
-      if (trial == 0) {
-        st ^= st << 13, st ^= st >> 7, st ^= st << 17;
-        v[k] = (double)(st >> 11) * (1.0 / 9007199254740992.0) - 0.5;
-      } else {
-        v[k] = (k % 3 == 0) ? 1.0 : (k % 3 == 1 ? 0.5 : 0.25);
-      }
-    }
-    CG_CUDA(cudaMemcpyAsync(tmp_in.p, v.data(), n3 * sizeof(double), cudaMemcpyHostToDevice,
-                            stream));
-    apply64(tmp_in.p, tmp_out.p, false, NEAR_DD);
-    CG_CUDA(cudaMemcpyAsync(a64.data(), tmp_out.p, n3 * sizeof(double), cudaMemcpyDeviceToHost,
-                            stream));
-    apply_inexact = true, have_inexact = true;
-    apply32_widen(tmp_in.p, tmp_out.p);
-    apply_inexact = false, have_inexact = false;
-    CG_CUDA(cudaMemcpyAsync(a32.data(), tmp_out.p, n3 * sizeof(double), cudaMemcpyDeviceToHost,
-                            stream));
-    CG_CUDA(cudaStreamSynchronize(stream));
-    double num = 0.0, den = 0.0;
-    for (size_t k = 0; k < n3; ++k) num += (a32[k] - a64[k]) * (a32[k] - a64[k]), den += a64[k] * a64[k];
-    if (den > 0.0) worst = std::max(worst, std::sqrt(num / den));
+  for (size_t k = 0; k < n3; ++k) {
+    st ^= st << 13, st ^= st >> 7, st ^= st << 17;
+    vin[0][k] = (double)(st >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+    vin[1][k] = (k % 3 == 0) ? 1.0 : (k % 3 == 1 ? 0.5 : 0.25);
   }
-  inexact_delta = 3.0 * worst;
-  have_inexact  = worst > 0.0 && inexact_delta < 1e-2;
+  for (int trial = 0; trial < 2; ++trial) {
+    CG_CUDA(cudaMemcpyAsync(tmp_in.p, vin[trial].data(), n3 * sizeof(double),
+                            cudaMemcpyHostToDevice, stream));
+    apply64(tmp_in.p, tmp_out.p, false, NEAR_DD);
+    CG_CUDA(cudaMemcpyAsync(a64[trial].data(), tmp_out.p, n3 * sizeof(double),
+                            cudaMemcpyDeviceToHost, stream));
+    CG_CUDA(cudaStreamSynchronize(stream));
+  }
+  for (int lev = 0; lev < NINEXACT; ++lev) {
+    if (opt.theta >= INEXACT_THETA[lev]) break;
+    Geometry& gx = geo_x[lev];
+    gx.damping   = geo.damping;
+    gx.build(n, xyz, sd, excl_ptr_h.empty() ? nullptr : excl_ptr_h.data(),
+             excl_idx_h.empty() ? nullptr : excl_idx_h.data(), true, opt.tree_ncrit,
+             INEXACT_THETA[lev], stream);
+    // the opening angle changes the lists, not the tree: same site order
+    if (gx.layout.perm != geo.layout.perm) break;
+    double worst = 0.0;
+    std::vector<double> out(n3);
+    for (int trial = 0; trial < 2; ++trial) {
+      CG_CUDA(cudaMemcpyAsync(tmp_in.p, vin[trial].data(), n3 * sizeof(double),
+                              cudaMemcpyHostToDevice, stream));
+      apply_level = lev;
+      n_inexact   = lev + 1;
+      apply32_widen(tmp_in.p, tmp_out.p);
+      apply_level = -1;
+      n_inexact   = lev;
+      CG_CUDA(cudaMemcpyAsync(out.data(), tmp_out.p, n3 * sizeof(double), cudaMemcpyDeviceToHost,
+                              stream));
+      CG_CUDA(cudaStreamSynchronize(stream));
+      double num = 0.0, den = 0.0;
+      for (size_t k = 0; k < n3; ++k) {
+        const double d = out[k] - a64[trial][k];
+        num += d * d, den += a64[trial][k] * a64[trial][k];
+      }
+      if (den > 0.0) worst = std::max(worst, std::sqrt(num / den));
+    }
+    inexact_delta[lev] = 3.0 * worst;
+    if (!(worst > 0.0 && inexact_delta[lev] < 1e-2)) break;
+    n_inexact = lev + 1;
+  }
 }
 
 void System::apply32_widen(const double* in, double* out) {
@@ -444,8 +460,9 @@ double System::autotune(int reps) {
   cudaEventDestroy(e1);
   CG_CUDA(cudaStreamSynchronize(stream));
   // captured inner loops hold the old schedule's buffers: rebuild on next use
-  for (auto& e : inner_exec)
-    if (e) cudaGraphExecDestroy(e), e = nullptr;
+  for (auto& row : inner_exec)
+    for (auto& e : row)
+      if (e) cudaGraphExecDestroy(e), e = nullptr;
   return best;
 }
 
@@ -460,8 +477,9 @@ void System::apply64(const double* in, double* out, bool with_dot, int near_mode
 
 void System::apply32(const float* in, float* out, bool with_dot) {
   ReduceSlots rs = slots(S_PAP);
-  const bool inexact = apply_inexact && have_inexact;
-  eval_field<float>(inexact ? geo2 : geo, ops.get(), inexact ? w32b : w32, 1, in,
+  const bool inexact = apply_level >= 0 && apply_level < n_inexact;
+  eval_field<float>(inexact ? geo_x[apply_level] : geo, ops.get(),
+                    inexact ? w32x[apply_level] : w32, 1, in,
                     opt.damp != 0, opt.damping_factor, FINISH_APPLY, ainv32.p, out, nullptr, 1.0,
                     with_dot ? &rs : nullptr, stream, nullptr, NEAR_FP64, &side);
 }
@@ -547,45 +565,52 @@ int System::solve_fp64(bool zero_guess, double* hist_out, int hist_cap, int* ite
 // which is also kept (S_RSTAGE); the iterations of the previous inner solve
 // are added to flags[3] (stage 0 clears it); flags[2] = 1 when the residual
 // already meets t, which makes the following k_cg_start start a finished solve.
-// With an inexact operator (delta > 0) the solve runs with the operator
-// down to S_TOL = max(threshold, switch point) and then with the inexact one
-// down to S_TOL2 = the threshold.  Switch points: where the inexact
-// operator's effect on the residual, ~delta ||r||, stays below 0.3 of the
+// With inexact operators (delta1, delta2 > 0; 0: absent) the solve runs with
+// the operator down to S_TOL = max(final threshold, S_SW1), then with
+// inexact operator 1 down to max(final, S_SW2), then with operator 2 down to
+// the final threshold S_TOLF.  Hand-over points: where each inexact
+// operator's effect on the residual, ~delta ||r||, stays below 0.15 of the
 // stage's target (stage 0: eta ||r0||), or, for the last stage, where
-// 1.5 delta ||r|| stays below 0.4 t (the residual is then formed from the
-// recursion, which carries that difference).
+// 1.5 delta ||r|| stays below 0.2 t (the residual is then formed from the
+// recursion, which carries those differences).
 __global__ void k_inner_stage(double* scal, int* flags, double t, double eta, int stage,
-                              double delta) {
+                              double delta1, double delta2) {
   const double rn  = scal[S_RNORM];
   const double tol = fmax(eta * rn, 0.5 * t);
-  double sw        = tol;
-  if (delta > 0.0) sw = stage == 0 ? 0.3 * eta * rn / delta : 0.4 * t / (1.5 * delta);
-  scal[S_TOL2]     = tol;
-  scal[S_TOL]      = fmax(tol, sw);
-  scal[S_RSTAGE]   = rn;
-  scal[S_RSWITCH]  = 0.0;
-  flags[3]         = stage == 0 ? 0 : flags[3] + flags[1];
-  flags[2]         = 0;
+  auto sw = [&](double d) {
+    if (d <= 0.0) return tol;
+    return fmax(tol, stage == 0 ? 0.15 * eta * rn / d : 0.2 * t / (1.5 * d));
+  };
+  const double sw1 = delta1 > 0.0 ? sw(delta1) : tol;
+  const double sw2 = delta2 > 0.0 ? fmin(sw1, sw(delta2)) : tol;
+  scal[S_TOLF]   = tol;
+  scal[S_SW1]    = sw1;
+  scal[S_SW2]    = sw2;
+  scal[S_TOL]    = sw1;
+  scal[S_RSTAGE] = rn;
+  scal[S_RSW1] = scal[S_RSW2] = 0.0;
+  flags[3]       = stage == 0 ? 0 : flags[3] + flags[1];
+  flags[2]       = 0;
   // flags[2] = 1 makes the following k_cg_start start a finished solve
   if (stage > 0 && rn < t) {
-    flags[2]     = 1;  // nothing left to do: neither part runs
-    scal[S_TOL2] = 1e300;
+    flags[2]     = 1;  // nothing left to do: no part runs
+    scal[S_TOLF] = scal[S_SW1] = scal[S_SW2] = 1e300;
   } else if (stage > 0 && rn < scal[S_TOL]) {
     flags[2] = 1;  // the operator's part has nothing to do
   }
 }
 
-// Hand-over from the operator to the inexact one inside an inner solve: the
-// solve continues (same direction and scalars) unless it has reached its
-// final threshold or the iteration limit.
-// flags[0] = 0 lets the stopping iteration's skipped direction update run
-// before the inexact part; 3 (no iteration ran) skips it, k_inner_resume
-// then clears it.
-__global__ void k_inner_switch(double* scal, int* flags) {
-  const double rn = scal[S_RNORM];
-  scal[S_RSWITCH] = rn;
-  scal[S_TOL]     = scal[S_TOL2];
-  if (flags[0] == 1 && rn >= scal[S_TOL2]) flags[0] = flags[1] > 0 ? 0 : 3;
+// Hand-over to inexact operator `level` (0, 1) inside an inner solve: the
+// solve continues (same direction and scalars) unless it has reached the
+// next part's threshold or the iteration limit.  flags[0] = 0 lets the
+// stopping iteration's skipped direction update run first; 3 (no iteration
+// ran yet) skips it, and k_inner_resume then clears it.
+__global__ void k_inner_switch(double* scal, int* flags, int level, int last) {
+  const double rn  = scal[S_RNORM];
+  const double nxt = last ? scal[S_TOLF] : scal[S_SW2];
+  scal[level == 0 ? S_RSW1 : S_RSW2] = rn;
+  scal[S_TOL]                        = nxt;
+  if (flags[0] == 1 && rn >= nxt) flags[0] = flags[1] > 0 ? 0 : 3;
 }
 __global__ void k_inner_resume(int* flags) {
   if (flags[0] == 3) flags[0] = 0;
@@ -619,8 +644,9 @@ void System::inner_iteration_fp32(int nb, int nb3) {
 // iteration.  Built once per system and learned/plain variant and operator,
 // after the buffers it uses exist.  Where graph construction is refused, the
 // iterations are launched from the host.
-bool System::inner_graph_ready(int nb, int nb3, bool inexact) {
-  const int v = (use_model ? 1 : 0) + (inexact && have_inexact ? 2 : 0);
+bool System::inner_graph_ready(int nb, int nb3, int level) {
+  const int v = use_model ? 1 : 0;
+  const int l = level >= 0 && level < n_inexact ? level + 1 : 0;
   // CPPE_GPU_GRAPHS=0 launches the iterations from the host instead (same
   // kernels; for profilers that do not descend into conditional graph nodes)
   static const bool graphs = [] {
@@ -628,7 +654,7 @@ bool System::inner_graph_ready(int nb, int nb3, bool inexact) {
     return !(e && e[0] == '0');
   }();
   if (!graphs) inner_graph_failed = true;
-  if (!inner_exec[v] && !inner_graph_failed) {
+  if (!inner_exec[v][l] && !inner_graph_failed) {
     cudaGraph_t g = nullptr;
     bool ok       = cudaGraphCreate(&g, 0) == cudaSuccess;
     cudaGraphConditionalHandle h{};
@@ -663,7 +689,7 @@ bool System::inner_graph_ready(int nb, int nb3, bool inexact) {
                                          cudaStreamCaptureModeThreadLocal) == cudaSuccess;
       if (ok) {
         const long long c0 = launch_counter();
-        apply_inexact      = inexact && have_inexact;
+        apply_level        = l - 1;
         try {
           inner_iteration_fp32(nb, nb3);
           k_while_running<<<1, 1, 0, stream>>>(h, flags.p);
@@ -671,32 +697,32 @@ bool System::inner_graph_ready(int nb, int nb3, bool inexact) {
         } catch (const Failure&) {
           ok = false;
         }
-        apply_inexact = false;
-        inner_body_launches[v] = launch_counter() - c0;
+        apply_level = -1;
+        inner_body_launches[v][l] = launch_counter() - c0;
         launch_counter()       = c0;
         cudaGraph_t captured   = nullptr;
         ok = (cudaStreamEndCapture(stream, &captured) == cudaSuccess) && ok;
       }
     }
-    if (ok) ok = cudaGraphInstantiate(&inner_exec[v], g, 0) == cudaSuccess;
+    if (ok) ok = cudaGraphInstantiate(&inner_exec[v][l], g, 0) == cudaSuccess;
     if (g) cudaGraphDestroy(g);
     if (!ok) {
       cudaGetLastError();  // clear the refusal; fall back to host-launched iterations
-      if (inner_exec[v]) cudaGraphExecDestroy(inner_exec[v]);
-      inner_exec[v]      = nullptr;
+      if (inner_exec[v][l]) cudaGraphExecDestroy(inner_exec[v][l]);
+      inner_exec[v][l]   = nullptr;
       inner_graph_failed = true;
     }
   }
-  return inner_exec[v] != nullptr;
+  return inner_exec[v][l] != nullptr;
 }
 
 void System::run_inner_fp32(int nb, int nb3) {
   const int v = use_model ? 1 : 0;
   if (inner_graph_ready(nb, nb3)) {
-    CG_CUDA(cudaGraphLaunch(inner_exec[v], stream));
+    CG_CUDA(cudaGraphLaunch(inner_exec[v][0], stream));
     CG_CUDA(cudaMemcpyAsync(h_flags, flags.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream));
     CG_CUDA(cudaStreamSynchronize(stream));
-    launch_counter() += inner_body_launches[v] * std::max(1, h_flags[1]);
+    launch_counter() += inner_body_launches[v][0] * h_flags[1] + 1;
     return;
   }
   Poller poll(stream, flags.p, h_flags);
@@ -751,28 +777,31 @@ int System::solve_mixed(bool zero_guess, double* hist_out, int hist_cap, int* it
   // the recursion -- queued at once with the decisions on the device and one
   // host synchronisation; the loop below takes over where it does not end
   // the solve (or where the inner iterations cannot run as a graph).
-  if (!zero_guess && inner_graph_ready(nb, nb3) &&
-      (!have_inexact || inner_graph_ready(nb, nb3, true))) {
+  bool graphs_ok = !zero_guess && inner_graph_ready(nb, nb3);
+  for (int lev = 0; lev < n_inexact && graphs_ok; ++lev) graphs_ok = inner_graph_ready(nb, nb3, lev);
+  if (graphs_ok) {
     const int v      = use_model ? 1 : 0;
-    const bool inex  = have_inexact;
-    const double dlt = inex ? inexact_delta : 0.0;
-    // one inner solve: the operator's graph, then (with an inexact operator)
-    // the hand-over and the inexact graph
+    const int nx     = n_inexact;
+    const double d1  = nx > 0 ? inexact_delta[0] : 0.0;
+    const double d2  = nx > 1 ? inexact_delta[1] : 0.0;
+    // one inner solve: the operator's graph, then for each inexact operator
+    // the hand-over and its graph
     auto inner = [&]() {
-      CG_CUDA(cudaGraphLaunch(inner_exec[v], stream));
-      if (!inex) return;
-      k_inner_switch<<<1, 1, 0, stream>>>(scal.p, flags.p);
-      CG_LAUNCH();
-      // the direction update the stopping iteration skipped (no-ops if the
-      // solve stays finished)
-      const float* zd = use_model ? learned_precond<float>(z32.p, r32.p, p32.p, false) : z32.p;
-      k_cg_dir<float><<<nb3, VB, 0, stream>>>(3 * n, zd, p32.p, scal.p, flags.p);
-      CG_LAUNCH();
-      k_inner_resume<<<1, 1, 0, stream>>>(flags.p);
-      CG_LAUNCH();
-      CG_CUDA(cudaGraphLaunch(inner_exec[v + 2], stream));
+      CG_CUDA(cudaGraphLaunch(inner_exec[v][0], stream));
+      for (int lev = 0; lev < nx; ++lev) {
+        k_inner_switch<<<1, 1, 0, stream>>>(scal.p, flags.p, lev, lev + 1 == nx);
+        CG_LAUNCH();
+        // the direction update the stopping iteration skipped (no-ops if the
+        // solve stays finished)
+        const float* zd = use_model ? learned_precond<float>(z32.p, r32.p, p32.p, false) : z32.p;
+        k_cg_dir<float><<<nb3, VB, 0, stream>>>(3 * n, zd, p32.p, scal.p, flags.p);
+        CG_LAUNCH();
+        k_inner_resume<<<1, 1, 0, stream>>>(flags.p);
+        CG_LAUNCH();
+        CG_CUDA(cudaGraphLaunch(inner_exec[v][lev + 1], stream));
+      }
     };
-    k_inner_stage<<<1, 1, 0, stream>>>(scal.p, flags.p, t, eta, 0, dlt);
+    k_inner_stage<<<1, 1, 0, stream>>>(scal.p, flags.p, t, eta, 0, d1, d2);
     CG_LAUNCH();
     inner();
     k_accumulate<<<nb3, VB, 0, stream>>>(n3, x.p, d32.p);
@@ -780,7 +809,7 @@ int System::solve_mixed(bool zero_guess, double* hist_out, int hist_cap, int* it
     apply64(x.p, Ap.p, false, NEAR_DD);
     k_residual<<<nb3, VB, 0, stream>>>(n3, F.p, Ap.p, r.p, slots(S_RED), scal.p);
     CG_LAUNCH();
-    k_inner_stage<<<1, 1, 0, stream>>>(scal.p, flags.p, t, eta, 1, dlt);
+    k_inner_stage<<<1, 1, 0, stream>>>(scal.p, flags.p, t, eta, 1, d1, d2);
     CG_LAUNCH();
     k_cg_start<float><<<nb, VB, 0, stream>>>(n, r.p, nullptr, alpha32.p, r32.p, z32.p, p32.p,
                                              slots(S_RED), scal.p, flags.p,
@@ -800,15 +829,16 @@ int System::solve_mixed(bool zero_guess, double* hist_out, int hist_cap, int* it
     total_inner += it1 + it2;
     last.fp32_applies += it1 + it2;
     last.fp64_applies++;
-    launch_counter() += inner_body_launches[v] * (it1 + it2) + (inex ? 8 : 2);
+    launch_counter() += inner_body_launches[v][0] * (it1 + it2) + 2 + 8 * nx;
     const double r1 = h_scal[S_RSTAGE];  // FP64 residual after the first inner solve
     outer_hist.push_back(r1);
     have_fp64_residual = true;
     have_inner_start   = false;
     // the residual from the recursion stands where its error bound is below
     // t / 10 (the inexact operator adds ~1.5 delta ||r|| from the hand-over on)
-    const double rsw = inex ? std::min(r1, h_scal[S_RSWITCH]) : 0.0;
-    const double bound = REC_ERR * r1 + 1.5 * dlt * rsw;
+    const double rsw1 = nx > 0 ? std::min(r1, h_scal[S_RSW1]) : 0.0;
+    const double rsw2 = nx > 1 ? std::min(r1, h_scal[S_RSW2]) : 0.0;
+    const double bound = REC_ERR * r1 + 1.5 * (d1 * rsw1 + d2 * rsw2);
     const bool recursion_ok = r1 < t || bound < 0.4 * t;
     if (recursion_ok && r1 >= t) rerr = bound;
     if (recursion_ok && h_scal[S_RNORM] + rerr < t) {

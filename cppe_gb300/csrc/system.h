@@ -19,11 +19,14 @@ enum Scalar {
   S_RNORM,    // ||r||_2 after the last update
   S_TOL,      // stopping threshold of the running loop
   S_RZOLD,    // r . z before the last update (flexible CG)
-  S_RSTAGE = 12,  // ||r|| at the set-up of the running inner solve
-  S_TOL2   = 13,  // threshold of the inner solve's inexact part
-  S_RSWITCH = 14, // ||r|| where the inner solve went over to the inexact operator
-  S_RED = 8,  // 4 slots receiving grid reductions
-  S_NSCAL = 16
+  S_RED = 8,       // 4 slots receiving grid reductions
+  S_RSTAGE = 12,   // ||r|| at the set-up of the running inner solve
+  S_TOLF   = 13,   // final threshold of the running inner solve
+  S_SW1    = 14,   // threshold handing over to inexact operator 1 (index 0)
+  S_SW2    = 15,   //                        ... to inexact operator 2
+  S_RSW1   = 16,   // ||r|| where the inner solve went over to inexact operator 1
+  S_RSW2   = 17,   //                                      ... inexact operator 2
+  S_NSCAL = 24
 };
 
 struct SolveStats {
@@ -41,16 +44,18 @@ struct System {
   std::unique_ptr<DeviceOps> ops;  // m = 1, p = order (FMM only)
   FieldWork<double> w64;
   FieldWork<float> w32;
-  // The inexact inner operator of the mixed solver: the same tree walked with
-  // a larger opening angle (fewer near pairs), in FP32; `inexact_delta`
-  // bounds its relative difference from the operator (measured at set-up,
-  // times 3).  Used by the inner solves once their residual is small enough
-  // that the difference stays below what they must resolve.
-  Geometry geo2;
-  FieldWork<float> w32b;
-  bool have_inexact    = false;
-  double inexact_delta = 0.0;
-  bool apply_inexact   = false;  // apply32 uses geo2 (set while capturing)
+  // Inexact inner operators of the mixed solver: the same tree walked with
+  // larger opening angles (fewer near pairs), in FP32; inexact_delta[k]
+  // bounds operator k's relative difference from the operator (measured at
+  // set-up, times 3).  The inner solves go over to them, in order, once their
+  // residual is small enough that the difference stays below what they must
+  // resolve.  n_inexact counts the operators in use (a prefix).
+  static constexpr int NINEXACT = 2;
+  Geometry geo_x[NINEXACT];
+  FieldWork<float> w32x[NINEXACT];
+  int n_inexact = 0;
+  double inexact_delta[NINEXACT] = {0.0, 0.0};
+  int apply_level = -1;  // apply32 uses geo_x[apply_level] (set while capturing)
   void setup_inexact(const double* xyz, const double* sd);
   // operator data in device order
   DBuf<double> ainv64, alpha64;  // 6 per site
@@ -113,10 +118,10 @@ struct System {
   void inner_iteration_fp32(int nb, int nb3);
   void run_inner_fp32(int nb, int nb3);
   // builds the inner loop's graph on first use; false where graphs are off
-  bool inner_graph_ready(int nb, int nb3, bool inexact = false);
-  // plain / learned body, with the operator / the inexact operator
-  cudaGraphExec_t inner_exec[4] = {nullptr, nullptr, nullptr, nullptr};
-  long long inner_body_launches[4] = {0, 0, 0, 0};
+  bool inner_graph_ready(int nb, int nb3, int level = -1);
+  // [plain / learned body][operator, inexact operator 1, 2]
+  cudaGraphExec_t inner_exec[2][1 + NINEXACT] = {};
+  long long inner_body_launches[2][1 + NINEXACT] = {};
   bool inner_graph_failed = false;
   int solve_device(const double* d_rhs, const double* d_guess, int make_guess, double* d_mu,
                    int* iters, double* hist_out, int hist_cap);
