@@ -275,20 +275,22 @@ __global__ void k_features(NearListView nl, const float* __restrict__ a6,
 }
 
 // Lane `sub` of eight: its share of sum_j T_ij in_j over site i's entries,
-// four entries per step with their loads issued together (the loop is
-// bound by the latency of the entry load and the dependent gather).
+// NB entries per step with their loads issued together (the loop is bound
+// by the latency of the entry load and the dependent gather; about 90
+// entries per site make two steps of eight).
 template <typename T>
 __device__ __forceinline__ void near_T_lane(const NearListView& nl, int i, int sub,
                                             const T* __restrict__ in, T& wx, T& wy, T& wz,
                                             const float4* __restrict__ in4 = nullptr) {
+  constexpr int NB = 8;
   const int k0 = nl.ptr[i] + sub, k1 = nl.ptr[i + 1];
-  for (int k = k0; k < k1; k += 32) {
-    int4 e[4];
+  for (int k = k0; k < k1; k += 8 * NB) {
+    int4 e[NB];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) e[u] = k + 8 * u < k1 ? nl.ent[k + 8 * u] : make_int4(-1, 0, 0, 0);
-    T v[4][3];
+    for (int u = 0; u < NB; ++u) e[u] = k + 8 * u < k1 ? nl.ent[k + 8 * u] : make_int4(-1, 0, 0, 0);
+    T v[NB][3];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < NB; ++u) {
       const int j = e[u].x;
       if (in4) {
         const float4 q = j >= 0 ? in4[j] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -300,7 +302,7 @@ __device__ __forceinline__ void near_T_lane(const NearListView& nl, int i, int s
       }
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < NB; ++u) {
       const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&e[u].y));
       const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&e[u].z));
       const float2 c = __half22float2(*reinterpret_cast<const __half2*>(&e[u].w));
@@ -450,7 +452,7 @@ void precond_near(const NearListView& nl, const T* a6, const float* c, const T* 
                   double* scal, const int* flags, cudaStream_t s, const float4* a4) {
   ReduceSlots rs{partials, ticket, scal + S_RED};
   const long threads = 8L * nl.n;
-  k_precond_near<T><<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
+  k_precond_near<T><<<(unsigned)((threads + 127) / 128), 128, 0, s>>>(
         nl, a6, c, a, r, r_old, zc, p, start ? 1 : 0, rs, scal, flags, a4);
   CG_LAUNCH();
 }

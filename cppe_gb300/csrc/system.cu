@@ -282,8 +282,8 @@ void System::init(int n_, const double* xyz, const double* alpha6, const int* ex
   scal.alloc(S_NSCAL);
   scal.zero(stream);
   // partial sums of the grid reductions: the widest grid is the learned
-  // preconditioner's (eight lanes per site, 256-thread blocks, two sums)
-  const size_t maxblocks = std::max<size_t>(1024, (8 * (size_t)n + 255) / 256 + 1);
+  // preconditioner's (eight lanes per site, 128-thread blocks, two sums)
+  const size_t maxblocks = std::max<size_t>(1024, (8 * (size_t)n + 127) / 128 + 1);
   partials.alloc(4 * maxblocks);
   hist.alloc(std::max(1, o.maxiter) + 64);
   ticket.alloc(1);
@@ -1032,7 +1032,7 @@ void System::learned_start() {
 template <typename T>
 T* System::learned_precond(T* zv, const T* rv, T* pv, bool start) {
   const NearListView nl = view(*near);
-  if ((8 * (size_t)n + 255) / 256 * 2 > partials.n)
+  if ((8 * (size_t)n + 127) / 128 * 2 > partials.n)
     fail(CPPE_GPU_INVALID_ARG, "reduction buffer too small for the learned preconditioner");
   if constexpr (std::is_same<T, double>::value) {
     precond_near<double>(nl, alpha64.p, lf_c.p, zv, rv, lf_rold64.p, lf_w64.p, pv, start,
