@@ -382,8 +382,12 @@ __global__ void k_precond_near(NearListView nl, const T* __restrict__ a6,
                                double* scal, const int* flags, const float4* __restrict__ a4) {
   __shared__ double sh[64];
   if (!start && flags[0]) return;
-  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = gid >> 3, sub = gid & 7;
+  T v[2] = {T(0), T(0)};  // (FP32 products for the FP32 solve: see block_sum)
+  // a grid of a few blocks per SM striding over the sites: fewer partial
+  // sums (and tickets) for the grid reduction than a block per 16 sites
+  const int per_block = blockDim.x >> 3;
+  for (int base = blockIdx.x * per_block; base < nl.n; base += gridDim.x * per_block) {
+  const int i = base + (threadIdx.x >> 3), sub = threadIdx.x & 7;
   T wx = 0, wy = 0, wz = 0;
   if (i < nl.n) {
     near_T_lane<T>(nl, i, sub, a, wx, wy, wz, a4);
@@ -394,7 +398,6 @@ __global__ void k_precond_near(NearListView nl, const T* __restrict__ a6,
     wy += __shfl_down_sync(0xffffffffu, wy, o, 8);
     wz += __shfl_down_sync(0xffffffffu, wz, o, 8);
   }
-  T v[2] = {T(0), T(0)};  // (FP32 products for the FP32 solve: see block_sum)
   if (i < nl.n && sub == 0) {
     const T* al = a6 + 6 * (size_t)i;
     const T c   = (T)cw[i];
@@ -409,6 +412,7 @@ __global__ void k_precond_near(NearListView nl, const T* __restrict__ a6,
       v[0] += zk * r[k];
       if (!start) v[1] += zk * r_old[k];
     }
+  }
   }
   if (grid_sum_last<2>(v, sh, rs.partials, rs.ticket, rs.out)) {
     if (!start) scal[S_BETA] = (rs.out[0] - rs.out[1]) / scal[S_RZOLD];
@@ -446,13 +450,14 @@ void learned_guess(int n, const float* Y, const float* v1, const float* v2, cons
   CG_LAUNCH();
 }
 
+constexpr long PRECOND_BLOCKS = 4 * 152;  // 4 per SM of a GB300 (grid stride beyond)
 template <typename T>
 void precond_near(const NearListView& nl, const T* a6, const float* c, const T* a, const T* r,
                   const T* r_old, T* zc, T* p, bool start, double* partials, unsigned* ticket,
                   double* scal, const int* flags, cudaStream_t s, const float4* a4) {
   ReduceSlots rs{partials, ticket, scal + S_RED};
-  const long threads = 8L * nl.n;
-  k_precond_near<T><<<(unsigned)((threads + 127) / 128), 128, 0, s>>>(
+  const long blocks = std::min<long>((8L * nl.n + 127) / 128, PRECOND_BLOCKS);
+  k_precond_near<T><<<(unsigned)std::max(1L, blocks), 128, 0, s>>>(
         nl, a6, c, a, r, r_old, zc, p, start ? 1 : 0, rs, scal, flags, a4);
   CG_LAUNCH();
 }
