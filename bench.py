@@ -258,6 +258,9 @@ def batched_section(dev, steps, flush):
     batch = capi.Batch(boxes, nrhs, direct_below=4000, precision=capi.MIXED, damp=True,
                        order=5, ncrit=64, theta=0.5, thresh=1e-8, device=dev)
     setup = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    tuned_ms = batch.autotune(2)
+    tune = time.perf_counter() - t0
     d_rhs = torch.tensor(flat, dtype=torch.float64, device=f"cuda:{dev}")
     d_mu = torch.zeros_like(d_rhs)
     st = torch.cuda.ExternalStream(batch.stream())
@@ -301,7 +304,8 @@ def batched_section(dev, steps, flush):
             "plain_fp64_note": "first RHS of each snapshot solved and timed one at a time, x8",
             "speedup_vs_plain_fp64": plain / t_batch,
             "fp32_applies": bst["fp32_applies"], "fp64_applies": bst["fp64_applies"],
-            "max_fp64_residual": worst, "setup_s": setup}
+            "max_fp64_residual": worst, "setup_s": setup, "autotune_s": tune,
+            "fp32_apply_ms": tuned_ms}
 
 
 def large_section(cfg, dev, flush, model_path=None, zero_guess=True):

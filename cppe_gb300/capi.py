@@ -85,6 +85,7 @@ def lib():
         l.cppe_gpu_fma_peak.argtypes = [ctypes.c_int, ctypes.c_int, D]
         l.cppe_gpu_batch_stats.argtypes = [ctypes.c_void_p, I, I, D]
         l.cppe_gpu_batch_stream.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]
+        l.cppe_gpu_batch_autotune.argtypes = [ctypes.c_void_p, ctypes.c_int, D]
         F = ctypes.POINTER(ctypes.c_float)
         l.cppe_gpu_mlp_nparams.argtypes = [I]
         l.cppe_gpu_mlp_create.argtypes = [ctypes.c_int, ctypes.c_uint,
@@ -246,6 +247,13 @@ class Batch:
         s = ctypes.c_void_p()
         check(lib().cppe_gpu_batch_stream(self.h, ctypes.byref(s)))
         return s.value or 0
+
+    def autotune(self, reps=3):
+        """Keeps the fastest near-field / M2L schedule and far-field stream
+        priority for this batch's FP32 operator; returns its apply time (ms)."""
+        ms = ctypes.c_double(0)
+        check(lib().cppe_gpu_batch_autotune(self.h, reps, ctypes.byref(ms)))
+        return ms.value
 
 
 def launch_count():

@@ -726,6 +726,15 @@ int cppe_gpu_batch_stats(cppe_gpu_batch* bh, int* fp64_applies, int* fp32_applie
   });
 }
 
+int cppe_gpu_batch_autotune(cppe_gpu_batch* bh, int reps, double* best_ms) {
+  return guard([&]() -> int {
+    need(bh && reps > 0, "null argument");
+    const double ms = bh->b.autotune(reps);
+    if (best_ms) *best_ms = ms;
+    return CPPE_GPU_OK;
+  });
+}
+
 int cppe_gpu_batch_stream(cppe_gpu_batch* bh, void** stream) {
   return guard([&]() -> int {
     need(bh && stream, "null argument");

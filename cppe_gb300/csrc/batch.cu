@@ -7,6 +7,7 @@
 // for every segment at once; a converged segment stops updating).
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <map>
 #include <numeric>
 
@@ -92,6 +93,7 @@ void Geometry::combine(const std::vector<const Geometry*>& parts, int copies, Ge
     for (int a = 0; a < P.nleaves; ++a) {
       const int k = cmap[s][P.leaf_cell[a]];
       L.leaf_cell.push_back(k);
+      out.h_leaf_seg.push_back(s);
       L.leaf_of_cell[k] = leaf0 + a;
       L.leaf_start.push_back(site0 + P.leaf_start[a + 1]);
       for (int q = P.p2p_ptr[a]; q < P.p2p_ptr[a + 1]; ++q) L.p2p_src.push_back(leaf0 + P.p2p_src[q]);
@@ -304,6 +306,8 @@ BatchSystem::~BatchSystem() {
     side.destroy();
     cudaStreamDestroy(stream);
   }
+  for (auto& e : pcg_exec)
+    if (e) cudaGraphExecDestroy(e);
   if (h_active) cudaFreeHost(h_active);
 }
 
@@ -405,48 +409,168 @@ void BatchSystem::init(int nsys, const int* site_offset, const double* xyz, cons
 }
 
 template <typename T>
-void BatchSystem::apply_seg(const T* in, T* out, int near_mode) {
+void BatchSystem::apply_seg(const T* in, T* out, int near_mode, bool skip_done) {
   ReduceSlots rs{nullptr, nullptr, nullptr};
   rs.site_values = site_a.p;
   FieldWork<T>& w = work<T>();
   const T* ainv   = std::is_same<T, double>::value ? (const T*)ainv64.p : (const T*)ainv32.p;
   eval_field<T>(geo, ops.get(), w, 1, in, opt.damp != 0, opt.damping_factor, FINISH_APPLY, ainv,
-                out, nullptr, 1.0, &rs, stream, nullptr, near_mode, &side);
+                out, nullptr, 1.0, &rs, stream, nullptr, near_mode, &side,
+                skip_done ? done.p : nullptr);
   k_seg_sum<<<nseg, BB, 0, stream>>>(seg_start.p, site_a.p, nullptr, seg_pap.p, nullptr);
   CG_LAUNCH();
 }
 
+// Sets the first condition of the batched loop: some segment still running.
+__global__ void k_bcg_any(cudaGraphConditionalHandle h, int nseg, const int* __restrict__ done,
+                          int* __restrict__ active) {
+  int any = 0;
+  for (int g = threadIdx.x; g < nseg; g += blockDim.x) any |= done[g] == 0;
+  any = __syncthreads_or(any);
+  if (threadIdx.x == 0) {
+    *active = 0;
+    cudaGraphSetConditional(h, any ? 1u : 0u);
+  }
+}
+
+// Continues the batched loop while k_bcg_finalize counted a running segment.
+__global__ void k_bcg_continue(cudaGraphConditionalHandle h, int* __restrict__ active) {
+  const int a = *active;
+  *active     = 0;
+  cudaGraphSetConditional(h, a > 0 ? 1u : 0u);
+}
+
+// One PCG iteration over every segment; kernels of converged segments are
+// no-ops.  Host-launched, the running-segment counter is cleared here; in the
+// graph k_bcg_any / k_bcg_continue clear it.
 template <typename T>
-int BatchSystem::run_pcg(T* xv, T* rv, T* zv, T* pv, T* Apv, const T* a6, int maxiter) {
-  // (r, z, p, per-segment rz / rnorm / done set by the caller's start step)
+void BatchSystem::pcg_iteration(T* xv, T* rv, T* zv, T* pv, T* Apv, const T* a6, int maxiter,
+                                bool graph) {
   const int nb = (n + BB - 1) / BB, gb = (nseg + 127) / 128;
-  int k = 0;
-  for (; k < maxiter; ++k) {
-    apply_seg<T>(pv, Apv);
-    if (std::is_same<T, double>::value)
-      stats.fp64_applies++;
-    else
-      stats.fp32_applies++;
-    k_bcg_update<T><<<nb, BB, 0, stream>>>(n, site_seg.p, pv, Apv, a6, xv, rv, zv, seg_rz.p,
-                                           seg_pap.p, done.p, site_a.p, site_b.p);
-    CG_LAUNCH();
-    k_seg_sum<<<nseg, BB, 0, stream>>>(seg_start.p, site_a.p, site_b.p, seg_rr.p, seg_rznew.p);
-    CG_LAUNCH();
-    CG_CUDA(cudaMemsetAsync(active.p, 0, sizeof(int), stream));
-    k_bcg_finalize<<<gb, 128, 0, stream>>>(nseg, seg_rr.p, seg_rznew.p, seg_rz.p, seg_beta.p,
-                                           seg_rnorm.p, done.p, iters.p, seg_tol.p, maxiter,
-                                           active.p);
-    CG_LAUNCH();
-    k_bcg_dir<T><<<nb, BB, 0, stream>>>(n, site_seg.p, zv, pv, seg_beta.p, done.p);
-    CG_LAUNCH();
-    CG_CUDA(cudaMemcpyAsync(h_active, active.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
-    CG_CUDA(cudaStreamSynchronize(stream));
-    if (*h_active == 0) {
-      ++k;
-      break;
+  // the near field of finished segments is skipped: their p, Ap and scalars
+  // are no longer read
+  apply_seg<T>(pv, Apv, NEAR_FP64, true);
+  k_bcg_update<T><<<nb, BB, 0, stream>>>(n, site_seg.p, pv, Apv, a6, xv, rv, zv, seg_rz.p,
+                                         seg_pap.p, done.p, site_a.p, site_b.p);
+  CG_LAUNCH();
+  k_seg_sum<<<nseg, BB, 0, stream>>>(seg_start.p, site_a.p, site_b.p, seg_rr.p, seg_rznew.p);
+  CG_LAUNCH();
+  if (!graph) CG_CUDA(cudaMemsetAsync(active.p, 0, sizeof(int), stream));
+  k_bcg_finalize<<<gb, 128, 0, stream>>>(nseg, seg_rr.p, seg_rznew.p, seg_rz.p, seg_beta.p,
+                                         seg_rnorm.p, done.p, iters.p, seg_tol.p, maxiter,
+                                         active.p);
+  CG_LAUNCH();
+  k_bcg_dir<T><<<nb, BB, 0, stream>>>(n, site_seg.p, zv, pv, seg_beta.p, done.p);
+  CG_LAUNCH();
+}
+
+template <typename T>
+bool BatchSystem::pcg_graph_ready(T* xv, T* rv, T* zv, T* pv, T* Apv, const T* a6, int maxiter) {
+  const int v = std::is_same<T, double>::value ? 0 : 1;
+  static const bool graphs = [] {
+    const char* e = std::getenv("CPPE_GPU_GRAPHS");
+    return !(e && e[0] == '0');
+  }();
+  if (!graphs) pcg_graph_failed = true;
+  if (!pcg_exec[v] && !pcg_graph_failed) {
+    cudaGraph_t g = nullptr;
+    bool ok       = cudaGraphCreate(&g, 0) == cudaSuccess;
+    cudaGraphConditionalHandle h{};
+    ok = ok && cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault) ==
+                     cudaSuccess;
+    cudaGraphNode_t pre{}, node{};
+    cudaGraphNodeParams np{};
+    if (ok) {
+      ok = cudaStreamBeginCaptureToGraph(stream, g, nullptr, nullptr, 0,
+                                         cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+      if (ok) {
+        k_bcg_any<<<1, 256, 0, stream>>>(h, nseg, done.p, active.p);
+        ok = cudaGetLastError() == cudaSuccess;
+        cudaGraph_t captured = nullptr;
+        ok = (cudaStreamEndCapture(stream, &captured) == cudaSuccess) && ok;
+      }
+      size_t nn = 1;
+      ok = ok && cudaGraphGetNodes(g, &pre, &nn) == cudaSuccess && nn == 1;
+    }
+    if (ok) {
+      np.type               = cudaGraphNodeTypeConditional;
+      np.conditional.handle = h;
+      np.conditional.type   = cudaGraphCondTypeWhile;
+      np.conditional.size   = 1;
+      ok = cudaGraphAddNode(&node, g, &pre, nullptr, 1, &np) == cudaSuccess;
+    }
+    if (ok) {
+      cudaGraph_t body = np.conditional.phGraph_out[0];
+      ok = cudaStreamBeginCaptureToGraph(stream, body, nullptr, nullptr, 0,
+                                         cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+      if (ok) {
+        const long long c0 = launch_counter();
+        try {
+          pcg_iteration<T>(xv, rv, zv, pv, Apv, a6, maxiter, true);
+          k_bcg_continue<<<1, 1, 0, stream>>>(h, active.p);
+          CG_LAUNCH();
+        } catch (const Failure&) {
+          ok = false;
+        }
+        pcg_body_launches[v] = launch_counter() - c0;
+        launch_counter()     = c0;
+        cudaGraph_t captured = nullptr;
+        ok = (cudaStreamEndCapture(stream, &captured) == cudaSuccess) && ok;
+      }
+    }
+    if (ok) ok = cudaGraphInstantiate(&pcg_exec[v], g, 0) == cudaSuccess;
+    if (g) cudaGraphDestroy(g);
+    if (!ok) {
+      cudaGetLastError();  // clear the refusal; fall back to host-launched iterations
+      if (pcg_exec[v]) cudaGraphExecDestroy(pcg_exec[v]);
+      pcg_exec[v]      = nullptr;
+      pcg_graph_failed = true;
     }
   }
+  return pcg_exec[v] != nullptr;
+}
+
+template <typename T>
+int BatchSystem::run_pcg(T* xv, T* rv, T* zv, T* pv, T* Apv, const T* a6, int maxiter) {
+  // (r, z, p, per-segment rz / rnorm / done / iters set by the caller's start step)
+  const int v = std::is_same<T, double>::value ? 0 : 1;
+  int k       = 0;
+  if (pcg_graph_ready<T>(xv, rv, zv, pv, Apv, a6, maxiter)) {
+    // the whole loop on the device; iterations = the largest segment count
+    CG_CUDA(cudaGraphLaunch(pcg_exec[v], stream));
+    h_iters.resize(nseg);
+    CG_CUDA(cudaMemcpyAsync(h_iters.data(), iters.p, nseg * sizeof(int), cudaMemcpyDeviceToHost,
+                            stream));
+    CG_CUDA(cudaStreamSynchronize(stream));
+    k = *std::max_element(h_iters.begin(), h_iters.end());
+    launch_counter() += pcg_body_launches[v] * k + 1;
+  } else {
+    for (; k < maxiter; ++k) {
+      pcg_iteration<T>(xv, rv, zv, pv, Apv, a6, maxiter, false);
+      CG_CUDA(cudaMemcpyAsync(h_active, active.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+      CG_CUDA(cudaStreamSynchronize(stream));
+      if (*h_active == 0) {
+        ++k;
+        break;
+      }
+    }
+  }
+  if (std::is_same<T, double>::value)
+    stats.fp64_applies += k;
+  else
+    stats.fp32_applies += k;
   return k;
+}
+
+double BatchSystem::autotune(int reps) {
+  CG_CUDA(cudaSetDevice(device));
+  CG_CUDA(cudaMemsetAsync(p32.p, 0, sizeof(float) * 3 * (size_t)n, stream));
+  const double best = autotune_schedule(geo, side, stream, reps,
+                                        [&] { apply_seg<float>(p32.p, Ap32.p); });
+  // captured loops hold the old schedule's buffers: rebuild on next use
+  for (auto& e : pcg_exec)
+    if (e) cudaGraphExecDestroy(e), e = nullptr;
+  return best;
 }
 
 void BatchSystem::seg_norms_from_site_b() {

@@ -45,11 +45,31 @@ struct BatchSystem {
     else
       return w32;
   }
+  // the operator over every segment; skip_done leaves the near field of the
+  // segments flagged in `done` out (their output is then not meaningful)
   template <typename T>
-  void apply_seg(const T* in, T* out, int near_mode = NEAR_FP64);
+  void apply_seg(const T* in, T* out, int near_mode = NEAR_FP64, bool skip_done = false);
+  // PCG iterations over all segments until each has converged or reached
+  // maxiter; returns the number of iterations run (operator applications)
   template <typename T>
   int run_pcg(T* x, T* r, T* z, T* p, T* Ap, const T* a6, int maxiter);
+  template <typename T>
+  void pcg_iteration(T* x, T* r, T* z, T* p, T* Ap, const T* a6, int maxiter, bool graph);
   void seg_norms_from_site_b();
+  // The iterations as one CUDA graph with a conditional while node, per
+  // precision ([FP64, FP32]); built on first use, dropped when the schedule
+  // changes.  CPPE_GPU_GRAPHS=0 or a refused construction launches the
+  // iterations from the host.
+  template <typename T>
+  bool pcg_graph_ready(T* x, T* r, T* z, T* p, T* Ap, const T* a6, int maxiter);
+  cudaGraphExec_t pcg_exec[2] = {};
+  long long pcg_body_launches[2] = {};
+  bool pcg_graph_failed = false;
+  std::vector<int> h_iters;
+  // Times the FP32 operator under several near-field work-item sizes, M2L
+  // chunk sizes and far-field stream priorities and keeps the fastest;
+  // returns its apply time (ms).
+  double autotune(int reps);
 };
 
 }  // namespace cg

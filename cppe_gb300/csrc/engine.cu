@@ -397,6 +397,7 @@ void Geometry::upload(cudaStream_t s) {
   items.upload(h_items, s);
   item_split.upload(h_item_split, s);
   leaf_nslot.upload(h_leaf_nslot, s);
+  if (!h_leaf_seg.empty()) leaf_seg.upload(h_leaf_seg, s);
   if (!h_p2m_tasks.empty()) p2m_tasks.upload(h_p2m_tasks, s);
   task_leaf.upload(h_task_leaf, s);
   if (!h_m2l_chunks.empty()) m2l_chunks.upload(h_m2l_chunks, s);
@@ -594,7 +595,8 @@ template <typename T, int M, bool DAMP, bool FAST>
 __global__ void __launch_bounds__(P2P_BLOCK)
       k_p2p(int n, const int* __restrict__ leaf_start, const int4* __restrict__ items,
             const int* __restrict__ p2p_src, PosArgs<T> pa, const T* __restrict__ src,
-            T damping, T* __restrict__ Fnear) {
+            T damping, T* __restrict__ Fnear, const int* __restrict__ leaf_seg,
+            const int* __restrict__ seg_done) {
   constexpr int NS = ncomp(M);
   __shared__ SiteRec<T> s_rec[P2P_TILE];
   __shared__ T s_S[P2P_TILE * NS];
@@ -603,6 +605,7 @@ __global__ void __launch_bounds__(P2P_BLOCK)
 
   const int4 it = items[blockIdx.x];
   const int A = it.x, b0 = it.y, b1 = it.z, slot = it.w;
+  if (seg_done && seg_done[leaf_seg[A]]) return;  // finished segment of a batch
   const int a0 = leaf_start[A], nA = leaf_start[A + 1] - a0;
 
   for (int tb = 0; tb < nA; tb += 2 * P2P_BLOCK) {
@@ -767,7 +770,8 @@ __global__ void __launch_bounds__(P2P_BLOCK)
       k_p2p32_m1(int n, const int* __restrict__ leaf_start, const int4* __restrict__ items,
                  const int* __restrict__ item_split, const int* __restrict__ p2p_src, const float4* __restrict__ hi,
                  const float4* __restrict__ lo, const float* __restrict__ src, float damping,
-                 float* __restrict__ Fnear) {
+                 float* __restrict__ Fnear, const int* __restrict__ leaf_seg,
+                 const int* __restrict__ seg_done) {
   constexpr int TILE = 2 * P2P32_PAIRS;
   __shared__ float4 s_xy[P2P32_PAIRS];   // x_j, x_j+1, y_j, y_j+1
   __shared__ float4 s_zs[P2P32_PAIRS];   // z_j, z_j+1, s_j, s_j+1
@@ -778,6 +782,7 @@ __global__ void __launch_bounds__(P2P_BLOCK)
 
   const int4 it = items[blockIdx.x];
   const int A = it.x, b0 = it.y, b1 = it.z, slot = it.w;
+  if (seg_done && seg_done[leaf_seg[A]]) return;  // finished segment of a batch
   const int sp = item_split[blockIdx.x];
   const int a0 = leaf_start[A], nA = leaf_start[A + 1] - a0;
   const float4 oh = hi[a0], ol = lo[a0];
@@ -1579,21 +1584,26 @@ CellPos<float> cell_pos<float>(const Geometry& g) {
 
 template <typename T, int M>
 static void launch_p2p(const Geometry& g, bool damp, bool fast, const T* src, T damping,
-                       T* Fnear, cudaStream_t s) {
+                       T* Fnear, cudaStream_t s, const int* seg_done) {
   const int grid = (int)g.h_items.size();
+  const int* lseg = seg_done ? g.leaf_seg.p : nullptr;
+  if (seg_done && !lseg) fail(CPPE_GPU_INVALID_ARG, "segment mask without segments");
   if constexpr (std::is_same<T, float>::value && M == 1) {
     if (damp)
       k_p2p32_m1<true><<<grid, P2P_BLOCK, 0, s>>>(
-            g.n, g.leaf_start.p, g.items.p, g.item_split.p, g.p2p_src.p, g.hi32.p, g.lo32.p, src, damping, Fnear);
+            g.n, g.leaf_start.p, g.items.p, g.item_split.p, g.p2p_src.p, g.hi32.p, g.lo32.p, src,
+            damping, Fnear, lseg, seg_done);
     else
       k_p2p32_m1<false><<<grid, P2P_BLOCK, 0, s>>>(
-            g.n, g.leaf_start.p, g.items.p, g.item_split.p, g.p2p_src.p, g.hi32.p, g.lo32.p, src, damping, Fnear);
+            g.n, g.leaf_start.p, g.items.p, g.item_split.p, g.p2p_src.p, g.hi32.p, g.lo32.p, src,
+            damping, Fnear, lseg, seg_done);
     CG_LAUNCH();
     return;
   }
 #define CG_P2P(D, F)                                                                            \
   k_p2p<T, M, D, F><<<grid, P2P_BLOCK, 0, s>>>(g.n, g.leaf_start.p, g.items.p, g.p2p_src.p, \
-                                               pos_args<T>(g), src, damping, Fnear)
+                                               pos_args<T>(g), src, damping, Fnear, lseg,   \
+                                               seg_done)
   if (damp && fast)
     CG_P2P(true, true);
   else if (damp)
@@ -1667,7 +1677,8 @@ template <typename T>
 void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m, const T* src,
                 bool damp, double damping, FinishMode mode, const T* ainv6, T* out,
                 double* out64, double sign, const ReduceSlots* dot, cudaStream_t s,
-                const PhaseEvents* pe, int near_mode, const SideStream* side) {
+                const PhaseEvents* pe, int near_mode, const SideStream* side,
+                const int* seg_done) {
   const TreeView tv = g.view();
   OpsView ov{};
   int fixedP  = 0;  // order of the straight-line expansion operators in use (0: tables)
@@ -1774,9 +1785,9 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
       done = true;
     }
   }
-  if (!done && m == 0) launch_p2p<T, 0>(g, damp, fast, src, dampT, w.Fnear.p, s);
-  if (!done && m == 1) launch_p2p<T, 1>(g, damp, fast, src, dampT, w.Fnear.p, s);
-  if (!done && m == 2) launch_p2p<T, 2>(g, damp, fast, src, dampT, w.Fnear.p, s);
+  if (!done && m == 0) launch_p2p<T, 0>(g, damp, fast, src, dampT, w.Fnear.p, s, seg_done);
+  if (!done && m == 1) launch_p2p<T, 1>(g, damp, fast, src, dampT, w.Fnear.p, s, seg_done);
+  if (!done && m == 2) launch_p2p<T, 2>(g, damp, fast, src, dampT, w.Fnear.p, s, seg_done);
   mark(4);
   if (fs != s) CG_CUDA(cudaStreamWaitEvent(s, side->join, 0));
 
@@ -1813,11 +1824,11 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
 template void eval_field<double>(const Geometry&, const DeviceOps*, FieldWork<double>&, int,
                                  const double*, bool, double, FinishMode, const double*,
                                  double*, double*, double, const ReduceSlots*, cudaStream_t,
-                                 const PhaseEvents*, int, const SideStream*);
+                                 const PhaseEvents*, int, const SideStream*, const int*);
 template void eval_field<float>(const Geometry&, const DeviceOps*, FieldWork<float>&, int,
                                 const float*, bool, double, FinishMode, const float*, float*,
                                 double*, double, const ReduceSlots*, cudaStream_t,
-                                const PhaseEvents*, int, const SideStream*);
+                                const PhaseEvents*, int, const SideStream*, const int*);
 
 // ---------------------------------------------------------------------------
 // Permutations

@@ -4,6 +4,7 @@
 // contiguous for FMM, caller order for direct summation).
 #pragma once
 
+#include <functional>
 #include <memory>
 #include <vector>
 
@@ -98,6 +99,11 @@ struct Geometry {
   std::vector<int> h_leaf_nslot, h_leaf_split, h_item_split;
   DBuf<int4> items;
   DBuf<int> leaf_nslot, item_split;
+  // Segment of each leaf where several systems share one geometry (a batch;
+  // empty otherwise): a near-field pass given the segments' done flags skips
+  // the items of finished segments.
+  std::vector<int> h_leaf_seg;
+  DBuf<int> leaf_seg;
 
   // Upward pass without level-by-level M2M: leaf multipoles (P2M), then the
   // multipole of every non-leaf cell that is an M2L source from M2M shifts of
@@ -212,7 +218,15 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
                 bool damp, double damping, FinishMode mode, const T* ainv6, T* out,
                 double* out64, double sign, const ReduceSlots* dot, cudaStream_t s,
                 const PhaseEvents* pe = nullptr, int near_mode = NEAR_FP64,
-                const SideStream* side = nullptr);
+                const SideStream* side = nullptr, const int* seg_done = nullptr);
+
+// Times `apply` (one FP32 operator application ordered on `stream`) under
+// three near-field work-item sizes and, with FMM, three M2L chunk sizes;
+// keeps the fastest schedule in g (uploaded), then picks the priority of the
+// far-field stream under it.  Returns the best apply time (ms).  The operator
+// does not change, only how its work is cut into launches.
+double autotune_schedule(Geometry& g, SideStream& side, cudaStream_t stream, int reps,
+                         const std::function<void()>& apply);
 
 // Permutation helpers (caller order <-> device order), all 3-vectors.
 void permute_in(const Geometry& g, const double* in_caller, double* out_perm, int ncomp,

@@ -399,8 +399,8 @@ void System::phase_timings(int precision, int reps, double* ms) {
   for (int k = 0; k < 6; ++k) ms[k] = acc[k] / std::max(1, reps);
 }
 
-double System::autotune(int reps) {
-  CG_CUDA(cudaSetDevice(device));
+double autotune_schedule(Geometry& geo, SideStream& side, cudaStream_t stream, int reps,
+                         const std::function<void()>& apply) {
   reps = std::max(1, reps);
   // the built-in work-item size, for the candidates around it
   long total = 0;
@@ -416,7 +416,16 @@ double System::autotune(int reps) {
   cudaEvent_t e0, e1;
   CG_CUDA(cudaEventCreate(&e0));
   CG_CUDA(cudaEventCreate(&e1));
-  CG_CUDA(cudaMemsetAsync(p32.p, 0, sizeof(float) * 3 * (size_t)n, stream));
+  auto time_applies = [&]() {
+    apply();  // warm-up (sizes the work buffers)
+    CG_CUDA(cudaEventRecord(e0, stream));
+    for (int r = 0; r < reps; ++r) apply();
+    CG_CUDA(cudaEventRecord(e1, stream));
+    CG_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    return (double)ms / reps;
+  };
   double best = 1e300;
   long best_w = w0;
   int best_c  = 64;
@@ -426,14 +435,8 @@ double System::autotune(int reps) {
       geo.m2l_chunk  = chs[ci];
       geo.make_schedules();
       geo.upload_schedules(stream);
-      apply32(p32.p, Ap32.p, false);  // warm-up (sizes the work buffers)
-      CG_CUDA(cudaEventRecord(e0, stream));
-      for (int r = 0; r < reps; ++r) apply32(p32.p, Ap32.p, false);
-      CG_CUDA(cudaEventRecord(e1, stream));
-      CG_CUDA(cudaEventSynchronize(e1));
-      float ms = 0.f;
-      CG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-      if (ms / reps < best) best = ms / reps, best_w = w, best_c = chs[ci];
+      const double ms = time_applies();
+      if (ms < best) best = ms, best_w = w, best_c = chs[ci];
     }
   geo.item_pairs = best_w;
   geo.m2l_chunk  = best_c;
@@ -444,14 +447,7 @@ double System::autotune(int reps) {
     double t_side[2] = {0.0, 0.0};  // high, default priority
     for (int k = 0; k < 2; ++k) {
       side.use_high_priority(k == 0);
-      apply32(p32.p, Ap32.p, false);
-      CG_CUDA(cudaEventRecord(e0, stream));
-      for (int r = 0; r < reps; ++r) apply32(p32.p, Ap32.p, false);
-      CG_CUDA(cudaEventRecord(e1, stream));
-      CG_CUDA(cudaEventSynchronize(e1));
-      float ms = 0.f;
-      CG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-      t_side[k] = ms / reps;
+      t_side[k] = time_applies();
     }
     side.use_high_priority(t_side[0] <= t_side[1]);
     best = std::min(t_side[0], t_side[1]);
@@ -459,6 +455,14 @@ double System::autotune(int reps) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   CG_CUDA(cudaStreamSynchronize(stream));
+  return best;
+}
+
+double System::autotune(int reps) {
+  CG_CUDA(cudaSetDevice(device));
+  CG_CUDA(cudaMemsetAsync(p32.p, 0, sizeof(float) * 3 * (size_t)n, stream));
+  const double best =
+        autotune_schedule(geo, side, stream, reps, [&] { apply32(p32.p, Ap32.p, false); });
   // captured inner loops hold the old schedule's buffers: rebuild on next use
   for (auto& row : inner_exec)
     for (auto& e : row)

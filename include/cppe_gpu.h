@@ -272,6 +272,10 @@ int cppe_gpu_batch_solve_device(cppe_gpu_batch* b, const double* d_rhs, double* 
  * segment) and the largest final residual norm over the segments. */
 int cppe_gpu_batch_stats(cppe_gpu_batch* b, int* fp64_applies, int* fp32_applies,
                          double* max_rnorm);
+/* Schedule autotuning of a batch, as cppe_gpu_autotune: the FP32 operator
+ * over all segments under three near-field work-item sizes, three M2L chunk
+ * sizes and both far-field stream priorities; keeps the fastest. */
+int cppe_gpu_batch_autotune(cppe_gpu_batch* b, int reps, double* best_ms);
 /* The cudaStream_t the batch's work is ordered on. */
 int cppe_gpu_batch_stream(cppe_gpu_batch* b, void** stream);
 

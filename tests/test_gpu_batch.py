@@ -51,3 +51,49 @@ def test_batch_matches_individual_solves(gpu, precision):
                 assert its[bi * nrhs + r] == it
             off += 3 * b.n
     assert off == rhs.size
+
+
+def test_batch_autotune_keeps_the_solution(gpu):
+    boxes = _snapshots()
+    nrhs = 2
+    rhs = _rhs(boxes, nrhs, seed=1)
+    batch = cabi.Batch(boxes, nrhs, direct_below=1000, damp=True, precision=cabi.FP64)
+    mu1, its1 = batch.solve(rhs)
+    ms = batch.autotune(2)
+    assert ms > 0.0
+    mu2, its2 = batch.solve(rhs)
+    # only the partition of the work into launches changed
+    np.testing.assert_array_equal(its1, its2)
+    np.testing.assert_allclose(mu2, mu1, rtol=0, atol=1e-10)
+
+
+_HOST_LOOP = r"""
+import os, sys, numpy as np
+sys.path[:0] = [sys.argv[1], os.path.dirname(sys.argv[1])]
+import cabi
+from test_gpu_batch import _snapshots, _rhs
+boxes = _snapshots()
+b = cabi.Batch(boxes, 2, direct_below=1000, damp=True, precision=int(sys.argv[3]))
+mu, its = b.solve(_rhs(boxes, 2, seed=2))
+np.savez(sys.argv[2], mu=mu, its=its)
+"""
+
+
+@pytest.mark.parametrize("precision", [cabi.FP64, cabi.MIXED])
+def test_batch_graph_loop_matches_host_loop(gpu, precision, tmp_path):
+    """The device-side loop (conditional graph node) takes the same steps as
+    the host-launched iterations (CPPE_GPU_GRAPHS=0, a separate process)."""
+    import os
+    import subprocess
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    out = str(tmp_path / "host.npz")
+    env = dict(os.environ, CPPE_GPU_GRAPHS="0")
+    subprocess.run([sys.executable, "-c", _HOST_LOOP, here, out, str(precision)], env=env,
+                   check=True, timeout=600)
+    host = np.load(out)
+    boxes = _snapshots()
+    b = cabi.Batch(boxes, 2, direct_below=1000, damp=True, precision=precision)
+    mu, its = b.solve(_rhs(boxes, 2, seed=2))
+    np.testing.assert_array_equal(its, host["its"])
+    np.testing.assert_allclose(mu, host["mu"], rtol=0, atol=1e-12)
