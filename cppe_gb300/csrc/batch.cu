@@ -65,6 +65,7 @@ void Geometry::combine(const std::vector<const Geometry*>& parts, int copies, Ge
       seg_of_cell[k]   = s;
       local_of_cell[k] = c;
     }
+  out.h_cell_seg = seg_of_cell;
   L.child_ptr.assign(nc + 1, 0);
   L.m2l_ptr.assign(nc + 1, 0);
   for (int k = 0; k < nc; ++k) {

@@ -398,6 +398,7 @@ void Geometry::upload(cudaStream_t s) {
   item_split.upload(h_item_split, s);
   leaf_nslot.upload(h_leaf_nslot, s);
   if (!h_leaf_seg.empty()) leaf_seg.upload(h_leaf_seg, s);
+  if (!h_cell_seg.empty()) cell_seg.upload(h_cell_seg, s);
   if (!h_p2m_tasks.empty()) p2m_tasks.upload(h_p2m_tasks, s);
   task_leaf.upload(h_task_leaf, s);
   if (!h_m2l_chunks.empty()) m2l_chunks.upload(h_m2l_chunks, s);
@@ -1272,7 +1273,7 @@ struct Shifts;
 #define CPPE_DEF_SHIFTS(MM, PP, LS, MS)                                                          \
   template <>                                                                                   \
   struct Shifts<PP> {                                                                           \
-    static constexpr int ls = LS, ms = MS;                                                      \
+    static constexpr int ls = LS, ms = MS, mst = m_stride(MS);                                  \
     template <typename T>                                                                       \
     __device__ static void p2m(T x, T y, T z, T s0, T s1, T s2, T* acc) {                      \
       p2m_m1_p##PP<T>(x, y, z, s0, s1, s2, acc);                                                \
@@ -1295,10 +1296,12 @@ CPPE_SHIFTS_GENERATED(CPPE_DEF_SHIFTS)
 
 template <typename T, int P>
 __global__ void __launch_bounds__(SHIFT_THREADS)
-      k_p2m_leaf_fixed(TreeView tv, CellPos<T> cp, const T* __restrict__ src, T* __restrict__ M) {
-  constexpr int MS = Shifts<P>::ms;
+      k_p2m_leaf_fixed(TreeView tv, CellPos<T> cp, const T* __restrict__ src, T* __restrict__ M,
+                       const int* __restrict__ leaf_seg, const int* __restrict__ seg_done) {
+  constexpr int MS = Shifts<P>::ms, MST = Shifts<P>::mst;
   __shared__ T s_part[SHIFT_THREADS * (MS + 1)];
   const int leaf = blockIdx.x, cell = tv.leaf_cell[leaf];
+  if (seg_done && seg_done[leaf_seg[leaf]]) return;  // finished segment of a batch
   const int a0 = tv.leaf_start[leaf], a1 = tv.leaf_start[leaf + 1];
   T acc[MS];
 #pragma unroll
@@ -1312,10 +1315,11 @@ __global__ void __launch_bounds__(SHIFT_THREADS)
 #pragma unroll
   for (int r = 0; r < MS; ++r) s_part[threadIdx.x * (MS + 1) + r] = acc[r];
   __syncthreads();
-  for (int r = threadIdx.x; r < MS; r += SHIFT_THREADS) {
+  for (int r = threadIdx.x; r < MST; r += SHIFT_THREADS) {
     T v = T(0);
-    for (int t = 0; t < SHIFT_THREADS; ++t) v += s_part[t * (MS + 1) + r];
-    M[(size_t)cell * MS + r] = v;
+    if (r < MS)
+      for (int t = 0; t < SHIFT_THREADS; ++t) v += s_part[t * (MS + 1) + r];
+    M[(size_t)cell * MST + r] = v;
   }
 }
 
@@ -1324,7 +1328,7 @@ __global__ void __launch_bounds__(SHIFT_THREADS)
       k_m2m_tasks_fixed(TreeView tv, const int4* __restrict__ tasks, int ntask,
                         const int* __restrict__ task_leaf, CellPos<T> cp, const T* __restrict__ M,
                         T* __restrict__ Mpart) {
-  constexpr int MS  = Shifts<P>::ms;
+  constexpr int MS  = Shifts<P>::ms, MST = Shifts<P>::mst;
   constexpr int TPB = SHIFT_THREADS / M2M_TASK_LEAVES;  // tasks per block
   __shared__ T s_part[SHIFT_THREADS * (MS + 1)];
   const int g = threadIdx.x / M2M_TASK_LEAVES, sl = threadIdx.x % M2M_TASK_LEAVES;
@@ -1338,18 +1342,20 @@ __global__ void __launch_bounds__(SHIFT_THREADS)
       const int lc = tv.leaf_cell[task_leaf[tk.y + sl]];
       T x, y, z;
       centre_diff<T>(tv, cp, tk.x, lc, x, y, z);
-      Shifts<P>::m2m(x, y, z, M + (size_t)lc * MS, acc);
+      Shifts<P>::m2m(x, y, z, M + (size_t)lc * MST, acc);
     }
   }
 #pragma unroll
   for (int r = 0; r < MS; ++r) s_part[threadIdx.x * (MS + 1) + r] = acc[r];
   __syncthreads();
-  for (int idx = threadIdx.x; idx < TPB * MS; idx += SHIFT_THREADS) {
-    const int gg = idx / MS, r = idx - gg * MS, tsk = blockIdx.x * TPB + gg;
+  for (int idx = threadIdx.x; idx < TPB * MST; idx += SHIFT_THREADS) {
+    const int gg = idx / MST, r = idx - gg * MST, tsk = blockIdx.x * TPB + gg;
     if (tsk >= ntask) continue;
     T v = T(0);
-    for (int k = 0; k < M2M_TASK_LEAVES; ++k) v += s_part[(gg * M2M_TASK_LEAVES + k) * (MS + 1) + r];
-    Mpart[(size_t)tsk * MS + r] = v;
+    if (r < MS)
+      for (int k = 0; k < M2M_TASK_LEAVES; ++k)
+        v += s_part[(gg * M2M_TASK_LEAVES + k) * (MS + 1) + r];
+    Mpart[(size_t)tsk * MST + r] = v;
   }
 }
 
@@ -1695,25 +1701,35 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
     CG_CUDA(cudaStreamWaitEvent(side->s, side->fork, 0));
     fs = side->s;
   }
+  // finished segments of a batch (near field, leaf multipoles and M2L skip them)
+  const int* lseg = seg_done ? g.leaf_seg.p : nullptr;
+  const int* cseg = seg_done ? g.cell_seg.p : nullptr;
+  if (seg_done && (!lseg || (g.fmm && !cseg)))
+    fail(CPPE_GPU_INVALID_ARG, "segment mask without segments");
   if (g.fmm) {
     if (!ops || ops->host.m != m) fail(CPPE_GPU_INVALID_ARG, "FMM tables missing for order");
     ov = ops->view();
     fixedP = (m == 1 && (ov.p == 5 || ov.p == 6)) ? ov.p : 0;
-    w.M.alloc((size_t)tv.ncells * ov.msize);
+    // the fixed-order kernels store multipoles with a stride of a multiple
+    // of four coefficients (16-byte aligned rows, vector loads in M2L)
+    const int mst = fixedP ? m_stride(ov.msize) : ov.msize;
+    w.M.alloc((size_t)tv.ncells * mst);
     w.L.alloc((size_t)tv.ncells * ov.lsize);
     const int TB = 128;
     const int ntask = (int)g.h_p2m_tasks.size();
     if (tv.nleaves > 0) {
       if (fixedP == 5)
-        k_p2m_leaf_fixed<T, 5><<<tv.nleaves, SHIFT_THREADS, 0, fs>>>(tv, cell_pos<T>(g), src, w.M.p);
+        k_p2m_leaf_fixed<T, 5><<<tv.nleaves, SHIFT_THREADS, 0, fs>>>(tv, cell_pos<T>(g), src, w.M.p,
+                                                                       lseg, seg_done);
       else if (fixedP == 6)
-        k_p2m_leaf_fixed<T, 6><<<tv.nleaves, SHIFT_THREADS, 0, fs>>>(tv, cell_pos<T>(g), src, w.M.p);
+        k_p2m_leaf_fixed<T, 6><<<tv.nleaves, SHIFT_THREADS, 0, fs>>>(tv, cell_pos<T>(g), src, w.M.p,
+                                                                       lseg, seg_done);
       else
         k_p2m_leaf<T><<<tv.nleaves, TB, 0, fs>>>(tv, ov, cell_pos<T>(g), src, w.M.p);
       CG_LAUNCH();
     }
     if (ntask > 0) {
-      w.Mpart.alloc((size_t)ntask * ov.msize);
+      w.Mpart.alloc((size_t)ntask * mst);
       const int tb = (ntask + SHIFT_THREADS / M2M_TASK_LEAVES - 1) / (SHIFT_THREADS / M2M_TASK_LEAVES);
       if (fixedP == 5)
         k_m2m_tasks_fixed<T, 5><<<tb, SHIFT_THREADS, 0, fs>>>(
@@ -1725,9 +1741,9 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
         k_m2m_tasks<T><<<ntask, TB, 0, fs>>>(tv, ov, g.p2m_tasks.p, g.task_leaf.p,
                                             cell_pos<T>(g), w.M.p, w.Mpart.p);
       CG_LAUNCH();
-      const long work = (long)tv.ncells * ov.msize;
+      const long work = (long)tv.ncells * mst;
       k_msum<T><<<(unsigned)((work + 255) / 256), 256, 0, fs>>>(
-            tv.ncells, ov.msize, g.cell_task_ptr.p, w.Mpart.p, w.M.p);
+            tv.ncells, mst, g.cell_task_ptr.p, w.Mpart.p, w.M.p);
       CG_LAUNCH();
     }
     mark(1);
@@ -1735,15 +1751,15 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
     bool m2l_done = false;
     if constexpr (std::is_same<T, double>::value) {
       if (near_mode == NEAR_DD) {
-        w.Mdd.alloc((size_t)std::max(1, tv.ncells) * ov.msize);
+        w.Mdd.alloc((size_t)std::max(1, tv.ncells) * mst);
         m2l_done = launch_m2l_dd(tv, ov.m, ov.p, g.m2l_chunks.p, (int)g.h_m2l_chunks.size(),
-                                 g.cell_chunk_ptr.p, w.M.p, ov.msize, w.Mdd.p, w.Lpart.p, w.L.p,
+                                 g.cell_chunk_ptr.p, w.M.p, mst, w.Mdd.p, w.Lpart.p, w.L.p,
                                  ov.lsize, fs);
       }
     }
     if (m2l_done ||
         launch_m2l_fixed<T>(tv, ov.m, ov.p, g.m2l_chunks.p, (int)g.h_m2l_chunks.size(),
-                            g.cell_chunk_ptr.p, w.M.p, w.Lpart.p, w.L.p, ov.lsize, fs)) {
+                            g.cell_chunk_ptr.p, w.M.p, w.Lpart.p, w.L.p, ov.lsize, fs, cseg, seg_done)) {
     } else {
       size_t smem = (size_t)(ov.nm2l_terms + 9 * ov.nt) * sizeof(int);
       smem        = (smem + 15) & ~(size_t)15;

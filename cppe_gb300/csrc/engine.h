@@ -68,6 +68,11 @@ struct DeviceOps {
   OpsView view() const;
 };
 
+// Row stride (coefficients) of the multipole storage of the fixed-order
+// expansion kernels: the coefficient count rounded up to a multiple of four,
+// so that rows start on 16-byte boundaries.
+__host__ __device__ constexpr int m_stride(int ms) { return (ms + 3) & ~3; }
+
 // Geometry: the sites, their permutation and the interaction structure.
 struct Geometry {
   int n       = 0;
@@ -99,11 +104,12 @@ struct Geometry {
   std::vector<int> h_leaf_nslot, h_leaf_split, h_item_split;
   DBuf<int4> items;
   DBuf<int> leaf_nslot, item_split;
-  // Segment of each leaf where several systems share one geometry (a batch;
-  // empty otherwise): a near-field pass given the segments' done flags skips
-  // the items of finished segments.
-  std::vector<int> h_leaf_seg;
-  DBuf<int> leaf_seg;
+  // Segment of each leaf and cell where several systems share one geometry
+  // (a batch; empty otherwise): an evaluation given the segments' done flags
+  // skips the near-field items, leaf multipoles and M2L chunks of finished
+  // segments.
+  std::vector<int> h_leaf_seg, h_cell_seg;
+  DBuf<int> leaf_seg, cell_seg;
 
   // Upward pass without level-by-level M2M: leaf multipoles (P2M), then the
   // multipole of every non-leaf cell that is an M2L source from M2M shifts of

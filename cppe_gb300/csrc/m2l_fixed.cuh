@@ -20,22 +20,25 @@ namespace cg {
 
 #define CPPE_DEF_M2L_KERNEL(M, P, NAME, LS, MS)                                            \
   template <typename T>                                                                    \
-  __global__ void __launch_bounds__(128)                                                   \
+  __global__ void __launch_bounds__(128, sizeof(T) == 4 ? ((P) == 5 ? 4 : 3) : 1)          \
         k_##NAME(TreeView tv, const int4* __restrict__ chunks, int nchunks,                \
-                 const T* __restrict__ Mexp, T* __restrict__ Lpart) {                      \
+                 const T* __restrict__ Mexp, T* __restrict__ Lpart,                        \
+                 const int* __restrict__ cell_seg, const int* __restrict__ seg_done) {     \
     const int lane = threadIdx.x & 31;                                                     \
     const int w    = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;                         \
     if (w >= nchunks) return;                                                              \
     const int4 ch = chunks[w];                                                             \
     const int A   = ch.x;                                                                  \
+    if (seg_done && seg_done[cell_seg[A]]) return; /* finished segment of a batch */       \
     T acc[LS];                                                                             \
     _Pragma("unroll") for (int q = 0; q < LS; ++q) acc[q] = T(0);                          \
     const double4_32a cA = tv.center[A];                                                   \
     for (int idx = ch.y + lane; idx < ch.z; idx += 32) {                                   \
       const int B          = tv.m2l_src[idx];                                              \
       const double4_32a cB = tv.center[B];                                                 \
-      NAME<T>((T)(cA.x - cB.x), (T)(cA.y - cB.y), (T)(cA.z - cB.z),                        \
-              Mexp + (size_t)B * (MS), acc);                                               \
+      const T* Mb = static_cast<const T*>(                                                 \
+            __builtin_assume_aligned(Mexp + (size_t)B * m_stride(MS), 16));                \
+      NAME<T>((T)(cA.x - cB.x), (T)(cA.y - cB.y), (T)(cA.z - cB.z), Mb, acc);              \
     }                                                                                      \
     _Pragma("unroll") for (int q = 0; q < LS; ++q) {                                       \
       T v = acc[q];                                                                        \
@@ -66,9 +69,10 @@ CPPE_M2L_GENERATED(CPPE_DEF_M2L_KERNEL)
     for (int idx = ch.y + lane; idx < ch.z; idx += 32) {                                    \
       const int B          = tv.m2l_src[idx];                                               \
       const double4_32a cB = tv.center[B];                                                  \
+      const float2* Mb = static_cast<const float2*>(                                        \
+            __builtin_assume_aligned(Mdd + (size_t)B * m_stride(MS), 16));                  \
       NAME<ddv>(ddv(dd_from(cA.x - cB.x)), ddv(dd_from(cA.y - cB.y)),                       \
-                ddv(dd_from(cA.z - cB.z)),                                                  \
-                reinterpret_cast<const ddv*>(Mdd + (size_t)B * (MS)), acc);                 \
+                ddv(dd_from(cA.z - cB.z)), reinterpret_cast<const ddv*>(Mb), acc);          \
     }                                                                                       \
     double* LA = Lpart + (size_t)w * (LS);                                                  \
     _Pragma("unroll") for (int q = 0; q < LS; ++q) {                                        \
@@ -104,13 +108,15 @@ __global__ void k_lsum(int ncells, int lsize, const int* __restrict__ cell_chunk
 template <typename T>
 bool launch_m2l_fixed(const TreeView& tv, int m, int p, const int4* chunks, int nchunks,
                       const int* cell_chunk_ptr, const T* Mexp, T* Lpart, T* L, int lsize,
-                      cudaStream_t s) {
+                      cudaStream_t s, const int* cell_seg = nullptr,
+                      const int* seg_done = nullptr) {
   const int blocks = (int)(((long)std::max(1, nchunks) * 32 + 127) / 128);
   bool ok = false;
 #define CPPE_LAUNCH_M2L(MM, PP, NAME, LS, MS)                              \
   if (!ok && m == MM && p == PP) {                                         \
     if (nchunks > 0) {                                                     \
-      k_##NAME<T><<<blocks, 128, 0, s>>>(tv, chunks, nchunks, Mexp, Lpart); \
+      k_##NAME<T><<<blocks, 128, 0, s>>>(tv, chunks, nchunks, Mexp, Lpart,  \
+                                         cell_seg, seg_done);                \
       CG_LAUNCH();                                                         \
     }                                                                      \
     ok = true;                                                             \
