@@ -99,6 +99,55 @@ def emit(m, p):
     return "\n".join(lines), name, ls, nterms(p) - moff
 
 
+def emit_tables(m, p):
+    """Tables of the loop form of the same translation (the double-float M2L,
+    whose straight-line form is too long for the instruction cache):
+    rec[j] = {D indices of n-e_x, n-e_y, n-e_z, n-2e_x, n-2e_y, n-2e_z (-1:
+    none), |n|, 0}, coef[j] = {(2|n|-1) n_i (3), (|n|-1) n_i (n_i-1) (3),
+    1/|n| as a double-float pair}, and w: for every multipole coefficient k
+    (in order) the D index of n + k for the local coefficients n < nterms(p -
+    |k|), so that L_n += D_w M_k."""
+    mi = multi_indices(p)
+    idx = {t: j for j, t in enumerate(mi)}
+    nt, moff = nterms(p), nterms(m - 1)
+    rec, coef = [], []
+    for j, n in enumerate(mi):
+        o = sum(n)
+        q, c = [-1] * 6, [0.0] * 6
+        if j > 0:
+            for i in range(3):
+                if n[i] >= 1:
+                    t = list(n)
+                    t[i] -= 1
+                    q[i], c[i] = idx[tuple(t)], float((2 * o - 1) * n[i])
+                if n[i] >= 2:
+                    t = list(n)
+                    t[i] -= 2
+                    q[3 + i], c[3 + i] = idx[tuple(t)], float((o - 1) * n[i] * (n[i] - 1))
+        inv = 1.0 / o if o > 0 else 0.0
+        import struct
+        hi = struct.unpack("f", struct.pack("f", inv))[0]
+        lo = struct.unpack("f", struct.pack("f", inv - hi))[0]
+        rec.append(q + [o, 0])
+        coef.append(c + [hi, lo])
+    w = []
+    for k in range(moff, nt):
+        ka, kb, kc = mi[k]
+        for nidx in range(nterms(p - (ka + kb + kc))):
+            na, nb, nc = mi[nidx]
+            w.append(idx[(na + ka, nb + kb, nc + kc)])
+    name = f"m{m}_p{p}"
+    fl = lambda v: repr(float(v)) + "f"
+    lines = [f"// loop-form tables of M2L, source order {m}, expansion order {p}"]
+    lines.append(f"static __constant__ short m2l_rec_{name}[{8 * nt}] = {{")
+    lines.append("  " + ", ".join(str(v) for r in rec for v in r) + "};")
+    lines.append(f"static __constant__ float m2l_coef_{name}[{8 * nt}] = {{")
+    lines.append("  " + ", ".join(fl(v) for r in coef for v in r) + "};")
+    lines.append(f"static __constant__ unsigned char m2l_w_{name}[{len(w)}] = {{")
+    lines.append("  " + ", ".join(str(v) for v in w) + "};")
+    return "\n".join(lines), name, nt
+
+
 def powers_lines(q):
     """Scaled powers px_a = x^a / a!, a = 1..q (px_0 = 1 is left out)."""
     out = []
@@ -226,12 +275,23 @@ def main(out_path):
         code, ls, ms = emit_shifts(m, p)
         parts.append(code)
         parts.append("")
+    tabs = []
+    for m, p in ORDERS:
+        code, name, nt = emit_tables(m, p)
+        parts.append(code)
+        parts.append("")
+        tabs.append((m, p, name, nt))
     parts.append("#define CPPE_M2L_GENERATED(X) \\")
     parts.append(" \\\n".join(f"  X({m}, {p}, {name}, {ls}, {ms})" for m, p, name, ls, ms in table))
     parts.append("")
     # (m, p, Lsize, Msize) of the straight-line shifts
     parts.append("#define CPPE_SHIFTS_GENERATED(X) \\")
     parts.append(" \\\n".join(f"  X({m}, {p}, {ls}, {ms})" for m, p, name, ls, ms in table))
+    parts.append("")
+    # (m, p, name suffix of the tables, nterms(p), Lsize, Msize) of the loop form
+    parts.append("#define CPPE_M2L_TABLES(X) \\")
+    parts.append(" \\\n".join(f"  X({m}, {p}, {name}, {nt}, {ls}, {ms})"
+                              for (m, p, name, nt), (_, _, _, ls, ms) in zip(tabs, table)))
     parts.append("")
     src = "\n".join(parts)
     if os.path.exists(out_path) and open(out_path).read() == src:

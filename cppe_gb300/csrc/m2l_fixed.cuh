@@ -55,24 +55,81 @@ CPPE_M2L_GENERATED(CPPE_DEF_M2L_KERNEL)
 
 // Double-float variant for the mixed solver's FP64-accurate residual: the
 // same chunks, the source multipoles as double-float pairs (split once per
-// apply), the partial expansions written in FP64.
-#define CPPE_DEF_M2L_DD_KERNEL(M, P, NAME, LS, MS)                                          \
+// apply), the partial expansions written in FP64.  In double-float the
+// straight-line translation is longer than the instruction cache holds, so
+// this kernel runs the loop form of the same arithmetic from the generated
+// tables: each lane builds the derivative tensor of its source in its own
+// slice of shared memory (a row of nterms(p) | 1 pairs: conflict-free), then
+// adds D_{n+k} M_k over the multipole coefficients k, order by order, with
+// the local coefficients n unrolled into registers.
+constexpr int nterms_c(int p) { return p < 0 ? 0 : (p + 1) * (p + 2) * (p + 3) / 6; }
+// first w-table entry of the multipole coefficients of order ko
+constexpr int m2l_wbase(int m, int p, int ko) {
+  int b = 0;
+  for (int o = m; o < ko; ++o) b += (nterms_c(o) - nterms_c(o - 1)) * nterms_c(p - o);
+  return b;
+}
+template <int M, int P, int KO, typename WT>
+__device__ __forceinline__ void m2l_contract_dd(const float2* __restrict__ D,
+                                                const float2* __restrict__ Mb, WT wtab,
+                                                dd* acc) {
+  constexpr int R = nterms_c(P - KO), k0 = nterms_c(KO - 1), k1 = nterms_c(KO);
+  constexpr int base = m2l_wbase(M, P, KO), moff = nterms_c(M - 1);
+#pragma unroll 1
+  for (int k = k0; k < k1; ++k) {
+    const float2 mv = Mb[k - moff];
+    const int wr    = base + (k - k0) * R;
+#pragma unroll
+    for (int n = 0; n < R; ++n) {
+      const float2 d = D[wtab(wr + n)];
+      acc[n]         = dd_fma_lazy(dd{d.x, d.y}, dd{mv.x, mv.y}, acc[n]);
+    }
+  }
+  if constexpr (KO < P) m2l_contract_dd<M, P, KO + 1>(D, Mb, wtab, acc);
+}
+
+#define CPPE_DEF_M2L_DD_KERNEL(MM, PP, NAME, NT, LS, MS)                                    \
   __global__ void __launch_bounds__(64)                                                     \
-        k_##NAME##_dd(TreeView tv, const int4* __restrict__ chunks, int nchunks,            \
-                      const float2* __restrict__ Mdd, double* __restrict__ Lpart) {         \
+        k_m2l_##NAME##_dd(TreeView tv, const int4* __restrict__ chunks, int nchunks,        \
+                          const float2* __restrict__ Mdd, double* __restrict__ Lpart) {     \
+    constexpr int DS = (NT) | 1;                                                            \
+    __shared__ float2 s_D[2 * 32 * DS];                                                     \
     const int lane = threadIdx.x & 31;                                                      \
     const int w    = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;                          \
     if (w >= nchunks) return;                                                               \
+    float2* D     = s_D + (threadIdx.x >> 5) * 32 * DS + lane * DS;                         \
     const int4 ch = chunks[w];                                                              \
-    ddv acc[LS];                                                                            \
+    dd acc[LS];                                                                             \
+    _Pragma("unroll") for (int q = 0; q < LS; ++q) acc[q] = dd{0.f, 0.f};                   \
     const double4_32a cA = tv.center[ch.x];                                                 \
+    auto wtab = [](int i) { return (int)m2l_w_##NAME[i]; };                                 \
     for (int idx = ch.y + lane; idx < ch.z; idx += 32) {                                    \
       const int B          = tv.m2l_src[idx];                                               \
       const double4_32a cB = tv.center[B];                                                  \
+      const dd x = dd_from(cA.x - cB.x), y = dd_from(cA.y - cB.y), z = dd_from(cA.z - cB.z); \
+      const dd r2  = dd_add(dd_add(dd_sqr(x), dd_sqr(y)), dd_sqr(z));                       \
+      const ddv ir2 = ddv(1) / ddv(r2);                                                     \
+      const dd d0  = dd_rsqrt(r2);                                                          \
+      D[0]         = make_float2(d0.h, d0.l);                                               \
+      _Pragma("unroll 1") for (int j = 1; j < (NT); ++j) {                                  \
+        const short* q = m2l_rec_##NAME + 8 * j;                                            \
+        const float* c = m2l_coef_##NAME + 8 * j;                                           \
+        dd s           = {0.f, 0.f};                                                        \
+        const dd rv[3] = {x, y, z};                                                         \
+        _Pragma("unroll") for (int i = 0; i < 3; ++i) if (q[i] >= 0) {                      \
+          const float2 t = D[q[i]];                                                         \
+          s = dd_add(s, dd_mul_f(dd_mul(rv[i], dd{t.x, t.y}), c[i]));                       \
+        }                                                                                   \
+        _Pragma("unroll") for (int i = 3; i < 6; ++i) if (q[i] >= 0) {                      \
+          const float2 t = D[q[i]];                                                         \
+          s = dd_add(s, dd_mul_f(dd{t.x, t.y}, c[i]));                                      \
+        }                                                                                   \
+        const dd v = dd_mul(s, dd_mul(ir2, dd{c[6], c[7]}));                                \
+        D[j]       = make_float2(-v.h, -v.l);                                               \
+      }                                                                                     \
       const float2* Mb = static_cast<const float2*>(                                        \
             __builtin_assume_aligned(Mdd + (size_t)B * m_stride(MS), 16));                  \
-      NAME<ddv>(ddv(dd_from(cA.x - cB.x)), ddv(dd_from(cA.y - cB.y)),                       \
-                ddv(dd_from(cA.z - cB.z)), reinterpret_cast<const ddv*>(Mb), acc);          \
+      m2l_contract_dd<MM, PP, MM>(D, Mb, wtab, acc);                                        \
     }                                                                                       \
     double* LA = Lpart + (size_t)w * (LS);                                                  \
     _Pragma("unroll") for (int q = 0; q < LS; ++q) {                                        \
@@ -86,7 +143,7 @@ CPPE_M2L_GENERATED(CPPE_DEF_M2L_KERNEL)
     }                                                                                       \
   }
 
-CPPE_M2L_GENERATED(CPPE_DEF_M2L_DD_KERNEL)
+CPPE_M2L_TABLES(CPPE_DEF_M2L_DD_KERNEL)
 #undef CPPE_DEF_M2L_DD_KERNEL
 
 // L of every cell: the sum of its chunk partials in order (0 without chunks).
@@ -141,19 +198,18 @@ inline bool launch_m2l_dd(const TreeView& tv, int m, int p, const int4* chunks, 
                           float2* Mdd, double* Lpart, double* L, int lsize, cudaStream_t s) {
   bool ok = false;
   const long nm = (long)tv.ncells * msize;
-#define CPPE_LAUNCH_M2L_DD(MM, PP, NAME, LS, MS)                                           \
+#define CPPE_LAUNCH_M2L_DD(MM, PP, NAME, NT, LS, MS)                                       \
   if (!ok && m == MM && p == PP) {                                                         \
     if (nchunks > 0) {                                                                     \
       k_split_dd_vec<<<(unsigned)((nm + 255) / 256), 256, 0, s>>>(nm, Mexp, Mdd);          \
       CG_LAUNCH();                                                                         \
-      k_##NAME##_dd<<<(unsigned)(((long)nchunks * 32 + 63) / 64), 64, 0, s>>>(tv, chunks,  \
-                                                                             nchunks, Mdd, \
-                                                                             Lpart);       \
+      k_m2l_##NAME##_dd<<<(unsigned)(((long)nchunks * 32 + 63) / 64), 64, 0, s>>>(         \
+            tv, chunks, nchunks, Mdd, Lpart);                                              \
       CG_LAUNCH();                                                                         \
     }                                                                                      \
     ok = true;                                                                             \
   }
-  CPPE_M2L_GENERATED(CPPE_LAUNCH_M2L_DD)
+  CPPE_M2L_TABLES(CPPE_LAUNCH_M2L_DD)
 #undef CPPE_LAUNCH_M2L_DD
   if (!ok) return false;
   const long work = (long)tv.ncells * lsize;

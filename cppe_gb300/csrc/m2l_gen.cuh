@@ -5035,6 +5035,22 @@ __device__ __forceinline__ void l2p_m1_p6(T x, T y, T z, const T* __restrict__ L
   }
 }
 
+// loop-form tables of M2L, source order 1, expansion order 5
+static __constant__ short m2l_rec_m1_p5[448] = {
+  -1, -1, -1, -1, -1, -1, 0, 0, 0, -1, -1, -1, -1, -1, 1, 0, -1, 0, -1, -1, -1, -1, 1, 0, -1, -1, 0, -1, -1, -1, 1, 0, 1, -1, -1, 0, -1, -1, 2, 0, 2, 1, -1, -1, -1, -1, 2, 0, 3, -1, 1, -1, -1, -1, 2, 0, -1, 2, -1, -1, 0, -1, 2, 0, -1, 3, 2, -1, -1, -1, 2, 0, -1, -1, 3, -1, -1, 0, 2, 0, 4, -1, -1, 1, -1, -1, 3, 0, 5, 4, -1, 2, -1, -1, 3, 0, 6, -1, 4, 3, -1, -1, 3, 0, 7, 5, -1, -1, 1, -1, 3, 0, 8, 6, 5, -1, -1, -1, 3, 0, 9, -1, 6, -1, -1, 1, 3, 0, -1, 7, -1, -1, 2, -1, 3, 0, -1, 8, 7, -1, 3, -1, 3, 0, -1, 9, 8, -1, -1, 2, 3, 0, -1, -1, 9, -1, -1, 3, 3, 0, 10, -1, -1, 4, -1, -1, 4, 0, 11, 10, -1, 5, -1, -1, 4, 0, 12, -1, 10, 6, -1, -1, 4, 0, 13, 11, -1, 7, 4, -1, 4, 0, 14, 12, 11, 8, -1, -1, 4, 0, 15, -1, 12, 9, -1, 4, 4, 0, 16, 13, -1, -1, 5, -1, 4, 0, 17, 14, 13, -1, 6, -1, 4, 0, 18, 15, 14, -1, -1, 5, 4, 0, 19, -1, 15, -1, -1, 6, 4, 0, -1, 16, -1, -1, 7, -1, 4, 0, -1, 17, 16, -1, 8, -1, 4, 0, -1, 18, 17, -1, 9, 7, 4, 0, -1, 19, 18, -1, -1, 8, 4, 0, -1, -1, 19, -1, -1, 9, 4, 0, 20, -1, -1, 10, -1, -1, 5, 0, 21, 20, -1, 11, -1, -1, 5, 0, 22, -1, 20, 12, -1, -1, 5, 0, 23, 21, -1, 13, 10, -1, 5, 0, 24, 22, 21, 14, -1, -1, 5, 0, 25, -1, 22, 15, -1, 10, 5, 0, 26, 23, -1, 16, 11, -1, 5, 0, 27, 24, 23, 17, 12, -1, 5, 0, 28, 25, 24, 18, -1, 11, 5, 0, 29, -1, 25, 19, -1, 12, 5, 0, 30, 26, -1, -1, 13, -1, 5, 0, 31, 27, 26, -1, 14, -1, 5, 0, 32, 28, 27, -1, 15, 13, 5, 0, 33, 29, 28, -1, -1, 14, 5, 0, 34, -1, 29, -1, -1, 15, 5, 0, -1, 30, -1, -1, 16, -1, 5, 0, -1, 31, 30, -1, 17, -1, 5, 0, -1, 32, 31, -1, 18, 16, 5, 0, -1, 33, 32, -1, 19, 17, 5, 0, -1, 34, 33, -1, -1, 18, 5, 0, -1, -1, 34, -1, -1, 19, 5, 0};
+static __constant__ float m2l_coef_m1_p5[448] = {
+  0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f, 6.0f, 0.0f, 0.0f, 2.0f, 0.0f, 0.0f, 0.5f, 0.0f, 3.0f, 3.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.5f, 0.0f, 3.0f, 0.0f, 3.0f, 0.0f, 0.0f, 0.0f, 0.5f, 0.0f, 0.0f, 6.0f, 0.0f, 0.0f, 2.0f, 0.0f, 0.5f, 0.0f, 0.0f, 3.0f, 3.0f, 0.0f, 0.0f, 0.0f, 0.5f, 0.0f, 0.0f, 0.0f, 6.0f, 0.0f, 0.0f, 2.0f, 0.5f, 0.0f, 15.0f, 0.0f, 0.0f, 12.0f, 0.0f, 0.0f, 0.3333333432674408f, -9.934107758624577e-09f, 10.0f, 5.0f, 0.0f, 4.0f, 0.0f, 0.0f, 0.3333333432674408f, -9.934107758624577e-09f, 10.0f, 0.0f, 5.0f, 4.0f, 0.0f, 0.0f, 0.3333333432674408f, -9.934107758624577e-09f, 5.0f, 10.0f, 0.0f, 0.0f, 4.0f, 0.0f, 0.3333333432674408f, -9.934107758624577e-09f, 5.0f, 5.0f, 5.0f, 0.0f, 0.0f, 0.0f, 0.3333333432674408f, -9.934107758624577e-09f, 5.0f, 0.0f, 10.0f, 0.0f, 0.0f, 4.0f, 0.3333333432674408f, -9.934107758624577e-09f, 0.0f, 15.0f, 0.0f, 0.0f, 12.0f, 0.0f, 0.3333333432674408f, -9.934107758624577e-09f, 0.0f, 10.0f, 5.0f, 0.0f, 4.0f, 0.0f, 0.3333333432674408f, -9.934107758624577e-09f, 0.0f, 5.0f, 10.0f, 0.0f, 0.0f, 4.0f, 0.3333333432674408f, -9.934107758624577e-09f, 0.0f, 0.0f, 15.0f, 0.0f, 0.0f, 12.0f, 0.3333333432674408f, -9.934107758624577e-09f, 28.0f, 0.0f, 0.0f, 36.0f, 0.0f, 0.0f, 0.25f, 0.0f, 21.0f, 7.0f, 0.0f, 18.0f, 0.0f, 0.0f, 0.25f, 0.0f, 21.0f, 0.0f, 7.0f, 18.0f, 0.0f, 0.0f, 0.25f, 0.0f, 14.0f, 14.0f, 0.0f, 6.0f, 6.0f, 0.0f, 0.25f, 0.0f, 14.0f, 7.0f, 7.0f, 6.0f, 0.0f, 0.0f, 0.25f, 0.0f, 14.0f, 0.0f, 14.0f, 6.0f, 0.0f, 6.0f, 0.25f, 0.0f, 7.0f, 21.0f, 0.0f, 0.0f, 18.0f, 0.0f, 0.25f, 0.0f, 7.0f, 14.0f, 7.0f, 0.0f, 6.0f, 0.0f, 0.25f, 0.0f, 7.0f, 7.0f, 14.0f, 0.0f, 0.0f, 6.0f, 0.25f, 0.0f, 7.0f, 0.0f, 21.0f, 0.0f, 0.0f, 18.0f, 0.25f, 0.0f, 0.0f, 28.0f, 0.0f, 0.0f, 36.0f, 0.0f, 0.25f, 0.0f, 0.0f, 21.0f, 7.0f, 0.0f, 18.0f, 0.0f, 0.25f, 0.0f, 0.0f, 14.0f, 14.0f, 0.0f, 6.0f, 6.0f, 0.25f, 0.0f, 0.0f, 7.0f, 21.0f, 0.0f, 0.0f, 18.0f, 0.25f, 0.0f, 0.0f, 0.0f, 28.0f, 0.0f, 0.0f, 36.0f, 0.25f, 0.0f, 45.0f, 0.0f, 0.0f, 80.0f, 0.0f, 0.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 36.0f, 9.0f, 0.0f, 48.0f, 0.0f, 0.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 36.0f, 0.0f, 9.0f, 48.0f, 0.0f, 0.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 27.0f, 18.0f, 0.0f, 24.0f, 8.0f, 0.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 27.0f, 9.0f, 9.0f, 24.0f, 0.0f, 0.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 27.0f, 0.0f, 18.0f, 24.0f, 0.0f, 8.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 18.0f, 27.0f, 0.0f, 8.0f, 24.0f, 0.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 18.0f, 18.0f, 9.0f, 8.0f, 8.0f, 0.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 18.0f, 9.0f, 18.0f, 8.0f, 0.0f, 8.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 18.0f, 0.0f, 27.0f, 8.0f, 0.0f, 24.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 9.0f, 36.0f, 0.0f, 0.0f, 48.0f, 0.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 9.0f, 27.0f, 9.0f, 0.0f, 24.0f, 0.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 9.0f, 18.0f, 18.0f, 0.0f, 8.0f, 8.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 9.0f, 9.0f, 27.0f, 0.0f, 0.0f, 24.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 9.0f, 0.0f, 36.0f, 0.0f, 0.0f, 48.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 0.0f, 45.0f, 0.0f, 0.0f, 80.0f, 0.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 0.0f, 36.0f, 9.0f, 0.0f, 48.0f, 0.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 0.0f, 27.0f, 18.0f, 0.0f, 24.0f, 8.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 0.0f, 18.0f, 27.0f, 0.0f, 8.0f, 24.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 0.0f, 9.0f, 36.0f, 0.0f, 0.0f, 48.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 0.0f, 0.0f, 45.0f, 0.0f, 0.0f, 80.0f, 0.20000000298023224f, -2.9802322831784522e-09f};
+static __constant__ unsigned char m2l_w_m1_p5[406] = {
+  1, 4, 5, 6, 10, 11, 12, 13, 14, 15, 20, 21, 22, 23, 24, 25, 26, 27, 28, 29, 35, 36, 37, 38, 39, 40, 41, 42, 43, 44, 45, 46, 47, 48, 49, 2, 5, 7, 8, 11, 13, 14, 16, 17, 18, 21, 23, 24, 26, 27, 28, 30, 31, 32, 33, 36, 38, 39, 41, 42, 43, 45, 46, 47, 48, 50, 51, 52, 53, 54, 3, 6, 8, 9, 12, 14, 15, 17, 18, 19, 22, 24, 25, 27, 28, 29, 31, 32, 33, 34, 37, 39, 40, 42, 43, 44, 46, 47, 48, 49, 51, 52, 53, 54, 55, 4, 10, 11, 12, 20, 21, 22, 23, 24, 25, 35, 36, 37, 38, 39, 40, 41, 42, 43, 44, 5, 11, 13, 14, 21, 23, 24, 26, 27, 28, 36, 38, 39, 41, 42, 43, 45, 46, 47, 48, 6, 12, 14, 15, 22, 24, 25, 27, 28, 29, 37, 39, 40, 42, 43, 44, 46, 47, 48, 49, 7, 13, 16, 17, 23, 26, 27, 30, 31, 32, 38, 41, 42, 45, 46, 47, 50, 51, 52, 53, 8, 14, 17, 18, 24, 27, 28, 31, 32, 33, 39, 42, 43, 46, 47, 48, 51, 52, 53, 54, 9, 15, 18, 19, 25, 28, 29, 32, 33, 34, 40, 43, 44, 47, 48, 49, 52, 53, 54, 55, 10, 20, 21, 22, 35, 36, 37, 38, 39, 40, 11, 21, 23, 24, 36, 38, 39, 41, 42, 43, 12, 22, 24, 25, 37, 39, 40, 42, 43, 44, 13, 23, 26, 27, 38, 41, 42, 45, 46, 47, 14, 24, 27, 28, 39, 42, 43, 46, 47, 48, 15, 25, 28, 29, 40, 43, 44, 47, 48, 49, 16, 26, 30, 31, 41, 45, 46, 50, 51, 52, 17, 27, 31, 32, 42, 46, 47, 51, 52, 53, 18, 28, 32, 33, 43, 47, 48, 52, 53, 54, 19, 29, 33, 34, 44, 48, 49, 53, 54, 55, 20, 35, 36, 37, 21, 36, 38, 39, 22, 37, 39, 40, 23, 38, 41, 42, 24, 39, 42, 43, 25, 40, 43, 44, 26, 41, 45, 46, 27, 42, 46, 47, 28, 43, 47, 48, 29, 44, 48, 49, 30, 45, 50, 51, 31, 46, 51, 52, 32, 47, 52, 53, 33, 48, 53, 54, 34, 49, 54, 55, 35, 36, 37, 38, 39, 40, 41, 42, 43, 44, 45, 46, 47, 48, 49, 50, 51, 52, 53, 54, 55};
+
+// loop-form tables of M2L, source order 1, expansion order 6
+static __constant__ short m2l_rec_m1_p6[672] = {
+  -1, -1, -1, -1, -1, -1, 0, 0, 0, -1, -1, -1, -1, -1, 1, 0, -1, 0, -1, -1, -1, -1, 1, 0, -1, -1, 0, -1, -1, -1, 1, 0, 1, -1, -1, 0, -1, -1, 2, 0, 2, 1, -1, -1, -1, -1, 2, 0, 3, -1, 1, -1, -1, -1, 2, 0, -1, 2, -1, -1, 0, -1, 2, 0, -1, 3, 2, -1, -1, -1, 2, 0, -1, -1, 3, -1, -1, 0, 2, 0, 4, -1, -1, 1, -1, -1, 3, 0, 5, 4, -1, 2, -1, -1, 3, 0, 6, -1, 4, 3, -1, -1, 3, 0, 7, 5, -1, -1, 1, -1, 3, 0, 8, 6, 5, -1, -1, -1, 3, 0, 9, -1, 6, -1, -1, 1, 3, 0, -1, 7, -1, -1, 2, -1, 3, 0, -1, 8, 7, -1, 3, -1, 3, 0, -1, 9, 8, -1, -1, 2, 3, 0, -1, -1, 9, -1, -1, 3, 3, 0, 10, -1, -1, 4, -1, -1, 4, 0, 11, 10, -1, 5, -1, -1, 4, 0, 12, -1, 10, 6, -1, -1, 4, 0, 13, 11, -1, 7, 4, -1, 4, 0, 14, 12, 11, 8, -1, -1, 4, 0, 15, -1, 12, 9, -1, 4, 4, 0, 16, 13, -1, -1, 5, -1, 4, 0, 17, 14, 13, -1, 6, -1, 4, 0, 18, 15, 14, -1, -1, 5, 4, 0, 19, -1, 15, -1, -1, 6, 4, 0, -1, 16, -1, -1, 7, -1, 4, 0, -1, 17, 16, -1, 8, -1, 4, 0, -1, 18, 17, -1, 9, 7, 4, 0, -1, 19, 18, -1, -1, 8, 4, 0, -1, -1, 19, -1, -1, 9, 4, 0, 20, -1, -1, 10, -1, -1, 5, 0, 21, 20, -1, 11, -1, -1, 5, 0, 22, -1, 20, 12, -1, -1, 5, 0, 23, 21, -1, 13, 10, -1, 5, 0, 24, 22, 21, 14, -1, -1, 5, 0, 25, -1, 22, 15, -1, 10, 5, 0, 26, 23, -1, 16, 11, -1, 5, 0, 27, 24, 23, 17, 12, -1, 5, 0, 28, 25, 24, 18, -1, 11, 5, 0, 29, -1, 25, 19, -1, 12, 5, 0, 30, 26, -1, -1, 13, -1, 5, 0, 31, 27, 26, -1, 14, -1, 5, 0, 32, 28, 27, -1, 15, 13, 5, 0, 33, 29, 28, -1, -1, 14, 5, 0, 34, -1, 29, -1, -1, 15, 5, 0, -1, 30, -1, -1, 16, -1, 5, 0, -1, 31, 30, -1, 17, -1, 5, 0, -1, 32, 31, -1, 18, 16, 5, 0, -1, 33, 32, -1, 19, 17, 5, 0, -1, 34, 33, -1, -1, 18, 5, 0, -1, -1, 34, -1, -1, 19, 5, 0, 35, -1, -1, 20, -1, -1, 6, 0, 36, 35, -1, 21, -1, -1, 6, 0, 37, -1, 35, 22, -1, -1, 6, 0, 38, 36, -1, 23, 20, -1, 6, 0, 39, 37, 36, 24, -1, -1, 6, 0, 40, -1, 37, 25, -1, 20, 6, 0, 41, 38, -1, 26, 21, -1, 6, 0, 42, 39, 38, 27, 22, -1, 6, 0, 43, 40, 39, 28, -1, 21, 6, 0, 44, -1, 40, 29, -1, 22, 6, 0, 45, 41, -1, 30, 23, -1, 6, 0, 46, 42, 41, 31, 24, -1, 6, 0, 47, 43, 42, 32, 25, 23, 6, 0, 48, 44, 43, 33, -1, 24, 6, 0, 49, -1, 44, 34, -1, 25, 6, 0, 50, 45, -1, -1, 26, -1, 6, 0, 51, 46, 45, -1, 27, -1, 6, 0, 52, 47, 46, -1, 28, 26, 6, 0, 53, 48, 47, -1, 29, 27, 6, 0, 54, 49, 48, -1, -1, 28, 6, 0, 55, -1, 49, -1, -1, 29, 6, 0, -1, 50, -1, -1, 30, -1, 6, 0, -1, 51, 50, -1, 31, -1, 6, 0, -1, 52, 51, -1, 32, 30, 6, 0, -1, 53, 52, -1, 33, 31, 6, 0, -1, 54, 53, -1, 34, 32, 6, 0, -1, 55, 54, -1, -1, 33, 6, 0, -1, -1, 55, -1, -1, 34, 6, 0};
+static __constant__ float m2l_coef_m1_p6[672] = {
+  0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f, 6.0f, 0.0f, 0.0f, 2.0f, 0.0f, 0.0f, 0.5f, 0.0f, 3.0f, 3.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.5f, 0.0f, 3.0f, 0.0f, 3.0f, 0.0f, 0.0f, 0.0f, 0.5f, 0.0f, 0.0f, 6.0f, 0.0f, 0.0f, 2.0f, 0.0f, 0.5f, 0.0f, 0.0f, 3.0f, 3.0f, 0.0f, 0.0f, 0.0f, 0.5f, 0.0f, 0.0f, 0.0f, 6.0f, 0.0f, 0.0f, 2.0f, 0.5f, 0.0f, 15.0f, 0.0f, 0.0f, 12.0f, 0.0f, 0.0f, 0.3333333432674408f, -9.934107758624577e-09f, 10.0f, 5.0f, 0.0f, 4.0f, 0.0f, 0.0f, 0.3333333432674408f, -9.934107758624577e-09f, 10.0f, 0.0f, 5.0f, 4.0f, 0.0f, 0.0f, 0.3333333432674408f, -9.934107758624577e-09f, 5.0f, 10.0f, 0.0f, 0.0f, 4.0f, 0.0f, 0.3333333432674408f, -9.934107758624577e-09f, 5.0f, 5.0f, 5.0f, 0.0f, 0.0f, 0.0f, 0.3333333432674408f, -9.934107758624577e-09f, 5.0f, 0.0f, 10.0f, 0.0f, 0.0f, 4.0f, 0.3333333432674408f, -9.934107758624577e-09f, 0.0f, 15.0f, 0.0f, 0.0f, 12.0f, 0.0f, 0.3333333432674408f, -9.934107758624577e-09f, 0.0f, 10.0f, 5.0f, 0.0f, 4.0f, 0.0f, 0.3333333432674408f, -9.934107758624577e-09f, 0.0f, 5.0f, 10.0f, 0.0f, 0.0f, 4.0f, 0.3333333432674408f, -9.934107758624577e-09f, 0.0f, 0.0f, 15.0f, 0.0f, 0.0f, 12.0f, 0.3333333432674408f, -9.934107758624577e-09f, 28.0f, 0.0f, 0.0f, 36.0f, 0.0f, 0.0f, 0.25f, 0.0f, 21.0f, 7.0f, 0.0f, 18.0f, 0.0f, 0.0f, 0.25f, 0.0f, 21.0f, 0.0f, 7.0f, 18.0f, 0.0f, 0.0f, 0.25f, 0.0f, 14.0f, 14.0f, 0.0f, 6.0f, 6.0f, 0.0f, 0.25f, 0.0f, 14.0f, 7.0f, 7.0f, 6.0f, 0.0f, 0.0f, 0.25f, 0.0f, 14.0f, 0.0f, 14.0f, 6.0f, 0.0f, 6.0f, 0.25f, 0.0f, 7.0f, 21.0f, 0.0f, 0.0f, 18.0f, 0.0f, 0.25f, 0.0f, 7.0f, 14.0f, 7.0f, 0.0f, 6.0f, 0.0f, 0.25f, 0.0f, 7.0f, 7.0f, 14.0f, 0.0f, 0.0f, 6.0f, 0.25f, 0.0f, 7.0f, 0.0f, 21.0f, 0.0f, 0.0f, 18.0f, 0.25f, 0.0f, 0.0f, 28.0f, 0.0f, 0.0f, 36.0f, 0.0f, 0.25f, 0.0f, 0.0f, 21.0f, 7.0f, 0.0f, 18.0f, 0.0f, 0.25f, 0.0f, 0.0f, 14.0f, 14.0f, 0.0f, 6.0f, 6.0f, 0.25f, 0.0f, 0.0f, 7.0f, 21.0f, 0.0f, 0.0f, 18.0f, 0.25f, 0.0f, 0.0f, 0.0f, 28.0f, 0.0f, 0.0f, 36.0f, 0.25f, 0.0f, 45.0f, 0.0f, 0.0f, 80.0f, 0.0f, 0.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 36.0f, 9.0f, 0.0f, 48.0f, 0.0f, 0.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 36.0f, 0.0f, 9.0f, 48.0f, 0.0f, 0.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 27.0f, 18.0f, 0.0f, 24.0f, 8.0f, 0.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 27.0f, 9.0f, 9.0f, 24.0f, 0.0f, 0.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 27.0f, 0.0f, 18.0f, 24.0f, 0.0f, 8.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 18.0f, 27.0f, 0.0f, 8.0f, 24.0f, 0.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 18.0f, 18.0f, 9.0f, 8.0f, 8.0f, 0.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 18.0f, 9.0f, 18.0f, 8.0f, 0.0f, 8.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 18.0f, 0.0f, 27.0f, 8.0f, 0.0f, 24.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 9.0f, 36.0f, 0.0f, 0.0f, 48.0f, 0.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 9.0f, 27.0f, 9.0f, 0.0f, 24.0f, 0.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 9.0f, 18.0f, 18.0f, 0.0f, 8.0f, 8.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 9.0f, 9.0f, 27.0f, 0.0f, 0.0f, 24.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 9.0f, 0.0f, 36.0f, 0.0f, 0.0f, 48.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 0.0f, 45.0f, 0.0f, 0.0f, 80.0f, 0.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 0.0f, 36.0f, 9.0f, 0.0f, 48.0f, 0.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 0.0f, 27.0f, 18.0f, 0.0f, 24.0f, 8.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 0.0f, 18.0f, 27.0f, 0.0f, 8.0f, 24.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 0.0f, 9.0f, 36.0f, 0.0f, 0.0f, 48.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 0.0f, 0.0f, 45.0f, 0.0f, 0.0f, 80.0f, 0.20000000298023224f, -2.9802322831784522e-09f, 66.0f, 0.0f, 0.0f, 150.0f, 0.0f, 0.0f, 0.1666666716337204f, -4.967053879312289e-09f, 55.0f, 11.0f, 0.0f, 100.0f, 0.0f, 0.0f, 0.1666666716337204f, -4.967053879312289e-09f, 55.0f, 0.0f, 11.0f, 100.0f, 0.0f, 0.0f, 0.1666666716337204f, -4.967053879312289e-09f, 44.0f, 22.0f, 0.0f, 60.0f, 10.0f, 0.0f, 0.1666666716337204f, -4.967053879312289e-09f, 44.0f, 11.0f, 11.0f, 60.0f, 0.0f, 0.0f, 0.1666666716337204f, -4.967053879312289e-09f, 44.0f, 0.0f, 22.0f, 60.0f, 0.0f, 10.0f, 0.1666666716337204f, -4.967053879312289e-09f, 33.0f, 33.0f, 0.0f, 30.0f, 30.0f, 0.0f, 0.1666666716337204f, -4.967053879312289e-09f, 33.0f, 22.0f, 11.0f, 30.0f, 10.0f, 0.0f, 0.1666666716337204f, -4.967053879312289e-09f, 33.0f, 11.0f, 22.0f, 30.0f, 0.0f, 10.0f, 0.1666666716337204f, -4.967053879312289e-09f, 33.0f, 0.0f, 33.0f, 30.0f, 0.0f, 30.0f, 0.1666666716337204f, -4.967053879312289e-09f, 22.0f, 44.0f, 0.0f, 10.0f, 60.0f, 0.0f, 0.1666666716337204f, -4.967053879312289e-09f, 22.0f, 33.0f, 11.0f, 10.0f, 30.0f, 0.0f, 0.1666666716337204f, -4.967053879312289e-09f, 22.0f, 22.0f, 22.0f, 10.0f, 10.0f, 10.0f, 0.1666666716337204f, -4.967053879312289e-09f, 22.0f, 11.0f, 33.0f, 10.0f, 0.0f, 30.0f, 0.1666666716337204f, -4.967053879312289e-09f, 22.0f, 0.0f, 44.0f, 10.0f, 0.0f, 60.0f, 0.1666666716337204f, -4.967053879312289e-09f, 11.0f, 55.0f, 0.0f, 0.0f, 100.0f, 0.0f, 0.1666666716337204f, -4.967053879312289e-09f, 11.0f, 44.0f, 11.0f, 0.0f, 60.0f, 0.0f, 0.1666666716337204f, -4.967053879312289e-09f, 11.0f, 33.0f, 22.0f, 0.0f, 30.0f, 10.0f, 0.1666666716337204f, -4.967053879312289e-09f, 11.0f, 22.0f, 33.0f, 0.0f, 10.0f, 30.0f, 0.1666666716337204f, -4.967053879312289e-09f, 11.0f, 11.0f, 44.0f, 0.0f, 0.0f, 60.0f, 0.1666666716337204f, -4.967053879312289e-09f, 11.0f, 0.0f, 55.0f, 0.0f, 0.0f, 100.0f, 0.1666666716337204f, -4.967053879312289e-09f, 0.0f, 66.0f, 0.0f, 0.0f, 150.0f, 0.0f, 0.1666666716337204f, -4.967053879312289e-09f, 0.0f, 55.0f, 11.0f, 0.0f, 100.0f, 0.0f, 0.1666666716337204f, -4.967053879312289e-09f, 0.0f, 44.0f, 22.0f, 0.0f, 60.0f, 10.0f, 0.1666666716337204f, -4.967053879312289e-09f, 0.0f, 33.0f, 33.0f, 0.0f, 30.0f, 30.0f, 0.1666666716337204f, -4.967053879312289e-09f, 0.0f, 22.0f, 44.0f, 0.0f, 10.0f, 60.0f, 0.1666666716337204f, -4.967053879312289e-09f, 0.0f, 11.0f, 55.0f, 0.0f, 0.0f, 100.0f, 0.1666666716337204f, -4.967053879312289e-09f, 0.0f, 0.0f, 66.0f, 0.0f, 0.0f, 150.0f, 0.1666666716337204f, -4.967053879312289e-09f};
+static __constant__ unsigned char m2l_w_m1_p6[840] = {
+  1, 4, 5, 6, 10, 11, 12, 13, 14, 15, 20, 21, 22, 23, 24, 25, 26, 27, 28, 29, 35, 36, 37, 38, 39, 40, 41, 42, 43, 44, 45, 46, 47, 48, 49, 56, 57, 58, 59, 60, 61, 62, 63, 64, 65, 66, 67, 68, 69, 70, 71, 72, 73, 74, 75, 76, 2, 5, 7, 8, 11, 13, 14, 16, 17, 18, 21, 23, 24, 26, 27, 28, 30, 31, 32, 33, 36, 38, 39, 41, 42, 43, 45, 46, 47, 48, 50, 51, 52, 53, 54, 57, 59, 60, 62, 63, 64, 66, 67, 68, 69, 71, 72, 73, 74, 75, 77, 78, 79, 80, 81, 82, 3, 6, 8, 9, 12, 14, 15, 17, 18, 19, 22, 24, 25, 27, 28, 29, 31, 32, 33, 34, 37, 39, 40, 42, 43, 44, 46, 47, 48, 49, 51, 52, 53, 54, 55, 58, 60, 61, 63, 64, 65, 67, 68, 69, 70, 72, 73, 74, 75, 76, 78, 79, 80, 81, 82, 83, 4, 10, 11, 12, 20, 21, 22, 23, 24, 25, 35, 36, 37, 38, 39, 40, 41, 42, 43, 44, 56, 57, 58, 59, 60, 61, 62, 63, 64, 65, 66, 67, 68, 69, 70, 5, 11, 13, 14, 21, 23, 24, 26, 27, 28, 36, 38, 39, 41, 42, 43, 45, 46, 47, 48, 57, 59, 60, 62, 63, 64, 66, 67, 68, 69, 71, 72, 73, 74, 75, 6, 12, 14, 15, 22, 24, 25, 27, 28, 29, 37, 39, 40, 42, 43, 44, 46, 47, 48, 49, 58, 60, 61, 63, 64, 65, 67, 68, 69, 70, 72, 73, 74, 75, 76, 7, 13, 16, 17, 23, 26, 27, 30, 31, 32, 38, 41, 42, 45, 46, 47, 50, 51, 52, 53, 59, 62, 63, 66, 67, 68, 71, 72, 73, 74, 77, 78, 79, 80, 81, 8, 14, 17, 18, 24, 27, 28, 31, 32, 33, 39, 42, 43, 46, 47, 48, 51, 52, 53, 54, 60, 63, 64, 67, 68, 69, 72, 73, 74, 75, 78, 79, 80, 81, 82, 9, 15, 18, 19, 25, 28, 29, 32, 33, 34, 40, 43, 44, 47, 48, 49, 52, 53, 54, 55, 61, 64, 65, 68, 69, 70, 73, 74, 75, 76, 79, 80, 81, 82, 83, 10, 20, 21, 22, 35, 36, 37, 38, 39, 40, 56, 57, 58, 59, 60, 61, 62, 63, 64, 65, 11, 21, 23, 24, 36, 38, 39, 41, 42, 43, 57, 59, 60, 62, 63, 64, 66, 67, 68, 69, 12, 22, 24, 25, 37, 39, 40, 42, 43, 44, 58, 60, 61, 63, 64, 65, 67, 68, 69, 70, 13, 23, 26, 27, 38, 41, 42, 45, 46, 47, 59, 62, 63, 66, 67, 68, 71, 72, 73, 74, 14, 24, 27, 28, 39, 42, 43, 46, 47, 48, 60, 63, 64, 67, 68, 69, 72, 73, 74, 75, 15, 25, 28, 29, 40, 43, 44, 47, 48, 49, 61, 64, 65, 68, 69, 70, 73, 74, 75, 76, 16, 26, 30, 31, 41, 45, 46, 50, 51, 52, 62, 66, 67, 71, 72, 73, 77, 78, 79, 80, 17, 27, 31, 32, 42, 46, 47, 51, 52, 53, 63, 67, 68, 72, 73, 74, 78, 79, 80, 81, 18, 28, 32, 33, 43, 47, 48, 52, 53, 54, 64, 68, 69, 73, 74, 75, 79, 80, 81, 82, 19, 29, 33, 34, 44, 48, 49, 53, 54, 55, 65, 69, 70, 74, 75, 76, 80, 81, 82, 83, 20, 35, 36, 37, 56, 57, 58, 59, 60, 61, 21, 36, 38, 39, 57, 59, 60, 62, 63, 64, 22, 37, 39, 40, 58, 60, 61, 63, 64, 65, 23, 38, 41, 42, 59, 62, 63, 66, 67, 68, 24, 39, 42, 43, 60, 63, 64, 67, 68, 69, 25, 40, 43, 44, 61, 64, 65, 68, 69, 70, 26, 41, 45, 46, 62, 66, 67, 71, 72, 73, 27, 42, 46, 47, 63, 67, 68, 72, 73, 74, 28, 43, 47, 48, 64, 68, 69, 73, 74, 75, 29, 44, 48, 49, 65, 69, 70, 74, 75, 76, 30, 45, 50, 51, 66, 71, 72, 77, 78, 79, 31, 46, 51, 52, 67, 72, 73, 78, 79, 80, 32, 47, 52, 53, 68, 73, 74, 79, 80, 81, 33, 48, 53, 54, 69, 74, 75, 80, 81, 82, 34, 49, 54, 55, 70, 75, 76, 81, 82, 83, 35, 56, 57, 58, 36, 57, 59, 60, 37, 58, 60, 61, 38, 59, 62, 63, 39, 60, 63, 64, 40, 61, 64, 65, 41, 62, 66, 67, 42, 63, 67, 68, 43, 64, 68, 69, 44, 65, 69, 70, 45, 66, 71, 72, 46, 67, 72, 73, 47, 68, 73, 74, 48, 69, 74, 75, 49, 70, 75, 76, 50, 71, 77, 78, 51, 72, 78, 79, 52, 73, 79, 80, 53, 74, 80, 81, 54, 75, 81, 82, 55, 76, 82, 83, 56, 57, 58, 59, 60, 61, 62, 63, 64, 65, 66, 67, 68, 69, 70, 71, 72, 73, 74, 75, 76, 77, 78, 79, 80, 81, 82, 83};
+
 #define CPPE_M2L_GENERATED(X) \
   X(1, 5, m2l_m1_p5, 35, 55) \
   X(1, 6, m2l_m1_p6, 56, 83)
@@ -5042,3 +5058,7 @@ __device__ __forceinline__ void l2p_m1_p6(T x, T y, T z, const T* __restrict__ L
 #define CPPE_SHIFTS_GENERATED(X) \
   X(1, 5, 35, 55) \
   X(1, 6, 56, 83)
+
+#define CPPE_M2L_TABLES(X) \
+  X(1, 5, m1_p5, 56, 35, 55) \
+  X(1, 6, m1_p6, 84, 56, 83)
