@@ -176,3 +176,61 @@ def test_synthetic_potfile_round_trip(cppe, tmp_path):
     np.testing.assert_allclose(xyz, b.xyz, atol=1e-10)
     assert all(p.exclusions == list(b.excl_idx[2 * i:2 * i + 2]) for i, p in enumerate(pots))
     np.testing.assert_allclose([p.polarizability.isotropic_value for p in pots], b.alpha_iso)
+
+
+def _straight_line_m2l(gen, m, p, x, y, z, Mb):
+    """Evaluates the generated straight-line translation (C source of
+    m2l_gen.cuh) in FP64 by rewriting it as Python."""
+    import re
+    code, _, ls, _ = gen.emit(m, p)
+    body = code.split("{", 1)[1].rsplit("}", 1)[0]
+    lines = []
+    for ln in body.split("\n"):
+        ln = ln.strip().replace("const T ", "").replace("cinv<T>(", "1.0/(").replace("T(", "float(")
+        ln = ln.replace("rsqrt_t(r2)", "r2**-0.5")
+        ln = re.sub(r"fma\((D\d+), mk, (acc\[\d+\])\)", r"\1*mk + \2", ln)
+        ln = ln.replace("{ ", "").replace(";", "").replace("}", "").strip()
+        if ln:
+            lines.append(ln)
+    env = dict(x=x, y=y, z=z, Mb=Mb, acc=[0.0] * ls)
+    exec("\n".join(lines), env)
+    return np.array(env["acc"])
+
+
+@pytest.mark.parametrize("m,p", [(1, 5), (1, 6)])
+def test_m2l_loop_tables_match_straight_line(m, p):
+    """The tables of the loop-form (double-float) M2L encode the same
+    translation as the generated straight-line code: the derivative
+    recurrence and every D_{n+k} M_k term, evaluated here in FP64."""
+    import os
+    import re
+    import sys
+    sys.path.insert(0, os.path.join(cabi.LIB_PATH.rsplit(os.sep, 1)[0], "csrc"))
+    import gen_m2l as gen
+    rng = np.random.default_rng(p)
+    tcode, _, nt = gen.emit_tables(m, p)
+    arrs = re.findall(r"\{\n  (.*?)\};", tcode, re.S)
+    rec = np.array([int(v) for v in arrs[0].split(",")]).reshape(nt, 8)
+    coef = np.array([float(v.strip().rstrip("f")) for v in arrs[1].split(",")]).reshape(nt, 8)
+    w = [int(v) for v in arrs[2].split(",")]
+    mi = gen.multi_indices(p)
+    moff, ls, ms = gen.nterms(m - 1), gen.nterms(p - m), gen.nterms(p) - gen.nterms(m - 1)
+    for _ in range(4):
+        x, y, z = rng.normal(size=3) * 3.0
+        Mb = rng.normal(size=ms)
+        ref = _straight_line_m2l(gen, m, p, x, y, z, Mb)
+        r2 = x * x + y * y + z * z
+        D = np.zeros(nt)
+        D[0] = r2 ** -0.5
+        for j in range(1, nt):
+            q, c = rec[j], coef[j]
+            s = sum(c[i] * rv * D[q[i]] for i, rv in enumerate((x, y, z)) if q[i] >= 0)
+            s += sum(c[3 + i] * D[q[3 + i]] for i in range(3) if q[3 + i] >= 0)
+            D[j] = -s / r2 * (c[6] + c[7])
+        out, t = np.zeros(ls), 0
+        for k in range(moff, nt):
+            for n in range(gen.nterms(p - sum(mi[k]))):
+                out[n] += D[w[t]] * Mb[k - moff]
+                t += 1
+        assert t == len(w)
+        np.testing.assert_allclose(out, ref, rtol=0, atol=1e-12 * np.max(np.abs(ref)))
