@@ -22,10 +22,12 @@
 #include <cstring>
 #include <numeric>
 #include <type_traits>
+#include <unordered_map>
 
 #include "engine.h"
 #include "dd.cuh"
 #include "m2l_fixed.cuh"
+
 
 namespace cg {
 
@@ -39,6 +41,7 @@ constexpr int M2L_WARPS  = 4;
 constexpr int P2M_LEAF_SITES  = 128;  // sites staged per round of the leaf P2M
 constexpr int M2M_TASK_LEAVES = 8;    // leaf multipoles shifted per upward-pass task
 constexpr int M2L_CHUNK       = 64;   // sources of one target cell per M2L warp
+constexpr bool M2L_TABLE_FP64 = true;  // FP64 M2L from tabulated derivative tensors
 constexpr int PW = PMAX + 1;          // powers 0..PMAX of one coordinate
 constexpr int FINISH_BLOCK = 128;
 
@@ -228,6 +231,47 @@ void Geometry::prepare(int n_, const double* xyz, const double* s_damp, const in
   // near-field / direct loops (self pairs and excluded pairs are skipped there)
   alg_pairs = near_pairs - n - (long)cidx.size();
   make_schedules();
+  make_vectors();
+}
+
+void Geometry::make_vectors() {
+  h_m2l_vid.clear();
+  h_vec.clear();
+  const TreeLayout& L = layout;
+  if (!fmm || L.m2l_src.empty()) return;
+  // centres are the root centre plus multiples of the deepest half-width
+  double rmin = 1e300;
+  for (int c = 0; c < L.ncells; ++c) rmin = std::min(rmin, L.center[4 * (size_t)c + 3]);
+  if (!(rmin > 0.0)) return;
+  const double u = 0.5 * rmin;
+  constexpr long long OFF = 1LL << 20;
+  std::unordered_map<long long, int> ids;
+  h_m2l_vid.resize(L.m2l_src.size());
+  for (int A = 0; A < L.ncells; ++A)
+    for (int q = L.m2l_ptr[A]; q < L.m2l_ptr[A + 1]; ++q) {
+      const int B = L.m2l_src[q];
+      long long k[3];
+      for (int c = 0; c < 3; ++c) {
+        const double d = (L.center[4 * (size_t)A + c] - L.center[4 * (size_t)B + c]) / u;
+        k[c]           = std::llround(d);
+        if (std::fabs(d - (double)k[c]) > 1e-3 || std::llabs(k[c]) >= OFF) {
+          h_m2l_vid.clear();  // off the grid: tensors per translation
+          h_vec.clear();
+          return;
+        }
+      }
+      const long long key = (k[0] + OFF) | ((k[1] + OFF) << 21) | ((k[2] + OFF) << 42);
+      const auto it       = ids.find(key);
+      if (it == ids.end()) {
+        ids.emplace(key, (int)h_vec.size());
+        h_m2l_vid[q] = (int)h_vec.size();
+        double4_32a v;
+        v.x = (double)k[0] * u, v.y = (double)k[1] * u, v.z = (double)k[2] * u, v.w = 0.0;
+        h_vec.push_back(v);
+      } else {
+        h_m2l_vid[q] = it->second;
+      }
+    }
 }
 
 // Cuts every target leaf's source list into pieces of about `W` pairs so that
@@ -397,6 +441,10 @@ void Geometry::upload(cudaStream_t s) {
   items.upload(h_items, s);
   item_split.upload(h_item_split, s);
   leaf_nslot.upload(h_leaf_nslot, s);
+  if (!h_vec.empty()) {
+    m2l_vid.upload(h_m2l_vid, s);
+    vec.upload(h_vec, s);
+  }
   if (!h_leaf_seg.empty()) leaf_seg.upload(h_leaf_seg, s);
   if (!h_cell_seg.empty()) cell_seg.upload(h_cell_seg, s);
   if (!h_p2m_tasks.empty()) p2m_tasks.upload(h_p2m_tasks, s);
@@ -1749,17 +1797,27 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
     mark(1);
     w.Lpart.alloc((size_t)std::max<size_t>(1, g.h_m2l_chunks.size()) * ov.lsize);
     bool m2l_done = false;
+    // tabulated tensors of the distinct M2L vectors (fixed orders): in FP64
+    // and double-float, where the recurrence is the expensive part; the FP32
+    // translation builds its tensor in registers faster than it loads one
+    const T* dtab_t = nullptr;
+    if constexpr (std::is_same<T, double>::value)
+      if (fixedP && M2L_TABLE_FP64)
+        dtab_t = static_cast<const T*>(m2l_dtab<T>(g, ov.m, ov.p, w, false, fs));
     if constexpr (std::is_same<T, double>::value) {
       if (near_mode == NEAR_DD) {
         w.Mdd.alloc((size_t)std::max(1, tv.ncells) * mst);
+        const float2* dtdd =
+              static_cast<const float2*>(m2l_dtab<T>(g, ov.m, ov.p, w, true, fs));
         m2l_done = launch_m2l_dd(tv, ov.m, ov.p, g.m2l_chunks.p, (int)g.h_m2l_chunks.size(),
                                  g.cell_chunk_ptr.p, w.M.p, mst, w.Mdd.p, w.Lpart.p, w.L.p,
-                                 ov.lsize, fs);
+                                 ov.lsize, fs, dtdd, dtdd ? g.m2l_vid.p : nullptr);
       }
     }
     if (m2l_done ||
         launch_m2l_fixed<T>(tv, ov.m, ov.p, g.m2l_chunks.p, (int)g.h_m2l_chunks.size(),
-                            g.cell_chunk_ptr.p, w.M.p, w.Lpart.p, w.L.p, ov.lsize, fs, cseg, seg_done)) {
+                            g.cell_chunk_ptr.p, w.M.p, w.Lpart.p, w.L.p, ov.lsize, fs, cseg,
+                            seg_done, dtab_t, dtab_t ? g.m2l_vid.p : nullptr)) {
     } else {
       size_t smem = (size_t)(ov.nm2l_terms + 9 * ov.nt) * sizeof(int);
       smem        = (smem + 15) & ~(size_t)15;

@@ -104,6 +104,19 @@ struct Geometry {
   std::vector<int> h_leaf_nslot, h_leaf_split, h_item_split;
   DBuf<int4> items;
   DBuf<int> leaf_nslot, item_split;
+  // Distinct M2L translation vectors.  Cell centres lie on the tree's grid,
+  // so the centre differences of the M2L list entries take few distinct
+  // values (about 5,000 for 300,000 sites against 14.7 M entries): m2l_vid
+  // gives each list entry's vector, vec the vectors, and the derivative
+  // tensors of 1/R are tabulated once per vector (FieldWork::dtab*).  Empty
+  // where the lists come from several trees (a batch) or a difference is off
+  // the grid: the M2L then builds each tensor itself.
+  std::vector<int> h_m2l_vid;
+  std::vector<double4_32a> h_vec;
+  DBuf<int> m2l_vid;
+  DBuf<double4_32a> vec;
+  void make_vectors();
+
   // Segment of each leaf and cell where several systems share one geometry
   // (a batch; empty otherwise): an evaluation given the segments' done flags
   // skips the near-field items, leaf multipoles and M2L chunks of finished
@@ -173,6 +186,10 @@ struct FieldWork {
   DBuf<T> M, L, Fnear, Mpart, Lleaf, Lpart;
   DBuf<float2> dd_src;  // double-float copy of the sources (double-float pass)
   DBuf<float2> Mdd;     // double-float copy of the multipoles (double-float M2L)
+  // derivative tensors of the geometry's M2L vectors, in T and in
+  // double-float (built on first use)
+  DBuf<T> dtab;
+  DBuf<float2> dtab_dd;
 };
 
 // Output modes of the finishing pass.

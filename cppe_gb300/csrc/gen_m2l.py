@@ -86,15 +86,37 @@ def emit(m, p):
         if t2 and o > 1:
             expr += f" + T({o - 1}) * ({' + '.join(t2)})"
         lines.append(f"  const T D{j} = -({expr}) * ir2 * cinv<T>({o});")
+    dlines = lines[3:]  # the derivative recurrence (r2, ir2, D0 .. D{nt-1})
+    contr = []
     for k in range(moff, nterms(p)):
         ka, kb, kc = mi[k]
         ko = ka + kb + kc
-        lines.append(f"  {{ const T mk = Mb[{k - moff}];")
+        contr.append(f"  {{ const T mk = Mb[{k - moff}];")
         for nidx in range(nterms(p - ko)):
             na, nb, nc = mi[nidx]
             w = idx[(na + ka, nb + kb, nc + kc)]
-            lines.append(f"    acc[{nidx}] = fma(D{w}, mk, acc[{nidx}]);")
-        lines.append("  }")
+            contr.append(f"    acc[{nidx}] = fma(D{w}, mk, acc[{nidx}]);")
+        contr.append("  }")
+    lines += contr
+    lines.append("}")
+    # the derivative tensor alone (tabulated once per distinct translation
+    # vector) and the contraction with a tabulated tensor
+    nt = nterms(p)
+    lines.append(f"// derivative tensor D_j = d^j (1/R), j < {nt}, of M2L m{m} p{p}")
+    lines.append("template <typename T>")
+    lines.append(f"__device__ __forceinline__ void dtensor_m{m}_p{p}(T x, T y, T z, "
+                 "T* __restrict__ Dout) {")
+    lines += dlines
+    for j in range(nt):
+        lines.append(f"  Dout[{j}] = D{j};")
+    lines.append("}")
+    lines.append(f"// M2L m{m} p{p} with the derivative tensor read from Dt")
+    lines.append("template <typename T>")
+    lines.append(f"__device__ __forceinline__ void {name}_pre(const T* __restrict__ Dt, "
+                 "const T* __restrict__ Mb, T* __restrict__ acc) {")
+    for j in range(nt):
+        lines.append(f"  const T D{j} = Dt[{j}];")
+    lines += contr
     lines.append("}")
     return "\n".join(lines), name, ls, nterms(p) - moff
 

@@ -18,12 +18,71 @@ namespace cg {
 // generated straight-line translations (function templates + an X-macro list)
 #include "m2l_gen.cuh"
 
+constexpr int nterms_c(int p) { return p < 0 ? 0 : (p + 1) * (p + 2) * (p + 3) / 6; }
+
+// Derivative tensors of the distinct M2L vectors (Geometry::make_vectors),
+// thread per vector, in T or in double-float.
+#define CPPE_DEF_DTAB(MM, PP, NAME, NT, LS, MS)                                             \
+  template <typename T>                                                                     \
+  __global__ void k_dtab_##NAME(int nvec, const double4_32a* __restrict__ vec,              \
+                                T* __restrict__ D) {                                        \
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;                                    \
+    if (v >= nvec) return;                                                                  \
+    const double4_32a r = vec[v];                                                           \
+    dtensor_##NAME<T>((T)r.x, (T)r.y, (T)r.z, D + (size_t)v * (NT));                        \
+  }                                                                                         \
+  __global__ void k_dtab_##NAME##_dd(int nvec, const double4_32a* __restrict__ vec,         \
+                                     float2* __restrict__ D) {                              \
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;                                    \
+    if (v >= nvec) return;                                                                  \
+    const double4_32a r = vec[v];                                                           \
+    ddv t[NT];                                                                              \
+    dtensor_##NAME<ddv>(ddv(dd_from(r.x)), ddv(dd_from(r.y)), ddv(dd_from(r.z)), t);       \
+    _Pragma("unroll") for (int j = 0; j < (NT); ++j)                                        \
+          D[(size_t)v * (NT) + j] = make_float2(t[j].h, t[j].l);                            \
+  }
+CPPE_M2L_TABLES(CPPE_DEF_DTAB)
+#undef CPPE_DEF_DTAB
+
+// Builds the tensor table of g's M2L vectors for order p into w (T, or
+// double-float when dd) on first use; returns it, or null when g has no
+// vector table or no fixed-order kernel serves (m, p).
+template <typename T>
+const void* m2l_dtab(const Geometry& g, int m, int p, FieldWork<T>& w, bool dd, cudaStream_t s) {
+  const int nv = (int)g.h_vec.size();
+  if (nv == 0) return nullptr;
+  const void* out = nullptr;
+#define CPPE_BUILD_DTAB(MM, PP, NAME, NT, LS, MS)                                            \
+  if (!out && m == MM && p == PP) {                                                          \
+    const size_t cnt = (size_t)nv * (NT);                                                    \
+    if (dd) {                                                                                \
+      if (w.dtab_dd.n != cnt) {                                                              \
+        w.dtab_dd.alloc(cnt);                                                                \
+        k_dtab_##NAME##_dd<<<(nv + 63) / 64, 64, 0, s>>>(nv, g.vec.p, w.dtab_dd.p);          \
+        CG_LAUNCH();                                                                         \
+      }                                                                                      \
+      out = w.dtab_dd.p;                                                                     \
+    } else {                                                                                 \
+      if (w.dtab.n != cnt) {                                                                 \
+        w.dtab.alloc(cnt);                                                                   \
+        k_dtab_##NAME<T><<<(nv + 63) / 64, 64, 0, s>>>(nv, g.vec.p, w.dtab.p);               \
+        CG_LAUNCH();                                                                         \
+      }                                                                                      \
+      out = w.dtab.p;                                                                        \
+    }                                                                                        \
+  }
+  CPPE_M2L_TABLES(CPPE_BUILD_DTAB)
+#undef CPPE_BUILD_DTAB
+  return out;
+}
+
 #define CPPE_DEF_M2L_KERNEL(M, P, NAME, LS, MS)                                            \
-  template <typename T>                                                                    \
+  template <typename T, bool PRE>                                                          \
   __global__ void __launch_bounds__(128, sizeof(T) == 4 ? ((P) == 5 ? 4 : 3) : 1)          \
         k_##NAME(TreeView tv, const int4* __restrict__ chunks, int nchunks,                \
                  const T* __restrict__ Mexp, T* __restrict__ Lpart,                        \
-                 const int* __restrict__ cell_seg, const int* __restrict__ seg_done) {     \
+                 const int* __restrict__ cell_seg, const int* __restrict__ seg_done,       \
+                 const T* __restrict__ Dtab, const int* __restrict__ vid) {                \
     const int lane = threadIdx.x & 31;                                                     \
     const int w    = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;                         \
     if (w >= nchunks) return;                                                              \
@@ -34,11 +93,17 @@ namespace cg {
     _Pragma("unroll") for (int q = 0; q < LS; ++q) acc[q] = T(0);                          \
     const double4_32a cA = tv.center[A];                                                   \
     for (int idx = ch.y + lane; idx < ch.z; idx += 32) {                                   \
-      const int B          = tv.m2l_src[idx];                                              \
-      const double4_32a cB = tv.center[B];                                                 \
+      const int B = tv.m2l_src[idx];                                                       \
       const T* Mb = static_cast<const T*>(                                                 \
             __builtin_assume_aligned(Mexp + (size_t)B * m_stride(MS), 16));                \
-      NAME<T>((T)(cA.x - cB.x), (T)(cA.y - cB.y), (T)(cA.z - cB.z), Mb, acc);              \
+      if constexpr (PRE) {                                                                 \
+        const T* Dv = static_cast<const T*>(                                               \
+              __builtin_assume_aligned(Dtab + (size_t)vid[idx] * nterms_c(P), 16));        \
+        NAME##_pre<T>(Dv, Mb, acc);                                                        \
+      } else {                                                                             \
+        const double4_32a cB = tv.center[B];                                               \
+        NAME<T>((T)(cA.x - cB.x), (T)(cA.y - cB.y), (T)(cA.z - cB.z), Mb, acc);            \
+      }                                                                                    \
     }                                                                                      \
     _Pragma("unroll") for (int q = 0; q < LS; ++q) {                                       \
       T v = acc[q];                                                                        \
@@ -62,7 +127,6 @@ CPPE_M2L_GENERATED(CPPE_DEF_M2L_KERNEL)
 // slice of shared memory (a row of nterms(p) | 1 pairs: conflict-free), then
 // adds D_{n+k} M_k over the multipole coefficients k, order by order, with
 // the local coefficients n unrolled into registers.
-constexpr int nterms_c(int p) { return p < 0 ? 0 : (p + 1) * (p + 2) * (p + 3) / 6; }
 // first w-table entry of the multipole coefficients of order ko
 constexpr int m2l_wbase(int m, int p, int ko) {
   int b = 0;
@@ -91,7 +155,8 @@ __device__ __forceinline__ void m2l_contract_dd(const float2* __restrict__ D,
 #define CPPE_DEF_M2L_DD_KERNEL(MM, PP, NAME, NT, LS, MS)                                    \
   __global__ void __launch_bounds__(64)                                                     \
         k_m2l_##NAME##_dd(TreeView tv, const int4* __restrict__ chunks, int nchunks,        \
-                          const float2* __restrict__ Mdd, double* __restrict__ Lpart) {     \
+                          const float2* __restrict__ Mdd, double* __restrict__ Lpart,       \
+                          const float2* __restrict__ Dtab, const int* __restrict__ vid) {   \
     constexpr int DS = (NT) | 1;                                                            \
     __shared__ float2 s_D[2 * 32 * DS];                                                     \
     const int lane = threadIdx.x & 31;                                                      \
@@ -104,7 +169,20 @@ __device__ __forceinline__ void m2l_contract_dd(const float2* __restrict__ D,
     const double4_32a cA = tv.center[ch.x];                                                 \
     auto wtab = [](int i) { return (int)m2l_w_##NAME[i]; };                                 \
     for (int idx = ch.y + lane; idx < ch.z; idx += 32) {                                    \
-      const int B          = tv.m2l_src[idx];                                               \
+      const int B = tv.m2l_src[idx];                                                        \
+      const float2* Mb = static_cast<const float2*>(                                        \
+            __builtin_assume_aligned(Mdd + (size_t)B * m_stride(MS), 16));                  \
+      if (Dtab) {                                                                           \
+        /* the tabulated tensor of this entry's vector into the lane's row */               \
+        const float4* Dv = reinterpret_cast<const float4*>(Dtab + (size_t)vid[idx] * (NT)); \
+        _Pragma("unroll 6") for (int i = 0; i < (NT) / 2; ++i) {                            \
+          const float4 t = Dv[i];                                                           \
+          D[2 * i]       = make_float2(t.x, t.y);                                           \
+          D[2 * i + 1]   = make_float2(t.z, t.w);                                           \
+        }                                                                                   \
+        m2l_contract_dd<MM, PP, MM>(D, Mb, wtab, acc);                                      \
+        continue;                                                                           \
+      }                                                                                     \
       const double4_32a cB = tv.center[B];                                                  \
       const dd x = dd_from(cA.x - cB.x), y = dd_from(cA.y - cB.y), z = dd_from(cA.z - cB.z); \
       const dd r2  = dd_add(dd_add(dd_sqr(x), dd_sqr(y)), dd_sqr(z));                       \
@@ -127,8 +205,6 @@ __device__ __forceinline__ void m2l_contract_dd(const float2* __restrict__ D,
         const dd v = dd_mul(s, dd_mul(ir2, dd{c[6], c[7]}));                                \
         D[j]       = make_float2(-v.h, -v.l);                                               \
       }                                                                                     \
-      const float2* Mb = static_cast<const float2*>(                                        \
-            __builtin_assume_aligned(Mdd + (size_t)B * m_stride(MS), 16));                  \
       m2l_contract_dd<MM, PP, MM>(D, Mb, wtab, acc);                                        \
     }                                                                                       \
     double* LA = Lpart + (size_t)w * (LS);                                                  \
@@ -166,14 +242,24 @@ template <typename T>
 bool launch_m2l_fixed(const TreeView& tv, int m, int p, const int4* chunks, int nchunks,
                       const int* cell_chunk_ptr, const T* Mexp, T* Lpart, T* L, int lsize,
                       cudaStream_t s, const int* cell_seg = nullptr,
-                      const int* seg_done = nullptr) {
+                      const int* seg_done = nullptr, const T* dtab = nullptr,
+                      const int* vid = nullptr) {
   const int blocks = (int)(((long)std::max(1, nchunks) * 32 + 127) / 128);
   bool ok = false;
 #define CPPE_LAUNCH_M2L(MM, PP, NAME, LS, MS)                              \
   if (!ok && m == MM && p == PP) {                                         \
     if (nchunks > 0) {                                                     \
-      k_##NAME<T><<<blocks, 128, 0, s>>>(tv, chunks, nchunks, Mexp, Lpart,  \
-                                         cell_seg, seg_done);                \
+      bool pre = false;                                                    \
+      if constexpr (sizeof(T) == 8) {                                      \
+        if (dtab) {                                                        \
+          k_##NAME<T, true><<<blocks, 128, 0, s>>>(tv, chunks, nchunks,      \
+                Mexp, Lpart, cell_seg, seg_done, dtab, vid);                 \
+          pre = true;                                                      \
+        }                                                                  \
+      }                                                                    \
+      if (!pre)                                                            \
+        k_##NAME<T, false><<<blocks, 128, 0, s>>>(tv, chunks, nchunks, Mexp, \
+              Lpart, cell_seg, seg_done, nullptr, nullptr);                  \
       CG_LAUNCH();                                                         \
     }                                                                      \
     ok = true;                                                             \
@@ -195,7 +281,8 @@ bool launch_m2l_fixed(const TreeView& tv, int m, int p, const int4* chunks, int 
 __global__ void k_split_dd_vec(long n, const double* __restrict__ in, float2* __restrict__ out);
 inline bool launch_m2l_dd(const TreeView& tv, int m, int p, const int4* chunks, int nchunks,
                           const int* cell_chunk_ptr, const double* Mexp, int msize,
-                          float2* Mdd, double* Lpart, double* L, int lsize, cudaStream_t s) {
+                          float2* Mdd, double* Lpart, double* L, int lsize, cudaStream_t s,
+                          const float2* dtab = nullptr, const int* vid = nullptr) {
   bool ok = false;
   const long nm = (long)tv.ncells * msize;
 #define CPPE_LAUNCH_M2L_DD(MM, PP, NAME, NT, LS, MS)                                       \
@@ -204,7 +291,7 @@ inline bool launch_m2l_dd(const TreeView& tv, int m, int p, const int4* chunks, 
       k_split_dd_vec<<<(unsigned)((nm + 255) / 256), 256, 0, s>>>(nm, Mexp, Mdd);          \
       CG_LAUNCH();                                                                         \
       k_m2l_##NAME##_dd<<<(unsigned)(((long)nchunks * 32 + 63) / 64), 64, 0, s>>>(         \
-            tv, chunks, nchunks, Mdd, Lpart);                                              \
+            tv, chunks, nchunks, Mdd, Lpart, dtab, vid);                                   \
       CG_LAUNCH();                                                                         \
     }                                                                                      \
     ok = true;                                                                             \

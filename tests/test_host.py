@@ -183,7 +183,7 @@ def _straight_line_m2l(gen, m, p, x, y, z, Mb):
     m2l_gen.cuh) in FP64 by rewriting it as Python."""
     import re
     code, _, ls, _ = gen.emit(m, p)
-    body = code.split("{", 1)[1].rsplit("}", 1)[0]
+    body = code.split("\n}\n", 1)[0].split("{", 1)[1]  # the first function
     lines = []
     for ln in body.split("\n"):
         ln = ln.strip().replace("const T ", "").replace("cinv<T>(", "1.0/(").replace("T(", "float(")
