@@ -242,7 +242,7 @@ def _event_time(stream, fn):
     return e0.elapsed_time(e1) * 1e-3, out
 
 
-def batched_section(dev, steps, flush):
+def batched_section(dev, steps, flush, compare=True):
     """256 snapshots of 500-20,000 sites (log-uniform; direct summation below
     4,000 sites, FMM p5 above), 8 point-charge right-hand sides each, solved
     as one batch in mixed precision; against the plain FP64 GPU PCG solving the
@@ -273,6 +273,11 @@ def batched_section(dev, steps, flush):
         times.append(t)
     bst = batch.stats()
     t_batch = float(np.mean(times))
+    if not compare:
+        # the batch alone (profiling): no one-at-a-time FP64 solves
+        return {"workload": "256 snapshots x 8 RHS (batch only)", "value": t_batch, "unit": "s",
+                "fp32_applies": bst["fp32_applies"], "fp64_applies": bst["fp64_applies"],
+                "max_rnorm": bst["max_rnorm"]}
     mu = d_mu.cpu().numpy()
     # plain FP64, one segment at a time: the first right-hand side of every
     # snapshot is solved and timed; the 8 right-hand sides of a snapshot cost
@@ -601,11 +606,19 @@ def main():
                     help="time the mixed solves only (no FP64, e2e or CPU legs)")
     ap.add_argument("--apply-only", type=int, default=0, metavar="K",
                     help="run K FP32 and K FP64 operator applies and print phase timings")
+    ap.add_argument("--batch-only", action="store_true",
+                    help="time the batched solve alone (no one-at-a-time FP64 solves)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.batch_only:
+        import torch
+        torch.cuda.set_device(0)
+        flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda:0")
+        print(json.dumps({"batch_only": batched_section(0, args.steps, flush, compare=False)}),
+              flush=True)
     else:
         run_ours(args)
 
