@@ -39,6 +39,7 @@ void Geometry::combine(const std::vector<const Geometry*>& parts, int copies, Ge
   out.ncrit     = parts[0]->ncrit;
   out.damping   = parts[0]->damping;
   out.theta     = parts[0]->theta;
+  out.ncopies   = copies;
   // cells: by (level, segment, cell)
   std::vector<std::vector<int>> cmap(nseg);
   for (int s = 0; s < nseg; ++s) cmap[s].assign(parts[part_of(s)]->layout.ncells, -1);
@@ -95,6 +96,8 @@ void Geometry::combine(const std::vector<const Geometry*>& parts, int copies, Ge
       const int k = cmap[s][P.leaf_cell[a]];
       L.leaf_cell.push_back(k);
       out.h_leaf_seg.push_back(s);
+      out.h_leaf_copy.push_back(r);
+      out.h_leaf_cstride.push_back(make_int2(p->n, P.nleaves));
       L.leaf_of_cell[k] = leaf0 + a;
       L.leaf_start.push_back(site0 + P.leaf_start[a + 1]);
       for (int q = P.p2p_ptr[a]; q < P.p2p_ptr[a + 1]; ++q) L.p2p_src.push_back(leaf0 + P.p2p_src[q]);

@@ -419,9 +419,23 @@ void Geometry::make_schedules() {
     h_item_split[k] = std::max(v.y, std::min(v.z, h_leaf_split[v.x]));
     nslot           = std::max(nslot, v.w + 1);
   }
+  // a batch's copy-0 items, for the near-field pass over all its copies
+  h_mitems.clear(), h_mitem_split.clear(), h_mitem_stride.clear();
+  if (ncopies > 1 && (int)h_leaf_copy.size() == L.nleaves)
+    for (size_t k = 0; k < h_items.size(); ++k)
+      if (h_leaf_copy[h_items[k].x] == 0) {
+        h_mitems.push_back(h_items[k]);
+        h_mitem_split.push_back(h_item_split[k]);
+        h_mitem_stride.push_back(h_leaf_cstride[h_items[k].x]);
+      }
 }
 
 void Geometry::upload_schedules(cudaStream_t s) {
+  if (!h_mitems.empty()) {
+    mitems.upload(h_mitems, s);
+    mitem_split.upload(h_mitem_split, s);
+    mitem_stride.upload(h_mitem_stride, s);
+  }
   items.upload(h_items, s);
   item_split.upload(h_item_split, s);
   leaf_nslot.upload(h_leaf_nslot, s);
@@ -444,6 +458,11 @@ void Geometry::upload(cudaStream_t s) {
   if (!h_vec.empty()) {
     m2l_vid.upload(h_m2l_vid, s);
     vec.upload(h_vec, s);
+  }
+  if (!h_mitems.empty()) {
+    mitems.upload(h_mitems, s);
+    mitem_split.upload(h_mitem_split, s);
+    mitem_stride.upload(h_mitem_stride, s);
   }
   if (!h_leaf_seg.empty()) leaf_seg.upload(h_leaf_seg, s);
   if (!h_cell_seg.empty()) cell_seg.upload(h_cell_seg, s);
@@ -932,6 +951,195 @@ __global__ void __launch_bounds__(P2P_BLOCK)
         float* o = Fnear + (size_t)slot * 3 * n + 3 * (size_t)(a0 + tb + idx);
         o[0] = f0, o[1] = f1, o[2] = f2v;
       }
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Near field, FP32, dipole sources, for the right-hand sides of a batch
+// together.  A batch repeats each snapshot's geometry once per right-hand
+// side (segments s*R + r, r < R, laid out one after another: copy r of a
+// site sits `stride.x` sites, and of a leaf `stride.y` leaves, after copy 0).
+// The pair tensor (separation, 1/R powers, Thole factors) does not depend on
+// the right-hand side, so this kernel runs the items of copy 0 only and
+// applies each tensor to the R copies' source moments: about 21 of the 31
+// FP32 operations of a damped pair are shared, leaving 10 per right-hand
+// side.  Same tiles, damping split and self-pair handling as k_p2p32_m1,
+// one target per thread (the accumulators of R right-hand sides take the
+// registers of the second target).  Copies whose segments have finished
+// take no work (their output is not read); items whose copies have all
+// finished return at once.
+// ---------------------------------------------------------------------------
+constexpr int P2PM_PAIRS = 144;  // staged source pairs per tile
+constexpr int P2PM_MAXR  = 8;    // right-hand sides per launch
+template <bool DAMP>
+__global__ void __launch_bounds__(P2P_BLOCK)
+      k_p2p32_m1_multi(int n, const int* __restrict__ leaf_start, const int4* __restrict__ items,
+                       const int* __restrict__ item_split, const int2* __restrict__ item_stride,
+                       int nr, const int* __restrict__ p2p_src, const float4* __restrict__ hi,
+                       const float4* __restrict__ lo, const float* __restrict__ src,
+                       float damping, float* __restrict__ Fnear, const int* __restrict__ leaf_seg,
+                       const int* __restrict__ seg_done) {
+  constexpr int TILE = 2 * P2PM_PAIRS;
+  constexpr int R    = P2PM_MAXR;
+  __shared__ float4 s_xy[P2PM_PAIRS];       // x_j, x_j+1, y_j, y_j+1
+  __shared__ float4 s_zs[P2PM_PAIRS];       // z_j, z_j+1, s_j, s_j+1
+  __shared__ float4 s_mxy[P2PM_PAIRS * R];  // per copy: mx_j, mx_j+1, my_j, my_j+1
+  __shared__ float2 s_mz[P2PM_PAIRS * R];   // per copy: mz_j, mz_j+1
+  __shared__ int s_site[TILE];              // copy-0 site of each tile slot
+  __shared__ TilePlan s_plan;
+  __shared__ float s_red[P2P_BLOCK * 3 * R];
+
+  const int4 it = items[blockIdx.x];
+  const int A = it.x, b0 = it.y, b1 = it.z, slot = it.w;
+  const int2 st = item_stride[blockIdx.x];  // sites, leaves between copies
+  // copies still iterating (bit r); finished copies take no work
+  unsigned live = 0;
+  for (int r = 0; r < nr; ++r)
+    if (!seg_done || seg_done[leaf_seg[A + r * st.y]] == 0) live |= 1u << r;
+  if (!live) return;
+  const int sp = item_split[blockIdx.x];
+  const int a0 = leaf_start[A], nA = leaf_start[A + 1] - a0;
+  const float4 oh = hi[a0], ol = lo[a0];
+  auto rel = [&](int k) {
+    const float4 h = hi[k], l = lo[k];
+    return make_float4((h.x - oh.x) + (l.x - ol.x), (h.y - oh.y) + (l.y - ol.y),
+                       (h.z - oh.z) + (l.z - ol.z), h.w > 0.f ? h.w : 1e15f);
+  };
+
+  for (int tb = 0; tb < nA; tb += P2P_BLOCK) {
+    const int nT = min(P2P_BLOCK, nA - tb);
+    const int S  = P2P_BLOCK / nT;  // groups of nT threads
+    const int t = threadIdx.x % nT, g = threadIdx.x / nT;
+    const bool active = g < S;
+    float2 nX, nY, nZ, AI;
+    {
+      const float4 m = rel(a0 + tb + t);
+      nX = f2(-m.x), nY = f2(-m.y), nZ = f2(-m.z);
+      AI = f2(-1.4426950408889634f * damping * m.w);
+    }
+    Comp3<float> acc[R];
+    for (int ph = 0; ph < 2; ++ph) {
+      const int pend = ph == 0 ? sp : b1;
+      if (threadIdx.x == 0) s_plan.cur = ph == 0 ? b0 : sp, s_plan.coff = 0;
+      __syncthreads();
+      while (true) {
+        if (threadIdx.x < 32) plan_tile<TILE>(s_plan, pend, p2p_src, leaf_start);
+        __syncthreads();
+        const int np = s_plan.np;
+        if (np == 0) break;
+        const int total  = s_plan.poff[np];
+        const int npairs = (total + 1) >> 1;
+        for (int q = threadIdx.x; q < npairs; q += P2P_BLOCK) {
+          const int j0    = tile_site(s_plan, 2 * q);
+          const float4 r0 = rel(j0);
+          // an odd tile ends with a source of zero moment far from the leaf
+          const bool two  = 2 * q + 1 < total;
+          const int j1    = two ? tile_site(s_plan, 2 * q + 1) : j0;
+          const float4 r1 = two ? rel(j1) : make_float4(1e4f, 0.f, 0.f, 1.f);
+          s_xy[q] = make_float4(r0.x, r1.x, r0.y, r1.y);
+          s_zs[q] = make_float4(r0.z, r1.z, r0.w, r1.w);
+          s_site[2 * q]     = j0;
+          s_site[2 * q + 1] = two ? j1 : -1;
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < npairs * nr; e += P2P_BLOCK) {
+          const int q = e / nr, r = e - q * nr;
+          if (!((live >> r) & 1u)) continue;
+          const float* m0 = src + 3 * ((size_t)s_site[2 * q] + (size_t)r * st.x);
+          float mx1 = 0.f, my1 = 0.f, mz1 = 0.f;
+          if (s_site[2 * q + 1] >= 0) {
+            const float* m1 = src + 3 * ((size_t)s_site[2 * q + 1] + (size_t)r * st.x);
+            mx1 = m1[0], my1 = m1[1], mz1 = m1[2];
+          }
+          s_mxy[q * R + r] = make_float4(m0[0], mx1, m0[1], my1);
+          s_mz[q * R + r]  = make_float2(m0[2], mz1);
+        }
+        __syncthreads();
+        if (active) {
+          float2 FX[R], FY[R], FZ[R];
+#pragma unroll
+          for (int r = 0; r < R; ++r) FX[r] = FY[r] = FZ[r] = f2(0.f);
+          auto sweep = [&](auto damped) {
+            constexpr bool D = decltype(damped)::value;
+#pragma unroll 1
+            for (int jj = g; jj < npairs; jj += S) {
+              const float4 xy = s_xy[jj], zs = s_zs[jj];
+              const float2 x  = __fadd2_rn(make_float2(xy.x, xy.y), nX);
+              const float2 y  = __fadd2_rn(make_float2(xy.z, xy.w), nY);
+              const float2 z  = __fadd2_rn(make_float2(zs.x, zs.y), nZ);
+              const float2 r2 = __ffma2_rn(x, x, __ffma2_rn(y, y, __fmul2_rn(z, z)));
+              float2 ir;
+              if (D) {
+                ir.x = fminf(rsqrt_approx(r2.x), 1e4f);
+                ir.y = fminf(rsqrt_approx(r2.y), 1e4f);
+              } else {
+                ir.x = r2.x > 0.f ? rsqrt_approx(r2.x) : 0.f;
+                ir.y = r2.y > 0.f ? rsqrt_approx(r2.y) : 0.f;
+              }
+              const float2 ir2 = __fmul2_rn(ir, ir);
+              const float2 ir3 = __fmul2_rn(ir2, ir);
+              const float2 ir5 = __fmul2_rn(ir3, ir2);
+              float2 Af, Bn;
+              if (D) {
+                float2 tt = __fmul2_rn(__fmul2_rn(AI, make_float2(zs.z, zs.w)), __fmul2_rn(r2, ir));
+                tt.x = fmaxf(tt.x, -126.f);
+                tt.y = fmaxf(tt.y, -126.f);
+                const float2 e  = make_float2(ex2_approx(tt.x), ex2_approx(tt.y));
+                const float2 np2 = __ffma2_rn(tt, __ffma2_rn(tt, f2(-LN2SQ_2), f2(LN2)), f2(-1.f));
+                const float2 q3 = __ffma2_rn(
+                      tt, __ffma2_rn(tt, __ffma2_rn(tt, f2(-LN2CU_2), f2(LN2SQ_3_2)), f2(-3.f * LN2)),
+                      f2(3.f));
+                Af = __fmul2_rn(ir3, __ffma2_rn(np2, e, f2(1.f)));
+                Bn = __fmul2_rn(ir5, __ffma2_rn(q3, e, f2(-3.f)));
+              } else {
+                Af = ir3;
+                Bn = __fmul2_rn(ir5, f2(-3.f));
+              }
+#pragma unroll
+              for (int r = 0; r < R; ++r) {
+                if ((live >> r) & 1u) {
+                  const float4 mxy = s_mxy[jj * R + r];
+                  const float2 mz  = s_mz[jj * R + r];
+                  const float2 mx = make_float2(mxy.x, mxy.y), my = make_float2(mxy.z, mxy.w);
+                  const float2 md = __ffma2_rn(mx, x, __ffma2_rn(my, y, __fmul2_rn(mz, z)));
+                  const float2 nC = __fmul2_rn(md, Bn);
+                  FX[r] = __ffma2_rn(x, nC, __ffma2_rn(mx, Af, FX[r]));
+                  FY[r] = __ffma2_rn(y, nC, __ffma2_rn(my, Af, FY[r]));
+                  FZ[r] = __ffma2_rn(z, nC, __ffma2_rn(mz, Af, FZ[r]));
+                }
+              }
+            }
+          };
+          if (DAMP && ph == 0)
+            sweep(std::true_type{});
+          else
+            sweep(std::false_type{});
+#pragma unroll
+          for (int r = 0; r < R; ++r)
+            acc[r].add(FX[r].x + FX[r].y, FY[r].x + FY[r].y, FZ[r].x + FZ[r].y);
+        }
+        __syncthreads();
+      }
+    }
+    if (active) {
+      float* rr = &s_red[(g * nT + t) * 3 * R];
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+        rr[3 * r] = acc[r].gx(), rr[3 * r + 1] = acc[r].gy(), rr[3 * r + 2] = acc[r].gz();
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nT * nr; e += P2P_BLOCK) {
+      const int i = e / nr, r = e - i * nr;
+      if (!((live >> r) & 1u)) continue;
+      float f0 = 0.f, f1 = 0.f, f2v = 0.f;
+      for (int gg = 0; gg < S; ++gg) {
+        const float* rr = &s_red[(gg * nT + i) * 3 * R + 3 * r];
+        f0 += rr[0], f1 += rr[1], f2v += rr[2];
+      }
+      float* o = Fnear + (size_t)slot * 3 * n + 3 * ((size_t)a0 + tb + i + (size_t)r * st.x);
+      o[0] = f0, o[1] = f1, o[2] = f2v;
     }
     __syncthreads();
   }
@@ -1643,6 +1851,20 @@ static void launch_p2p(const Geometry& g, bool damp, bool fast, const T* src, T 
   const int* lseg = seg_done ? g.leaf_seg.p : nullptr;
   if (seg_done && !lseg) fail(CPPE_GPU_INVALID_ARG, "segment mask without segments");
   if constexpr (std::is_same<T, float>::value && M == 1) {
+    if (!g.h_mitems.empty() && g.ncopies > 1 && g.ncopies <= P2PM_MAXR) {
+      // a batch's right-hand sides together
+      const int mg = (int)g.h_mitems.size();
+      if (damp)
+        k_p2p32_m1_multi<true><<<mg, P2P_BLOCK, 0, s>>>(
+              g.n, g.leaf_start.p, g.mitems.p, g.mitem_split.p, g.mitem_stride.p, g.ncopies,
+              g.p2p_src.p, g.hi32.p, g.lo32.p, src, damping, Fnear, lseg, seg_done);
+      else
+        k_p2p32_m1_multi<false><<<mg, P2P_BLOCK, 0, s>>>(
+              g.n, g.leaf_start.p, g.mitems.p, g.mitem_split.p, g.mitem_stride.p, g.ncopies,
+              g.p2p_src.p, g.hi32.p, g.lo32.p, src, damping, Fnear, lseg, seg_done);
+      CG_LAUNCH();
+      return;
+    }
     if (damp)
       k_p2p32_m1<true><<<grid, P2P_BLOCK, 0, s>>>(
             g.n, g.leaf_start.p, g.items.p, g.item_split.p, g.p2p_src.p, g.hi32.p, g.lo32.p, src,

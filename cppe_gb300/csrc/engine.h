@@ -117,6 +117,20 @@ struct Geometry {
   DBuf<double4_32a> vec;
   void make_vectors();
 
+  // Batches whose snapshots repeat once per right-hand side (ncopies):
+  // the copy of each leaf's segment, the sites and leaves between copies,
+  // and the items of the copy-0 leaves, which one near-field pass runs for
+  // every copy (k_p2p32_m1_multi).
+  int ncopies = 1;
+  std::vector<int> h_leaf_copy;
+  std::vector<int2> h_leaf_cstride;
+  std::vector<int4> h_mitems;
+  std::vector<int> h_mitem_split;
+  std::vector<int2> h_mitem_stride;
+  DBuf<int4> mitems;
+  DBuf<int> mitem_split;
+  DBuf<int2> mitem_stride;
+
   // Segment of each leaf and cell where several systems share one geometry
   // (a batch; empty otherwise): an evaluation given the segments' done flags
   // skips the near-field items, leaf multipoles and M2L chunks of finished
