@@ -1332,6 +1332,206 @@ __global__ void __launch_bounds__(P2P_BLOCK)
 }
 
 // ---------------------------------------------------------------------------
+// Double-float near field over a batch's right-hand sides together (the
+// residual counterpart of k_p2p32_m1_multi): the pair tensor G1 I + G2 r r^T
+// in double-float (separation, 1/R powers, Thole factors) once per pair,
+// applied to the source moments of every copy.  Same arithmetic per term as
+// dd2_pair_m1; one target per thread with R packed accumulators; the
+// per-copy sums are reduced and written one copy at a time.
+// ---------------------------------------------------------------------------
+template <bool DAMP, int MODE>
+__device__ __forceinline__ void dd2_pair_tensor(const dd2& tx, const dd2& ty, const dd2& tz,
+                                                const dd2& ai, const dd2& qx, const dd2& qy,
+                                                const dd2& qz, const dd2& qs, const float* eh,
+                                                const float* el, dd2& x, dd2& y, dd2& z,
+                                                dd2& G1, dd2& G2) {
+  x = {psub(tx.h, qx.h), psub(tx.l, qx.l)};
+  y = {psub(ty.h, qy.h), psub(ty.l, qy.l)};
+  z = {psub(tz.h, qz.h), psub(tz.l, qz.l)};
+  const dd2 r2 = dd2_add(dd2_add_lazy(dd2_sqr_full(x), dd2_sqr_full(y)), dd2_sqr_full(z));
+  const bool okx = r2.h.x > 0.f, oky = r2.h.y > 0.f;  // false: a site paired with itself
+  const dd2 zero = {p2(0.f), p2(0.f)};
+  const dd2 ir   = dd2_sel(okx, oky, dd2_rsqrt(dd2_sel(okx, oky, r2, {p2(1.f), p2(0.f)})), zero);
+  const dd2 ir2  = dd2_sqr(ir);
+  const dd2 ir3  = dd2_mul(ir2, ir);
+  G1 = dd2_neg(ir3);
+  G2 = dd2_mul_f(dd2_mul(ir3, ir2), p2(3.f));
+  if (DAMP && MODE < 2) {
+    const dd2 a   = dd2_mul(ai, qs);
+    const dd2 v   = dd2_mul(a, dd2_mul(r2, ir));
+    const bool dx = a.h.x > 0.f && v.h.x < 50.f, dy = a.h.y > 0.f && v.h.y < 50.f;
+    const float2 e32 = make_float2(expf(-v.h.x), expf(-v.h.y));
+    const float2 u32 = pmul(pfma(v.h, pfma(v.h, p2(0.5f), p2(1.f)), p2(1.f)), e32);
+    const float2 w32 = pmul(pmul(pmul(pmul(v.h, v.h), v.h), p2(1.f / 6.f)), e32);
+    dd2 fE = dd2_fast_two_sum(p2(1.f), pneg(u32));
+    dd2 fT = dd2_fast_two_sum(p2(1.f), pneg(padd(u32, w32)));
+    const bool sx = MODE == 0 && v.h.x < 20.f, sy = MODE == 0 && v.h.y < 20.f;
+    if (sx || sy) {
+      const dd2 vc  = dd2_sel(sx, sy, v, zero);
+      const dd2 e   = dd2_exp_neg(vc, eh, el);
+      const dd2 v2  = dd2_sqr(vc);
+      const dd2 u   = dd2_add(dd2_two_sum(p2(1.f), vc.h),
+                              {pmul(p2(0.5f), v2.h), pfma(p2(0.5f), v2.l, vc.l)});
+      const dd2 w   = dd2_mul(dd2_mul(v2, vc), {p2(1.f / 6.f), p2(DD_SIXTH_LO)});
+      const dd2 fEd = dd2_add(dd2{p2(1.f), p2(0.f)}, dd2_neg(dd2_mul(u, e)));
+      const dd2 fTd = dd2_add(fEd, dd2_neg(dd2_mul(w, e)));
+      fE = dd2_sel(sx, sy, fEd, fE);
+      fT = dd2_sel(sx, sy, fTd, fT);
+    }
+    G1 = dd2_sel(dx, dy, dd2_mul(G1, fE), G1);
+    G2 = dd2_sel(dx, dy, dd2_mul(G2, fT), G2);
+  }
+}
+
+constexpr int P2PM_DD_PAIRS = 80;  // staged source pairs per tile (160 sources)
+template <bool DAMP>
+__global__ void __launch_bounds__(P2P_BLOCK)
+      k_p2p_dd2_multi(int n, const int* __restrict__ leaf_start, const int4* __restrict__ items,
+                      const int* __restrict__ item_split, const int2* __restrict__ item_stride,
+                      int nr, const int* __restrict__ p2p_src, PosArgs<float> pa,
+                      const float2* __restrict__ src, const float2* __restrict__ etab,
+                      double damping, double* __restrict__ Fnear) {
+  constexpr int TILE = 2 * P2PM_DD_PAIRS;
+  constexpr int R    = P2PM_MAXR;
+  __shared__ float4 s_g[4][P2PM_DD_PAIRS];       // positions (high, low) and s
+  __shared__ float4 s_m[3][P2PM_DD_PAIRS * R];   // per copy: the moments' pairs
+  __shared__ int s_site[TILE];
+  __shared__ float s_eh[DD_EXP_TAB], s_el[DD_EXP_TAB];
+  __shared__ TilePlan s_plan;
+  __shared__ double s_red[P2P_BLOCK * 3];
+
+  for (int k = threadIdx.x; k < DD_EXP_TAB; k += P2P_BLOCK) {
+    const float2 e = etab[k];
+    s_eh[k] = e.x, s_el[k] = e.y;
+  }
+  const int4 it = items[blockIdx.x];
+  const int A = it.x, b0 = it.y, b1 = it.z, slot = it.w;
+  const int2 st = item_stride[blockIdx.x];
+  const int sp  = item_split[blockIdx.x];
+  const int a0 = leaf_start[A], nA = leaf_start[A + 1] - a0;
+  const dd dmp = dd_from(damping);
+
+  for (int tb = 0; tb < nA; tb += P2P_BLOCK) {
+    const int nT = min(P2P_BLOCK, nA - tb);
+    const int S  = P2P_BLOCK / nT;
+    const int t = threadIdx.x % nT, g = threadIdx.x / nT;
+    const bool active = g < S;
+    const SiteRec<float> me = pa.load(a0 + tb + t);
+    const dd2 tx = {p2(me.x), p2(me.lx)}, ty = {p2(me.y), p2(me.ly)}, tz = {p2(me.z), p2(me.lz)};
+    const dd ai1 = dd_mul(dmp, dd{me.s, me.ls});
+    const dd2 ai = {p2(ai1.h), p2(ai1.l)};
+    const dd2 zero = {p2(0.f), p2(0.f)};
+    dd2 f[R][3];
+#pragma unroll
+    for (int r = 0; r < R; ++r) f[r][0] = f[r][1] = f[r][2] = zero;
+    for (int ph = 0; ph < 2; ++ph) {
+      const int pend = ph == 0 ? sp : b1;
+      if (threadIdx.x == 0) s_plan.cur = ph == 0 ? b0 : sp, s_plan.coff = 0;
+      __syncthreads();
+      while (true) {
+        if (threadIdx.x < 32) plan_tile<TILE>(s_plan, pend, p2p_src, leaf_start);
+        __syncthreads();
+        const int np = s_plan.np;
+        if (np == 0) break;
+        const int total  = s_plan.poff[np];
+        const int npairs = (total + 1) >> 1;
+        for (int q = threadIdx.x; q < npairs; q += P2P_BLOCK) {
+          const int j0 = tile_site(s_plan, 2 * q);
+          const SiteRec<float> r0 = pa.load(j0);
+          // an odd tile ends with a source of zero moment far from the leaf
+          SiteRec<float> r1 = r0;
+          r1.x += 1e4f, r1.s = 1.f, r1.ls = 0.f;
+          int j1 = -1;
+          if (2 * q + 1 < total) j1 = tile_site(s_plan, 2 * q + 1), r1 = pa.load(j1);
+          s_g[0][q] = make_float4(r0.x, r1.x, r0.y, r1.y);
+          s_g[1][q] = make_float4(r0.z, r1.z, r0.s, r1.s);
+          s_g[2][q] = make_float4(r0.lx, r1.lx, r0.ly, r1.ly);
+          s_g[3][q] = make_float4(r0.lz, r1.lz, r0.ls, r1.ls);
+          s_site[2 * q] = j0, s_site[2 * q + 1] = j1;
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < npairs * nr; e += P2P_BLOCK) {
+          const int q = e / nr, r = e - q * nr;
+          const float2* m0 = src + 3 * ((size_t)s_site[2 * q] + (size_t)r * st.x);
+          float2 m1x = make_float2(0.f, 0.f), m1y = m1x, m1z = m1x;
+          if (s_site[2 * q + 1] >= 0) {
+            const float2* m1 = src + 3 * ((size_t)s_site[2 * q + 1] + (size_t)r * st.x);
+            m1x = m1[0], m1y = m1[1], m1z = m1[2];
+          }
+          const float2 m0x = m0[0], m0y = m0[1], m0z = m0[2];
+          // {mx.h pair, my.h pair}, {mz.h pair, mx.l pair}, {my.l pair, mz.l pair}
+          s_m[0][q * R + r] = make_float4(m0x.x, m1x.x, m0y.x, m1y.x);
+          s_m[1][q * R + r] = make_float4(m0z.x, m1z.x, m0x.y, m1x.y);
+          s_m[2][q * R + r] = make_float4(m0y.y, m1y.y, m0z.y, m1z.y);
+        }
+        __syncthreads();
+        if (active) {
+          auto sweep = [&](auto mode) {
+            constexpr int MD = decltype(mode)::value;
+#pragma unroll 1
+            for (int jj = g; jj < npairs; jj += S) {
+              const float4 A0 = s_g[0][jj], B0 = s_g[1][jj], C0 = s_g[2][jj], D0 = s_g[3][jj];
+              const dd2 qx = {make_float2(A0.x, A0.y), make_float2(C0.x, C0.y)};
+              const dd2 qy = {make_float2(A0.z, A0.w), make_float2(C0.z, C0.w)};
+              const dd2 qz = {make_float2(B0.x, B0.y), make_float2(D0.x, D0.y)};
+              const dd2 qs = {make_float2(B0.z, B0.w), make_float2(D0.z, D0.w)};
+              dd2 x, y, z, G1, G2;
+              dd2_pair_tensor<DAMP, MD>(tx, ty, tz, ai, qx, qy, qz, qs, s_eh, s_el, x, y, z, G1,
+                                        G2);
+#pragma unroll
+              for (int r = 0; r < R; ++r) {
+                if (r < nr) {
+                  const float4 E0 = s_m[0][jj * R + r], F0 = s_m[1][jj * R + r],
+                               G0 = s_m[2][jj * R + r];
+                  const dd2 mx = {make_float2(E0.x, E0.y), make_float2(F0.z, F0.w)};
+                  const dd2 my = {make_float2(E0.z, E0.w), make_float2(G0.x, G0.y)};
+                  const dd2 mz = {make_float2(F0.x, F0.y), make_float2(G0.z, G0.w)};
+                  const dd2 mr =
+                        dd2_add(dd2_add_lazy(dd2_mul(mx, x), dd2_mul(my, y)), dd2_mul(mz, z));
+                  const dd2 sg = dd2_mul(mr, G2);
+                  f[r][0] = dd2_add_lazy(f[r][0], dd2_neg(dd2_add_lazy(dd2_mul(mx, G1), dd2_mul(sg, x))));
+                  f[r][1] = dd2_add_lazy(f[r][1], dd2_neg(dd2_add_lazy(dd2_mul(my, G1), dd2_mul(sg, y))));
+                  f[r][2] = dd2_add_lazy(f[r][2], dd2_neg(dd2_add_lazy(dd2_mul(mz, G1), dd2_mul(sg, z))));
+                }
+              }
+            }
+          };
+          if (!DAMP || ph == 0)
+            sweep(std::integral_constant<int, 0>{});
+          else
+            sweep(std::integral_constant<int, 1>{});
+        }
+        __syncthreads();
+      }
+    }
+    // one copy at a time through the reduction buffer
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      if (r >= nr) break;
+      if (active) {
+        double* rr = &s_red[(g * nT + t) * 3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const dd h0 = {f[r][c].h.x, f[r][c].l.x}, h1 = {f[r][c].h.y, f[r][c].l.y};
+          rr[c] = dd_to(dd_add(h0, h1));
+        }
+      }
+      __syncthreads();
+      if (threadIdx.x < nT) {
+        double o3[3] = {0, 0, 0};
+        for (int gg = 0; gg < S; ++gg)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) o3[c] += s_red[(gg * nT + threadIdx.x) * 3 + c];
+        double* o = Fnear + (size_t)slot * 3 * n +
+                    3 * ((size_t)a0 + tb + threadIdx.x + (size_t)r * st.x);
+        o[0] = o3[0], o[1] = o3[1], o[2] = o3[2];
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // FMM passes
 // ---------------------------------------------------------------------------
 template <typename T>
@@ -1937,6 +2137,20 @@ static void launch_p2p_dd(const Geometry& g, bool damp, const double* src, doubl
   w.dd_src.alloc(std::max(1L, n3));
   k_split_dd<<<(unsigned)((n3 + 255) / 256), 256, 0, s>>>(n3, src, w.dd_src.p);
   CG_LAUNCH();
+  if (!g.h_mitems.empty() && g.ncopies > 1 && g.ncopies <= P2PM_MAXR) {
+    // a batch's right-hand sides together
+    const int mg = (int)g.h_mitems.size();
+    if (damp)
+      k_p2p_dd2_multi<true><<<mg, P2P_BLOCK, 0, s>>>(
+            g.n, g.leaf_start.p, g.mitems.p, g.mitem_split.p, g.mitem_stride.p, g.ncopies,
+            g.p2p_src.p, pos_args<float>(g), w.dd_src.p, g.dd_exp.p, damping, w.Fnear.p);
+    else
+      k_p2p_dd2_multi<false><<<mg, P2P_BLOCK, 0, s>>>(
+            g.n, g.leaf_start.p, g.mitems.p, g.mitem_split.p, g.mitem_stride.p, g.ncopies,
+            g.p2p_src.p, pos_args<float>(g), w.dd_src.p, g.dd_exp.p, damping, w.Fnear.p);
+    CG_LAUNCH();
+    return;
+  }
   const int grid = (int)g.h_items.size();
   if (damp)
     k_p2p_dd2<true><<<grid, P2P_BLOCK, 0, s>>>(g.n, g.leaf_start.p, g.items.p, g.item_split.p,
