@@ -977,10 +977,10 @@ template <bool DAMP>
 __global__ void __launch_bounds__(P2P_BLOCK)
       k_p2p32_m1_multi(int n, const int* __restrict__ leaf_start, const int4* __restrict__ items,
                        const int* __restrict__ item_split, const int2* __restrict__ item_stride,
-                       int nr, const int* __restrict__ p2p_src, const float4* __restrict__ hi,
-                       const float4* __restrict__ lo, const float* __restrict__ src,
-                       float damping, float* __restrict__ Fnear, const int* __restrict__ leaf_seg,
-                       const int* __restrict__ seg_done) {
+                       int c0, int nr, const int* __restrict__ p2p_src,
+                       const float4* __restrict__ hi, const float4* __restrict__ lo,
+                       const float* __restrict__ src, float damping, float* __restrict__ Fnear,
+                       const int* __restrict__ leaf_seg, const int* __restrict__ seg_done) {
   constexpr int TILE = 2 * P2PM_PAIRS;
   constexpr int R    = P2PM_MAXR;
   __shared__ float4 s_xy[P2PM_PAIRS];       // x_j, x_j+1, y_j, y_j+1
@@ -994,10 +994,10 @@ __global__ void __launch_bounds__(P2P_BLOCK)
   const int4 it = items[blockIdx.x];
   const int A = it.x, b0 = it.y, b1 = it.z, slot = it.w;
   const int2 st = item_stride[blockIdx.x];  // sites, leaves between copies
-  // copies still iterating (bit r); finished copies take no work
+  // copies c0 .. c0 + nr - 1 of this launch; those still iterating (bit r)
   unsigned live = 0;
   for (int r = 0; r < nr; ++r)
-    if (!seg_done || seg_done[leaf_seg[A + r * st.y]] == 0) live |= 1u << r;
+    if (!seg_done || seg_done[leaf_seg[A + (c0 + r) * st.y]] == 0) live |= 1u << r;
   if (!live) return;
   const int sp = item_split[blockIdx.x];
   const int a0 = leaf_start[A], nA = leaf_start[A + 1] - a0;
@@ -1047,10 +1047,10 @@ __global__ void __launch_bounds__(P2P_BLOCK)
         for (int e = threadIdx.x; e < npairs * nr; e += P2P_BLOCK) {
           const int q = e / nr, r = e - q * nr;
           if (!((live >> r) & 1u)) continue;
-          const float* m0 = src + 3 * ((size_t)s_site[2 * q] + (size_t)r * st.x);
+          const float* m0 = src + 3 * ((size_t)s_site[2 * q] + (size_t)(c0 + r) * st.x);
           float mx1 = 0.f, my1 = 0.f, mz1 = 0.f;
           if (s_site[2 * q + 1] >= 0) {
-            const float* m1 = src + 3 * ((size_t)s_site[2 * q + 1] + (size_t)r * st.x);
+            const float* m1 = src + 3 * ((size_t)s_site[2 * q + 1] + (size_t)(c0 + r) * st.x);
             mx1 = m1[0], my1 = m1[1], mz1 = m1[2];
           }
           s_mxy[q * R + r] = make_float4(m0[0], mx1, m0[1], my1);
@@ -1138,7 +1138,7 @@ __global__ void __launch_bounds__(P2P_BLOCK)
         const float* rr = &s_red[(gg * nT + i) * 3 * R + 3 * r];
         f0 += rr[0], f1 += rr[1], f2v += rr[2];
       }
-      float* o = Fnear + (size_t)slot * 3 * n + 3 * ((size_t)a0 + tb + i + (size_t)r * st.x);
+      float* o = Fnear + (size_t)slot * 3 * n + 3 * ((size_t)a0 + tb + i + (size_t)(c0 + r) * st.x);
       o[0] = f0, o[1] = f1, o[2] = f2v;
     }
     __syncthreads();
@@ -1388,7 +1388,7 @@ template <bool DAMP>
 __global__ void __launch_bounds__(P2P_BLOCK)
       k_p2p_dd2_multi(int n, const int* __restrict__ leaf_start, const int4* __restrict__ items,
                       const int* __restrict__ item_split, const int2* __restrict__ item_stride,
-                      int nr, const int* __restrict__ p2p_src, PosArgs<float> pa,
+                      int c0, int nr, const int* __restrict__ p2p_src, PosArgs<float> pa,
                       const float2* __restrict__ src, const float2* __restrict__ etab,
                       double damping, double* __restrict__ Fnear) {
   constexpr int TILE = 2 * P2PM_DD_PAIRS;
@@ -1452,10 +1452,10 @@ __global__ void __launch_bounds__(P2P_BLOCK)
         __syncthreads();
         for (int e = threadIdx.x; e < npairs * nr; e += P2P_BLOCK) {
           const int q = e / nr, r = e - q * nr;
-          const float2* m0 = src + 3 * ((size_t)s_site[2 * q] + (size_t)r * st.x);
+          const float2* m0 = src + 3 * ((size_t)s_site[2 * q] + (size_t)(c0 + r) * st.x);
           float2 m1x = make_float2(0.f, 0.f), m1y = m1x, m1z = m1x;
           if (s_site[2 * q + 1] >= 0) {
-            const float2* m1 = src + 3 * ((size_t)s_site[2 * q + 1] + (size_t)r * st.x);
+            const float2* m1 = src + 3 * ((size_t)s_site[2 * q + 1] + (size_t)(c0 + r) * st.x);
             m1x = m1[0], m1y = m1[1], m1z = m1[2];
           }
           const float2 m0x = m0[0], m0y = m0[1], m0z = m0[2];
@@ -1523,7 +1523,7 @@ __global__ void __launch_bounds__(P2P_BLOCK)
 #pragma unroll
           for (int c = 0; c < 3; ++c) o3[c] += s_red[(gg * nT + threadIdx.x) * 3 + c];
         double* o = Fnear + (size_t)slot * 3 * n +
-                    3 * ((size_t)a0 + tb + threadIdx.x + (size_t)r * st.x);
+                    3 * ((size_t)a0 + tb + threadIdx.x + (size_t)(c0 + r) * st.x);
         o[0] = o3[0], o[1] = o3[1], o[2] = o3[2];
       }
       __syncthreads();
@@ -2051,18 +2051,21 @@ static void launch_p2p(const Geometry& g, bool damp, bool fast, const T* src, T 
   const int* lseg = seg_done ? g.leaf_seg.p : nullptr;
   if (seg_done && !lseg) fail(CPPE_GPU_INVALID_ARG, "segment mask without segments");
   if constexpr (std::is_same<T, float>::value && M == 1) {
-    if (!g.h_mitems.empty() && g.ncopies > 1 && g.ncopies <= P2PM_MAXR) {
-      // a batch's right-hand sides together
+    if (!g.h_mitems.empty() && g.ncopies > 1) {
+      // a batch's right-hand sides together, up to P2PM_MAXR per launch
       const int mg = (int)g.h_mitems.size();
-      if (damp)
-        k_p2p32_m1_multi<true><<<mg, P2P_BLOCK, 0, s>>>(
-              g.n, g.leaf_start.p, g.mitems.p, g.mitem_split.p, g.mitem_stride.p, g.ncopies,
-              g.p2p_src.p, g.hi32.p, g.lo32.p, src, damping, Fnear, lseg, seg_done);
-      else
-        k_p2p32_m1_multi<false><<<mg, P2P_BLOCK, 0, s>>>(
-              g.n, g.leaf_start.p, g.mitems.p, g.mitem_split.p, g.mitem_stride.p, g.ncopies,
-              g.p2p_src.p, g.hi32.p, g.lo32.p, src, damping, Fnear, lseg, seg_done);
-      CG_LAUNCH();
+      for (int c0 = 0; c0 < g.ncopies; c0 += P2PM_MAXR) {
+        const int nr = std::min(P2PM_MAXR, g.ncopies - c0);
+        if (damp)
+          k_p2p32_m1_multi<true><<<mg, P2P_BLOCK, 0, s>>>(
+                g.n, g.leaf_start.p, g.mitems.p, g.mitem_split.p, g.mitem_stride.p, c0, nr,
+                g.p2p_src.p, g.hi32.p, g.lo32.p, src, damping, Fnear, lseg, seg_done);
+        else
+          k_p2p32_m1_multi<false><<<mg, P2P_BLOCK, 0, s>>>(
+                g.n, g.leaf_start.p, g.mitems.p, g.mitem_split.p, g.mitem_stride.p, c0, nr,
+                g.p2p_src.p, g.hi32.p, g.lo32.p, src, damping, Fnear, lseg, seg_done);
+        CG_LAUNCH();
+      }
       return;
     }
     if (damp)
@@ -2137,18 +2140,21 @@ static void launch_p2p_dd(const Geometry& g, bool damp, const double* src, doubl
   w.dd_src.alloc(std::max(1L, n3));
   k_split_dd<<<(unsigned)((n3 + 255) / 256), 256, 0, s>>>(n3, src, w.dd_src.p);
   CG_LAUNCH();
-  if (!g.h_mitems.empty() && g.ncopies > 1 && g.ncopies <= P2PM_MAXR) {
-    // a batch's right-hand sides together
+  if (!g.h_mitems.empty() && g.ncopies > 1) {
+    // a batch's right-hand sides together, up to P2PM_MAXR per launch
     const int mg = (int)g.h_mitems.size();
-    if (damp)
-      k_p2p_dd2_multi<true><<<mg, P2P_BLOCK, 0, s>>>(
-            g.n, g.leaf_start.p, g.mitems.p, g.mitem_split.p, g.mitem_stride.p, g.ncopies,
-            g.p2p_src.p, pos_args<float>(g), w.dd_src.p, g.dd_exp.p, damping, w.Fnear.p);
-    else
-      k_p2p_dd2_multi<false><<<mg, P2P_BLOCK, 0, s>>>(
-            g.n, g.leaf_start.p, g.mitems.p, g.mitem_split.p, g.mitem_stride.p, g.ncopies,
-            g.p2p_src.p, pos_args<float>(g), w.dd_src.p, g.dd_exp.p, damping, w.Fnear.p);
-    CG_LAUNCH();
+    for (int c0 = 0; c0 < g.ncopies; c0 += P2PM_MAXR) {
+      const int nr = std::min(P2PM_MAXR, g.ncopies - c0);
+      if (damp)
+        k_p2p_dd2_multi<true><<<mg, P2P_BLOCK, 0, s>>>(
+              g.n, g.leaf_start.p, g.mitems.p, g.mitem_split.p, g.mitem_stride.p, c0, nr,
+              g.p2p_src.p, pos_args<float>(g), w.dd_src.p, g.dd_exp.p, damping, w.Fnear.p);
+      else
+        k_p2p_dd2_multi<false><<<mg, P2P_BLOCK, 0, s>>>(
+              g.n, g.leaf_start.p, g.mitems.p, g.mitem_split.p, g.mitem_stride.p, c0, nr,
+              g.p2p_src.p, pos_args<float>(g), w.dd_src.p, g.dd_exp.p, damping, w.Fnear.p);
+      CG_LAUNCH();
+    }
     return;
   }
   const int grid = (int)g.h_items.size();

@@ -97,3 +97,24 @@ def test_batch_graph_loop_matches_host_loop(gpu, precision, tmp_path):
     mu, its = b.solve(_rhs(boxes, 2, seed=2))
     np.testing.assert_array_equal(its, host["its"])
     np.testing.assert_allclose(mu, host["mu"], rtol=0, atol=1e-12)
+
+
+def test_batch_more_rhs_than_one_pass(gpu):
+    """Ten right-hand sides per snapshot: the near-field passes take a
+    snapshot's copies eight at a time; every segment still meets the
+    reference's stopping rule with its own FP64 operator."""
+    boxes = _snapshots()[:2]  # 300 sites (direct) and 900 sites (FMM)
+    nrhs = 10
+    rhs = _rhs(boxes, nrhs, seed=3)
+    batch = cabi.Batch(boxes, nrhs, direct_below=500, damp=True, precision=cabi.MIXED)
+    mu, its = batch.solve(rhs)
+    assert its.shape == (len(boxes) * nrhs,)
+    off = 0
+    for b in boxes:
+        summ = cabi.FMM if b.n >= 500 else cabi.DIRECT
+        s64 = cabi.System(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, summation=summ, damp=True)
+        for r in range(nrhs):
+            seg = slice(off, off + 3 * b.n)
+            assert np.linalg.norm(rhs[seg] - s64.apply(mu[seg])) < 1e-8
+            off += 3 * b.n
+    assert off == rhs.size
