@@ -65,6 +65,7 @@ def lib():
         l.cppe_gpu_tree_info.argtypes = [ctypes.c_int, D, ctypes.c_int, ctypes.c_double, I, I,
                                          L, L, L]
         l.cppe_gpu_tree_lists.argtypes = [ctypes.c_int, D, ctypes.c_int, ctypes.c_double, I, I]
+        l.cppe_gpu_tree_vectors.argtypes = [ctypes.c_int, D, ctypes.c_int, ctypes.c_double, I, L]
         l.cppe_gpu_device_count.argtypes = [I]
         l.cppe_gpu_batch_create.argtypes = [ctypes.c_int, I, D, D, I, I, ctypes.c_int,
                                             ctypes.c_int, ctypes.POINTER(Options),
@@ -453,6 +454,16 @@ def tree_info(xyz, ncrit=64, theta=0.5):
                                    ctypes.byref(pairs)))
     return dict(ncells=nc.value, nleaves=nl.value, nm2l=nm.value, np2p=npp.value,
                 p2p_pairs=pairs.value)
+
+
+def tree_vectors(xyz, ncrit=64, theta=0.5):
+    """(distinct M2L translation vectors, M2L list entries) of the tree; the
+    count is -1 where the table would not be used."""
+    xyz = f64(xyz)
+    nv, ne = ctypes.c_int(0), ctypes.c_long(0)
+    check(lib().cppe_gpu_tree_vectors(xyz.shape[0], dp(xyz), ncrit, theta, ctypes.byref(nv),
+                                      ctypes.byref(ne)))
+    return nv.value, ne.value
 
 
 def tree_lists(xyz, ncrit=64, theta=0.5):

@@ -652,6 +652,23 @@ int cppe_gpu_tree_info(int n, const double* xyz, int ncrit, double theta, int* n
   });
 }
 
+int cppe_gpu_tree_vectors(int n, const double* xyz, int ncrit, double theta, int* nvec,
+                          long* nentries) {
+  return guard([&]() -> int {
+    need(xyz && nvec, "null argument");
+    RefTree t;
+    std::string err;
+    if (!build_ref_tree(n, xyz, ncrit, theta, t, err)) fail(CPPE_GPU_INVALID_ARG, err);
+    TreeLayout L;
+    make_layout(t, n, L);
+    std::vector<int> vid;
+    std::vector<double4_32a> vec;
+    *nvec = m2l_vectors(L, vid, vec) ? (int)vec.size() : -1;
+    if (nentries) *nentries = (long)L.m2l_src.size();
+    return CPPE_GPU_OK;
+  });
+}
+
 int cppe_gpu_tree_lists(int n, const double* xyz, int ncrit, double theta, int* m2l, int* p2p) {
   return guard([&]() -> int {
     need(xyz && m2l && p2p, "null argument");

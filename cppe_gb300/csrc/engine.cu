@@ -234,19 +234,18 @@ void Geometry::prepare(int n_, const double* xyz, const double* s_damp, const in
   make_vectors();
 }
 
-void Geometry::make_vectors() {
-  h_m2l_vid.clear();
-  h_vec.clear();
-  const TreeLayout& L = layout;
-  if (!fmm || L.m2l_src.empty()) return;
+bool m2l_vectors(const TreeLayout& L, std::vector<int>& vid, std::vector<double4_32a>& vec) {
+  vid.clear();
+  vec.clear();
+  if (L.m2l_src.empty()) return true;
   // centres are the root centre plus multiples of the deepest half-width
   double rmin = 1e300;
   for (int c = 0; c < L.ncells; ++c) rmin = std::min(rmin, L.center[4 * (size_t)c + 3]);
-  if (!(rmin > 0.0)) return;
+  if (!(rmin > 0.0)) return false;
   const double u = 0.5 * rmin;
   constexpr long long OFF = 1LL << 20;
   std::unordered_map<long long, int> ids;
-  h_m2l_vid.resize(L.m2l_src.size());
+  vid.resize(L.m2l_src.size());
   for (int A = 0; A < L.ncells; ++A)
     for (int q = L.m2l_ptr[A]; q < L.m2l_ptr[A + 1]; ++q) {
       const int B = L.m2l_src[q];
@@ -255,23 +254,29 @@ void Geometry::make_vectors() {
         const double d = (L.center[4 * (size_t)A + c] - L.center[4 * (size_t)B + c]) / u;
         k[c]           = std::llround(d);
         if (std::fabs(d - (double)k[c]) > 1e-3 || std::llabs(k[c]) >= OFF) {
-          h_m2l_vid.clear();  // off the grid: tensors per translation
-          h_vec.clear();
-          return;
+          vid.clear();  // off the grid
+          vec.clear();
+          return false;
         }
       }
       const long long key = (k[0] + OFF) | ((k[1] + OFF) << 21) | ((k[2] + OFF) << 42);
       const auto it       = ids.find(key);
       if (it == ids.end()) {
-        ids.emplace(key, (int)h_vec.size());
-        h_m2l_vid[q] = (int)h_vec.size();
+        ids.emplace(key, (int)vec.size());
+        vid[q] = (int)vec.size();
         double4_32a v;
         v.x = (double)k[0] * u, v.y = (double)k[1] * u, v.z = (double)k[2] * u, v.w = 0.0;
-        h_vec.push_back(v);
+        vec.push_back(v);
       } else {
-        h_m2l_vid[q] = it->second;
+        vid[q] = it->second;
       }
     }
+  return true;
+}
+
+void Geometry::make_vectors() {
+  // off the grid: the M2L builds each tensor itself
+  if (!fmm || !m2l_vectors(layout, h_m2l_vid, h_vec)) h_m2l_vid.clear(), h_vec.clear();
 }
 
 // Cuts every target leaf's source list into pieces of about `W` pairs so that

@@ -68,6 +68,11 @@ struct DeviceOps {
   OpsView view() const;
 };
 
+// Distinct centre differences of a tree's M2L list entries (target minus
+// source, on the grid of half the deepest half-width): vid[q] indexes vec for
+// list entry q.  False (and empty outputs) where a difference is off the grid.
+bool m2l_vectors(const TreeLayout& L, std::vector<int>& vid, std::vector<double4_32a>& vec);
+
 // Row stride (coefficients) of the multipole storage of the fixed-order
 // expansion kernels: the coefficient count rounded up to a multiple of four,
 // so that rows start on 16-byte boundaries.

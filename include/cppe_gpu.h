@@ -160,6 +160,11 @@ int cppe_gpu_tree_info(int n, const double* xyz, int ncrit, double theta, int* n
  * (np2p x 2, (target, source)). */
 int cppe_gpu_tree_lists(int n, const double* xyz, int ncrit, double theta, int* m2l,
                         int* p2p);
+/* Host-only: the number of distinct centre differences among the M2L list
+ * entries (nentries), whose derivative tensors the FMM tabulates; -1 where a
+ * difference is off the tree's grid (no table). */
+int cppe_gpu_tree_vectors(int n, const double* xyz, int ncrit, double theta, int* nvec,
+                          long* nentries);
 
 /* Allocation-free direct-summation apply (no counterpart in the reference).
  * d_out = B d_in with direct summation in FP64, the operator of

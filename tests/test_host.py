@@ -51,6 +51,25 @@ def test_tree_lists_match_oracle_deep_tree(loprop, port):
                                   np.sort(t["m2l"].view(np.int64).ravel()))
 
 
+@pytest.mark.parametrize("nw,ncrit", [(1000, 64), (3000, 16)])
+def test_m2l_translation_vectors(port, nw, ncrit):
+    """The FMM tabulates its M2L derivative tensors per distinct centre
+    difference: the count it finds equals the distinct differences of the
+    oracle tree's M2L list, and is well below the list's length (the ratio
+    grows with the tree: 4,832 for 14.6 M entries at 300k sites)."""
+    from cppe_gb300 import synthetic
+    b = synthetic.water_box(nw, seed=7)
+    nvec, nent = cabi.tree_vectors(b.xyz, ncrit=ncrit, theta=0.5)
+    t = port.tree_lists(b.xyz, ncrit=ncrit, order=5, theta=0.5)
+    c, m = t["cells"][:, :3], t["m2l"]
+    assert nent == len(m)
+    # differences are multiples of the deepest half-width: exact on its grid
+    u = 0.5 * t["cells"][:, 3].min()
+    keys = np.round((c[m[:, 1]] - c[m[:, 0]]) / u).astype(np.int64)
+    assert nvec == len(np.unique(keys, axis=0))
+    assert 0 < nvec < nent // 4
+
+
 def test_tree_rejects_coincident_sites():
     xyz = np.zeros((80, 3))
     with pytest.raises(RuntimeError, match="coincide"):
