@@ -169,19 +169,23 @@ int cppe_gpu_tree_vectors(int n, const double* xyz, int ncrit, double theta, int
 /* Allocation-free direct-summation apply (no counterpart in the reference).
  * d_out = B d_in with direct summation in FP64, the operator of
  * cppe_gpu_bmatrix_apply for summation = CPPE_GPU_DIRECT, for callers that
- * cannot allocate GPU memory at this point (a host program that owns a fixed
- * device pool, code running inside a CUDA stream capture, real-time loops
- * that must not enter the allocator).  All pointers are device pointers the
- * caller owns: d_xyz (3n), d_alpha6 (6n), d_excl_ptr (n+1) / d_excl_idx (CSR
- * exclusions, both NULL for none), d_in and d_out (3n).  No cudaMalloc or
+ * cannot allocate GPU memory at this point: a host program that owns a fixed
+ * device pool and forbids further cudaMalloc, or a real-time loop that must
+ * not enter the allocator.  All pointers are device pointers the caller owns:
+ * d_xyz (3n), d_alpha6 (6n), d_excl_ptr (n+1) / d_excl_idx (CSR exclusions,
+ * both NULL for none), d_in and d_out (3n).  d_out must not overlap any input
+ * buffer (CPPE_GPU_INVALID_ARG otherwise).  Excluded pairs are skipped, as in
+ * the reference.  Two distinct, non-excluded sites at the same position make
+ * the operator undefined; the output of such a site is NaN.  No cudaMalloc or
  * cudaFree is made; the only scratch is a fixed 1.75 MiB device array that
  * every GPU loading the library holds until exit, which limits n to 8192
- * (larger n returns CPPE_GPU_INVALID_ARG).  The work is enqueued on `stream`
- * (a cudaStream_t, NULL for the default stream) and not synchronized.  The
- * first call on a device looks the scratch address up with that device
- * current; make that first call before any stream capture.  Calls share the
- * scratch, so calls that overlap on the GPU (different streams, no ordering)
- * race; calls ordered on one stream are safe. */
+ * (larger n returns CPPE_GPU_INVALID_ARG before any GPU work).  The work is
+ * enqueued on `stream` (a cudaStream_t, NULL for the default stream) and not
+ * synchronized.  The first call on a device looks the scratch address up with
+ * that device current and keeps it for the life of the process (it does not
+ * survive a cudaDeviceReset); make that first call before any stream capture.
+ * Calls share the scratch, so calls that overlap on the GPU (different
+ * streams, no ordering) race; calls ordered on one stream are safe. */
 int cppe_gpu_bmatrix_apply_direct_noalloc(int n, const double* d_xyz, const double* d_alpha6,
                                           const int* d_excl_ptr, const int* d_excl_idx,
                                           int damp, double damping_factor, const double* d_in,
