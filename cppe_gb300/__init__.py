@@ -13,25 +13,53 @@ no CPU fallback: without the built module every public name raises
 ImportError, and operations that need the GPU raise RuntimeError when no CUDA
 device is present.
 """
+import importlib as _importlib
 import os as _os
 
 _here = _os.path.dirname(_os.path.abspath(__file__))
 __version__ = "0.1.0"
 LIBRARY_PATH = _os.path.join(_here, "libcppe_gpu.so")
 
-try:
-    from .pycppe import *  # noqa: F401,F403
-    from .pycppe import __build_type__, __parallel__  # noqa: F401
-    _IMPORT_ERROR = None
-except ImportError as _e:  # only before the in-tree build has run
-    _IMPORT_ERROR = _e
+# The native module (and with it libcppe_gpu.so) loads on the first access to
+# one of its names, not at package import: the package's pure-Python modules
+# (``synthetic``, the seeded input generators) stay usable without mapping the
+# CUDA library.
+_PY_SUBMODULES = {"synthetic", "capi", "learned", "shard"}
+_native = None
+_IMPORT_ERROR = None
 
-    def __getattr__(name):
-        if name.startswith("_"):  # submodules such as _build stay importable
-            raise AttributeError(name)
-        raise ImportError(
-            f"cppe_gb300.{name}: the native module is not built "
-            "(run `python -c 'import __graft_entry__ as g; g.build()'`, needs nvcc)"
-        ) from _IMPORT_ERROR
+
+def _load_native():
+    global _native, _IMPORT_ERROR
+    if _native is None:
+        try:
+            _native = _importlib.import_module(".pycppe", __name__)
+        except ImportError as e:  # only before the in-tree build has run
+            _IMPORT_ERROR = e
+            raise ImportError(
+                "cppe_gb300: the native module is not built "
+                "(run `python -c 'import __graft_entry__ as g; g.build()'`, needs nvcc)") from e
+    return _native
+
+
+def __getattr__(name):
+    if name.startswith("_") and name not in ("__build_type__", "__parallel__"):
+        raise AttributeError(name)  # private names and submodules such as _build
+    if name in _PY_SUBMODULES:
+        raise AttributeError(name)  # let the import system load the submodule
+    try:
+        value = getattr(_load_native(), name)
+    except AttributeError:
+        raise AttributeError(f"module 'cppe_gb300' has no attribute '{name}'") from None
+    globals()[name] = value
+    return value
+
+
+def __dir__():
+    names = set(globals())
+    if _native is not None:
+        names.update(n for n in dir(_native) if not n.startswith("_"))
+    return sorted(names)
+
 
 __all__ = ["__build_type__", "__parallel__", "__version__"]
