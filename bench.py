@@ -1,21 +1,32 @@
 #!/usr/bin/env python
 """Benchmark of the induced-dipole solve (time to a 1e-8 residual).
 
-Workload (default): 10,000 rigid waters = 30,000 polarizable sites, FMM
-expansion order 5, theta 0.5, ncrit 64, Thole damping a = 2.1304, one
-right-hand side = field of 12 point charges + static multipole field, solved
-from the reference's first-call guess alpha*F to ||F - B mu||_2 < 1e-8 with
-the FP64 FMM operator.  A step is one complete solve.
+Workload (default, the largest single-GPU configuration): 333,334 rigid
+waters = 1,000,002 polarizable sites, FMM expansion order 6, theta 0.5,
+ncrit 64, Thole damping a = 2.1304, one right-hand side = field of 12 point
+charges + static multipole field, solved from the reference's first-call
+guess alpha*F to ||F - B mu||_2 < 1e-8 with the FP64 FMM operator.  A step is
+one complete solve.
 
-value     mixed-precision solve (FP32 inner PCG + FP64 refinement), inputs and
+value     the method: mixed-precision solve (FP32 inner PCG + FP64-accurate
+          refinement) with the trained guess/preconditioner model, inputs and
           outputs resident on the GPU, CUDA events on the library's stream.
 e2e       the same solve through the C ABI with host buffers
           (cppe_gpu_solve: H2D of F, D2H of mu inside the timed region).
 plain     the plain FP64 GPU PCG (the reference's algorithm on the GPU) on the
           same system, reported next to the headline.
+vs_oracle the headline's answer checked against the reference: the oracle's
+          FP64 operator applied to the GPU solution (the reference's own
+          stopping criterion), and the reference engine's committed solution
+          summary of the same box (tests/golden/config_solutions.json).
+
+Extra sections: the 30,000-site order-5 system (with a full oracle solve to
+compare against), the 300,000-site order-6 system, and the 256 x 8 batch.
 
 `--impl reference` times the reference algorithm on the host cores (the
-oracle's C++ restatement with OpenMP, all threads) on the same workload.
+oracle's C++ restatement with OpenMP, all threads) on the same workload: full
+solves where one fits a few seconds, else FMM applies (tree rebuilt per
+apply, as the reference does) times the reference's applies per solve.
 """
 from __future__ import annotations
 
@@ -163,7 +174,7 @@ def static_rhs_gpu(b, summation, order):
     Fm = capi.multipole_fields(b.xyz, b.q, b.mu, b.quad, 2, np.ones(b.n, np.int32),
                                b.alpha_iso, b.excl_ptr, b.excl_idx,
                                fmm=(summation == "fmm"), ncrit=64, order=order)
-    return b.external_field() + Fm
+    return (b.external_field() + Fm).ravel()
 
 
 def peaks():
@@ -174,60 +185,124 @@ def peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
+GOLDEN_PATH = os.path.join(ROOT, "tests", "golden", "config_solutions.json")
+GOLDEN_KEY = {"30k-fmm5": "30k", "300k-fmm6": "300k", "1m-fmm6": "1m"}
+# configurations whose reference solve takes too long for a bench step: the
+# reference arm times FMM applies and scales them by the applies per solve
+APPLY_SAMPLED = {"300k-fmm6", "1m-fmm6"}
+
+
+def golden(cfg):
+    """The reference engine's solution summary of a workload's box, or None."""
+    if cfg not in GOLDEN_KEY or not os.path.exists(GOLDEN_PATH):
+        return None
+    with open(GOLDEN_PATH) as f:
+        return json.load(f).get(GOLDEN_KEY[cfg])
+
+
+def oracle_port():
+    from oracle import oracle as O
+    if not os.path.exists(O.PORT_LIB):
+        O.build_port()
+    return O.port()
+
+
+def oracle_kw(summation, order):
+    return dict(fmm=int(summation == "fmm"), ncrit=64, order=order, theta=0.5, damping=2.1304)
+
+
 def run_reference(args):
     """The reference algorithm on the host cores (oracle restatement)."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    from oracle import oracle as O
-    if not os.path.exists(O.PORT_LIB):
-        O.build_port()
-    P = O.port()
+    P = oracle_port()
     b, summation, order = make_problem(args.config)
-    fmm = summation == "fmm"
-    sites = O.Sites(xyz=b.xyz, elements=b.elements, q=b.q, mu=b.mu, quad=b.quad, max_order=2,
-                    alpha6=b.alpha6, polarizable=np.ones(b.n, np.int32), excl_ptr=b.excl_ptr,
-                    excl_idx=b.excl_idx)
-    rhs = b.external_field() + P.multipole_fields(sites, fmm=fmm, order=order)
-    kw = dict(fmm=int(fmm), ncrit=64, order=order, theta=0.5, damping=2.1304, thresh=1e-8)
-    for _ in range(args.warmup):
-        P.solve(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, rhs, **kw)
-    times, its = [], []
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        mu, it, hist, ok = P.solve(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, rhs, **kw)
-        times.append(time.perf_counter() - t0)
-        its.append(it)
-    v = float(np.mean(times))
+    kw = oracle_kw(summation, order)
     cores = os.cpu_count()
+    if args.config in APPLY_SAMPLED:
+        g = golden(args.config)
+        iters = g["iterations"] if g else None
+        if iters is None:
+            print(json.dumps({"impl": "reference", "unavailable":
+                              "no reference iteration count for this workload"}), flush=True)
+            return
+        applies = iters + 1  # one apply per PCG iteration plus the initial residual
+        v = b.external_field().ravel()
+        for _ in range(args.warmup):
+            P.bmatrix_apply(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, v, **kw)
+        times = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            P.bmatrix_apply(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, v, **kw)
+            times.append(time.perf_counter() - t0)
+        t_apply = float(np.mean(times))
+        v_solve = t_apply * applies
+        sample = (f"{args.steps} FMM applies B*v of the {b.n:,}-site system (octree rebuilt per "
+                  "apply, as the reference does), OpenMP over all host threads; solve time = "
+                  f"{t_apply:.3f} s per apply x {applies} applies (the reference engine's PCG "
+                  f"takes {iters} iterations on this system, "
+                  "tests/golden/config_solutions.json)")
+    else:
+        rhs = b.external_field().ravel() + P.multipole_fields(
+            _oracle_sites(b), fmm=summation == "fmm", order=order)
+        for _ in range(args.warmup):
+            P.solve(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, rhs, thresh=1e-8, **kw)
+        times, its = [], []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            mu, it, hist, ok = P.solve(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, rhs,
+                                       thresh=1e-8, **kw)
+            times.append(time.perf_counter() - t0)
+            its.append(it)
+        v_solve = float(np.mean(times))
+        sample = (f"{args.steps} full solves ({int(np.mean(its))} CG iterations each), OpenMP "
+                  "over all host threads")
     line = {
-        "impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3,
+        "impl": "reference", "metric": METRIC, "value": v_solve, "unit": "s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": v_solve * 1e3,
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded water box, 12 point charges)",
         "config": dict(workload_config(args.config, b.n), parallelism="host threads"),
-        "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port",
-                         "sample": f"{args.steps} full solves ({int(np.mean(its))} CG "
-                                   "iterations each), OpenMP over all host threads"},
-        "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "cpu_baseline": {"value": v_solve, "unit": "s", "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": v_solve, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
-def cpu_baseline_sample(b, rhs, summation, order):
-    """One bounded CPU solve of the same workload (oracle restatement)."""
+def _oracle_sites(b):
     from oracle import oracle as O
-    if not os.path.exists(O.PORT_LIB):
-        O.build_port()
-    P = O.port()
-    kw = dict(fmm=int(summation == "fmm"), ncrit=64, order=order, theta=0.5, damping=2.1304,
-              thresh=1e-8)
+    return O.Sites(xyz=b.xyz, elements=b.elements, q=b.q, mu=b.mu, quad=b.quad, max_order=2,
+                   alpha6=b.alpha6, polarizable=np.ones(b.n, np.int32), excl_ptr=b.excl_ptr,
+                   excl_idx=b.excl_idx)
+
+
+def oracle_residual(P, b, rhs, mu, summation, order):
+    """||rhs - B mu||_2 with the oracle's FP64 operator (the reference's
+    stopping criterion evaluated by the reference algorithm) and its time."""
     t0 = time.perf_counter()
-    mu, it, hist, ok = P.solve(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, rhs, **kw)
-    dt = time.perf_counter() - t0
-    return {"value": dt, "unit": "s", "cores": os.cpu_count(), "kind": "port",
-            "sample": f"1 full solve of the same system ({it} CG iterations), OpenMP over all "
-                      "host threads"}, mu
+    Bmu = P.bmatrix_apply(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, mu,
+                          **oracle_kw(summation, order))
+    return float(np.linalg.norm(rhs - Bmu)), time.perf_counter() - t0
+
+
+def vs_reference_solution(cfg, rhs, mu):
+    """A GPU solution against the reference engine's committed summary of the
+    same box: energy -1/2 mu.F, mu at 64 seeded sites, mu over 64 site blocks,
+    and the right-hand side (static fields) at the same sites."""
+    g = golden(cfg)
+    if g is None or g["sites"] * 3 != mu.size:
+        return None
+    idx = np.asarray(g["sample_sites"])
+    m3, f3 = mu.reshape(-1, 3), rhs.reshape(-1, 3)
+    edges = np.linspace(0, g["sites"], len(g["mu_block_sums"]) + 1).astype(np.int64)
+    blocks = np.array([m3[a:c].sum(axis=0) for a, c in zip(edges[:-1], edges[1:])])
+    return {"epol_hartree_diff": float(abs(-0.5 * mu @ rhs - g["epol"])),
+            "mu_sample_maxabs": float(np.abs(m3[idx] - np.asarray(g["mu_samples"])).max()),
+            "mu_block_sum_maxabs": float(np.abs(blocks - np.asarray(g["mu_block_sums"])).max()),
+            "F_sample_maxabs": float(np.abs(f3[idx] - np.asarray(g["F_samples"])).max()),
+            "reference_iterations": g["iterations"], "reference_epol": g["epol"]}
 
 
 def _event_time(stream, fn):
@@ -301,6 +376,33 @@ def batched_section(dev, steps, flush, compare=True):
         off += nrhs * 3 * b.n
         s64.close()
     plain *= nrhs
+    # against the oracle: its FP64 operator's residual of every right-hand side
+    # of four snapshots (the smallest and largest direct-summation ones, the
+    # smallest and largest FMM ones), and full oracle solves of the first
+    # right-hand side of the largest direct and the largest FMM snapshot
+    P = oracle_port()
+    offs = np.concatenate([[0], np.cumsum([nrhs * 3 * b.n for b in boxes])])
+    direct = [i for i, b in enumerate(boxes) if b.n < 4000]
+    fmm = [i for i, b in enumerate(boxes) if b.n >= 4000]
+    by_n = lambda ids: sorted(ids, key=lambda i: boxes[i].n)  # noqa: E731
+    picks = [by_n(direct)[0], by_n(direct)[-1], by_n(fmm)[0], by_n(fmm)[-1]]
+    worst_o, mu_diff = 0.0, {}
+    for i in picks:
+        b = boxes[i]
+        summation = "fmm" if b.n >= 4000 else "direct"
+        for r in range(nrhs):
+            seg = mu[offs[i] + r * 3 * b.n:offs[i] + (r + 1) * 3 * b.n]
+            worst_o = max(worst_o, oracle_residual(P, b, rhs[i][r], seg, summation, 5)[0])
+    for i in (picks[1], picks[3]):
+        b = boxes[i]
+        summation = "fmm" if b.n >= 4000 else "direct"
+        mu_o, it_o, _, ok = P.solve(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, rhs[i][0],
+                                    thresh=1e-8, **oracle_kw(summation, 5))
+        mu_diff[f"{summation}_{b.n}_sites"] = float(
+            np.abs(mu[offs[i]:offs[i] + 3 * b.n] - mu_o).max())
+    vs_oracle = {"snapshots": [int(boxes[i].n) for i in picks],
+                 "max_oracle_residual": worst_o, "rhs_checked": 4 * nrhs,
+                 "mu_maxabs_vs_oracle_solve": mu_diff}
     return {"workload": "256 snapshots x 8 RHS, sites log-uniform 500-20,000 "
                         f"({int(sum(sizes))} sites, {int(sum(sizes)) * nrhs} site-RHS), direct "
                         "< 4,000 sites, FMM p5 above, mixed precision, tol 1e-8",
@@ -309,61 +411,63 @@ def batched_section(dev, steps, flush, compare=True):
             "plain_fp64_note": "first RHS of each snapshot solved and timed one at a time, x8",
             "speedup_vs_plain_fp64": plain / t_batch,
             "fp32_applies": bst["fp32_applies"], "fp64_applies": bst["fp64_applies"],
-            "max_fp64_residual": worst, "setup_s": setup, "autotune_s": tune,
-            "fp32_apply_ms": tuned_ms}
+            "max_fp64_residual": worst, "vs_oracle": vs_oracle, "setup_s": setup,
+            "autotune_s": tune, "fp32_apply_ms": tuned_ms}
 
 
-def large_section(cfg, dev, flush, model_path=None, zero_guess=True):
-    """One larger system solved once per arithmetic: plain FP64 PCG (from
-    alpha*F and, optionally, from zero), mixed precision, and mixed precision
-    with the trained model.  Errors of the mixed solutions against the FP64
-    one: induced dipoles, polarization energy (-1/2 mu.E_ext), the induced
-    field B mu and the FP64 residual."""
+def system_section(cfg, dev, flush, steps, model_path=None, oracle_check="residual"):
+    """One system solved by the plain FP64 PCG and by the mixed solver with and
+    without the trained model.  Errors of the mixed solutions against the FP64
+    one: induced dipoles, polarization energy (-1/2 mu.E_ext), the induced field
+    B mu and the FP64 residual.  Against the reference: a full oracle solve
+    (`oracle_check="solve"`) or the oracle operator's residual of the mixed
+    solution ("residual"), and the reference engine's committed summary."""
     import torch
     from cppe_gb300 import capi, learned
     t0 = time.perf_counter()
     b, summation, order = make_problem(cfg)
     rhs = static_rhs_gpu(b, summation, order)
     setup = time.perf_counter() - t0
-    kw = dict(summation=capi.FMM, ncrit=64, order=order, theta=0.5, damp=True, thresh=1e-8,
-              device=dev)
+    kw = dict(summation=capi.FMM if summation == "fmm" else capi.DIRECT, ncrit=64, order=order,
+              theta=0.5, damp=True, thresh=1e-8, device=dev)
     d_rhs = torch.tensor(rhs, dtype=torch.float64, device=f"cuda:{dev}")
     d_mu = torch.zeros_like(d_rhs)
-    E = b.external_field()
+    E = b.external_field().ravel()
     out = {"workload": f"{cfg}: {CONFIGS[cfg][4]}, Thole damping, tol 1e-8", "sites": b.n,
            "setup_s": setup}
 
-    def timed(sys_, make_guess=True):
+    def timed(sys_):
         flush.fill_(1.0)
         torch.cuda.synchronize()
         t, _ = _event_time(torch.cuda.ExternalStream(sys_.stream()),
-                           lambda: sys_.solve_device(d_rhs.data_ptr(), d_mu.data_ptr(),
-                                                     make_guess=make_guess))
-        return t, d_mu.cpu().numpy(), sys_.stats()
+                           lambda: sys_.solve_device(d_rhs.data_ptr(), d_mu.data_ptr()))
+        return t
 
     s64 = capi.System(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, precision=capi.FP64, **kw)
-    t64, mu64, st64 = timed(s64)
-    out["plain_fp64"] = {"s": t64, "iterations": st64["fp64_applies"] - 1}
-    if zero_guess:
-        tz, _, stz = timed(s64, make_guess=False)
-        out["plain_fp64_zero_guess"] = {"s": tz, "iterations": stz["fp64_applies"]}
+    s64.apply(rhs)  # first-use allocations
+    t64 = timed(s64)
+    mu64 = d_mu.cpu().numpy()
+    it64 = s64.stats()["fp64_applies"] - 1
+    out["plain_fp64"] = {"s": t64, "iterations": it64}
     Bmu64 = s64.apply(mu64)
     smx = capi.System(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, precision=capi.MIXED, **kw)
     t0 = time.perf_counter()
     out["autotune"] = {"apply_ms": smx.autotune(2), "s": time.perf_counter() - t0}  # set-up
-    timed(smx)  # warm-up (first-use allocations)
     variants = [("mixed", None)]
     if model_path and os.path.exists(model_path):
         variants.append(("mixed_learned", learned.load(model_path, device=dev)))
+    mus = {"plain_fp64": mu64}
     for name, model in variants:
         smx.set_model(model)
-        if model is not None:
-            timed(smx)
-        t, mu, st = timed(smx)
+        timed(smx)  # warm-up (first-use allocations)
+        ts = [timed(smx) for _ in range(steps)]
+        mu = d_mu.cpu().numpy()
+        st = smx.stats()
         Bmu = s64.apply(mu)
+        mus[name] = mu
         out[name] = {
-            "s": t, "fp32_applies": st["fp32_applies"], "fp64_applies": st["fp64_applies"],
-            "speedup_vs_plain_fp64": t64 / t,
+            "s": float(np.mean(ts)), "fp32_applies": st["fp32_applies"],
+            "fp64_applies": st["fp64_applies"], "speedup_vs_plain_fp64": t64 / float(np.mean(ts)),
             "error_vs_fp64": {
                 "mu_maxabs": float(np.abs(mu - mu64).max()),
                 "epol_hartree": float(abs(0.5 * (mu - mu64) @ E)),
@@ -372,6 +476,25 @@ def large_section(cfg, dev, flush, model_path=None, zero_guess=True):
     smx.set_model(None)
     smx.close()
     s64.close()
+    best = variants[-1][0]
+    P = oracle_port()
+    if oracle_check == "solve":
+        t0 = time.perf_counter()
+        mu_o, it_o, _, ok = P.solve(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, rhs, thresh=1e-8,
+                                    **oracle_kw(summation, order))
+        vo = {"oracle_solve_s": time.perf_counter() - t0, "oracle_iterations": it_o,
+              "plain_fp64_iterations": it64}
+        for name, mu in mus.items():
+            vo[name] = {"mu_maxabs": float(np.abs(mu - mu_o).max()),
+                        "epol_hartree": float(abs(0.5 * (mu - mu_o) @ rhs))}
+        vo["oracle_residual_" + best], _ = oracle_residual(P, b, rhs, mus[best], summation,
+                                                           order)
+    else:
+        r, t = oracle_residual(P, b, rhs, mus[best], summation, order)
+        vo = {"oracle_residual_" + best: r, "oracle_apply_s": t}
+    out["vs_oracle"] = vo
+    out["vs_reference_solution"] = {k: vs_reference_solution(cfg, rhs, mus[k])
+                                    for k in ("plain_fp64", best)}
     return out
 
 
@@ -390,6 +513,10 @@ def profiled_traffic(md_name):
                     tot += float(cells[1]) * scale.get(cells[2], 1.0)
                     found += 1
     return tot if found == 2 else None
+
+
+PROFILE_OF = {"30k-fmm5": "k_p2p32_m1_30k_sites.md", "300k-fmm6": "k_p2p32_m1_300k_sites.md",
+              "1m-fmm6": "k_p2p32_m1_1m_sites.md"}
 
 
 def run_ours(args):
@@ -413,7 +540,8 @@ def run_ours(args):
         # operator applies only (FP32 then FP64), e.g. for kernel profiling
         t32 = smx.kernel_timings(capi.MIXED, reps=args.apply_only)
         tdd = smx.kernel_timings(DD_RESIDUAL, reps=args.apply_only)
-        t64 = s64.kernel_timings(capi.FP64, reps=args.apply_only)
+        t64 = s64.kernel_timings(capi.FP64, reps=args.apply_only) if not args.no_fp64 else \
+            ({}, 0, 0)
         print(json.dumps({"apply_only": args.apply_only, "config": args.config,
                           "fp32_ms": t32[0], "dd_ms": tdd[0], "fp64_ms": t64[0],
                           "alg_pairs": t32[1], "m2l_pairs": t32[2]}), flush=True)
@@ -424,11 +552,13 @@ def run_ours(args):
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{dev}")  # 256 MB
     ext = torch.cuda.ExternalStream(smx.stream())
     ext64 = torch.cuda.ExternalStream(s64.stream())
+    model = None
+    if not args.no_learned and args.model and os.path.exists(args.model):
+        from cppe_gb300 import learned
+        model = learned.load(args.model, device=dev)
     if args.solve_only:
         # mixed solves only (with the model when given), e.g. for launch lists
-        if args.model and os.path.exists(args.model) and not args.no_learned:
-            from cppe_gb300 import learned
-            smx.set_model(learned.load(args.model, device=dev))
+        smx.set_model(model)
         ts = []
         for k in range(args.warmup + args.steps):
             flush.fill_(1.0)
@@ -437,9 +567,9 @@ def run_ours(args):
                                                              make_guess=True))
             if k >= args.warmup:
                 ts.append(t)
-        print(json.dumps({"solve_only": args.steps, "config": args.config, "ms": [t * 1e3 for t in ts],
-                          "stats": smx.stats(), "learned": smx._model is not None
-                          if hasattr(smx, "_model") else False}), flush=True)
+        print(json.dumps({"solve_only": args.steps, "config": args.config,
+                          "ms": [t * 1e3 for t in ts], "stats": smx.stats(),
+                          "learned": model is not None}), flush=True)
         return
 
     def timed_solve(sys_, stream):
@@ -454,14 +584,9 @@ def run_ours(args):
         return e0.elapsed_time(e1) * 1e-3, it
 
     # the method: mixed precision, with the trained model when one is shipped
-    model = None
-    if not args.no_learned and args.model and os.path.exists(args.model):
-        from cppe_gb300 import learned
-        model = learned.load(args.model, device=dev)
     smx.set_model(model)
     for _ in range(args.warmup):
         timed_solve(smx, ext)
-        timed_solve(s64, ext64)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -493,31 +618,27 @@ def run_ours(args):
     e2e_v = float(np.mean(e2e))
 
     # the mixed solver without the model, for the learned part's gain
-    without = None
+    lrn = None
     if model is not None:
         smx.set_model(None)
         timed_solve(smx, ext)
         tw = [timed_solve(smx, ext)[0] for _ in range(args.steps)]
-        without = {"s": float(np.mean(tw)), "stats": smx.stats()}
-    lrn = None
-    if model is not None:
-        lrn = {"with_model_s": t_head, "with_model_stats": st, "without_model_s": without["s"],
-               "without_model_stats": without["stats"],
+        lrn = {"with_model_s": t_head, "with_model_stats": st,
+               "without_model_s": float(np.mean(tw)), "without_model_stats": smx.stats(),
+               "gain": 1.0 - t_head / float(np.mean(tw)),
                "model": os.path.relpath(args.model, ROOT)}
+        smx.set_model(model)
 
-    # plain FP64 GPU PCG on the same system
-    t64 = []
-    for _ in range(max(1, min(args.steps, 3))):
-        t, it64 = timed_solve(s64, ext64)
-        t64.append(t)
+    # plain FP64 GPU PCG on the same system (one solve after a warm-up apply)
+    s64.apply(rhs)
+    plain, _ = timed_solve(s64, ext64)
     mu64 = d_mu.cpu().numpy()
     st64 = s64.stats()
-    plain = float(np.mean(t64))
 
     # roofline of the dominant kernel (FP32 near-field pair pass)
     tim32, alg_pairs, m2l_pairs = smx.kernel_timings(capi.MIXED, reps=5)
-    tim64, _, _ = s64.kernel_timings(capi.FP64, reps=3)
     timdd, _, _ = smx.kernel_timings(DD_RESIDUAL, reps=3)
+    tim64, _, _ = s64.kernel_timings(capi.FP64, reps=2)
     fp32_peak = capi.fma_peak_tflops(False, dev)
     fp64_peak = capi.fma_peak_tflops(True, dev)
     achieved = alg_pairs * FLOP_PER_PAIR / (tim32["near"] * 1e-3) / 1e12
@@ -527,17 +648,47 @@ def run_ours(args):
                    "fp64": alg_pairs / (tim64["near"] * 1e-3)}
     pk, pk_kind = peaks()
 
-    resid = float(np.linalg.norm(rhs - s64.apply(mu_head)))
-    E = b.external_field()
-    de = float(abs(0.5 * (mu_head - mu64) @ E))
-    batched = batched_section(dev, 1, flush) if (not args.no_batched and world == 1) else None
-    large = {}
+    E = b.external_field().ravel()
+    Bmu_head = s64.apply(mu_head)
+    Bmu64 = s64.apply(mu64)
+    parity = {
+        "fp64_residual": float(np.linalg.norm(rhs - Bmu_head)),
+        "vs_plain_fp64_gpu": {
+            "mu_maxabs": float(np.abs(mu_head - mu64).max()),
+            "epol_hartree": float(abs(0.5 * (mu_head - mu64) @ E)),
+            "induced_field_rel": float(np.linalg.norm(Bmu_head - Bmu64) /
+                                       np.linalg.norm(Bmu64))}}
+    smx.set_model(None)
+    smx.close()
+    s64.close()
+    del d_rhs, d_mu
+    sections = {}
     if not args.no_large and world == 1:
-        large["precision_300k"] = large_section("300k-fmm6", dev, flush, zero_guess=False)
-        large["learned_1m"] = large_section("1m-fmm6", dev, flush, model_path=args.model)
+        if args.config != "30k-fmm5":
+            sections["small_30k"] = system_section("30k-fmm5", dev, flush, args.steps,
+                                                   args.model, oracle_check="solve")
+        if args.config != "300k-fmm6":
+            sections["precision_300k"] = system_section("300k-fmm6", dev, flush, 2,
+                                                        args.model)
+    batched = batched_section(dev, 1, flush) if (not args.no_batched and world == 1) else None
     if rank != 0:
         return
-    cpu, _ = cpu_baseline_sample(b, rhs, summation, order) if not args.no_cpu else (None, None)
+    # against the reference: the oracle's FP64 operator applied to the headline
+    # solution (timed: the CPU baseline sample) and the reference engine's summary
+    cpu, vs_oracle = None, None
+    if not args.no_cpu:
+        P = oracle_port()
+        r_o, t_o = oracle_residual(P, b, rhs, mu_head, summation, order)
+        g = golden(args.config)
+        applies = (g["iterations"] + 1) if g else (st64["fp64_applies"])
+        cpu = {"value": t_o * applies, "unit": "s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"1 FMM apply B*mu of the {b.n:,}-site system by the oracle "
+                         "(octree rebuilt, as the reference does per apply), OpenMP over all "
+                         f"host threads, {t_o:.3f} s, x {applies} applies per reference solve"}
+        vs_oracle = {"oracle_residual": r_o,
+                     "reference_solution": vs_reference_solution(args.config, rhs, mu_head),
+                     "plain_fp64_gpu_vs_reference_solution":
+                         vs_reference_solution(args.config, rhs, mu64)}
     total = world
     line = {
         "metric": METRIC, "value": t_head, "unit": "s", "n_gpus": world,
@@ -545,7 +696,9 @@ def run_ours(args):
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic (seeded water box, 12 point charges)",
         "config": dict(workload_config(args.config, b.n),
-                       l2="256 MB buffer written between timed steps",
+                       l2="256 MB buffer written between timed steps; the system's "
+                          "device data exceed L2" if b.n > 100000 else
+                          "256 MB buffer written between timed steps",
                        parallelism=f"replicas x{world}" if world > 1 else "1 GPU"),
         "solves_per_s": total / t_head,
         "method": "mixed precision + learned guess/preconditioner" if lrn else
@@ -555,25 +708,24 @@ def run_ours(args):
         "autotuned_fp32_apply_ms": tuned_ms,
         "iterations": {"fp32_applies": st["fp32_applies"],
                        "fp64_applies": st["fp64_applies"],
-                       "plain_fp64_iterations": st64["fp64_applies"]},
-        "parity": {"fp64_residual": resid, "mu_maxabs_vs_fp64": float(
-            np.abs(mu_head - mu64).max()), "epol_diff_hartree": de},
+                       "plain_fp64_iterations": st64["fp64_applies"] - 1},
+        "parity": parity,
+        "vs_oracle": vs_oracle,
+        "sections": sections or None,
         "batched": batched,
-        "large": large or None,
         "roofline": {"bound": "fp32", "kernel": "k_p2p32_m1<true> (FP32 dipole near field)",
                      "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak,
-                     "traffic": profiled_traffic("k_p2p32_m1_30k_sites.md")
-                     if args.config == "30k-fmm5" else None,
-                     "traffic_note": "DRAM bytes per launch from the committed ncu capture of "
-                                     "this workload (profiles/k_p2p32_m1_30k_sites.md); the "
-                                     "kernel's working set is L2-resident",
+                     "traffic": profiled_traffic(PROFILE_OF.get(args.config, "")),
+                     "traffic_note": "DRAM bytes per launch from the committed ncu capture "
+                                     f"profiles/{PROFILE_OF.get(args.config)}",
                      "peak_kind": "measured FFMA probe (cppe_gpu_fma_peak), no FP32 CUDA-core "
                                   "figure in MEASURED_PEAKS.json",
                      "algorithmic": f"{alg_pairs} pairs x {FLOP_PER_PAIR} FLOP per launch"},
         "roofline_fp64": {"bound": "fp64", "achieved": achieved64, "peak": fp64_peak,
                           "unit": "TFLOP/s", "frac": achieved64 / fp64_peak},
         "phases_ms": {"fp32": tim32, "double_float_residual": timdd, "fp64": tim64},
+        "m2l_translations_per_apply": m2l_pairs,
         "near_pairs_per_s": pairs_per_s,
         "peaks": {"hbm_gbs": pk.get("hbm_gbs"), "bf16_tflops": pk.get("bf16_tflops"),
                   "kind": pk_kind, "fp32_fma_tflops": fp32_peak, "fp64_fma_tflops": fp64_peak},
@@ -592,13 +744,15 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="30k-fmm5", choices=sorted(CONFIGS))
+    ap.add_argument("--config", default="1m-fmm6", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched section")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the built-in near-field / M2L schedule")
     ap.add_argument("--no-large", action="store_true",
-                    help="skip the 300k- and 1M-site sections")
+                    help="skip the extra 30k- and 300k-site sections")
+    ap.add_argument("--no-fp64", action="store_true",
+                    help="with --apply-only: skip the FP64 operator")
     ap.add_argument("--no-learned", action="store_true", help="skip the trained model")
     ap.add_argument("--model", default=os.path.join(ROOT, "cppe_gb300", "data",
                                                     "learned_water.npz"))
