@@ -47,9 +47,14 @@ def __getattr__(name):
         raise AttributeError(name)  # private names and submodules such as _build
     if name in _PY_SUBMODULES:
         raise AttributeError(name)  # let the import system load the submodule
-    try:
-        value = getattr(_load_native(), name)
-    except AttributeError:
+    native = _load_native()
+    # the reference package also re-exports its tensors submodule at the top
+    # level (src/cppe/__init__.py:3)
+    for src in (native, native.tensors):
+        if hasattr(src, name):
+            value = getattr(src, name)
+            break
+    else:
         raise AttributeError(f"module 'cppe_gb300' has no attribute '{name}'") from None
     globals()[name] = value
     return value
@@ -59,6 +64,7 @@ def __dir__():
     names = set(globals())
     if _native is not None:
         names.update(n for n in dir(_native) if not n.startswith("_"))
+        names.update(n for n in dir(_native.tensors) if not n.startswith("_"))
     return sorted(names)
 
 

@@ -181,6 +181,89 @@ __global__ void k_mp_energy(int n, const double* __restrict__ xyz, const double*
   grid_sum_last<1>(e, sh, rs.partials, rs.ticket, rs.out);
 }
 
+// Derivatives of the charge fields with respect to the charges' positions
+// (NuclearFields::nuclear_gradient, electric_fields.cc:77-104):
+// G[3a + c][3i + d] = q_a T2(r_i - R_a)_{cd}, T2 = grad grad 1/R; a thread per
+// (charge, target) pair writes its 3 x 3 block.
+__global__ void k_charge_field_grad(int nt, const double* __restrict__ xt, int ns,
+                                    const double* __restrict__ xs, const double* __restrict__ q,
+                                    double* __restrict__ G) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)nt * ns) return;
+  const int a = (int)(t / nt), i = (int)(t % nt);
+  const double d[3] = {xt[3 * i] - xs[3 * a], xt[3 * i + 1] - xs[3 * a + 1],
+                       xt[3 * i + 2] - xs[3 * a + 2]};
+  const double ir = rsqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+  const double ir3 = ir * ir * ir, ir5 = ir3 * ir * ir;
+  const size_t row = 3 * (size_t)nt;
+  for (int c = 0; c < 3; ++c)
+    for (int e = 0; e < 3; ++e)
+      G[(3 * (size_t)a + c) * row + 3 * (size_t)i + e] =
+            q[a] * (3.0 * d[c] * d[e] * ir5 - (c == e ? ir3 : 0.0));
+}
+
+// Gradient of sum_a Z_a phi_multipoles(R_a) with respect to the charges'
+// positions R_a (MultipoleExpansion::nuclear_gradient,
+// multipole_expansion.cc:35-62, through multipole_derivative with l = 1):
+//   dE/dR_a = Z_a sum_i [ q_i T1(d) - T2(d) mu_i + 1/2 sum_jk Theta_jk T3(d)_jkm ],
+//   d = R_a - r_i, T_n = n-th Cartesian derivative tensor of 1/R, with the
+// signs of the reference's Taylor prefactors (-1)^(k+1)/k!.  Block (b, a)
+// sums its sites for charge a into partials[(a * gridDim.x + b) * 3 + m].
+__global__ void k_mp_energy_grad(int n, const double* __restrict__ xyz,
+                                 const double* __restrict__ q, const double* __restrict__ mu,
+                                 const double* __restrict__ quad, int max_order,
+                                 const double* __restrict__ ax, const double* __restrict__ az,
+                                 double* __restrict__ partials) {
+  __shared__ double sh[32 * 3];
+  const int a = blockIdx.y;
+  double g[3] = {0.0, 0.0, 0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double d[3] = {ax[3 * a] - xyz[3 * i], ax[3 * a + 1] - xyz[3 * i + 1],
+                         ax[3 * a + 2] - xyz[3 * i + 2]};
+    const double ir = rsqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    const double ir3 = ir * ir * ir, ir5 = ir3 * ir * ir, ir7 = ir5 * ir * ir;
+    // charge: -q d / R^3 (= q T1)
+    const double qi = q ? q[i] : 0.0;
+    for (int m = 0; m < 3; ++m) g[m] -= qi * d[m] * ir3;
+    if (max_order > 0 && mu) {
+      // -T2 mu, T2_cm = 3 d_c d_m / R^5 - delta_cm / R^3
+      const double* u = mu + 3 * (size_t)i;
+      const double du = d[0] * u[0] + d[1] * u[1] + d[2] * u[2];
+      for (int m = 0; m < 3; ++m) g[m] -= 3.0 * du * d[m] * ir5 - u[m] * ir3;
+    }
+    if (max_order > 1 && quad) {
+      // 1/2 Theta_jk T3_jkm, T3_jkm = -15 d_j d_k d_m / R^7
+      //                              + 3 (delta_jk d_m + delta_jm d_k + delta_km d_j) / R^5
+      const double* Q = quad + 6 * (size_t)i;
+      const double Qm[3][3] = {{Q[0], Q[1], Q[2]}, {Q[1], Q[3], Q[4]}, {Q[2], Q[4], Q[5]}};
+      double Qd[3], dQd = 0.0;
+      const double tr = Q[0] + Q[3] + Q[5];
+      for (int j = 0; j < 3; ++j) {
+        Qd[j] = Qm[j][0] * d[0] + Qm[j][1] * d[1] + Qm[j][2] * d[2];
+        dQd += d[j] * Qd[j];
+      }
+      for (int m = 0; m < 3; ++m)
+        g[m] += 0.5 * (-15.0 * dQd * d[m] * ir7 + 3.0 * (tr * d[m] + 2.0 * Qd[m]) * ir5);
+    }
+  }
+  const double z = az[a];
+  for (int m = 0; m < 3; ++m) g[m] *= z;
+  block_sum<3>(g, sh);
+  if (threadIdx.x == 0)
+    for (int m = 0; m < 3; ++m) partials[((size_t)a * gridDim.x + blockIdx.x) * 3 + m] = g[m];
+}
+
+// grad[a][m] = sum of the blocks' partials in block order (fixed order).
+__global__ void k_mp_energy_grad_sum(int na, int nb, const double* __restrict__ partials,
+                                     double* __restrict__ grad) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 3 * na) return;
+  const int a = t / 3, m = t % 3;
+  double s = 0.0;
+  for (int b = 0; b < nb; ++b) s += partials[((size_t)a * nb + b) * 3 + m];
+  grad[t] = s;
+}
+
 }  // namespace cg
 
 using namespace cg;
@@ -559,6 +642,61 @@ int cppe_gpu_multipole_potential_energy(int n, const double* xyz, const double* 
                              ReduceSlots{part.p, tk.p, outv.p});
     CG_LAUNCH();
     CG_CUDA(cudaMemcpy(energy, outv.p, sizeof(double), cudaMemcpyDeviceToHost));
+    return CPPE_GPU_OK;
+  });
+}
+
+int cppe_gpu_charge_field_gradient(int ntgt, const double* xyz_tgt, int nsrc,
+                                   const double* xyz_src, const double* q, int device,
+                                   double* G) {
+  return guard([&]() -> int {
+    need(ntgt >= 0 && nsrc >= 0 && G, "null argument");
+    if (ntgt == 0 || nsrc == 0) return CPPE_GPU_OK;
+    need(xyz_tgt && xyz_src && q, "null argument");
+    CG_CUDA(cudaSetDevice(device));
+    DBuf<double> xt, xs, dq, dG;
+    xt.upload(xyz_tgt, 3 * (size_t)ntgt, 0);
+    xs.upload(xyz_src, 3 * (size_t)nsrc, 0);
+    dq.upload(q, nsrc, 0);
+    const size_t cnt = 9 * (size_t)ntgt * nsrc;
+    dG.alloc(cnt);
+    const long pairs = (long)ntgt * nsrc;
+    k_charge_field_grad<<<(unsigned)((pairs + 127) / 128), 128>>>(ntgt, xt.p, nsrc, xs.p, dq.p,
+                                                                  dG.p);
+    CG_LAUNCH();
+    CG_CUDA(cudaMemcpy(G, dG.p, cnt * sizeof(double), cudaMemcpyDeviceToHost));
+    return CPPE_GPU_OK;
+  });
+}
+
+int cppe_gpu_multipole_energy_gradient(int n, const double* xyz, const double* q,
+                                       const double* mu, const double* quad, int max_order,
+                                       int natoms, const double* atom_xyz,
+                                       const double* atom_charge, int device, double* grad) {
+  return guard([&]() -> int {
+    need(natoms >= 0 && n >= 0 && (grad || natoms == 0), "null argument");
+    if (natoms == 0) return CPPE_GPU_OK;
+    std::fill(grad, grad + 3 * (size_t)natoms, 0.0);
+    if (n == 0) return CPPE_GPU_OK;
+    need(xyz && atom_xyz && atom_charge, "null argument");
+    need(max_order >= 0 && max_order <= 2, "multipoles above order 2 are not supported");
+    CG_CUDA(cudaSetDevice(device));
+    DBuf<double> dx, dq, dm, dQ, ax, az, part, dg;
+    dx.upload(xyz, 3 * (size_t)n, 0);
+    if (q) dq.upload(q, n, 0);
+    if (mu && max_order > 0) dm.upload(mu, 3 * (size_t)n, 0);
+    if (quad && max_order > 1) dQ.upload(quad, 6 * (size_t)n, 0);
+    ax.upload(atom_xyz, 3 * (size_t)natoms, 0);
+    az.upload(atom_charge, natoms, 0);
+    const int nb = std::max(1, std::min((n + 255) / 256, 304));
+    part.alloc(3 * (size_t)natoms * nb);
+    dg.alloc(3 * (size_t)natoms);
+    k_mp_energy_grad<<<dim3(nb, natoms), 256>>>(n, dx.p, dq.p, dm.p, dQ.p, max_order, ax.p,
+                                                az.p, part.p);
+    CG_LAUNCH();
+    k_mp_energy_grad_sum<<<(3 * natoms + 127) / 128, 128>>>(natoms, nb, part.p, dg.p);
+    CG_LAUNCH();
+    CG_CUDA(cudaMemcpy(grad, dg.p, 3 * (size_t)natoms * sizeof(double), cudaMemcpyDeviceToHost));
     return CPPE_GPU_OK;
   });
 }

@@ -31,6 +31,8 @@
 #include <unordered_map>
 #include <vector>
 
+#include "cppe_gpu.h"
+
 struct cppe_gpu_system;
 
 namespace libcppe {
@@ -215,6 +217,8 @@ class NuclearFields {
  public:
   NuclearFields(Molecule mol, std::vector<Potential> potentials);
   Vector compute();
+  // (3 natoms) x (3 npolsites): d(field at site i)/d(position of atom a)
+  Matrix nuclear_gradient();
 };
 
 class MultipoleFields {
@@ -254,6 +258,8 @@ class MultipoleExpansion {
   MultipoleExpansion(Molecule core, std::vector<Potential> potentials)
         : m_mol(std::move(core)), m_potentials(std::move(potentials)) {}
   double interaction_energy();
+  // natoms x 3: gradient of interaction_energy with respect to the atom positions
+  Matrix nuclear_gradient();
 };
 
 using PeEnergy = std::unordered_map<std::string, std::unordered_map<std::string, double>>;
@@ -268,6 +274,7 @@ class CppeState {
   bool m_make_guess = true;
   PrintCallback m_printer;
   std::shared_ptr<InducedMoments> m_solver;  // reused across SCF steps
+  std::shared_ptr<void> m_eef;               // 3-right-hand-side batch of induced_moments_eef
 
  public:
   CppeState() = default;
@@ -292,6 +299,27 @@ class CppeState {
   Vector get_multipole_fields() const { return m_multipole_fields; }
   std::string get_energy_summary_string();
   Matrix induced_moments_eef();
+  Matrix nuclear_interaction_energy_gradient();
+  Matrix nuclear_field_gradient();
+};
+
+// Field of dipole sources at the sites, as the reference's Tree<1,3>
+// computes it (src/core/fmm/tree.cc:350-394): F = -T S, by FMM or direct
+// summation, on the GPU.  The reference's Python module exposes the class as
+// fmm.Tree without a constructor (src/python_iface/export_fmm.cc:25-31); this
+// one is built from positions and options.
+class DipoleTree {
+  std::vector<double> m_xyz, m_aiso;
+  std::vector<int> m_eptr, m_eidx;
+  int m_ncrit, m_order;
+  double m_theta, m_damping;
+
+ public:
+  DipoleTree(std::vector<double> xyz, int ncrit, int order, double theta, double damping,
+             std::vector<double> alpha_iso, std::vector<std::vector<int>> exclusions);
+  int size() const { return (int)m_aiso.size(); }
+  // S: 3n dipoles; F: 3n field values (overwritten)
+  void compute_field(const double* S, double* F, bool fmm) const;
 };
 
 // math.hh helpers
@@ -304,6 +332,19 @@ std::vector<double> prefactors_nuclei(unsigned k);
 int multipole_components(int k);
 std::array<double, 9> triangle_to_mat(const std::vector<double>& y);
 std::vector<double> mat_to_triangle(const std::array<double, 9>& m);
+
+// tensors submodule (tensors_autogen.hh, tensors_recursive.hh): Cartesian
+// derivative tensors of 1/R and of the Thole-damped potential
+Vector T_tensor(int k, const std::array<double, 3>& R);
+Vector T_tensor_damp_thole(int k, const std::array<double, 3>& R, double a);
+Vector T_recursive(int k, const std::array<double, 3>& R, double damping_factor = 0.0);
+int xyz2idx(int x, int y, int z);
+
+// PeOptions as C-ABI options (precision and device from gpu_config()), and a
+// site list's exclusions as CSR (global site indices, as the reference keeps them)
+cppe_gpu_options to_gpu(const PeOptions& o);
+void pack_exclusions(const std::vector<Potential>& pots, std::vector<int>& ptr,
+                     std::vector<int>& idx);
 
 // Throws the exception that matches a C-ABI status (std::runtime_error with
 // the library message; NOT_CONVERGED carries the reference's message).

@@ -7,6 +7,7 @@
 #include <numeric>
 #include <sstream>
 
+#include "cppe_gpu.h"
 #include "cppe_host.hh"
 
 namespace libcppe {
@@ -47,6 +48,7 @@ void CppeState::set_potentials(std::vector<Potential> potentials) {
     }
   }
   m_solver.reset();
+  m_eef.reset();
 }
 
 void CppeState::calculate_static_energies_and_fields() {
@@ -96,18 +98,76 @@ void CppeState::update_induced_moments(const Vector& elec_fields, bool elec_only
   }
 }
 
+namespace {
+// The three unit-field solves of induced_moments_eef as one batch (one system,
+// three right-hand sides): one set of launches per iteration for all three,
+// with the near-field pair tensors shared between them.
+struct EefBatch {
+  cppe_gpu_batch* b = nullptr;
+  int n             = 0;
+  ~EefBatch() {
+    if (b) cppe_gpu_batch_destroy(b);
+  }
+};
+}  // namespace
+
+// CppeState::induced_moments_eef (cppe_state.cc:111-128): induced moments for
+// unit external fields along x, y and z at every polarizable site, each from
+// the first-call guess alpha F to the same threshold.  The reference solves
+// them one after another with a new InducedMoments; here they are one batched
+// solve on a handle kept across calls.  The printer receives one line per
+// field direction with its iteration count (the batch records no per-iteration
+// norms).
 Matrix CppeState::induced_moments_eef() {
-  InducedMoments ind(m_potentials, m_options);
-  ind.set_print_callback(m_printer);
   const size_t n3 = 3 * m_polarizable_sites;
   Matrix ret(n3, 3);
-  for (int a = 0; a < 3; ++a) {
-    Vector f(n3, 0.0);
-    for (size_t s = 0; s < m_polarizable_sites; ++s) f[3 * s + a] = 1.0;
-    Vector col = ind.compute(f, Vector(n3, 0.0), true);
-    for (size_t i = 0; i < n3; ++i) ret(i, a) = col[i];
+  if (m_polarizable_sites == 0) return ret;
+  if (!m_eef) {
+    auto polsites = get_polarizable_sites(m_potentials);
+    std::vector<double> xyz, a6;
+    for (const auto& p : polsites) {
+      xyz.insert(xyz.end(), {p.m_x, p.m_y, p.m_z});
+      auto a = p.get_polarizability().get_values_vec();
+      a6.insert(a6.end(), a.begin(), a.end());
+    }
+    std::vector<int> eptr, eidx;
+    pack_exclusions(polsites, eptr, eidx);
+    const int n               = (int)polsites.size();
+    const int off[2]          = {0, n};
+    cppe_gpu_options g        = to_gpu(m_options);
+    const int direct_below    = g.summation == CPPE_GPU_FMM ? 0 : n + 1;
+    auto eb                   = std::make_shared<EefBatch>();
+    eb->n                     = n;
+    throw_on_status(cppe_gpu_batch_create(1, off, xyz.data(), a6.data(), eptr.data(),
+                                          eidx.empty() ? nullptr : eidx.data(), 3,
+                                          direct_below, &g, &eb->b));
+    m_eef = eb;
   }
+  auto* eb = static_cast<EefBatch*>(m_eef.get());
+  Vector f(3 * n3, 0.0), mu(3 * n3, 0.0);
+  for (int a = 0; a < 3; ++a)
+    for (size_t s = 0; s < m_polarizable_sites; ++s) f[a * n3 + 3 * s + a] = 1.0;
+  int iters[3] = {0, 0, 0};
+  const int st = cppe_gpu_batch_solve(eb->b, f.data(), mu.data(), iters);
+  for (int a = 0; a < 3; ++a)
+    m_printer("eef " + std::string(1, "xyz"[a]) + ": " + std::to_string(iters[a]) +
+              " iterations");
+  if (st == CPPE_GPU_NOT_CONVERGED)
+    throw std::runtime_error("Failed to converge induced dipole moments.");
+  throw_on_status(st);
+  for (int a = 0; a < 3; ++a)
+    for (size_t i = 0; i < n3; ++i) ret(i, a) = mu[a * n3 + i];
   return ret;
+}
+
+// CppeState::nuclear_interaction_energy_gradient / nuclear_field_gradient
+// (cppe_state.cc:73-81)
+Matrix CppeState::nuclear_interaction_energy_gradient() {
+  return MultipoleExpansion(m_mol, m_potentials).nuclear_gradient();
+}
+
+Matrix CppeState::nuclear_field_gradient() {
+  return NuclearFields(m_mol, m_potentials).nuclear_gradient();
 }
 
 double CppeState::get_total_energy_for_category(const std::string& c) {

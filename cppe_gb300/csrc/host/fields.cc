@@ -11,7 +11,6 @@
 
 namespace libcppe {
 
-namespace {
 cppe_gpu_options to_gpu(const PeOptions& o) {
   cppe_gpu_options g;
   cppe_gpu_default_options(&g);
@@ -39,6 +38,7 @@ void pack_exclusions(const std::vector<Potential>& pots, std::vector<int>& ptr,
   }
 }
 
+namespace {
 void check_size(const Vector& v, size_t n, const char* what) {
   if (v.size() != n)
     throw std::invalid_argument(std::string(what) + ": expected a vector of length " +
@@ -134,6 +134,21 @@ Vector NuclearFields::compute() {
   return F;
 }
 
+Matrix NuclearFields::nuclear_gradient() {
+  const int n = (int)m_polsites.size(), na = (int)m_mol.size();
+  Matrix G(3 * (size_t)na, 3 * (size_t)n);
+  if (n == 0 || na == 0) return G;
+  std::vector<double> xt, xs, q;
+  for (const auto& p : m_polsites) xt.insert(xt.end(), {p.m_x, p.m_y, p.m_z});
+  for (const auto& a : m_mol) {
+    xs.insert(xs.end(), {a.m_x, a.m_y, a.m_z});
+    q.push_back((double)a.charge);
+  }
+  throw_on_status(cppe_gpu_charge_field_gradient(n, xt.data(), na, xs.data(), q.data(),
+                                                 gpu_config().device, G.data.data()));
+  return G;
+}
+
 // --- MultipoleFields (electric_fields.cc:106-189) -------------------------------
 Vector MultipoleFields::compute() {
   const int n = (int)m_potentials.size();
@@ -215,38 +230,99 @@ Vector InducedMoments::compute(const Vector& rhs, Vector guess, bool make_guess)
   return mu;
 }
 
-// --- MultipoleExpansion (multipole_expansion.cc:10-33) --------------------------
+// --- MultipoleExpansion (multipole_expansion.cc:10-62) --------------------------
+namespace {
+struct PackedSites {
+  std::vector<double> xyz, q, mu, quad, ax, az;
+  int max_order = 0;
+};
+PackedSites pack_multipoles(const std::vector<Potential>& pots, const Molecule& mol) {
+  PackedSites p;
+  const size_t n = pots.size();
+  p.q.assign(n, 0.0), p.mu.assign(3 * n, 0.0), p.quad.assign(6 * n, 0.0);
+  for (size_t i = 0; i < n; ++i) {
+    const Potential& s = pots[i];
+    p.xyz.insert(p.xyz.end(), {s.m_x, s.m_y, s.m_z});
+    for (const auto& m : s.get_multipoles()) {
+      auto v = m.get_values_vec();
+      if (m.m_k == 0)
+        p.q[i] += v.at(0);
+      else if (m.m_k == 1)
+        for (int c = 0; c < 3; ++c) p.mu[3 * i + c] += v.at(c);
+      else if (m.m_k == 2)
+        for (int c = 0; c < 6; ++c) p.quad[6 * i + c] += v.at(c);
+      else
+        throw std::runtime_error("multipoles above order 2 are not supported");
+      p.max_order = std::max<int>(p.max_order, m.m_k);
+    }
+  }
+  for (const auto& a : mol) {
+    p.ax.insert(p.ax.end(), {a.m_x, a.m_y, a.m_z});
+    p.az.push_back((double)a.charge);
+  }
+  return p;
+}
+}  // namespace
+
 double MultipoleExpansion::interaction_energy() {
   const int n = (int)m_potentials.size();
   if (n == 0 || m_mol.empty()) return 0.0;
-  std::vector<double> xyz, q(n, 0.0), mu(3 * (size_t)n, 0.0), quad(6 * (size_t)n, 0.0);
-  int max_order = 0;
-  for (int i = 0; i < n; ++i) {
-    const Potential& p = m_potentials[i];
-    xyz.insert(xyz.end(), {p.m_x, p.m_y, p.m_z});
-    for (const auto& m : p.get_multipoles()) {
-      auto v = m.get_values_vec();
-      if (m.m_k == 0)
-        q[i] += v.at(0);
-      else if (m.m_k == 1)
-        for (int c = 0; c < 3; ++c) mu[3 * i + c] += v.at(c);
-      else if (m.m_k == 2)
-        for (int c = 0; c < 6; ++c) quad[6 * i + c] += v.at(c);
-      else
-        throw std::runtime_error("multipoles above order 2 are not supported");
-      max_order = std::max<int>(max_order, m.m_k);
-    }
-  }
-  std::vector<double> ax, az;
-  for (const auto& a : m_mol) {
-    ax.insert(ax.end(), {a.m_x, a.m_y, a.m_z});
-    az.push_back((double)a.charge);
-  }
+  const PackedSites p = pack_multipoles(m_potentials, m_mol);
   double e = 0.0;
   throw_on_status(cppe_gpu_multipole_potential_energy(
-        n, xyz.data(), q.data(), mu.data(), quad.data(), max_order, (int)m_mol.size(),
-        ax.data(), az.data(), gpu_config().device, &e));
+        n, p.xyz.data(), p.q.data(), p.mu.data(), p.quad.data(), p.max_order,
+        (int)m_mol.size(), p.ax.data(), p.az.data(), gpu_config().device, &e));
   return e;
+}
+
+Matrix MultipoleExpansion::nuclear_gradient() {
+  const int n = (int)m_potentials.size(), na = (int)m_mol.size();
+  Matrix G(na, 3);
+  if (n == 0 || na == 0) return G;
+  const PackedSites p = pack_multipoles(m_potentials, m_mol);
+  throw_on_status(cppe_gpu_multipole_energy_gradient(
+        n, p.xyz.data(), p.q.data(), p.mu.data(), p.quad.data(), p.max_order, na,
+        p.ax.data(), p.az.data(), gpu_config().device, G.data.data()));
+  return G;
+}
+
+// --- DipoleTree (fmm/tree.cc:350-394, Tree<1,3>) -------------------------------
+DipoleTree::DipoleTree(std::vector<double> xyz, int ncrit, int order, double theta,
+                       double damping, std::vector<double> alpha_iso,
+                       std::vector<std::vector<int>> exclusions)
+      : m_xyz(std::move(xyz)), m_ncrit(ncrit), m_order(order), m_theta(theta),
+        m_damping(damping) {
+  if (m_xyz.size() % 3 != 0) throw std::invalid_argument("positions must be n x 3");
+  const size_t n = m_xyz.size() / 3;
+  m_aiso         = alpha_iso.empty() ? std::vector<double>(n, 0.0) : std::move(alpha_iso);
+  if (m_aiso.size() != n) throw std::invalid_argument("one polarizability per site");
+  if (m_damping > 0.0)
+    for (double a : m_aiso)
+      if (!(a > 0.0))
+        throw std::invalid_argument("Thole damping needs a positive polarizability per site");
+  if (!exclusions.empty() && exclusions.size() != n)
+    throw std::invalid_argument("one exclusion list per site");
+  m_eptr.assign(1, 0);
+  for (size_t i = 0; i < n; ++i) {
+    if (!exclusions.empty())
+      for (int e : exclusions[i]) m_eidx.push_back(e);
+    m_eptr.push_back((int)m_eidx.size());
+  }
+}
+
+void DipoleTree::compute_field(const double* S, double* F, bool fmm) const {
+  const int n = size();
+  if (n == 0) return;
+  // MultipoleFields' dipole term is -F_tree(mu) (electric_fields.cc:164-176):
+  // the static-field entry point with only dipoles gives -F_tree.
+  std::vector<double> q(n, 0.0), quad(6 * (size_t)n, 0.0), out(3 * (size_t)n, 0.0);
+  std::vector<int> pol(n, 1);
+  throw_on_status(cppe_gpu_multipole_fields(
+        n, m_xyz.data(), q.data(), S, quad.data(), 1, pol.data(), m_aiso.data(),
+        m_eptr.data(), m_eidx.empty() ? nullptr : m_eidx.data(),
+        fmm ? CPPE_GPU_FMM : CPPE_GPU_DIRECT, m_ncrit, m_order, m_theta,
+        m_damping > 0.0 ? 1 : 0, m_damping, gpu_config().device, out.data()));
+  for (size_t i = 0; i < out.size(); ++i) F[i] = -out[i];
 }
 
 }  // namespace libcppe

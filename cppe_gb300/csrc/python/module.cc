@@ -94,10 +94,29 @@ py::dict options_to_dict(const PeOptions& o) {
   return d;
 }
 
-[[noreturn]] void unsupported(const char* what) {
-  throw std::runtime_error(std::string(what) +
-                           " is not provided by cppe_gb300 (outside the induced-dipole path)");
+std::array<double, 3> vec3(const Arr& a, const char* what) {
+  if (a.size() != 3) throw std::invalid_argument(std::string(what) + " must have 3 components");
+  return {a.data()[0], a.data()[1], a.data()[2]};
 }
+
+// fmm.Tree: a DipoleTree and the caller's source array
+struct PyDipoleTree {
+  std::shared_ptr<DipoleTree> tree;
+  py::object sources = py::none();
+  void compute(py::array field, bool fmm) {
+    const size_t n3 = 3 * (size_t)tree->size();
+    if (sources.is_none()) throw std::runtime_error("Tree: call set_sources first");
+    auto S = py::array_t<double, py::array::c_style | py::array::forcecast>::ensure(sources);
+    if (!S || (size_t)S.size() != n3)
+      throw std::invalid_argument("Tree: sources must hold 3 values per site");
+    if (!py::isinstance<py::array_t<double>>(field) || (size_t)field.size() != n3 ||
+        !(field.flags() & py::array::c_style) || !field.writeable())
+      throw std::invalid_argument(
+            "Tree: field must be a writable C-contiguous float64 array of 3 values per site");
+    tree->compute_field(S.data(), static_cast<double*>(field.mutable_data()), fmm);
+  }
+};
+
 
 }  // namespace
 
@@ -165,8 +184,9 @@ PYBIND11_MODULE(pycppe, m) {
         .def("set_potentials", &CppeState::set_potentials)
         .def("calculate_static_energies_and_fields", &CppeState::calculate_static_energies_and_fields)
         .def("nuclear_interaction_energy_gradient",
-             [](CppeState&) { unsupported("nuclear_interaction_energy_gradient"); })
-        .def("nuclear_field_gradient", [](CppeState&) { unsupported("nuclear_field_gradient"); })
+             [](CppeState& s) { return from_mat(s.nuclear_interaction_energy_gradient()); })
+        .def("nuclear_field_gradient",
+             [](CppeState& s) { return from_mat(s.nuclear_field_gradient()); })
         .def("get_induced_moments", &CppeState::get_induced_moments)
         .def("induced_moments_eef", [](CppeState& s) { return from_mat(s.induced_moments_eef()); })
         .def_readwrite("energies", &CppeState::m_pe_energy)
@@ -188,7 +208,7 @@ PYBIND11_MODULE(pycppe, m) {
   py::class_<NuclearFields>(m, "NuclearFields", "Electric fields created by nuclei")
         .def(py::init<Molecule, std::vector<Potential>>())
         .def("compute", [](NuclearFields& f) { return from_vec(f.compute()); })
-        .def("nuclear_gradient", [](NuclearFields&) { unsupported("NuclearFields.nuclear_gradient"); });
+        .def("nuclear_gradient", [](NuclearFields& f) { return from_mat(f.nuclear_gradient()); });
   py::class_<MultipoleFields, std::shared_ptr<MultipoleFields>>(m, "MultipoleFields",
                                                                 "Electric fields created by multipoles")
         .def(py::init([](std::vector<Potential> p, py::dict o) {
@@ -230,7 +250,7 @@ PYBIND11_MODULE(pycppe, m) {
         .def(py::init<Molecule, std::vector<Potential>>())
         .def("interaction_energy", &MultipoleExpansion::interaction_energy)
         .def("nuclear_gradient",
-             [](MultipoleExpansion&) { unsupported("MultipoleExpansion.nuclear_gradient"); });
+             [](MultipoleExpansion& e) { return from_mat(e.nuclear_gradient()); });
 
   // export_math.cc
   m.def("triangle_to_mat", [](std::vector<double> y) {
@@ -255,6 +275,56 @@ PYBIND11_MODULE(pycppe, m) {
   m.def("prefactors", &prefactors, "Prefactors for the multipole components (alphabetical order)");
   m.def("prefactors_nuclei", &prefactors_nuclei);
   m.def("multipole_components", &multipole_components);
+
+  // export_tensors.cc: Cartesian derivative tensors of 1/R and of the
+  // Thole-damped potential.  The reference binds T1_damp_thole under the name
+  // T0_damp_thole (export_tensors.cc:32), so it is unreachable there; here
+  // every order has its own name.
+  py::module ten = m.def_submodule("tensors", "Tensor submodule");
+  ten.def("T_recursive",
+          [](int k, Arr R, double damping_factor) {
+            return from_vec(T_recursive(k, vec3(R, "Rij"), damping_factor));
+          },
+          py::arg("k"), py::arg("Rij"), py::arg("damping_factor") = 0.0);
+  ten.def("xyz2idx", &xyz2idx);
+  py::list T, Td;
+  for (int k = 0; k <= 6; ++k) {
+    auto f  = [k](Arr R) { return from_vec(T_tensor(k, vec3(R, "rij"))); };
+    auto fd = [k](Arr R, double a) { return from_vec(T_tensor_damp_thole(k, vec3(R, "rij"), a)); };
+    const std::string nm = "T" + std::to_string(k);
+    ten.def(nm.c_str(), f);
+    ten.def((nm + "_damp_thole").c_str(), fd);
+    T.append(ten.attr(nm.c_str()));
+    Td.append(ten.attr((nm + "_damp_thole").c_str()));
+  }
+  ten.attr("T")            = T;
+  ten.attr("T_damp_thole") = Td;
+
+  // export_fmm.cc: Tree<1,3> -- the field of dipole sources at the sites by
+  // FMM or by direct summation.  The reference gives the class no Python
+  // constructor; this one takes positions (n x 3, bohr) and the tree options.
+  // set_sources keeps a reference to the caller's array (the reference keeps a
+  // pointer to it), read again by every compute call.
+  py::module fmm = m.def_submodule("fmm", "Module for fast multipole methods.");
+  py::class_<PyDipoleTree, std::shared_ptr<PyDipoleTree>>(fmm, "Tree", "Tree class for FMM/BH.")
+        .def(py::init([](Arr positions, int ncrit, int order, double theta, double damping,
+                         py::object polarizabilities, py::object exclusions) {
+               auto t = std::make_shared<PyDipoleTree>();
+               std::vector<double> aiso;
+               if (!polarizabilities.is_none()) aiso = to_vec(polarizabilities.cast<Arr>());
+               std::vector<std::vector<int>> ex;
+               if (!exclusions.is_none()) ex = exclusions.cast<std::vector<std::vector<int>>>();
+               t->tree = std::make_shared<DipoleTree>(to_vec(positions), ncrit, order, theta,
+                                                      damping, aiso, ex);
+               return t;
+             }),
+             py::arg("positions"), py::arg("ncrit") = 64, py::arg("order") = 5,
+             py::arg("theta") = 0.5, py::arg("damping") = 0.0,
+             py::arg("polarizabilities") = py::none(), py::arg("exclusions") = py::none())
+        .def("set_sources", [](PyDipoleTree& t, py::array sources) { t.sources = sources; })
+        .def("compute_field_fmm", [](PyDipoleTree& t, py::array field) { t.compute(field, true); })
+        .def("compute_field_exact",
+             [](PyDipoleTree& t, py::array field) { t.compute(field, false); });
 
   // GPU controls (no counterpart in the reference)
   m.def("set_gpu_options",

@@ -28,6 +28,11 @@
  *   cppe_gpu_multipole_potential_energy
  *                                    MultipoleExpansion::interaction_energy
  *                                                            src/core/multipole_expansion.cc:10-33
+ *   cppe_gpu_charge_field_gradient   NuclearFields::nuclear_gradient
+ *                                                            src/core/electric_fields.cc:77-104
+ *   cppe_gpu_multipole_energy_gradient
+ *                                    MultipoleExpansion::nuclear_gradient
+ *                                                            src/core/multipole_expansion.cc:35-62
  *   cppe_gpu_tree_info               build_shared_tree + interact_dehnen_lazy
  *                                    src/core/fmm/tree.cc:134-237, calculate.cc:74-127
  *                                    (host-only; no GPU needed)
@@ -151,6 +156,24 @@ int cppe_gpu_multipole_potential_energy(int n, const double* xyz, const double* 
                                         int natoms, const double* atom_xyz,
                                         const double* atom_charge, int device,
                                         double* energy);
+
+/* Derivative of the point-charge fields at the ntgt targets with respect to
+ * the nsrc charge positions (NuclearFields::nuclear_gradient,
+ * src/core/electric_fields.cc:77-104): G is (3 nsrc) x (3 ntgt), row-major,
+ * G[3a + c][3i + d] = q_a T2(r_i - R_a)_cd with T2 = grad grad 1/R. */
+int cppe_gpu_charge_field_gradient(int ntgt, const double* xyz_tgt, int nsrc,
+                                   const double* xyz_src, const double* q, int device,
+                                   double* G);
+
+/* Gradient of sum_atoms Z_a * phi_multipoles(R_a) with respect to the atom
+ * positions (MultipoleExpansion::nuclear_gradient,
+ * src/core/multipole_expansion.cc:35-62): grad is natoms x 3, row-major.
+ * Multipoles up to order 2 (q, mu, quad as in
+ * cppe_gpu_multipole_potential_energy). */
+int cppe_gpu_multipole_energy_gradient(int n, const double* xyz, const double* q,
+                                       const double* mu, const double* quad, int max_order,
+                                       int natoms, const double* atom_xyz,
+                                       const double* atom_charge, int device, double* grad);
 
 /* Host-only: octree and interaction-list sizes for a geometry (no GPU). */
 int cppe_gpu_tree_info(int n, const double* xyz, int ncrit, double theta, int* ncells,
