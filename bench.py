@@ -498,6 +498,49 @@ def system_section(cfg, dev, flush, steps, model_path=None, oracle_check="residu
     return out
 
 
+def ingest_section(dev):
+    """The 1,000,002-site water box as a .pot file (AA, 12 decimals; written
+    before timing), read into arrays with CSR exclusions through the C ABI
+    (cppe_gpu_potfile_read + _arrays), read into the reference's per-site
+    objects (PotfileReader.read), and turned into a GPU system (octree, lists
+    and uploads: cppe_gpu_create, FMM order 6)."""
+    import ctypes
+    import tempfile
+    import cppe_gb300 as cppe
+    from cppe_gb300 import capi, synthetic
+    b = synthetic.water_box(333334, seed=4)
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "w1m.pot")
+        synthetic.write_potfile(b, path)
+        size = os.path.getsize(path)
+        L = capi.lib()
+        h = ctypes.c_void_p()
+        t0 = time.perf_counter()
+        capi.check(L.cppe_gpu_potfile_read(os.fsencode(path), ctypes.byref(h)))
+        n = b.n
+        xyz, a6 = np.zeros((n, 3)), np.zeros((n, 6))
+        q, mu, quad = np.zeros(n), np.zeros((n, 3)), np.zeros((n, 6))
+        pol, ep, ei = np.zeros(n, np.int32), np.zeros(n + 1, np.int32), np.zeros(2 * n, np.int32)
+        capi.check(L.cppe_gpu_potfile_arrays(h, capi.dp(xyz), capi.dp(q), capi.dp(mu),
+                                             capi.dp(quad), capi.dp(a6), capi.ip(pol),
+                                             capi.ip(ep), capi.ip(ei), None))
+        t_arrays = time.perf_counter() - t0
+        L.cppe_gpu_potfile_free(h)
+        t0 = time.perf_counter()
+        pots = cppe.PotfileReader(path).read()
+        t_obj = time.perf_counter() - t0
+        del pots
+    t0 = time.perf_counter()
+    s = capi.System(xyz, a6, ep, ei, summation=capi.FMM, order=6, ncrit=64, theta=0.5,
+                    damp=True, device=dev)
+    t_create = time.perf_counter() - t0
+    s.close()
+    return {"workload": "1,000,002-site water box, .pot file in AA", "file_bytes": size,
+            "arrays_csr_s": t_arrays, "objects_s": t_obj, "gpu_system_create_s": t_create,
+            "exclusions_match": bool(np.array_equal(ep, b.excl_ptr) and
+                                     np.array_equal(ei, b.excl_idx))}
+
+
 def profiled_traffic(md_name):
     """DRAM bytes (read + write) per launch from a committed ncu summary."""
     path = os.path.join(ROOT, "profiles", md_name)
@@ -670,6 +713,7 @@ def run_ours(args):
         if args.config != "300k-fmm6":
             sections["precision_300k"] = system_section("300k-fmm6", dev, flush, 2,
                                                         args.model)
+        sections["ingest_1m"] = ingest_section(dev)
     batched = batched_section(dev, 1, flush) if (not args.no_batched and world == 1) else None
     if rank != 0:
         return

@@ -103,6 +103,11 @@ def lib():
                                          ctypes.c_uint, D]
         l.cppe_gpu_learned_data.argtypes = [ctypes.c_void_p, D, D, F, F]
         l.cppe_gpu_set_model.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        l.cppe_gpu_potfile_read.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)]
+        l.cppe_gpu_potfile_info.argtypes = [ctypes.c_void_p, I, I, I, L]
+        l.cppe_gpu_potfile_arrays.argtypes = [ctypes.c_void_p, D, D, D, D, D, I, I, I,
+                                              ctypes.c_char_p]
+        l.cppe_gpu_potfile_free.argtypes = [ctypes.c_void_p]
     return _lib
 
 
@@ -443,6 +448,34 @@ def multipole_fields(xyz, q, mu, quad, max_order, polarizable=None, alpha_iso=No
         dp(args[4]), ip(args[5]), ip(args[6]), FMM if fmm else DIRECT, ncrit, order, theta,
         int(damp), damping, device, dp(F)))
     return F
+
+
+def read_potfile(path):
+    """Sites of a .pot file as arrays (cppe_gpu_potfile_*): xyz (n,3) bohr, q,
+    mu (n,3), quad (n,6), alpha6 (n,6), polarizable, excl_ptr, excl_idx
+    (CSR), elements, max_order."""
+    h = ctypes.c_void_p()
+    check(lib().cppe_gpu_potfile_read(os.fsencode(path), ctypes.byref(h)))
+    try:
+        n, mo, npol, ne = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0), ctypes.c_long(0)
+        check(lib().cppe_gpu_potfile_info(h, ctypes.byref(n), ctypes.byref(mo),
+                                          ctypes.byref(npol), ctypes.byref(ne)))
+        n, ne = n.value, ne.value
+        out = dict(xyz=np.zeros((n, 3)), q=np.zeros(n), mu=np.zeros((n, 3)),
+                   quad=np.zeros((n, 6)), alpha6=np.zeros((n, 6)),
+                   polarizable=np.zeros(n, np.int32), excl_ptr=np.zeros(n + 1, np.int32),
+                   excl_idx=np.zeros(max(ne, 1), np.int32))
+        el = ctypes.create_string_buffer(4 * max(n, 1))
+        check(lib().cppe_gpu_potfile_arrays(
+            h, dp(out["xyz"]), dp(out["q"]), dp(out["mu"]), dp(out["quad"]), dp(out["alpha6"]),
+            ip(out["polarizable"]), ip(out["excl_ptr"]), ip(out["excl_idx"]), el))
+        out["excl_idx"] = out["excl_idx"][:ne]
+        raw = el.raw  # one copy of the buffer (each .raw access copies it)
+        out["elements"] = [raw[4 * i:4 * i + 4].rstrip(b"\0").decode() for i in range(n)]
+        out["max_order"] = mo.value
+        return out
+    finally:
+        lib().cppe_gpu_potfile_free(h)
 
 
 def tree_info(xyz, ncrit=64, theta=0.5):

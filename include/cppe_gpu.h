@@ -28,6 +28,7 @@
  *   cppe_gpu_multipole_potential_energy
  *                                    MultipoleExpansion::interaction_energy
  *                                                            src/core/multipole_expansion.cc:10-33
+ *   cppe_gpu_potfile_*               PotfileReader::read     src/core/potfile_reader.cc:31-179
  *   cppe_gpu_charge_field_gradient   NuclearFields::nuclear_gradient
  *                                                            src/core/electric_fields.cc:77-104
  *   cppe_gpu_multipole_energy_gradient
@@ -174,6 +175,24 @@ int cppe_gpu_multipole_energy_gradient(int n, const double* xyz, const double* q
                                        const double* mu, const double* quad, int max_order,
                                        int natoms, const double* atom_xyz,
                                        const double* atom_charge, int device, double* grad);
+
+/* Host-only potfile ingest (PotfileReader::read, src/core/potfile_reader.cc:
+ * 31-179) straight into the arrays cppe_gpu_create and
+ * cppe_gpu_multipole_fields take: same format, unit conversion (AA -> bohr),
+ * quadrupole trace removal, zero defaults and error messages, with the
+ * exclusion lists as CSR (0-based site indices, file order per site) instead
+ * of per-site lists.  Multipoles up to order 2.  cppe_gpu_potfile_arrays
+ * copies into caller buffers (any may be NULL): xyz 3n, q n, mu 3n, quad 6n
+ * (xx,xy,xz,yy,yz,zz), alpha6 6n, polarizable n, excl_ptr n+1,
+ * excl_idx nexcl, elements 4n (NUL-padded symbols). */
+typedef struct cppe_gpu_potfile cppe_gpu_potfile;
+int cppe_gpu_potfile_read(const char* path, cppe_gpu_potfile** out);
+int cppe_gpu_potfile_info(const cppe_gpu_potfile* p, int* n, int* max_order, int* npolarizable,
+                          long* nexcl);
+int cppe_gpu_potfile_arrays(const cppe_gpu_potfile* p, double* xyz, double* q, double* mu,
+                            double* quad, double* alpha6, int* polarizable, int* excl_ptr,
+                            int* excl_idx, char* elements);
+int cppe_gpu_potfile_free(cppe_gpu_potfile* p);
 
 /* Host-only: octree and interaction-list sizes for a geometry (no GPU). */
 int cppe_gpu_tree_info(int n, const double* xyz, int ncrit, double theta, int* ncells,

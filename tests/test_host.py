@@ -253,3 +253,51 @@ def test_m2l_loop_tables_match_straight_line(m, p):
                 t += 1
         assert t == len(w)
         np.testing.assert_allclose(out, ref, rtol=0, atol=1e-12 * np.max(np.abs(ref)))
+
+
+# --- potfile ingest into arrays and CSR (cppe_gpu_potfile_*) -----------------
+@pytest.mark.parametrize("name", ["pna_6w.pot", "pna_6w_isopol.pot", "loprop_solvated_20.pot"])
+def test_potfile_arrays_match_oracle_reader(unpacked, name):
+    from oracle import oracle as O
+    got = cabi.read_potfile(unpacked[name])
+    ref = O.read_potfile(unpacked[name])
+    np.testing.assert_array_equal(got["xyz"], ref.xyz)
+    np.testing.assert_array_equal(got["q"], ref.q)
+    np.testing.assert_array_equal(got["mu"], ref.mu)
+    np.testing.assert_array_equal(got["quad"], ref.quad)
+    np.testing.assert_array_equal(got["alpha6"], ref.alpha6)
+    np.testing.assert_array_equal(got["polarizable"], ref.polarizable)
+    np.testing.assert_array_equal(got["excl_ptr"], ref.excl_ptr)
+    np.testing.assert_array_equal(got["excl_idx"], ref.excl_idx)
+    assert got["elements"] == list(ref.elements)
+
+
+def test_potfile_arrays_million_sites(tmp_path):
+    """A 1,000,002-site water box written as a .pot file (AA, 12 decimals) and
+    read back into arrays and CSR exclusions; the object reader
+    (PotfileReader.read) gives the same sites."""
+    import time
+    import cppe_gb300 as cppe
+    from cppe_gb300 import synthetic
+    b = synthetic.water_box(333334, seed=4)
+    path = str(tmp_path / "w1m.pot")
+    synthetic.write_potfile(b, path)
+    t0 = time.perf_counter()
+    got = cabi.read_potfile(path)
+    t_soa = time.perf_counter() - t0
+    assert got["xyz"].shape == (1000002, 3)
+    np.testing.assert_allclose(got["xyz"], b.xyz, rtol=0, atol=1e-10)
+    np.testing.assert_allclose(got["mu"], b.mu, rtol=0, atol=1e-12)
+    np.testing.assert_allclose(got["quad"], b.quad, rtol=0, atol=1e-12)
+    np.testing.assert_allclose(got["alpha6"], b.alpha6, rtol=0, atol=1e-12)
+    np.testing.assert_array_equal(got["excl_ptr"], b.excl_ptr)
+    np.testing.assert_array_equal(got["excl_idx"], b.excl_idx)
+    t0 = time.perf_counter()
+    pots = cppe.PotfileReader(path).read()
+    t_obj = time.perf_counter() - t0
+    assert len(pots) == b.n
+    for i in (0, 1, 499999, b.n - 1):
+        np.testing.assert_array_equal(pots[i].position, got["xyz"][i])
+        assert sorted(pots[i].exclusions) == sorted(
+            got["excl_idx"][got["excl_ptr"][i]:got["excl_ptr"][i + 1]])
+    print(f"1M-site potfile: arrays + CSR {t_soa:.2f} s, objects {t_obj:.2f} s")
