@@ -96,6 +96,7 @@ def lib():
         l.cppe_gpu_mlp_set_params.argtypes = [ctypes.c_void_p, F]
         l.cppe_gpu_mlp_normalization.argtypes = [ctypes.c_void_p, F, F, F, F]
         l.cppe_gpu_mlp_forward.argtypes = [ctypes.c_void_p, ctypes.c_int, F, F]
+        l.cppe_gpu_mlp_infer.argtypes = [ctypes.c_void_p, ctypes.c_int, F, F]
         l.cppe_gpu_mlp_loss_grad.argtypes = [ctypes.c_void_p, ctypes.c_int, F, F,
                                              ctypes.c_float, D, F]
         l.cppe_gpu_mlp_train.argtypes = [ctypes.c_void_p, ctypes.c_int, F, F, ctypes.c_int,
@@ -170,6 +171,13 @@ class Mlp:
         feats = f32(feats)
         y = np.zeros((feats.shape[0], N_OUT), np.float32)
         check(lib().cppe_gpu_mlp_forward(self.h, feats.shape[0], fp(feats), fp(y)))
+        return y
+
+    def infer(self, feats):
+        """The tensor-core inference kernel (TF32 operands, FP32 accumulation)."""
+        feats = f32(feats)
+        y = np.zeros((feats.shape[0], N_OUT), np.float32)
+        check(lib().cppe_gpu_mlp_infer(self.h, feats.shape[0], fp(feats), fp(y)))
         return y
 
     def loss_grad(self, feats, rows, lam=1.0):

@@ -974,6 +974,24 @@ int cppe_gpu_mlp_forward(cppe_gpu_mlp* h, int rows, const float* feats, float* y
   });
 }
 
+int cppe_gpu_mlp_infer(cppe_gpu_mlp* h, int rows, const float* feats, float* y) {
+  return guard([&]() -> int {
+    need(h && feats && y && rows > 0, "null argument");
+    Mlp& M = h->m;
+    CG_CUDA(cudaSetDevice(M.device));
+    DBuf<float> f, yo;
+    f.upload(feats, (size_t)rows * Mlp::IN, M.stream);
+    yo.alloc((size_t)rows * Mlp::OUT);
+    M.infer(rows, f.p, yo.p, M.stream);
+    int e = 0;
+    CG_CUDA(cudaMemcpyAsync(y, yo.p, (size_t)rows * Mlp::OUT * 4, cudaMemcpyDeviceToHost, M.stream));
+    CG_CUDA(cudaMemcpyAsync(&e, M.tc_err.p, sizeof(int), cudaMemcpyDeviceToHost, M.stream));
+    CG_CUDA(cudaStreamSynchronize(M.stream));
+    if (e) fail(CPPE_GPU_TIMEOUT, "tensor-core MLP inference: a wait on the MMA barrier timed out");
+    return CPPE_GPU_OK;
+  });
+}
+
 int cppe_gpu_mlp_loss_grad(cppe_gpu_mlp* h, int rows, const float* feats, const float* targets,
                            float lam, double* loss, float* grads) {
   return guard([&]() -> int {

@@ -239,6 +239,8 @@ void Mlp::init(int dev, unsigned seed) {
   loss.alloc(1);
   ticket.alloc(1);
   ticket.zero(stream);
+  tc_err.alloc(1);
+  tc_err.zero(stream);
   step = 0;
   CG_CUDA(cudaStreamSynchronize(stream));
 }
@@ -255,93 +257,11 @@ void Mlp::reserve(int rows) {
   loss_part.alloc((rows + 255) / 256 + 1);
 }
 
-// Inference in one pass: a row per thread.  The parameters are staged in
-// shared memory (the first layer transposed, so that both layers read
-// contiguous float4 broadcasts) with the input normalisation;
-// the first hidden layer stays in registers (layer 1 loops over inputs with
-// the 128 outputs unrolled, layer 2 loops over outputs with the 128 inputs
-// unrolled, so that every register index is a compile-time constant and the
-// loop bodies stay small), and each second-layer unit is folded into the
-// output as soon as it is computed.
-constexpr int INFER_BLOCK = 128;
-constexpr int INFER_SMEM  = (Mlp::NPARAM + 3) / 4 * 4 + 2 * Mlp::IN;  // floats
-__global__ void __launch_bounds__(INFER_BLOCK)
-      k_mlp_infer(int rows, const float* __restrict__ raw, const float* __restrict__ params,
-                  const float* __restrict__ mean, const float* __restrict__ inv_std,
-                  float* __restrict__ Y) {
-  extern __shared__ float4 smem4[];
-  float* sm   = reinterpret_cast<float*>(smem4);
-  float* W1T  = sm;                    // [IN][H]
-  float* rest = sm + Mlp::NW1;         // b1, W2, b2, W3, b3 as in params
-  float* nrm  = sm + ((Mlp::NPARAM + 3) / 4 * 4);  // mean, inv_std
-  for (int k = threadIdx.x; k < Mlp::NW1; k += blockDim.x) {
-    const int o = k / Mlp::IN, i = k % Mlp::IN;
-    W1T[i * Mlp::H + o] = params[k];
-  }
-  for (int k = threadIdx.x; k < Mlp::NPARAM - Mlp::NW1; k += blockDim.x)
-    rest[k] = params[Mlp::NW1 + k];
-  for (int k = threadIdx.x; k < Mlp::IN; k += blockDim.x)
-    nrm[k] = mean[k], nrm[Mlp::IN + k] = inv_std[k];
-  __syncthreads();
-  const int row = blockIdx.x * blockDim.x + threadIdx.x;
-  if (row >= rows) return;
-  const float* xr = raw + (size_t)row * Mlp::IN;
-  const float* b1 = rest;
-  const float* W2 = b1 + Mlp::NB1;
-  const float* b2 = W2 + Mlp::NW2;
-  const float* W3 = b2 + Mlp::NB2;
-  const float* b3 = W3 + Mlp::NW3;
-  float h[Mlp::H];
-#pragma unroll
-  for (int o = 0; o < Mlp::H; ++o) h[o] = b1[o];
-#pragma unroll 1
-  for (int i = 0; i < Mlp::IN; ++i) {
-    const float xi  = (xr[i] - nrm[i]) * nrm[Mlp::IN + i];
-    const float4* w = reinterpret_cast<const float4*>(W1T + i * Mlp::H);
-#pragma unroll
-    for (int q = 0; q < Mlp::H / 4; ++q) {
-      const float4 v = w[q];
-      h[4 * q]       = fmaf(v.x, xi, h[4 * q]);
-      h[4 * q + 1]   = fmaf(v.y, xi, h[4 * q + 1]);
-      h[4 * q + 2]   = fmaf(v.z, xi, h[4 * q + 2]);
-      h[4 * q + 3]   = fmaf(v.w, xi, h[4 * q + 3]);
-    }
-  }
-#pragma unroll
-  for (int o = 0; o < Mlp::H; ++o) h[o] = gelu(h[o]);
-  float y[Mlp::OUT];
-#pragma unroll
-  for (int k = 0; k < Mlp::OUT; ++k) y[k] = b3[k];
-#pragma unroll 1
-  for (int o = 0; o < Mlp::H; ++o) {
-    const float4* w = reinterpret_cast<const float4*>(W2 + o * Mlp::H);
-    float a0 = b2[o], a1 = 0.f, a2 = 0.f, a3 = 0.f;
-#pragma unroll
-    for (int q = 0; q < Mlp::H / 4; ++q) {
-      const float4 v = w[q];
-      a0 = fmaf(v.x, h[4 * q], a0), a1 = fmaf(v.y, h[4 * q + 1], a1);
-      a2 = fmaf(v.z, h[4 * q + 2], a2), a3 = fmaf(v.w, h[4 * q + 3], a3);
-    }
-    const float g = gelu((a0 + a1) + (a2 + a3));
-#pragma unroll
-    for (int k = 0; k < Mlp::OUT; ++k) y[k] = fmaf(W3[k * Mlp::H + o], g, y[k]);
-  }
-#pragma unroll
-  for (int k = 0; k < Mlp::OUT; ++k) Y[(size_t)row * Mlp::OUT + k] = y[k];
-}
-
+// Inference on the tensor cores (mlp_tc.cu); tc_err reports a timed-out wait.
 void Mlp::infer(int rows, const float* raw, float* Y_out, cudaStream_t s) {
   if (rows <= 0) return;
-  static int attr_device = -1;
-  if (attr_device != device) {
-    CG_CUDA(cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 INFER_SMEM * (int)sizeof(float)));
-    attr_device = device;
-  }
-  k_mlp_infer<<<(rows + INFER_BLOCK - 1) / INFER_BLOCK, INFER_BLOCK,
-                INFER_SMEM * sizeof(float), s>>>(rows, raw, params.p, feat_mean.p,
-                                                 feat_inv_std.p, Y_out);
-  CG_LAUNCH();
+  tc_err.zero(s);
+  mlp_infer_tc(device, rows, raw, params.p, feat_mean.p, feat_inv_std.p, Y_out, tc_err.p, s);
 }
 
 void Mlp::forward(int rows, const float* raw, float* Y_out, cudaStream_t s) {

@@ -25,6 +25,7 @@ struct Mlp {
   DBuf<float> X, Z1, H1, Z2, H2, Y, dY, dA, dB, part;
   DBuf<double> loss_part, loss;
   DBuf<unsigned> ticket;
+  DBuf<int> tc_err;  // error code of the tensor-core inference (0: none)
 
   ~Mlp();
   void init(int device, unsigned seed);
@@ -43,6 +44,11 @@ struct Mlp {
   double loss_grad(int rows, const float* raw, const float* targets, float lam);
   void adam(float lr, float b1 = 0.9f, float b2 = 0.999f, float eps = 1e-8f);
 };
+
+// Y (rows x 4) = MLP(normalised raw) on the tensor cores (tcgen05, TF32
+// operands, FP32 accumulation); *err receives 1 if a wait timed out.
+void mlp_infer_tc(int device, int rows, const float* raw, const float* params,
+                  const float* mean, const float* inv_std, float* Y, int* err, cudaStream_t s);
 
 // C = op(A) op(B) (+ bias over columns), row-major, FP32; split over K into
 // `splits` partial products added in fixed order.

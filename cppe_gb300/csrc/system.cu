@@ -290,7 +290,7 @@ void System::init(int n_, const double* xyz, const double* alpha6, const int* ex
   ticket.zero(stream);
   flags.alloc(4);
   flags.zero(stream);
-  CG_CUDA(cudaMallocHost(&h_flags, 4 * sizeof(int)));
+  CG_CUDA(cudaMallocHost(&h_flags, 8 * sizeof(int)));  // [4]: the model's error code
   CG_CUDA(cudaMallocHost(&h_scal, S_NSCAL * sizeof(double)));
   CG_CUDA(cudaStreamSynchronize(stream));
   setup_inexact(xyz, sd.data());
@@ -954,6 +954,7 @@ int System::solve_device(const double* d_rhs, const double* d_guess, int make_gu
   permute_in(geo, d_rhs, F.p, 3, stream);
   bool zero = false;
   use_model = make_guess && model != nullptr;
+  const bool ran_model = use_model;
   if (use_model) {
     learned_start();
   } else if (make_guess) {
@@ -977,7 +978,14 @@ int System::solve_device(const double* d_rhs, const double* d_guess, int make_gu
   }
   use_model = false;
   permute_out(geo, x.p, d_mu, 3, stream);
+  if (ran_model)
+    CG_CUDA(cudaMemcpyAsync(h_flags + 4, model->tc_err.p, sizeof(int), cudaMemcpyDeviceToHost,
+                            stream));
   CG_CUDA(cudaStreamSynchronize(stream));
+  if (ran_model && h_flags[4])
+    fail(CPPE_GPU_TIMEOUT,
+         "tensor-core MLP inference: a wait on the MMA barrier timed out (the answer still "
+         "met the FP64 stopping rule)");
   return st;
 }
 

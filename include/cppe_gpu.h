@@ -257,6 +257,10 @@ int cppe_gpu_mlp_normalization(cppe_gpu_mlp* m, const float* mean, const float* 
                                float* mean_out, float* inv_std_out);
 /* y (rows x 4) for raw descriptors (rows x 64), host buffers. */
 int cppe_gpu_mlp_forward(cppe_gpu_mlp* m, int rows, const float* feats, float* y);
+/* The same network on the tensor cores (tcgen05, TF32 operands with FP32
+ * accumulation; the kernel the learned solves use): rows x 4 outputs.
+ * CPPE_GPU_TIMEOUT if a wait on the MMA completion barrier ran out. */
+int cppe_gpu_mlp_infer(cppe_gpu_mlp* m, int rows, const float* feats, float* y);
 /* Loss and gradient (cppe_gpu_mlp_nparams floats) of one batch; targets are
  * rows of 24 floats: v1 v2 v3 mu* a w e (3 each), the two loss weights, pad. */
 int cppe_gpu_mlp_loss_grad(cppe_gpu_mlp* m, int rows, const float* feats,

@@ -106,3 +106,28 @@ def test_shipped_model_on_a_large_system(gpu):
     s.set_model(None)
     s64 = cabi.System(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, summation=cabi.FMM, damp=True)
     assert np.linalg.norm(rhs - s64.apply(mu)) < 1e-8
+
+
+@pytest.mark.parametrize("rows", [1000, 131072 + 77])
+def test_tensor_core_inference_matches_fp32(gpu, rows):
+    """The tcgen05 inference kernel (TF32 operands rounded to nearest, FP32
+    accumulation in tensor memory) against the FP32 GEMM forward pass, with
+    the shipped model, on descriptor-like rows (partial last tile, and many
+    tiles per CTA).  Bound: 1e-2 of the largest output and 1e-3 in norm; TF32
+    keeps 11 significant bits per operand (2^-12 relative rounding)."""
+    import os
+    from cppe_gb300 import learned
+    m = learned.load(learned.DEFAULT_MODEL)
+    mean, inv = m.normalization()
+    rng = np.random.default_rng(rows)
+    std = np.where(inv > 0, 1.0 / np.maximum(inv, 1e-30), 0.0)
+    feats = (mean + std * rng.normal(size=(rows, 64))).astype(np.float32)
+    y32 = m.forward(feats)
+    ytc = m.infer(feats)
+    assert np.all(np.isfinite(ytc))
+    scale = np.abs(y32).max()
+    assert np.abs(ytc - y32).max() < 1e-2 * scale
+    assert np.linalg.norm(ytc - y32) < 1e-3 * np.linalg.norm(y32)
+    ytc2 = m.infer(feats)
+    np.testing.assert_array_equal(ytc, ytc2)  # deterministic
+    m.close()
