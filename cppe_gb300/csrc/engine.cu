@@ -424,6 +424,12 @@ void Geometry::make_schedules() {
     h_item_split[k] = std::max(v.y, std::min(v.z, h_leaf_split[v.x]));
     nslot           = std::max(nslot, v.w + 1);
   }
+  // the symmetric schedule of single systems (a batch keeps per-leaf items:
+  // its passes skip finished segments and serve several right-hand sides)
+  if (sym_enabled && h_leaf_seg.empty() && ncopies == 1)
+    make_sym_schedule(W);
+  else
+    h_usrc.clear(), h_sym_items.clear();
   // a batch's copy-0 items, for the near-field pass over all its copies
   h_mitems.clear(), h_mitem_split.clear(), h_mitem_stride.clear();
   if (ncopies > 1 && (int)h_leaf_copy.size() == L.nleaves)
@@ -435,7 +441,96 @@ void Geometry::make_schedules() {
       }
 }
 
+// Upper lists (partners B >= A of each leaf A, in the order of A's P2P list:
+// damping class first), items over them of about W target-source pairs
+// (each cross pair counts twice: both directions are evaluated), and the
+// output rows: per item one row of its target leaf, and per (item, partner
+// B != A) one row of B, numbered leaf by leaf in item order.
+void Geometry::make_sym_schedule(long W) {
+  const TreeLayout& L = layout;
+  const int nl        = L.nleaves;
+  h_usrc.clear(), h_usrc_off.clear(), h_sym_split.clear(), h_sym_aoff.clear();
+  h_sym_items.clear();
+  h_sym_leaf_rows.assign(nl, 0);
+  h_sym_leaf_off.assign(nl + 1, 0);
+  if (nl == 0) return;
+  auto nsite = [&](int a) { return (long)(L.leaf_start[a + 1] - L.leaf_start[a]); };
+  std::vector<int> uptr(nl + 1, 0), usplit(nl, 0);
+  for (int a = 0; a < nl; ++a) {
+    for (int q = L.p2p_ptr[a]; q < L.p2p_ptr[a + 1]; ++q) {
+      if (q == h_leaf_split[a]) usplit[a] = (int)h_usrc.size();
+      if (L.p2p_src[q] >= a) h_usrc.push_back(L.p2p_src[q]);
+    }
+    if (h_leaf_split[a] >= L.p2p_ptr[a + 1]) usplit[a] = (int)h_usrc.size();
+    uptr[a + 1] = (int)h_usrc.size();
+  }
+  // items: pieces of the upper lists, and their row owners
+  struct Item {
+    long w;
+    int4 v;
+    int split;
+  };
+  std::vector<Item> its;
+  std::vector<int> item_of_entry(h_usrc.size(), -1);
+  for (int a = 0; a < nl; ++a) {
+    const long na = nsite(a);
+    int q0        = uptr[a];
+    long acc      = 0;
+    for (int q = uptr[a]; q < uptr[a + 1]; ++q) {
+      const int b = h_usrc[q];
+      acc += (b == a ? 1 : 2) * na * nsite(b);
+      if (acc >= W || q + 1 == uptr[a + 1]) {
+        its.push_back({acc, make_int4(a, q0, q + 1, 0), std::max(q0, std::min(q + 1, usplit[a]))});
+        q0 = q + 1, acc = 0;
+      }
+    }
+    if (uptr[a] == uptr[a + 1])  // no partner at all (not even itself): zeros
+      its.push_back({0, make_int4(a, uptr[a], uptr[a], 0), uptr[a]});
+  }
+  // rows, leaf by leaf: first each leaf's own items, then its rows as a partner
+  std::vector<std::vector<std::pair<int, int>>> partner_rows(nl);  // (item, entry)
+  for (size_t k = 0; k < its.size(); ++k)
+    for (int q = its[k].v.y; q < its[k].v.z; ++q)
+      if (h_usrc[q] != its[k].v.x) partner_rows[h_usrc[q]].push_back({(int)k, q});
+  std::vector<std::vector<int>> own(nl);
+  for (size_t k = 0; k < its.size(); ++k) own[its[k].v.x].push_back((int)k);
+  h_sym_aoff.assign(its.size(), 0);
+  h_usrc_off.assign(h_usrc.size(), -1);
+  long long off = 0;
+  for (int a = 0; a < nl; ++a) {
+    h_sym_leaf_off[a] = off;
+    const long row    = 3 * nsite(a);
+    for (int k : own[a]) h_sym_aoff[k] = off, off += row;
+    for (const auto& pr : partner_rows[a]) h_usrc_off[pr.second] = off, off += row;
+    h_sym_leaf_rows[a] = (int)(own[a].size() + partner_rows[a].size());
+  }
+  h_sym_leaf_off[nl] = off;
+  sym_floats         = off;
+  // largest first; the row offsets travel with the items
+  std::vector<int> order(its.size());
+  for (size_t k = 0; k < its.size(); ++k) order[k] = (int)k;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return its[x].w > its[y].w; });
+  h_sym_items.resize(its.size());
+  h_sym_split.resize(its.size());
+  std::vector<long long> aoff(its.size());
+  for (size_t k = 0; k < its.size(); ++k) {
+    h_sym_items[k] = its[order[k]].v;
+    h_sym_split[k] = its[order[k]].split;
+    aoff[k]        = h_sym_aoff[order[k]];
+  }
+  h_sym_aoff.swap(aoff);
+}
+
 void Geometry::upload_schedules(cudaStream_t s) {
+  if (has_sym()) {
+    usrc.upload(h_usrc, s);
+    usrc_off.upload(h_usrc_off, s);
+    sym_split.upload(h_sym_split, s);
+    sym_aoff.upload(h_sym_aoff, s);
+    sym_items.upload(h_sym_items, s);
+    sym_leaf_rows.upload(h_sym_leaf_rows, s);
+    sym_leaf_off.upload(h_sym_leaf_off, s);
+  }
   if (!h_mitems.empty()) {
     mitems.upload(h_mitems, s);
     mitem_split.upload(h_mitem_split, s);
@@ -460,6 +555,15 @@ void Geometry::upload(cudaStream_t s) {
   items.upload(h_items, s);
   item_split.upload(h_item_split, s);
   leaf_nslot.upload(h_leaf_nslot, s);
+  if (has_sym()) {
+    usrc.upload(h_usrc, s);
+    usrc_off.upload(h_usrc_off, s);
+    sym_split.upload(h_sym_split, s);
+    sym_aoff.upload(h_sym_aoff, s);
+    sym_items.upload(h_sym_items, s);
+    sym_leaf_rows.upload(h_sym_leaf_rows, s);
+    sym_leaf_off.upload(h_sym_leaf_off, s);
+  }
   if (!h_vec.empty()) {
     m2l_vid.upload(h_m2l_vid, s);
     vec.upload(h_vec, s);
@@ -601,6 +705,7 @@ struct TilePlan {
   int pstart[33];  // first site of each piece
   int poff[34];    // tile offset of each piece (poff[np] = tile size)
   int np, cur, coff;
+  int cur0;        // list position of the tile's first piece
 };
 
 template <int TILE = P2P_TILE>
@@ -633,6 +738,7 @@ __device__ __forceinline__ void plan_tile(TilePlan& tp, int b1, const int* __res
   const int lasttake = __shfl_sync(0xffffffffu, takecnt, last);
   if (take) tp.pstart[lane] = start, tp.poff[lane] = excl;
   if (lane == 0) {
+    tp.cur0     = cur;
     tp.np       = np;
     tp.poff[np] = np ? tot : 0;
     if (np > 0) {
@@ -788,14 +894,19 @@ struct Src2 {
   float2 mz;   // mz_j, mz_j+1
 };
 
+// The pair tensor of a target against two sources (one per half): the
+// separation (source - target), A = R^-3 f_E and Bn = -3 R^-5 f_T, so that
+// the field of a dipole mu is mu A + r (mu.r) Bn (even in r: the same tensor
+// serves both directions).
 template <bool DAMP>
-__device__ __forceinline__ void f32x2_pair_m1(const float2& nX, const float2& nY,
-                                              const float2& nZ, const float2& AI,
-                                              const Src2& q, float2& FX, float2& FY,
-                                              float2& FZ) {
-  const float2 x  = __fadd2_rn(make_float2(q.xy.x, q.xy.y), nX);
-  const float2 y  = __fadd2_rn(make_float2(q.xy.z, q.xy.w), nY);
-  const float2 z  = __fadd2_rn(make_float2(q.zs.x, q.zs.y), nZ);
+__device__ __forceinline__ void f32x2_tensor_m1(const float2& nX, const float2& nY,
+                                                const float2& nZ, const float2& AI,
+                                                const float2& sx, const float2& sy,
+                                                const float2& sz, const float2& ss, float2& x,
+                                                float2& y, float2& z, float2& A, float2& Bn) {
+  x               = __fadd2_rn(sx, nX);
+  y               = __fadd2_rn(sy, nY);
+  z               = __fadd2_rn(sz, nZ);
   const float2 r2 = __ffma2_rn(x, x, __ffma2_rn(y, y, __fmul2_rn(z, z)));
   float2 ir;
   if (DAMP) {
@@ -808,14 +919,13 @@ __device__ __forceinline__ void f32x2_pair_m1(const float2& nX, const float2& nY
   const float2 ir2 = __fmul2_rn(ir, ir);
   const float2 ir3 = __fmul2_rn(ir2, ir);
   const float2 ir5 = __fmul2_rn(ir3, ir2);
-  float2 A, Bn;  // field = mu A - r (mu.r) B, Bn = -B
   if (DAMP) {
     // t = -v log2(e) with v = damping s_i s_j R (AI = -log2(e) damping s_i);
     // with v = -t ln 2 the damping functions are
     //   f_E = 1 - e^-v (1 + v + v^2/2)          = 1 + e np,
     //   f_T = 1 - e^-v (1 + v + v^2/2 + v^3/6)  = 1 - e q3 / 3,
     // np = -1 + t ln2 - t^2 ln2^2/2, q3 = 3 - 3 t ln2 + 3 t^2 ln2^2/2 - t^3 ln2^3/2
-    float2 t = __fmul2_rn(__fmul2_rn(AI, make_float2(q.zs.z, q.zs.w)), __fmul2_rn(r2, ir));
+    float2 t = __fmul2_rn(__fmul2_rn(AI, ss), __fmul2_rn(r2, ir));
     t.x = fmaxf(t.x, -126.f);
     t.y = fmaxf(t.y, -126.f);
     const float2 e  = make_float2(ex2_approx(t.x), ex2_approx(t.y));
@@ -828,13 +938,31 @@ __device__ __forceinline__ void f32x2_pair_m1(const float2& nX, const float2& nY
     A  = ir3;
     Bn = __fmul2_rn(ir5, f2(-3.f));
   }
-  const float2 mx = make_float2(q.mxy.x, q.mxy.y), my = make_float2(q.mxy.z, q.mxy.w);
-  const float2 mz = q.mz;
+}
+
+// F += mu A + r (mu.r) Bn for packed moments (mx, my, mz)
+__device__ __forceinline__ void f32x2_apply_m1(const float2& x, const float2& y, const float2& z,
+                                               const float2& A, const float2& Bn,
+                                               const float2& mx, const float2& my,
+                                               const float2& mz, float2& FX, float2& FY,
+                                               float2& FZ) {
   const float2 md = __ffma2_rn(mx, x, __ffma2_rn(my, y, __fmul2_rn(mz, z)));
   const float2 nC = __fmul2_rn(md, Bn);
   FX = __ffma2_rn(x, nC, __ffma2_rn(mx, A, FX));
   FY = __ffma2_rn(y, nC, __ffma2_rn(my, A, FY));
   FZ = __ffma2_rn(z, nC, __ffma2_rn(mz, A, FZ));
+}
+
+template <bool DAMP>
+__device__ __forceinline__ void f32x2_pair_m1(const float2& nX, const float2& nY,
+                                              const float2& nZ, const float2& AI,
+                                              const Src2& q, float2& FX, float2& FY,
+                                              float2& FZ) {
+  float2 x, y, z, A, Bn;
+  f32x2_tensor_m1<DAMP>(nX, nY, nZ, AI, make_float2(q.xy.x, q.xy.y), make_float2(q.xy.z, q.xy.w),
+                        make_float2(q.zs.x, q.zs.y), make_float2(q.zs.z, q.zs.w), x, y, z, A, Bn);
+  f32x2_apply_m1(x, y, z, A, Bn, make_float2(q.mxy.x, q.mxy.y), make_float2(q.mxy.z, q.mxy.w),
+                 q.mz, FX, FY, FZ);
 }
 
 constexpr int P2P32_PAIRS = 512;  // staged source pairs per tile (1,024 sources)
@@ -959,6 +1087,223 @@ __global__ void __launch_bounds__(P2P_BLOCK)
     }
     __syncthreads();
   }
+}
+
+// ---------------------------------------------------------------------------
+// Near field, FP32, dipole sources, every unordered leaf pair once.
+// The P2P lists are symmetric (B is in A's list exactly when A is in B's), so
+// an item of leaf A takes its upper list (partners B >= A, damping class
+// first; see Geometry::make_sym_schedule) and evaluates each pair tensor once
+// for both directions (T(r) = T(-r)): 21 of a damped pair's 31 operations are
+// the tensor, so a cross pair costs 41 operations instead of 62.
+//  - Lanes own sources: each of the 4 warps takes 64 consecutive sources of
+//    a 256-source tile (two per lane, packed FP32x2), with positions relative
+//    to the first site of A (hi/lo differences) in registers.
+//  - The targets of A (64 per pass) are staged in shared memory and broadcast
+//    one at a time.  Per target the lane's two pair tensors give the sources'
+//    fields (F_j += T mu_i, accumulated in registers over all targets) and
+//    the target's field (T mu_j), which a butterfly adds over the warp and
+//    lane (i mod 32) keeps (compensated).
+//  - A source's field goes to its leaf's output row for this item; the self
+//    leaf (B = A) is evaluated one way only.  The four warps' target fields
+//    are added in warp order into the item's row of A.  Rows are fixed at
+//    set-up and added by k_sym_gather in a fixed order (no atomics).
+//  - Damping as in k_p2p32_m1: the damping class first with the Thole
+//    factors, then the partners with v >= 27 for every pair without them;
+//    1/R capped at 1e4 (self pairs give an exact zero); lanes without a
+//    source hold a zero moment 1e4 bohr away.
+// ---------------------------------------------------------------------------
+constexpr int SYM_TILE = 256;  // sources per tile: 4 warps x 32 lanes x 2
+constexpr int SYM_TGT  = 64;   // targets per pass over the sources
+
+template <bool DAMP>
+__global__ void __launch_bounds__(P2P_BLOCK)
+      k_p2p32_m1_sym(const int* __restrict__ leaf_start, const int4* __restrict__ items,
+                     const int* __restrict__ item_split, const long long* __restrict__ item_aoff,
+                     const int* __restrict__ usrc, const long long* __restrict__ usrc_off,
+                     const float4* __restrict__ hi, const float4* __restrict__ lo,
+                     const float* __restrict__ src, float damping, float* __restrict__ rows) {
+  __shared__ float4 s_t[SYM_TGT];   // target x, y, z, AI (padded to a multiple of 8)
+  __shared__ float4 s_tm[SYM_TGT];  // target mx, my, mz
+  __shared__ float s_acc[4][SYM_TGT][6];  // per warp: target field sums and their errors
+  __shared__ TilePlan s_plan;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int4 it = items[blockIdx.x];
+  const int A = it.x, b0 = it.y, b1 = it.z;
+  const int sp = item_split[blockIdx.x];
+  const long long aoff = item_aoff[blockIdx.x];
+  const int a0 = leaf_start[A], nA = leaf_start[A + 1] - a0;
+  const float4 oh = hi[a0], ol = lo[a0];
+  auto rel = [&](int k) {
+    const float4 h = hi[k], l = lo[k];
+    return make_float4((h.x - oh.x) + (l.x - ol.x), (h.y - oh.y) + (l.y - ol.y),
+                       (h.z - oh.z) + (l.z - ol.z), h.w > 0.f ? h.w : 1e15f);
+  };
+  for (int tb = 0; tb < nA; tb += SYM_TGT) {
+    const int nT = min(SYM_TGT, nA - tb);
+    __syncthreads();
+    for (int k = threadIdx.x; k < SYM_TGT; k += blockDim.x) {
+      if (k < nT) {
+        const float4 m = rel(a0 + tb + k);
+        s_t[k]  = make_float4(-m.x, -m.y, -m.z, -1.4426950408889634f * damping * m.w);
+        const size_t j = a0 + tb + k;
+        s_tm[k] = make_float4(src[3 * j], src[3 * j + 1], src[3 * j + 2], 0.f);
+      } else {  // padding: a zero moment far away (its fields are dropped)
+        s_t[k]  = make_float4(-1e4f, 0.f, 0.f, -1.4426950408889634f * damping);
+        s_tm[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+#pragma unroll
+      for (int w = 0; w < 4; ++w)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) s_acc[w][k][c] = 0.f;
+    }
+    for (int ph = 0; ph < 2; ++ph) {
+      const int pend = ph == 0 ? sp : b1;
+      if (threadIdx.x == 0) s_plan.cur = ph == 0 ? b0 : sp, s_plan.coff = 0;
+      __syncthreads();
+      while (true) {
+        if (threadIdx.x < 32) plan_tile<SYM_TILE>(s_plan, pend, usrc, leaf_start);
+        __syncthreads();
+        const int np = s_plan.np;
+        if (np == 0) break;
+        const int total = s_plan.poff[np];
+        // this lane's two sources
+        float2 sx, sy, sz, ss, mx, my, mz;
+        long long o0 = -1, o1 = -1;  // output positions (-1: none)
+        {
+          float4 r[2];
+          float m[2][3];
+          long long o[2];
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int q = 64 * warp + 2 * lane + h;
+            o[h] = -1;
+            if (q < total) {
+              // piece of tile slot q (as tile_site) and its list entry
+              int lo_ = 0, hi_ = np - 1;
+              while (lo_ < hi_) {
+                const int mid = (lo_ + hi_ + 1) >> 1;
+                if (s_plan.poff[mid] <= q) lo_ = mid; else hi_ = mid - 1;
+              }
+              const int j = s_plan.pstart[lo_] + (q - s_plan.poff[lo_]);
+              const int e = s_plan.cur0 + lo_;
+              const int B = usrc[e];
+              r[h] = rel(j);
+              m[h][0] = src[3 * (size_t)j], m[h][1] = src[3 * (size_t)j + 1],
+              m[h][2] = src[3 * (size_t)j + 2];
+              if (B != A) o[h] = usrc_off[e] + 3 * (long long)(j - leaf_start[B]);
+            } else {
+              r[h] = make_float4(1e4f, 0.f, 0.f, 1.f);
+              m[h][0] = m[h][1] = m[h][2] = 0.f;
+            }
+          }
+          sx = make_float2(r[0].x, r[1].x), sy = make_float2(r[0].y, r[1].y);
+          sz = make_float2(r[0].z, r[1].z), ss = make_float2(r[0].w, r[1].w);
+          mx = make_float2(m[0][0], m[1][0]), my = make_float2(m[0][1], m[1][1]);
+          mz = make_float2(m[0][2], m[1][2]);
+          o0 = o[0], o1 = o[1];
+        }
+        float2 FX = f2(0.f), FY = f2(0.f), FZ = f2(0.f);
+        auto sweep = [&](auto damped) {
+          constexpr bool D = decltype(damped)::value;
+#pragma unroll 1
+          for (int g = 0; g < nT; g += 8) {
+            // eight targets (padded with zero moments); their fields from the
+            // lane's two sources stay per lane until the reduce-scatter below
+            float p[8][3];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+              const float4 t = s_t[g + u], tm = s_tm[g + u];
+              float2 x, y, z, Av, Bn;
+              f32x2_tensor_m1<D>(f2(t.x), f2(t.y), f2(t.z), f2(t.w), sx, sy, sz, ss, x, y, z,
+                                 Av, Bn);
+              f32x2_apply_m1(x, y, z, Av, Bn, f2(tm.x), f2(tm.y), f2(tm.z), FX, FY, FZ);
+              float2 cx = f2(0.f), cy = f2(0.f), cz = f2(0.f);
+              f32x2_apply_m1(x, y, z, Av, Bn, mx, my, mz, cx, cy, cz);
+              p[u][0] = cx.x + cx.y, p[u][1] = cy.x + cy.y, p[u][2] = cz.x + cz.y;
+            }
+            // reduce-scatter over the warp: after the xor-16, -8 and -4 steps
+            // lane l holds target (l >> 2) & 7 for its quarter of lanes, the
+            // xor-2 and -1 steps add the four quarters
+            const bool h16 = lane & 16, h8 = lane & 8, h4 = lane & 4;
+            float q4[4][3], q2[2][3], q1[3];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+              for (int c = 0; c < 3; ++c) {
+                const float keep = h16 ? p[u + 4][c] : p[u][c];
+                const float send = h16 ? p[u][c] : p[u + 4][c];
+                q4[u][c]         = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+              }
+#pragma unroll
+            for (int u = 0; u < 2; ++u)
+#pragma unroll
+              for (int c = 0; c < 3; ++c) {
+                const float keep = h8 ? q4[u + 2][c] : q4[u][c];
+                const float send = h8 ? q4[u][c] : q4[u + 2][c];
+                q2[u][c]         = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+              }
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              const float keep = h4 ? q2[1][c] : q2[0][c];
+              const float send = h4 ? q2[0][c] : q2[1][c];
+              float v          = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+              v += __shfl_xor_sync(0xffffffffu, v, 2);
+              v += __shfl_xor_sync(0xffffffffu, v, 1);
+              q1[c] = v;
+            }
+            const int u = (lane >> 2) & 7;
+            if ((lane & 3) == 0 && g + u < nT) {
+              // compensated accumulation of this warp's share of target g + u
+              float* acc = s_acc[warp][g + u];
+#pragma unroll
+              for (int c = 0; c < 3; ++c) {
+                float sum, err;
+                two_sum(acc[c], q1[c], sum, err);
+                acc[c] = sum, acc[3 + c] += err;
+              }
+            }
+          }
+        };
+        if (DAMP && ph == 0)
+          sweep(std::true_type{});
+        else
+          sweep(std::false_type{});
+        if (o0 >= 0) rows[o0] = FX.x, rows[o0 + 1] = FY.x, rows[o0 + 2] = FZ.x;
+        if (o1 >= 0) rows[o1] = FX.y, rows[o1 + 1] = FY.y, rows[o1 + 2] = FZ.y;
+        __syncthreads();
+      }
+    }
+    // the targets' fields: the warps' sums in warp order
+    __syncthreads();
+    for (int k = threadIdx.x; k < nT; k += blockDim.x) {
+      float* o = rows + aoff + 3 * (long long)(tb + k);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        float v = 0.f;
+#pragma unroll
+        for (int w = 0; w < 4; ++w) v += s_acc[w][k][c] + s_acc[w][k][3 + c];
+        o[c] = v;
+      }
+    }
+  }
+}
+
+// Near-field totals of the symmetric pass: each site adds its leaf's rows in
+// row order into slot 0 of the near-field buffer.
+__global__ void k_sym_gather(int n, const int* __restrict__ site_leaf,
+                             const int* __restrict__ leaf_start, const int* __restrict__ leaf_rows,
+                             const long long* __restrict__ leaf_off, const float* __restrict__ rows,
+                             float* __restrict__ Fnear) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int L = site_leaf[i];
+  const int p = i - leaf_start[L];
+  const long long stride = 3 * (long long)(leaf_start[L + 1] - leaf_start[L]);
+  const float* r = rows + leaf_off[L] + 3 * (long long)p;
+  float fx = 0.f, fy = 0.f, fz = 0.f;
+  for (int k = 0; k < leaf_rows[L]; ++k, r += stride) fx += r[0], fy += r[1], fz += r[2];
+  Fnear[3 * (size_t)i] = fx, Fnear[3 * (size_t)i + 1] = fy, Fnear[3 * (size_t)i + 2] = fz;
 }
 
 // ---------------------------------------------------------------------------
@@ -1962,7 +2307,7 @@ __global__ void __launch_bounds__(FINISH_BLOCK) k_finish(int n, const int* __res
   T dv[1]     = {T(0)};  // (FP32 products for the FP32 apply: see block_sum)
   if (i < n) {
     T f[3] = {0, 0, 0};
-    const int nsl = leaf_nslot[tv.site_leaf[i]];
+    const int nsl = leaf_nslot ? leaf_nslot[tv.site_leaf[i]] : 1;
     for (int s = 0; s < nsl; ++s) {
       const T* q = Fnear + (size_t)s * 3 * n + 3 * (size_t)i;
       f[0] += q[0], f[1] += q[1], f[2] += q[2];
@@ -2306,6 +2651,29 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
       done = true;
     }
   }
+  const int* finish_nslot = g.leaf_nslot.p;
+  if constexpr (std::is_same<T, float>::value) {
+    if (!done && m == 1 && g.has_sym() && !seg_done) {
+      // every unordered pair once (k_p2p32_m1_sym), then each site's rows
+      w.Fsym.alloc((size_t)g.sym_floats);
+      const int ni = (int)g.h_sym_items.size();
+      if (damp)
+        k_p2p32_m1_sym<true><<<ni, P2P_BLOCK, 0, s>>>(
+              g.leaf_start.p, g.sym_items.p, g.sym_split.p, g.sym_aoff.p, g.usrc.p,
+              g.usrc_off.p, g.hi32.p, g.lo32.p, src, dampT, w.Fsym.p);
+      else
+        k_p2p32_m1_sym<false><<<ni, P2P_BLOCK, 0, s>>>(
+              g.leaf_start.p, g.sym_items.p, g.sym_split.p, g.sym_aoff.p, g.usrc.p,
+              g.usrc_off.p, g.hi32.p, g.lo32.p, src, dampT, w.Fsym.p);
+      CG_LAUNCH();
+      k_sym_gather<<<(n + 255) / 256, 256, 0, s>>>(n, g.site_leaf.p, g.leaf_start.p,
+                                                   g.sym_leaf_rows.p, g.sym_leaf_off.p, w.Fsym.p,
+                                                   w.Fnear.p);
+      CG_LAUNCH();
+      finish_nslot = nullptr;  // one slot per site
+      done         = true;
+    }
+  }
   if (!done && m == 0) launch_p2p<T, 0>(g, damp, fast, src, dampT, w.Fnear.p, s, seg_done);
   if (!done && m == 1) launch_p2p<T, 1>(g, damp, fast, src, dampT, w.Fnear.p, s, seg_done);
   if (!done && m == 2) launch_p2p<T, 2>(g, damp, fast, src, dampT, w.Fnear.p, s, seg_done);
@@ -2318,7 +2686,7 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
   if (dot) rs = *dot;
   const T* Lp = g.fmm ? w.Lleaf.p : nullptr;
 #define CG_FINISH(TT, MM, MODE, PP)                                                           \
-  k_finish<TT, MM, MODE, PP><<<nb, FB, 0, s>>>(n, g.leaf_nslot.p, w.Fnear.p, g.fmm ? 1 : 0, tv, ov, Lp, \
+  k_finish<TT, MM, MODE, PP><<<nb, FB, 0, s>>>(n, finish_nslot, w.Fnear.p, g.fmm ? 1 : 0, tv, ov, Lp, \
                                            pos_args<TT>(g), cell_pos<TT>(g), src, damp ? 1 : 0, \
                                            dampT, g.corr_ptr.p, g.corr_idx.p, ainv6, out,    \
                                            out64, sign, rs)

@@ -109,6 +109,26 @@ struct Geometry {
   std::vector<int> h_leaf_nslot, h_leaf_split, h_item_split;
   DBuf<int4> items;
   DBuf<int> leaf_nslot, item_split;
+  // Symmetric near field (single systems, FP32 dipole sources): P2P lists
+  // are symmetric, so every unordered leaf pair is evaluated once, by an item
+  // of the lower-numbered leaf A over its "upper" list (partners B >= A,
+  // damping class first; B = A is the self leaf, evaluated one way).  An item
+  // writes its targets' fields to its row of A and each partner's fields to
+  // that partner's row for this item; leaf L owns sym_leaf_rows[L] rows of
+  // 3 n_L floats from float offset sym_leaf_off[L], and a gather pass adds
+  // them in row order (fixed at set-up: deterministic, no atomics).
+  std::vector<int> h_usrc, h_sym_split;
+  std::vector<long long> h_usrc_off, h_sym_aoff, h_sym_leaf_off;
+  std::vector<int4> h_sym_items;  // {A, first, last, 0} in the upper list
+  std::vector<int> h_sym_leaf_rows;
+  long long sym_floats = 0;       // size of the row buffer
+  DBuf<int> usrc, sym_split, sym_leaf_rows;
+  DBuf<long long> usrc_off, sym_aoff, sym_leaf_off;
+  DBuf<int4> sym_items;
+  bool sym_enabled = true;  // the schedule autotuner may switch it off
+  bool has_sym() const { return !h_sym_items.empty(); }
+  void make_sym_schedule(long W);
+
   // Distinct M2L translation vectors.  Cell centres lie on the tree's grid,
   // so the centre differences of the M2L list entries take few distinct
   // values (about 5,000 for 300,000 sites against 14.7 M entries): m2l_vid
@@ -203,6 +223,7 @@ struct Geometry {
 template <typename T>
 struct FieldWork {
   DBuf<T> M, L, Fnear, Mpart, Lleaf, Lpart;
+  DBuf<T> Fsym;  // rows of the symmetric near field (Geometry::sym_*)
   DBuf<float2> dd_src;  // double-float copy of the sources (double-float pass)
   DBuf<float2> Mdd;     // double-float copy of the multipoles (double-float M2L)
   // derivative tensors of the geometry's M2L vectors, in T and in

@@ -429,17 +429,23 @@ double autotune_schedule(Geometry& geo, SideStream& side, cudaStream_t stream, i
   double best = 1e300;
   long best_w = w0;
   int best_c  = 64;
-  for (long w : ws)
-    for (int ci = 0; ci < nch; ++ci) {
-      geo.item_pairs = w;
-      geo.m2l_chunk  = chs[ci];
-      geo.make_schedules();
-      geo.upload_schedules(stream);
-      const double ms = time_applies();
-      if (ms < best) best = ms, best_w = w, best_c = chs[ci];
-    }
-  geo.item_pairs = best_w;
-  geo.m2l_chunk  = best_c;
+  bool best_s = geo.sym_enabled;
+  // symmetric near field (single systems) or per-target items
+  const int nsym = (geo.h_leaf_seg.empty() && geo.ncopies == 1) ? 2 : 1;
+  for (int si = 0; si < nsym; ++si)
+    for (long w : ws)
+      for (int ci = 0; ci < nch; ++ci) {
+        geo.sym_enabled = nsym == 2 ? si == 0 : geo.sym_enabled;
+        geo.item_pairs  = w;
+        geo.m2l_chunk   = chs[ci];
+        geo.make_schedules();
+        geo.upload_schedules(stream);
+        const double ms = time_applies();
+        if (ms < best) best = ms, best_w = w, best_c = chs[ci], best_s = geo.sym_enabled;
+      }
+  geo.sym_enabled = best_s;
+  geo.item_pairs  = best_w;
+  geo.m2l_chunk   = best_c;
   geo.make_schedules();
   geo.upload_schedules(stream);
   // priority of the far-field stream under the chosen schedule
@@ -463,6 +469,13 @@ double System::autotune(int reps) {
   CG_CUDA(cudaMemsetAsync(p32.p, 0, sizeof(float) * 3 * (size_t)n, stream));
   const double best =
         autotune_schedule(geo, side, stream, reps, [&] { apply32(p32.p, Ap32.p, false); });
+  // the inexact operators' lists share the leaves: the same near-field form
+  for (int k = 0; k < n_inexact; ++k)
+    if (geo_x[k].sym_enabled != geo.sym_enabled) {
+      geo_x[k].sym_enabled = geo.sym_enabled;
+      geo_x[k].make_schedules();
+      geo_x[k].upload_schedules(stream);
+    }
   // captured inner loops hold the old schedule's buffers: rebuild on next use
   for (auto& row : inner_exec)
     for (auto& e : row)
