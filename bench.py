@@ -558,8 +558,9 @@ def profiled_traffic(md_name):
     return tot if found == 2 else None
 
 
-PROFILE_OF = {"30k-fmm5": "k_p2p32_m1_30k_sites.md", "300k-fmm6": "k_p2p32_m1_300k_sites.md",
-              "1m-fmm6": "k_p2p32_m1_1m_sites.md"}
+# committed ncu summaries of the FP32 near field, by workload and form
+PROFILE_OF = {("30k-fmm5", False): "k_p2p32_m1_30k_sites.md",
+              ("1m-fmm6", True): "k_p2p32_m1_sym_1m_sites.md"}
 
 
 def run_ours(args):
@@ -682,6 +683,10 @@ def run_ours(args):
     tim32, alg_pairs, m2l_pairs = smx.kernel_timings(capi.MIXED, reps=5)
     timdd, _, _ = smx.kernel_timings(DD_RESIDUAL, reps=3)
     tim64, _, _ = s64.kernel_timings(capi.FP64, reps=2)
+    sched = smx.schedule()
+    near_kernel = "k_p2p32_m1_sym<true> (FP32 dipole near field, each leaf pair once)" \
+        if sched["symmetric_near"] else "k_p2p32_m1<true> (FP32 dipole near field)"
+    prof = PROFILE_OF.get((args.config, sched["symmetric_near"]))
     fp32_peak = capi.fma_peak_tflops(False, dev)
     fp64_peak = capi.fma_peak_tflops(True, dev)
     achieved = alg_pairs * FLOP_PER_PAIR / (tim32["near"] * 1e-3) / 1e12
@@ -757,12 +762,16 @@ def run_ours(args):
         "vs_oracle": vs_oracle,
         "sections": sections or None,
         "batched": batched,
-        "roofline": {"bound": "fp32", "kernel": "k_p2p32_m1<true> (FP32 dipole near field)",
+        "roofline": {"bound": "fp32", "kernel": near_kernel,
                      "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak,
-                     "traffic": profiled_traffic(PROFILE_OF.get(args.config, "")),
-                     "traffic_note": "DRAM bytes per launch from the committed ncu capture "
-                                     f"profiles/{PROFILE_OF.get(args.config)}",
+                     "traffic": profiled_traffic(prof) if prof else None,
+                     "traffic_note": ("DRAM bytes per launch from the committed ncu capture "
+                                      f"profiles/{prof}" +
+                                      ("; mostly the output rows the gather pass adds"
+                                       if sched["symmetric_near"] else "")) if prof else
+                                     "no committed capture of this form and workload",
+                     "schedule": sched,
                      "peak_kind": "measured FFMA probe (cppe_gpu_fma_peak), no FP32 CUDA-core "
                                   "figure in MEASURED_PEAKS.json",
                      "algorithmic": f"{alg_pairs} pairs x {FLOP_PER_PAIR} FLOP per launch"},

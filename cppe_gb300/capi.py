@@ -424,6 +424,14 @@ class System:
         check(lib().cppe_gpu_autotune(self.h, reps, ctypes.byref(ms)))
         return ms.value
 
+    def schedule(self):
+        """The schedule in use: symmetric near field, near-field items, M2L chunk."""
+        sym, items, ch = ctypes.c_int(0), ctypes.c_long(0), ctypes.c_int(0)
+        lib().cppe_gpu_schedule_info.argtypes = [ctypes.c_void_p, I, L, I]
+        check(lib().cppe_gpu_schedule_info(self.h, ctypes.byref(sym), ctypes.byref(items),
+                                           ctypes.byref(ch)))
+        return dict(symmetric_near=bool(sym.value), near_items=items.value, m2l_chunk=ch.value)
+
     def kernel_timings(self, precision=FP64, reps=5):
         ms = np.zeros(6)
         npair, nm2l = ctypes.c_longlong(0), ctypes.c_longlong(0)

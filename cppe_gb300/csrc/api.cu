@@ -737,6 +737,19 @@ int cppe_gpu_autotune(cppe_gpu_system* sys, int reps, double* best_ms) {
   });
 }
 
+int cppe_gpu_schedule_info(cppe_gpu_system* sys, int* symmetric_near, long* near_items,
+                           int* m2l_chunk) {
+  return guard([&]() -> int {
+    need(sys, "null argument");
+    const Geometry& g = sys->s.geo;
+    if (symmetric_near) *symmetric_near = g.has_sym() ? 1 : 0;
+    if (near_items)
+      *near_items = (long)(g.has_sym() ? g.h_sym_items.size() : g.h_items.size());
+    if (m2l_chunk) *m2l_chunk = g.m2l_chunk > 0 ? g.m2l_chunk : M2L_CHUNK;
+    return CPPE_GPU_OK;
+  });
+}
+
 int cppe_gpu_fma_peak(int device, int fp64, double* tflops) {
   return guard([&]() -> int {
     need(tflops, "null argument");

@@ -40,7 +40,7 @@ constexpr double P2P_UNDAMPED_V = 27.0;
 constexpr int M2L_WARPS  = 4;
 constexpr int P2M_LEAF_SITES  = 128;  // sites staged per round of the leaf P2M
 constexpr int M2M_TASK_LEAVES = 8;    // leaf multipoles shifted per upward-pass task
-constexpr int M2L_CHUNK       = 64;   // sources of one target cell per M2L warp
+// M2L_CHUNK (engine.h): sources of one target cell per M2L warp
 constexpr bool M2L_TABLE_FP64 = true;  // FP64 M2L from tabulated derivative tensors
 constexpr int PW = PMAX + 1;          // powers 0..PMAX of one coordinate
 constexpr int FINISH_BLOCK = 128;
@@ -1102,12 +1102,13 @@ __global__ void __launch_bounds__(P2P_BLOCK)
 //  - The targets of A (64 per pass) are staged in shared memory and broadcast
 //    one at a time.  Per target the lane's two pair tensors give the sources'
 //    fields (F_j += T mu_i, accumulated in registers over all targets) and
-//    the target's field (T mu_j), which a butterfly adds over the warp and
-//    lane (i mod 32) keeps (compensated).
+//    the target's field (T mu_j).  The targets' fields of eight targets are
+//    reduce-scattered over the warp (9 shuffles and adds per component) and
+//    added, compensated, to the warp's accumulators in shared memory.
 //  - A source's field goes to its leaf's output row for this item; the self
 //    leaf (B = A) is evaluated one way only.  The four warps' target fields
 //    are added in warp order into the item's row of A.  Rows are fixed at
-//    set-up and added by k_sym_gather in a fixed order (no atomics).
+//    set-up and added by the finishing pass in a fixed order (no atomics).
 //  - Damping as in k_p2p32_m1: the damping class first with the Thole
 //    factors, then the partners with v >= 27 for every pair without them;
 //    1/R capped at 1e4 (self pairs give an exact zero); lanes without a
@@ -1117,7 +1118,7 @@ constexpr int SYM_TILE = 256;  // sources per tile: 4 warps x 32 lanes x 2
 constexpr int SYM_TGT  = 64;   // targets per pass over the sources
 
 template <bool DAMP>
-__global__ void __launch_bounds__(P2P_BLOCK)
+__global__ void __launch_bounds__(P2P_BLOCK, 6)
       k_p2p32_m1_sym(const int* __restrict__ leaf_start, const int4* __restrict__ items,
                      const int* __restrict__ item_split, const long long* __restrict__ item_aoff,
                      const int* __restrict__ usrc, const long long* __restrict__ usrc_off,
@@ -1289,22 +1290,6 @@ __global__ void __launch_bounds__(P2P_BLOCK)
   }
 }
 
-// Near-field totals of the symmetric pass: each site adds its leaf's rows in
-// row order into slot 0 of the near-field buffer.
-__global__ void k_sym_gather(int n, const int* __restrict__ site_leaf,
-                             const int* __restrict__ leaf_start, const int* __restrict__ leaf_rows,
-                             const long long* __restrict__ leaf_off, const float* __restrict__ rows,
-                             float* __restrict__ Fnear) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const int L = site_leaf[i];
-  const int p = i - leaf_start[L];
-  const long long stride = 3 * (long long)(leaf_start[L + 1] - leaf_start[L]);
-  const float* r = rows + leaf_off[L] + 3 * (long long)p;
-  float fx = 0.f, fy = 0.f, fz = 0.f;
-  for (int k = 0; k < leaf_rows[L]; ++k, r += stride) fx += r[0], fy += r[1], fz += r[2];
-  Fnear[3 * (size_t)i] = fx, Fnear[3 * (size_t)i + 1] = fy, Fnear[3 * (size_t)i + 2] = fz;
-}
 
 // ---------------------------------------------------------------------------
 // Near field, FP32, dipole sources, for the right-hand sides of a batch
@@ -1321,9 +1306,12 @@ __global__ void k_sym_gather(int n, const int* __restrict__ site_leaf,
 // take no work (their output is not read); items whose copies have all
 // finished return at once.
 // ---------------------------------------------------------------------------
-constexpr int P2PM_PAIRS = 144;  // staged source pairs per tile
+// staged source pairs per tile: 96, 120 or 144 (built in; static shared
+// memory stays below 48 KB), chosen by the batch's schedule autotuner
+// (Geometry::multi_tile)
+constexpr int P2PM_PAIRS = 144;
 constexpr int P2PM_MAXR  = 8;    // right-hand sides per launch
-template <bool DAMP>
+template <bool DAMP, int PAIRS = P2PM_PAIRS>
 __global__ void __launch_bounds__(P2P_BLOCK)
       k_p2p32_m1_multi(int n, const int* __restrict__ leaf_start, const int4* __restrict__ items,
                        const int* __restrict__ item_split, const int2* __restrict__ item_stride,
@@ -1331,12 +1319,12 @@ __global__ void __launch_bounds__(P2P_BLOCK)
                        const float4* __restrict__ hi, const float4* __restrict__ lo,
                        const float* __restrict__ src, float damping, float* __restrict__ Fnear,
                        const int* __restrict__ leaf_seg, const int* __restrict__ seg_done) {
-  constexpr int TILE = 2 * P2PM_PAIRS;
+  constexpr int TILE = 2 * PAIRS;
   constexpr int R    = P2PM_MAXR;
-  __shared__ float4 s_xy[P2PM_PAIRS];       // x_j, x_j+1, y_j, y_j+1
-  __shared__ float4 s_zs[P2PM_PAIRS];       // z_j, z_j+1, s_j, s_j+1
-  __shared__ float4 s_mxy[P2PM_PAIRS * R];  // per copy: mx_j, mx_j+1, my_j, my_j+1
-  __shared__ float2 s_mz[P2PM_PAIRS * R];   // per copy: mz_j, mz_j+1
+  __shared__ float4 s_xy[PAIRS];       // x_j, x_j+1, y_j, y_j+1
+  __shared__ float4 s_zs[PAIRS];       // z_j, z_j+1, s_j, s_j+1
+  __shared__ float4 s_mxy[PAIRS * R];  // per copy: mx_j, mx_j+1, my_j, my_j+1
+  __shared__ float2 s_mz[PAIRS * R];   // per copy: mz_j, mz_j+1
   __shared__ int s_site[TILE];              // copy-0 site of each tile slot
   __shared__ TilePlan s_plan;
   __shared__ float s_red[P2P_BLOCK * 3 * R];
@@ -2292,8 +2280,18 @@ __global__ void __launch_bounds__(32 * M2L_WARPS)
 // the far field (L2P of the site's leaf), removes excluded pairs, then either
 // adds alpha^-1 src (apply) or accumulates sign * F into an FP64 field.
 // ---------------------------------------------------------------------------
+// Rows of the symmetric near field (Geometry::sym_*), read by the finishing
+// pass in place of the near-field slots when `buf` is set.
+template <typename T>
+struct SymRows {
+  const int* rows = nullptr;        // rows per leaf
+  const long long* off = nullptr;   // first float of each leaf's rows
+  const T* buf = nullptr;
+};
+
 template <typename T, int M, int MODE, int P = 0>
 __global__ void __launch_bounds__(FINISH_BLOCK) k_finish(int n, const int* __restrict__ leaf_nslot, const T* __restrict__ Fnear,
+                         SymRows<T> sr,
                          int use_fmm,
                          TreeView tv, OpsView ov, const T* __restrict__ L, PosArgs<T> pa,
                          CellPos<T> cp, const T* __restrict__ src,
@@ -2307,10 +2305,19 @@ __global__ void __launch_bounds__(FINISH_BLOCK) k_finish(int n, const int* __res
   T dv[1]     = {T(0)};  // (FP32 products for the FP32 apply: see block_sum)
   if (i < n) {
     T f[3] = {0, 0, 0};
-    const int nsl = leaf_nslot ? leaf_nslot[tv.site_leaf[i]] : 1;
-    for (int s = 0; s < nsl; ++s) {
-      const T* q = Fnear + (size_t)s * 3 * n + 3 * (size_t)i;
-      f[0] += q[0], f[1] += q[1], f[2] += q[2];
+    if (sr.buf) {
+      // the site's rows of the symmetric near field, in row order
+      const int Lf = tv.site_leaf[i];
+      const int a  = tv.leaf_start[Lf];
+      const long long stride = 3 * (long long)(tv.leaf_start[Lf + 1] - a);
+      const T* q = sr.buf + sr.off[Lf] + 3 * (long long)(i - a);
+      for (int k = 0; k < sr.rows[Lf]; ++k, q += stride) f[0] += q[0], f[1] += q[1], f[2] += q[2];
+    } else {
+      const int nsl = leaf_nslot[tv.site_leaf[i]];
+      for (int s = 0; s < nsl; ++s) {
+        const T* q = Fnear + (size_t)s * 3 * n + 3 * (size_t)i;
+        f[0] += q[0], f[1] += q[1], f[2] += q[2];
+      }
     }
     if (use_fmm) {
       // L2P of the leaf's accumulated local expansion
@@ -2406,14 +2413,19 @@ static void launch_p2p(const Geometry& g, bool damp, bool fast, const T* src, T 
       const int mg = (int)g.h_mitems.size();
       for (int c0 = 0; c0 < g.ncopies; c0 += P2PM_MAXR) {
         const int nr = std::min(P2PM_MAXR, g.ncopies - c0);
-        if (damp)
-          k_p2p32_m1_multi<true><<<mg, P2P_BLOCK, 0, s>>>(
-                g.n, g.leaf_start.p, g.mitems.p, g.mitem_split.p, g.mitem_stride.p, c0, nr,
-                g.p2p_src.p, g.hi32.p, g.lo32.p, src, damping, Fnear, lseg, seg_done);
-        else
-          k_p2p32_m1_multi<false><<<mg, P2P_BLOCK, 0, s>>>(
-                g.n, g.leaf_start.p, g.mitems.p, g.mitem_split.p, g.mitem_stride.p, c0, nr,
-                g.p2p_src.p, g.hi32.p, g.lo32.p, src, damping, Fnear, lseg, seg_done);
+#define CG_MULTI(D, P)                                                                      \
+  k_p2p32_m1_multi<D, P><<<mg, P2P_BLOCK, 0, s>>>(                                          \
+        g.n, g.leaf_start.p, g.mitems.p, g.mitem_split.p, g.mitem_stride.p, c0, nr,         \
+        g.p2p_src.p, g.hi32.p, g.lo32.p, src, damping, Fnear, lseg, seg_done)
+        const int tile = g.multi_tile > 0 ? g.multi_tile : P2PM_PAIRS;
+        if (tile == 96) {
+          if (damp) CG_MULTI(true, 96); else CG_MULTI(false, 96);
+        } else if (tile == 120) {
+          if (damp) CG_MULTI(true, 120); else CG_MULTI(false, 120);
+        } else {
+          if (damp) CG_MULTI(true, P2PM_PAIRS); else CG_MULTI(false, P2PM_PAIRS);
+        }
+#undef CG_MULTI
         CG_LAUNCH();
       }
       return;
@@ -2651,7 +2663,7 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
       done = true;
     }
   }
-  const int* finish_nslot = g.leaf_nslot.p;
+  SymRows<T> sym_rows;  // set when the symmetric near field ran
   if constexpr (std::is_same<T, float>::value) {
     if (!done && m == 1 && g.has_sym() && !seg_done) {
       // every unordered pair once (k_p2p32_m1_sym), then each site's rows
@@ -2666,12 +2678,8 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
               g.leaf_start.p, g.sym_items.p, g.sym_split.p, g.sym_aoff.p, g.usrc.p,
               g.usrc_off.p, g.hi32.p, g.lo32.p, src, dampT, w.Fsym.p);
       CG_LAUNCH();
-      k_sym_gather<<<(n + 255) / 256, 256, 0, s>>>(n, g.site_leaf.p, g.leaf_start.p,
-                                                   g.sym_leaf_rows.p, g.sym_leaf_off.p, w.Fsym.p,
-                                                   w.Fnear.p);
-      CG_LAUNCH();
-      finish_nslot = nullptr;  // one slot per site
-      done         = true;
+      sym_rows.rows = g.sym_leaf_rows.p, sym_rows.off = g.sym_leaf_off.p, sym_rows.buf = w.Fsym.p;
+      done          = true;
     }
   }
   if (!done && m == 0) launch_p2p<T, 0>(g, damp, fast, src, dampT, w.Fnear.p, s, seg_done);
@@ -2686,7 +2694,7 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
   if (dot) rs = *dot;
   const T* Lp = g.fmm ? w.Lleaf.p : nullptr;
 #define CG_FINISH(TT, MM, MODE, PP)                                                           \
-  k_finish<TT, MM, MODE, PP><<<nb, FB, 0, s>>>(n, finish_nslot, w.Fnear.p, g.fmm ? 1 : 0, tv, ov, Lp, \
+  k_finish<TT, MM, MODE, PP><<<nb, FB, 0, s>>>(n, g.leaf_nslot.p, w.Fnear.p, sym_rows, g.fmm ? 1 : 0, tv, ov, Lp, \
                                            pos_args<TT>(g), cell_pos<TT>(g), src, damp ? 1 : 0, \
                                            dampT, g.corr_ptr.p, g.corr_idx.p, ainv6, out,    \
                                            out64, sign, rs)

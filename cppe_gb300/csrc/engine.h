@@ -78,6 +78,8 @@ bool m2l_vectors(const TreeLayout& L, std::vector<int>& vid, std::vector<double4
 // so that rows start on 16-byte boundaries.
 __host__ __device__ constexpr int m_stride(int ms) { return (ms + 3) & ~3; }
 
+constexpr int M2L_CHUNK = 64;  // built-in sources of one target cell per M2L warp
+
 // Geometry: the sites, their permutation and the interaction structure.
 struct Geometry {
   int n       = 0;
@@ -115,7 +117,7 @@ struct Geometry {
   // damping class first; B = A is the self leaf, evaluated one way).  An item
   // writes its targets' fields to its row of A and each partner's fields to
   // that partner's row for this item; leaf L owns sym_leaf_rows[L] rows of
-  // 3 n_L floats from float offset sym_leaf_off[L], and a gather pass adds
+  // 3 n_L floats from float offset sym_leaf_off[L], and the finishing pass adds
   // them in row order (fixed at set-up: deterministic, no atomics).
   std::vector<int> h_usrc, h_sym_split;
   std::vector<long long> h_usrc_off, h_sym_aoff, h_sym_leaf_off;
@@ -189,6 +191,7 @@ struct Geometry {
   // tunable schedule parameters (0: the built-in choice)
   long item_pairs = 0;  // target pairs per near-field work item
   int m2l_chunk   = 0;  // sources per M2L warp
+  int multi_tile  = 0;  // source pairs per tile of a batch's multi-RHS near field (96/120/144)
   // builds both schedules from `layout` and h_pos64
   void make_schedules();
   // re-uploads what make_schedules changes (near-field items, M2L chunks)

@@ -303,6 +303,11 @@ int cppe_gpu_kernel_timings(cppe_gpu_system* sys, int precision, int reps, doubl
  * apply time.  The operator is unchanged; only the work partition and the
  * stream scheduling differ. */
 int cppe_gpu_autotune(cppe_gpu_system* sys, int reps, double* best_ms);
+/* The schedule in use (no counterpart in the reference): whether the FP32
+ * near field evaluates each leaf pair once for both directions (1) or per
+ * target leaf (0), its number of work items, and the sources per M2L warp. */
+int cppe_gpu_schedule_info(cppe_gpu_system* sys, int* symmetric_near, long* near_items,
+                           int* m2l_chunk);
 /* Measured FMA throughput of the device in TFLOP/s (2 FLOP per FMA), FP32 or FP64. */
 int cppe_gpu_fma_peak(int device, int fp64, double* tflops);
 
