@@ -13,10 +13,12 @@
 // so the leading-dimension offset (next core matrix along K) is 128 bytes and
 // the stride-dimension offset (next 8 rows) is SBO.  One thread issues the
 // tcgen05.mma instructions (K = 8 each) into an FP32 accumulator of 128 lanes
-// x N columns in tensor memory and commits them to an mbarrier; the four warps
-// read their 32 lanes back with tcgen05.ld, add the bias, apply GELU and store
-// the next layer's operand.  The weights stay in shared memory for the CTA's
-// lifetime (persistent CTAs, one per SM, looping over row tiles).
+// x N columns in tensor memory and commits them to an mbarrier; sixteen warps
+// read the accumulator back with tcgen05.ld (warp w: lanes 32 (w mod 4) on,
+// columns 32 (w / 4) on -- a warp may only reach its own quarter of the
+// lanes), add the bias, apply GELU and store the next layer's operand.  The
+// weights stay in shared memory for the CTA's lifetime (persistent CTAs, one
+// per SM, looping over row tiles).
 //
 // Every mbarrier wait is bounded by the global timer (1 s): on expiry the
 // kernel records an error code, stops issuing work, waits (bounded again) for
@@ -29,7 +31,8 @@ namespace cg {
 
 namespace {
 
-constexpr int TC_ROWS = 128;  // rows (sites) per tile = MMA M
+constexpr int TC_ROWS    = 128;  // rows (sites) per tile = MMA M
+constexpr int TC_THREADS = 512;  // 16 warps: 4 lane quarters x 4 column groups
 constexpr int TC_W3N  = 16;   // layer-3 N (4 outputs padded to the smallest N for M = 128)
 constexpr int TC_COLS = 128;  // tensor-memory columns of the accumulator
 
@@ -148,7 +151,7 @@ __device__ __forceinline__ float gelu_tc(float z) {
 }  // namespace
 
 // Error codes written to *err: 1 = an mbarrier wait ran out of time.
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(TC_THREADS, 1)
       k_mlp_infer_tc(int rows, const float* __restrict__ raw, const float* __restrict__ params,
                      const float* __restrict__ mean, const float* __restrict__ inv_std,
                      float* __restrict__ Y, int* __restrict__ err) {
@@ -212,8 +215,9 @@ __global__ void __launch_bounds__(128, 1)
   __syncthreads();
   fence_after();
   const uint32_t tmem = *tslot;
-  const uint32_t lane_base = tmem + ((uint32_t)(32 * warp) << 16);
-  const int row_local = tid;  // TMEM lane = row of the tile
+  const int quarter = warp & 3, cgroup = warp >> 2;
+  const uint32_t lane_base = tmem + ((uint32_t)(32 * quarter) << 16);
+  const int row_local = 32 * quarter + (tid & 31);  // TMEM lane = row of the tile
   uint32_t parity = 0;
   const uint32_t aX = smem_addr(sm + OFF_X), aH = smem_addr(sm + OFF_H);
   const uint32_t aW1 = smem_addr(sm + OFF_W1), aW2 = smem_addr(sm + OFF_W2),
@@ -241,8 +245,8 @@ __global__ void __launch_bounds__(128, 1)
   };
   // hidden-layer epilogue: GELU(acc + b) into the next layer's operand
   auto hidden_epilogue = [&](const float* bias) {
-#pragma unroll 1
-    for (int c = 0; c < Mlp::H / 32; ++c) {
+    {
+      const int c = cgroup;  // this warp's 32 columns
       float v[32];
       tmem_ld32(lane_base + 32 * c, v);
 #pragma unroll
@@ -283,7 +287,7 @@ __global__ void __launch_bounds__(128, 1)
     if (!run_layer(aH, aW2, Mlp::H, Mlp::H)) break;
     hidden_epilogue(b2);
     if (!run_layer(aH, aW3, Mlp::H, TC_W3N)) break;
-    {
+    if (cgroup == 0) {
       float v[32];
       tmem_ld32(lane_base, v);  // columns 0..31; 0..3 are the outputs
       const long row = row0 + row_local;
@@ -323,7 +327,7 @@ void mlp_infer_tc(int device, int rows, const float* raw, const float* params,
   CG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
   const int ntiles = (rows + TC_ROWS - 1) / TC_ROWS;
   const int grid   = std::max(1, std::min(ntiles, sms));
-  k_mlp_infer_tc<<<grid, 128, SMEM_BYTES, s>>>(rows, raw, params, mean, inv_std, Y, err);
+  k_mlp_infer_tc<<<grid, TC_THREADS, SMEM_BYTES, s>>>(rows, raw, params, mean, inv_std, Y, err);
   CG_LAUNCH();
 }
 
