@@ -1311,7 +1311,7 @@ __global__ void __launch_bounds__(P2P_BLOCK, 6)
 // (Geometry::multi_tile)
 constexpr int P2PM_PAIRS = 144;
 constexpr int P2PM_MAXR  = 8;    // right-hand sides per launch
-template <bool DAMP, int PAIRS = P2PM_PAIRS>
+template <bool DAMP, int PAIRS = P2PM_PAIRS, int RC = P2PM_MAXR>
 __global__ void __launch_bounds__(P2P_BLOCK)
       k_p2p32_m1_multi(int n, const int* __restrict__ leaf_start, const int4* __restrict__ items,
                        const int* __restrict__ item_split, const int2* __restrict__ item_stride,
@@ -1320,7 +1320,7 @@ __global__ void __launch_bounds__(P2P_BLOCK)
                        const float* __restrict__ src, float damping, float* __restrict__ Fnear,
                        const int* __restrict__ leaf_seg, const int* __restrict__ seg_done) {
   constexpr int TILE = 2 * PAIRS;
-  constexpr int R    = P2PM_MAXR;
+  constexpr int R    = RC;  // right-hand sides per pass
   __shared__ float4 s_xy[PAIRS];       // x_j, x_j+1, y_j, y_j+1
   __shared__ float4 s_zs[PAIRS];       // z_j, z_j+1, s_j, s_j+1
   __shared__ float4 s_mxy[PAIRS * R];  // per copy: mx_j, mx_j+1, my_j, my_j+1
@@ -2411,20 +2411,26 @@ static void launch_p2p(const Geometry& g, bool damp, bool fast, const T* src, T 
     if (!g.h_mitems.empty() && g.ncopies > 1) {
       // a batch's right-hand sides together, up to P2PM_MAXR per launch
       const int mg = (int)g.h_mitems.size();
-      for (int c0 = 0; c0 < g.ncopies; c0 += P2PM_MAXR) {
-        const int nr = std::min(P2PM_MAXR, g.ncopies - c0);
-#define CG_MULTI(D, P)                                                                      \
-  k_p2p32_m1_multi<D, P><<<mg, P2P_BLOCK, 0, s>>>(                                          \
+      // right-hand sides per pass (8, or 4 with fewer registers) and tile size,
+      // as the batch's schedule autotuner chose them
+      const int rc = g.multi_copies == 4 ? 4 : P2PM_MAXR;
+      for (int c0 = 0; c0 < g.ncopies; c0 += rc) {
+        const int nr = std::min(rc, g.ncopies - c0);
+#define CG_MULTI(D, P, R)                                                                   \
+  k_p2p32_m1_multi<D, P, R><<<mg, P2P_BLOCK, 0, s>>>(                                       \
         g.n, g.leaf_start.p, g.mitems.p, g.mitem_split.p, g.mitem_stride.p, c0, nr,         \
         g.p2p_src.p, g.hi32.p, g.lo32.p, src, damping, Fnear, lseg, seg_done)
+#define CG_MULTI_R(D, P) \
+  if (rc == 4) CG_MULTI(D, P, 4); else CG_MULTI(D, P, P2PM_MAXR)
         const int tile = g.multi_tile > 0 ? g.multi_tile : P2PM_PAIRS;
         if (tile == 96) {
-          if (damp) CG_MULTI(true, 96); else CG_MULTI(false, 96);
+          if (damp) { CG_MULTI_R(true, 96); } else { CG_MULTI_R(false, 96); }
         } else if (tile == 120) {
-          if (damp) CG_MULTI(true, 120); else CG_MULTI(false, 120);
+          if (damp) { CG_MULTI_R(true, 120); } else { CG_MULTI_R(false, 120); }
         } else {
-          if (damp) CG_MULTI(true, P2PM_PAIRS); else CG_MULTI(false, P2PM_PAIRS);
+          if (damp) { CG_MULTI_R(true, P2PM_PAIRS); } else { CG_MULTI_R(false, P2PM_PAIRS); }
         }
+#undef CG_MULTI_R
 #undef CG_MULTI
         CG_LAUNCH();
       }

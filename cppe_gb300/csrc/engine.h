@@ -192,6 +192,7 @@ struct Geometry {
   long item_pairs = 0;  // target pairs per near-field work item
   int m2l_chunk   = 0;  // sources per M2L warp
   int multi_tile  = 0;  // source pairs per tile of a batch's multi-RHS near field (96/120/144)
+  int multi_copies = 0;  // right-hand sides per pass of it (4 or 8; 0: 8)
   // builds both schedules from `layout` and h_pos64
   void make_schedules();
   // re-uploads what make_schedules changes (near-field items, M2L chunks)

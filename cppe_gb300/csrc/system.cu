@@ -430,29 +430,34 @@ double autotune_schedule(Geometry& geo, SideStream& side, cudaStream_t stream, i
   long best_w = w0;
   int best_c  = 64;
   bool best_s = geo.sym_enabled;
-  int best_t  = geo.multi_tile;
+  int best_t  = geo.multi_tile, best_r = geo.multi_copies;
   // symmetric near field (single systems) or per-target items; for a batch
-  // whose snapshots repeat per right-hand side, the multi-RHS tile size
+  // whose snapshots repeat per right-hand side, the multi-RHS tile size and
+  // the right-hand sides per pass
   const int nsym = (geo.h_leaf_seg.empty() && geo.ncopies == 1) ? 2 : 1;
   const int tiles[3] = {96, 120, 144};
   const int ntile    = geo.ncopies > 1 ? 3 : 1;
-  for (int ti = 0; ti < ntile; ++ti)
-    for (int si = 0; si < nsym; ++si)
-      for (long w : ws)
-        for (int ci = 0; ci < nch; ++ci) {
-          geo.sym_enabled = nsym == 2 ? si == 0 : geo.sym_enabled;
-          geo.multi_tile  = ntile == 3 ? tiles[ti] : geo.multi_tile;
-          geo.item_pairs  = w;
-          geo.m2l_chunk   = chs[ci];
-          geo.make_schedules();
-          geo.upload_schedules(stream);
-          const double ms = time_applies();
-          if (ms < best)
-            best = ms, best_w = w, best_c = chs[ci], best_s = geo.sym_enabled,
-            best_t = geo.multi_tile;
-        }
-  geo.sym_enabled = best_s;
-  geo.multi_tile  = best_t;
+  const int nrc      = geo.ncopies > 4 ? 2 : 1;
+  for (int ri = 0; ri < nrc; ++ri)
+    for (int ti = 0; ti < ntile; ++ti)
+      for (int si = 0; si < nsym; ++si)
+        for (long w : ws)
+          for (int ci = 0; ci < nch; ++ci) {
+            geo.sym_enabled  = nsym == 2 ? si == 0 : geo.sym_enabled;
+            geo.multi_tile   = ntile == 3 ? tiles[ti] : geo.multi_tile;
+            geo.multi_copies = nrc == 2 ? (ri == 0 ? 8 : 4) : geo.multi_copies;
+            geo.item_pairs   = w;
+            geo.m2l_chunk    = chs[ci];
+            geo.make_schedules();
+            geo.upload_schedules(stream);
+            const double ms = time_applies();
+            if (ms < best)
+              best = ms, best_w = w, best_c = chs[ci], best_s = geo.sym_enabled,
+              best_t = geo.multi_tile, best_r = geo.multi_copies;
+          }
+  geo.sym_enabled  = best_s;
+  geo.multi_tile   = best_t;
+  geo.multi_copies = best_r;
   geo.item_pairs  = best_w;
   geo.m2l_chunk   = best_c;
   geo.make_schedules();

@@ -67,6 +67,21 @@ def test_batch_autotune_keeps_the_solution(gpu):
     np.testing.assert_allclose(mu2, mu1, rtol=0, atol=1e-10)
 
 
+def test_batch_autotune_mixed_keeps_the_solution(gpu):
+    """In mixed precision the tuner also picks the multi-RHS near field's tile
+    size (96, 120 or 144 source pairs): the FP32 sums are reordered, the
+    answer still meets the same FP64 stopping rule."""
+    boxes = _snapshots()
+    nrhs = 2
+    rhs = _rhs(boxes, nrhs, seed=3)
+    batch = cabi.Batch(boxes, nrhs, direct_below=1000, damp=True, precision=cabi.MIXED)
+    mu1, _ = batch.solve(rhs)
+    assert batch.autotune(2) > 0.0
+    mu2, _ = batch.solve(rhs)
+    assert batch.stats()["max_rnorm"] < 1e-8
+    np.testing.assert_allclose(mu2, mu1, rtol=0, atol=5e-8)
+
+
 _HOST_LOOP = r"""
 import os, sys, numpy as np
 sys.path[:0] = [sys.argv[1], os.path.dirname(sys.argv[1])]
