@@ -559,8 +559,12 @@ def profiled_traffic(md_name):
 
 
 # committed ncu summaries of the FP32 near field, by workload and form
-PROFILE_OF = {("30k-fmm5", False): "k_p2p32_m1_30k_sites.md",
-              ("1m-fmm6", True): "k_p2p32_m1_sym_1m_sites.md"}
+# (workload, near-field form: 0 per target, 1 or 2 symmetric with two or
+# four sources a lane) -> the committed capture of that kernel
+PROFILE_OF = {("30k-fmm5", 0): "k_p2p32_m1_30k_sites.md",
+              ("30k-fmm5", 1): "k_p2p32_m1_sym_30k_sites.md",
+              ("1m-fmm6", 1): "k_p2p32_m1_sym_1m_sites.md",
+              ("1m-fmm6", 2): "k_p2p32_m1_sym_4src_1m_sites.md"}
 
 
 def run_ours(args):
@@ -582,6 +586,8 @@ def run_ours(args):
     s64 = capi.System(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, precision=capi.FP64, **kw)
     if args.apply_only:
         # operator applies only (FP32 then FP64), e.g. for kernel profiling
+        if args.near_form >= 0:
+            smx.set_schedule(args.near_form)
         t32 = smx.kernel_timings(capi.MIXED, reps=args.apply_only)
         tdd = smx.kernel_timings(DD_RESIDUAL, reps=args.apply_only)
         t64 = s64.kernel_timings(capi.FP64, reps=args.apply_only) if not args.no_fp64 else \
@@ -684,9 +690,10 @@ def run_ours(args):
     timdd, _, _ = smx.kernel_timings(DD_RESIDUAL, reps=3)
     tim64, _, _ = s64.kernel_timings(capi.FP64, reps=2)
     sched = smx.schedule()
-    near_kernel = "k_p2p32_m1_sym<true> (FP32 dipole near field, each leaf pair once)" \
+    near_kernel = (f"k_p2p32_m1_sym<true, {sched['sym_pack']}> (FP32 dipole near field, each "
+                   f"leaf pair once, {2 * sched['sym_pack']} sources a lane)") \
         if sched["symmetric_near"] else "k_p2p32_m1<true> (FP32 dipole near field)"
-    prof = PROFILE_OF.get((args.config, sched["symmetric_near"]))
+    prof = PROFILE_OF.get((args.config, sched["sym_pack"]))
     fp32_peak = capi.fma_peak_tflops(False, dev)
     fp64_peak = capi.fma_peak_tflops(True, dev)
     achieved = alg_pairs * FLOP_PER_PAIR / (tim32["near"] * 1e-3) / 1e12
@@ -806,6 +813,9 @@ def main():
                     help="skip the extra 30k- and 300k-site sections")
     ap.add_argument("--no-fp64", action="store_true",
                     help="with --apply-only: skip the FP64 operator")
+    ap.add_argument("--near-form", type=int, default=-1, choices=(-1, 0, 1, 2),
+                    help="with --apply-only: FP32 near-field form (0 per target, 1 or 2 "
+                         "symmetric with two or four sources a lane; -1 the built-in one)")
     ap.add_argument("--no-learned", action="store_true", help="skip the trained model")
     ap.add_argument("--model", default=os.path.join(ROOT, "cppe_gb300", "data",
                                                     "learned_water.npz"))

@@ -425,12 +425,22 @@ class System:
         return ms.value
 
     def schedule(self):
-        """The schedule in use: symmetric near field, near-field items, M2L chunk."""
+        """The schedule in use: symmetric near field (and its packed source
+        pairs per lane, 0 when per target), near-field items, M2L chunk."""
         sym, items, ch = ctypes.c_int(0), ctypes.c_long(0), ctypes.c_int(0)
         lib().cppe_gpu_schedule_info.argtypes = [ctypes.c_void_p, I, L, I]
         check(lib().cppe_gpu_schedule_info(self.h, ctypes.byref(sym), ctypes.byref(items),
                                            ctypes.byref(ch)))
-        return dict(symmetric_near=bool(sym.value), near_items=items.value, m2l_chunk=ch.value)
+        return dict(symmetric_near=bool(sym.value), sym_pack=sym.value, near_items=items.value,
+                    m2l_chunk=ch.value)
+
+    def set_schedule(self, near_form=-1, item_pairs=0, m2l_chunk=0):
+        """Sets the schedule: near_form 0 per target, 1 or 2 symmetric with two
+        or four sources a lane (-1 keeps it); item_pairs and m2l_chunk <= 0
+        keep theirs."""
+        lib().cppe_gpu_set_schedule.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_long,
+                                                ctypes.c_int]
+        check(lib().cppe_gpu_set_schedule(self.h, near_form, item_pairs, m2l_chunk))
 
     def kernel_timings(self, precision=FP64, reps=5):
         ms = np.zeros(6)

@@ -737,12 +737,25 @@ int cppe_gpu_autotune(cppe_gpu_system* sys, int reps, double* best_ms) {
   });
 }
 
+int cppe_gpu_set_schedule(cppe_gpu_system* sys, int near_form, long item_pairs,
+                          int m2l_chunk) {
+  return guard([&]() -> int {
+    need(sys, "null argument");
+    need(near_form >= -1 && near_form <= 2, "near_form must be -1, 0, 1 or 2");
+    need(m2l_chunk <= 0 || m2l_chunk == 32 || m2l_chunk == 64 || m2l_chunk == 128,
+         "m2l_chunk must be 32, 64 or 128");
+    need(item_pairs <= 0 || item_pairs >= 1024, "item_pairs must be at least 1024");
+    sys->s.set_schedule(near_form, item_pairs, m2l_chunk);
+    return CPPE_GPU_OK;
+  });
+}
+
 int cppe_gpu_schedule_info(cppe_gpu_system* sys, int* symmetric_near, long* near_items,
                            int* m2l_chunk) {
   return guard([&]() -> int {
     need(sys, "null argument");
     const Geometry& g = sys->s.geo;
-    if (symmetric_near) *symmetric_near = g.has_sym() ? 1 : 0;
+    if (symmetric_near) *symmetric_near = g.has_sym() ? g.sym_pack : 0;
     if (near_items)
       *near_items = (long)(g.has_sym() ? g.h_sym_items.size() : g.h_items.size());
     if (m2l_chunk) *m2l_chunk = g.m2l_chunk > 0 ? g.m2l_chunk : M2L_CHUNK;

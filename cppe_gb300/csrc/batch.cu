@@ -67,6 +67,16 @@ void Geometry::combine(const std::vector<const Geometry*>& parts, int copies, Ge
       local_of_cell[k] = c;
     }
   out.h_cell_seg = seg_of_cell;
+  // the parts' tables of distinct M2L vectors, concatenated (each snapshot
+  // keeps its own grid of translation vectors): the FP64 and double-float
+  // M2L then read tabulated tensors as they do for one system
+  bool tables = true;
+  std::vector<int> vec_off(np + 1, 0);
+  for (int g = 0; g < np; ++g) {
+    const Geometry* p = parts[g];
+    if (p->layout.m2l_src.size() != p->h_m2l_vid.size()) tables = false;
+    vec_off[g + 1] = vec_off[g] + (int)p->h_vec.size();
+  }
   L.child_ptr.assign(nc + 1, 0);
   L.m2l_ptr.assign(nc + 1, 0);
   for (int k = 0; k < nc; ++k) {
@@ -78,10 +88,16 @@ void Geometry::combine(const std::vector<const Geometry*>& parts, int copies, Ge
     for (int q = P.child_ptr[c]; q < P.child_ptr[c + 1]; ++q)
       L.child_idx.push_back(cmap[s][P.child_idx[q]]);
     L.child_ptr[k + 1] = (int)L.child_idx.size();
-    for (int q = P.m2l_ptr[c]; q < P.m2l_ptr[c + 1]; ++q)
+    for (int q = P.m2l_ptr[c]; q < P.m2l_ptr[c + 1]; ++q) {
       L.m2l_src.push_back(cmap[s][P.m2l_src[q]]);
+      if (tables) out.h_m2l_vid.push_back(vec_off[part_of(s)] + parts[part_of(s)]->h_m2l_vid[q]);
+    }
     L.m2l_ptr[k + 1] = (int)L.m2l_src.size();
   }
+  if (tables && !L.m2l_src.empty())
+    for (auto* p : parts) out.h_vec.insert(out.h_vec.end(), p->h_vec.begin(), p->h_vec.end());
+  else
+    out.h_m2l_vid.clear(), out.h_vec.clear();
   // leaves and particles: segment after segment
   L.leaf_of_cell.assign(nc, -1);
   L.leaf_start.assign(1, 0);
@@ -510,6 +526,7 @@ bool BatchSystem::pcg_graph_ready(T* xv, T* rv, T* zv, T* pv, T* Apv, const T* a
       if (ok) {
         const long long c0 = launch_counter();
         try {
+          CaptureScope cs;
           pcg_iteration<T>(xv, rv, zv, pv, Apv, a6, maxiter, true);
           k_bcg_continue<<<1, 1, 0, stream>>>(h, active.p);
           CG_LAUNCH();

@@ -45,6 +45,14 @@ long long& launch_counter();
     ++::cg::launch_counter();                                                   \
   } while (0)
 
+// Set while this thread captures a CUDA graph.  Work buffers must have their
+// size by then: a cudaFree or cudaMalloc inside the capture would end it.
+inline thread_local bool g_capturing = false;
+struct CaptureScope {
+  CaptureScope() { g_capturing = true; }
+  ~CaptureScope() { g_capturing = false; }
+};
+
 // Device buffer owning cudaMalloc'd memory.
 template <class T>
 struct DBuf {
@@ -67,6 +75,7 @@ struct DBuf {
   }
   void alloc(size_t count) {
     if (count == n && p) return;
+    if (g_capturing) fail(CPPE_GPU_CUDA_ERROR, "device buffer resized during graph capture");
     release();
     if (count == 0) return;
     CG_CUDA(cudaMalloc(&p, count * sizeof(T)));

@@ -1096,17 +1096,19 @@ __global__ void __launch_bounds__(P2P_BLOCK)
 // first; see Geometry::make_sym_schedule) and evaluates each pair tensor once
 // for both directions (T(r) = T(-r)): 21 of a damped pair's 31 operations are
 // the tensor, so a cross pair costs 41 operations instead of 62.
-//  - Lanes own sources: each of the 4 warps takes 64 consecutive sources of
-//    a 256-source tile (two per lane, packed FP32x2), with positions relative
-//    to the first site of A (hi/lo differences) in registers.
+//  - Lanes own sources: each warp takes consecutive sources of a 256-source
+//    tile, two or four per lane (one or two packed FP32x2 pairs; 4 or 2
+//    warps), with positions relative to the first site of A (hi/lo
+//    differences) in registers.
 //  - The targets of A (64 per pass) are staged in shared memory and broadcast
-//    one at a time.  Per target the lane's two pair tensors give the sources'
+//    one at a time.  Per target the lane's pair tensors give the sources'
 //    fields (F_j += T mu_i, accumulated in registers over all targets) and
-//    the target's field (T mu_j).  The targets' fields of eight targets are
-//    reduce-scattered over the warp (9 shuffles and adds per component) and
-//    added, compensated, to the warp's accumulators in shared memory.
+//    the target's field (T mu_j, summed over the lane's sources).  The
+//    targets' fields of eight targets are reduce-scattered over the warp (9
+//    shuffles and adds per component) and added, compensated, to the warp's
+//    accumulators in shared memory.
 //  - A source's field goes to its leaf's output row for this item; the self
-//    leaf (B = A) is evaluated one way only.  The four warps' target fields
+//    leaf (B = A) is evaluated one way only.  The warps' target fields
 //    are added in warp order into the item's row of A.  Rows are fixed at
 //    set-up and added by the finishing pass in a fixed order (no atomics).
 //  - Damping as in k_p2p32_m1: the damping class first with the Thole
@@ -1114,19 +1116,30 @@ __global__ void __launch_bounds__(P2P_BLOCK)
 //    1/R capped at 1e4 (self pairs give an exact zero); lanes without a
 //    source hold a zero moment 1e4 bohr away.
 // ---------------------------------------------------------------------------
-constexpr int SYM_TILE = 256;  // sources per tile: 4 warps x 32 lanes x 2
+constexpr int SYM_TILE = 256;  // sources per tile: (4 / NPK) warps x 32 lanes x 2 NPK
 constexpr int SYM_TGT  = 64;   // targets per pass over the sources
 
-template <bool DAMP>
-__global__ void __launch_bounds__(P2P_BLOCK, 6)
+// NPK packed source pairs per lane: 1 (128 threads, two sources a lane) or 2
+// (64 threads, four sources a lane: the target broadcasts and reduce-scatters
+// are shared by twice the pairs, at fewer resident warps).  The schedule
+// autotuner picks one (Geometry::sym_pack).
+template <int NPK>
+constexpr int sym_threads() { return 128 / NPK; }
+template <int NPK>
+constexpr int sym_min_blocks() { return NPK == 1 ? 6 : 10; }
+
+template <bool DAMP, int NPK>
+__global__ void __launch_bounds__(sym_threads<NPK>(), sym_min_blocks<NPK>())
       k_p2p32_m1_sym(const int* __restrict__ leaf_start, const int4* __restrict__ items,
                      const int* __restrict__ item_split, const long long* __restrict__ item_aoff,
                      const int* __restrict__ usrc, const long long* __restrict__ usrc_off,
                      const float4* __restrict__ hi, const float4* __restrict__ lo,
                      const float* __restrict__ src, float damping, float* __restrict__ rows) {
+  constexpr int NW  = 4 / NPK;  // warps
+  constexpr int SPL = 2 * NPK;  // sources per lane
   __shared__ float4 s_t[SYM_TGT];   // target x, y, z, AI (padded to a multiple of 8)
   __shared__ float4 s_tm[SYM_TGT];  // target mx, my, mz
-  __shared__ float s_acc[4][SYM_TGT][6];  // per warp: target field sums and their errors
+  __shared__ float s_acc[NW][SYM_TGT][6];  // per warp: target field sums and their errors
   __shared__ TilePlan s_plan;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int4 it = items[blockIdx.x];
@@ -1154,7 +1167,7 @@ __global__ void __launch_bounds__(P2P_BLOCK, 6)
         s_tm[k] = make_float4(0.f, 0.f, 0.f, 0.f);
       }
 #pragma unroll
-      for (int w = 0; w < 4; ++w)
+      for (int w = 0; w < NW; ++w)
 #pragma unroll
         for (int c = 0; c < 6; ++c) s_acc[w][k][c] = 0.f;
     }
@@ -1168,16 +1181,15 @@ __global__ void __launch_bounds__(P2P_BLOCK, 6)
         const int np = s_plan.np;
         if (np == 0) break;
         const int total = s_plan.poff[np];
-        // this lane's two sources
-        float2 sx, sy, sz, ss, mx, my, mz;
-        long long o0 = -1, o1 = -1;  // output positions (-1: none)
+        // this lane's sources, packed in pairs
+        float2 sx[NPK], sy[NPK], sz[NPK], ss[NPK], mx[NPK], my[NPK], mz[NPK];
+        long long o[SPL];  // output positions (-1: none)
         {
-          float4 r[2];
-          float m[2][3];
-          long long o[2];
+          float4 r[SPL];
+          float m[SPL][3];
 #pragma unroll
-          for (int h = 0; h < 2; ++h) {
-            const int q = 64 * warp + 2 * lane + h;
+          for (int h = 0; h < SPL; ++h) {
+            const int q = 32 * SPL * warp + SPL * lane + h;
             o[h] = -1;
             if (q < total) {
               // piece of tile slot q (as tile_site) and its list entry
@@ -1198,29 +1210,38 @@ __global__ void __launch_bounds__(P2P_BLOCK, 6)
               m[h][0] = m[h][1] = m[h][2] = 0.f;
             }
           }
-          sx = make_float2(r[0].x, r[1].x), sy = make_float2(r[0].y, r[1].y);
-          sz = make_float2(r[0].z, r[1].z), ss = make_float2(r[0].w, r[1].w);
-          mx = make_float2(m[0][0], m[1][0]), my = make_float2(m[0][1], m[1][1]);
-          mz = make_float2(m[0][2], m[1][2]);
-          o0 = o[0], o1 = o[1];
+#pragma unroll
+          for (int k = 0; k < NPK; ++k) {
+            const int h0 = 2 * k, h1 = 2 * k + 1;
+            sx[k] = make_float2(r[h0].x, r[h1].x), sy[k] = make_float2(r[h0].y, r[h1].y);
+            sz[k] = make_float2(r[h0].z, r[h1].z), ss[k] = make_float2(r[h0].w, r[h1].w);
+            mx[k] = make_float2(m[h0][0], m[h1][0]), my[k] = make_float2(m[h0][1], m[h1][1]);
+            mz[k] = make_float2(m[h0][2], m[h1][2]);
+          }
         }
-        float2 FX = f2(0.f), FY = f2(0.f), FZ = f2(0.f);
+        float2 FX[NPK], FY[NPK], FZ[NPK];
+#pragma unroll
+        for (int k = 0; k < NPK; ++k) FX[k] = FY[k] = FZ[k] = f2(0.f);
         auto sweep = [&](auto damped) {
           constexpr bool D = decltype(damped)::value;
 #pragma unroll 1
           for (int g = 0; g < nT; g += 8) {
             // eight targets (padded with zero moments); their fields from the
-            // lane's two sources stay per lane until the reduce-scatter below
+            // lane's sources stay per lane until the reduce-scatter below
             float p[8][3];
 #pragma unroll
             for (int u = 0; u < 8; ++u) {
               const float4 t = s_t[g + u], tm = s_tm[g + u];
-              float2 x, y, z, Av, Bn;
-              f32x2_tensor_m1<D>(f2(t.x), f2(t.y), f2(t.z), f2(t.w), sx, sy, sz, ss, x, y, z,
-                                 Av, Bn);
-              f32x2_apply_m1(x, y, z, Av, Bn, f2(tm.x), f2(tm.y), f2(tm.z), FX, FY, FZ);
               float2 cx = f2(0.f), cy = f2(0.f), cz = f2(0.f);
-              f32x2_apply_m1(x, y, z, Av, Bn, mx, my, mz, cx, cy, cz);
+#pragma unroll
+              for (int k = 0; k < NPK; ++k) {
+                float2 x, y, z, Av, Bn;
+                f32x2_tensor_m1<D>(f2(t.x), f2(t.y), f2(t.z), f2(t.w), sx[k], sy[k], sz[k],
+                                   ss[k], x, y, z, Av, Bn);
+                f32x2_apply_m1(x, y, z, Av, Bn, f2(tm.x), f2(tm.y), f2(tm.z), FX[k], FY[k],
+                               FZ[k]);
+                f32x2_apply_m1(x, y, z, Av, Bn, mx[k], my[k], mz[k], cx, cy, cz);
+              }
               p[u][0] = cx.x + cx.y, p[u][1] = cy.x + cy.y, p[u][2] = cz.x + cz.y;
             }
             // reduce-scatter over the warp: after the xor-16, -8 and -4 steps
@@ -1270,8 +1291,12 @@ __global__ void __launch_bounds__(P2P_BLOCK, 6)
           sweep(std::true_type{});
         else
           sweep(std::false_type{});
-        if (o0 >= 0) rows[o0] = FX.x, rows[o0 + 1] = FY.x, rows[o0 + 2] = FZ.x;
-        if (o1 >= 0) rows[o1] = FX.y, rows[o1 + 1] = FY.y, rows[o1 + 2] = FZ.y;
+#pragma unroll
+        for (int k = 0; k < NPK; ++k) {
+          const long long oa = o[2 * k], ob = o[2 * k + 1];
+          if (oa >= 0) rows[oa] = FX[k].x, rows[oa + 1] = FY[k].x, rows[oa + 2] = FZ[k].x;
+          if (ob >= 0) rows[ob] = FX[k].y, rows[ob + 1] = FY[k].y, rows[ob + 2] = FZ[k].y;
+        }
         __syncthreads();
       }
     }
@@ -1283,7 +1308,7 @@ __global__ void __launch_bounds__(P2P_BLOCK, 6)
       for (int c = 0; c < 3; ++c) {
         float v = 0.f;
 #pragma unroll
-        for (int w = 0; w < 4; ++w) v += s_acc[w][k][c] + s_acc[w][k][3 + c];
+        for (int w = 0; w < NW; ++w) v += s_acc[w][k][c] + s_acc[w][k][3 + c];
         o[c] = v;
       }
     }
@@ -2663,26 +2688,28 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
   const T dampT = (T)damping;
   const bool fast = near_mode != NEAR_FP64;
   bool done       = false;
+  SymRows<T> sym_rows;  // set when the symmetric near field ran
   if constexpr (std::is_same<T, double>::value) {
     if (near_mode == NEAR_DD && m == 1) {
       launch_p2p_dd(g, damp, src, damping, w, s);
       done = true;
     }
   }
-  SymRows<T> sym_rows;  // set when the symmetric near field ran
   if constexpr (std::is_same<T, float>::value) {
     if (!done && m == 1 && g.has_sym() && !seg_done) {
       // every unordered pair once (k_p2p32_m1_sym), then each site's rows
       w.Fsym.alloc((size_t)g.sym_floats);
       const int ni = (int)g.h_sym_items.size();
-      if (damp)
-        k_p2p32_m1_sym<true><<<ni, P2P_BLOCK, 0, s>>>(
-              g.leaf_start.p, g.sym_items.p, g.sym_split.p, g.sym_aoff.p, g.usrc.p,
-              g.usrc_off.p, g.hi32.p, g.lo32.p, src, dampT, w.Fsym.p);
-      else
-        k_p2p32_m1_sym<false><<<ni, P2P_BLOCK, 0, s>>>(
-              g.leaf_start.p, g.sym_items.p, g.sym_split.p, g.sym_aoff.p, g.usrc.p,
-              g.usrc_off.p, g.hi32.p, g.lo32.p, src, dampT, w.Fsym.p);
+#define CG_SYM(D, K)                                                                    \
+  k_p2p32_m1_sym<D, K><<<ni, sym_threads<K>(), 0, s>>>(                                 \
+        g.leaf_start.p, g.sym_items.p, g.sym_split.p, g.sym_aoff.p, g.usrc.p, g.usrc_off.p, \
+        g.hi32.p, g.lo32.p, src, dampT, w.Fsym.p)
+      if (g.sym_pack == 2) {
+        if (damp) CG_SYM(true, 2); else CG_SYM(false, 2);
+      } else {
+        if (damp) CG_SYM(true, 1); else CG_SYM(false, 1);
+      }
+#undef CG_SYM
       CG_LAUNCH();
       sym_rows.rows = g.sym_leaf_rows.p, sym_rows.off = g.sym_leaf_off.p, sym_rows.buf = w.Fsym.p;
       done          = true;

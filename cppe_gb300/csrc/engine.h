@@ -128,6 +128,7 @@ struct Geometry {
   DBuf<long long> usrc_off, sym_aoff, sym_leaf_off;
   DBuf<int4> sym_items;
   bool sym_enabled = true;  // the schedule autotuner may switch it off
+  int sym_pack     = 1;     // packed source pairs per lane of the symmetric kernel (1 or 2)
   bool has_sym() const { return !h_sym_items.empty(); }
   void make_sym_schedule(long W);
 

@@ -430,11 +430,12 @@ double autotune_schedule(Geometry& geo, SideStream& side, cudaStream_t stream, i
   long best_w = w0;
   int best_c  = 64;
   bool best_s = geo.sym_enabled;
+  int best_k  = geo.sym_pack;
   int best_t  = geo.multi_tile, best_r = geo.multi_copies;
-  // symmetric near field (single systems) or per-target items; for a batch
-  // whose snapshots repeat per right-hand side, the multi-RHS tile size and
-  // the right-hand sides per pass
-  const int nsym = (geo.h_leaf_seg.empty() && geo.ncopies == 1) ? 2 : 1;
+  // symmetric near field (single systems; two or four sources a lane) or
+  // per-target items; for a batch whose snapshots repeat per right-hand
+  // side, the multi-RHS tile size and the right-hand sides per pass
+  const int nsym = (geo.h_leaf_seg.empty() && geo.ncopies == 1) ? 3 : 1;
   const int tiles[3] = {96, 120, 144};
   const int ntile    = geo.ncopies > 1 ? 3 : 1;
   const int nrc      = geo.ncopies > 4 ? 2 : 1;
@@ -443,7 +444,8 @@ double autotune_schedule(Geometry& geo, SideStream& side, cudaStream_t stream, i
       for (int si = 0; si < nsym; ++si)
         for (long w : ws)
           for (int ci = 0; ci < nch; ++ci) {
-            geo.sym_enabled  = nsym == 2 ? si == 0 : geo.sym_enabled;
+            geo.sym_enabled  = nsym == 3 ? si < 2 : geo.sym_enabled;
+            geo.sym_pack     = nsym == 3 ? (si == 1 ? 2 : 1) : geo.sym_pack;
             geo.multi_tile   = ntile == 3 ? tiles[ti] : geo.multi_tile;
             geo.multi_copies = nrc == 2 ? (ri == 0 ? 8 : 4) : geo.multi_copies;
             geo.item_pairs   = w;
@@ -453,9 +455,10 @@ double autotune_schedule(Geometry& geo, SideStream& side, cudaStream_t stream, i
             const double ms = time_applies();
             if (ms < best)
               best = ms, best_w = w, best_c = chs[ci], best_s = geo.sym_enabled,
-              best_t = geo.multi_tile, best_r = geo.multi_copies;
+              best_k = geo.sym_pack, best_t = geo.multi_tile, best_r = geo.multi_copies;
           }
   geo.sym_enabled  = best_s;
+  geo.sym_pack     = best_k;
   geo.multi_tile   = best_t;
   geo.multi_copies = best_r;
   geo.item_pairs  = best_w;
@@ -485,8 +488,9 @@ double System::autotune(int reps) {
         autotune_schedule(geo, side, stream, reps, [&] { apply32(p32.p, Ap32.p, false); });
   // the inexact operators' lists share the leaves: the same near-field form
   for (int k = 0; k < n_inexact; ++k)
-    if (geo_x[k].sym_enabled != geo.sym_enabled) {
+    if (geo_x[k].sym_enabled != geo.sym_enabled || geo_x[k].sym_pack != geo.sym_pack) {
       geo_x[k].sym_enabled = geo.sym_enabled;
+      geo_x[k].sym_pack    = geo.sym_pack;
       geo_x[k].make_schedules();
       geo_x[k].upload_schedules(stream);
     }
@@ -494,7 +498,42 @@ double System::autotune(int reps) {
   for (auto& row : inner_exec)
     for (auto& e : row)
       if (e) cudaGraphExecDestroy(e), e = nullptr;
+  size_work_buffers();
   return best;
+}
+
+// One FP32 apply with each operator (outside any capture), which gives the
+// work buffers the sizes of the current schedules before the inner loops are
+// captured again.
+void System::size_work_buffers() {
+  for (int lev = -1; lev < n_inexact; ++lev) {
+    apply_level = lev;
+    try {
+      apply32(p32.p, Ap32.p, false);
+    } catch (...) {
+      apply_level = -1;
+      throw;
+    }
+  }
+  apply_level = -1;
+  CG_CUDA(cudaStreamSynchronize(stream));
+}
+
+void System::set_schedule(int near_form, long item_pairs, int m2l_chunk) {
+  CG_CUDA(cudaSetDevice(device));
+  auto set = [&](Geometry& g) {
+    if (near_form >= 0) g.sym_enabled = near_form > 0, g.sym_pack = near_form > 0 ? near_form : 1;
+    if (item_pairs > 0) g.item_pairs = item_pairs;
+    if (m2l_chunk > 0) g.m2l_chunk = m2l_chunk;
+    g.make_schedules();
+    g.upload_schedules(stream);
+  };
+  set(geo);
+  for (int k = 0; k < n_inexact; ++k) set(geo_x[k]);
+  for (auto& row : inner_exec)
+    for (auto& e : row)
+      if (e) cudaGraphExecDestroy(e), e = nullptr;
+  size_work_buffers();
 }
 
 ReduceSlots System::slots(int k) const { return ReduceSlots{partials.p, ticket.p, scal.p + k}; }
@@ -722,6 +761,7 @@ bool System::inner_graph_ready(int nb, int nb3, int level) {
         const long long c0 = launch_counter();
         apply_level        = l - 1;
         try {
+          CaptureScope cs;
           inner_iteration_fp32(nb, nb3);
           k_while_running<<<1, 1, 0, stream>>>(h, flags.p);
           CG_LAUNCH();

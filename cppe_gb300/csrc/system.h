@@ -114,6 +114,11 @@ struct System {
   // Times the FP32 apply for a few near-field work-item sizes and M2L chunk
   // sizes and keeps the fastest schedule; returns its apply time (ms).
   double autotune(int reps);
+  // Sets the schedule directly: FP32 near-field form (0 per target leaf, 1 or
+  // 2 packed source pairs a lane of the symmetric kernel; -1 keeps it), the
+  // near-field work-item size in pairs and the M2L chunk (<= 0 keep them).
+  void set_schedule(int near_form, long item_pairs, int m2l_chunk);
+  void size_work_buffers();
   // inner FP32 PCG loop of the mixed solver (graph-launched when possible)
   void inner_iteration_fp32(int nb, int nb3);
   void run_inner_fp32(int nb, int nb3);

@@ -304,10 +304,19 @@ int cppe_gpu_kernel_timings(cppe_gpu_system* sys, int precision, int reps, doubl
  * stream scheduling differ. */
 int cppe_gpu_autotune(cppe_gpu_system* sys, int reps, double* best_ms);
 /* The schedule in use (no counterpart in the reference): whether the FP32
- * near field evaluates each leaf pair once for both directions (1) or per
- * target leaf (0), its number of work items, and the sources per M2L warp. */
+ * near field evaluates each leaf pair once for both directions (1: two
+ * sources a lane, 2: four sources a lane) or per target leaf (0), its number
+ * of work items, and the sources per M2L warp. */
 int cppe_gpu_schedule_info(cppe_gpu_system* sys, int* symmetric_near, long* near_items,
                            int* m2l_chunk);
+/* Sets the schedule directly (no counterpart in the reference), e.g. one that
+ * cppe_gpu_autotune chose earlier for the same system: near_form 0 (per
+ * target leaf), 1 or 2 (each leaf pair once, two or four sources a lane; the
+ * symmetric form applies to single systems with dipole sources), -1 keeps
+ * it; item_pairs (>= 1024) and m2l_chunk (32, 64 or 128) keep theirs when
+ * <= 0.  The operator is unchanged. */
+int cppe_gpu_set_schedule(cppe_gpu_system* sys, int near_form, long item_pairs,
+                          int m2l_chunk);
 /* Measured FMA throughput of the device in TFLOP/s (2 FLOP per FMA), FP32 or FP64. */
 int cppe_gpu_fma_peak(int device, int fp64, double* tflops);
 

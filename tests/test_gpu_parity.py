@@ -217,6 +217,31 @@ def test_autotune_keeps_the_operator(gpu):
     assert np.linalg.norm(rhs - s.apply(mu)) < 1e-8
 
 
+@pytest.mark.parametrize("fmm", [False, True])
+def test_near_field_forms_give_the_operator(gpu, fmm):
+    """The FP32 near field per target leaf and in both symmetric forms (two
+    and four sources a lane), at two work-item sizes: the same operator to
+    FP32 accuracy, and the mixed solve meets the threshold with each."""
+    from cppe_gb300 import synthetic
+    b = synthetic.water_box(1700, seed=35)
+    s = cabi.System(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, precision=cabi.MIXED,
+                    summation=cabi.FMM if fmm else cabi.DIRECT, damp=True)
+    v = np.random.default_rng(8).normal(0, 0.1, size=3 * b.n)
+    a64 = s.apply(v)
+    scale = np.abs(a64).max()
+    rhs = b.external_field()
+    for form in (0, 1, 2):
+        for pairs in (4096, 65536):
+            s.set_schedule(form, pairs)
+            sched = s.schedule()
+            assert sched["sym_pack"] == form or (form > 0 and not sched["symmetric_near"])
+            np.testing.assert_allclose(s.apply(v, fp32=True), a64, rtol=0, atol=2e-6 * scale,
+                                       err_msg=f"form {form}, {pairs} pairs")
+        mu, _, _, _ = s.solve(rhs)
+        assert np.linalg.norm(rhs - s.apply(mu)) < 1e-8, f"form {form}"
+    s.close()
+
+
 def test_fmm_solve_matches_oracle(gpu, port):
     from cppe_gb300 import synthetic
     b = synthetic.water_box(1500, seed=4)
