@@ -1424,8 +1424,12 @@ __global__ void __launch_bounds__(P2P_BLOCK)
           float2 FX[R], FY[R], FZ[R];
 #pragma unroll
           for (int r = 0; r < R; ++r) FX[r] = FY[r] = FZ[r] = f2(0.f);
-          auto sweep = [&](auto damped) {
-            constexpr bool D = decltype(damped)::value;
+          // every copy live: the copies' updates run unguarded, so that
+          // their eight independent chains interleave
+          const bool all_live = nr == R && live == (R == 32 ? ~0u : (1u << R) - 1u);
+          auto sweep = [&](auto damped, auto all) {
+            constexpr bool D  = decltype(damped)::value;
+            constexpr bool AL = decltype(all)::value;
 #pragma unroll 1
             for (int jj = g; jj < npairs; jj += S) {
               const float4 xy = s_xy[jj], zs = s_zs[jj];
@@ -1462,7 +1466,7 @@ __global__ void __launch_bounds__(P2P_BLOCK)
               }
 #pragma unroll
               for (int r = 0; r < R; ++r) {
-                if ((live >> r) & 1u) {
+                if (AL || ((live >> r) & 1u)) {
                   const float4 mxy = s_mxy[jj * R + r];
                   const float2 mz  = s_mz[jj * R + r];
                   const float2 mx = make_float2(mxy.x, mxy.y), my = make_float2(mxy.z, mxy.w);
@@ -1475,10 +1479,17 @@ __global__ void __launch_bounds__(P2P_BLOCK)
               }
             }
           };
-          if (DAMP && ph == 0)
-            sweep(std::true_type{});
-          else
-            sweep(std::false_type{});
+          if (all_live) {
+            if (DAMP && ph == 0)
+              sweep(std::true_type{}, std::true_type{});
+            else
+              sweep(std::false_type{}, std::true_type{});
+          } else {
+            if (DAMP && ph == 0)
+              sweep(std::true_type{}, std::false_type{});
+            else
+              sweep(std::false_type{}, std::false_type{});
+          }
 #pragma unroll
           for (int r = 0; r < R; ++r)
             acc[r].add(FX[r].x + FX[r].y, FY[r].x + FY[r].y, FZ[r].x + FZ[r].y);
@@ -1829,8 +1840,10 @@ __global__ void __launch_bounds__(P2P_BLOCK)
         }
         __syncthreads();
         if (active) {
-          auto sweep = [&](auto mode) {
-            constexpr int MD = decltype(mode)::value;
+          // all R copies in this pass: their updates run unguarded
+          auto sweep = [&](auto mode, auto all) {
+            constexpr int MD  = decltype(mode)::value;
+            constexpr bool AL = decltype(all)::value;
 #pragma unroll 1
             for (int jj = g; jj < npairs; jj += S) {
               const float4 A0 = s_g[0][jj], B0 = s_g[1][jj], C0 = s_g[2][jj], D0 = s_g[3][jj];
@@ -1843,7 +1856,7 @@ __global__ void __launch_bounds__(P2P_BLOCK)
                                         G2);
 #pragma unroll
               for (int r = 0; r < R; ++r) {
-                if (r < nr) {
+                if (AL || r < nr) {
                   const float4 E0 = s_m[0][jj * R + r], F0 = s_m[1][jj * R + r],
                                G0 = s_m[2][jj * R + r];
                   const dd2 mx = {make_float2(E0.x, E0.y), make_float2(F0.z, F0.w)};
@@ -1859,10 +1872,17 @@ __global__ void __launch_bounds__(P2P_BLOCK)
               }
             }
           };
-          if (!DAMP || ph == 0)
-            sweep(std::integral_constant<int, 0>{});
-          else
-            sweep(std::integral_constant<int, 1>{});
+          if (nr == R) {
+            if (!DAMP || ph == 0)
+              sweep(std::integral_constant<int, 0>{}, std::true_type{});
+            else
+              sweep(std::integral_constant<int, 1>{}, std::true_type{});
+          } else {
+            if (!DAMP || ph == 0)
+              sweep(std::integral_constant<int, 0>{}, std::false_type{});
+            else
+              sweep(std::integral_constant<int, 1>{}, std::false_type{});
+          }
         }
         __syncthreads();
       }
