@@ -1534,6 +1534,55 @@ __global__ void __launch_bounds__(P2P_BLOCK)
 // FP32 deficit (< 5e-7 there) elsewhere; with MODE 1 (every v >= 20) from
 // the FP32 deficit only.
 // ---------------------------------------------------------------------------
+// Thole factors of pairs whose v = a R is at least 20 (every pair of the
+// partners with v >= 27 for the whole leaf pair): 1 - f_E = (1 + v + v^2/2)
+// e^-v <= 4.6e-7 and 1 - f_T = 1 - f_E + v^3/6 e^-v, so G1 f_E = G1 - G1 (1 -
+// f_E) with the correction formed in FP32 from FP32 v (its rounding, ~1e-7 of
+// a term below 4.6e-7 of G1, stays below 1e-13 of G1) and added to the low
+// part; pairs with v >= 50 or without a damping partner (a = 0) keep G1, G2.
+__device__ __forceinline__ void dd2_damp_far(const float2& a, const float2& v, dd2& G1,
+                                             dd2& G2) {
+  const bool dx = a.x > 0.f && v.x < 50.f, dy = a.y > 0.f && v.y < 50.f;
+  const float2 e = make_float2(expf(-v.x), expf(-v.y));
+  const float2 u = pmul(pfma(v, pfma(v, p2(0.5f), p2(1.f)), p2(1.f)), e);
+  const float2 w = pmul(pmul(pmul(pmul(v, v), v), p2(1.f / 6.f)), e);
+  G1.l = psel(dx, dy, pfma(pneg(G1.h), u, G1.l), G1.l);
+  G2.l = psel(dx, dy, pfma(pneg(G2.h), padd(u, w), G2.l), G2.l);
+}
+
+// The Thole factors of a packed pair, in place on G1 = -R^-3 and
+// G2 = 3 R^-5: v in FP32 chooses the form, the double-float exponential
+// where v < 20 (MODE 0 only) and the FP32 correction of dd2_damp_far
+// elsewhere.
+template <int MODE>
+__device__ __forceinline__ void dd2_thole(const dd2& ai, const dd2& s, const dd2& r2,
+                                          const dd2& ir, const float* eh, const float* el,
+                                          dd2& G1, dd2& G2) {
+  const dd2 zero = {p2(0.f), p2(0.f)};
+  const float2 a32 = pmul(ai.h, s.h);
+  const float2 v32 = pmul(a32, pmul(r2.h, ir.h));
+  const bool sx = MODE == 0 && v32.x < 20.f, sy = MODE == 0 && v32.y < 20.f;
+  dd2 G1n = G1, G2n = G2;
+  if (sx || sy) {
+    const dd2 a   = dd2_mul(ai, s);
+    const dd2 v   = dd2_mul(a, dd2_mul(r2, ir));
+    const dd2 vc  = dd2_sel(sx, sy, v, zero);  // in range of the exponential's table
+    const dd2 e   = dd2_exp_neg(vc, eh, el);
+    const dd2 v2  = dd2_sqr(vc);
+    const dd2 u   = dd2_add(dd2_two_sum(p2(1.f), vc.h),
+                            {pmul(p2(0.5f), v2.h), pfma(p2(0.5f), v2.l, vc.l)});
+    const dd2 w   = dd2_mul(dd2_mul(v2, vc), {p2(1.f / 6.f), p2(DD_SIXTH_LO)});
+    const dd2 fEd = dd2_add(dd2{p2(1.f), p2(0.f)}, dd2_neg(dd2_mul(u, e)));
+    const dd2 fTd = dd2_add(fEd, dd2_neg(dd2_mul(w, e)));
+    const bool nx = sx && a.h.x > 0.f, ny = sy && a.h.y > 0.f;
+    G1n = dd2_sel(nx, ny, dd2_mul(G1, fEd), G1);
+    G2n = dd2_sel(nx, ny, dd2_mul(G2, fTd), G2);
+  }
+  dd2_damp_far(a32, v32, G1, G2);
+  G1 = dd2_sel(sx, sy, G1n, G1);
+  G2 = dd2_sel(sx, sy, G2n, G2);
+}
+
 struct DDSrc2 {
   dd2 x, y, z, s, mx, my, mz;
 };
@@ -1552,32 +1601,7 @@ __device__ __forceinline__ void dd2_pair_m1(const dd2& tx, const dd2& ty, const 
   const dd2 ir3  = dd2_mul(ir2, ir);
   dd2 G1         = dd2_neg(ir3);
   dd2 G2         = dd2_mul_f(dd2_mul(ir3, ir2), p2(3.f));
-  if (DAMP && MODE < 2) {
-    const dd2 a  = dd2_mul(ai, q.s);
-    const dd2 v  = dd2_mul(a, dd2_mul(r2, ir));
-    const bool dx = a.h.x > 0.f && v.h.x < 50.f, dy = a.h.y > 0.f && v.h.y < 50.f;
-    // FP32 deficit (used where v >= 20)
-    const float2 e32 = make_float2(expf(-v.h.x), expf(-v.h.y));
-    const float2 u32 = pmul(pfma(v.h, pfma(v.h, p2(0.5f), p2(1.f)), p2(1.f)), e32);
-    const float2 w32 = pmul(pmul(pmul(pmul(v.h, v.h), v.h), p2(1.f / 6.f)), e32);
-    dd2 fE           = dd2_fast_two_sum(p2(1.f), pneg(u32));
-    dd2 fT           = dd2_fast_two_sum(p2(1.f), pneg(padd(u32, w32)));
-    const bool sx = MODE == 0 && v.h.x < 20.f, sy = MODE == 0 && v.h.y < 20.f;
-    if (sx || sy) {
-      const dd2 vc  = dd2_sel(sx, sy, v, zero);  // in range of the exponential's table
-      const dd2 e   = dd2_exp_neg(vc, eh, el);
-      const dd2 v2  = dd2_sqr(vc);
-      const dd2 u   = dd2_add(dd2_two_sum(p2(1.f), vc.h),
-                              {pmul(p2(0.5f), v2.h), pfma(p2(0.5f), v2.l, vc.l)});
-      const dd2 w   = dd2_mul(dd2_mul(v2, vc), {p2(1.f / 6.f), p2(DD_SIXTH_LO)});
-      const dd2 fEd = dd2_add(dd2{p2(1.f), p2(0.f)}, dd2_neg(dd2_mul(u, e)));
-      const dd2 fTd = dd2_add(fEd, dd2_neg(dd2_mul(w, e)));
-      fE = dd2_sel(sx, sy, fEd, fE);
-      fT = dd2_sel(sx, sy, fTd, fT);
-    }
-    G1 = dd2_sel(dx, dy, dd2_mul(G1, fE), G1);
-    G2 = dd2_sel(dx, dy, dd2_mul(G2, fT), G2);
-  }
+  if (DAMP && MODE < 2) dd2_thole<MODE>(ai, q.s, r2, ir, eh, el, G1, G2);
   const dd2 mr = dd2_add(dd2_add_lazy(dd2_mul(q.mx, x), dd2_mul(q.my, y)), dd2_mul(q.mz, z));
   const dd2 sg = dd2_mul(mr, G2);
   f[0] = dd2_add_lazy(f[0], dd2_neg(dd2_add_lazy(dd2_mul(q.mx, G1), dd2_mul(sg, x))));
@@ -1730,31 +1754,7 @@ __device__ __forceinline__ void dd2_pair_tensor(const dd2& tx, const dd2& ty, co
   const dd2 ir3  = dd2_mul(ir2, ir);
   G1 = dd2_neg(ir3);
   G2 = dd2_mul_f(dd2_mul(ir3, ir2), p2(3.f));
-  if (DAMP && MODE < 2) {
-    const dd2 a   = dd2_mul(ai, qs);
-    const dd2 v   = dd2_mul(a, dd2_mul(r2, ir));
-    const bool dx = a.h.x > 0.f && v.h.x < 50.f, dy = a.h.y > 0.f && v.h.y < 50.f;
-    const float2 e32 = make_float2(expf(-v.h.x), expf(-v.h.y));
-    const float2 u32 = pmul(pfma(v.h, pfma(v.h, p2(0.5f), p2(1.f)), p2(1.f)), e32);
-    const float2 w32 = pmul(pmul(pmul(pmul(v.h, v.h), v.h), p2(1.f / 6.f)), e32);
-    dd2 fE = dd2_fast_two_sum(p2(1.f), pneg(u32));
-    dd2 fT = dd2_fast_two_sum(p2(1.f), pneg(padd(u32, w32)));
-    const bool sx = MODE == 0 && v.h.x < 20.f, sy = MODE == 0 && v.h.y < 20.f;
-    if (sx || sy) {
-      const dd2 vc  = dd2_sel(sx, sy, v, zero);
-      const dd2 e   = dd2_exp_neg(vc, eh, el);
-      const dd2 v2  = dd2_sqr(vc);
-      const dd2 u   = dd2_add(dd2_two_sum(p2(1.f), vc.h),
-                              {pmul(p2(0.5f), v2.h), pfma(p2(0.5f), v2.l, vc.l)});
-      const dd2 w   = dd2_mul(dd2_mul(v2, vc), {p2(1.f / 6.f), p2(DD_SIXTH_LO)});
-      const dd2 fEd = dd2_add(dd2{p2(1.f), p2(0.f)}, dd2_neg(dd2_mul(u, e)));
-      const dd2 fTd = dd2_add(fEd, dd2_neg(dd2_mul(w, e)));
-      fE = dd2_sel(sx, sy, fEd, fE);
-      fT = dd2_sel(sx, sy, fTd, fT);
-    }
-    G1 = dd2_sel(dx, dy, dd2_mul(G1, fE), G1);
-    G2 = dd2_sel(dx, dy, dd2_mul(G2, fT), G2);
-  }
+  if (DAMP && MODE < 2) dd2_thole<MODE>(ai, qs, r2, ir, eh, el, G1, G2);
 }
 
 constexpr int P2PM_DD_PAIRS = 80;  // staged source pairs per tile (160 sources)
