@@ -13,7 +13,9 @@ reference engine.
   4,000 sites, FMM order 5 above), two right-hand sides each, solved as one
   batch in FP64 and in mixed precision, against full oracle solves.
 * 1,000,002 sites, FMM order 6: the mixed solve with the shipped model, by the
-  oracle's residual rule and against the reference summary.
+  oracle's residual rule and against the reference summary; and, at that
+  size, bitwise-repeatable solves and FP32 applies and the double-float
+  operator's linearity (5e-12 in norm).
 
 The reference summaries (tests/golden/config_solutions.json) hold the
 reference engine's solutions of the same seeded boxes (energy, mu and F at 64
@@ -178,5 +180,15 @@ def test_config_1m_mixed_learned_solve(gpu, port):
     assert np.linalg.norm(rhs - s.apply(mu)) < 1e-8  # the library's FP64 operator
     assert oracle_residual(port, b, rhs, mu, 6) < 1e-8  # the oracle's
     check_against_summary(g, rhs, mu, 5e-8)
+    # size-independent properties at full size: a repeated solve gives the
+    # same bits (no atomics in any reduction), and the double-float operator
+    # is linear to its accuracy
+    mu2, _, _, _ = s.solve(rhs)
+    assert np.array_equal(mu, mu2)
+    v = np.random.default_rng(13).normal(size=3 * b.n)
+    a1, a2 = s.apply(mu, dd=True), s.apply(v, dd=True)
+    a12 = s.apply(mu + 0.5 * v, dd=True)
+    assert np.linalg.norm(a12 - (a1 + 0.5 * a2)) < 5e-12 * np.linalg.norm(a12)
+    assert np.array_equal(s.apply(v, fp32=True), s.apply(v, fp32=True))
     s.set_model(None)
     s.close()
