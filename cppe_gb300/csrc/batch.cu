@@ -16,6 +16,8 @@
 namespace cg {
 
 constexpr int BB = 256;
+// opening angles of the inexact inner operators (as the single-system solver's)
+constexpr double BATCH_INEXACT_THETA[BatchSystem::NINEXACT] = {0.6, 0.8};
 
 // ---------------------------------------------------------------------------
 // Geometry concatenation
@@ -318,6 +320,55 @@ __global__ void k_bguess(int n, const double* __restrict__ a6, const double* __r
 // ---------------------------------------------------------------------------
 // BatchSystem
 // ---------------------------------------------------------------------------
+// Per operator level L (0: the operator, 1 + k: inexact operator k), the
+// segments its pass leaves out: finished ones and those at another level.
+__global__ void k_blevel_masks(int nseg, int nlev, const int* __restrict__ done,
+                               const int* __restrict__ level, int* __restrict__ m0,
+                               int* __restrict__ m1, int* __restrict__ m2) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= nseg) return;
+  const int d = done[g] != 0, l = level[g];
+  m0[g] = d || l != 0;
+  if (nlev > 1) m1[g] = d || l != 1;
+  if (nlev > 2) m2[g] = d || l != 2;
+}
+
+// Hand-over of a snapshot's running segments (its right-hand sides) to the
+// next inexact operator once every one of them is below that operator's
+// hand-over point (sw <= 0: never).  The right-hand sides of a snapshot move
+// together, so that the near-field pass keeps serving them all from one
+// pair tensor.  The residual at the hand-over is kept for the error bound of
+// the residual formed from the recursion.
+__global__ void k_blevel_update(int nsys, int nrhs, int nx, const double* __restrict__ rnorm,
+                                const int* __restrict__ done, int* __restrict__ level,
+                                const double* __restrict__ sw0, const double* __restrict__ sw1,
+                                double* __restrict__ rsw0, double* __restrict__ rsw1) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsys) return;
+  const int g0 = s * nrhs;
+  bool any = false, all0 = nx > 0, all1 = nx > 1;
+  int l = 0;
+  for (int r = 0; r < nrhs; ++r) {
+    const int g = g0 + r;
+    if (done[g]) continue;
+    any = true;
+    l   = level[g];  // the same for every running right-hand side
+    const double rn = rnorm[g];
+    all0 = all0 && rn < sw0[g];
+    all1 = all1 && rn < sw1[g];
+  }
+  if (!any) return;
+  const int nl = l == 0 && all0 ? (all1 ? 2 : 1) : (l == 1 && all1 ? 2 : l);
+  if (nl == l) return;
+  for (int r = 0; r < nrhs; ++r) {
+    const int g = g0 + r;
+    if (done[g]) continue;
+    if (l == 0) rsw0[g] = rnorm[g];
+    if (nl == 2) rsw1[g] = rnorm[g];
+    level[g] = nl;
+  }
+}
+
 BatchSystem::~BatchSystem() {
   if (stream) {
     cudaSetDevice(device);
@@ -348,6 +399,16 @@ void BatchSystem::init(int nsys, const int* site_offset, const double* xyz, cons
     fail(CPPE_GPU_INVALID_ARG, "tree_expansion_order must be in [2, 7]");
   std::vector<Geometry> parts(nsys);
   std::vector<const Geometry*> pp;
+  // the inexact inner operators' parts (FMM snapshots; a direct snapshot
+  // serves every level as it is)
+  const bool want_x = o.precision == CPPE_GPU_MIXED;
+  std::vector<Geometry> parts_x[NINEXACT];
+  bool x_ok[NINEXACT];
+  for (int k = 0; k < NINEXACT; ++k) {
+    x_ok[k] = want_x && o.theta < BATCH_INEXACT_THETA[k];
+    if (x_ok[k]) parts_x[k].resize(nsys);
+  }
+  std::vector<char> sys_fmm(nsys, 0);
   std::vector<double> a_inv, a_dir;
   sys_sites.assign(site_offset, site_offset + nsys + 1);
   for (int s = 0; s < nsys; ++s) {
@@ -366,13 +427,34 @@ void BatchSystem::init(int nsys, const int* site_offset, const double* xyz, cons
       ei.assign(excl_idx + excl_ptr[o0], excl_idx + excl_ptr[o0 + ns]);
     }
     const bool fmm = ns >= direct_below;
+    sys_fmm[s]       = fmm;
     parts[s].damping = o.damp ? o.damping_factor : 0.0;
     parts[s].prepare(ns, xyz + 3 * (size_t)o0, sd.data(), excl_ptr ? ep.data() : nullptr,
                      ei.empty() ? nullptr : ei.data(), fmm, o.tree_ncrit, o.theta);
     pp.push_back(&parts[s]);
+    for (int k = 0; k < NINEXACT; ++k) {
+      if (!x_ok[k] || !fmm) continue;
+      Geometry& gx = parts_x[k][s];
+      gx.damping   = parts[s].damping;
+      gx.prepare(ns, xyz + 3 * (size_t)o0, sd.data(), excl_ptr ? ep.data() : nullptr,
+                 ei.empty() ? nullptr : ei.data(), true, o.tree_ncrit, BATCH_INEXACT_THETA[k]);
+      // the opening angle changes the lists, not the tree: same site order
+      if (gx.layout.perm != parts[s].layout.perm) x_ok[k] = false;
+    }
   }
   Geometry::combine(pp, nrhs, geo);
   geo.upload(stream);
+  const bool any_fmm = std::any_of(sys_fmm.begin(), sys_fmm.end(), [](char f) { return f; });
+  n_inexact = 0;
+  for (int k = 0; k < NINEXACT && any_fmm && x_ok[k]; ++k) {
+    std::vector<const Geometry*> ppx(nsys);
+    for (int s = 0; s < nsys; ++s) ppx[s] = sys_fmm[s] ? &parts_x[k][s] : &parts[s];
+    Geometry::combine(ppx, nrhs, geo_x[k]);
+    if (geo_x[k].layout.perm != geo.layout.perm) break;
+    geo_x[k].upload(stream);
+    n_inexact = k + 1;
+  }
+  for (auto& v : parts_x) v.clear();
   if (geo.fmm) {
     ops = std::make_unique<DeviceOps>();
     ops->build(1, o.tree_expansion_order, stream);
@@ -425,6 +507,11 @@ void BatchSystem::init(int nsys, const int* site_offset, const double* xyz, cons
   iters.alloc(nseg);
   active.alloc(1);
   CG_CUDA(cudaMallocHost(&h_active, sizeof(int)));
+  if (n_inexact > 0) {
+    std::vector<char> seg_fmm(nseg);
+    for (int g = 0; g < nseg; ++g) seg_fmm[g] = sys_fmm[g / nrhs];
+    measure_inexact(seg_start_h, seg_fmm);
+  }
   CG_CUDA(cudaStreamSynchronize(stream));
 }
 
@@ -439,6 +526,92 @@ void BatchSystem::apply_seg(const T* in, T* out, int near_mode, bool skip_done) 
                 skip_done ? done.p : nullptr);
   k_seg_sum<<<nseg, BB, 0, stream>>>(seg_start.p, site_a.p, nullptr, seg_pap.p, nullptr);
   CG_LAUNCH();
+}
+
+void BatchSystem::apply_level32(int k, const float* in, float* out, const int* mask) {
+  ReduceSlots rs{nullptr, nullptr, nullptr};
+  rs.site_values = site_a.p;
+  eval_field<float>(geo_x[k], ops.get(), w32x[k], 1, in, opt.damp != 0, opt.damping_factor,
+                    FINISH_APPLY, ainv32.p, out, nullptr, 1.0, &rs, stream, nullptr, NEAR_FP64,
+                    &side, mask);
+}
+
+// The iteration's FP32 operator: each running segment with the operator of
+// its level (the passes of the other operators skip it), then the segments'
+// p.Ap sums.
+void BatchSystem::apply_levels32(const float* in, float* out) {
+  const int gb = (nseg + 127) / 128;
+  k_blevel_masks<<<gb, 128, 0, stream>>>(nseg, 1 + n_inexact, done.p, seg_level.p,
+                                         lvl_mask[0].p, lvl_mask[1].p, lvl_mask[2].p);
+  CG_LAUNCH();
+  ReduceSlots rs{nullptr, nullptr, nullptr};
+  rs.site_values = site_a.p;
+  eval_field<float>(geo, ops.get(), w32, 1, in, opt.damp != 0, opt.damping_factor, FINISH_APPLY,
+                    ainv32.p, out, nullptr, 1.0, &rs, stream, nullptr, NEAR_FP64, &side,
+                    lvl_mask[0].p);
+  for (int k = 0; k < n_inexact; ++k) apply_level32(k, in, out, lvl_mask[1 + k].p);
+  k_seg_sum<<<nseg, BB, 0, stream>>>(seg_start.p, site_a.p, nullptr, seg_pap.p, nullptr);
+  CG_LAUNCH();
+}
+
+// Each segment's relative difference between the operator (double-float)
+// and each inexact FP32 operator on a random vector and on a smooth one (the
+// response to a uniform field), times 3 as the bound delta used for the
+// hand-over points; a segment whose difference reaches 1e-2, or a direct
+// snapshot's segment, keeps the operator throughout.
+void BatchSystem::measure_inexact(const std::vector<int>& seg_start_h,
+                                  const std::vector<char>& seg_fmm) {
+  const size_t n3 = 3 * (size_t)n;
+  seg_level.alloc(nseg);
+  for (int k = 0; k <= NINEXACT; ++k) lvl_mask[k].alloc(nseg);
+  for (int k = 0; k < NINEXACT; ++k) seg_sw[k].alloc(nseg), seg_rsw[k].alloc(nseg);
+  std::vector<double> vin[2] = {std::vector<double>(n3), std::vector<double>(n3)};
+  unsigned long long st = 0x9e3779b97f4a7c15ull;
+  for (size_t k = 0; k < n3; ++k) {
+    st ^= st << 13, st ^= st >> 7, st ^= st << 17;
+    vin[0][k] = (double)(st >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+    vin[1][k] = (k % 3 == 0) ? 1.0 : (k % 3 == 1 ? 0.5 : 0.25);
+  }
+  std::vector<double> a64(n3), ax(n3);
+  std::vector<float> in32(n3), out32(n3);
+  std::vector<double> worst[NINEXACT];
+  for (int k = 0; k < n_inexact; ++k) worst[k].assign(nseg, 0.0);
+  auto seg_rel = [&](const std::vector<double>& ref, const std::vector<double>& got, int g) {
+    double num = 0.0, den = 0.0;
+    for (size_t q = 3 * (size_t)seg_start_h[g]; q < 3 * (size_t)seg_start_h[g + 1]; ++q) {
+      const double d = got[q] - ref[q];
+      num += d * d, den += ref[q] * ref[q];
+    }
+    return den > 0.0 ? std::sqrt(num / den) : 0.0;
+  };
+  for (int trial = 0; trial < 2; ++trial) {
+    CG_CUDA(cudaMemcpyAsync(x.p, vin[trial].data(), n3 * sizeof(double), cudaMemcpyHostToDevice,
+                            stream));
+    apply_seg<double>(x.p, Ap.p, NEAR_DD);
+    CG_CUDA(cudaMemcpyAsync(a64.data(), Ap.p, n3 * sizeof(double), cudaMemcpyDeviceToHost,
+                            stream));
+    for (size_t q = 0; q < n3; ++q) in32[q] = (float)vin[trial][q];
+    CG_CUDA(cudaMemcpyAsync(p32.p, in32.data(), n3 * sizeof(float), cudaMemcpyHostToDevice,
+                            stream));
+    for (int k = 0; k < n_inexact; ++k) {
+      apply_level32(k, p32.p, Ap32.p, nullptr);
+      CG_CUDA(cudaMemcpyAsync(out32.data(), Ap32.p, n3 * sizeof(float), cudaMemcpyDeviceToHost,
+                              stream));
+      CG_CUDA(cudaStreamSynchronize(stream));
+      for (size_t q = 0; q < n3; ++q) ax[q] = out32[q];
+      for (int g = 0; g < nseg; ++g) worst[k][g] = std::max(worst[k][g], seg_rel(a64, ax, g));
+    }
+  }
+  for (int k = 0; k < NINEXACT; ++k) h_delta[k].assign(nseg, 0.0);
+  for (int g = 0; g < nseg; ++g) {
+    if (!seg_fmm[g]) continue;
+    for (int k = 0; k < n_inexact; ++k) {
+      const double d = 3.0 * worst[k][g];
+      if (!(worst[k][g] > 0.0 && d < 1e-2)) break;  // this level and the ones after it off
+      h_delta[k][g] = d;
+    }
+  }
+  CG_CUDA(cudaStreamSynchronize(stream));
 }
 
 // Sets the first condition of the batched loop: some segment still running.
@@ -468,8 +641,14 @@ void BatchSystem::pcg_iteration(T* xv, T* rv, T* zv, T* pv, T* Apv, const T* a6,
                                 bool graph) {
   const int nb = (n + BB - 1) / BB, gb = (nseg + 127) / 128;
   // the near field of finished segments is skipped: their p, Ap and scalars
-  // are no longer read
-  apply_seg<T>(pv, Apv, NEAR_FP64, true);
+  // are no longer read; in FP32 with inexact operators each segment takes
+  // the operator of its level
+  bool levels = false;
+  if constexpr (std::is_same<T, float>::value) levels = n_inexact > 0;
+  if constexpr (std::is_same<T, float>::value) {
+    if (levels) apply_levels32(pv, Apv);
+  }
+  if (!levels) apply_seg<T>(pv, Apv, NEAR_FP64, true);
   k_bcg_update<T><<<nb, BB, 0, stream>>>(n, site_seg.p, pv, Apv, a6, xv, rv, zv, seg_rz.p,
                                          seg_pap.p, done.p, site_a.p, site_b.p);
   CG_LAUNCH();
@@ -480,6 +659,13 @@ void BatchSystem::pcg_iteration(T* xv, T* rv, T* zv, T* pv, T* Apv, const T* a6,
                                          seg_rnorm.p, done.p, iters.p, seg_tol.p, maxiter,
                                          active.p);
   CG_LAUNCH();
+  if (levels) {
+    const int nsys = nseg / nrhs;
+    k_blevel_update<<<(nsys + 127) / 128, 128, 0, stream>>>(
+          nsys, nrhs, n_inexact, seg_rnorm.p, done.p, seg_level.p, seg_sw[0].p, seg_sw[1].p,
+          seg_rsw[0].p, seg_rsw[1].p);
+    CG_LAUNCH();
+  }
   k_bcg_dir<T><<<nb, BB, 0, stream>>>(n, site_seg.p, zv, pv, seg_beta.p, done.p);
   CG_LAUNCH();
 }
@@ -659,6 +845,8 @@ int BatchSystem::solve_device(const double* d_rhs, double* d_mu, int* iters_out)
     // the FP64 operator (as in System::solve_mixed, over the largest norm)
     constexpr double REC_ERR = 3e-6, CORR_ERR = 3e-7;
     double rerr = 0.0;
+    std::vector<double> swv[NINEXACT], rswv[NINEXACT];
+    for (int k = 0; k < NINEXACT; ++k) swv[k].assign(nseg, -1.0), rswv[k].assign(nseg, 0.0);
     for (int outer = 0; outer < 12; ++outer) {
       // inner tolerances; segments already below the threshold stay put
       for (int g = 0; g < nseg; ++g) tolv[g] = std::max(eta * rn[g], 0.5 * t);
@@ -677,20 +865,55 @@ int BatchSystem::solve_device(const double* d_rhs, double* d_mu, int* iters_out)
       }
       CG_CUDA(cudaMemcpyAsync(seg_tol.p, tolv.data(), nseg * sizeof(double),
                               cudaMemcpyHostToDevice, stream));
+      if (n_inexact > 0) {
+        // hand-over points of this inner solve, as System's k_inner_stage:
+        // in the first one where an inexact operator's effect, ~delta ||r||,
+        // stays below 0.15 of the target eta ||r0||; in later ones (whose
+        // residual is then formed from the recursion) where 1.5 delta ||r||
+        // stays below 0.04 t per operator
+        const int stage = outer == 0 ? 0 : 1;
+        for (int g = 0; g < nseg; ++g) {
+          auto sw = [&](double d) {
+            if (!(d > 0.0)) return -1.0;
+            return std::max(tolv[g], stage == 0 ? 0.15 * eta * rn[g] / d : 0.04 * t / (1.5 * d));
+          };
+          swv[0][g] = sw(h_delta[0][g]);
+          swv[1][g] = n_inexact > 1 && swv[0][g] > 0.0 ? std::min(swv[0][g], sw(h_delta[1][g]))
+                                                       : -1.0;
+        }
+        for (int k = 0; k < NINEXACT; ++k) {
+          CG_CUDA(cudaMemcpyAsync(seg_sw[k].p, swv[k].data(), nseg * sizeof(double),
+                                  cudaMemcpyHostToDevice, stream));
+          CG_CUDA(cudaMemsetAsync(seg_rsw[k].p, 0, nseg * sizeof(double), stream));
+        }
+        CG_CUDA(cudaMemsetAsync(seg_level.p, 0, nseg * sizeof(int), stream));
+      }
       k_bcg_init_seg<<<(nseg + 127) / 128, 128, 0, stream>>>(
             nseg, seg_rz.p, seg_rr.p, seg_rz.p, seg_rnorm.p, done.p, iters.p, seg_tol.p);
       CG_LAUNCH();
       run_pcg<float>(d32.p, r32.p, z32.p, p32.p, Ap32.p, alpha32.p, std::max(1, opt.maxiter));
       CG_CUDA(cudaMemcpyAsync(it_h.data(), iters.p, nseg * sizeof(int), cudaMemcpyDeviceToHost,
                               stream));
+      // the inexact operators' share of the recursion's error: 1.5 delta
+      // times the residual at each hand-over
+      double extra = 0.0;
+      if (n_inexact > 0) {
+        for (int k = 0; k < NINEXACT; ++k)
+          CG_CUDA(cudaMemcpyAsync(rswv[k].data(), seg_rsw[k].p, nseg * sizeof(double),
+                                  cudaMemcpyDeviceToHost, stream));
+        CG_CUDA(cudaStreamSynchronize(stream));
+        for (int g = 0; g < nseg; ++g)
+          extra = std::max(extra, 1.5 * (h_delta[0][g] * rswv[0][g] +
+                                         (n_inexact > 1 ? h_delta[1][g] * rswv[1][g] : 0.0)));
+      }
       const double rmax = *std::max_element(rn.begin(), rn.end());
-      if (exact && rerr + REC_ERR * rmax < 0.1 * t) {
+      if (exact && rerr + REC_ERR * rmax + extra < 0.1 * t) {
         // residual from the inner recursion (as System::solve_mixed)
         k_bres<<<nb, BB, 0, stream>>>(n, nullptr, nullptr, nullptr, r.p, site_b.p, r32.p);
         CG_LAUNCH();
         k_bacc<<<nb3, BB, 0, stream>>>(n3, x.p, d32.p);
         CG_LAUNCH();
-        rerr += REC_ERR * rmax;
+        rerr += REC_ERR * rmax + extra;
       } else if (!(exact && rerr + CORR_ERR * rmax < 0.1 * t)) {
         k_bacc<<<nb3, BB, 0, stream>>>(n3, x.p, d32.p);
         CG_LAUNCH();

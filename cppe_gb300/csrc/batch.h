@@ -28,6 +28,19 @@ struct BatchSystem {
   DBuf<double> seg_rz, seg_pap, seg_rr, seg_rznew, seg_beta, seg_rnorm, seg_tol;
   DBuf<int> done, iters, active;
   int* h_active = nullptr;
+  // Inexact inner operators of the mixed solver (FMM snapshots): the same
+  // segments at the single-system solver's opening angles 0.6 and 0.8, a
+  // per-segment level set on the device from the segment's residual, and
+  // each operator applied to the segments at its level only.
+  static constexpr int NINEXACT = 2;
+  int n_inexact = 0;
+  Geometry geo_x[NINEXACT];
+  FieldWork<float> w32x[NINEXACT];
+  std::vector<double> h_delta[NINEXACT];  // per segment: operator difference bound (0: off)
+  DBuf<double> seg_sw[NINEXACT];          // hand-over residuals of the running inner solve
+  DBuf<double> seg_rsw[NINEXACT];         // residual where the segment handed over (0: not)
+  DBuf<int> seg_level;                    // 0: the operator, 1 + k: inexact operator k
+  DBuf<int> lvl_mask[1 + NINEXACT];       // per operator: segment finished or at another level
   SolveStats stats;
   std::vector<double> last_rnorm;
 
@@ -49,6 +62,14 @@ struct BatchSystem {
   // segments flagged in `done` out (their output is then not meaningful)
   template <typename T>
   void apply_seg(const T* in, T* out, int near_mode = NEAR_FP64, bool skip_done = false);
+  // FP32 operator of inexact level k (0, 1) over the segments not in `mask`
+  // (every segment when null); with a segmented dot of in and out in site_a
+  void apply_level32(int k, const float* in, float* out, const int* mask);
+  // the iteration's FP32 apply: each segment with the operator of its level
+  void apply_levels32(const float* in, float* out);
+  // measures each segment's difference between the operator and the
+  // inexact ones (part of init, after the inexact geometries are built)
+  void measure_inexact(const std::vector<int>& seg_start_h, const std::vector<char>& seg_fmm);
   // PCG iterations over all segments until each has converged or reached
   // maxiter; returns the number of iterations run (operator applications)
   template <typename T>

@@ -2166,7 +2166,8 @@ template <typename T, int P>
 __global__ void __launch_bounds__(SHIFT_THREADS)
       k_m2m_tasks_fixed(TreeView tv, const int4* __restrict__ tasks, int ntask,
                         const int* __restrict__ task_leaf, CellPos<T> cp, const T* __restrict__ M,
-                        T* __restrict__ Mpart) {
+                        T* __restrict__ Mpart, const int* __restrict__ cell_seg,
+                        const int* __restrict__ seg_done) {
   constexpr int MS  = Shifts<P>::ms, MST = Shifts<P>::mst;
   constexpr int TPB = SHIFT_THREADS / M2M_TASK_LEAVES;  // tasks per block
   __shared__ T s_part[SHIFT_THREADS * (MS + 1)];
@@ -2175,7 +2176,9 @@ __global__ void __launch_bounds__(SHIFT_THREADS)
   T acc[MS];
 #pragma unroll
   for (int r = 0; r < MS; ++r) acc[r] = T(0);
-  if (task < ntask) {
+  // a batch's masked segment: its partials are not read
+  const bool live = task < ntask && !(seg_done && seg_done[cell_seg[tasks[task].x]]);
+  if (live) {
     const int4 tk = tasks[task];
     if (tk.y + sl < tk.z) {
       const int lc = tv.leaf_cell[task_leaf[tk.y + sl]];
@@ -2201,10 +2204,12 @@ __global__ void __launch_bounds__(SHIFT_THREADS)
 template <typename T, int P>
 __global__ void __launch_bounds__(SHIFT_THREADS)
       k_l2l_leaf_fixed(TreeView tv, CellPos<T> cp, const T* __restrict__ L,
-                       T* __restrict__ Lleaf) {
+                       T* __restrict__ Lleaf, const int* __restrict__ leaf_seg,
+                       const int* __restrict__ seg_done) {
   constexpr int LS = Shifts<P>::ls;
   const int leaf = blockIdx.x * SHIFT_THREADS + threadIdx.x;
   if (leaf >= tv.nleaves) return;
+  if (seg_done && seg_done[leaf_seg[leaf]]) return;  // a batch's masked segment
   const int lc = tv.leaf_cell[leaf];
   T acc[LS];
 #pragma unroll
@@ -2222,10 +2227,12 @@ __global__ void __launch_bounds__(SHIFT_THREADS)
 // M of every cell with upward tasks: the sum of its task partials in order.
 template <typename T>
 __global__ void k_msum(int ncells, int msize, const int* __restrict__ cell_task_ptr,
-                       const T* __restrict__ Mpart, T* __restrict__ M) {
+                       const T* __restrict__ Mpart, T* __restrict__ M,
+                       const int* __restrict__ cell_seg, const int* __restrict__ seg_done) {
   const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const int cell = (int)(gid / msize), row = (int)(gid % msize);
   if (cell >= ncells) return;
+  if (seg_done && seg_done[cell_seg[cell]]) return;  // a batch's masked segment
   const int t0 = cell_task_ptr[cell], t1 = cell_task_ptr[cell + 1];
   if (t0 == t1) return;
   T acc = 0;
@@ -2334,9 +2341,16 @@ struct SymRows {
   const T* buf = nullptr;
 };
 
+// Segments whose sites the finishing pass leaves alone (a batch's segments
+// that are finished or evaluated by another operator): skip[leaf_seg[leaf]].
+struct SegSkip {
+  const int* leaf_seg = nullptr;
+  const int* skip     = nullptr;
+};
+
 template <typename T, int M, int MODE, int P = 0>
 __global__ void __launch_bounds__(FINISH_BLOCK) k_finish(int n, const int* __restrict__ leaf_nslot, const T* __restrict__ Fnear,
-                         SymRows<T> sr,
+                         SymRows<T> sr, SegSkip sk,
                          int use_fmm,
                          TreeView tv, OpsView ov, const T* __restrict__ L, PosArgs<T> pa,
                          CellPos<T> cp, const T* __restrict__ src,
@@ -2348,6 +2362,7 @@ __global__ void __launch_bounds__(FINISH_BLOCK) k_finish(int n, const int* __res
   __shared__ double sh[32];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   T dv[1]     = {T(0)};  // (FP32 products for the FP32 apply: see block_sum)
+  if (sk.skip && i < n && sk.skip[sk.leaf_seg[tv.site_leaf[i]]]) return;  // (no grid sum then)
   if (i < n) {
     T f[3] = {0, 0, 0};
     if (sr.buf) {
@@ -2636,17 +2651,19 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
       const int tb = (ntask + SHIFT_THREADS / M2M_TASK_LEAVES - 1) / (SHIFT_THREADS / M2M_TASK_LEAVES);
       if (fixedP == 5)
         k_m2m_tasks_fixed<T, 5><<<tb, SHIFT_THREADS, 0, fs>>>(
-              tv, g.p2m_tasks.p, ntask, g.task_leaf.p, cell_pos<T>(g), w.M.p, w.Mpart.p);
+              tv, g.p2m_tasks.p, ntask, g.task_leaf.p, cell_pos<T>(g), w.M.p, w.Mpart.p, cseg,
+              seg_done);
       else if (fixedP == 6)
         k_m2m_tasks_fixed<T, 6><<<tb, SHIFT_THREADS, 0, fs>>>(
-              tv, g.p2m_tasks.p, ntask, g.task_leaf.p, cell_pos<T>(g), w.M.p, w.Mpart.p);
+              tv, g.p2m_tasks.p, ntask, g.task_leaf.p, cell_pos<T>(g), w.M.p, w.Mpart.p, cseg,
+              seg_done);
       else
         k_m2m_tasks<T><<<ntask, TB, 0, fs>>>(tv, ov, g.p2m_tasks.p, g.task_leaf.p,
                                             cell_pos<T>(g), w.M.p, w.Mpart.p);
       CG_LAUNCH();
       const long work = (long)tv.ncells * mst;
       k_msum<T><<<(unsigned)((work + 255) / 256), 256, 0, fs>>>(
-            tv.ncells, mst, g.cell_task_ptr.p, w.Mpart.p, w.M.p);
+            tv.ncells, mst, g.cell_task_ptr.p, w.Mpart.p, w.M.p, cseg, seg_done);
       CG_LAUNCH();
     }
     mark(1);
@@ -2692,9 +2709,11 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
     if (tv.nleaves > 0) {
       const int lb = (tv.nleaves + SHIFT_THREADS - 1) / SHIFT_THREADS;
       if (fixedP == 5)
-        k_l2l_leaf_fixed<T, 5><<<lb, SHIFT_THREADS, 0, fs>>>(tv, cell_pos<T>(g), w.L.p, w.Lleaf.p);
+        k_l2l_leaf_fixed<T, 5><<<lb, SHIFT_THREADS, 0, fs>>>(tv, cell_pos<T>(g), w.L.p, w.Lleaf.p,
+                                                             lseg, seg_done);
       else if (fixedP == 6)
-        k_l2l_leaf_fixed<T, 6><<<lb, SHIFT_THREADS, 0, fs>>>(tv, cell_pos<T>(g), w.L.p, w.Lleaf.p);
+        k_l2l_leaf_fixed<T, 6><<<lb, SHIFT_THREADS, 0, fs>>>(tv, cell_pos<T>(g), w.L.p, w.Lleaf.p,
+                                                             lseg, seg_done);
       else
         k_l2l_leaf<T><<<tv.nleaves, 128, 0, fs>>>(tv, ov, cell_pos<T>(g), w.L.p, w.Lleaf.p);
       CG_LAUNCH();
@@ -2746,8 +2765,10 @@ void eval_field(const Geometry& g, const DeviceOps* ops, FieldWork<T>& w, int m,
   ReduceSlots rs{nullptr, nullptr, nullptr};
   if (dot) rs = *dot;
   const T* Lp = g.fmm ? w.Lleaf.p : nullptr;
+  SegSkip sk;  // a batch's masked segments (site-value dots only: no grid sum)
+  if (seg_done && (!dot || !dot->partials)) sk.leaf_seg = g.leaf_seg.p, sk.skip = seg_done;
 #define CG_FINISH(TT, MM, MODE, PP)                                                           \
-  k_finish<TT, MM, MODE, PP><<<nb, FB, 0, s>>>(n, g.leaf_nslot.p, w.Fnear.p, sym_rows, g.fmm ? 1 : 0, tv, ov, Lp, \
+  k_finish<TT, MM, MODE, PP><<<nb, FB, 0, s>>>(n, g.leaf_nslot.p, w.Fnear.p, sym_rows, sk, g.fmm ? 1 : 0, tv, ov, Lp, \
                                            pos_args<TT>(g), cell_pos<TT>(g), src, damp ? 1 : 0, \
                                            dampT, g.corr_ptr.p, g.corr_idx.p, ainv6, out,    \
                                            out64, sign, rs)

@@ -225,10 +225,13 @@ CPPE_M2L_TABLES(CPPE_DEF_M2L_DD_KERNEL)
 // L of every cell: the sum of its chunk partials in order (0 without chunks).
 template <typename T>
 __global__ void k_lsum(int ncells, int lsize, const int* __restrict__ cell_chunk_ptr,
-                       const T* __restrict__ Lpart, T* __restrict__ L) {
+                       const T* __restrict__ Lpart, T* __restrict__ L,
+                       const int* __restrict__ cell_seg = nullptr,
+                       const int* __restrict__ seg_done = nullptr) {
   const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const int cell = (int)(gid / lsize), row = (int)(gid % lsize);
   if (cell >= ncells) return;
+  if (seg_done && seg_done[cell_seg[cell]]) return;  // a batch's masked segment
   T acc = 0;
   for (int t = cell_chunk_ptr[cell]; t < cell_chunk_ptr[cell + 1]; ++t)
     acc += Lpart[(size_t)t * lsize + row];
@@ -270,7 +273,7 @@ bool launch_m2l_fixed(const TreeView& tv, int m, int p, const int4* chunks, int 
   const long work = (long)tv.ncells * lsize;
   if (work > 0) {
     k_lsum<T><<<(unsigned)((work + 255) / 256), 256, 0, s>>>(tv.ncells, lsize, cell_chunk_ptr,
-                                                             Lpart, L);
+                                                             Lpart, L, cell_seg, seg_done);
     CG_LAUNCH();
   }
   return true;
