@@ -847,6 +847,7 @@ int BatchSystem::solve_device(const double* d_rhs, double* d_mu, int* iters_out)
     double rerr = 0.0;
     std::vector<double> swv[NINEXACT], rswv[NINEXACT];
     for (int k = 0; k < NINEXACT; ++k) swv[k].assign(nseg, -1.0), rswv[k].assign(nseg, 0.0);
+    std::vector<int> lvlv(nseg, 0);
     for (int outer = 0; outer < 12; ++outer) {
       // inner tolerances; segments already below the threshold stay put
       for (int g = 0; g < nseg; ++g) tolv[g] = std::max(eta * rn[g], 0.5 * t);
@@ -870,23 +871,48 @@ int BatchSystem::solve_device(const double* d_rhs, double* d_mu, int* iters_out)
         // in the first one where an inexact operator's effect, ~delta ||r||,
         // stays below 0.15 of the target eta ||r0||; in later ones (whose
         // residual is then formed from the recursion) where 1.5 delta ||r||
-        // stays below 0.04 t per operator
+        // stays below 0.18 t per operator
         const int stage = outer == 0 ? 0 : 1;
         for (int g = 0; g < nseg; ++g) {
           auto sw = [&](double d) {
             if (!(d > 0.0)) return -1.0;
-            return std::max(tolv[g], stage == 0 ? 0.15 * eta * rn[g] / d : 0.04 * t / (1.5 * d));
+            return std::max(tolv[g], stage == 0 ? 0.15 * eta * rn[g] / d : 0.18 * t / (1.5 * d));
           };
           swv[0][g] = sw(h_delta[0][g]);
           swv[1][g] = n_inexact > 1 && swv[0][g] > 0.0 ? std::min(swv[0][g], sw(h_delta[1][g]))
                                                        : -1.0;
         }
+        // a snapshot whose every running right-hand side already starts
+        // below a hand-over point starts with that operator (as
+        // k_blevel_update would set it after the first iteration)
+        std::fill(lvlv.begin(), lvlv.end(), 0);
+        for (auto& v : rswv) std::fill(v.begin(), v.end(), 0.0);
+        const int nsys = nseg / nrhs;
+        for (int sy = 0; sy < nsys; ++sy) {
+          bool any = false, all0 = true, all1 = n_inexact > 1;
+          for (int r = 0; r < nrhs; ++r) {
+            const int g = sy * nrhs + r;
+            if (rn[g] < tolv[g]) continue;  // done at once
+            any  = true;
+            all0 = all0 && rn[g] < swv[0][g];
+            all1 = all1 && rn[g] < swv[1][g];
+          }
+          const int l = !any ? 0 : (all0 ? (all1 ? 2 : 1) : 0);
+          for (int r = 0; r < nrhs && l > 0; ++r) {
+            const int g = sy * nrhs + r;
+            lvlv[g]     = l;
+            rswv[0][g]  = rn[g];
+            if (l == 2) rswv[1][g] = rn[g];
+          }
+        }
         for (int k = 0; k < NINEXACT; ++k) {
           CG_CUDA(cudaMemcpyAsync(seg_sw[k].p, swv[k].data(), nseg * sizeof(double),
                                   cudaMemcpyHostToDevice, stream));
-          CG_CUDA(cudaMemsetAsync(seg_rsw[k].p, 0, nseg * sizeof(double), stream));
+          CG_CUDA(cudaMemcpyAsync(seg_rsw[k].p, rswv[k].data(), nseg * sizeof(double),
+                                  cudaMemcpyHostToDevice, stream));
         }
-        CG_CUDA(cudaMemsetAsync(seg_level.p, 0, nseg * sizeof(int), stream));
+        CG_CUDA(cudaMemcpyAsync(seg_level.p, lvlv.data(), nseg * sizeof(int),
+                                cudaMemcpyHostToDevice, stream));
       }
       k_bcg_init_seg<<<(nseg + 127) / 128, 128, 0, stream>>>(
             nseg, seg_rz.p, seg_rr.p, seg_rz.p, seg_rnorm.p, done.p, iters.p, seg_tol.p);
@@ -907,7 +933,10 @@ int BatchSystem::solve_device(const double* d_rhs, double* d_mu, int* iters_out)
                                          (n_inexact > 1 ? h_delta[1][g] * rswv[1][g] : 0.0)));
       }
       const double rmax = *std::max_element(rn.begin(), rn.end());
-      if (exact && rerr + REC_ERR * rmax + extra < 0.1 * t) {
+      // the residual from the recursion stands where its error bound stays
+      // below 0.4 t: the inner solves stop at 0.5 t, so a segment's residual
+      // plus the bound stays below t (as System::solve_mixed)
+      if (exact && rerr + REC_ERR * rmax + extra < 0.4 * t) {
         // residual from the inner recursion (as System::solve_mixed)
         k_bres<<<nb, BB, 0, stream>>>(n, nullptr, nullptr, nullptr, r.p, site_b.p, r32.p);
         CG_LAUNCH();
