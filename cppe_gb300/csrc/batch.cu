@@ -333,6 +333,27 @@ __global__ void k_blevel_masks(int nseg, int nlev, const int* __restrict__ done,
   if (nlev > 2) m2[g] = d || l != 2;
 }
 
+// Whether some running segment is at each operator level: the conditions of
+// the graph's per-level passes.
+__global__ void k_blevel_any(int nseg, int nlev, const int* __restrict__ done,
+                             const int* __restrict__ level, cudaGraphConditionalHandle h0,
+                             cudaGraphConditionalHandle h1, cudaGraphConditionalHandle h2) {
+  int a0 = 0, a1 = 0, a2 = 0;
+  for (int g = threadIdx.x; g < nseg; g += blockDim.x)
+    if (!done[g]) {
+      const int l = level[g];
+      a0 |= l == 0, a1 |= l == 1, a2 |= l == 2;
+    }
+  a0 = __syncthreads_or(a0);
+  a1 = __syncthreads_or(a1);
+  a2 = __syncthreads_or(a2);
+  if (threadIdx.x == 0) {
+    cudaGraphSetConditional(h0, a0 ? 1u : 0u);
+    if (nlev > 1) cudaGraphSetConditional(h1, a1 ? 1u : 0u);
+    if (nlev > 2) cudaGraphSetConditional(h2, a2 ? 1u : 0u);
+  }
+}
+
 // Hand-over of a snapshot's running segments (its right-hand sides) to the
 // next inexact operator once every one of them is below that operator's
 // hand-over point (sw <= 0: never).  The right-hand sides of a snapshot move
@@ -376,6 +397,7 @@ BatchSystem::~BatchSystem() {
     if (side.s) cudaStreamSynchronize(side.s);
     side.destroy();
     cudaStreamDestroy(stream);
+    if (cap_stream) cudaStreamDestroy(cap_stream);
   }
   for (auto& e : pcg_exec)
     if (e) cudaGraphExecDestroy(e);
@@ -394,6 +416,7 @@ void BatchSystem::init(int nsys, const int* site_offset, const double* xyz, cons
   device = o.device;
   CG_CUDA(cudaSetDevice(device));
   CG_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  CG_CUDA(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
   side.create();
   if (o.tree_expansion_order < 2 || o.tree_expansion_order > 7)
     fail(CPPE_GPU_INVALID_ARG, "tree_expansion_order must be in [2, 7]");
@@ -554,6 +577,63 @@ void BatchSystem::apply_levels32(const float* in, float* out) {
   CG_LAUNCH();
 }
 
+void BatchSystem::apply_levels32_graph(const float* in, float* out) {
+  const int gb = (nseg + 127) / 128, nlev = 1 + n_inexact;
+  k_blevel_masks<<<gb, 128, 0, stream>>>(nseg, nlev, done.p, seg_level.p, lvl_mask[0].p,
+                                         lvl_mask[1].p, lvl_mask[2].p);
+  CG_LAUNCH();
+  cudaStreamCaptureStatus st{};
+  cudaGraph_t cg = nullptr;
+  CG_CUDA(cudaStreamGetCaptureInfo(stream, &st, nullptr, &cg, nullptr, nullptr, nullptr));
+  if (st != cudaStreamCaptureStatusActive || !cg)
+    fail(CPPE_GPU_CUDA_ERROR, "per-level passes outside a graph capture");
+  cudaGraphConditionalHandle hl[1 + NINEXACT] = {};
+  for (int l = 0; l < nlev; ++l)
+    CG_CUDA(cudaGraphConditionalHandleCreate(&hl[l], cg, 0, cudaGraphCondAssignDefault));
+  k_blevel_any<<<1, 256, 0, stream>>>(nseg, nlev, done.p, seg_level.p, hl[0], hl[1],
+                                      hl[NINEXACT]);
+  CG_LAUNCH();
+  ReduceSlots rs{nullptr, nullptr, nullptr};
+  rs.site_values = site_a.p;
+  for (int l = 0; l < nlev; ++l) {
+    // a conditional node after the capture's current tip; the stream's
+    // later work follows it
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd                   = 0;
+    CG_CUDA(cudaStreamGetCaptureInfo(stream, &st, nullptr, &cg, &deps, nullptr, &nd));
+    cudaGraphNodeParams ip{};
+    ip.type               = cudaGraphNodeTypeConditional;
+    ip.conditional.handle = hl[l];
+    ip.conditional.type   = cudaGraphCondTypeIf;
+    ip.conditional.size   = 1;
+    cudaGraphNode_t node{};
+    CG_CUDA(cudaGraphAddNode(&node, cg, deps, nullptr, nd, &ip));
+    CG_CUDA(cudaStreamUpdateCaptureDependencies(stream, &node, nullptr, 1,
+                                                cudaStreamSetCaptureDependencies));
+    // the pass itself, captured into the node's body
+    CG_CUDA(cudaStreamBeginCaptureToGraph(cap_stream, ip.conditional.phGraph_out[0], nullptr,
+                                          nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    try {
+      if (l == 0)
+        eval_field<float>(geo, ops.get(), w32, 1, in, opt.damp != 0, opt.damping_factor,
+                          FINISH_APPLY, ainv32.p, out, nullptr, 1.0, &rs, cap_stream, nullptr,
+                          NEAR_FP64, nullptr, lvl_mask[0].p);
+      else
+        eval_field<float>(geo_x[l - 1], ops.get(), w32x[l - 1], 1, in, opt.damp != 0,
+                          opt.damping_factor, FINISH_APPLY, ainv32.p, out, nullptr, 1.0, &rs,
+                          cap_stream, nullptr, NEAR_FP64, nullptr, lvl_mask[l].p);
+    } catch (...) {
+      cudaGraph_t dropped = nullptr;
+      cudaStreamEndCapture(cap_stream, &dropped);
+      throw;
+    }
+    cudaGraph_t captured = nullptr;
+    CG_CUDA(cudaStreamEndCapture(cap_stream, &captured));
+  }
+  k_seg_sum<<<nseg, BB, 0, stream>>>(seg_start.p, site_a.p, nullptr, seg_pap.p, nullptr);
+  CG_LAUNCH();
+}
+
 // Each segment's relative difference between the operator (double-float)
 // and each inexact FP32 operator on a random vector and on a smooth one (the
 // response to a uniform field), times 3 as the bound delta used for the
@@ -646,7 +726,10 @@ void BatchSystem::pcg_iteration(T* xv, T* rv, T* zv, T* pv, T* Apv, const T* a6,
   bool levels = false;
   if constexpr (std::is_same<T, float>::value) levels = n_inexact > 0;
   if constexpr (std::is_same<T, float>::value) {
-    if (levels) apply_levels32(pv, Apv);
+    if (levels && graph)
+      apply_levels32_graph(pv, Apv);
+    else if (levels)
+      apply_levels32(pv, Apv);
   }
   if (!levels) apply_seg<T>(pv, Apv, NEAR_FP64, true);
   k_bcg_update<T><<<nb, BB, 0, stream>>>(n, site_seg.p, pv, Apv, a6, xv, rv, zv, seg_rz.p,

@@ -67,6 +67,11 @@ struct BatchSystem {
   void apply_level32(int k, const float* in, float* out, const int* mask);
   // the iteration's FP32 apply: each segment with the operator of its level
   void apply_levels32(const float* in, float* out);
+  // the same inside a graph capture on `stream`: each operator's pass in a
+  // conditional node that runs only when some segment is at its level (the
+  // passes captured on cap_stream, far field in line)
+  void apply_levels32_graph(const float* in, float* out);
+  cudaStream_t cap_stream = nullptr;
   // measures each segment's difference between the operator and the
   // inexact ones (part of init, after the inexact geometries are built)
   void measure_inexact(const std::vector<int>& seg_start_h, const std::vector<char>& seg_fmm);
