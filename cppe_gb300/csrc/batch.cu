@@ -950,16 +950,18 @@ int BatchSystem::solve_device(const double* d_rhs, double* d_mu, int* iters_out)
       CG_CUDA(cudaMemcpyAsync(seg_tol.p, tolv.data(), nseg * sizeof(double),
                               cudaMemcpyHostToDevice, stream));
       if (n_inexact > 0) {
-        // hand-over points of this inner solve, as System's k_inner_stage:
-        // in the first one where an inexact operator's effect, ~delta ||r||,
-        // stays below 0.15 of the target eta ||r0||; in later ones (whose
-        // residual is then formed from the recursion) where 1.5 delta ||r||
-        // stays below 0.18 t per operator
+        // hand-over points of this inner solve: in the first one where an
+        // inexact operator's effect, ~delta ||r||, stays below 0.6 of the
+        // target eta ||r0|| (the double-float residual that follows is
+        // exact; System's k_inner_stage keeps 0.15, but here the operator's
+        // iterations over every segment are the expensive ones); in later
+        // ones (whose residual is then formed from the recursion) where
+        // 1.5 delta ||r|| stays below 0.18 t per operator
         const int stage = outer == 0 ? 0 : 1;
         for (int g = 0; g < nseg; ++g) {
           auto sw = [&](double d) {
             if (!(d > 0.0)) return -1.0;
-            return std::max(tolv[g], stage == 0 ? 0.15 * eta * rn[g] / d : 0.18 * t / (1.5 * d));
+            return std::max(tolv[g], stage == 0 ? 0.6 * eta * rn[g] / d : 0.18 * t / (1.5 * d));
           };
           swv[0][g] = sw(h_delta[0][g]);
           swv[1][g] = n_inexact > 1 && swv[0][g] > 0.0 ? std::min(swv[0][g], sw(h_delta[1][g]))
