@@ -950,13 +950,12 @@ int BatchSystem::solve_device(const double* d_rhs, double* d_mu, int* iters_out)
       CG_CUDA(cudaMemcpyAsync(seg_tol.p, tolv.data(), nseg * sizeof(double),
                               cudaMemcpyHostToDevice, stream));
       if (n_inexact > 0) {
-        // hand-over points of this inner solve: in the first one where an
-        // inexact operator's effect, ~delta ||r||, stays below 0.6 of the
-        // target eta ||r0|| (the double-float residual that follows is
-        // exact; System's k_inner_stage keeps 0.15, but here the operator's
-        // iterations over every segment are the expensive ones); in later
-        // ones (whose residual is then formed from the recursion) where
-        // 1.5 delta ||r|| stays below 0.18 t per operator
+        // hand-over points of this inner solve, as System's k_inner_stage:
+        // in the first one where an inexact operator's effect, ~delta ||r||,
+        // stays below 0.6 of the target eta ||r0|| (the double-float
+        // residual that follows is exact); in later ones (whose residual is
+        // then formed from the recursion) where 1.5 delta ||r|| stays below
+        // 0.18 t per operator
         const int stage = outer == 0 ? 0 : 1;
         for (int g = 0; g < nseg; ++g) {
           auto sw = [&](double d) {

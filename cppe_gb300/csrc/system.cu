@@ -639,17 +639,19 @@ int System::solve_fp64(bool zero_guess, double* hist_out, int hist_cap, int* ite
 // the operator down to S_TOL = max(final threshold, S_SW1), then with
 // inexact operator 1 down to max(final, S_SW2), then with operator 2 down to
 // the final threshold S_TOLF.  Hand-over points: where each inexact
-// operator's effect on the residual, ~delta ||r||, stays below 0.15 of the
-// stage's target (stage 0: eta ||r0||), or, for the last stage, where
-// 1.5 delta ||r|| stays below 0.2 t (the residual is then formed from the
-// recursion, which carries those differences).
+// operator's effect on the residual, ~delta ||r||, stays below 0.6 of the
+// first stage's target eta ||r0|| (the double-float residual that follows
+// is exact; the inner solve's true residual then stays below 1.6 eta ||r0||),
+// or, for the last stage, where 1.5 delta ||r|| stays below 0.2 t (the
+// residual is then formed from the recursion, which carries those
+// differences).
 __global__ void k_inner_stage(double* scal, int* flags, double t, double eta, int stage,
                               double delta1, double delta2) {
   const double rn  = scal[S_RNORM];
   const double tol = fmax(eta * rn, 0.5 * t);
   auto sw = [&](double d) {
     if (d <= 0.0) return tol;
-    return fmax(tol, stage == 0 ? 0.15 * eta * rn / d : 0.2 * t / (1.5 * d));
+    return fmax(tol, stage == 0 ? 0.6 * eta * rn / d : 0.2 * t / (1.5 * d));
   };
   const double sw1 = delta1 > 0.0 ? sw(delta1) : tol;
   const double sw2 = delta2 > 0.0 ? fmin(sw1, sw(delta2)) : tol;
