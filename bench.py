@@ -352,7 +352,7 @@ def batched_section(dev, steps, flush, compare=True):
         # the batch alone (profiling): no one-at-a-time FP64 solves
         return {"workload": "256 snapshots x 8 RHS (batch only)", "value": t_batch, "unit": "s",
                 "fp32_applies": bst["fp32_applies"], "fp64_applies": bst["fp64_applies"],
-                "max_rnorm": bst["max_rnorm"]}
+                "host_waits": bst["host_waits"], "max_rnorm": bst["max_rnorm"]}
     mu = d_mu.cpu().numpy()
     # plain FP64, one segment at a time: the first right-hand side of every
     # snapshot is solved and timed; the 8 right-hand sides of a snapshot cost
@@ -411,7 +411,7 @@ def batched_section(dev, steps, flush, compare=True):
             "plain_fp64_note": "first RHS of each snapshot solved and timed one at a time, x8",
             "speedup_vs_plain_fp64": plain / t_batch,
             "fp32_applies": bst["fp32_applies"], "fp64_applies": bst["fp64_applies"],
-            "max_fp64_residual": worst, "vs_oracle": vs_oracle, "setup_s": setup,
+            "host_waits": bst["host_waits"], "max_fp64_residual": worst, "vs_oracle": vs_oracle, "setup_s": setup,
             "autotune_s": tune, "fp32_apply_ms": tuned_ms}
 
 

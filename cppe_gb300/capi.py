@@ -85,6 +85,7 @@ def lib():
                                               ctypes.POINTER(ctypes.c_longlong)]
         l.cppe_gpu_fma_peak.argtypes = [ctypes.c_int, ctypes.c_int, D]
         l.cppe_gpu_batch_stats.argtypes = [ctypes.c_void_p, I, I, D]
+        l.cppe_gpu_batch_host_waits.argtypes = [ctypes.c_void_p, I]
         l.cppe_gpu_batch_stream.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]
         l.cppe_gpu_batch_autotune.argtypes = [ctypes.c_void_p, ctypes.c_int, D]
         F = ctypes.POINTER(ctypes.c_float)
@@ -255,7 +256,10 @@ class Batch:
         a, b, r = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_double(0)
         check(lib().cppe_gpu_batch_stats(self.h, ctypes.byref(a), ctypes.byref(b),
                                          ctypes.byref(r)))
-        return dict(fp64_applies=a.value, fp32_applies=b.value, max_rnorm=r.value)
+        w = ctypes.c_int(0)
+        check(lib().cppe_gpu_batch_host_waits(self.h, ctypes.byref(w)))
+        return dict(fp64_applies=a.value, fp32_applies=b.value, max_rnorm=r.value,
+                    host_waits=w.value)
 
     def stream(self):
         s = ctypes.c_void_p()

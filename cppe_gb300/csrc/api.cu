@@ -907,6 +907,14 @@ int cppe_gpu_batch_stats(cppe_gpu_batch* bh, int* fp64_applies, int* fp32_applie
   });
 }
 
+int cppe_gpu_batch_host_waits(cppe_gpu_batch* bh, int* waits) {
+  return guard([&]() -> int {
+    need(bh && waits, "null argument");
+    *waits = bh->b.host_waits;
+    return CPPE_GPU_OK;
+  });
+}
+
 int cppe_gpu_batch_autotune(cppe_gpu_batch* bh, int reps, double* best_ms) {
   return guard([&]() -> int {
     need(bh && reps > 0, "null argument");

@@ -18,6 +18,8 @@ namespace cg {
 constexpr int BB = 256;
 // opening angles of the inexact inner operators (as the single-system solver's)
 constexpr double BATCH_INEXACT_THETA[BatchSystem::NINEXACT] = {0.6, 0.8};
+// the mixed solve's inner tolerance relative to the residual at its start
+constexpr double BATCH_ETA = 3e-6;
 
 // ---------------------------------------------------------------------------
 // Geometry concatenation
@@ -390,6 +392,52 @@ __global__ void k_blevel_update(int nsys, int nrhs, int nx, const double* __rest
   }
 }
 
+// The tolerances and hand-over points of a mixed solve's inner solve, per
+// snapshot (its right-hand sides share the operator level), from the
+// residual norms at its start -- what solve_device's host loop sets for
+// outer iteration 0 (stage 0) and 1 (stage 1, after the double-float
+// residual, where segments already below the threshold are done at once).
+// With inexact operators (nx > 0) also the hand-over points and the starting
+// levels: stage 0 hands over where the operator's effect delta ||r|| stays
+// below 0.6 of the target eta ||r0||, stage 1 where 1.5 delta ||r|| stays
+// below 0.18 t; a snapshot already below a point starts at its level.
+__global__ void k_bstage(int nsys, int nrhs, int nx, int stage, double t, double eta,
+                         const double* __restrict__ rnorm, const double* __restrict__ d0,
+                         const double* __restrict__ d1, double* __restrict__ tol,
+                         double* __restrict__ sw0, double* __restrict__ sw1,
+                         double* __restrict__ rsw0, double* __restrict__ rsw1,
+                         int* __restrict__ level) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsys) return;
+  bool any = false, all0 = true, all1 = nx > 1;
+  for (int r = 0; r < nrhs; ++r) {
+    const int g     = s * nrhs + r;
+    const double rn = rnorm[g];
+    double tl       = fmax(eta * rn, 0.5 * t);
+    if (stage > 0 && rn < t) tl = 1e300;
+    tol[g] = tl;
+    if (nx == 0) continue;
+    auto sw = [&](double d) {
+      return d > 0.0 ? fmax(tl, stage == 0 ? 0.6 * eta * rn / d : 0.18 * t / (1.5 * d)) : -1.0;
+    };
+    const double s0 = sw(d0[g]);
+    const double s1 = nx > 1 && s0 > 0.0 ? fmin(s0, sw(d1[g])) : -1.0;
+    sw0[g] = s0, sw1[g] = s1;
+    if (rn < tl) continue;  // done at once
+    any  = true;
+    all0 = all0 && rn < s0;
+    all1 = all1 && rn < s1;
+  }
+  if (nx == 0) return;
+  const int l = !any ? 0 : (all0 ? (all1 ? 2 : 1) : 0);
+  for (int r = 0; r < nrhs; ++r) {
+    const int g = s * nrhs + r;
+    level[g]    = l;
+    rsw0[g]     = l > 0 ? rnorm[g] : 0.0;
+    rsw1[g]     = l == 2 ? rnorm[g] : 0.0;
+  }
+}
+
 BatchSystem::~BatchSystem() {
   if (stream) {
     cudaSetDevice(device);
@@ -398,9 +446,11 @@ BatchSystem::~BatchSystem() {
     side.destroy();
     cudaStreamDestroy(stream);
     if (cap_stream) cudaStreamDestroy(cap_stream);
+    if (cap_stream2) cudaStreamDestroy(cap_stream2);
   }
   for (auto& e : pcg_exec)
     if (e) cudaGraphExecDestroy(e);
+  if (course_exec) cudaGraphExecDestroy(course_exec);
   if (h_active) cudaFreeHost(h_active);
 }
 
@@ -417,6 +467,8 @@ void BatchSystem::init(int nsys, const int* site_offset, const double* xyz, cons
   CG_CUDA(cudaSetDevice(device));
   CG_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
   CG_CUDA(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
+  CG_CUDA(cudaStreamCreateWithFlags(&cap_stream2, cudaStreamNonBlocking));
+  if_stream = cap_stream;
   side.create();
   if (o.tree_expansion_order < 2 || o.tree_expansion_order > 7)
     fail(CPPE_GPU_INVALID_ARG, "tree_expansion_order must be in [2, 7]");
@@ -611,24 +663,24 @@ void BatchSystem::apply_levels32_graph(const float* in, float* out) {
     CG_CUDA(cudaStreamUpdateCaptureDependencies(stream, &node, nullptr, 1,
                                                 cudaStreamSetCaptureDependencies));
     // the pass itself, captured into the node's body
-    CG_CUDA(cudaStreamBeginCaptureToGraph(cap_stream, ip.conditional.phGraph_out[0], nullptr,
+    CG_CUDA(cudaStreamBeginCaptureToGraph(if_stream, ip.conditional.phGraph_out[0], nullptr,
                                           nullptr, 0, cudaStreamCaptureModeThreadLocal));
     try {
       if (l == 0)
         eval_field<float>(geo, ops.get(), w32, 1, in, opt.damp != 0, opt.damping_factor,
-                          FINISH_APPLY, ainv32.p, out, nullptr, 1.0, &rs, cap_stream, nullptr,
+                          FINISH_APPLY, ainv32.p, out, nullptr, 1.0, &rs, if_stream, nullptr,
                           NEAR_FP64, nullptr, lvl_mask[0].p);
       else
         eval_field<float>(geo_x[l - 1], ops.get(), w32x[l - 1], 1, in, opt.damp != 0,
                           opt.damping_factor, FINISH_APPLY, ainv32.p, out, nullptr, 1.0, &rs,
-                          cap_stream, nullptr, NEAR_FP64, nullptr, lvl_mask[l].p);
+                          if_stream, nullptr, NEAR_FP64, nullptr, lvl_mask[l].p);
     } catch (...) {
       cudaGraph_t dropped = nullptr;
-      cudaStreamEndCapture(cap_stream, &dropped);
+      cudaStreamEndCapture(if_stream, &dropped);
       throw;
     }
     cudaGraph_t captured = nullptr;
-    CG_CUDA(cudaStreamEndCapture(cap_stream, &captured));
+    CG_CUDA(cudaStreamEndCapture(if_stream, &captured));
   }
   k_seg_sum<<<nseg, BB, 0, stream>>>(seg_start.p, site_a.p, nullptr, seg_pap.p, nullptr);
   CG_LAUNCH();
@@ -691,6 +743,7 @@ void BatchSystem::measure_inexact(const std::vector<int>& seg_start_h,
       h_delta[k][g] = d;
     }
   }
+  for (int k = 0; k < NINEXACT; ++k) seg_delta_d[k].upload(h_delta[k], stream);
   CG_CUDA(cudaStreamSynchronize(stream));
 }
 
@@ -831,14 +884,14 @@ int BatchSystem::run_pcg(T* xv, T* rv, T* zv, T* pv, T* Apv, const T* a6, int ma
     h_iters.resize(nseg);
     CG_CUDA(cudaMemcpyAsync(h_iters.data(), iters.p, nseg * sizeof(int), cudaMemcpyDeviceToHost,
                             stream));
-    CG_CUDA(cudaStreamSynchronize(stream));
+    host_wait();
     k = *std::max_element(h_iters.begin(), h_iters.end());
     launch_counter() += pcg_body_launches[v] * k + 1;
   } else {
     for (; k < maxiter; ++k) {
       pcg_iteration<T>(xv, rv, zv, pv, Apv, a6, maxiter, false);
       CG_CUDA(cudaMemcpyAsync(h_active, active.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
-      CG_CUDA(cudaStreamSynchronize(stream));
+      host_wait();
       if (*h_active == 0) {
         ++k;
         break;
@@ -860,7 +913,154 @@ double BatchSystem::autotune(int reps) {
   // captured loops hold the old schedule's buffers: rebuild on next use
   for (auto& e : pcg_exec)
     if (e) cudaGraphExecDestroy(e), e = nullptr;
+  if (course_exec) cudaGraphExecDestroy(course_exec), course_exec = nullptr;
   return best;
+}
+
+void BatchSystem::capture_pcg_loop(int maxiter) {
+  cudaStreamCaptureStatus st{};
+  cudaGraph_t cg = nullptr;
+  CG_CUDA(cudaStreamGetCaptureInfo(stream, &st, nullptr, &cg, nullptr, nullptr, nullptr));
+  if (st != cudaStreamCaptureStatusActive || !cg)
+    fail(CPPE_GPU_CUDA_ERROR, "inner solve outside a graph capture");
+  cudaGraphConditionalHandle h{};
+  CG_CUDA(cudaGraphConditionalHandleCreate(&h, cg, 0, cudaGraphCondAssignDefault));
+  k_bcg_any<<<1, 256, 0, stream>>>(h, nseg, done.p, active.p);
+  CG_LAUNCH();
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd                   = 0;
+  CG_CUDA(cudaStreamGetCaptureInfo(stream, &st, nullptr, &cg, &deps, nullptr, &nd));
+  cudaGraphNodeParams wp{};
+  wp.type               = cudaGraphNodeTypeConditional;
+  wp.conditional.handle = h;
+  wp.conditional.type   = cudaGraphCondTypeWhile;
+  wp.conditional.size   = 1;
+  cudaGraphNode_t node{};
+  CG_CUDA(cudaGraphAddNode(&node, cg, deps, nullptr, nd, &wp));
+  CG_CUDA(cudaStreamUpdateCaptureDependencies(stream, &node, nullptr, 1,
+                                              cudaStreamSetCaptureDependencies));
+  // the body on the second capture stream; its per-level passes on the third
+  CG_CUDA(cudaStreamBeginCaptureToGraph(cap_stream, wp.conditional.phGraph_out[0], nullptr,
+                                        nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  const cudaStream_t outer = stream, outer_if = if_stream;
+  stream = cap_stream, if_stream = cap_stream2;
+  const long long c0 = launch_counter();
+  try {
+    pcg_iteration<float>(d32.p, r32.p, z32.p, p32.p, Ap32.p, alpha32.p, maxiter, true);
+    k_bcg_continue<<<1, 1, 0, stream>>>(h, active.p);
+    CG_LAUNCH();
+  } catch (...) {
+    stream = outer, if_stream = outer_if;
+    launch_counter()    = c0;
+    cudaGraph_t dropped = nullptr;
+    cudaStreamEndCapture(cap_stream, &dropped);
+    throw;
+  }
+  course_body_launches = launch_counter() - c0;
+  launch_counter()     = c0;
+  stream = outer, if_stream = outer_if;
+  cudaGraph_t captured = nullptr;
+  CG_CUDA(cudaStreamEndCapture(cap_stream, &captured));
+}
+
+// The usual course of a mixed solve from the guess x = alpha F, as
+// solve_device's host loop runs it when every choice goes the usual way.
+void BatchSystem::course_body(int maxiter) {
+  const int nb = (n + BB - 1) / BB, n3 = 3 * n, nb3 = (n3 + BB - 1) / BB;
+  const int gb = (nseg + 127) / 128, nsys = nseg / nrhs, sb = (nsys + 127) / 128;
+  const double t = opt.induced_thresh;
+  // the start residual F - B x with the FP32 operator
+  k_bf32<<<nb3, BB, 0, stream>>>(n3, x.p, p32.p);
+  CG_LAUNCH();
+  apply_seg<float>(p32.p, Ap32.p);
+  CG_CUDA(cudaMemsetAsync(d32.p, 0, sizeof(float) * n3, stream));
+  k_bcg_start<float><<<nb, BB, 0, stream>>>(n, F.p, Ap32.p, alpha32.p, r32.p, z32.p, p32.p,
+                                            site_a.p, site_b.p);
+  CG_LAUNCH();
+  k_seg_sum<<<nseg, BB, 0, stream>>>(seg_start.p, site_a.p, site_b.p, seg_rz.p, seg_rr.p);
+  CG_LAUNCH();
+  k_bsqrt<<<gb, 128, 0, stream>>>(nseg, seg_rr.p, seg_rnorm.p);
+  CG_LAUNCH();
+  // the first inner solve
+  const int nx = n_inexact;
+  auto stage = [&](int sg) {
+    k_bstage<<<sb, 128, 0, stream>>>(nsys, nrhs, nx, sg, t, BATCH_ETA, seg_rnorm.p,
+                                     seg_delta_d[0].p, seg_delta_d[1].p, seg_tol.p, seg_sw[0].p,
+                                     seg_sw[1].p, seg_rsw[0].p, seg_rsw[1].p, seg_level.p);
+    CG_LAUNCH();
+  };
+  stage(0);
+  k_bcg_init_seg<<<gb, 128, 0, stream>>>(nseg, seg_rz.p, seg_rr.p, seg_rz.p, seg_rnorm.p, done.p,
+                                          iters.p, seg_tol.p);
+  CG_LAUNCH();
+  capture_pcg_loop(maxiter);
+  CG_CUDA(cudaMemcpyAsync(iters_first.p, iters.p, nseg * sizeof(int), cudaMemcpyDeviceToDevice,
+                          stream));
+  // the double-float residual of x + d
+  k_bacc<<<nb3, BB, 0, stream>>>(n3, x.p, d32.p);
+  CG_LAUNCH();
+  apply_seg<double>(x.p, Ap.p, NEAR_DD);
+  k_bres<<<nb, BB, 0, stream>>>(n, F.p, Ap.p, nullptr, r.p, site_b.p);
+  CG_LAUNCH();
+  seg_norms_from_site_b();
+  CG_CUDA(cudaMemcpyAsync(rn_second.p, seg_rnorm.p, nseg * sizeof(double),
+                          cudaMemcpyDeviceToDevice, stream));
+  // the second inner solve, for the right-hand side fl(r)
+  stage(1);
+  k_bcg_start<float><<<nb, BB, 0, stream>>>(n, r.p, nullptr, alpha32.p, r32.p, z32.p, p32.p,
+                                            site_a.p, site_b.p);
+  CG_LAUNCH();
+  k_seg_sum<<<nseg, BB, 0, stream>>>(seg_start.p, site_a.p, site_b.p, seg_rz.p, seg_rr.p);
+  CG_LAUNCH();
+  k_bcg_init_seg<<<gb, 128, 0, stream>>>(nseg, seg_rz.p, seg_rr.p, seg_rz.p, seg_rnorm.p, done.p,
+                                          iters.p, seg_tol.p);
+  CG_LAUNCH();
+  capture_pcg_loop(maxiter);
+  // the residual from the recursion; x += d
+  k_bres<<<nb, BB, 0, stream>>>(n, nullptr, nullptr, nullptr, r.p, site_b.p, r32.p);
+  CG_LAUNCH();
+  k_bacc<<<nb3, BB, 0, stream>>>(n3, x.p, d32.p);
+  CG_LAUNCH();
+  seg_norms_from_site_b();
+}
+
+bool BatchSystem::course_graph_ready(int maxiter) {
+  static const bool graphs = [] {
+    const char* e = std::getenv("CPPE_GPU_GRAPHS");
+    return !(e && e[0] == '0');
+  }();
+  if (!graphs) course_failed = true;
+  if (course_exec || course_failed) return course_exec != nullptr;
+  iters_first.alloc(nseg);
+  rn_second.alloc(nseg);
+  // the operators' work buffers at their sizes (a capture cannot resize
+  // them); what these applies write the course writes again first
+  apply_seg<float>(p32.p, Ap32.p);
+  apply_seg<double>(x.p, Ap.p, NEAR_DD);
+  CG_CUDA(cudaStreamSynchronize(stream));
+  cudaGraph_t g = nullptr;
+  bool ok = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+  const long long c0 = launch_counter();
+  if (ok) {
+    try {
+      CaptureScope cs;
+      course_body(maxiter);
+    } catch (const Failure&) {
+      ok = false;
+    }
+    ok = (cudaStreamEndCapture(stream, &g) == cudaSuccess) && ok;
+  }
+  course_launches  = launch_counter() - c0;
+  launch_counter() = c0;
+  if (ok) ok = cudaGraphInstantiate(&course_exec, g, 0) == cudaSuccess;
+  if (g) cudaGraphDestroy(g);
+  if (!ok) {
+    cudaGetLastError();  // clear the refusal; the host loop runs the whole solve
+    if (course_exec) cudaGraphExecDestroy(course_exec);
+    course_exec   = nullptr;
+    course_failed = true;
+  }
+  return course_exec != nullptr;
 }
 
 void BatchSystem::seg_norms_from_site_b() {
@@ -870,9 +1070,15 @@ void BatchSystem::seg_norms_from_site_b() {
   CG_LAUNCH();
 }
 
+void BatchSystem::host_wait() {
+  ++host_waits;
+  CG_CUDA(cudaStreamSynchronize(stream));
+}
+
 int BatchSystem::solve_device(const double* d_rhs, double* d_mu, int* iters_out) {
   CG_CUDA(cudaSetDevice(device));
-  stats = SolveStats();
+  stats      = SolveStats();
+  host_waits = 0;
   const int nb = (n + BB - 1) / BB, n3 = 3 * n, nb3 = (n3 + BB - 1) / BB;
   const double t = opt.induced_thresh;
   permute_in(geo, d_rhs, F.p, 3, stream);
@@ -900,29 +1106,15 @@ int BatchSystem::solve_device(const double* d_rhs, double* d_mu, int* iters_out)
     CG_CUDA(cudaMemcpyAsync(dn.data(), done.p, nseg * sizeof(int), cudaMemcpyDeviceToHost, stream));
     CG_CUDA(cudaMemcpyAsync(it_h.data(), iters.p, nseg * sizeof(int), cudaMemcpyDeviceToHost,
                             stream));
-    CG_CUDA(cudaStreamSynchronize(stream));
+    host_wait();
     status = std::all_of(dn.begin(), dn.end(), [](int d) { return d == 1; }) ? CPPE_GPU_OK
                                                                              : CPPE_GPU_NOT_CONVERGED;
     total = it_h;
   } else {
     // mixed precision, as System::solve_mixed but with per-segment scalars
-    const double eta = 3e-6;
-    k_bf32<<<nb3, BB, 0, stream>>>(n3, x.p, p32.p);
-    CG_LAUNCH();
-    apply_seg<float>(p32.p, Ap32.p);
-    stats.fp32_applies++;
-    CG_CUDA(cudaMemsetAsync(d32.p, 0, sizeof(float) * n3, stream));
-    k_bcg_start<float><<<nb, BB, 0, stream>>>(n, F.p, Ap32.p, alpha32.p, r32.p, z32.p, p32.p,
-                                              site_a.p, site_b.p);
-    CG_LAUNCH();
-    k_seg_sum<<<nseg, BB, 0, stream>>>(seg_start.p, site_a.p, site_b.p, seg_rz.p, seg_rr.p);
-    CG_LAUNCH();
+    const double eta = BATCH_ETA;
+    const int maxit  = std::max(1, opt.maxiter);
     std::vector<double> rn(nseg);
-    k_bsqrt<<<(nseg + 127) / 128, 128, 0, stream>>>(nseg, seg_rr.p, seg_rnorm.p);
-    CG_LAUNCH();
-    CG_CUDA(cudaMemcpyAsync(rn.data(), seg_rnorm.p, nseg * sizeof(double), cudaMemcpyDeviceToHost,
-                            stream));
-    CG_CUDA(cudaStreamSynchronize(stream));
     bool exact = false;
     // bound of the residual norms' error where they were not recomputed with
     // the FP64 operator (as in System::solve_mixed, over the largest norm)
@@ -931,7 +1123,77 @@ int BatchSystem::solve_device(const double* d_rhs, double* d_mu, int* iters_out)
     std::vector<double> swv[NINEXACT], rswv[NINEXACT];
     for (int k = 0; k < NINEXACT; ++k) swv[k].assign(nseg, -1.0), rswv[k].assign(nseg, 0.0);
     std::vector<int> lvlv(nseg, 0);
-    for (int outer = 0; outer < 12; ++outer) {
+    int outer0 = 0;
+    if (course_graph_ready(maxit)) {
+      // outer iterations 0 and 1 in one launch; the host then takes the
+      // choices the course assumed: the solve ends after the double-float
+      // residual where every segment is below the threshold (the second
+      // inner solve then took no step and changed neither x nor r), the
+      // residual from the recursion stands where its bound stays below
+      // 0.4 t, and is replaced by the double-float one where it does not
+      CG_CUDA(cudaGraphLaunch(course_exec, stream));
+      std::vector<int> it1(nseg);
+      std::vector<double> rn2(nseg);
+      CG_CUDA(cudaMemcpyAsync(it1.data(), iters_first.p, nseg * sizeof(int),
+                              cudaMemcpyDeviceToHost, stream));
+      CG_CUDA(cudaMemcpyAsync(it_h.data(), iters.p, nseg * sizeof(int), cudaMemcpyDeviceToHost,
+                              stream));
+      CG_CUDA(cudaMemcpyAsync(rn2.data(), rn_second.p, nseg * sizeof(double),
+                              cudaMemcpyDeviceToHost, stream));
+      CG_CUDA(cudaMemcpyAsync(rn.data(), seg_rnorm.p, nseg * sizeof(double),
+                              cudaMemcpyDeviceToHost, stream));
+      for (int k = 0; k < n_inexact; ++k)
+        CG_CUDA(cudaMemcpyAsync(rswv[k].data(), seg_rsw[k].p, nseg * sizeof(double),
+                                cudaMemcpyDeviceToHost, stream));
+      host_wait();
+      const int k1 = *std::max_element(it1.begin(), it1.end());
+      const int k2 = *std::max_element(it_h.begin(), it_h.end());
+      stats.fp32_applies += 1 + k1 + k2;
+      stats.fp64_applies += 1;
+      launch_counter() += course_launches + course_body_launches * (k1 + k2);
+      for (int g = 0; g < nseg; ++g) total[g] = it1[g] + it_h[g];
+      exact  = true;
+      outer0 = 2;
+      if (std::all_of(rn2.begin(), rn2.end(), [&](double v) { return v < t; })) {
+        status = CPPE_GPU_OK;
+        rn     = rn2;
+      } else {
+        double extra = 0.0;
+        for (int g = 0; g < nseg; ++g)
+          extra = std::max(extra, 1.5 * ((n_inexact > 0 ? h_delta[0][g] * rswv[0][g] : 0.0) +
+                                         (n_inexact > 1 ? h_delta[1][g] * rswv[1][g] : 0.0)));
+        const double bound = REC_ERR * *std::max_element(rn2.begin(), rn2.end()) + extra;
+        if (bound < 0.4 * t) {
+          rerr = bound;
+        } else {
+          apply_seg<double>(x.p, Ap.p, NEAR_DD);
+          stats.fp64_applies++;
+          k_bres<<<nb, BB, 0, stream>>>(n, F.p, Ap.p, nullptr, r.p, site_b.p);
+          CG_LAUNCH();
+          seg_norms_from_site_b();
+          CG_CUDA(cudaMemcpyAsync(rn.data(), seg_rnorm.p, nseg * sizeof(double),
+                                  cudaMemcpyDeviceToHost, stream));
+          host_wait();
+        }
+      }
+    } else {
+      k_bf32<<<nb3, BB, 0, stream>>>(n3, x.p, p32.p);
+      CG_LAUNCH();
+      apply_seg<float>(p32.p, Ap32.p);
+      stats.fp32_applies++;
+      CG_CUDA(cudaMemsetAsync(d32.p, 0, sizeof(float) * n3, stream));
+      k_bcg_start<float><<<nb, BB, 0, stream>>>(n, F.p, Ap32.p, alpha32.p, r32.p, z32.p, p32.p,
+                                                site_a.p, site_b.p);
+      CG_LAUNCH();
+      k_seg_sum<<<nseg, BB, 0, stream>>>(seg_start.p, site_a.p, site_b.p, seg_rz.p, seg_rr.p);
+      CG_LAUNCH();
+      k_bsqrt<<<(nseg + 127) / 128, 128, 0, stream>>>(nseg, seg_rr.p, seg_rnorm.p);
+      CG_LAUNCH();
+      CG_CUDA(cudaMemcpyAsync(rn.data(), seg_rnorm.p, nseg * sizeof(double),
+                              cudaMemcpyDeviceToHost, stream));
+      host_wait();
+    }
+    for (int outer = outer0; outer < 12 && status != CPPE_GPU_OK; ++outer) {
       // inner tolerances; segments already below the threshold stay put
       for (int g = 0; g < nseg; ++g) tolv[g] = std::max(eta * rn[g], 0.5 * t);
       if (outer > 0) {
@@ -1001,7 +1263,7 @@ int BatchSystem::solve_device(const double* d_rhs, double* d_mu, int* iters_out)
       k_bcg_init_seg<<<(nseg + 127) / 128, 128, 0, stream>>>(
             nseg, seg_rz.p, seg_rr.p, seg_rz.p, seg_rnorm.p, done.p, iters.p, seg_tol.p);
       CG_LAUNCH();
-      run_pcg<float>(d32.p, r32.p, z32.p, p32.p, Ap32.p, alpha32.p, std::max(1, opt.maxiter));
+      run_pcg<float>(d32.p, r32.p, z32.p, p32.p, Ap32.p, alpha32.p, maxit);
       CG_CUDA(cudaMemcpyAsync(it_h.data(), iters.p, nseg * sizeof(int), cudaMemcpyDeviceToHost,
                               stream));
       // the inexact operators' share of the recursion's error: 1.5 delta
@@ -1011,7 +1273,7 @@ int BatchSystem::solve_device(const double* d_rhs, double* d_mu, int* iters_out)
         for (int k = 0; k < NINEXACT; ++k)
           CG_CUDA(cudaMemcpyAsync(rswv[k].data(), seg_rsw[k].p, nseg * sizeof(double),
                                   cudaMemcpyDeviceToHost, stream));
-        CG_CUDA(cudaStreamSynchronize(stream));
+        host_wait();
         for (int g = 0; g < nseg; ++g)
           extra = std::max(extra, 1.5 * (h_delta[0][g] * rswv[0][g] +
                                          (n_inexact > 1 ? h_delta[1][g] * rswv[1][g] : 0.0)));
@@ -1048,7 +1310,7 @@ int BatchSystem::solve_device(const double* d_rhs, double* d_mu, int* iters_out)
       seg_norms_from_site_b();
       CG_CUDA(cudaMemcpyAsync(rn.data(), seg_rnorm.p, nseg * sizeof(double),
                               cudaMemcpyDeviceToHost, stream));
-      CG_CUDA(cudaStreamSynchronize(stream));
+      host_wait();
       for (int g = 0; g < nseg; ++g) total[g] += it_h[g];
     }
     if (status != CPPE_GPU_OK &&
@@ -1061,7 +1323,7 @@ int BatchSystem::solve_device(const double* d_rhs, double* d_mu, int* iters_out)
     for (int g = 0; g < nseg; ++g) iters_out[g] = total[g];
   }
   permute_out(geo, x.p, d_mu, 3, stream);
-  CG_CUDA(cudaStreamSynchronize(stream));
+  host_wait();
   return status;
 }
 

@@ -69,9 +69,34 @@ struct BatchSystem {
   void apply_levels32(const float* in, float* out);
   // the same inside a graph capture on `stream`: each operator's pass in a
   // conditional node that runs only when some segment is at its level (the
-  // passes captured on cap_stream, far field in line)
+  // passes captured on if_stream, far field in line)
   void apply_levels32_graph(const float* in, float* out);
-  cudaStream_t cap_stream = nullptr;
+  // streams that capture nested bodies: a loop's body on cap_stream, the
+  // per-level passes on if_stream (cap_stream, or cap_stream2 inside a loop
+  // body that cap_stream captures)
+  cudaStream_t cap_stream  = nullptr;
+  cudaStream_t cap_stream2 = nullptr;
+  cudaStream_t if_stream   = nullptr;
+  DBuf<double> seg_delta_d[NINEXACT];  // h_delta on the device
+  // The usual course of a mixed solve -- start residual, first inner solve,
+  // double-float residual, second inner solve, residual from the recursion
+  // -- as one CUDA graph with the inner solves as conditional while nodes:
+  // one launch and one host synchronisation per solve; the host loop takes
+  // over where the course does not end the solve.
+  cudaGraphExec_t course_exec = nullptr;
+  bool course_failed          = false;
+  long long course_launches   = 0;  // launches captured outside the inner loops
+  long long course_body_launches = 0;  // launches captured into one inner iteration
+  // host synchronisations with the stream in the last solve
+  int host_waits = 0;
+  void host_wait();
+  DBuf<int> iters_first;     // the first inner solve's iterations per segment
+  DBuf<double> rn_second;    // residual norms at the second inner solve's start
+  bool course_graph_ready(int maxiter);
+  void course_body(int maxiter);
+  // a conditional while node after the capture's tip on `stream`, with one
+  // FP32 PCG iteration captured into its body
+  void capture_pcg_loop(int maxiter);
   // measures each segment's difference between the operator and the
   // inexact ones (part of init, after the inexact geometries are built)
   void measure_inexact(const std::vector<int>& seg_start_h, const std::vector<char>& seg_fmm);

@@ -341,6 +341,13 @@ int cppe_gpu_batch_solve_device(cppe_gpu_batch* b, const double* d_rhs, double* 
  * segment) and the largest final residual norm over the segments. */
 int cppe_gpu_batch_stats(cppe_gpu_batch* b, int* fp64_applies, int* fp32_applies,
                          double* max_rnorm);
+/* Host synchronisations with the batch's stream in the last batched solve
+ * (cppe_gpu_batch_solve_device): 2 where a mixed solve runs its usual course
+ * -- start residual, two inner solves around a double-float residual, the
+ * residual from the recursion -- as one graph launch (the second is the
+ * copy-out); more where the host loop takes further outer iterations, runs
+ * with graphs disabled (CPPE_GPU_GRAPHS=0), or solves in FP64. */
+int cppe_gpu_batch_host_waits(cppe_gpu_batch* b, int* waits);
 /* Schedule autotuning of a batch, as cppe_gpu_autotune: the FP32 operator
  * over all segments under three near-field work-item sizes, three M2L chunk
  * sizes and both far-field stream priorities; keeps the fastest. */

@@ -112,6 +112,10 @@ def test_batch_graph_loop_matches_host_loop(gpu, precision, tmp_path):
     mu, its = b.solve(_rhs(boxes, 2, seed=2))
     np.testing.assert_array_equal(its, host["its"])
     np.testing.assert_allclose(mu, host["mu"], rtol=0, atol=1e-12)
+    if precision == cabi.MIXED:
+        # the mixed solve ran its usual course as one graph launch: one wait
+        # for its results and one for the copy-out
+        assert b.stats()["host_waits"] == 2
 
 
 def test_batch_more_rhs_than_one_pass(gpu):
