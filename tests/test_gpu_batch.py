@@ -118,6 +118,30 @@ def test_batch_graph_loop_matches_host_loop(gpu, precision, tmp_path):
         assert b.stats()["host_waits"] == 2
 
 
+def test_batch_course_hands_over_to_the_host_loop(gpu):
+    """Inner solves capped at five iterations: the one-launch course of a
+    mixed solve ends short of the threshold and the host loop takes further
+    outer iterations; every segment still meets the reference's stopping
+    rule with its own FP64 operator."""
+    boxes = _snapshots()[:3]
+    nrhs = 2
+    rhs = _rhs(boxes, nrhs, seed=4)
+    batch = cabi.Batch(boxes, nrhs, direct_below=1000, damp=True, precision=cabi.MIXED,
+                       maxiter=5)
+    mu, _ = batch.solve(rhs)
+    assert batch.stats()["host_waits"] > 2
+    off = 0
+    for b in boxes:
+        summ = cabi.FMM if b.n >= 1000 else cabi.DIRECT
+        s64 = cabi.System(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, summation=summ, damp=True)
+        for r in range(nrhs):
+            seg = slice(off, off + 3 * b.n)
+            assert np.linalg.norm(rhs[seg] - s64.apply(mu[seg])) < 1e-8
+            off += 3 * b.n
+        s64.close()
+    batch.close()
+
+
 def test_batch_more_rhs_than_one_pass(gpu):
     """Ten right-hand sides per snapshot: the near-field passes take a
     snapshot's copies eight at a time; every segment still meets the
