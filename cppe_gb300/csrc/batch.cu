@@ -597,7 +597,7 @@ void BatchSystem::apply_seg(const T* in, T* out, int near_mode, bool skip_done) 
   FieldWork<T>& w = work<T>();
   const T* ainv   = std::is_same<T, double>::value ? (const T*)ainv64.p : (const T*)ainv32.p;
   eval_field<T>(geo, ops.get(), w, 1, in, opt.damp != 0, opt.damping_factor, FINISH_APPLY, ainv,
-                out, nullptr, 1.0, &rs, stream, nullptr, near_mode, &side,
+                out, nullptr, 1.0, &rs, stream, nullptr, near_mode, nested_body ? nullptr : &side,
                 skip_done ? done.p : nullptr);
   k_seg_sum<<<nseg, BB, 0, stream>>>(seg_start.p, site_a.p, nullptr, seg_pap.p, nullptr);
   CG_LAUNCH();
@@ -943,14 +943,14 @@ void BatchSystem::capture_pcg_loop(int maxiter) {
   CG_CUDA(cudaStreamBeginCaptureToGraph(cap_stream, wp.conditional.phGraph_out[0], nullptr,
                                         nullptr, 0, cudaStreamCaptureModeThreadLocal));
   const cudaStream_t outer = stream, outer_if = if_stream;
-  stream = cap_stream, if_stream = cap_stream2;
+  stream = cap_stream, if_stream = cap_stream2, nested_body = true;
   const long long c0 = launch_counter();
   try {
     pcg_iteration<float>(d32.p, r32.p, z32.p, p32.p, Ap32.p, alpha32.p, maxiter, true);
     k_bcg_continue<<<1, 1, 0, stream>>>(h, active.p);
     CG_LAUNCH();
   } catch (...) {
-    stream = outer, if_stream = outer_if;
+    stream = outer, if_stream = outer_if, nested_body = false;
     launch_counter()    = c0;
     cudaGraph_t dropped = nullptr;
     cudaStreamEndCapture(cap_stream, &dropped);
@@ -958,7 +958,7 @@ void BatchSystem::capture_pcg_loop(int maxiter) {
   }
   course_body_launches = launch_counter() - c0;
   launch_counter()     = c0;
-  stream = outer, if_stream = outer_if;
+  stream = outer, if_stream = outer_if, nested_body = false;
   cudaGraph_t captured = nullptr;
   CG_CUDA(cudaStreamEndCapture(cap_stream, &captured));
 }

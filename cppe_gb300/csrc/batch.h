@@ -77,6 +77,9 @@ struct BatchSystem {
   cudaStream_t cap_stream  = nullptr;
   cudaStream_t cap_stream2 = nullptr;
   cudaStream_t if_stream   = nullptr;
+  // set while a loop body nested in a larger capture is captured: the
+  // operator passes then keep their far field in line (no side stream)
+  bool nested_body = false;
   DBuf<double> seg_delta_d[NINEXACT];  // h_delta on the device
   // The usual course of a mixed solve -- start residual, first inner solve,
   // double-float residual, second inner solve, residual from the recursion

@@ -142,6 +142,28 @@ def test_batch_course_hands_over_to_the_host_loop(gpu):
     batch.close()
 
 
+def test_batch_mixed_direct_snapshots_in_one_launch(gpu):
+    """A mixed batch of direct-summation snapshots only (no inexact
+    operators): its course runs as one graph launch too, and every segment
+    meets the reference's stopping rule with its own FP64 operator."""
+    boxes = _snapshots()[:3]
+    nrhs = 2
+    rhs = _rhs(boxes, nrhs, seed=5)
+    batch = cabi.Batch(boxes, nrhs, direct_below=10**6, damp=True, precision=cabi.MIXED)
+    mu, _ = batch.solve(rhs)
+    assert batch.stats()["host_waits"] == 2
+    off = 0
+    for b in boxes:
+        s64 = cabi.System(b.xyz, b.alpha6, b.excl_ptr, b.excl_idx, summation=cabi.DIRECT,
+                          damp=True)
+        for r in range(nrhs):
+            seg = slice(off, off + 3 * b.n)
+            assert np.linalg.norm(rhs[seg] - s64.apply(mu[seg])) < 1e-8
+            off += 3 * b.n
+        s64.close()
+    batch.close()
+
+
 def test_batch_more_rhs_than_one_pass(gpu):
     """Ten right-hand sides per snapshot: the near-field passes take a
     snapshot's copies eight at a time; every segment still meets the
