@@ -219,7 +219,9 @@ __global__ void k_features(NearListView nl, const float* __restrict__ a6,
 #pragma unroll
   for (int k = 0; k < Mlp::IN; ++k) f[k] = 0.f;
   const float rc = (float)LEARN_RC;
-  const float w16 = (rc - 1.f) / 15.f, w8 = (rc - 1.f) / 7.f;
+  // Gaussian q of a family of width w centred at 1 + q w: its argument
+  // (r - 1 - q w) / w is t0 - q with t0 = (r - 1) / w
+  const float iw16 = 15.f / (rc - 1.f), iw8 = 7.f / (rc - 1.f);
   const int k0 = ok ? nl.ptr[ii] : 0, k1 = ok ? nl.ptr[ii + 1] : 0;
   // the next entry's loads (and its dependent polarizability gather) are
   // issued before this entry's arithmetic, which hides their latency
@@ -238,9 +240,10 @@ __global__ void k_features(NearListView nl, const float* __restrict__ a6,
     }
     const float r   = dv.w;
     const float fc  = 0.5f * (__cosf(3.14159265f * r / rc) + 1.f);
+    const float t16 = (r - 1.f) * iw16, t8 = (r - 1.f) * iw8;
 #pragma unroll
     for (int q = 0; q < 16; ++q) {
-      const float t = (r - (1.f + q * w16)) / w16;
+      const float t = t16 - (float)q;
       const float g = __expf(-t * t) * fc;
       f[1 + q] += g;
       f[17 + q] += aj * g;
@@ -249,7 +252,7 @@ __global__ void k_features(NearListView nl, const float* __restrict__ a6,
     const float p2 = 1.5f * ct * ct - 0.5f;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
-      const float t = (r - (1.f + q * w8)) / w8;
+      const float t = t8 - (float)q;
       const float g = __expf(-t * t) * fc;
       f[33 + q] += g * ct;
       f[41 + q] += g * p2;
