@@ -381,9 +381,17 @@ class System:
         check(lib().cppe_gpu_direct_inverse(self.h, dp(out)))
         return out
 
-    def solve(self, rhs, guess=None, make_guess=True, allow_not_converged=False):
+    def solve(self, rhs, guess=None, make_guess=True, allow_not_converged=False, out=None):
+        """out: optional float64 array of rhs's size that receives mu (for
+        example a view of pinned host memory, which the copies then use
+        directly)."""
         rhs = f64(rhs)
-        mu = np.zeros_like(rhs)
+        if out is None:
+            mu = np.zeros_like(rhs)
+        else:
+            if out.dtype != np.float64 or out.size != rhs.size or not out.flags.c_contiguous:
+                raise ValueError("out must be a contiguous float64 array of the rhs's size")
+            mu = out
         it = ctypes.c_int(0)
         cap = self.opts.maxiter + 64
         hist = np.zeros(cap)
