@@ -1045,8 +1045,8 @@ bool BatchSystem::course_graph_ready(int maxiter) {
     try {
       CaptureScope cs;
       course_body(maxiter);
-    } catch (const Failure&) {
-      ok = false;
+    } catch (...) {
+      ok = false;  // the capture still ends below, so the stream stays usable
     }
     ok = (cudaStreamEndCapture(stream, &g) == cudaSuccess) && ok;
   }
