@@ -394,15 +394,16 @@ __global__ void k_blevel_update(int nsys, int nrhs, int nx, const double* __rest
 
 // The tolerances and hand-over points of a mixed solve's inner solve, per
 // snapshot (its right-hand sides share the operator level), from the
-// residual norms at its start -- what solve_device's host loop sets for
-// outer iteration 0 (stage 0) and 1 (stage 1, after the double-float
-// residual, where segments already below the threshold are done at once).
+// residual norms at its start: stage 0 for the first inner solve, stage 1
+// for later ones, where segments whose residual plus its error bound rerr is
+// already below the threshold are done at once.
 // With inexact operators (nx > 0) also the hand-over points and the starting
 // levels: stage 0 hands over where the operator's effect delta ||r|| stays
 // below 0.6 of the target eta ||r0||, stage 1 where 1.5 delta ||r|| stays
 // below 0.18 t; a snapshot already below a point starts at its level.
 __global__ void k_bstage(int nsys, int nrhs, int nx, int stage, double t, double eta,
-                         const double* __restrict__ rnorm, const double* __restrict__ d0,
+                         double rerr, const double* __restrict__ rnorm,
+                         const double* __restrict__ d0,
                          const double* __restrict__ d1, double* __restrict__ tol,
                          double* __restrict__ sw0, double* __restrict__ sw1,
                          double* __restrict__ rsw0, double* __restrict__ rsw1,
@@ -414,7 +415,7 @@ __global__ void k_bstage(int nsys, int nrhs, int nx, int stage, double t, double
     const int g     = s * nrhs + r;
     const double rn = rnorm[g];
     double tl       = fmax(eta * rn, 0.5 * t);
-    if (stage > 0 && rn < t) tl = 1e300;
+    if (stage > 0 && rn + rerr < t) tl = 1e300;
     tol[g] = tl;
     if (nx == 0) continue;
     auto sw = [&](double d) {
@@ -984,7 +985,7 @@ void BatchSystem::course_body(int maxiter) {
   // the first inner solve
   const int nx = n_inexact;
   auto stage = [&](int sg) {
-    k_bstage<<<sb, 128, 0, stream>>>(nsys, nrhs, nx, sg, t, BATCH_ETA, seg_rnorm.p,
+    k_bstage<<<sb, 128, 0, stream>>>(nsys, nrhs, nx, sg, t, BATCH_ETA, 0.0, seg_rnorm.p,
                                      seg_delta_d[0].p, seg_delta_d[1].p, seg_tol.p, seg_sw[0].p,
                                      seg_sw[1].p, seg_rsw[0].p, seg_rsw[1].p, seg_level.p);
     CG_LAUNCH();
@@ -1120,9 +1121,8 @@ int BatchSystem::solve_device(const double* d_rhs, double* d_mu, int* iters_out)
     // the FP64 operator (as in System::solve_mixed, over the largest norm)
     constexpr double REC_ERR = 3e-6, CORR_ERR = 3e-7;
     double rerr = 0.0;
-    std::vector<double> swv[NINEXACT], rswv[NINEXACT];
-    for (int k = 0; k < NINEXACT; ++k) swv[k].assign(nseg, -1.0), rswv[k].assign(nseg, 0.0);
-    std::vector<int> lvlv(nseg, 0);
+    std::vector<double> rswv[NINEXACT];
+    for (int k = 0; k < NINEXACT; ++k) rswv[k].assign(nseg, 0.0);
     int outer0 = 0;
     if (course_graph_ready(maxit)) {
       // outer iterations 0 and 1 in one launch; the host then takes the
@@ -1194,71 +1194,26 @@ int BatchSystem::solve_device(const double* d_rhs, double* d_mu, int* iters_out)
       host_wait();
     }
     for (int outer = outer0; outer < 12 && status != CPPE_GPU_OK; ++outer) {
-      // inner tolerances; segments already below the threshold stay put
-      for (int g = 0; g < nseg; ++g) tolv[g] = std::max(eta * rn[g], 0.5 * t);
       if (outer > 0) {
         if (std::all_of(rn.begin(), rn.end(), [&](double v) { return v + rerr < t; })) {
           status = CPPE_GPU_OK;
           break;
         }
-        for (int g = 0; g < nseg; ++g)
-          if (rn[g] + rerr < t) tolv[g] = 1e300;  // done at once
+      }
+      // inner tolerances, hand-over points and starting levels from the
+      // norms in seg_rnorm (those in rn): the course's k_bstage
+      const int nsys = nseg / nrhs;
+      k_bstage<<<(nsys + 127) / 128, 128, 0, stream>>>(
+            nsys, nrhs, n_inexact, outer == 0 ? 0 : 1, t, eta, rerr, seg_rnorm.p,
+            seg_delta_d[0].p, seg_delta_d[1].p, seg_tol.p, seg_sw[0].p, seg_sw[1].p,
+            seg_rsw[0].p, seg_rsw[1].p, seg_level.p);
+      CG_LAUNCH();
+      if (outer > 0) {
         k_bcg_start<float><<<nb, BB, 0, stream>>>(n, r.p, nullptr, alpha32.p, r32.p, z32.p,
                                                   p32.p, site_a.p, site_b.p);
         CG_LAUNCH();
         k_seg_sum<<<nseg, BB, 0, stream>>>(seg_start.p, site_a.p, site_b.p, seg_rz.p, seg_rr.p);
         CG_LAUNCH();
-      }
-      CG_CUDA(cudaMemcpyAsync(seg_tol.p, tolv.data(), nseg * sizeof(double),
-                              cudaMemcpyHostToDevice, stream));
-      if (n_inexact > 0) {
-        // hand-over points of this inner solve, as System's k_inner_stage:
-        // in the first one where an inexact operator's effect, ~delta ||r||,
-        // stays below 0.6 of the target eta ||r0|| (the double-float
-        // residual that follows is exact); in later ones (whose residual is
-        // then formed from the recursion) where 1.5 delta ||r|| stays below
-        // 0.18 t per operator
-        const int stage = outer == 0 ? 0 : 1;
-        for (int g = 0; g < nseg; ++g) {
-          auto sw = [&](double d) {
-            if (!(d > 0.0)) return -1.0;
-            return std::max(tolv[g], stage == 0 ? 0.6 * eta * rn[g] / d : 0.18 * t / (1.5 * d));
-          };
-          swv[0][g] = sw(h_delta[0][g]);
-          swv[1][g] = n_inexact > 1 && swv[0][g] > 0.0 ? std::min(swv[0][g], sw(h_delta[1][g]))
-                                                       : -1.0;
-        }
-        // a snapshot whose every running right-hand side already starts
-        // below a hand-over point starts with that operator (as
-        // k_blevel_update would set it after the first iteration)
-        std::fill(lvlv.begin(), lvlv.end(), 0);
-        for (auto& v : rswv) std::fill(v.begin(), v.end(), 0.0);
-        const int nsys = nseg / nrhs;
-        for (int sy = 0; sy < nsys; ++sy) {
-          bool any = false, all0 = true, all1 = n_inexact > 1;
-          for (int r = 0; r < nrhs; ++r) {
-            const int g = sy * nrhs + r;
-            if (rn[g] < tolv[g]) continue;  // done at once
-            any  = true;
-            all0 = all0 && rn[g] < swv[0][g];
-            all1 = all1 && rn[g] < swv[1][g];
-          }
-          const int l = !any ? 0 : (all0 ? (all1 ? 2 : 1) : 0);
-          for (int r = 0; r < nrhs && l > 0; ++r) {
-            const int g = sy * nrhs + r;
-            lvlv[g]     = l;
-            rswv[0][g]  = rn[g];
-            if (l == 2) rswv[1][g] = rn[g];
-          }
-        }
-        for (int k = 0; k < NINEXACT; ++k) {
-          CG_CUDA(cudaMemcpyAsync(seg_sw[k].p, swv[k].data(), nseg * sizeof(double),
-                                  cudaMemcpyHostToDevice, stream));
-          CG_CUDA(cudaMemcpyAsync(seg_rsw[k].p, rswv[k].data(), nseg * sizeof(double),
-                                  cudaMemcpyHostToDevice, stream));
-        }
-        CG_CUDA(cudaMemcpyAsync(seg_level.p, lvlv.data(), nseg * sizeof(int),
-                                cudaMemcpyHostToDevice, stream));
       }
       k_bcg_init_seg<<<(nseg + 127) / 128, 128, 0, stream>>>(
             nseg, seg_rz.p, seg_rr.p, seg_rz.p, seg_rnorm.p, done.p, iters.p, seg_tol.p);
